@@ -1,0 +1,390 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 TRSK shallow-water step (cell-steps/s).
+
+Workload: icosahedral level 9 (2,621,442 cells, 7,864,320 edges,
+5,242,880 triangles), classic RK4, trsk10 / HTC / geodesic areas, seeded
+synthetic state (Williamson case 2 steady flow), dt = 55 s.  One "step" is
+one RK4 time step of the whole grid.
+
+  value      cell-steps/s of the FP32 path with the state resident in HBM
+             (graph-replayed steps, CUDA events on the library's stream)
+  fp64       the same for the FP64 reference-order path
+  e2e        cell-steps/s through the C ABI call imodel_swm_step with
+             pinned host buffers: every step copies h and u (FP64) to the
+             device and back inside the timed region
+  roofline   the dominant kernel (edge kernel: grad B + TRSK PV flux +
+             momentum update) against the measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle (C++ restatement of the Fortran, OpenMP on
+             all host threads) on a bounded sample of the same workload
+
+``--impl reference`` times that CPU implementation alone and prints its line.
+Run under torchrun for N GPUs: each rank advances its own replica (no data
+exchange), timing is the max over ranks and value sums all ranks' cells.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SWM cell-steps/s at icos-L9, plain FP64 vs FP32+learned at fixed error; HBM GB/s"
+UNIT = "cell-steps/s"
+LEVEL = 9
+DT = 55.0
+
+
+# ---------------------------------------------------------------------------
+# CUDA runtime helpers (events, pinned memory) through ctypes
+# ---------------------------------------------------------------------------
+class Cudart:
+    def __init__(self):
+        from imodel_gb300 import _build
+        path = os.path.join(_build._cuda_lib_dir(), "libcudart.so")
+        self.lib = ctypes.CDLL(path if os.path.exists(path) else "libcudart.so")
+        L = self.lib
+        L.cudaEventCreate.argtypes = [ctypes.POINTER(ctypes.c_void_p)]
+        L.cudaEventRecord.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.cudaEventSynchronize.argtypes = [ctypes.c_void_p]
+        L.cudaEventElapsedTime.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_void_p,
+                                           ctypes.c_void_p]
+        L.cudaEventDestroy.argtypes = [ctypes.c_void_p]
+        L.cudaStreamSynchronize.argtypes = [ctypes.c_void_p]
+        L.cudaMallocHost.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]
+        L.cudaFreeHost.argtypes = [ctypes.c_void_p]
+        L.cudaSetDevice.argtypes = [ctypes.c_int]
+
+    def event(self):
+        e = ctypes.c_void_p()
+        assert self.lib.cudaEventCreate(ctypes.byref(e)) == 0
+        return e
+
+    def record(self, ev, stream):
+        assert self.lib.cudaEventRecord(ev, ctypes.c_void_p(stream)) == 0
+
+    def elapsed_ms(self, a, b):
+        assert self.lib.cudaEventSynchronize(b) == 0
+        ms = ctypes.c_float()
+        assert self.lib.cudaEventElapsedTime(ctypes.byref(ms), a, b) == 0
+        return float(ms.value)
+
+    def sync(self):
+        self.lib.cudaDeviceSynchronize()
+
+    def pinned(self, n):
+        p = ctypes.c_void_p()
+        assert self.lib.cudaMallocHost(ctypes.byref(p), n * 8) == 0
+        arr = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_double)), shape=(n,))
+        return p, arr
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self, device):
+        self.ws, self.rank, self.local = dist_env()
+        self.torch = None
+        if self.ws > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(device)
+            dist.init_process_group("nccl")
+            self.torch, self.dist = torch, dist
+
+    def barrier(self):
+        if self.torch is not None:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.torch is None:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.torch is not None:
+            self.dist.destroy_process_group()
+
+
+def kernel_bytes(nv, ne, nt, precision):
+    """Algorithmic bytes of one launch of each stage kernel: every array
+    element the kernel reads or writes counted once (FP32 path layout)."""
+    w = 4 if precision == "fp32" else 8
+    tri = nt * (w + 3 * w + 3 * 4 + 3 * w + 3 * 4 + w) + ne * w + nv * w
+    edge_pre = ne * (8 + 8 + w + 3 * w) + nv * w + nt * w
+    cell = nv * (1 + 6 * 4 + 6 * w + 6 * w + w + w + w + 2 * w + w + w) + 2 * ne * w
+    edge = ne * (8 + w + w + 1 + 10 * 4 + 10 * w + w + 2 * w + w) + nv * w + ne * w
+    if precision == "fp64":
+        # FP64 path reads d_k (edhx%leng) per stencil edge and 1 extra coef
+        edge += ne * w
+        cell += ne * w
+    return {"triangle": tri, "edge_pre": edge_pre, "cell": cell, "edge": edge}
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline_sample(grid, h, u, budget_s=15.0, nthreads=0):
+    """Times the CPU oracle on whole RK4 steps of the same grid until about
+    budget_s seconds have passed."""
+    import oracle
+    nthreads = nthreads or (os.cpu_count() or 1)
+    o = oracle.Oracle(grid, 2, nthreads=nthreads)
+    o.ode_rk4(h, u, DT)  # warm-up step (page-in, thread pool)
+    steps, t0 = 0, time.perf_counter()
+    hh, uu = h, u
+    while True:
+        hh, uu = o.ode_rk4(hh, uu, DT)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= 1000:
+            break
+    return {"value": grid.nv * steps / el, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{steps} RK4 steps of icos-L{grid.level} ({grid.nv} cells) in {el:.1f} s, "
+                      f"C++ oracle, OpenMP {nthreads} threads"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from imodel_gb300 import _build, swm
+    from imodel_gb300.mesh import meshbuild
+    import oracle
+    _build.build_mesh_lib()
+    oracle.build()
+    g = meshbuild(args.level)
+    h, u = swm.initialize_fields_tc2(g)
+    nth = os.cpu_count() or 1
+    o = oracle.Oracle(g, 2, nthreads=nth)
+    hh, uu = h, u
+    for _ in range(max(args.warmup, 1)):
+        hh, uu = o.ode_rk4(hh, uu, DT)
+    budget = 150.0
+    steps, t0 = 0, time.perf_counter()
+    while steps < args.steps:
+        hh, uu = o.ode_rk4(hh, uu, DT)
+        steps += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    el = time.perf_counter() - t0
+    value = g.nv * steps / el
+    sample = (f"{steps} of {args.steps} requested RK4 steps of icos-L{args.level} "
+              f"({g.nv} cells), C++ oracle (restatement of the Fortran), {nth} threads")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * el / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (Williamson case 2 state)",
+            "config": config_dict(g, "fp64"),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def config_dict(g, precision):
+    return {"workload": f"icos-L{g.level} TRSK shallow-water RK4 step, trsk10/HTC/geo, "
+                        f"dt={DT:g} s, Williamson case 2 state",
+            "level": g.level, "cells": g.nv, "edges": g.ne, "triangles": g.nt,
+            "precision": precision, "learned_correction": "not built",
+            "l2": "inputs larger than L2 (state + geometry of several GB per step)",
+            "parallelism": "replicas"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--level", type=int, default=LEVEL)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    ws, rank, local = dist_env()
+    from imodel_gb300 import _build, swm
+    from imodel_gb300.mesh import meshbuild
+    _build.build_all()
+    cr = Cudart()
+    assert cr.lib.cudaSetDevice(local) == 0
+    D = Dist(local)
+
+    g = meshbuild(args.level)
+    h, u = swm.initialize_fields_tc2(g)
+    results = {}
+    for precision in ("fp64", "fp32"):
+        m = swm.SWM(g, precision=precision, device=local)
+        m.set_state(h, u)
+        stream = m.stream()
+        m.advance(DT, args.warmup)
+        cr.sync()
+        ev0, ev1 = cr.event(), cr.event()
+        sampler = ClockSampler(local) if precision == "fp32" else None
+        D.barrier()
+        cr.sync()
+        if sampler:
+            sampler.start()
+        cr.record(ev0, stream)
+        m.advance(DT, args.steps)
+        cr.record(ev1, stream)
+        ms = cr.elapsed_ms(ev0, ev1)
+        cr.sync()
+        clocks = sampler.stop() if sampler else None
+        D.barrier()
+        ms = D.max(ms)
+        diag = m.diagnostics()
+        prof = m.profile(DT, 3)
+        results[precision] = {"ms": ms, "clocks": clocks, "prof": prof, "diag": diag,
+                              "launches": m.launch_count(args.steps),
+                              "main_kernel": m.main_kernel()}
+        if precision == "fp32":
+            # e2e through the C ABI with pinned host buffers
+            ph, hbuf = cr.pinned(g.nv)
+            pu, ubuf = cr.pinned(g.ne)
+            hbuf[:] = h
+            ubuf[:] = u
+            lib = m.lib
+            fp = ctypes.POINTER(ctypes.c_double)
+            hp, up = ctypes.cast(ph, fp), ctypes.cast(pu, fp)
+            for _ in range(2):
+                assert lib.imodel_swm_step(m.handle, hp, up, DT, 1) == 0
+            D.barrier()
+            t0 = time.perf_counter()
+            for _ in range(args.e2e_steps):
+                rc = lib.imodel_swm_step(m.handle, hp, up, DT, 1)
+                assert rc == 0, rc
+            el = time.perf_counter() - t0
+            D.barrier()
+            el = D.max(el)
+            results["e2e"] = {"s": el, "steps": args.e2e_steps}
+            cr.lib.cudaFreeHost(ph)
+            cr.lib.cudaFreeHost(pu)
+        m.close()
+
+    if rank == 0:
+        r32, r64 = results["fp32"], results["fp64"]
+        total_cells = g.nv * ws
+        value = total_cells * args.steps / (r32["ms"] / 1000.0)
+        value64 = total_cells * args.steps / (r64["ms"] / 1000.0)
+        peak, peak_kind = load_peaks()
+        kb = kernel_bytes(g.nv, g.ne, g.nt, "fp32")
+        dom = max(r32["prof"], key=r32["prof"].get)
+        achieved = kb[dom] / (r32["prof"][dom] / 1000.0) / 1e9
+        step_bytes = 2000.0 * g.nv  # per-cell-step algorithmic bytes (FP32 model)
+        step_achieved = step_bytes / (r32["ms"] / args.steps / 1000.0) / 1e9
+        e2e = results["e2e"]
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": r32["ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: Williamson case 2 steady zonal flow on the grid (no dataset)",
+            "config": config_dict(g, "fp32"),
+            "fp64": {"value": value64, "unit": UNIT, "ms_per_step": r64["ms"] / args.steps,
+                     "kernel_ms": r64["prof"]},
+            "kernel_ms": r32["prof"],
+            "roofline": {"bound": "hbm", "kernel": r32["main_kernel"], "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_kind, "traffic": None,
+                         "algorithmic_bytes_per_launch": kb[dom]},
+            "step_roofline": {"bytes_per_cell_step": 2000.0, "achieved": step_achieved,
+                              "peak": peak, "unit": "GB/s", "frac": step_achieved / peak},
+            "e2e": {"value": total_cells * e2e["steps"] / e2e["s"], "unit": UNIT,
+                    "h2d_bytes_per_step": 8 * (g.nv + g.ne),
+                    "d2h_bytes_per_step": 8 * (g.nv + g.ne),
+                    "path": "imodel_swm_step(nsteps=1) with pinned host FP64 h,u"},
+            "gpu_launches": r32["launches"],
+            "clocks": r32["clocks"],
+        }
+        if not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline_sample(g, h, u, args.cpu_budget)
+        print(json.dumps(line))
+    D.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

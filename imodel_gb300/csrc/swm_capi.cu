@@ -1,0 +1,598 @@
+// C ABI of the GB300 TRSK shallow-water step (include/imodel_swm.h).
+//
+// A handle owns the device copy of the mesh layout, the state buffers of
+// classic RK4 and one CUDA stream.  One RK4 step is 4 stages x 4 kernels;
+// it is captured once into a CUDA graph per time step length and replayed.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "imodel_swm.h"
+#include "swm_common.cuh"
+#include "swm_layout.h"
+
+namespace imodel {
+namespace {
+
+struct Handle {
+  std::string err;
+  int device = 0;
+  int precision = IMODEL_SWM_FP64;
+  int testcase = 2;
+  int nv = 0, ne = 0, nt = 0;
+  double area_cells = 0.0, area_edges = 0.0;  // sum A_i, sum l d / 2
+  std::vector<double> h_areag;                 // reference order, for h_ref
+  bool href_fixed = false;
+  double h_ref = 0.0;
+  DevMesh M{};
+  std::vector<void *> allocs;
+  int32_t *d_cell_n2o = nullptr, *d_edge_n2o = nullptr;
+  double *d_stage_h = nullptr, *d_stage_u = nullptr;  // FP64, reference order
+  double *d_ref_h = nullptr, *d_ref_u = nullptr;      // FP64, device order
+  double *d_scratch = nullptr, *d_result = nullptr;
+  int *d_flags = nullptr;
+  int *h_flags = nullptr;      // pinned
+  double *h_result = nullptr;  // pinned
+  Work<double> W64{};
+  Work<float> W32{};
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  double graph_dt = 0.0;
+  bool state_set = false;
+};
+
+#define CK(call)                                                                  \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess) {                                                      \
+      H->err = std::string(#call) + ": " + cudaGetErrorString(e_);                \
+      return e_ == cudaErrorMemoryAllocation ? IMODEL_SWM_ENOMEM : IMODEL_SWM_ECUDA; \
+    }                                                                             \
+  } while (0)
+
+template <class V>
+int upload(Handle *H, const std::vector<V> &v, const V **dst) {
+  if (v.empty()) {
+    *dst = nullptr;
+    return IMODEL_SWM_OK;
+  }
+  void *p = nullptr;
+  CK(cudaMalloc(&p, v.size() * sizeof(V)));
+  H->allocs.push_back(p);
+  CK(cudaMemcpy(p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice));
+  *dst = static_cast<const V *>(p);
+  return IMODEL_SWM_OK;
+}
+
+template <class T>
+int dalloc(Handle *H, T **p, size_t n) {
+  void *q = nullptr;
+  CK(cudaMalloc(&q, (n > 0 ? n : 1) * sizeof(T)));
+  H->allocs.push_back(q);
+  CK(cudaMemset(q, 0, (n > 0 ? n : 1) * sizeof(T)));
+  *p = static_cast<T *>(q);
+  return IMODEL_SWM_OK;
+}
+
+template <class T>
+int alloc_work(Handle *H, Work<T> &W) {
+  int rc;
+  T **bufs_v[] = {&W.yn_h, &W.ya_h, &W.yb_h, &W.acc_h, &W.bern, &W.tend_h};
+  for (T **b : bufs_v)
+    if ((rc = dalloc(H, b, H->nv))) return rc;
+  T **bufs_e[] = {&W.yn_u, &W.ya_u, &W.yb_u, &W.acc_u, &W.h_ed, &W.uh, &W.q_ed, &W.tend_u};
+  for (T **b : bufs_e)
+    if ((rc = dalloc(H, b, H->ne))) return rc;
+  if ((rc = dalloc(H, &W.q_tr, H->nt))) return rc;
+  W.flags = H->d_flags;
+  W.pv_on = H->testcase >= 2 ? 1 : 0;
+  W.mom_on = H->testcase > 1 ? 1 : 0;
+  W.h_ref = T(0);
+  return IMODEL_SWM_OK;
+}
+
+int set_error(Handle *H, int code, const std::string &msg) {
+  H->err = msg;
+  return code;
+}
+
+// one RK4 step on the device state (4 stages; swm.f90:2600-2683)
+void enqueue_step(Handle *H, double dt) {
+  cudaStream_t s = H->stream;
+  if (H->precision == IMODEL_SWM_FP64) {
+    const Work<double> &W = H->W64;
+    launch_stage64(H->M, W, W.yn_h, W.yn_u, W.ya_h, W.ya_u, 0, dt, s);
+    launch_stage64(H->M, W, W.ya_h, W.ya_u, W.yb_h, W.yb_u, 1, dt, s);
+    launch_stage64(H->M, W, W.yb_h, W.yb_u, W.ya_h, W.ya_u, 2, dt, s);
+    launch_stage64(H->M, W, W.ya_h, W.ya_u, W.yn_h, W.yn_u, 3, dt, s);
+  } else {
+    const Work<float> &W = H->W32;
+    const float fdt = static_cast<float>(dt);
+    launch_stage32(H->M, W, W.yn_h, W.yn_u, W.ya_h, W.ya_u, 0, fdt, s);
+    launch_stage32(H->M, W, W.ya_h, W.ya_u, W.yb_h, W.yb_u, 1, fdt, s);
+    launch_stage32(H->M, W, W.yb_h, W.yb_u, W.ya_h, W.ya_u, 2, fdt, s);
+    launch_stage32(H->M, W, W.ya_h, W.ya_u, W.yn_h, W.yn_u, 3, fdt, s);
+  }
+}
+
+int ensure_graph(Handle *H, double dt) {
+  if (H->graph && H->graph_dt == dt) return IMODEL_SWM_OK;
+  if (H->graph) {
+    cudaGraphExecDestroy(H->graph);
+    H->graph = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(H->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_step(H, dt);
+  CK(cudaStreamEndCapture(H->stream, &g));
+  cudaError_t e = cudaGraphInstantiate(&H->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    H->graph = nullptr;
+    return set_error(H, IMODEL_SWM_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  }
+  H->graph_dt = dt;
+  return IMODEL_SWM_OK;
+}
+
+// host FP64 arrays (reference order) -> device state yn, plus h_ed and the
+// "last stage input" ya, as after the reference's initial tendency call
+// (swm.f90:214)
+int load_state(Handle *H, const double *h, const double *u) {
+  if (H->precision == IMODEL_SWM_FP32 && !H->href_fixed) {
+    double s = 0.0, a = 0.0;
+    for (int i = 0; i < H->nv; ++i) {
+      a += H->h_areag[i];
+      s += H->h_areag[i] * h[i];
+    }
+    H->h_ref = s / a;
+    H->W32.h_ref = static_cast<float>(H->h_ref);
+    H->h_ref = static_cast<double>(H->W32.h_ref);
+    H->href_fixed = true;
+  }
+  CK(cudaMemcpyAsync(H->d_stage_h, h, sizeof(double) * H->nv, cudaMemcpyHostToDevice, H->stream));
+  CK(cudaMemcpyAsync(H->d_stage_u, u, sizeof(double) * H->ne, cudaMemcpyHostToDevice, H->stream));
+  if (H->precision == IMODEL_SWM_FP64) {
+    Work<double> &W = H->W64;
+    launch_gather_in(H->nv, H->d_cell_n2o, H->d_stage_h, W.yn_h, 0.0, H->stream);
+    launch_gather_in(H->ne, H->d_edge_n2o, H->d_stage_u, W.yn_u, 0.0, H->stream);
+    launch_hed64(H->M, W, W.yn_h, H->stream);
+    CK(cudaMemcpyAsync(W.ya_h, W.yn_h, sizeof(double) * H->nv, cudaMemcpyDeviceToDevice, H->stream));
+    CK(cudaMemcpyAsync(W.ya_u, W.yn_u, sizeof(double) * H->ne, cudaMemcpyDeviceToDevice, H->stream));
+  } else {
+    Work<float> &W = H->W32;
+    launch_gather_in32(H->nv, H->d_cell_n2o, H->d_stage_h, W.yn_h, H->h_ref, H->stream);
+    launch_gather_in32(H->ne, H->d_edge_n2o, H->d_stage_u, W.yn_u, 0.0, H->stream);
+    launch_hed32(H->M, W, W.yn_h, H->stream);
+    CK(cudaMemcpyAsync(W.ya_h, W.yn_h, sizeof(float) * H->nv, cudaMemcpyDeviceToDevice, H->stream));
+    CK(cudaMemcpyAsync(W.ya_u, W.yn_u, sizeof(float) * H->ne, cudaMemcpyDeviceToDevice, H->stream));
+  }
+  CK(cudaGetLastError());
+  H->state_set = true;
+  return IMODEL_SWM_OK;
+}
+
+int store_state(Handle *H, double *h, double *u) {
+  if (H->precision == IMODEL_SWM_FP64) {
+    launch_scatter_out(H->nv, H->d_cell_n2o, H->W64.yn_h, H->d_stage_h, 0.0, H->d_flags, H->stream);
+    launch_scatter_out(H->ne, H->d_edge_n2o, H->W64.yn_u, H->d_stage_u, 0.0, H->d_flags, H->stream);
+  } else {
+    launch_scatter_out32(H->nv, H->d_cell_n2o, H->W32.yn_h, H->d_stage_h, H->h_ref, H->d_flags,
+                         H->stream);
+    launch_scatter_out32(H->ne, H->d_edge_n2o, H->W32.yn_u, H->d_stage_u, 0.0, H->d_flags,
+                         H->stream);
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(h, H->d_stage_h, sizeof(double) * H->nv, cudaMemcpyDeviceToHost, H->stream));
+  CK(cudaMemcpyAsync(u, H->d_stage_u, sizeof(double) * H->ne, cudaMemcpyDeviceToHost, H->stream));
+  return IMODEL_SWM_OK;
+}
+
+// reads and clears the device flags; maps them to a status
+int check_flags(Handle *H) {
+  CK(cudaMemcpyAsync(H->h_flags, H->d_flags, sizeof(int), cudaMemcpyDeviceToHost, H->stream));
+  CK(cudaMemsetAsync(H->d_flags, 0, sizeof(int), H->stream));
+  CK(cudaStreamSynchronize(H->stream));
+  const int f = *H->h_flags;
+  if (f & 1)
+    return set_error(H, IMODEL_SWM_EDIVZERO,
+                     "division by zero in PV (|h_tr| < eps/1e5), as scalar_elem_divide stops");
+  if (f & 2) return set_error(H, IMODEL_SWM_EBLOWUP, "state holds NaN or Inf");
+  return IMODEL_SWM_OK;
+}
+
+int advance(Handle *H, double dt, int nsteps) {
+  if (!H->state_set) return set_error(H, IMODEL_SWM_ESTATE, "no state set");
+  if (nsteps < 0 || !(std::isfinite(dt))) return set_error(H, IMODEL_SWM_EINVAL, "bad dt or nsteps");
+  if (nsteps == 0) return IMODEL_SWM_OK;
+  int rc = ensure_graph(H, dt);
+  if (rc) return rc;
+  for (int k = 0; k < nsteps; ++k) CK(cudaGraphLaunch(H->graph, H->stream));
+  return IMODEL_SWM_OK;
+}
+
+int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
+  H->precision = o ? o->precision : IMODEL_SWM_FP64;
+  H->testcase = o ? o->testcase : 2;
+  H->device = o ? o->device : 0;
+  if (H->precision != IMODEL_SWM_FP64 && H->precision != IMODEL_SWM_FP32)
+    return set_error(H, IMODEL_SWM_EINVAL, "precision must be IMODEL_SWM_FP64 or IMODEL_SWM_FP32");
+  if (o && o->learned)
+    return set_error(H, IMODEL_SWM_EINVAL, "learned correction is not available in this build");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return set_error(H, IMODEL_SWM_ENODEV, "no CUDA device");
+  if (H->device < 0 || H->device >= ndev) return set_error(H, IMODEL_SWM_EINVAL, "bad device ordinal");
+  CK(cudaSetDevice(H->device));
+  Layout L;
+  std::string msg = build_layout(*m, o ? o->bt : nullptr, L);
+  if (!msg.empty()) return set_error(H, IMODEL_SWM_EINVAL, msg);
+  H->nv = L.nv;
+  H->ne = L.ne;
+  H->nt = L.nt;
+  H->h_areag.assign(m->hx_areag, m->hx_areag + L.nv);
+  for (int i = 0; i < L.nv; ++i) H->area_cells += L.c_areag[i];
+  for (int e = 0; e < L.ne; ++e) H->area_edges += L.e_area[e];
+  if (o && H->precision == IMODEL_SWM_FP32 && o->h_ref != 0.0) {
+    H->W32.h_ref = static_cast<float>(o->h_ref);
+    H->h_ref = static_cast<double>(H->W32.h_ref);
+    H->href_fixed = true;
+  }
+  CK(cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking));
+  DevMesh &M = H->M;
+  M.nv = L.nv;
+  M.ne = L.ne;
+  M.nt = L.nt;
+  M.erad = L.erad;
+  M.grav = L.grav;
+  int rc = 0;
+  std::vector<float> bt32(L.c_bt.size());
+  for (size_t i = 0; i < bt32.size(); ++i) bt32[i] = static_cast<float>(L.c_bt[i]);
+  if ((rc = upload(H, L.c_nnb, &M.c_nnb)) || (rc = upload(H, L.c_ed, &M.c_ed)) ||
+      (rc = upload(H, L.c_sd, &M.c_sd)) || (rc = upload(H, L.c_areag, &M.c_areag)) ||
+      (rc = upload(H, L.c_cellarea, &M.c_cellarea)) || (rc = upload(H, L.c_bt, &M.c_bt)) ||
+      (rc = upload(H, L.e_v, &M.e_v)) || (rc = upload(H, L.e_sh, &M.e_sh)) ||
+      (rc = upload(H, L.e_leng, &M.e_leng)) || (rc = upload(H, L.e_dleng, &M.e_dleng)) ||
+      (rc = upload(H, L.e_kew, &M.e_kew)) || (rc = upload(H, L.e_area, &M.e_area)) ||
+      (rc = upload(H, L.e_nst, &M.e_nst)) || (rc = upload(H, L.e_stk, &M.e_stk)) ||
+      (rc = upload(H, L.e_stw, &M.e_stw)) || (rc = upload(H, L.t_ed, &M.t_ed)) ||
+      (rc = upload(H, L.t_v, &M.t_v)) || (rc = upload(H, L.t_lt, &M.t_lt)) ||
+      (rc = upload(H, L.t_kite, &M.t_kite)) || (rc = upload(H, L.t_areag, &M.t_areag)) ||
+      (rc = upload(H, L.t_f, &M.t_f)))
+    return rc;
+  if (H->precision == IMODEL_SWM_FP32) {
+    if ((rc = upload(H, L.c_div32, &M.c_div32)) || (rc = upload(H, L.c_kew32, &M.c_kew32)) ||
+        (rc = upload(H, bt32, &M.c_bt32)) || (rc = upload(H, L.e_grad32, &M.e_grad32)) ||
+        (rc = upload(H, L.e_stc32, &M.e_stc32)) || (rc = upload(H, L.t_circ32, &M.t_circ32)) ||
+        (rc = upload(H, L.t_kite32, &M.t_kite32)) || (rc = upload(H, L.t_f32, &M.t_f32)))
+      return rc;
+  }
+  const int32_t *cn2o = nullptr, *en2o = nullptr;
+  if ((rc = upload(H, L.cell_n2o, &cn2o)) || (rc = upload(H, L.edge_n2o, &en2o))) return rc;
+  H->d_cell_n2o = const_cast<int32_t *>(cn2o);
+  H->d_edge_n2o = const_cast<int32_t *>(en2o);
+  if ((rc = dalloc(H, &H->d_stage_h, L.nv)) || (rc = dalloc(H, &H->d_stage_u, L.ne)) ||
+      (rc = dalloc(H, &H->d_ref_h, L.nv)) || (rc = dalloc(H, &H->d_ref_u, L.ne)) ||
+      (rc = dalloc(H, &H->d_scratch, static_cast<size_t>(2) * kRedBlocks * 16)) ||
+      (rc = dalloc(H, &H->d_result, 16)) || (rc = dalloc(H, &H->d_flags, 1)))
+    return rc;
+  CK(cudaMallocHost(&H->h_flags, sizeof(int)));
+  CK(cudaMallocHost(&H->h_result, 16 * sizeof(double)));
+  if (H->precision == IMODEL_SWM_FP64) {
+    if ((rc = alloc_work(H, H->W64))) return rc;
+  } else {
+    const float keep = H->W32.h_ref;
+    if ((rc = alloc_work(H, H->W32))) return rc;
+    H->W32.h_ref = keep;
+  }
+  CK(cudaDeviceSynchronize());
+  return IMODEL_SWM_OK;
+}
+
+void destroy(Handle *H) {
+  if (!H) return;
+  if (H->graph) cudaGraphExecDestroy(H->graph);
+  if (H->stream) cudaStreamSynchronize(H->stream);
+  for (void *p : H->allocs) cudaFree(p);
+  if (H->h_flags) cudaFreeHost(H->h_flags);
+  if (H->h_result) cudaFreeHost(H->h_result);
+  if (H->stream) cudaStreamDestroy(H->stream);
+  delete H;
+}
+
+}  // namespace
+}  // namespace imodel
+
+using imodel::Handle;
+
+extern "C" {
+
+int imodel_swm_create(const imodel_swm_mesh *m, const imodel_swm_opts *o, void **handle) {
+  if (!handle) return IMODEL_SWM_EINVAL;
+  *handle = nullptr;
+  Handle *H = new (std::nothrow) Handle();
+  if (!H) return IMODEL_SWM_ENOMEM;
+  if (!m) {
+    *handle = H;
+    H->err = "mesh is NULL";
+    return IMODEL_SWM_EINVAL;
+  }
+  int rc;
+  try {
+    rc = imodel::create(H, m, o);
+  } catch (const std::bad_alloc &) {
+    rc = IMODEL_SWM_ENOMEM;
+    H->err = "host allocation failed";
+  }
+  // the handle is returned even on failure so that last_error can be read;
+  // it must still be destroyed
+  *handle = H;
+  return rc;
+}
+
+int imodel_swm_step(void *handle, double *h_io, double *u_io, double dt, int32_t nsteps) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H || !h_io || !u_io) return IMODEL_SWM_EINVAL;
+  if (H->nv == 0) return imodel::set_error(H, IMODEL_SWM_ESTATE, "handle was not created");
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  int rc = imodel::load_state(H, h_io, u_io);
+  if (rc) return rc;
+  rc = imodel::advance(H, dt, nsteps);
+  if (rc) return rc;
+  rc = imodel::store_state(H, h_io, u_io);
+  if (rc) return rc;
+  return imodel::check_flags(H);
+}
+
+int imodel_swm_set_state(void *handle, const double *h, const double *u) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H || !h || !u) return IMODEL_SWM_EINVAL;
+  if (H->nv == 0) return imodel::set_error(H, IMODEL_SWM_ESTATE, "handle was not created");
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  int rc = imodel::load_state(H, h, u);
+  if (rc) return rc;
+  if (cudaStreamSynchronize(H->stream) != cudaSuccess)
+    return imodel::set_error(H, IMODEL_SWM_ECUDA, "stream synchronize failed");
+  return IMODEL_SWM_OK;
+}
+
+int imodel_swm_get_state(void *handle, double *h, double *u) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H || !h || !u) return IMODEL_SWM_EINVAL;
+  if (!H->state_set) return imodel::set_error(H, IMODEL_SWM_ESTATE, "no state set");
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  int rc = imodel::store_state(H, h, u);
+  if (rc) return rc;
+  return imodel::check_flags(H);
+}
+
+int imodel_swm_advance(void *handle, double dt, int32_t nsteps) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H) return IMODEL_SWM_EINVAL;
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  int rc = imodel::advance(H, dt, nsteps);
+  if (rc) return rc;
+  return imodel::check_flags(H);
+}
+
+int imodel_swm_tendency(void *handle, const double *h, const double *u, double *masseq,
+                        double *momeq) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H || !h || !u || !masseq || !momeq) return IMODEL_SWM_EINVAL;
+  if (H->nv == 0) return imodel::set_error(H, IMODEL_SWM_ESTATE, "handle was not created");
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  if (H->precision == IMODEL_SWM_FP32 && !H->href_fixed) {
+    double s = 0.0, a = 0.0;
+    for (int i = 0; i < H->nv; ++i) {
+      a += H->h_areag[i];
+      s += H->h_areag[i] * h[i];
+    }
+    H->W32.h_ref = static_cast<float>(s / a);
+    H->h_ref = static_cast<double>(H->W32.h_ref);
+    H->href_fixed = true;
+  }
+  cudaError_t e;
+  e = cudaMemcpyAsync(H->d_stage_h, h, sizeof(double) * H->nv, cudaMemcpyHostToDevice, H->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(H->d_stage_u, u, sizeof(double) * H->ne, cudaMemcpyHostToDevice, H->stream);
+  if (e != cudaSuccess) return imodel::set_error(H, IMODEL_SWM_ECUDA, cudaGetErrorString(e));
+  // the tendency input becomes the "last stage input" the diagnostics use
+  if (H->precision == IMODEL_SWM_FP64) {
+    auto &W = H->W64;
+    imodel::launch_gather_in(H->nv, H->d_cell_n2o, H->d_stage_h, W.ya_h, 0.0, H->stream);
+    imodel::launch_gather_in(H->ne, H->d_edge_n2o, H->d_stage_u, W.ya_u, 0.0, H->stream);
+    imodel::launch_stage64(H->M, W, W.ya_h, W.ya_u, nullptr, nullptr, -1, 0.0, H->stream);
+    imodel::launch_scatter_out(H->nv, H->d_cell_n2o, W.tend_h, H->d_stage_h, 0.0, nullptr, H->stream);
+    imodel::launch_scatter_out(H->ne, H->d_edge_n2o, W.tend_u, H->d_stage_u, 0.0, nullptr, H->stream);
+  } else {
+    auto &W = H->W32;
+    imodel::launch_gather_in32(H->nv, H->d_cell_n2o, H->d_stage_h, W.ya_h, H->h_ref, H->stream);
+    imodel::launch_gather_in32(H->ne, H->d_edge_n2o, H->d_stage_u, W.ya_u, 0.0, H->stream);
+    imodel::launch_stage32(H->M, W, W.ya_h, W.ya_u, nullptr, nullptr, -1, 0.0f, H->stream);
+    imodel::launch_scatter_out32(H->nv, H->d_cell_n2o, W.tend_h, H->d_stage_h, 0.0, nullptr, H->stream);
+    imodel::launch_scatter_out32(H->ne, H->d_edge_n2o, W.tend_u, H->d_stage_u, 0.0, nullptr, H->stream);
+  }
+  e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(masseq, H->d_stage_h, sizeof(double) * H->nv, cudaMemcpyDeviceToHost, H->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(momeq, H->d_stage_u, sizeof(double) * H->ne, cudaMemcpyDeviceToHost, H->stream);
+  if (e != cudaSuccess) return imodel::set_error(H, IMODEL_SWM_ECUDA, cudaGetErrorString(e));
+  return imodel::check_flags(H);
+}
+
+int imodel_swm_diagnostics(void *handle, imodel_swm_diag *out) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H || !out) return IMODEL_SWM_EINVAL;
+  if (!H->state_set) return imodel::set_error(H, IMODEL_SWM_ESTATE, "no state set");
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  if (H->precision == IMODEL_SWM_FP64) {
+    auto &W = H->W64;
+    imodel::launch_diag<double>(H->M, W, W.yn_h, W.yn_u, W.ya_h, W.ya_u, H->d_scratch,
+                                H->d_result, H->stream);
+  } else {
+    auto &W = H->W32;
+    imodel::launch_diag<float>(H->M, W, W.yn_h, W.yn_u, W.ya_h, W.ya_u, H->d_scratch,
+                               H->d_result, H->stream);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(H->h_result, H->d_result, sizeof(double) * imodel::kDiagQ,
+                        cudaMemcpyDeviceToHost, H->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+  if (e != cudaSuccess) return imodel::set_error(H, IMODEL_SWM_ECUDA, cudaGetErrorString(e));
+  const double *r = H->h_result;
+  const double g = H->M.grav;
+  const double A = r[imodel::Q_AREA];
+  std::memset(out, 0, sizeof(*out));
+  out->mass = r[imodel::Q_AH] / A;
+  out->penergy = r[imodel::Q_PE];
+  out->kenergy = r[imodel::Q_KE];
+  out->tenergy = out->penergy + out->kenergy;
+  const double mh = r[imodel::Q_AHB] / A;
+  const double unavail = 0.5 * g * (mh * mh * A - r[imodel::Q_AB2]);
+  out->availenergy = out->tenergy - unavail;
+  out->pot_enstrophy = r[imodel::Q_ENS];
+  out->rms_div = std::sqrt(r[imodel::Q_ADIV2] / A);
+  out->max_div = r[imodel::Q_MAXDIV];
+  out->nan_found = r[imodel::Q_NAN] != 0.0 ? 1 : 0;
+  out->learned_active = 0;
+  return IMODEL_SWM_OK;
+}
+
+int imodel_swm_errors(void *handle, const double *h_ref, const double *u_ref, double out[6]) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H || !h_ref || !u_ref || !out) return IMODEL_SWM_EINVAL;
+  if (!H->state_set) return imodel::set_error(H, IMODEL_SWM_ESTATE, "no state set");
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  cudaError_t e;
+  e = cudaMemcpyAsync(H->d_stage_h, h_ref, sizeof(double) * H->nv, cudaMemcpyHostToDevice, H->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(H->d_stage_u, u_ref, sizeof(double) * H->ne, cudaMemcpyHostToDevice, H->stream);
+  if (e != cudaSuccess) return imodel::set_error(H, IMODEL_SWM_ECUDA, cudaGetErrorString(e));
+  imodel::launch_gather_in(H->nv, H->d_cell_n2o, H->d_stage_h, H->d_ref_h, 0.0, H->stream);
+  imodel::launch_gather_in(H->ne, H->d_edge_n2o, H->d_stage_u, H->d_ref_u, 0.0, H->stream);
+  if (H->precision == IMODEL_SWM_FP64)
+    imodel::launch_errors<double>(H->M, H->W64.yn_h, H->W64.yn_u, 0.0, H->d_ref_h, H->d_ref_u,
+                                  H->d_scratch, H->d_result, H->stream);
+  else
+    imodel::launch_errors<float>(H->M, H->W32.yn_h, H->W32.yn_u, H->h_ref, H->d_ref_h,
+                                 H->d_ref_u, H->d_scratch, H->d_result, H->stream);
+  e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(H->h_result, H->d_result, sizeof(double) * 8, cudaMemcpyDeviceToHost,
+                        H->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+  if (e != cudaSuccess) return imodel::set_error(H, IMODEL_SWM_ECUDA, cudaGetErrorString(e));
+  const double *r = H->h_result;
+  // h: r[0] sum A dif^2, r[1] sum A ref^2, r[2] max|dif|, r[3] max|ref|
+  for (int f = 0; f < 2; ++f) {
+    const double *q = r + 4 * f;
+    const double area = f == 0 ? H->area_cells : H->area_edges;
+    out[3 * f + 0] = q[3] > 0 ? q[2] / q[3] : q[2];
+    out[3 * f + 1] = q[1] > 0 ? std::sqrt(q[0] / area) / std::sqrt(q[1] / area)
+                              : std::sqrt(q[0] / area);
+    out[3 * f + 2] = q[2];
+  }
+  return IMODEL_SWM_OK;
+}
+
+int imodel_swm_trsk_tangent(void *handle, const double *u, double *utg) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H || !u || !utg) return IMODEL_SWM_EINVAL;
+  if (H->nv == 0) return imodel::set_error(H, IMODEL_SWM_ESTATE, "handle was not created");
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  cudaError_t e = cudaMemcpyAsync(H->d_stage_u, u, sizeof(double) * H->ne,
+                                  cudaMemcpyHostToDevice, H->stream);
+  if (e != cudaSuccess) return imodel::set_error(H, IMODEL_SWM_ECUDA, cudaGetErrorString(e));
+  imodel::launch_gather_in(H->ne, H->d_edge_n2o, H->d_stage_u, H->d_ref_u, 0.0, H->stream);
+  imodel::launch_trsk_tangent(H->M, H->d_ref_u, H->d_stage_u, H->stream);
+  // d_stage_u now holds utg in device order; scatter it through d_ref_u
+  imodel::launch_scatter_out(H->ne, H->d_edge_n2o, H->d_stage_u, H->d_ref_u, 0.0, nullptr,
+                             H->stream);
+  e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(utg, H->d_ref_u, sizeof(double) * H->ne, cudaMemcpyDeviceToHost, H->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+  if (e != cudaSuccess) return imodel::set_error(H, IMODEL_SWM_ECUDA, cudaGetErrorString(e));
+  return IMODEL_SWM_OK;
+}
+
+int imodel_swm_profile(void *handle, double dt, int32_t nsteps, double avg_ms[4]) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H || !avg_ms || nsteps <= 0) return IMODEL_SWM_EINVAL;
+  if (!H->state_set) return imodel::set_error(H, IMODEL_SWM_ESTATE, "no state set");
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  cudaEvent_t ev[5];
+  for (int k = 0; k < 5; ++k)
+    if (cudaEventCreate(&ev[k]) != cudaSuccess)
+      return imodel::set_error(H, IMODEL_SWM_ECUDA, "cudaEventCreate failed");
+  double sum[4] = {0, 0, 0, 0};
+  cudaError_t e = cudaSuccess;
+  for (int step = 0; step < nsteps && e == cudaSuccess; ++step) {
+    for (int st = 0; st < 4 && e == cudaSuccess; ++st) {
+      if (H->precision == IMODEL_SWM_FP64) {
+        auto &W = H->W64;
+        const double *hi[4] = {W.yn_h, W.ya_h, W.yb_h, W.ya_h};
+        const double *ui[4] = {W.yn_u, W.ya_u, W.yb_u, W.ya_u};
+        double *ho[4] = {W.ya_h, W.yb_h, W.ya_h, W.yn_h};
+        double *uo[4] = {W.ya_u, W.yb_u, W.ya_u, W.yn_u};
+        imodel::launch_stage64(H->M, W, hi[st], ui[st], ho[st], uo[st], st, dt, H->stream, ev);
+      } else {
+        auto &W = H->W32;
+        const float *hi[4] = {W.yn_h, W.ya_h, W.yb_h, W.ya_h};
+        const float *ui[4] = {W.yn_u, W.ya_u, W.yb_u, W.ya_u};
+        float *ho[4] = {W.ya_h, W.yb_h, W.ya_h, W.yn_h};
+        float *uo[4] = {W.ya_u, W.yb_u, W.ya_u, W.yn_u};
+        imodel::launch_stage32(H->M, W, hi[st], ui[st], ho[st], uo[st], st,
+                               static_cast<float>(dt), H->stream, ev);
+      }
+      e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaEventSynchronize(ev[4]);
+      for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
+        float ms = 0.0f;
+        e = cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+        sum[k] += ms;
+      }
+    }
+  }
+  for (int k = 0; k < 5; ++k) cudaEventDestroy(ev[k]);
+  if (e != cudaSuccess) return imodel::set_error(H, IMODEL_SWM_ECUDA, cudaGetErrorString(e));
+  for (int k = 0; k < 4; ++k) avg_ms[k] = sum[k] / (4.0 * nsteps);
+  return imodel::check_flags(H);
+}
+
+int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count) {
+  if (!handle || !count || nsteps < 0) return IMODEL_SWM_EINVAL;
+  *count = static_cast<int64_t>(nsteps) * 4 * imodel::kLaunchesPerStage;
+  return IMODEL_SWM_OK;
+}
+
+const char *imodel_swm_main_kernel(void *handle) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H) return "";
+  return H->precision == IMODEL_SWM_FP64 ? "k_edge64" : "k_edge32";
+}
+
+void *imodel_swm_stream(void *handle) {
+  Handle *H = static_cast<Handle *>(handle);
+  return H ? static_cast<void *>(H->stream) : nullptr;
+}
+
+int imodel_swm_destroy(void *handle) {
+  imodel::destroy(static_cast<Handle *>(handle));
+  return IMODEL_SWM_OK;
+}
+
+const char *imodel_swm_last_error(void *handle) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H) return "NULL handle";
+  return H->err.c_str();
+}
+
+}  // extern "C"

@@ -1,0 +1,97 @@
+// Shared declarations of the TRSK shallow-water kernels (internal header).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace imodel {
+
+// Device copy of the layout (pointers into one device allocation each).
+struct DevMesh {
+  int nv, ne, nt;
+  double erad, grav;
+  // cells
+  const int8_t *c_nnb;
+  const int32_t *c_ed;
+  const double *c_sd, *c_areag, *c_cellarea, *c_bt;
+  const float *c_div32, *c_kew32, *c_bt32;
+  // edges
+  const int32_t *e_v, *e_sh;
+  const double *e_leng, *e_dleng, *e_kew, *e_area;
+  const float *e_grad32;
+  const int8_t *e_nst;
+  const int32_t *e_stk;
+  const double *e_stw;
+  const float *e_stc32;
+  // triangles
+  const int32_t *t_ed, *t_v;
+  const double *t_lt, *t_kite, *t_areag, *t_f;
+  const float *t_circ32, *t_kite32, *t_f32;
+};
+
+// Working fields of one handle, in the handle's precision T.
+template <class T>
+struct Work {
+  T *yn_h, *yn_u;    // state at t_n (advanced in place at the last stage)
+  T *ya_h, *ya_u;    // stage inputs (ping)
+  T *yb_h, *yb_u;    // stage inputs (pong)
+  T *acc_h, *acc_u;  // k0 + 2 k1 + 2 k2
+  T *q_tr;           // [nt] potential vorticity at triangles
+  T *h_ed, *uh, *q_ed;  // [ne]
+  T *bern;           // [nv] g (h + b) + K
+  T *tend_h, *tend_u;   // tendency outputs (tendency-only evaluations)
+  int *flags;        // bit 0: PV division by ~0
+  T h_ref;           // FP32: h is stored as h - h_ref
+  int pv_on;         // testcase >= 2: q = eta / h_tr, else q = 0
+  int mom_on;        // testcase >= 2: momentum tendency kept, else zeroed
+};
+
+// One tendency evaluation (stage < 0: write masseq/momeq to tend_*), or RK4
+// stage `stage` (0..3) of classic RK4 reading y_in and writing y_out.
+// ev (may be NULL): 5 events recorded before, between and after the four
+// kernels of the stage, for per-kernel timing outside graph capture.
+void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
+                    const double *u_in, double *h_out, double *u_out, int stage,
+                    double dt, cudaStream_t s, cudaEvent_t *ev = nullptr);
+void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
+                    const float *u_in, float *h_out, float *u_out, int stage, float dt,
+                    cudaStream_t s, cudaEvent_t *ev = nullptr);
+constexpr int kLaunchesPerStage = 4;
+
+// reference order <-> device order, with precision conversion
+void launch_gather_in(int n, const int32_t *n2o, const double *src, double *dst, double shift,
+                      cudaStream_t s);
+void launch_gather_in32(int n, const int32_t *n2o, const double *src, float *dst, double shift,
+                        cudaStream_t s);
+// flags may be NULL; otherwise bit 1 is set when a value is NaN/Inf
+void launch_scatter_out(int n, const int32_t *n2o, const double *src, double *dst, double shift,
+                        int *flags, cudaStream_t s);
+void launch_scatter_out32(int n, const int32_t *n2o, const float *src, double *dst,
+                          double shift, int *flags, cudaStream_t s);
+
+// edge averages h_ed (for the kinetic energy integral) of a state
+void launch_hed64(const DevMesh &M, const Work<double> &W, const double *h, cudaStream_t s);
+void launch_hed32(const DevMesh &M, const Work<float> &W, const float *h, cudaStream_t s);
+
+// Compensated FP64 integrals.  Scratch: partial sums, 2 doubles per block
+// and quantity; result[kDiagQ] on the device.
+constexpr int kDiagQ = 12;
+constexpr int kRedBlocks = 304;   // 2 blocks per SM on 152 SMs
+constexpr int kRedThreads = 256;
+// result indices
+enum {
+  Q_AREA = 0, Q_AH, Q_PE, Q_AHB, Q_AB2, Q_KE, Q_ENS, Q_ADIV2, Q_MAXDIV, Q_NAN,
+  Q_SPARE0, Q_SPARE1
+};
+template <class T>
+void launch_diag(const DevMesh &M, const Work<T> &W, const T *h, const T *u, const T *hs,
+                 const T *us, double *scratch, double *result, cudaStream_t s);
+// error_calc partials: {sum A dif^2, sum A ref^2, max|dif|, max|ref|} for h
+// then for u.
+template <class T>
+void launch_errors(const DevMesh &M, const T *h, const T *u, double h_ref, const double *href,
+                   const double *uref, double *scratch, double *result, cudaStream_t s);
+// vecrecon_trsk_tg at every edge (FP64, reference order); u and utg in
+// device order
+void launch_trsk_tangent(const DevMesh &M, const double *u, double *utg, cudaStream_t s);
+
+}  // namespace imodel

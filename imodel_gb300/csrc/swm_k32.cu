@@ -1,0 +1,160 @@
+// FP32 kernels of the TRSK shallow-water step.
+//
+// Same data flow as the FP64 kernels (triangle -> edge -> cell -> edge per
+// RK stage), with every constant factor of a term folded into one
+// coefficient computed in FP64 and rounded once, and the thickness stored as
+// a deviation from a constant reference depth h_ref so that the FP32 state
+// keeps ~1e-5 m resolution on ~3 km deep layers.
+#include "swm_common.cuh"
+
+namespace imodel {
+namespace {
+
+__device__ __forceinline__ float rk_stage32(int stage, float k, float yn, float *acc, float dt) {
+  // ode_rk4, swm.f90:2647-2678
+  if (stage == 0) {
+    *acc = k;
+    return yn + 0.5f * dt * k;
+  } else if (stage == 1) {
+    *acc = *acc + 2.0f * k;
+    return yn + 0.5f * dt * k;
+  } else if (stage == 2) {
+    *acc = *acc + 2.0f * k;
+    return yn + dt * k;
+  }
+  return yn + dt * (*acc + k) * (1.0f / 6.0f);
+}
+
+// q_t = (curl u / A + f) / h_t  (vort_tr + scalar_hx2tr + scalar_elem_divide)
+__global__ void __launch_bounds__(256) k_tri32(DevMesh M, const float *__restrict__ hd,
+                                               const float *__restrict__ u,
+                                               float *__restrict__ q_tr, float h_ref,
+                                               int pv_on, int *flags) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = M.nt;
+  if (t >= nt) return;
+  float eta = M.t_f32[t];
+  float ht = 0.0f;
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    eta += __ldg(&M.t_circ32[s * nt + t]) * u[__ldg(&M.t_ed[s * nt + t])];
+    ht += __ldg(&M.t_kite32[s * nt + t]) * hd[__ldg(&M.t_v[s * nt + t])];
+  }
+  ht += h_ref;
+  float q = 0.0f;
+  if (pv_on) {
+    // scalar_elem_divide guard, swm_operators.f90:1604-1606
+    if (fabsf(ht) < 1.1920928955078125e-12f)
+      atomicOr(flags, 1);
+    else
+      q = eta / ht;
+  }
+  q_tr[t] = q;
+}
+
+// h_e (deviation), flux F_e = u_e (h_ref + h_e), q_e
+__global__ void __launch_bounds__(256) k_edge_pre32(DevMesh M, const float *__restrict__ hd,
+                                                    const float *__restrict__ u,
+                                                    const float *__restrict__ q_tr,
+                                                    float *__restrict__ h_ed,
+                                                    float *__restrict__ uh,
+                                                    float *__restrict__ q_ed, float h_ref) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ne = M.ne;
+  if (e >= ne) return;
+  const float he = 0.5f * (hd[__ldg(&M.e_v[e])] + hd[__ldg(&M.e_v[ne + e])]);
+  h_ed[e] = he;
+  uh[e] = u[e] * (h_ref + he);
+  q_ed[e] = 0.5f * (q_tr[__ldg(&M.e_sh[e])] + q_tr[__ldg(&M.e_sh[ne + e])]);
+}
+
+// -div F, K, Bernoulli potential g (h - h_ref + b) + K, mass RK stage
+__global__ void __launch_bounds__(256) k_cell32(DevMesh M, const float *__restrict__ hd,
+                                                const float *__restrict__ u,
+                                                const float *__restrict__ uh,
+                                                float *__restrict__ bern,
+                                                const float *__restrict__ yn,
+                                                float *__restrict__ acc,
+                                                float *__restrict__ yout,
+                                                float *__restrict__ tend, int stage, float dt,
+                                                float grav) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nv = M.nv;
+  if (i >= nv) return;
+  const int n = M.c_nnb[i];
+  float d = 0.0f, k = 0.0f;
+  for (int j = 0; j < n; ++j) {
+    const int e = __ldg(&M.c_ed[j * nv + i]);
+    const float ue = u[e];
+    d += __ldg(&M.c_div32[j * nv + i]) * uh[e];
+    k += __ldg(&M.c_kew32[j * nv + i]) * (ue * ue);
+  }
+  bern[i] = grav * (hd[i] + __ldg(&M.c_bt32[i])) + k;
+  const float masseq = -d;
+  if (stage < 0)
+    tend[i] = masseq;
+  else
+    yout[i] = rk_stage32(stage, masseq, yn[i], acc + i, dt);
+}
+
+// -grad B - TRSK PV flux, momentum RK stage
+__global__ void __launch_bounds__(256) k_edge32(DevMesh M, const float *__restrict__ bern,
+                                                const float *__restrict__ uh,
+                                                const float *__restrict__ q_ed,
+                                                const float *__restrict__ yn,
+                                                float *__restrict__ acc,
+                                                float *__restrict__ yout,
+                                                float *__restrict__ tend, int stage, float dt,
+                                                int mom_on) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ne = M.ne;
+  if (e >= ne) return;
+  const float g = (bern[__ldg(&M.e_v[ne + e])] - bern[__ldg(&M.e_v[e])]) * __ldg(&M.e_grad32[e]);
+  const float qe = q_ed[e];
+  const int ns = M.e_nst[e];
+  float q = 0.0f;
+  for (int s = 0; s < ns; ++s) {
+    const int k = __ldg(&M.e_stk[s * ne + e]);
+    q += __ldg(&M.e_stc32[s * ne + e]) * uh[k] * (qe + q_ed[k]);
+  }
+  float momeq = -g - q;
+  if (!mom_on) momeq = 0.0f;
+  if (stage < 0)
+    tend[e] = momeq;
+  else
+    yout[e] = rk_stage32(stage, momeq, yn[e], acc + e, dt);
+}
+
+__global__ void k_hed32(DevMesh M, const float *__restrict__ hd, float *__restrict__ h_ed) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= M.ne) return;
+  h_ed[e] = 0.5f * (hd[M.e_v[e]] + hd[M.e_v[M.ne + e]]);
+}
+
+inline int nblocks(int n, int t) { return (n + t - 1) / t; }
+
+}  // namespace
+
+void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
+                    const float *u_in, float *h_out, float *u_out, int stage, float dt,
+                    cudaStream_t s, cudaEvent_t *ev) {
+  if (ev) cudaEventRecord(ev[0], s);
+  k_tri32<<<nblocks(M.nt, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ref, W.pv_on, W.flags);
+  if (ev) cudaEventRecord(ev[1], s);
+  k_edge_pre32<<<nblocks(M.ne, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ed, W.uh, W.q_ed,
+                                                   W.h_ref);
+  if (ev) cudaEventRecord(ev[2], s);
+  k_cell32<<<nblocks(M.nv, 256), 256, 0, s>>>(M, h_in, u_in, W.uh, W.bern, W.yn_h, W.acc_h,
+                                               h_out, W.tend_h, stage, dt,
+                                               static_cast<float>(M.grav));
+  if (ev) cudaEventRecord(ev[3], s);
+  k_edge32<<<nblocks(M.ne, 256), 256, 0, s>>>(M, W.bern, W.uh, W.q_ed, W.yn_u, W.acc_u, u_out,
+                                               W.tend_u, stage, dt, W.mom_on);
+  if (ev) cudaEventRecord(ev[4], s);
+}
+
+void launch_hed32(const DevMesh &M, const Work<float> &W, const float *h, cudaStream_t s) {
+  k_hed32<<<nblocks(M.ne, 256), 256, 0, s>>>(M, h, W.h_ed);
+}
+
+}  // namespace imodel

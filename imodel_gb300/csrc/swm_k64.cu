@@ -1,0 +1,481 @@
+// FP64 kernels in the reference's operation order, plus the layout
+// permutations and the compensated FP64 integrals.
+//
+// This translation unit is compiled with --fmad=false: every product and sum
+// below is rounded on its own, as in the Fortran built without contraction,
+// so that the FP64 step reproduces the reference arithmetic of
+// src/swm.f90:2416-2683 and src/swm_operators.f90 bit for bit.
+#include "swm_common.cuh"
+
+namespace imodel {
+namespace {
+
+// constants.f90:45 -- eps = epsilon(1.) (float epsilon)
+constexpr double kEps = 1.1920928955078125e-07;
+
+template <class T>
+__device__ __forceinline__ T rk_stage(int stage, T k, T yn, T *acc, T dt) {
+  // ode_rk4, swm.f90:2647-2678
+  if (stage == 0) {
+    *acc = k;
+    return yn + dt * k / T(2);
+  } else if (stage == 1) {
+    *acc = *acc + T(2) * k;
+    return yn + dt * k / T(2);
+  } else if (stage == 2) {
+    *acc = *acc + T(2) * k;
+    return yn + dt * k;
+  }
+  return yn + dt * (*acc + k) / T(6);
+}
+
+// vort_tr (:551-611) + scalar_hx2tr (:229-284) + scalar_elem_divide (:1579)
+__global__ void __launch_bounds__(256) k_tri64(DevMesh M, const double *__restrict__ h,
+                                               const double *__restrict__ u,
+                                               double *__restrict__ q_tr, int pv_on,
+                                               int *flags) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = M.nt;
+  if (t >= nt) return;
+  double e = 0.0;
+#pragma unroll
+  for (int s = 0; s < 3; ++s) e = e + u[M.t_ed[s * nt + t]] * M.t_lt[s * nt + t];
+  const double A = M.t_areag[t];
+  e = e / A / M.erad;
+  e = e + M.t_f[t];
+  double ht = 0.0;
+#pragma unroll
+  for (int s = 0; s < 3; ++s) ht = ht + M.t_kite[s * nt + t] * h[M.t_v[s * nt + t]];
+  ht = ht / A;
+  double q = 0.0;
+  if (pv_on) {
+    if (fabs(ht) < kEps / 100000.0)
+      atomicOr(flags, 1);
+    else
+      q = e / ht;
+  }
+  q_tr[t] = q;
+}
+
+// scalar_hx2ed (:89-97), scalar_elem_product (:1546), scalar_tr2ed (:124)
+__global__ void __launch_bounds__(256) k_edge_pre64(DevMesh M, const double *__restrict__ h,
+                                                    const double *__restrict__ u,
+                                                    const double *__restrict__ q_tr,
+                                                    double *__restrict__ h_ed,
+                                                    double *__restrict__ uh,
+                                                    double *__restrict__ q_ed) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ne = M.ne;
+  if (e >= ne) return;
+  const double he = (h[M.e_v[e]] + h[M.e_v[ne + e]]) * 0.5;
+  h_ed[e] = he;
+  uh[e] = u[e] * he;
+  q_ed[e] = 0.5 * (q_tr[M.e_sh[e]] + q_tr[M.e_sh[ne + e]]);
+}
+
+// div_hx(uh) (:613-661), kinetic_energy_hx trsk (:1162-1171), Bernoulli
+// potential (swm.f90:2533-2536) and the mass-equation RK stage
+__global__ void __launch_bounds__(256) k_cell64(DevMesh M, const double *__restrict__ h,
+                                                const double *__restrict__ u,
+                                                const double *__restrict__ uh,
+                                                double *__restrict__ bern,
+                                                const double *__restrict__ yn,
+                                                double *__restrict__ acc,
+                                                double *__restrict__ yout,
+                                                double *__restrict__ tend, int stage,
+                                                double dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nv = M.nv;
+  if (i >= nv) return;
+  const int n = M.c_nnb[i];
+  double d = 0.0, k = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const int e = M.c_ed[j * nv + i];
+    d = d + uh[e] * M.c_sd[j * nv + i];
+    const double ue = u[e];
+    k = k + M.e_kew[e] * (ue * ue);
+  }
+  const double divuh = d / M.c_areag[i] / M.erad;
+  const double ke = k / M.c_cellarea[i];
+  bern[i] = M.grav * (h[i] + M.c_bt[i]) + ke;
+  const double masseq = -divuh;
+  if (stage < 0)
+    tend[i] = masseq;
+  else
+    yout[i] = rk_stage(stage, masseq, yn[i], acc + i, dt);
+}
+
+// grad_ed (:511-548) + coriolis_ed TRSK (:1283-1308) and the momentum RK stage
+__global__ void __launch_bounds__(256) k_edge64(DevMesh M, const double *__restrict__ bern,
+                                                const double *__restrict__ uh,
+                                                const double *__restrict__ q_ed,
+                                                const double *__restrict__ yn,
+                                                double *__restrict__ acc,
+                                                double *__restrict__ yout,
+                                                double *__restrict__ tend, int stage,
+                                                double dt, int mom_on) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ne = M.ne;
+  if (e >= ne) return;
+  const double l = M.e_leng[e];
+  double g = bern[M.e_v[ne + e]] - bern[M.e_v[e]];
+  g = g / l / M.erad;
+  const double qe = q_ed[e];
+  const int ns = M.e_nst[e];
+  double q = 0.0;
+  for (int s = 0; s < ns; ++s) {
+    const int k = M.e_stk[s * ne + e];
+    const double qtmp = 0.5 * (qe + q_ed[k]);
+    q = q + uh[k] * qtmp * M.e_dleng[k] * M.e_stw[s * ne + e];
+  }
+  q = q / l;
+  double momeq = -g - q;
+  if (!mom_on) momeq = 0.0;
+  if (stage < 0)
+    tend[e] = momeq;
+  else
+    yout[e] = rk_stage(stage, momeq, yn[e], acc + e, dt);
+}
+
+__global__ void k_hed64(DevMesh M, const double *__restrict__ h, double *__restrict__ h_ed) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= M.ne) return;
+  h_ed[e] = (h[M.e_v[e]] + h[M.e_v[M.ne + e]]) * 0.5;
+}
+
+template <class T>
+__global__ void k_gather_in(int n, const int32_t *__restrict__ n2o, const double *__restrict__ src,
+                            T *__restrict__ dst, double shift) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = static_cast<T>(src[n2o[i]] - shift);
+}
+
+// scatter back to reference order; bit 1 of *flags marks a NaN/Inf value
+template <class T>
+__global__ void k_scatter_out(int n, const int32_t *__restrict__ n2o, const T *__restrict__ src,
+                              double *__restrict__ dst, double shift, int *flags) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double v = static_cast<double>(src[i]) + shift;
+    dst[n2o[i]] = v;
+    if (flags && !isfinite(v)) atomicOr(flags, 2);
+  }
+}
+
+// vecrecon_trsk_tg, interpack.f90:3852-3976 (var%pos == 6)
+__global__ void k_trsk_tangent(DevMesh M, const double *__restrict__ u, double *__restrict__ utg) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ne = M.ne;
+  if (e >= ne) return;
+  const int ns = M.e_nst[e];
+  double t = 0.0;
+  for (int s = 0; s < ns; ++s) {
+    const int k = M.e_stk[s * ne + e];
+    t = t + u[k] * M.e_dleng[k] * M.e_stw[s * ne + e];
+  }
+  utg[e] = -t / M.e_leng[e];
+}
+
+// ---- compensated summation (Neumaier) -------------------------------------
+struct KSum {
+  double s, c;
+  __device__ void add(double x) {
+    const double t = s + x;
+    if (fabs(s) >= fabs(x))
+      c = c + ((s - t) + x);
+    else
+      c = c + ((x - t) + s);
+    s = t;
+  }
+  __device__ void merge(const KSum &o) {
+    add(o.s);
+    c = c + o.c;
+  }
+};
+
+template <int NQ>
+__device__ void block_reduce_store(KSum (&acc)[NQ], double *__restrict__ scratch) {
+  // warp level
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    for (int off = 16; off > 0; off >>= 1) {
+      KSum o;
+      o.s = __shfl_down_sync(0xffffffffu, acc[q].s, off);
+      o.c = __shfl_down_sync(0xffffffffu, acc[q].c, off);
+      acc[q].merge(o);
+    }
+  }
+  __shared__ double sh[kRedThreads / 32][NQ][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      sh[warp][q][0] = acc[q].s;
+      sh[warp][q][1] = acc[q].c;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < NQ) {
+    const int q = threadIdx.x;
+    KSum t{0.0, 0.0};
+    for (int w = 0; w < kRedThreads / 32; ++w) {
+      KSum o{sh[w][q][0], sh[w][q][1]};
+      t.merge(o);
+    }
+    scratch[(q * gridDim.x + blockIdx.x) * 2] = t.s;
+    scratch[(q * gridDim.x + blockIdx.x) * 2 + 1] = t.c;
+  }
+}
+
+// one block: quantity q summed over nblk partials; "max" quantities use max
+__global__ void k_finalize(const double *__restrict__ scratch, int nblk, int nq,
+                           unsigned maxmask, double *__restrict__ result) {
+  const int q = blockIdx.x;
+  if (q >= nq) return;
+  __shared__ double ss[kRedThreads], sc[kRedThreads];
+  const bool is_max = (maxmask >> q) & 1u;
+  KSum a{0.0, 0.0};
+  double m = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+    const double s = scratch[(q * nblk + b) * 2], c = scratch[(q * nblk + b) * 2 + 1];
+    if (is_max) {
+      m = fmax(m, s);
+    } else {
+      KSum o{s, c};
+      a.merge(o);
+    }
+  }
+  ss[threadIdx.x] = is_max ? m : a.s;
+  sc[threadIdx.x] = is_max ? 0.0 : a.c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (is_max) {
+      double r = 0.0;
+      for (int t = 0; t < blockDim.x; ++t) r = fmax(r, ss[t]);
+      result[q] = r;
+    } else {
+      KSum r{0.0, 0.0};
+      for (int t = 0; t < blockDim.x; ++t) {
+        KSum o{ss[t], sc[t]};
+        r.merge(o);
+      }
+      result[q] = r.s + r.c;
+    }
+  }
+}
+
+// calc_energies (swm.f90:2686-2752), sumf_areas (:3394), potential enstrophy,
+// RMS divergence of the last stage input (hs, us), NaN scan.
+template <class T>
+__global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__restrict__ h,
+                                                      const T *__restrict__ u,
+                                                      const T *__restrict__ hs,
+                                                      const T *__restrict__ us,
+                                                      const T *__restrict__ h_ed, double h_ref,
+                                                      double *__restrict__ scratch) {
+  KSum acc[kDiagQ];
+#pragma unroll
+  for (int q = 0; q < kDiagQ; ++q) acc[q] = KSum{0.0, 0.0};
+  const int stride = gridDim.x * blockDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const double g = M.grav, erad = M.erad;
+  double maxdiv = 0.0;
+  double nan = 0.0;
+  for (int i = tid; i < M.nv; i += stride) {
+    const double A = M.c_areag[i];
+    const double hi = static_cast<double>(h[i]) + h_ref;
+    const double b = M.c_bt[i];
+    if (!isfinite(hi)) nan = 1.0;
+    acc[Q_AREA].add(A);
+    acc[Q_AH].add(A * hi);
+    acc[Q_PE].add(A * g * hi * (hi * 0.5 + b));
+    acc[Q_AHB].add(A * (hi + b));
+    acc[Q_AB2].add(A * b * b);
+    // div_hx(u) of the last stage input (diagnostic in tendency, :2570)
+    const int n = M.c_nnb[i];
+    double d = 0.0;
+    for (int j = 0; j < n; ++j) {
+      const int e = M.c_ed[j * M.nv + i];
+      d = d + static_cast<double>(us[e]) * M.c_sd[j * M.nv + i];
+    }
+    d = d / A / erad;
+    acc[Q_ADIV2].add(A * (d * d));
+    maxdiv = fmax(maxdiv, fabs(d));
+  }
+  for (int e = tid; e < M.ne; e += stride) {
+    const double ue = static_cast<double>(u[e]);
+    if (!isfinite(ue)) nan = 1.0;
+    const double he = static_cast<double>(h_ed[e]) + h_ref;
+    acc[Q_KE].add(M.e_area[e] * he * (ue * ue));
+  }
+  for (int t = tid; t < M.nt; t += stride) {
+    double eta = 0.0, ht = 0.0;
+    for (int s = 0; s < 3; ++s) {
+      eta = eta + static_cast<double>(us[M.t_ed[s * M.nt + t]]) * M.t_lt[s * M.nt + t];
+      ht = ht + M.t_kite[s * M.nt + t] * (static_cast<double>(hs[M.t_v[s * M.nt + t]]) + h_ref);
+    }
+    const double A = M.t_areag[t];
+    eta = eta / A / erad;
+    eta = eta + M.t_f[t];
+    ht = ht / A;
+    const double q = ht != 0.0 ? eta / ht : 0.0;
+    acc[Q_ENS].add(A * ht * (q * q) * 0.5);
+  }
+  acc[Q_MAXDIV].s = maxdiv;
+  acc[Q_NAN].s = nan;
+  // max-type entries are reduced with max, not a sum: pre-reduce them
+  for (int off = 16; off > 0; off >>= 1) {
+    acc[Q_MAXDIV].s = fmax(acc[Q_MAXDIV].s, __shfl_down_sync(0xffffffffu, acc[Q_MAXDIV].s, off));
+    acc[Q_NAN].s = fmax(acc[Q_NAN].s, __shfl_down_sync(0xffffffffu, acc[Q_NAN].s, off));
+  }
+  __shared__ double smax[2][kRedThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    smax[0][warp] = acc[Q_MAXDIV].s;
+    smax[1][warp] = acc[Q_NAN].s;
+  }
+  __syncthreads();
+  double bmax = 0.0, bnan = 0.0;
+  for (int w = 0; w < kRedThreads / 32; ++w) {
+    bmax = fmax(bmax, smax[0][w]);
+    bnan = fmax(bnan, smax[1][w]);
+  }
+  acc[Q_MAXDIV] = KSum{0.0, 0.0};
+  acc[Q_NAN] = KSum{0.0, 0.0};
+  block_reduce_store<kDiagQ>(acc, scratch);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    scratch[(Q_MAXDIV * gridDim.x + blockIdx.x) * 2] = bmax;
+    scratch[(Q_NAN * gridDim.x + blockIdx.x) * 2] = bnan;
+  }
+}
+
+// error_calc partials (swm.f90:3492-3543): weights A_i (cells) and l*d/2
+// (edges, sumfsq_areas :3468-3474)
+template <class T>
+__global__ void __launch_bounds__(kRedThreads) k_errors(DevMesh M, const T *__restrict__ h,
+                                                        const T *__restrict__ u, double h_ref,
+                                                        const double *__restrict__ href,
+                                                        const double *__restrict__ uref,
+                                                        double *__restrict__ scratch) {
+  constexpr int NQ = 8;
+  KSum acc[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) acc[q] = KSum{0.0, 0.0};
+  const int stride = gridDim.x * blockDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  double mdh = 0.0, mrh = 0.0, mdu = 0.0, mru = 0.0;
+  for (int i = tid; i < M.nv; i += stride) {
+    const double A = M.c_areag[i];
+    const double r = href[i];
+    const double dif = (static_cast<double>(h[i]) + h_ref) - r;
+    acc[0].add(A * (dif * dif));
+    acc[1].add(A * (r * r));
+    mdh = fmax(mdh, fabs(dif));
+    mrh = fmax(mrh, fabs(r));
+  }
+  for (int e = tid; e < M.ne; e += stride) {
+    const double w = M.e_area[e];
+    const double r = uref[e];
+    const double dif = static_cast<double>(u[e]) - r;
+    acc[4].add(w * (dif * dif));
+    acc[5].add(w * (r * r));
+    mdu = fmax(mdu, fabs(dif));
+    mru = fmax(mru, fabs(r));
+  }
+  double mx[4] = {mdh, mrh, mdu, mru};
+  for (int k = 0; k < 4; ++k)
+    for (int off = 16; off > 0; off >>= 1) mx[k] = fmax(mx[k], __shfl_down_sync(0xffffffffu, mx[k], off));
+  __shared__ double smax[4][kRedThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+    for (int k = 0; k < 4; ++k) smax[k][warp] = mx[k];
+  __syncthreads();
+  double bm[4] = {0, 0, 0, 0};
+  for (int k = 0; k < 4; ++k)
+    for (int w = 0; w < kRedThreads / 32; ++w) bm[k] = fmax(bm[k], smax[k][w]);
+  block_reduce_store<NQ>(acc, scratch);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    scratch[(2 * gridDim.x + blockIdx.x) * 2] = bm[0];
+    scratch[(3 * gridDim.x + blockIdx.x) * 2] = bm[1];
+    scratch[(6 * gridDim.x + blockIdx.x) * 2] = bm[2];
+    scratch[(7 * gridDim.x + blockIdx.x) * 2] = bm[3];
+  }
+}
+
+inline int nblocks(int n, int t) { return (n + t - 1) / t; }
+
+}  // namespace
+
+void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
+                    const double *u_in, double *h_out, double *u_out, int stage, double dt,
+                    cudaStream_t s, cudaEvent_t *ev) {
+  if (ev) cudaEventRecord(ev[0], s);
+  k_tri64<<<nblocks(M.nt, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.pv_on, W.flags);
+  if (ev) cudaEventRecord(ev[1], s);
+  k_edge_pre64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ed, W.uh, W.q_ed);
+  if (ev) cudaEventRecord(ev[2], s);
+  k_cell64<<<nblocks(M.nv, 256), 256, 0, s>>>(M, h_in, u_in, W.uh, W.bern, W.yn_h, W.acc_h,
+                                               h_out, W.tend_h, stage, dt);
+  if (ev) cudaEventRecord(ev[3], s);
+  k_edge64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, W.bern, W.uh, W.q_ed, W.yn_u, W.acc_u, u_out,
+                                               W.tend_u, stage, dt, W.mom_on);
+  if (ev) cudaEventRecord(ev[4], s);
+}
+
+void launch_hed64(const DevMesh &M, const Work<double> &W, const double *h, cudaStream_t s) {
+  k_hed64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, h, W.h_ed);
+}
+
+void launch_gather_in(int n, const int32_t *n2o, const double *src, double *dst, double shift,
+                      cudaStream_t s) {
+  k_gather_in<double><<<nblocks(n, 256), 256, 0, s>>>(n, n2o, src, dst, shift);
+}
+void launch_gather_in32(int n, const int32_t *n2o, const double *src, float *dst, double shift,
+                        cudaStream_t s) {
+  k_gather_in<float><<<nblocks(n, 256), 256, 0, s>>>(n, n2o, src, dst, shift);
+}
+void launch_scatter_out(int n, const int32_t *n2o, const double *src, double *dst, double shift,
+                        int *flags, cudaStream_t s) {
+  k_scatter_out<double><<<nblocks(n, 256), 256, 0, s>>>(n, n2o, src, dst, shift, flags);
+}
+void launch_scatter_out32(int n, const int32_t *n2o, const float *src, double *dst,
+                          double shift, int *flags, cudaStream_t s) {
+  k_scatter_out<float><<<nblocks(n, 256), 256, 0, s>>>(n, n2o, src, dst, shift, flags);
+}
+
+void launch_trsk_tangent(const DevMesh &M, const double *u, double *utg, cudaStream_t s) {
+  k_trsk_tangent<<<nblocks(M.ne, 256), 256, 0, s>>>(M, u, utg);
+}
+
+template <class T>
+void launch_diag(const DevMesh &M, const Work<T> &W, const T *h, const T *u, const T *hs,
+                 const T *us, double *scratch, double *result, cudaStream_t s) {
+  k_diag<T><<<kRedBlocks, kRedThreads, 0, s>>>(M, h, u, hs, us, W.h_ed,
+                                                static_cast<double>(W.h_ref), scratch);
+  const unsigned maxmask = (1u << Q_MAXDIV) | (1u << Q_NAN);
+  k_finalize<<<kDiagQ, kRedThreads, 0, s>>>(scratch, kRedBlocks, kDiagQ, maxmask, result);
+}
+template void launch_diag<double>(const DevMesh &, const Work<double> &, const double *,
+                                  const double *, const double *, const double *, double *,
+                                  double *, cudaStream_t);
+template void launch_diag<float>(const DevMesh &, const Work<float> &, const float *,
+                                 const float *, const float *, const float *, double *,
+                                 double *, cudaStream_t);
+
+template <class T>
+void launch_errors(const DevMesh &M, const T *h, const T *u, double h_ref, const double *href,
+                   const double *uref, double *scratch, double *result, cudaStream_t s) {
+  k_errors<T><<<kRedBlocks, kRedThreads, 0, s>>>(M, h, u, h_ref, href, uref, scratch);
+  const unsigned maxmask = (1u << 2) | (1u << 3) | (1u << 6) | (1u << 7);
+  k_finalize<<<8, kRedThreads, 0, s>>>(scratch, kRedBlocks, 8, maxmask, result);
+}
+template void launch_errors<double>(const DevMesh &, const double *, const double *, double,
+                                    const double *, const double *, double *, double *,
+                                    cudaStream_t);
+template void launch_errors<float>(const DevMesh &, const float *, const float *, double,
+                                   const double *, const double *, double *, double *,
+                                   cudaStream_t);
+
+}  // namespace imodel

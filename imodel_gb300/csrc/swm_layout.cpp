@@ -1,0 +1,253 @@
+// Host construction of the device layout (see swm_layout.h).
+#include "swm_layout.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+namespace imodel {
+namespace {
+
+// 3-D Hilbert index of integer coordinates (b bits each), following the
+// transpose formulation published by J. Skilling, "Programming the Hilbert
+// curve", AIP Conf. Proc. 707 (2004).
+uint64_t hilbert3(uint32_t x0, uint32_t x1, uint32_t x2, int b) {
+  uint32_t X[3] = {x0, x1, x2};
+  const uint32_t M = 1u << (b - 1);
+  for (uint32_t Q = M; Q > 1; Q >>= 1) {
+    const uint32_t P = Q - 1;
+    for (int i = 0; i < 3; ++i) {
+      if (X[i] & Q) {
+        X[0] ^= P;
+      } else {
+        uint32_t t = (X[0] ^ X[i]) & P;
+        X[0] ^= t;
+        X[i] ^= t;
+      }
+    }
+  }
+  for (int i = 1; i < 3; ++i) X[i] ^= X[i - 1];
+  uint32_t t = 0;
+  for (uint32_t Q = M; Q > 1; Q >>= 1)
+    if (X[2] & Q) t ^= Q - 1;
+  for (int i = 0; i < 3; ++i) X[i] ^= t;
+  uint64_t key = 0;
+  for (int bit = b - 1; bit >= 0; --bit)
+    for (int i = 0; i < 3; ++i) key = (key << 1) | ((X[i] >> bit) & 1u);
+  return key;
+}
+
+uint32_t quant(double x, int b) {
+  const double s = static_cast<double>((1u << b) - 1);
+  double q = (x + 1.0) * 0.5 * s + 0.5;
+  if (q < 0) q = 0;
+  if (q > s) q = s;
+  return static_cast<uint32_t>(q);
+}
+
+template <class Key>
+void sort_perm(std::vector<int32_t> &n2o, std::vector<int32_t> &o2n, const std::vector<Key> &key) {
+  const size_t n = key.size();
+  n2o.resize(n);
+  std::iota(n2o.begin(), n2o.end(), 0);
+  std::stable_sort(n2o.begin(), n2o.end(),
+                   [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+  o2n.resize(n);
+  for (size_t i = 0; i < n; ++i) o2n[n2o[i]] = static_cast<int32_t>(i);
+}
+
+}  // namespace
+
+std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) {
+  const int nv = m.nv, ne = m.ne, nt = m.nt;
+  if (nv < 4 || ne < 6 || nt < 4) return "mesh sizes too small";
+  if (!m.nnb || !m.v_ed || !m.v_tr || !m.hx_ttgout || !m.hx_tnrccw || !m.hx_areag ||
+      !m.hx_trskw || !m.v_p || !m.ed_v || !m.ed_sh || !m.ed_leng || !m.edhx_leng ||
+      !m.tr_v || !m.tr_ed || !m.tr_tg || !m.tr_areag || !m.tr_trhx_area || !m.tr_c_lat)
+    return "mesh array pointer is NULL";
+  if (!(m.erad > 0) || !(m.grav > 0)) return "erad and grav must be positive";
+  for (int i = 0; i < nv; ++i) {
+    int n = m.nnb[i];
+    if (n < 3 || n > kMaxNb) return "nnb outside 3..6 at cell " + std::to_string(i + 1);
+    for (int j = 0; j < n; ++j) {
+      int e = m.v_ed[6 * static_cast<size_t>(i) + j];
+      if (e < 1 || e > ne) return "v_ed index out of range at cell " + std::to_string(i + 1);
+    }
+    if (!(m.hx_areag[i] > 0)) return "non-positive hx_areag at cell " + std::to_string(i + 1);
+  }
+  for (int e = 0; e < ne; ++e) {
+    for (int s = 0; s < 2; ++s) {
+      int c = m.ed_v[2 * static_cast<size_t>(e) + s], t = m.ed_sh[2 * static_cast<size_t>(e) + s];
+      if (c < 1 || c > nv) return "ed_v index out of range at edge " + std::to_string(e + 1);
+      if (t < 1 || t > nt) return "ed_sh index out of range at edge " + std::to_string(e + 1);
+    }
+    if (!(m.ed_leng[e] > 0)) return "non-positive ed_leng at edge " + std::to_string(e + 1);
+  }
+  for (int t = 0; t < nt; ++t) {
+    for (int s = 0; s < 3; ++s) {
+      int c = m.tr_v[3 * static_cast<size_t>(t) + s], e = m.tr_ed[3 * static_cast<size_t>(t) + s];
+      if (c < 1 || c > nv || e < 1 || e > ne)
+        return "tr_v/tr_ed index out of range at triangle " + std::to_string(t + 1);
+    }
+    if (!(m.tr_areag[t] > 0)) return "non-positive tr_areag at triangle " + std::to_string(t + 1);
+  }
+
+  L.nv = nv;
+  L.ne = ne;
+  L.nt = nt;
+  L.erad = m.erad;
+  L.grav = m.grav;
+  L.omega = m.omega;
+
+  // --- orderings ------------------------------------------------------
+  {
+    std::vector<uint64_t> key(nv);
+    const int b = 20;
+    for (int i = 0; i < nv; ++i) {
+      const double *p = m.v_p + 3 * static_cast<size_t>(i);
+      key[i] = hilbert3(quant(p[0], b), quant(p[1], b), quant(p[2], b), b);
+    }
+    sort_perm(L.cell_n2o, L.cell_o2n, key);
+  }
+  {
+    std::vector<uint64_t> key(ne);
+    for (int e = 0; e < ne; ++e) {
+      uint64_t a = static_cast<uint64_t>(L.cell_o2n[m.ed_v[2 * static_cast<size_t>(e)] - 1]);
+      uint64_t c = static_cast<uint64_t>(L.cell_o2n[m.ed_v[2 * static_cast<size_t>(e) + 1] - 1]);
+      key[e] = (std::min(a, c) << 32) | std::max(a, c);
+    }
+    sort_perm(L.edge_n2o, L.edge_o2n, key);
+  }
+  {
+    std::vector<uint64_t> key(nt);
+    for (int t = 0; t < nt; ++t) {
+      uint64_t v[3];
+      for (int s = 0; s < 3; ++s)
+        v[s] = static_cast<uint64_t>(L.cell_o2n[m.tr_v[3 * static_cast<size_t>(t) + s] - 1]);
+      std::sort(v, v + 3);
+      key[t] = (v[0] << 42) | (v[1] << 21) | (v[2] & 0x1FFFFF);
+    }
+    sort_perm(L.tri_n2o, L.tri_o2n, key);
+  }
+
+  // --- cells ----------------------------------------------------------
+  const size_t NV = nv, NE = ne, NT = nt;
+  L.c_nnb.assign(NV, 0);
+  L.c_ed.assign(kMaxNb * NV, -1);
+  L.c_sd.assign(kMaxNb * NV, 0.0);
+  L.c_div32.assign(kMaxNb * NV, 0.0f);
+  L.c_kew32.assign(kMaxNb * NV, 0.0f);
+  L.c_areag.resize(NV);
+  L.c_cellarea.resize(NV);
+  L.c_bt.assign(NV, 0.0);
+  for (int i = 0; i < nv; ++i) {
+    const int c = L.cell_n2o[i];
+    const int n = m.nnb[c];
+    L.c_nnb[i] = static_cast<int8_t>(n);
+    L.c_areag[i] = m.hx_areag[c];
+    if (bt) L.c_bt[i] = bt[c];
+    double cell_area = 0.0;
+    for (int j = 0; j < n; ++j) {
+      const int e = m.v_ed[6 * static_cast<size_t>(c) + j] - 1;
+      cell_area = cell_area + 0.25 * m.ed_leng[e] * m.edhx_leng[e];
+    }
+    L.c_cellarea[i] = cell_area;
+    for (int j = 0; j < n; ++j) {
+      const int e = m.v_ed[6 * static_cast<size_t>(c) + j] - 1;
+      const double s = static_cast<double>(m.hx_ttgout[6 * static_cast<size_t>(c) + j]);
+      L.c_ed[j * NV + i] = L.edge_o2n[e];
+      L.c_sd[j * NV + i] = s * m.edhx_leng[e];
+      L.c_div32[j * NV + i] =
+          static_cast<float>(s * m.edhx_leng[e] / (m.hx_areag[c] * m.erad));
+      L.c_kew32[j * NV + i] =
+          static_cast<float>(0.25 * m.ed_leng[e] * m.edhx_leng[e] / cell_area);
+    }
+  }
+
+  // --- edges ----------------------------------------------------------
+  L.e_v.resize(2 * NE);
+  L.e_sh.resize(2 * NE);
+  L.e_leng.resize(NE);
+  L.e_dleng.resize(NE);
+  L.e_kew.resize(NE);
+  L.e_area.resize(NE);
+  L.e_grad32.resize(NE);
+  L.e_nst.assign(NE, 0);
+  L.e_stk.assign(kMaxSt * NE, 0);
+  L.e_stw.assign(kMaxSt * NE, 0.0);
+  L.e_stc32.assign(kMaxSt * NE, 0.0f);
+  for (int i = 0; i < ne; ++i) {
+    const int e = L.edge_n2o[i];
+    for (int s = 0; s < 2; ++s) {
+      L.e_v[s * NE + i] = L.cell_o2n[m.ed_v[2 * static_cast<size_t>(e) + s] - 1];
+      L.e_sh[s * NE + i] = L.tri_o2n[m.ed_sh[2 * static_cast<size_t>(e) + s] - 1];
+    }
+    const double l = m.ed_leng[e], d = m.edhx_leng[e];
+    L.e_leng[i] = l;
+    L.e_dleng[i] = d;
+    L.e_kew[i] = 0.25 * l * d;
+    L.e_area[i] = l * d * 0.5;
+    L.e_grad32[i] = static_cast<float>(1.0 / (l * m.erad));
+    // TRSK stencil, coriolis_ed order: cell ed%v(1) then ed%v(2), each in
+    // its ccw edge order, the edge's own slot (zero weight) left out.
+    int ns = 0;
+    for (int s = 0; s < 2; ++s) {
+      const int node = m.ed_v[2 * static_cast<size_t>(e) + s] - 1;
+      const int n = m.nnb[node];
+      int edcelli = -1;
+      for (int j = 0; j < n; ++j)
+        if (m.v_ed[6 * static_cast<size_t>(node) + j] - 1 == e) {
+          edcelli = j;
+          break;
+        }
+      if (edcelli < 0) return "edge " + std::to_string(e + 1) + " missing from its cell's edge list";
+      for (int j = 0; j < n; ++j) {
+        if (j == edcelli) continue;
+        if (ns >= kMaxSt) return "TRSK stencil longer than 10 at edge " + std::to_string(e + 1);
+        const int k = m.v_ed[6 * static_cast<size_t>(node) + j] - 1;
+        const double sc = std::copysign(
+            1.0, 1.0 * m.hx_ttgout[6 * static_cast<size_t>(node) + j] *
+                     m.hx_tnrccw[6 * static_cast<size_t>(node) + edcelli]);
+        const double w = m.hx_trskw[36 * static_cast<size_t>(node) + 6 * static_cast<size_t>(j) + edcelli];
+        L.e_stk[ns * NE + i] = L.edge_o2n[k];
+        L.e_stw[ns * NE + i] = w * sc;
+        L.e_stc32[ns * NE + i] = static_cast<float>(0.5 * w * sc * m.edhx_leng[k] / l);
+        ++ns;
+      }
+    }
+    L.e_nst[i] = static_cast<int8_t>(ns);
+  }
+
+  // --- triangles ------------------------------------------------------
+  L.t_ed.resize(3 * NT);
+  L.t_v.resize(3 * NT);
+  L.t_lt.resize(3 * NT);
+  L.t_kite.resize(3 * NT);
+  L.t_circ32.resize(3 * NT);
+  L.t_kite32.resize(3 * NT);
+  L.t_areag.resize(NT);
+  L.t_f.resize(NT);
+  L.t_f32.resize(NT);
+  for (int i = 0; i < nt; ++i) {
+    const int t = L.tri_n2o[i];
+    const double A = m.tr_areag[t];
+    L.t_areag[i] = A;
+    L.t_f[i] = 2.0 * m.omega * std::sin(m.tr_c_lat[t]);
+    L.t_f32[i] = static_cast<float>(L.t_f[i]);
+    for (int s = 0; s < 3; ++s) {
+      const int e = m.tr_ed[3 * static_cast<size_t>(t) + s] - 1;
+      const int v = m.tr_v[3 * static_cast<size_t>(t) + s] - 1;
+      const double tg = static_cast<double>(m.tr_tg[3 * static_cast<size_t>(t) + s]);
+      L.t_ed[s * NT + i] = L.edge_o2n[e];
+      L.t_v[s * NT + i] = L.cell_o2n[v];
+      L.t_lt[s * NT + i] = m.ed_leng[e] * tg;
+      L.t_kite[s * NT + i] = m.tr_trhx_area[3 * static_cast<size_t>(t) + s];
+      L.t_circ32[s * NT + i] = static_cast<float>(m.ed_leng[e] * tg / (A * m.erad));
+      L.t_kite32[s * NT + i] = static_cast<float>(m.tr_trhx_area[3 * static_cast<size_t>(t) + s] / A);
+    }
+  }
+  return "";
+}
+
+}  // namespace imodel

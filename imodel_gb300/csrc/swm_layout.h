@@ -1,0 +1,76 @@
+// Device data layout of the TRSK shallow-water step (internal header).
+//
+// Cells are renumbered along a 3-D Hilbert curve through their positions on
+// the sphere; edges are renumbered by their lower-numbered cell and
+// triangles by their lowest vertex, so that the entities one thread block
+// touches sit in a few contiguous runs of HBM.  All per-entity lists are
+// padded to a fixed width and stored slot-major (slot j of entity i at
+// [j * n + i]) so that a warp reading slot j of 32 consecutive entities
+// issues one coalesced request.
+//
+// Two coefficient sets are kept:
+//  * FP64 "reference order": the factors the Fortran multiplies by, in the
+//    Fortran's order, so the FP64 kernels reproduce the reference's
+//    rounding step by step (sign factors +-1 are folded into a coefficient,
+//    which is exact).
+//  * FP32 "folded": every constant factor of a term folded into one
+//    coefficient computed in FP64 and rounded once.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "imodel_swm.h"
+
+namespace imodel {
+
+constexpr int kMaxNb = 6;     // cells have 5 or 6 edges on icosahedral grids
+constexpr int kMaxSt = 10;    // TRSK stencil: nnb(c1) + nnb(c2) - 2 <= 10
+
+struct Layout {
+  int nv = 0, ne = 0, nt = 0;
+  double erad = 0, grav = 0, omega = 0;
+
+  // permutations (new index -> reference index, 0-based) and inverses
+  std::vector<int32_t> cell_n2o, cell_o2n, edge_n2o, edge_o2n, tri_n2o, tri_o2n;
+
+  // cells, slot-major [kMaxNb][nv]
+  std::vector<int8_t> c_nnb;                 // [nv]
+  std::vector<int32_t> c_ed;                 // edge of slot j (-1 pad)
+  std::vector<double> c_sd;                  // ttgout * edhx%leng of slot j
+  std::vector<double> c_areag;               // [nv] hx%areag
+  std::vector<double> c_cellarea;            // [nv] sum_j 0.25*l*d (KE tiled area)
+  std::vector<double> c_bt;                  // [nv] bottom topography
+  std::vector<float> c_div32;                // ttgout*d/(A*erad)
+  std::vector<float> c_kew32;                // 0.25*l*d / cell_area
+
+  // edges [ne] and [2][ne]
+  std::vector<int32_t> e_v;                  // [2][ne] cells (ed%v = edhx%sh)
+  std::vector<int32_t> e_sh;                 // [2][ne] triangles (ed%sh)
+  std::vector<double> e_leng;                // ed%leng
+  std::vector<double> e_dleng;               // edhx%leng
+  std::vector<double> e_kew;                 // 0.25*l*d (KE weight, FP64)
+  std::vector<float> e_grad32;               // 1/(l*erad)
+  std::vector<int8_t> e_nst;                 // stencil length
+  std::vector<int32_t> e_stk;                // [kMaxSt][ne] stencil edges
+  std::vector<double> e_stw;                 // [kMaxSt][ne] trskw * signcor
+  std::vector<float> e_stc32;                // [kMaxSt][ne] 0.5*w*s*d_k/l_e
+
+  // triangles, slot-major [3][nt]
+  std::vector<int32_t> t_ed, t_v;
+  std::vector<double> t_lt;                  // ed%leng * tr%tg
+  std::vector<double> t_kite;                // tr%trhx_area
+  std::vector<double> t_areag;               // [nt]
+  std::vector<double> t_f;                   // [nt] 2*omega*sin(lat_c)
+  std::vector<float> t_circ32;               // l*tg/(A*erad)
+  std::vector<float> t_kite32;               // kite/A
+  std::vector<float> t_f32;
+
+  // per-edge reference-ordered weight for edge integrals: l*d*0.5
+  std::vector<double> e_area;
+};
+
+// Builds the layout from a reference mesh; returns "" or an error message.
+std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L);
+
+}  // namespace imodel

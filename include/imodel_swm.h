@@ -1,0 +1,183 @@
+/*
+ * imodel_swm.h -- C ABI of the GB300 TRSK shallow-water time step.
+ *
+ * This is the seam a Fortran host reaches through iso_c_binding in place of
+ * the module procedures of iModel's shallow-water model:
+ *
+ *   reference call                                  replaced by
+ *   ---------------------------------------------   ---------------------------
+ *   initialize_gridprop   src/swm.f90:979-1041      imodel_swm_create
+ *   ode_rk4 (time loop)   src/swm.f90:249, :2600     imodel_swm_step / _advance
+ *   tendency              src/swm.f90:2416-2598      imodel_swm_tendency
+ *   sumf_areas, calc_energies, error_calc
+ *                         src/swm.f90:3394, :2686, :3492
+ *                                                    imodel_swm_diagnostics / _errors
+ *   vecrecon_trsk_tg      src/interpack.f90:3852    imodel_swm_trsk_tangent
+ *   print* + stop on errors (swm_operators.f90:82-85, :1604-1606,
+ *                          swm.f90:331-341)          int32 status codes below
+ *
+ * All functions return 0 on success and a positive IMODEL_SWM_E* code on
+ * failure; none of them aborts or exits.  imodel_swm_last_error() returns a
+ * one-line description of the last failure on a handle.
+ *
+ * Mesh arrays follow the reference's grid_structure (src/datastruct.f90:
+ * 121-560): indices are 1-based, per-cell lists are padded to 6 entries in
+ * counter-clockwise order (edge j lies between triangles j-1 and j), and
+ * "[n][k]" arrays are the Fortran (k, n) column-major layout, i.e. C row-major
+ * [n][k].  Lengths and areas are on the unit sphere as the reference stores
+ * them.  The library copies everything it needs during create; the caller may
+ * free the mesh arrays afterwards.
+ *
+ * Threading: a handle must not be used from two threads at once.  Separate
+ * handles may be used concurrently.
+ */
+#ifndef IMODEL_SWM_H
+#define IMODEL_SWM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define IMODEL_SWM_OK 0
+#define IMODEL_SWM_EINVAL 1     /* bad argument or inconsistent mesh          */
+#define IMODEL_SWM_ECUDA 2      /* CUDA runtime error (message has details)   */
+#define IMODEL_SWM_EBLOWUP 3    /* NaN/Inf in the state (swm.f90:331-341)     */
+#define IMODEL_SWM_EDIVZERO 4   /* |h_tr| < eps/1e5 in the PV division
+                                   (swm_operators.f90:1604-1606)              */
+#define IMODEL_SWM_ENOMEM 5     /* device allocation failed                   */
+#define IMODEL_SWM_ESTATE 6     /* call order violated (no state set, ...)    */
+#define IMODEL_SWM_ENODEV 7     /* no CUDA device available                   */
+
+/* ---- precision modes --------------------------------------------------- */
+#define IMODEL_SWM_FP64 0 /* reference operation order, FP64 everywhere      */
+#define IMODEL_SWM_FP32 1 /* FP32 state and operators, FP64 integrals        */
+
+/* ---- mesh (copied from grid_structure) --------------------------------- */
+typedef struct imodel_swm_mesh {
+  int32_t nv, ne, nt;
+  /* cells (Voronoi / hexagon-pentagon), datastruct.f90:121-160, :287-400 */
+  const int32_t *nnb;          /* [nv]      v%nnb                         */
+  const int32_t *v_nb;         /* [nv][6]   v%nb   (neighbour cells)       */
+  const int32_t *v_ed;         /* [nv][6]   v%ed   (edges, ccw)            */
+  const int32_t *v_tr;         /* [nv][6]   v%tr   (triangles, ccw)        */
+  const int32_t *hx_ttgout;    /* [nv][6]   hx%ttgout (+-1)                */
+  const int32_t *hx_tnrccw;    /* [nv][6]   hx%tnrccw (+-1)                */
+  const double *hx_areag;      /* [nv]      hx%areag                       */
+  const double *hx_hxtr_area;  /* [nv][6]   hx%hxtr_area (kite / areag)    */
+  const double *hx_trskw;      /* [nv][6][6] hx%trskw(i,j) at [c][j][i]    */
+  const double *v_p;           /* [nv][3]   v%p                            */
+  const double *v_lat;         /* [nv]      v%lat                          */
+  /* triangle edges (HTC velocity points), datastruct.f90:161-211 */
+  const int32_t *ed_v;         /* [ne][2]   ed%v  (cells; edhx%sh = ed%v)  */
+  const int32_t *ed_sh;        /* [ne][2]   ed%sh (triangles)              */
+  const double *ed_leng;       /* [ne]      ed%leng                        */
+  const double *edhx_leng;     /* [ne]      edhx%leng                      */
+  const double *ed_c;          /* [ne][3]   ed%c%p                         */
+  const double *ed_c_lat;      /* [ne]      ed%c%lat                       */
+  const double *ed_tg;         /* [ne][3]   ed%tg                          */
+  const double *ed_nr;         /* [ne][3]   ed%nr                          */
+  /* triangles, datastruct.f90:212-286 */
+  const int32_t *tr_v;         /* [nt][3]   tr%v                           */
+  const int32_t *tr_ed;        /* [nt][3]   tr%ed                          */
+  const int32_t *tr_tg;        /* [nt][3]   tr%tg (+-1)                    */
+  const double *tr_areag;      /* [nt]      tr%areag                       */
+  const double *tr_trhx_area;  /* [nt][3]   tr%trhx_area                   */
+  const double *tr_c_lat;      /* [nt]      tr%c%lat                       */
+  /* physical constants (constants.f90:55-67) */
+  double erad, grav, omega;
+} imodel_swm_mesh;
+
+/* ---- options (par/swm.par subset for the trsk10/HTC/geo path) ---------- */
+typedef struct imodel_swm_opts {
+  int32_t precision;  /* IMODEL_SWM_FP64 or IMODEL_SWM_FP32                 */
+  int32_t testcase;   /* reference testcase number: q_tr=0 if <2 and momeq=0
+                         if <=1 (swm.f90:2469-2471, :2592-2594)            */
+  const double *bt;   /* [nv] bottom topography (m) or NULL for flat        */
+  double h_ref;       /* FP32 mode: h is stored as h - h_ref in FP32.
+                         0 selects the area mean of the first state set.   */
+  int32_t device;     /* CUDA device ordinal                                */
+  int32_t learned;    /* 1: add the learned TRSK correction (needs weights) */
+  const void *mlp_weights;  /* packed MLP parameters (see imodel_swm_mlp.h) */
+  size_t mlp_bytes;
+  double drift_bound; /* |energy drift| above which the learned correction
+                         is switched off (0 = 1e-3)                       */
+} imodel_swm_opts;
+
+/* ---- diagnostics (swm.f90:293-322, :2686-2752, :3394-3440) ------------- */
+typedef struct imodel_swm_diag {
+  double mass;          /* sumf_areas(h) = sum A_i h_i / sum A_i           */
+  double penergy;       /* sum A_i g h_i (h_i/2 + b_i)                      */
+  double kenergy;       /* sum_e 1/2 l_e d_e h_e u_e^2 (h_e of the last
+                           tendency evaluation, as calc_energies uses)     */
+  double tenergy;       /* penergy + kenergy                               */
+  double availenergy;   /* tenergy - unavailable potential energy          */
+  double pot_enstrophy; /* sum_t A_t h_t q_t^2 / 2 (not in the reference)  */
+  double rms_div;       /* sqrt(sumfsq_areas(div u)) of the last tendency  */
+  double max_div;       /* max |div u|                                     */
+  int32_t learned_active; /* 1 while the learned correction is applied     */
+  int32_t nan_found;      /* 1 if h or u holds NaN/Inf                      */
+} imodel_swm_diag;
+
+/* Creates a handle: copies the mesh, reorders cells along a space-filling
+ * curve, builds the padded-CSR connectivity and uploads everything.  On
+ * failure *handle is still set, so that imodel_swm_last_error() can explain
+ * the failure; it must be released with imodel_swm_destroy() either way. */
+int imodel_swm_create(const imodel_swm_mesh *m, const imodel_swm_opts *o,
+                      void **handle);
+
+/* Runs nsteps classic RK4 steps (swm.f90:2600-2683) of length dt seconds.
+ * h_io[nv] and u_io[ne] (host, FP64, reference ordering) are read on entry
+ * and overwritten with the state after nsteps steps.  nsteps > 1 replays a
+ * CUDA graph of one step. */
+int imodel_swm_step(void *handle, double *h_io, double *u_io, double dt,
+                    int32_t nsteps);
+
+/* One evaluation of tendency(h, u, masseq, momeq) (swm.f90:2416) on host
+ * arrays.  Leaves the handle's current state untouched. */
+int imodel_swm_tendency(void *handle, const double *h, const double *u,
+                        double *masseq, double *momeq);
+
+/* Global integrals of the current state, FP64 with compensated summation. */
+int imodel_swm_diagnostics(void *handle, imodel_swm_diag *out);
+
+/* error_calc (swm.f90:3492-3543) of the current state against host
+ * reference fields.  out = {Linf_rel_h, L2_rel_h, Linf_h,
+ *                           Linf_rel_u, L2_rel_u, Linf_u}. */
+int imodel_swm_errors(void *handle, const double *h_ref, const double *u_ref,
+                      double out[6]);
+
+/* Tangential velocity reconstructed by TRSK at every edge, along ed%nr
+ * (vecrecon_trsk_tg, interpack.f90:3852-3976, var%pos == 6). */
+int imodel_swm_trsk_tangent(void *handle, const double *u, double *utg);
+
+int imodel_swm_destroy(void *handle);
+const char *imodel_swm_last_error(void *handle);
+
+/* ---- device-resident extensions ---------------------------------------- *
+ * A host that keeps the state on the GPU between calls (and a benchmark that
+ * measures the kernels alone) uploads once, advances, and reads back when it
+ * needs the fields.  These have no counterpart in the reference. */
+int imodel_swm_set_state(void *handle, const double *h, const double *u);
+int imodel_swm_get_state(void *handle, double *h, double *u);
+int imodel_swm_advance(void *handle, double dt, int32_t nsteps);
+/* Launches issued by one advance call for nsteps steps (kernels only). */
+int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count);
+/* Runs nsteps RK4 steps kernel by kernel (no graph) with CUDA events around
+ * each kernel on the handle's stream and returns the average duration in ms
+ * of the four kernels of a stage: {triangle (PV), edge pre-pass (h_e, F_e,
+ * q_e), cell (div F, K, B, mass update), edge (grad B + TRSK PV flux,
+ * momentum update)}.  Advances the state like imodel_swm_advance. */
+int imodel_swm_profile(void *handle, double dt, int32_t nsteps, double avg_ms[4]);
+/* Name of the kernel that dominates a step (for profilers). */
+const char *imodel_swm_main_kernel(void *handle);
+/* The CUDA stream (cudaStream_t) all work of the handle is issued on. */
+void *imodel_swm_stream(void *handle);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMODEL_SWM_H */

@@ -1,0 +1,531 @@
+// CPU restatement of iModel's TRSK shallow-water time step (FP64).
+//
+// TEST INFRASTRUCTURE ONLY: the correctness oracle for the GB300 kernels and
+// the CPU baseline timed beside them.  Nothing in the product links this.
+//
+// It follows the Fortran loop by loop for the branches the trsk10 wrapper,
+// HTC staggering and geodesic areas select (swm_data.f90:446-507), with the
+// same per-entity accumulation order and one OpenMP parallel loop per
+// operator, like the reference's `!$omp parallel do schedule(static)`.
+// Build with -ffp-contract=off so no multiply-add is fused.
+//
+// Parity status: unpinned against the Fortran binary (no Fortran compiler);
+// pinned by the reference's known answers (see tests/test_oracle_kat.py).
+
+#include "swm_oracle.h"
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+// constants.f90:31, :45 (pi from a float literal; eps = epsilon(1.))
+const double kPi = 4.0 * static_cast<double>(0.78539816339744830961566f);
+const double kEps = static_cast<double>(1.1920928955078125e-07f);
+
+struct Oracle {
+  imodel_swm_mesh m;
+  int testcase;
+  int nthreads;
+  std::vector<double> bt, fcor;
+  std::vector<double> h_ed, uh, eta, h_tr, eta_ed, q_tr, q_ed, divuh, ke, hbt, ghbK, grad,
+      uhq, divu, zeta, vhx;
+  std::vector<double> massf[4], momf[4], h_tmp, u_tmp;
+};
+
+#define I6(i, j) (static_cast<size_t>(i) * 6 + (j))
+
+// getedindexonhx, smeshpack.f90:4099-4125 (1-based result, 0 if absent)
+inline int getedindexonhx(const imodel_swm_mesh &m, int ed, int cell) {
+  for (int i = 0; i < m.nnb[cell]; ++i)
+    if (m.v_ed[I6(cell, i)] - 1 == ed) return i + 1;
+  return 0;
+}
+
+// tendency, swm.f90:2416-2598
+int tendency(Oracle &o, const double *h, const double *u, double *masseq, double *momeq) {
+  const imodel_swm_mesh &m = o.m;
+  const int nv = m.nv, ne = m.ne, nt = m.nt;
+  const double erad = m.erad, grav = m.grav;
+  int nth = o.nthreads;
+  // zero_vector x2 (swm_operators.f90:1652)
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l) momeq[l] = 0.0;
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int i = 0; i < nv; ++i) masseq[i] = 0.0;
+
+  // scalar_hx2ed (swm_operators.f90:89-97) and scalar_elem_product (:1546)
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l)
+    o.h_ed[l] = (h[m.ed_v[2 * l] - 1] + h[m.ed_v[2 * l + 1] - 1]) * 0.5;
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l) o.uh[l] = u[l] * o.h_ed[l];
+
+  // vort_tr (swm_operators.f90:551-611), HTC branch, fsphere=0
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int k = 0; k < nt; ++k) {
+    double e = 0.0;
+    for (int l = 0; l < 3; ++l) {
+      int ed = m.tr_ed[3 * k + l] - 1;
+      double signcor = static_cast<double>(m.tr_tg[3 * k + l]);
+      e = e + u[ed] * m.ed_leng[ed] * signcor;
+    }
+    e = e / m.tr_areag[k] / erad;
+    e = e + o.fcor[k];
+    o.eta[k] = e;
+  }
+
+  // scalar_hx2tr (swm_operators.f90:258-263), trsk branch
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int k = 0; k < nt; ++k) {
+    double f = 0.0;
+    for (int i = 0; i < 3; ++i) f = f + m.tr_trhx_area[3 * k + i] * h[m.tr_v[3 * k + i] - 1];
+    o.h_tr[k] = f / m.tr_areag[k];
+  }
+
+  // scalar_tr2ed(eta -> eta_ed) (swm_operators.f90:140-176)
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l)
+    o.eta_ed[l] = 0.5 * (o.eta[m.ed_sh[2 * l] - 1] + o.eta[m.ed_sh[2 * l + 1] - 1]);
+
+  // scalar_elem_divide (swm_operators.f90:1579-1615)
+  int divzero = 0;
+  if (o.testcase < 2) {
+    for (int k = 0; k < nt; ++k) o.q_tr[k] = 0.0;
+  } else {
+#pragma omp parallel for schedule(static) num_threads(nth) reduction(+ : divzero)
+    for (int k = 0; k < nt; ++k) {
+      if (std::fabs(o.h_tr[k]) < kEps / 100000.0)
+        divzero += 1;
+      else
+        o.q_tr[k] = o.eta[k] / o.h_tr[k];
+    }
+  }
+  if (divzero) return IMODEL_SWM_EDIVZERO;
+
+  // scalar_tr2ed(q_tr -> q_ed)
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l)
+    o.q_ed[l] = 0.5 * (o.q_tr[m.ed_sh[2 * l] - 1] + o.q_tr[m.ed_sh[2 * l + 1] - 1]);
+
+  // vector_edhx2hx_perot(u -> v_hx) (swm_operators.f90:454-509): computed by
+  // the reference on every call although trsk10 never reads it.
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int i = 0; i < nv; ++i) {
+    double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+    const double *p = m.v_p + 3 * static_cast<size_t>(i);
+    for (int l = 0; l < m.nnb[i]; ++l) {
+      int ed = m.v_ed[I6(i, l)] - 1;
+      double signcor = static_cast<double>(m.hx_ttgout[I6(i, l)]);
+      const double *c = m.ed_c + 3 * static_cast<size_t>(ed);
+      double s = signcor * u[ed];
+      v0 = v0 + s * (c[0] - p[0]) * m.edhx_leng[ed];
+      v1 = v1 + s * (c[1] - p[1]) * m.edhx_leng[ed];
+      v2 = v2 + s * (c[2] - p[2]) * m.edhx_leng[ed];
+    }
+    v0 = v0 / m.hx_areag[i];
+    v1 = v1 / m.hx_areag[i];
+    v2 = v2 / m.hx_areag[i];
+    double vp = v0 * p[0] + v1 * p[1] + v2 * p[2];
+    double np = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+    o.vhx[3 * static_cast<size_t>(i)] = v0 - vp * p[0] / np;
+    o.vhx[3 * static_cast<size_t>(i) + 1] = v1 - vp * p[1] / np;
+    o.vhx[3 * static_cast<size_t>(i) + 2] = v2 - vp * p[2] / np;
+  }
+
+  // div_hx(uh -> divuh) (swm_operators.f90:613-661), HTC: signcor = ttgout
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int i = 0; i < nv; ++i) {
+    double d = 0.0;
+    for (int j = 0; j < m.nnb[i]; ++j) {
+      int l = m.v_ed[I6(i, j)] - 1;
+      double signcor = static_cast<double>(m.hx_ttgout[I6(i, j)]);
+      d = d + signcor * o.uh[l] * m.edhx_leng[l];
+    }
+    o.divuh[i] = d / m.hx_areag[i] / erad;
+  }
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int i = 0; i < nv; ++i) masseq[i] = -o.divuh[i];
+
+  // kinetic_energy_hx, trsk branch (swm_operators.f90:1162-1171)
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int i = 0; i < nv; ++i) {
+    double k = 0.0, cell_area = 0.0;
+    for (int l = 0; l < m.nnb[i]; ++l) {
+      int ed = m.v_ed[I6(i, l)] - 1;
+      double ed_area = 0.25 * m.ed_leng[ed] * m.edhx_leng[ed];
+      cell_area = cell_area + ed_area;
+      k = k + ed_area * (u[ed] * u[ed]);
+    }
+    o.ke[i] = k / cell_area;
+  }
+
+  // hbt = h + bt ; ghbK = grav*hbt + ke (swm.f90:2533-2536)
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int i = 0; i < nv; ++i) {
+    o.hbt[i] = h[i] + o.bt[i];
+    o.ghbK[i] = grav * o.hbt[i] + o.ke[i];
+  }
+
+  // grad_ed, HTC (swm_operators.f90:511-548) ; momeq = -grad
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l) {
+    double g = o.ghbK[m.ed_v[2 * l + 1] - 1] - o.ghbK[m.ed_v[2 * l] - 1];
+    g = g / m.ed_leng[l] / erad;
+    o.grad[l] = g;
+    momeq[l] = -g;
+  }
+
+  // coriolis_ed, TRSK branch (swm_operators.f90:1283-1308)
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l) {
+    double q = 0.0;
+    for (int i = 0; i < 2; ++i) {
+      int node = m.ed_v[2 * l + i] - 1;
+      int edcelli = getedindexonhx(m, l, node);
+      for (int j = 0; j < m.nnb[node]; ++j) {
+        int k = m.v_ed[I6(node, j)] - 1;
+        double signcor = std::copysign(
+            1.0, 1.0 * m.hx_ttgout[I6(node, j)] * m.hx_tnrccw[I6(node, edcelli - 1)]);
+        double qtmp = 0.5 * (o.q_ed[l] + o.q_ed[k]);
+        double w = m.hx_trskw[static_cast<size_t>(node) * 36 + static_cast<size_t>(j) * 6 +
+                              (edcelli - 1)];
+        q = q + o.uh[k] * qtmp * m.edhx_leng[k] * w * signcor;
+      }
+    }
+    o.uhq[l] = q / m.ed_leng[l];
+  }
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l) momeq[l] = momeq[l] - o.uhq[l];
+
+  // div_hx(u -> divu) and rel_vort_tr(u -> zeta): diagnostics, every call
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int i = 0; i < nv; ++i) {
+    double d = 0.0;
+    for (int j = 0; j < m.nnb[i]; ++j) {
+      int l = m.v_ed[I6(i, j)] - 1;
+      double signcor = static_cast<double>(m.hx_ttgout[I6(i, j)]);
+      d = d + signcor * u[l] * m.edhx_leng[l];
+    }
+    o.divu[i] = d / m.hx_areag[i] / erad;
+  }
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int k = 0; k < nt; ++k) {
+    double z = 0.0;
+    for (int l = 0; l < 3; ++l) {
+      int ed = m.tr_ed[3 * k + l] - 1;
+      z = z + u[ed] * m.ed_leng[ed] * static_cast<double>(m.tr_tg[3 * k + l]);
+    }
+    o.zeta[k] = z / m.tr_areag[k] / erad;
+  }
+
+  if (o.testcase <= 1) {
+    for (int l = 0; l < ne; ++l) momeq[l] = 0.0;
+  }
+  return IMODEL_SWM_OK;
+}
+
+// ode_rk4, swm.f90:2600-2683
+int rk4(Oracle &o, const double *h, const double *u, double *h_new, double *u_new, double dt) {
+  const int nv = o.m.nv, ne = o.m.ne;
+  int nth = o.nthreads;
+  int rc = tendency(o, h, u, o.massf[0].data(), o.momf[0].data());
+  if (rc) return rc;
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l) u_new[l] = u[l] + dt * o.momf[0][l] / 2.0;
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int i = 0; i < nv; ++i) h_new[i] = h[i] + dt * o.massf[0][i] / 2.0;
+  rc = tendency(o, h_new, u_new, o.massf[1].data(), o.momf[1].data());
+  if (rc) return rc;
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l) u_new[l] = u[l] + dt * o.momf[1][l] / 2.0;
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int i = 0; i < nv; ++i) h_new[i] = h[i] + dt * o.massf[1][i] / 2.0;
+  rc = tendency(o, h_new, u_new, o.massf[2].data(), o.momf[2].data());
+  if (rc) return rc;
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l) u_new[l] = u[l] + dt * o.momf[2][l];
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int i = 0; i < nv; ++i) h_new[i] = h[i] + dt * o.massf[2][i];
+  rc = tendency(o, h_new, u_new, o.massf[3].data(), o.momf[3].data());
+  if (rc) return rc;
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l)
+    u_new[l] = u[l] + dt * (o.momf[0][l] + 2.0 * o.momf[1][l] + 2.0 * o.momf[2][l] +
+                            o.momf[3][l]) / 6.0;
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int i = 0; i < nv; ++i)
+    h_new[i] = h[i] + dt * (o.massf[0][i] + 2.0 * o.massf[1][i] + 2.0 * o.massf[2][i] +
+                            o.massf[3][i]) / 6.0;
+  return IMODEL_SWM_OK;
+}
+
+// sumf_areas / sumfsq_areas, swm.f90:3394-3490 (pos 0: cells, 1: triangles,
+// 6: HTC edges; the edge branch of sumf_areas uses hx%areag, as the
+// reference does)
+double sumfsq_areas(const imodel_swm_mesh &m, const double *f, int pos) {
+  double s = 0.0, a = 0.0;
+  if (pos == 0) {
+    for (int i = 0; i < m.nv; ++i) {
+      a = a + m.hx_areag[i];
+      s = s + m.hx_areag[i] * (f[i] * f[i]);
+    }
+  } else if (pos == 1) {
+    for (int i = 0; i < m.nt; ++i) {
+      a = a + m.tr_areag[i];
+      s = s + m.tr_areag[i] * (f[i] * f[i]);
+    }
+  } else {
+    for (int i = 0; i < m.ne; ++i) {
+      double area = m.ed_leng[i] * m.edhx_leng[i] * 0.5;
+      a = a + area;
+      s = s + area * (f[i] * f[i]);
+    }
+  }
+  return s / a;
+}
+
+double sumf_areas_cells(const imodel_swm_mesh &m, const double *f) {
+  double s = 0.0, a = 0.0;
+  for (int i = 0; i < m.nv; ++i) {
+    a = a + m.hx_areag[i];
+    s = s + m.hx_areag[i] * f[i];
+  }
+  return s / a;
+}
+
+}  // namespace
+
+extern "C" {
+
+void *oracle_create(const imodel_swm_mesh *m, int32_t testcase, const double *bt,
+                    int32_t nthreads) {
+  if (!m) return nullptr;
+  Oracle *o = new Oracle();
+  o->m = *m;
+  o->testcase = testcase;
+  o->nthreads = nthreads > 0 ? nthreads : 1;
+  const size_t nv = m->nv, ne = m->ne, nt = m->nt;
+  o->bt.assign(nv, 0.0);
+  if (bt) std::memcpy(o->bt.data(), bt, nv * sizeof(double));
+  o->fcor.resize(nt);
+  for (size_t k = 0; k < nt; ++k) o->fcor[k] = 2.0 * m->omega * std::sin(m->tr_c_lat[k]);
+  for (auto *v : {&o->h_ed, &o->uh, &o->eta_ed, &o->q_ed, &o->grad, &o->uhq}) v->assign(ne, 0.0);
+  for (auto *v : {&o->eta, &o->h_tr, &o->q_tr, &o->zeta}) v->assign(nt, 0.0);
+  for (auto *v : {&o->divuh, &o->ke, &o->hbt, &o->ghbK, &o->divu}) v->assign(nv, 0.0);
+  o->vhx.assign(3 * nv, 0.0);
+  for (int s = 0; s < 4; ++s) {
+    o->massf[s].assign(nv, 0.0);
+    o->momf[s].assign(ne, 0.0);
+  }
+  o->h_tmp.assign(nv, 0.0);
+  o->u_tmp.assign(ne, 0.0);
+  return o;
+}
+
+void oracle_destroy(void *o) { delete static_cast<Oracle *>(o); }
+
+int oracle_tendency(void *p, const double *h, const double *u, double *masseq, double *momeq) {
+  return tendency(*static_cast<Oracle *>(p), h, u, masseq, momeq);
+}
+
+int oracle_rk4(void *p, const double *h, const double *u, double *h_new, double *u_new,
+               double dt) {
+  return rk4(*static_cast<Oracle *>(p), h, u, h_new, u_new, dt);
+}
+
+// time loop of swm_tests (swm.f90:238-370) without diagnostics or output:
+// ode_rk4(h_old, u_old -> h, u); u_old = u; h_old = h
+int oracle_run(void *p, double *h, double *u, double dt, int32_t nsteps) {
+  Oracle &o = *static_cast<Oracle *>(p);
+  for (int k = 0; k < nsteps; ++k) {
+    int rc = rk4(o, h, u, o.h_tmp.data(), o.u_tmp.data(), dt);
+    if (rc) return rc;
+    std::memcpy(h, o.h_tmp.data(), sizeof(double) * o.m.nv);
+    std::memcpy(u, o.u_tmp.data(), sizeof(double) * o.m.ne);
+  }
+  return IMODEL_SWM_OK;
+}
+
+// calc_energies (swm.f90:2686-2752) + sumf_areas + RMS divergence; h_ed and
+// divu are those of the last tendency evaluation, as in the reference.
+int oracle_diagnostics(void *p, const double *h, const double *u, imodel_swm_diag *out) {
+  Oracle &o = *static_cast<Oracle *>(p);
+  const imodel_swm_mesh &m = o.m;
+  const double grav = m.grav;
+  std::memset(out, 0, sizeof(*out));
+  out->mass = sumf_areas_cells(m, h);
+  double pe = 0.0;
+  for (int i = 0; i < m.nv; ++i) pe = pe + m.hx_areag[i] * grav * h[i] * (h[i] * 0.5 + o.bt[i]);
+  std::vector<double> hbt(m.nv);
+  for (int i = 0; i < m.nv; ++i) hbt[i] = h[i] + o.bt[i];
+  double mean_height = sumf_areas_cells(m, hbt.data());
+  double unavail = 0.0;
+  for (int i = 0; i < m.nv; ++i) {
+    double mhb = mean_height - o.bt[i];
+    unavail = unavail + m.hx_areag[i] * grav * mhb * (mhb * 0.5 + o.bt[i]);
+  }
+  double ke = 0.0;
+  for (int l = 0; l < m.ne; ++l)
+    ke = ke + 0.5 * m.ed_leng[l] * m.edhx_leng[l] * o.h_ed[l] * (u[l] * u[l]);
+  out->penergy = pe;
+  out->kenergy = ke;
+  out->tenergy = pe + ke;
+  out->availenergy = out->tenergy - unavail;
+  double ens = 0.0;
+  for (int k = 0; k < m.nt; ++k) ens = ens + m.tr_areag[k] * o.h_tr[k] * (o.q_tr[k] * o.q_tr[k]) * 0.5;
+  out->pot_enstrophy = ens;
+  out->rms_div = std::sqrt(sumfsq_areas(m, o.divu.data(), 0));
+  double mx = 0.0;
+  for (int i = 0; i < m.nv; ++i) mx = std::fmax(mx, std::fabs(o.divu[i]));
+  out->max_div = mx;
+  int bad = 0;
+  for (int i = 0; i < m.nv; ++i) bad |= !std::isfinite(h[i]);
+  for (int l = 0; l < m.ne; ++l) bad |= !std::isfinite(u[l]);
+  out->nan_found = bad;
+  return IMODEL_SWM_OK;
+}
+
+// error_calc, swm.f90:3492-3543: out = {errormaxrel, error2rel, errormax}
+int oracle_error_calc(void *p, const double *f, const double *fref, int32_t pos, double out[3]) {
+  Oracle &o = *static_cast<Oracle *>(p);
+  const imodel_swm_mesh &m = o.m;
+  int n = pos == 0 ? m.nv : (pos == 1 ? m.nt : m.ne);
+  std::vector<double> dif(n);
+  for (int i = 0; i < n; ++i) dif[i] = f[i] - fref[i];
+  double refsum = sumfsq_areas(m, fref, pos);
+  double e2 = refsum > 0 ? std::sqrt(sumfsq_areas(m, dif.data(), pos)) / std::sqrt(refsum)
+                         : std::sqrt(sumfsq_areas(m, dif.data(), pos));
+  double refmax = 0.0, emax = 0.0;
+  for (int i = 0; i < n; ++i) {
+    refmax = std::fmax(refmax, std::fabs(fref[i]));
+    emax = std::fmax(emax, std::fabs(dif[i]));
+  }
+  out[0] = refmax > 0 ? emax / refmax : emax;
+  out[1] = e2;
+  out[2] = emax;
+  return IMODEL_SWM_OK;
+}
+
+// vecrecon_trsk_tg, interpack.f90:3852-3976 (var%pos == 6), scalar utg
+int oracle_trsk_tangent(void *p, const double *u, double *utg) {
+  Oracle &o = *static_cast<Oracle *>(p);
+  const imodel_swm_mesh &m = o.m;
+  int nth = o.nthreads;
+  int bad = 0;
+#pragma omp parallel for schedule(static) num_threads(nth) reduction(+ : bad)
+  for (int ed = 0; ed < m.ne; ++ed) {
+    double t = 0.0;
+    for (int i = 0; i < 2; ++i) {
+      int cell = m.ed_v[2 * ed + i] - 1;
+      int ed_celli = getedindexonhx(m, ed, cell);
+      if (ed_celli == 0) {
+        bad += 1;
+        continue;
+      }
+      for (int j = 0; j < m.nnb[cell]; ++j) {
+        int k = m.v_ed[I6(cell, j)] - 1;
+        double signcor =
+            -1.0 * m.hx_ttgout[I6(cell, j)] * m.hx_tnrccw[I6(cell, ed_celli - 1)];
+        double w = m.hx_trskw[static_cast<size_t>(cell) * 36 + static_cast<size_t>(j) * 6 +
+                              (ed_celli - 1)];
+        t = t + u[k] * m.edhx_leng[k] * w * signcor;
+      }
+    }
+    utg[ed] = t / m.ed_leng[ed];
+  }
+  return bad ? IMODEL_SWM_EINVAL : IMODEL_SWM_OK;
+}
+
+// calc_trisk_weights, interpack.f90:4046-4095, from hx%hxtr_area
+int oracle_trsk_weights(const imodel_swm_mesh *m, double *trskw) {
+  for (int c = 0; c < m->nv; ++c) {
+    int n = m->nnb[c];
+    const double *R = m->hx_hxtr_area + I6(c, 0);
+    for (int q = 0; q < 36; ++q) trskw[static_cast<size_t>(c) * 36 + q] = 0.0;
+    for (int i = 1; i <= n; ++i) {
+      for (int j = 1; j <= n; ++j) {
+        double rsum = 0.0;
+        double w;
+        if (i == j) {
+          w = 0.0;
+        } else {
+          if (j < i) {
+            for (int k = i; k <= n; ++k) rsum = rsum + R[k - 1];
+            for (int k = 1; k <= j - 1; ++k) rsum = rsum + R[k - 1];
+          } else {
+            for (int k = i; k <= j - 1; ++k) rsum = rsum + R[k - 1];
+          }
+          w = rsum - 0.5;
+        }
+        trskw[static_cast<size_t>(c) * 36 + static_cast<size_t>(j - 1) * 6 + (i - 1)] = w;
+      }
+    }
+  }
+  return IMODEL_SWM_OK;
+}
+
+// initialize_fields, testcase 2 with HTC staggering (swm.f90:1205-1262)
+int oracle_tc2(const imodel_swm_mesh *m, double *h, double *u) {
+  const double erad = m->erad, omega = m->omega;
+  const double gravi = 1.0 / m->grav;
+  const double pi2 = 2.0 * kPi;
+  const double day2sec = 86400.0;
+  const double u0 = pi2 * erad / (12.0 * day2sec);
+  const double h0 = 2.94e4 * gravi;
+  const double h_ct = (erad * omega * u0 + (u0 * u0) / 2.0) * gravi;
+  for (int i = 0; i < m->nv; ++i) {
+    double s = std::sin(m->v_lat[i]);
+    h[i] = h0 - h_ct * (s * s);
+  }
+  for (int l = 0; l < m->ne; ++l) {
+    const double *p = m->ed_c + 3 * static_cast<size_t>(l);
+    const double *tg = m->ed_tg + 3 * static_cast<size_t>(l);
+    double utmp = u0 * std::cos(m->ed_c_lat[l]);
+    double vtmp = 0.0;
+    // convert_vec_sph2cart, smeshpack.f90:4379-4417
+    double rho = std::sqrt(p[0] * p[0] + p[1] * p[1]);
+    double v[3];
+    if (rho == 0.0) {
+      v[0] = vtmp;
+      v[1] = utmp;
+      v[2] = 0.0;
+    } else {
+      v[0] = -(utmp * (p[1] / rho)) - (vtmp * p[0] * p[2]) / rho;
+      v[1] = utmp * (p[0] / rho) - (vtmp * p[1] * p[2]) / rho;
+      v[2] = vtmp * rho;
+    }
+    double d = v[0] * tg[0];
+    d = d + v[1] * tg[1];
+    d = d + v[2] * tg[2];
+    u[l] = d;
+  }
+  return IMODEL_SWM_OK;
+}
+
+int oracle_field(void *p, int32_t which, double *out) {
+  Oracle &o = *static_cast<Oracle *>(p);
+  const std::vector<double> *v = nullptr;
+  switch (which) {
+    case 0: v = &o.h_ed; break;
+    case 1: v = &o.uh; break;
+    case 2: v = &o.eta; break;
+    case 3: v = &o.h_tr; break;
+    case 4: v = &o.q_tr; break;
+    case 5: v = &o.q_ed; break;
+    case 6: v = &o.divuh; break;
+    case 7: v = &o.ke; break;
+    case 8: v = &o.ghbK; break;
+    case 9: v = &o.grad; break;
+    case 10: v = &o.uhq; break;
+    case 11: v = &o.divu; break;
+    case 12: v = &o.zeta; break;
+    case 13: v = &o.eta_ed; break;
+    default: return IMODEL_SWM_EINVAL;
+  }
+  std::memcpy(out, v->data(), v->size() * sizeof(double));
+  return IMODEL_SWM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,42 @@
+/*
+ * swm_oracle.h -- CPU restatement of iModel's TRSK shallow-water step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the correctness oracle and the CPU
+ * baseline of the GB300 library; the library never links or calls it.
+ * Parity status: the reference is Fortran and no Fortran compiler exists
+ * where this was written, so bit-level parity with the reference binary is
+ * unpinned; the restatement is pinned instead by the reference's own
+ * known-answer tests (Williamson TC2 steady state and its analytic operator
+ * values, swm.f90:1205-1326 and :382-734; mimetic identities :628-718).
+ */
+#ifndef IMODEL_SWM_ORACLE_H
+#define IMODEL_SWM_ORACLE_H
+#include <stdint.h>
+#include "../include/imodel_swm.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+void *oracle_create(const imodel_swm_mesh *m, int32_t testcase, const double *bt,
+                    int32_t nthreads);
+void oracle_destroy(void *o);
+int oracle_tendency(void *o, const double *h, const double *u, double *masseq,
+                    double *momeq);
+int oracle_rk4(void *o, const double *h, const double *u, double *h_new, double *u_new,
+               double dt);
+int oracle_run(void *o, double *h, double *u, double dt, int32_t nsteps);
+int oracle_diagnostics(void *o, const double *h, const double *u, imodel_swm_diag *out);
+int oracle_error_calc(void *o, const double *f, const double *fref, int32_t pos,
+                      double out[3]);
+int oracle_trsk_tangent(void *o, const double *u, double *utg);
+int oracle_trsk_weights(const imodel_swm_mesh *m, double *trskw);
+int oracle_tc2(const imodel_swm_mesh *m, double *h, double *u);
+/* copy an intermediate field of the last tendency call:
+ * 0 h_ed, 1 uh, 2 eta, 3 h_tr, 4 q_tr, 5 q_ed, 6 divuh, 7 ke, 8 ghbK,
+ * 9 grad_ghbK, 10 uhq_perp, 11 divu, 12 zeta, 13 eta_ed */
+int oracle_field(void *o, int32_t which, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
