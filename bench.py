@@ -272,13 +272,18 @@ def config_dict(g, precision):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--level", type=int, default=LEVEL)
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    # switches for profiler runs: time only the listed paths, skip the
+    # end-to-end and per-kernel passes
+    ap.add_argument("--precisions", default="fp64,fp32")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-kprof", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -295,7 +300,8 @@ def main():
     g = meshbuild(args.level)
     h, u = swm.initialize_fields_tc2(g)
     results = {}
-    for precision in ("fp64", "fp32"):
+    precisions = [p for p in args.precisions.split(",") if p]
+    for precision in precisions:
         m = swm.SWM(g, precision=precision, device=local)
         m.set_state(h, u)
         stream = m.stream()
@@ -316,11 +322,11 @@ def main():
         D.barrier()
         ms = D.max(ms)
         diag = m.diagnostics()
-        prof = m.profile(DT, 3)
+        prof = None if args.no_kprof else m.profile(DT, 3)
         results[precision] = {"ms": ms, "clocks": clocks, "prof": prof, "diag": diag,
                               "launches": m.launch_count(args.steps),
                               "main_kernel": m.main_kernel()}
-        if precision == "fp32":
+        if precision == "fp32" and not args.no_e2e:
             # e2e through the C ABI with pinned host buffers
             ph, hbuf = cr.pinned(g.nv)
             pu, ubuf = cr.pinned(g.ne)
@@ -344,7 +350,12 @@ def main():
             cr.lib.cudaFreeHost(pu)
         m.close()
 
-    if rank == 0:
+    if rank == 0 and not ("fp32" in results and "fp64" in results and "e2e" in results
+                          and results["fp32"]["prof"]):
+        # profiler runs: a short line with the timed paths only
+        print(json.dumps({k: {"ms_per_step": v["ms"] / args.steps} for k, v in results.items()
+                          if k in ("fp32", "fp64")}))
+    elif rank == 0:
         r32, r64 = results["fp32"], results["fp64"]
         total_cells = g.nv * ws
         value = total_cells * args.steps / (r32["ms"] / 1000.0)
