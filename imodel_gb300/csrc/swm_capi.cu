@@ -161,14 +161,12 @@ int load_state(Handle *H, const double *h, const double *u) {
     Work<double> &W = H->W64;
     launch_gather_in(H->nv, H->d_cell_n2o, H->d_stage_h, W.yn_h, 0.0, H->stream);
     launch_gather_in(H->ne, H->d_edge_n2o, H->d_stage_u, W.yn_u, 0.0, H->stream);
-    launch_hed64(H->M, W, W.yn_h, H->stream);
     CK(cudaMemcpyAsync(W.ya_h, W.yn_h, sizeof(double) * H->nv, cudaMemcpyDeviceToDevice, H->stream));
     CK(cudaMemcpyAsync(W.ya_u, W.yn_u, sizeof(double) * H->ne, cudaMemcpyDeviceToDevice, H->stream));
   } else {
     Work<float> &W = H->W32;
     launch_gather_in32(H->nv, H->d_cell_n2o, H->d_stage_h, W.yn_h, H->h_ref, H->stream);
     launch_gather_in32(H->ne, H->d_edge_n2o, H->d_stage_u, W.yn_u, 0.0, H->stream);
-    launch_hed32(H->M, W, W.yn_h, H->stream);
     CK(cudaMemcpyAsync(W.ya_h, W.yn_h, sizeof(float) * H->nv, cudaMemcpyDeviceToDevice, H->stream));
     CK(cudaMemcpyAsync(W.ya_u, W.yn_u, sizeof(float) * H->ne, cudaMemcpyDeviceToDevice, H->stream));
   }
@@ -269,7 +267,11 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
     if ((rc = upload(H, L.c_div32, &M.c_div32)) || (rc = upload(H, L.c_kew32, &M.c_kew32)) ||
         (rc = upload(H, bt32, &M.c_bt32)) || (rc = upload(H, L.e_grad32, &M.e_grad32)) ||
         (rc = upload(H, L.e_stc32, &M.e_stc32)) || (rc = upload(H, L.t_circ32, &M.t_circ32)) ||
-        (rc = upload(H, L.t_kite32, &M.t_kite32)) || (rc = upload(H, L.t_f32, &M.t_f32)))
+        (rc = upload(H, L.t_kite32, &M.t_kite32)) || (rc = upload(H, L.t_f32, &M.t_f32)) ||
+        (rc = upload(H, L.c_nb, &M.c_nb)) || (rc = upload(H, L.c_tr, &M.c_tr)) ||
+        (rc = upload(H, L.c_R32, &M.c_R32)) || (rc = upload(H, L.c_dg32, &M.c_dg32)) ||
+        (rc = upload(H, L.c_inva32, &M.c_inva32)) || (rc = upload(H, L.c_meta, &M.c_meta)) ||
+        (rc = upload(H, L.e_vs, &M.e_vs)))
       return rc;
   }
   const int32_t *cn2o = nullptr, *en2o = nullptr;
@@ -289,6 +291,7 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
     const float keep = H->W32.h_ref;
     if ((rc = alloc_work(H, H->W32))) return rc;
     H->W32.h_ref = keep;
+    if ((rc = dalloc(H, &H->W32.zflux, static_cast<size_t>(kMaxNb) * L.nv))) return rc;
   }
   CK(cudaDeviceSynchronize());
   return IMODEL_SWM_OK;
@@ -567,16 +570,139 @@ int imodel_swm_profile(void *handle, double dt, int32_t nsteps, double avg_ms[4]
   return imodel::check_flags(H);
 }
 
+int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[5]) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H || !choice || nsteps <= 0) return IMODEL_SWM_EINVAL;
+  if (!H->state_set) return imodel::set_error(H, IMODEL_SWM_ESTATE, "no state set");
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  if (H->precision == IMODEL_SWM_FP64) {
+    // the FP64 path has one variant; its launch shape is fixed
+    choice[0] = 0;
+    choice[1] = choice[2] = choice[3] = choice[4] = 256;
+    return IMODEL_SWM_OK;
+  }
+  auto &W = H->W32;
+  const size_t bh = sizeof(float) * H->nv, bu = sizeof(float) * H->ne;
+  float *save = nullptr;
+  if (cudaMalloc(&save, 2 * (bh + bu)) != cudaSuccess)
+    return imodel::set_error(H, IMODEL_SWM_ENOMEM, "autotune: no room to save the state");
+  char *sp = reinterpret_cast<char *>(save);
+  cudaError_t e = cudaSuccess;
+  auto cpy = [&](void *dst, const void *src, size_t n) {
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToDevice, H->stream);
+  };
+  cpy(sp, W.yn_h, bh);
+  cpy(sp + bh, W.yn_u, bu);
+  cpy(sp + bh + bu, W.ya_h, bh);
+  cpy(sp + 2 * bh + bu, W.ya_u, bu);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  auto trial = [&](const imodel::Tune &t) -> float {
+    W.tune = t;
+    if (H->graph) {
+      cudaGraphExecDestroy(H->graph);
+      H->graph = nullptr;
+    }
+    if (e != cudaSuccess || imodel::ensure_graph(H, dt)) return 1e30f;
+    if ((e = cudaGraphLaunch(H->graph, H->stream)) != cudaSuccess) return 1e30f;  // warm-up
+    cudaEventRecord(e0, H->stream);
+    for (int k = 0; k < nsteps && e == cudaSuccess; ++k) e = cudaGraphLaunch(H->graph, H->stream);
+    cudaEventRecord(e1, H->stream);
+    float ms = 1e30f;
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    return e == cudaSuccess ? ms : 1e30f;
+  };
+  const int sizes[3] = {128, 256, 512};
+  imodel::Tune best;
+  float best_ms = 1e30f;
+  for (int v = 0; v < 2; ++v)
+    for (int b : sizes) {
+      imodel::Tune t;
+      t.variant = v;
+      t.bs_tri = t.bs_pre = t.bs_cell = t.bs_edge = b;
+      const float ms = trial(t);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = t;
+      }
+    }
+  // refine the block size of each kernel with the others fixed
+  int imodel::Tune::*fields[4] = {&imodel::Tune::bs_tri, &imodel::Tune::bs_pre,
+                                  &imodel::Tune::bs_cell, &imodel::Tune::bs_edge};
+  for (int f = 0; f < 4; ++f) {
+    if (f == 1 && best.variant == 1) continue;
+    for (int b : sizes) {
+      if (best.*fields[f] == b) continue;
+      imodel::Tune t = best;
+      t.*fields[f] = b;
+      const float ms = trial(t);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = t;
+      }
+    }
+  }
+  W.tune = best;
+  if (H->graph) {
+    cudaGraphExecDestroy(H->graph);
+    H->graph = nullptr;
+  }
+  cpy(W.yn_h, sp, bh);
+  cpy(W.yn_u, sp + bh, bu);
+  cpy(W.ya_h, sp + bh + bu, bh);
+  cpy(W.ya_u, sp + 2 * bh + bu, bu);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(save);
+  if (e != cudaSuccess) return imodel::set_error(H, IMODEL_SWM_ECUDA, cudaGetErrorString(e));
+  choice[0] = best.variant;
+  choice[1] = best.bs_tri;
+  choice[2] = best.bs_pre;
+  choice[3] = best.bs_cell;
+  choice[4] = best.bs_edge;
+  return imodel::check_flags(H);
+}
+
+int imodel_swm_set_tuning(void *handle, const int32_t choice[5]) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H || !choice) return IMODEL_SWM_EINVAL;
+  if (H->precision == IMODEL_SWM_FP64) return IMODEL_SWM_OK;
+  for (int k = 1; k < 5; ++k)
+    if (choice[k] != 128 && choice[k] != 256 && choice[k] != 512)
+      return imodel::set_error(H, IMODEL_SWM_EINVAL, "block sizes must be 128, 256 or 512");
+  if (choice[0] != 0 && choice[0] != 1)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "variant must be 0 or 1");
+  imodel::Tune t;
+  t.variant = choice[0];
+  t.bs_tri = choice[1];
+  t.bs_pre = choice[2];
+  t.bs_cell = choice[3];
+  t.bs_edge = choice[4];
+  H->W32.tune = t;
+  if (H->graph) {
+    cudaGraphExecDestroy(H->graph);
+    H->graph = nullptr;
+  }
+  return IMODEL_SWM_OK;
+}
+
 int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count) {
-  if (!handle || !count || nsteps < 0) return IMODEL_SWM_EINVAL;
-  *count = static_cast<int64_t>(nsteps) * 4 * imodel::kLaunchesPerStage;
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H || !count || nsteps < 0) return IMODEL_SWM_EINVAL;
+  const int fp32 = H->precision == IMODEL_SWM_FP32;
+  *count = static_cast<int64_t>(nsteps) * 4 *
+           imodel::launches_per_stage(fp32, fp32 ? H->W32.tune.variant : 0);
   return IMODEL_SWM_OK;
 }
 
 const char *imodel_swm_main_kernel(void *handle) {
   Handle *H = static_cast<Handle *>(handle);
   if (!H) return "";
-  return H->precision == IMODEL_SWM_FP64 ? "k_edge64" : "k_edge32";
+  if (H->precision == IMODEL_SWM_FP64) return "k_edge64";
+  return H->W32.tune.variant == 1 ? "k_cell32v2" : "k_edge32";
 }
 
 void *imodel_swm_stream(void *handle) {

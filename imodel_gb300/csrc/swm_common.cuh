@@ -26,6 +26,19 @@ struct DevMesh {
   const int32_t *t_ed, *t_v;
   const double *t_lt, *t_kite, *t_areag, *t_f;
   const float *t_circ32, *t_kite32, *t_f32;
+  // cell-centred TRSK variant (FP32)
+  const int32_t *c_nb, *c_tr;
+  const float *c_R32, *c_dg32, *c_inva32;
+  const uint32_t *c_meta, *e_vs;
+};
+
+// Launch configuration of the FP32 stage kernels, chosen by the autotuner.
+//   variant 0: triangle -> edge pre-pass -> cell -> edge (10-entry stencil)
+//   variant 1: triangle -> cell (cell-centred TRSK, writes the PV flux
+//              contribution of each cell edge) -> edge (sums two cells)
+struct Tune {
+  int variant = 1;
+  int bs_tri = 256, bs_pre = 256, bs_cell = 256, bs_edge = 256;
 };
 
 // Working fields of one handle, in the handle's precision T.
@@ -39,6 +52,8 @@ struct Work {
   T *h_ed, *uh, *q_ed;  // [ne]
   T *bern;           // [nv] g (h + b) + K
   T *tend_h, *tend_u;   // tendency outputs (tendency-only evaluations)
+  T *zflux;          // [6][nv] cell-centred PV flux of each cell edge (variant 1)
+  Tune tune;
   int *flags;        // bit 0: PV division by ~0
   T h_ref;           // FP32: h is stored as h - h_ref
   int pv_on;         // testcase >= 2: q = eta / h_tr, else q = 0
@@ -55,7 +70,9 @@ void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
 void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
                     const float *u_in, float *h_out, float *u_out, int stage, float dt,
                     cudaStream_t s, cudaEvent_t *ev = nullptr);
-constexpr int kLaunchesPerStage = 4;
+inline int launches_per_stage(int precision_fp32, int variant) {
+  return (precision_fp32 && variant == 1) ? 3 : 4;
+}
 
 // reference order <-> device order, with precision conversion
 void launch_gather_in(int n, const int32_t *n2o, const double *src, double *dst, double shift,
@@ -68,9 +85,6 @@ void launch_scatter_out(int n, const int32_t *n2o, const double *src, double *ds
 void launch_scatter_out32(int n, const int32_t *n2o, const float *src, double *dst,
                           double shift, int *flags, cudaStream_t s);
 
-// edge averages h_ed (for the kinetic energy integral) of a state
-void launch_hed64(const DevMesh &M, const Work<double> &W, const double *h, cudaStream_t s);
-void launch_hed32(const DevMesh &M, const Work<float> &W, const float *h, cudaStream_t s);
 
 // Compensated FP64 integrals.  Scratch: partial sums, 2 doubles per block
 // and quantity; result[kDiagQ] on the device.

@@ -137,12 +137,6 @@ __global__ void __launch_bounds__(256) k_edge64(DevMesh M, const double *__restr
     yout[e] = rk_stage(stage, momeq, yn[e], acc + e, dt);
 }
 
-__global__ void k_hed64(DevMesh M, const double *__restrict__ h, double *__restrict__ h_ed) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= M.ne) return;
-  h_ed[e] = (h[M.e_v[e]] + h[M.e_v[M.ne + e]]) * 0.5;
-}
-
 template <class T>
 __global__ void k_gather_in(int n, const int32_t *__restrict__ n2o, const double *__restrict__ src,
                             T *__restrict__ dst, double shift) {
@@ -271,7 +265,7 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__rest
                                                       const T *__restrict__ u,
                                                       const T *__restrict__ hs,
                                                       const T *__restrict__ us,
-                                                      const T *__restrict__ h_ed, double h_ref,
+                                                      double h_ref,
                                                       double *__restrict__ scratch) {
   KSum acc[kDiagQ];
 #pragma unroll
@@ -305,7 +299,9 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__rest
   for (int e = tid; e < M.ne; e += stride) {
     const double ue = static_cast<double>(u[e]);
     if (!isfinite(ue)) nan = 1.0;
-    const double he = static_cast<double>(h_ed[e]) + h_ref;
+    // h_ed of the last stage input, as calc_energies uses (swm.f90:2738)
+    const double he =
+        (static_cast<double>(hs[M.e_v[e]]) + static_cast<double>(hs[M.e_v[M.ne + e]])) * 0.5 + h_ref;
     acc[Q_KE].add(M.e_area[e] * he * (ue * ue));
   }
   for (int t = tid; t < M.nt; t += stride) {
@@ -424,10 +420,6 @@ void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
   if (ev) cudaEventRecord(ev[4], s);
 }
 
-void launch_hed64(const DevMesh &M, const Work<double> &W, const double *h, cudaStream_t s) {
-  k_hed64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, h, W.h_ed);
-}
-
 void launch_gather_in(int n, const int32_t *n2o, const double *src, double *dst, double shift,
                       cudaStream_t s) {
   k_gather_in<double><<<nblocks(n, 256), 256, 0, s>>>(n, n2o, src, dst, shift);
@@ -452,7 +444,7 @@ void launch_trsk_tangent(const DevMesh &M, const double *u, double *utg, cudaStr
 template <class T>
 void launch_diag(const DevMesh &M, const Work<T> &W, const T *h, const T *u, const T *hs,
                  const T *us, double *scratch, double *result, cudaStream_t s) {
-  k_diag<T><<<kRedBlocks, kRedThreads, 0, s>>>(M, h, u, hs, us, W.h_ed,
+  k_diag<T><<<kRedBlocks, kRedThreads, 0, s>>>(M, h, u, hs, us,
                                                 static_cast<double>(W.h_ref), scratch);
   const unsigned maxmask = (1u << Q_MAXDIV) | (1u << Q_NAN);
   k_finalize<<<kDiagQ, kRedThreads, 0, s>>>(scratch, kRedBlocks, kDiagQ, maxmask, result);

@@ -141,6 +141,39 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
   L.c_areag.resize(NV);
   L.c_cellarea.resize(NV);
   L.c_bt.assign(NV, 0.0);
+  L.c_nb.assign(kMaxNb * NV, 0);
+  L.c_tr.assign(kMaxNb * NV, 0);
+  L.c_R32.assign(kMaxNb * NV, 0.0f);
+  L.c_dg32.assign(kMaxNb * NV, 0.0f);
+  L.c_inva32.resize(NV);
+  L.c_meta.resize(NV);
+  if (nv >= (1 << 28)) return "more than 2^28 cells";
+  for (int i = 0; i < nv; ++i) {
+    const int c = L.cell_n2o[i];
+    const int n = m.nnb[c];
+    uint32_t tbits = 0;
+    for (int j = 0; j < n; ++j) {
+      const size_t q = 6 * static_cast<size_t>(c) + j;
+      const int e = m.v_ed[q] - 1;
+      // the neighbour across slot j is the other end of edge j
+      const int a = m.ed_v[2 * static_cast<size_t>(e)] - 1, b = m.ed_v[2 * static_cast<size_t>(e) + 1] - 1;
+      if (a != c && b != c) return "edge " + std::to_string(e + 1) + " does not touch cell " + std::to_string(c + 1);
+      L.c_nb[j * NV + i] = L.cell_o2n[a == c ? b : a];
+      const int t = m.v_tr[q] - 1;
+      if (t < 0 || t >= nt) return "v_tr index out of range at cell " + std::to_string(c + 1);
+      // edge j lies between triangles j-1 and j (smeshpack.f90:1071-1082)
+      const int tp = m.v_tr[6 * static_cast<size_t>(c) + (j + n - 1) % n] - 1;
+      const int s0 = m.ed_sh[2 * static_cast<size_t>(e)] - 1, s1 = m.ed_sh[2 * static_cast<size_t>(e) + 1] - 1;
+      if (!((s0 == t && s1 == tp) || (s0 == tp && s1 == t)))
+        return "v_tr order does not match v_ed at cell " + std::to_string(c + 1);
+      L.c_tr[j * NV + i] = L.tri_o2n[t];
+      L.c_R32[j * NV + i] = static_cast<float>(m.hx_hxtr_area[q]);
+      L.c_dg32[j * NV + i] = static_cast<float>(m.hx_ttgout[q] * m.edhx_leng[e]);
+      if (m.hx_tnrccw[q] < 0) tbits |= 1u << j;
+    }
+    L.c_meta[i] = static_cast<uint32_t>(n) | (tbits << 8);
+    L.c_inva32[i] = static_cast<float>(1.0 / (m.hx_areag[c] * m.erad));
+  }
   for (int i = 0; i < nv; ++i) {
     const int c = L.cell_n2o[i];
     const int n = m.nnb[c];
@@ -177,6 +210,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
   L.e_stk.assign(kMaxSt * NE, 0);
   L.e_stw.assign(kMaxSt * NE, 0.0);
   L.e_stc32.assign(kMaxSt * NE, 0.0f);
+  L.e_vs.assign(2 * NE, 0u);
   for (int i = 0; i < ne; ++i) {
     const int e = L.edge_n2o[i];
     for (int s = 0; s < 2; ++s) {
@@ -202,6 +236,8 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
           break;
         }
       if (edcelli < 0) return "edge " + std::to_string(e + 1) + " missing from its cell's edge list";
+      L.e_vs[s * NE + i] = static_cast<uint32_t>(L.cell_o2n[node]) |
+                           (static_cast<uint32_t>(edcelli) << 28);
       for (int j = 0; j < n; ++j) {
         if (j == edcelli) continue;
         if (ns >= kMaxSt) return "TRSK stencil longer than 10 at edge " + std::to_string(e + 1);

@@ -43,6 +43,15 @@ struct Layout {
   std::vector<double> c_bt;                  // [nv] bottom topography
   std::vector<float> c_div32;                // ttgout*d/(A*erad)
   std::vector<float> c_kew32;                // 0.25*l*d / cell_area
+  // cell-centred TRSK variant (FP32): the PV flux of an edge is assembled
+  // from the two cells' kite fractions instead of a 10-entry edge stencil
+  std::vector<int32_t> c_nb;                 // neighbour cell across slot j
+  std::vector<int32_t> c_tr;                 // triangle v%tr(j) (edges j, j+1)
+  std::vector<float> c_R32;                  // kite fraction hxtr_area(j)
+  std::vector<float> c_dg32;                 // ttgout(j) * edhx%leng(j)
+  std::vector<float> c_inva32;               // [nv] 1/(A*erad)
+  std::vector<uint32_t> c_meta;              // [nv] nnb | tnrccw<0 bits << 8
+  std::vector<uint32_t> e_vs;                // [2][ne] cell | slot << 28
 
   // edges [ne] and [2][ne]
   std::vector<int32_t> e_v;                  // [2][ne] cells (ed%v = edhx%sh)

@@ -232,6 +232,18 @@ class SWM:
         self._check(self.lib.imodel_swm_profile(self._handle, dt, nsteps, _capi.as_f64p(out)))
         return dict(zip(self.KERNELS, out.tolist()))
 
+    def autotune(self, dt: float, nsteps: int = 5) -> dict:
+        """Times the FP32 fusion variants and block sizes on the current
+        state, keeps the fastest, restores the state."""
+        c = np.zeros(5, dtype=np.int32)
+        self._check(self.lib.imodel_swm_autotune(self._handle, dt, nsteps, _capi.as_i32p(c)))
+        return dict(zip(("variant", "bs_tri", "bs_pre", "bs_cell", "bs_edge"), c.tolist()))
+
+    def set_tuning(self, variant: int = 1, bs_tri: int = 256, bs_pre: int = 256,
+                   bs_cell: int = 256, bs_edge: int = 256):
+        c = np.array([variant, bs_tri, bs_pre, bs_cell, bs_edge], dtype=np.int32)
+        self._check(self.lib.imodel_swm_set_tuning(self._handle, _capi.as_i32p(c)))
+
     def launch_count(self, nsteps: int) -> int:
         c = ctypes.c_int64()
         self._check(self.lib.imodel_swm_launch_count(self._handle, nsteps, ctypes.byref(c)))

@@ -152,6 +152,52 @@ def test_fp32_error_against_fp64(grid_at):
     assert eh < disc / 100
 
 
+@pytest.mark.parametrize("variant", [0, 1])
+def test_fp32_variants_against_fp64(grid_at, variant):
+    """Both FP32 fusion variants (edge stencil, cell-centred TRSK) stay within
+    FP32 round-off of the FP64 oracle over 5 days of case 2 at level 5."""
+    g = grid_at(5)
+    h, u = swm.initialize_fields_tc2(g)
+    n = swm.ntime_for(5.0, 450.0)
+    m = SWM(g, "fp32")
+    m.set_tuning(variant=variant)
+    m.set_state(h, u)
+    m.advance(450.0, n)
+    hg, ug = m.get_state()
+    hr, ur = oracle.Oracle(g, 2).run(h, u, 450.0, n)
+    eh = rel_l2(hg, hr, g.hx_areag)
+    eu = rel_l2(ug, ur, g.ed_leng * g.edhx_leng)
+    print(f"FP32 variant {variant} vs FP64, L5 5 days: rel L2 h {eh:.3e} u {eu:.3e}")
+    assert eh < 1e-6 and eu < 1e-4
+
+
+def test_fp32_block_sizes_do_not_change_results(grid_at):
+    g = grid_at(4)
+    h, u = swm.initialize_fields_tc2(g)
+    out = []
+    for bs in (128, 256, 512):
+        m = SWM(g, "fp32")
+        m.set_tuning(variant=1, bs_tri=bs, bs_pre=bs, bs_cell=bs, bs_edge=bs)
+        out.append(m.ode_rk4(h, u, 900.0, 5))
+    for o in out[1:]:
+        assert np.array_equal(o[0], out[0][0]) and np.array_equal(o[1], out[0][1])
+
+
+def test_autotune_keeps_state(grid_at):
+    g = grid_at(6)
+    h, u = swm.initialize_fields_tc2(g)
+    m = SWM(g, "fp32")
+    m.set_state(h, u)
+    choice = m.autotune(225.0, 3)
+    assert choice["variant"] in (0, 1)
+    h1, u1 = m.get_state()
+    np.testing.assert_allclose(h1, h, rtol=0, atol=1e-3)   # FP32 storage of h - h_ref
+    np.testing.assert_allclose(u1, u, rtol=0, atol=1e-5)
+    m.advance(225.0, 2)
+    d = m.diagnostics()
+    assert d["nan_found"] == 0
+
+
 def test_fp32_tendency_close(grid_at):
     g = grid_at(4)
     h, u = swm.initialize_fields_tc2(g)
