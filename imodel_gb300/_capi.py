@@ -24,6 +24,7 @@ EDIVZERO = 4
 ENOMEM = 5
 ESTATE = 6
 ENODEV = 7
+ETOOBIG = 8
 
 FP64 = 0
 FP32 = 1
@@ -31,6 +32,7 @@ FP32 = 1
 STATUS_NAMES = {
     OK: "OK", EINVAL: "EINVAL", ECUDA: "ECUDA", EBLOWUP: "EBLOWUP",
     EDIVZERO: "EDIVZERO", ENOMEM: "ENOMEM", ESTATE: "ESTATE", ENODEV: "ENODEV",
+    ETOOBIG: "ETOOBIG",
 }
 
 
@@ -100,7 +102,7 @@ SWM_SYMBOLS = [
     "imodel_swm_destroy", "imodel_swm_last_error", "imodel_swm_set_state",
     "imodel_swm_get_state", "imodel_swm_advance", "imodel_swm_profile",
     "imodel_swm_autotune", "imodel_swm_set_tuning", "imodel_swm_launch_count",
-    "imodel_swm_main_kernel", "imodel_swm_stream",
+    "imodel_swm_main_kernel", "imodel_swm_stream", "imodel_swm_weighted_sums_noalloc",
 ]
 
 _libs: dict = {}
@@ -168,6 +170,7 @@ def swm_lib() -> ctypes.CDLL:
         lib.imodel_swm_main_kernel.restype = ctypes.c_char_p
         lib.imodel_swm_stream.argtypes = [vp]
         lib.imodel_swm_stream.restype = ctypes.c_void_p
+        lib.imodel_swm_weighted_sums_noalloc.argtypes = [vp, vp, ctypes.c_int64, vp, vp]
         lib._typed = True
     return lib
 

@@ -51,6 +51,7 @@ extern "C" {
 #define IMODEL_SWM_ENOMEM 5     /* device allocation failed                   */
 #define IMODEL_SWM_ESTATE 6     /* call order violated (no state set, ...)    */
 #define IMODEL_SWM_ENODEV 7     /* no CUDA device available                   */
+#define IMODEL_SWM_ETOOBIG 8    /* input longer than a fixed-size buffer holds */
 
 /* ---- precision modes --------------------------------------------------- */
 #define IMODEL_SWM_FP64 0 /* reference operation order, FP64 everywhere      */
@@ -185,6 +186,30 @@ int imodel_swm_profile(void *handle, double dt, int32_t nsteps, double avg_ms[4]
 const char *imodel_swm_main_kernel(void *handle);
 /* The CUDA stream (cudaStream_t) all work of the handle is issued on. */
 void *imodel_swm_stream(void *handle);
+
+/* Area-weighted sums of one field with no device allocation.  No counterpart
+ * in the reference: it is the compensated reduction behind
+ * imodel_swm_diagnostics (sumf_areas / sumfsq_areas) for callers that cannot
+ * call cudaMalloc -- a host whose device memory is all handed out by another
+ * runtime's pool, code running inside a CUDA stream capture (where an
+ * allocation would break the capture), or a plugin that may only touch the
+ * buffers its caller gives it.  Instead of a handle's buffer it uses a
+ * 256 KiB block-partials array built into the library (every GPU that loads
+ * the library keeps it until the process exits).
+ *
+ * w, f: device arrays of n doubles (weights, field); out: device array of 4
+ * doubles receiving {sum w, sum w*f, sum w*f^2, max |f|}, the sums
+ * Neumaier-compensated.  stream: a cudaStream_t (NULL = legacy default
+ * stream); the call only enqueues work, out is valid once the stream reaches
+ * it.  n may be at most 33,554,432 (4096 blocks x 256 threads x 32 elements);
+ * a longer input returns IMODEL_SWM_ETOOBIG and launches nothing.  Runs on the
+ * current device.  Its first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  All calls share the one array: calls whose work overlaps on the
+ * GPU (different streams, or different host threads on one device) race and
+ * must be serialised by the caller. */
+int imodel_swm_weighted_sums_noalloc(const double *w, const double *f, int64_t n, double *out,
+                                     void *stream);
 
 #ifdef __cplusplus
 }
