@@ -302,6 +302,9 @@ def main():
     ap.add_argument("--precisions", default="fp64,fp32")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-kprof", action="store_true")
+    ap.add_argument("--tuning", default="",
+                    help="FP32 launch choice 'variant,bs_tri,bs_pre,bs_cell,bs_edge' "
+                         "instead of autotuning")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -322,7 +325,14 @@ def main():
     for precision in precisions:
         m = swm.SWM(g, precision=precision, device=local)
         m.set_state(h, u)
-        tuning = m.autotune(DT, 5) if precision == "fp32" else None
+        tuning = None
+        if precision == "fp32":
+            if args.tuning:
+                c = [int(x) for x in args.tuning.split(",")]
+                m.set_tuning(*c)
+                tuning = dict(zip(("variant", "bs_tri", "bs_pre", "bs_cell", "bs_edge"), c))
+            else:
+                tuning = m.autotune(DT, 5)
         stream = m.stream()
         m.advance(DT, args.warmup)
         cr.sync()
