@@ -87,6 +87,8 @@ def build_swm_lib(force: bool = False) -> str:
         "swm_k64.cu": ["--fmad=false"],
         "swm_k32.cu": [],
         "swm_capi.cu": [],
+        "swm_ens.cu": [],
+        "mlp.cu": [],
         # allocation-free weighted sums: compensated summation, no contraction
         "swm_noalloc.cu": ["--fmad=false"],
     }

@@ -103,6 +103,16 @@ SWM_SYMBOLS = [
     "imodel_swm_get_state", "imodel_swm_advance", "imodel_swm_profile",
     "imodel_swm_autotune", "imodel_swm_set_tuning", "imodel_swm_launch_count",
     "imodel_swm_main_kernel", "imodel_swm_stream", "imodel_swm_weighted_sums_noalloc",
+    "imodel_swm_ensemble_create", "imodel_swm_ensemble_set_state",
+    "imodel_swm_ensemble_get_state", "imodel_swm_ensemble_advance", "imodel_swm_ensemble_tune",
+    "imodel_swm_ensemble_destroy", "imodel_swm_ensemble_last_error",
+    "imodel_swm_ensemble_stream",
+]
+
+MLP_SYMBOLS = [
+    "imodel_mlp_create", "imodel_mlp_set_params", "imodel_mlp_get_params",
+    "imodel_mlp_forward", "imodel_mlp_grad", "imodel_mlp_load_dataset", "imodel_mlp_train",
+    "imodel_mlp_destroy", "imodel_mlp_last_error",
 ]
 
 _libs: dict = {}
@@ -171,6 +181,34 @@ def swm_lib() -> ctypes.CDLL:
         lib.imodel_swm_stream.argtypes = [vp]
         lib.imodel_swm_stream.restype = ctypes.c_void_p
         lib.imodel_swm_weighted_sums_noalloc.argtypes = [vp, vp, ctypes.c_int64, vp, vp]
+        lib.imodel_swm_ensemble_create.argtypes = [ctypes.POINTER(Mesh), ctypes.c_int32, c_i32p,
+                                                   ctypes.c_int32, ctypes.c_int32,
+                                                   ctypes.POINTER(vp)]
+        lib.imodel_swm_ensemble_set_state.argtypes = [vp, ctypes.c_int32, ctypes.c_int32,
+                                                      c_f64p, c_f64p]
+        lib.imodel_swm_ensemble_get_state.argtypes = [vp, ctypes.c_int32, ctypes.c_int32,
+                                                      c_f64p, c_f64p]
+        lib.imodel_swm_ensemble_advance.argtypes = [vp, c_f64p, c_i32p]
+        lib.imodel_swm_ensemble_tune.argtypes = [vp, c_f64p, ctypes.c_int32, c_i32p]
+        lib.imodel_swm_ensemble_destroy.argtypes = [vp]
+        lib.imodel_swm_ensemble_last_error.argtypes = [vp]
+        lib.imodel_swm_ensemble_last_error.restype = ctypes.c_char_p
+        lib.imodel_swm_ensemble_stream.argtypes = [vp]
+        lib.imodel_swm_ensemble_stream.restype = ctypes.c_void_p
+        u16p = ctypes.POINTER(ctypes.c_uint16)
+        f32p = ctypes.POINTER(ctypes.c_float)
+        lib.imodel_mlp_create.argtypes = [ctypes.c_int32, ctypes.POINTER(vp)]
+        lib.imodel_mlp_set_params.argtypes = [vp, f32p, ctypes.c_int32]
+        lib.imodel_mlp_get_params.argtypes = [vp, f32p, ctypes.c_int32]
+        lib.imodel_mlp_forward.argtypes = [vp, u16p, ctypes.c_int64, f32p]
+        lib.imodel_mlp_grad.argtypes = [vp, u16p, f32p, ctypes.c_int64, ctypes.c_uint64,
+                                        ctypes.c_int64, f32p, ctypes.POINTER(ctypes.c_double)]
+        lib.imodel_mlp_load_dataset.argtypes = [vp, u16p, f32p, ctypes.c_int64]
+        lib.imodel_mlp_train.argtypes = [vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_float,
+                                         ctypes.c_uint64, f32p]
+        lib.imodel_mlp_destroy.argtypes = [vp]
+        lib.imodel_mlp_last_error.argtypes = [vp]
+        lib.imodel_mlp_last_error.restype = ctypes.c_char_p
         lib._typed = True
     return lib
 

@@ -1,0 +1,728 @@
+// Per-edge MLP of the learned TRSK correction: 24 -> 64 -> 64 -> 1, GELU,
+// BF16 operands with FP32 accumulation on the 5th-generation tensor cores
+// (tcgen05, accumulators in TMEM), forward, backward and Adam.
+//
+// Parameter vector (FP32 master copy, 5825 values):
+//     W1[64][24] (out-major), b1[64], W2[64][64] (out-major), b2[64], w3[64], b3
+// Inputs x[n][24] are BF16 (bit patterns in uint16).
+//
+// Tiles of 128 rows; one thread per row.  Forward per tile:
+//     D1 = X W1^T      (M=128, N=64, K=32: inputs padded 24 -> 32)
+//     H1 = GELU(D1 + b1) -> BF16 -> shared memory
+//     D2 = H1 W2^T     (M=128, N=64, K=64)
+//     y  = GELU(D2 + b2) . w3 + b3   (FP32, CUDA cores)
+// Backward per tile (mean squared error):
+//     dZ2 = dy w3 * GELU'(Z2) -> BF16;   dH1 = dZ2 W2 (M=128, N=64, K=64)
+//     dZ1 = dH1 * GELU'(Z1) -> BF16
+//     one accumulating MMA per tile gives dW2, dW1, db2, db1 at once:
+//     DW += AW BW^T, AW = [H1^T; X^T; ones] (128 x batch), BW = [dZ2^T; dZ1^T]
+//     (128 x batch), so DW[i][o] = dW2[o][i], DW[64+i][64+o] = dW1[o][i],
+//     DW[96][o] = db2[o], DW[96][64+o] = db1[o].
+// dw3 and db3 are warp-shuffle sums.  Each CTA writes its partial gradient;
+// a second kernel sums the partials in a fixed order (deterministic).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "imodel_mlp.h"
+#include "imodel_swm.h"
+#include "tc05.cuh"
+
+namespace imodel {
+namespace {
+
+using namespace tc05;
+
+constexpr int NIN = 24, K1 = 32, NH = 64, TM = 128;
+constexpr int OFF_W1 = 0, OFF_B1 = 1536, OFF_W2 = 1600, OFF_B2 = 5696, OFF_W3 = 5760,
+              OFF_B3 = 5824;
+constexpr int NPARAM = 5825;
+constexpr int NPART = NPARAM + 1;  // + loss
+constexpr int ERR_WAIT = 8;
+
+struct Weights {
+  const uint16_t *w1img;   // B operand of layer 1: [64 out][32 in], K-major image
+  const uint16_t *w2img;   // B operand of layer 2: [64 out][64 in]
+  const uint16_t *w2timg;  // B operand of dH1:     [64 in][64 out]
+  const float *p;          // FP32 master parameters
+};
+
+__device__ __forceinline__ uint16_t bf16bits(float v) {
+  return __bfloat16_as_ushort(__float2bfloat16_rn(v));
+}
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+  return static_cast<uint32_t>(bf16bits(a)) | (static_cast<uint32_t>(bf16bits(b)) << 16);
+}
+// GELU in its tanh form (Hendrycks & Gimpel 2016),
+//   gelu(z) = z/2 (1 + tanh(c (z + a z^3))),  c = sqrt(2/pi), a = 0.044715,
+// with the tanh of the hardware's special-function unit (tanh.approx.f32).
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float gelu(float z) {
+  const float u = 0.7978845608028654f * (z + 0.044715f * z * z * z);
+  return 0.5f * z * (1.0f + tanh_fast(u));
+}
+__device__ __forceinline__ float gelu_grad(float z) {
+  const float u = 0.7978845608028654f * (z + 0.044715f * z * z * z);
+  const float th = tanh_fast(u);
+  return 0.5f * (1.0f + th) +
+         0.5f * z * (1.0f - th * th) * 0.7978845608028654f * (1.0f + 3.0f * 0.044715f * z * z);
+}
+
+// row `r` of a K-major 16-bit operand with `kc` columns, from 64 FP32 values
+__device__ __forceinline__ void store_row64(uint8_t *op, int r, const float (&v)[64], int kc) {
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    uint4 q;
+    q.x = pack2(v[8 * c + 0], v[8 * c + 1]);
+    q.y = pack2(v[8 * c + 2], v[8 * c + 3]);
+    q.z = pack2(v[8 * c + 4], v[8 * c + 5]);
+    q.w = pack2(v[8 * c + 6], v[8 * c + 7]);
+    *reinterpret_cast<uint4 *>(op + kmaj_off(r, 8 * c, kc)) = q;
+  }
+}
+
+// 64 FP32 columns [col, col+64) of this thread's TMEM lane
+__device__ __forceinline__ void ld64(uint32_t taddr, float (&v)[64]) {
+  float t[16];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    ld16(taddr + 16 * q, t);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[16 * q + i] = t[i];
+  }
+  wait_ld();
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+__host__ __device__ __forceinline__ uint64_t splitmix(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+// ---- weight images ---------------------------------------------------------
+__global__ void k_make_images(const float *__restrict__ p, uint16_t *w1img, uint16_t *w2img,
+                              uint16_t *w2timg) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < NH * K1) {  // layer-1 B operand, zero-padded inputs 24..31
+    const int o = t / K1, i = t % K1;
+    const float w = i < NIN ? p[OFF_W1 + o * NIN + i] : 0.0f;
+    w1img[kmaj_off(o, i, K1) / 2] = bf16bits(w);
+  }
+  if (t < NH * NH) {
+    const int o = t / NH, i = t % NH;
+    const uint16_t w = bf16bits(p[OFF_W2 + o * NH + i]);
+    w2img[kmaj_off(o, i, NH) / 2] = w;   // [out][in]
+    w2timg[kmaj_off(i, o, NH) / 2] = w;  // [in][out]
+  }
+}
+
+// ---- forward (inference) ---------------------------------------------------
+// dynamic shared memory: A1 8 KiB | B1 4 KiB | A2 16 KiB | B2 8 KiB
+constexpr int FWD_SMEM = 8192 + 4096 + 16384 + 8192;
+
+__global__ void __launch_bounds__(TM) k_mlp_forward(Weights W, const uint16_t *__restrict__ x,
+                                                     int64_t n, float *__restrict__ y, int *err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t *A1 = smem, *B1 = smem + 8192, *A2 = B1 + 4096, *B2 = A2 + 16384;
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tslot;
+  __shared__ float sb1[NH], sb2[NH], sw3[NH];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int i = tid; i < 4096 / 16; i += TM)
+    reinterpret_cast<uint4 *>(B1)[i] = reinterpret_cast<const uint4 *>(W.w1img)[i];
+  for (int i = tid; i < 8192 / 16; i += TM)
+    reinterpret_cast<uint4 *>(B2)[i] = reinterpret_cast<const uint4 *>(W.w2img)[i];
+  if (tid < NH) {
+    sb1[tid] = W.p[OFF_B1 + tid];
+    sb2[tid] = W.p[OFF_B2 + tid];
+    sw3[tid] = W.p[OFF_W3 + tid];
+  }
+  const float b3 = W.p[OFF_B3];
+  if (tid == 0) mbar_init(&mbar, 1);
+  if (warp == 0) tmem_alloc(&tslot, 128);
+  fence_async_smem();
+  sync_cta();
+  const uint32_t tmem = tslot;
+  const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+  const uint32_t id64 = idesc_bf16(TM, NH);
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int64_t tile = blockIdx.x; ok && tile * TM < n; tile += gridDim.x) {
+    const int64_t row = tile * TM + tid;
+    uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0, c2 = c0;
+    if (row < n) {
+      const uint4 *src = reinterpret_cast<const uint4 *>(x + row * NIN);
+      c0 = src[0];
+      c1 = src[1];
+      c2 = src[2];
+    }
+    *reinterpret_cast<uint4 *>(A1 + kmaj_off(tid, 0, K1)) = c0;
+    *reinterpret_cast<uint4 *>(A1 + kmaj_off(tid, 8, K1)) = c1;
+    *reinterpret_cast<uint4 *>(A1 + kmaj_off(tid, 16, K1)) = c2;
+    *reinterpret_cast<uint4 *>(A1 + kmaj_off(tid, 24, K1)) = make_uint4(0, 0, 0, 0);
+    fence_async_smem();
+    sync_cta();
+    if (tid == 0) {
+      for (int s = 0; s < K1 / 16; ++s)
+        mma(tmem, smem_desc(smem_u32(A1) + 256 * s, 128, K1 * 16),
+            smem_desc(smem_u32(B1) + 256 * s, 128, K1 * 16), id64, s);
+      commit(&mbar);
+    }
+    ok = __syncthreads_and(mbar_wait(&mbar, phase, err, ERR_WAIT)) != 0;
+    phase ^= 1u;
+    fence_after_sync();
+    float v[64];
+    if (ok) {
+      ld64(tmem + lane_base, v);
+#pragma unroll
+      for (int j = 0; j < NH; ++j) v[j] = gelu(v[j] + sb1[j]);
+      store_row64(A2, tid, v, NH);
+    }
+    fence_async_smem();
+    sync_cta();
+    if (ok && tid == 0) {
+      for (int s = 0; s < NH / 16; ++s)
+        mma(tmem + 64, smem_desc(smem_u32(A2) + 256 * s, 128, NH * 16),
+            smem_desc(smem_u32(B2) + 256 * s, 128, NH * 16), id64, s);
+      commit(&mbar);
+    }
+    if (ok) {  // ok is uniform across the CTA
+      ok = __syncthreads_and(mbar_wait(&mbar, phase, err, ERR_WAIT)) != 0;
+      phase ^= 1u;
+    }
+    fence_after_sync();
+    if (ok) {
+      ld64(tmem + lane_base + 64, v);
+      float acc = b3;
+#pragma unroll
+      for (int j = 0; j < NH; ++j) acc += gelu(v[j] + sb2[j]) * sw3[j];
+      if (row < n) y[row] = acc;
+    }
+    sync_cta();
+  }
+  sync_cta();
+  if (warp == 0) tmem_dealloc(tmem, 128);
+}
+
+// ---- fused forward + backward over a batch ---------------------------------
+// dynamic shared memory: A1 8K | B1 4K | A2 16K | B2 8K | B2T 8K | A3 16K |
+// AW 32K | BW 32K
+constexpr int TRN_SMEM = 8192 + 4096 + 16384 + 8192 + 8192 + 16384 + 32768 + 32768;
+
+__global__ void __launch_bounds__(TM, 1)
+    k_mlp_train(Weights W, const uint16_t *__restrict__ x, const float *__restrict__ t,
+                int64_t n, int64_t batch, uint64_t seed, float inv_batch,
+                float *__restrict__ partials, int *err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t *A1 = smem, *B1 = A1 + 8192, *A2 = B1 + 4096, *B2 = A2 + 16384, *B2T = B2 + 8192,
+          *A3 = B2T + 8192, *AW = A3 + 16384, *BW = AW + 32768;
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tslot;
+  __shared__ float sb1[NH], sb2[NH], sw3[NH], sdw3[NH], sdb3, sloss;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int i = tid; i < 4096 / 16; i += TM)
+    reinterpret_cast<uint4 *>(B1)[i] = reinterpret_cast<const uint4 *>(W.w1img)[i];
+  for (int i = tid; i < 8192 / 16; i += TM) {
+    reinterpret_cast<uint4 *>(B2)[i] = reinterpret_cast<const uint4 *>(W.w2img)[i];
+    reinterpret_cast<uint4 *>(B2T)[i] = reinterpret_cast<const uint4 *>(W.w2timg)[i];
+  }
+  // AW rows 88..127 stay zero except row 96 (ones, for the bias sums)
+  for (int i = tid; i < 32768 / 16; i += TM) reinterpret_cast<uint4 *>(AW)[i] = make_uint4(0, 0, 0, 0);
+  if (tid < NH) {
+    sb1[tid] = W.p[OFF_B1 + tid];
+    sb2[tid] = W.p[OFF_B2 + tid];
+    sw3[tid] = W.p[OFF_W3 + tid];
+    sdw3[tid] = 0.0f;
+  }
+  if (tid == 0) {
+    sdb3 = 0.0f;
+    sloss = 0.0f;
+  }
+  const float b3 = W.p[OFF_B3];
+  __syncthreads();
+  *reinterpret_cast<uint16_t *>(AW + kmaj_off(96, tid, TM)) = bf16bits(1.0f);
+  if (tid == 0) mbar_init(&mbar, 1);
+  if (warp == 0) tmem_alloc(&tslot, 256);
+  fence_async_smem();
+  sync_cta();
+  const uint32_t tmem = tslot;
+  const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+  const uint32_t id64 = idesc_bf16(TM, NH), id128 = idesc_bf16(TM, 128);
+  uint32_t phase = 0;
+  bool ok = true;
+  bool first = true;
+  const int64_t ntiles = (batch + TM - 1) / TM;
+  for (int64_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+    const int64_t pos = tile * TM + tid;  // position in the batch
+    const bool live = pos < batch;
+    // seed 0: rows 0..batch-1 in order; otherwise rows drawn with replacement
+    const int64_t row =
+        !live ? 0
+              : (seed == 0 ? pos
+                           : static_cast<int64_t>(splitmix(seed ^ static_cast<uint64_t>(pos)) %
+                                                  static_cast<uint64_t>(n)));
+    // --- inputs: A1 (row-major) and X^T rows 64..87 of AW ----------------
+    uint4 c[3] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
+    if (live) {
+      const uint4 *src = reinterpret_cast<const uint4 *>(x + row * NIN);
+      c[0] = src[0];
+      c[1] = src[1];
+      c[2] = src[2];
+    }
+    const float target = live ? t[row] : 0.0f;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) *reinterpret_cast<uint4 *>(A1 + kmaj_off(tid, 8 * q, K1)) = c[q];
+    *reinterpret_cast<uint4 *>(A1 + kmaj_off(tid, 24, K1)) = make_uint4(0, 0, 0, 0);
+    const uint16_t *xs = reinterpret_cast<const uint16_t *>(c);
+#pragma unroll
+    for (int i = 0; i < NIN; ++i) *reinterpret_cast<uint16_t *>(AW + kmaj_off(64 + i, tid, TM)) = xs[i];
+    fence_async_smem();
+    sync_cta();
+    if (tid == 0) {
+      for (int s = 0; s < K1 / 16; ++s)
+        mma(tmem, smem_desc(smem_u32(A1) + 256 * s, 128, K1 * 16),
+            smem_desc(smem_u32(B1) + 256 * s, 128, K1 * 16), id64, s);
+      commit(&mbar);
+    }
+    ok = __syncthreads_and(mbar_wait(&mbar, phase, err, ERR_WAIT)) != 0;
+    phase ^= 1u;
+    fence_after_sync();
+    float v[64];
+    if (ok) {  // H1 = GELU(Z1 + b1): A2 (row-major) and AW rows 0..63 (H1^T)
+      ld64(tmem + lane_base, v);
+#pragma unroll
+      for (int j = 0; j < NH; ++j) v[j] = gelu(v[j] + sb1[j]);
+      store_row64(A2, tid, v, NH);
+#pragma unroll
+      for (int j = 0; j < NH; ++j)
+        *reinterpret_cast<uint16_t *>(AW + kmaj_off(j, tid, TM)) = live ? bf16bits(v[j]) : 0;
+    }
+    fence_async_smem();
+    sync_cta();
+    if (ok && tid == 0) {
+      for (int s = 0; s < NH / 16; ++s)
+        mma(tmem + 64, smem_desc(smem_u32(A2) + 256 * s, 128, NH * 16),
+            smem_desc(smem_u32(B2) + 256 * s, 128, NH * 16), id64, s);
+      commit(&mbar);
+    }
+    if (ok) {  // ok is uniform across the CTA
+      ok = __syncthreads_and(mbar_wait(&mbar, phase, err, ERR_WAIT)) != 0;
+      phase ^= 1u;
+    }
+    fence_after_sync();
+    if (ok) {  // output, loss, dZ2
+      ld64(tmem + lane_base + 64, v);
+      float h2[64];
+      float yv = b3;
+#pragma unroll
+      for (int j = 0; j < NH; ++j) {
+        v[j] += sb2[j];
+        h2[j] = gelu(v[j]);
+        yv += h2[j] * sw3[j];
+      }
+      const float r = live ? yv - target : 0.0f;
+      const float dy = 2.0f * r * inv_batch;
+      float ls = warp_sum(r * r), sdy = warp_sum(dy);
+      if (lane == 0) {
+        atomicAdd(&sloss, ls);
+        atomicAdd(&sdb3, sdy);
+      }
+#pragma unroll
+      for (int j = 0; j < NH; ++j) {
+        const float dw = warp_sum(h2[j] * dy);
+        if (lane == 0) atomicAdd(&sdw3[j], dw);
+        v[j] = dy * sw3[j] * gelu_grad(v[j]);  // dZ2
+      }
+      store_row64(A3, tid, v, NH);
+#pragma unroll
+      for (int j = 0; j < NH; ++j)
+        *reinterpret_cast<uint16_t *>(BW + kmaj_off(j, tid, TM)) = bf16bits(v[j]);
+    }
+    fence_async_smem();
+    sync_cta();
+    if (ok && tid == 0) {  // dH1 = dZ2 W2 into the second TMEM block
+      for (int s = 0; s < NH / 16; ++s)
+        mma(tmem + 64, smem_desc(smem_u32(A3) + 256 * s, 128, NH * 16),
+            smem_desc(smem_u32(B2T) + 256 * s, 128, NH * 16), id64, s);
+      commit(&mbar);
+    }
+    if (ok) {  // ok is uniform across the CTA
+      ok = __syncthreads_and(mbar_wait(&mbar, phase, err, ERR_WAIT)) != 0;
+      phase ^= 1u;
+    }
+    fence_after_sync();
+    if (ok) {  // dZ1 = dH1 * GELU'(Z1): BW rows 64..127
+      float z1[64];
+      ld64(tmem + lane_base, z1);
+      ld64(tmem + lane_base + 64, v);
+#pragma unroll
+      for (int j = 0; j < NH; ++j) {
+        const float dz1 = v[j] * gelu_grad(z1[j] + sb1[j]);
+        *reinterpret_cast<uint16_t *>(BW + kmaj_off(64 + j, tid, TM)) = bf16bits(dz1);
+      }
+    }
+    fence_async_smem();
+    sync_cta();
+    if (ok && tid == 0) {  // DW += AW BW^T over the 128 batch rows of the tile
+      for (int s = 0; s < TM / 16; ++s)
+        mma(tmem + 128, smem_desc(smem_u32(AW) + 256 * s, 128, TM * 16),
+            smem_desc(smem_u32(BW) + 256 * s, 128, TM * 16), id128, (first && s == 0) ? 0u : 1u);
+      commit(&mbar);
+    }
+    if (ok) {  // ok is uniform across the CTA
+      ok = __syncthreads_and(mbar_wait(&mbar, phase, err, ERR_WAIT)) != 0;
+      phase ^= 1u;
+    }
+    first = false;
+    sync_cta();
+  }
+  // partial gradients of this CTA
+  float *out = partials + static_cast<int64_t>(blockIdx.x) * NPART;
+  if (ok && !first) {
+    float dw[64];
+    // columns 0..63 of DW: rows 0..63 -> dW2^T; row 96 -> db2
+    ld64(tmem + lane_base + 128, dw);
+    if (tid < NH) {
+#pragma unroll
+      for (int o = 0; o < NH; ++o) out[OFF_W2 + o * NH + tid] = dw[o];
+    } else if (tid == 96) {
+#pragma unroll
+      for (int o = 0; o < NH; ++o) out[OFF_B2 + o] = dw[o];
+    }
+    // columns 64..127: rows 64..87 -> dW1^T; row 96 -> db1
+    ld64(tmem + lane_base + 192, dw);
+    if (tid >= 64 && tid < 64 + NIN) {
+#pragma unroll
+      for (int o = 0; o < NH; ++o) out[OFF_W1 + o * NIN + (tid - 64)] = dw[o];
+    } else if (tid == 96) {
+#pragma unroll
+      for (int o = 0; o < NH; ++o) out[OFF_B1 + o] = dw[o];
+    }
+  } else if (tid < NH) {
+    for (int o = 0; o < NH; ++o) out[OFF_W2 + o * NH + tid] = 0.0f;
+    out[OFF_B2 + tid] = 0.0f;
+    out[OFF_B1 + tid] = 0.0f;
+    if (tid < NIN)
+      for (int o = 0; o < NH; ++o) out[OFF_W1 + o * NIN + tid] = 0.0f;
+  }
+  __syncthreads();
+  if (tid < NH) out[OFF_W3 + tid] = sdw3[tid];
+  if (tid == 0) {
+    out[OFF_B3] = sdb3;
+    out[NPARAM] = sloss;
+  }
+  sync_cta();
+  if (warp == 0) tmem_dealloc(tmem, 256);
+}
+
+// sum of the CTAs' partial gradients in a fixed order
+__global__ void k_reduce(const float *__restrict__ partials, int nblk, float *__restrict__ grad) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= NPART) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b) s += partials[static_cast<int64_t>(b) * NPART + p];
+  grad[p] = static_cast<float>(s);
+}
+
+__global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
+                       float *__restrict__ v, float lr, float b1, float b2, float eps, float c1,
+                       float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NPARAM) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.0f - b1) * gi;
+  const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+struct Mlp {
+  std::string err;
+  int device = 0;
+  float *p = nullptr, *m = nullptr, *v = nullptr, *g = nullptr, *partials = nullptr;
+  uint16_t *img = nullptr;  // w1img | w2img | w2timg
+  int *d_err = nullptr;
+  int *h_err = nullptr;
+  int sms = 0;
+  int64_t step = 0;
+  // dataset
+  uint16_t *dx = nullptr;
+  float *dt = nullptr;
+  int64_t dn = 0;
+  cudaStream_t stream = nullptr;
+};
+
+int fail(Mlp *P, int code, const std::string &msg) {
+  P->err = msg;
+  return code;
+}
+
+#define MK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return imodel::fail(P, e_ == cudaErrorMemoryAllocation ? IMODEL_SWM_ENOMEM          \
+                                                             : IMODEL_SWM_ECUDA,          \
+                          std::string(#call) + ": " + cudaGetErrorString(e_));           \
+  } while (0)
+
+Weights weights(Mlp *P) {
+  Weights W;
+  W.w1img = P->img;
+  W.w2img = P->img + NH * K1;
+  W.w2timg = P->img + NH * K1 + NH * NH;
+  W.p = P->p;
+  return W;
+}
+
+int images(Mlp *P) {
+  Weights W = weights(P);
+  k_make_images<<<(NH * NH + 255) / 256, 256, 0, P->stream>>>(
+      P->p, const_cast<uint16_t *>(W.w1img), const_cast<uint16_t *>(W.w2img),
+      const_cast<uint16_t *>(W.w2timg));
+  MK(cudaGetLastError());
+  return IMODEL_SWM_OK;
+}
+
+int check_err(Mlp *P) {
+  MK(cudaMemcpyAsync(P->h_err, P->d_err, sizeof(int), cudaMemcpyDeviceToHost, P->stream));
+  MK(cudaMemsetAsync(P->d_err, 0, sizeof(int), P->stream));
+  MK(cudaStreamSynchronize(P->stream));
+  if (*P->h_err) return fail(P, IMODEL_SWM_ECUDA, "tensor-core completion wait timed out");
+  return IMODEL_SWM_OK;
+}
+
+int run_grad(Mlp *P, const uint16_t *x, const float *t, int64_t n, int64_t batch, uint64_t seed,
+             int *nblk_out) {
+  const int64_t ntiles = (batch + TM - 1) / TM;
+  const int nblk = static_cast<int>(std::min<int64_t>(ntiles, P->sms));
+  k_mlp_train<<<nblk, TM, TRN_SMEM, P->stream>>>(weights(P), x, t, n, batch, seed,
+                                                 1.0f / static_cast<float>(batch), P->partials,
+                                                 P->d_err);
+  MK(cudaGetLastError());
+  k_reduce<<<(NPART + 255) / 256, 256, 0, P->stream>>>(P->partials, nblk, P->g);
+  MK(cudaGetLastError());
+  *nblk_out = nblk;
+  return IMODEL_SWM_OK;
+}
+
+}  // namespace
+}  // namespace imodel
+
+using imodel::Mlp;
+
+extern "C" {
+
+int imodel_mlp_create(int32_t device, void **mlp) {
+  if (!mlp) return IMODEL_SWM_EINVAL;
+  Mlp *P = new (std::nothrow) Mlp();
+  *mlp = P;
+  if (!P) return IMODEL_SWM_ENOMEM;
+  P->device = device;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return imodel::fail(P, IMODEL_SWM_ENODEV, "no CUDA device");
+  MK(cudaSetDevice(device));
+  MK(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
+  MK(cudaDeviceGetAttribute(&P->sms, cudaDevAttrMultiProcessorCount, device));
+  MK(cudaFuncSetAttribute(imodel::k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          imodel::FWD_SMEM));
+  MK(cudaFuncSetAttribute(imodel::k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          imodel::TRN_SMEM));
+  MK(cudaMalloc(&P->p, imodel::NPART * sizeof(float)));
+  MK(cudaMalloc(&P->m, imodel::NPART * sizeof(float)));
+  MK(cudaMalloc(&P->v, imodel::NPART * sizeof(float)));
+  MK(cudaMalloc(&P->g, imodel::NPART * sizeof(float)));
+  MK(cudaMalloc(&P->partials, static_cast<size_t>(P->sms) * imodel::NPART * sizeof(float)));
+  MK(cudaMalloc(&P->img, (imodel::NH * imodel::K1 + 2 * imodel::NH * imodel::NH) * 2));
+  MK(cudaMalloc(&P->d_err, sizeof(int)));
+  MK(cudaMemset(P->p, 0, imodel::NPART * sizeof(float)));
+  MK(cudaMemset(P->m, 0, imodel::NPART * sizeof(float)));
+  MK(cudaMemset(P->v, 0, imodel::NPART * sizeof(float)));
+  MK(cudaMemset(P->d_err, 0, sizeof(int)));
+  MK(cudaMallocHost(&P->h_err, sizeof(int)));
+  return IMODEL_SWM_OK;
+}
+
+int imodel_mlp_set_params(void *mlp, const float *params, int32_t n) {
+  Mlp *P = static_cast<Mlp *>(mlp);
+  if (!P || !params || n != imodel::NPARAM) return IMODEL_SWM_EINVAL;
+  MK(cudaSetDevice(P->device));
+  MK(cudaMemcpyAsync(P->p, params, n * sizeof(float), cudaMemcpyHostToDevice, P->stream));
+  MK(cudaMemsetAsync(P->m, 0, n * sizeof(float), P->stream));
+  MK(cudaMemsetAsync(P->v, 0, n * sizeof(float), P->stream));
+  P->step = 0;
+  int rc = imodel::images(P);
+  if (rc) return rc;
+  MK(cudaStreamSynchronize(P->stream));
+  return IMODEL_SWM_OK;
+}
+
+int imodel_mlp_get_params(void *mlp, float *params, int32_t n) {
+  Mlp *P = static_cast<Mlp *>(mlp);
+  if (!P || !params || n != imodel::NPARAM) return IMODEL_SWM_EINVAL;
+  MK(cudaSetDevice(P->device));
+  MK(cudaMemcpyAsync(params, P->p, n * sizeof(float), cudaMemcpyDeviceToHost, P->stream));
+  MK(cudaStreamSynchronize(P->stream));
+  return IMODEL_SWM_OK;
+}
+
+int imodel_mlp_forward(void *mlp, const uint16_t *x, int64_t n, float *y) {
+  Mlp *P = static_cast<Mlp *>(mlp);
+  if (!P || !x || !y || n <= 0) return IMODEL_SWM_EINVAL;
+  MK(cudaSetDevice(P->device));
+  uint16_t *dx = nullptr;
+  float *dy = nullptr;
+  MK(cudaMalloc(&dx, static_cast<size_t>(n) * imodel::NIN * 2));
+  cudaError_t e = cudaMalloc(&dy, static_cast<size_t>(n) * sizeof(float));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dx, x, static_cast<size_t>(n) * imodel::NIN * 2, cudaMemcpyHostToDevice,
+                        P->stream);
+  if (e == cudaSuccess) {
+    const int64_t ntiles = (n + imodel::TM - 1) / imodel::TM;
+    const int nblk = static_cast<int>(std::min<int64_t>(ntiles, 4LL * P->sms));
+    imodel::k_mlp_forward<<<nblk, imodel::TM, imodel::FWD_SMEM, P->stream>>>(imodel::weights(P), dx,
+                                                                           n, dy, P->d_err);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(y, dy, static_cast<size_t>(n) * sizeof(float), cudaMemcpyDeviceToHost,
+                        P->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
+  cudaFree(dx);
+  cudaFree(dy);
+  if (e != cudaSuccess) return imodel::fail(P, IMODEL_SWM_ECUDA, cudaGetErrorString(e));
+  return imodel::check_err(P);
+}
+
+int imodel_mlp_grad(void *mlp, const uint16_t *x, const float *t, int64_t n, uint64_t seed,
+                    int64_t batch, float *grad, double *loss) {
+  Mlp *P = static_cast<Mlp *>(mlp);
+  if (!P || !x || !t || !grad || n <= 0 || batch <= 0) return IMODEL_SWM_EINVAL;
+  MK(cudaSetDevice(P->device));
+  uint16_t *dx = nullptr;
+  float *dt = nullptr;
+  MK(cudaMalloc(&dx, static_cast<size_t>(n) * imodel::NIN * 2));
+  MK(cudaMalloc(&dt, static_cast<size_t>(n) * sizeof(float)));
+  MK(cudaMemcpyAsync(dx, x, static_cast<size_t>(n) * imodel::NIN * 2, cudaMemcpyHostToDevice,
+                     P->stream));
+  MK(cudaMemcpyAsync(dt, t, static_cast<size_t>(n) * sizeof(float), cudaMemcpyHostToDevice,
+                     P->stream));
+  int nblk = 0;
+  int rc = imodel::run_grad(P, dx, dt, n, batch, seed, &nblk);
+  std::vector<float> g(imodel::NPART);
+  if (!rc) {
+    cudaError_t e = cudaMemcpyAsync(g.data(), P->g, imodel::NPART * sizeof(float),
+                                    cudaMemcpyDeviceToHost, P->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
+    if (e != cudaSuccess) rc = imodel::fail(P, IMODEL_SWM_ECUDA, cudaGetErrorString(e));
+  }
+  cudaFree(dx);
+  cudaFree(dt);
+  if (rc) return rc;
+  rc = imodel::check_err(P);
+  if (rc) return rc;
+  std::memcpy(grad, g.data(), imodel::NPARAM * sizeof(float));
+  if (loss) *loss = static_cast<double>(g[imodel::NPARAM]) / static_cast<double>(batch);
+  return IMODEL_SWM_OK;
+}
+
+int imodel_mlp_load_dataset(void *mlp, const uint16_t *x, const float *t, int64_t n) {
+  Mlp *P = static_cast<Mlp *>(mlp);
+  if (!P || !x || !t || n <= 0) return IMODEL_SWM_EINVAL;
+  MK(cudaSetDevice(P->device));
+  if (P->dx) cudaFree(P->dx);
+  if (P->dt) cudaFree(P->dt);
+  P->dx = nullptr;
+  P->dt = nullptr;
+  P->dn = 0;
+  MK(cudaMalloc(&P->dx, static_cast<size_t>(n) * imodel::NIN * 2));
+  MK(cudaMalloc(&P->dt, static_cast<size_t>(n) * sizeof(float)));
+  MK(cudaMemcpyAsync(P->dx, x, static_cast<size_t>(n) * imodel::NIN * 2, cudaMemcpyHostToDevice,
+                     P->stream));
+  MK(cudaMemcpyAsync(P->dt, t, static_cast<size_t>(n) * sizeof(float), cudaMemcpyHostToDevice,
+                     P->stream));
+  MK(cudaStreamSynchronize(P->stream));
+  P->dn = n;
+  return IMODEL_SWM_OK;
+}
+
+int imodel_mlp_train(void *mlp, int64_t steps, int64_t batch, float lr, uint64_t seed,
+                     float *losses) {
+  Mlp *P = static_cast<Mlp *>(mlp);
+  if (!P || steps <= 0 || batch <= 0) return IMODEL_SWM_EINVAL;
+  if (!P->dn) return imodel::fail(P, IMODEL_SWM_ESTATE, "no dataset loaded");
+  MK(cudaSetDevice(P->device));
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  std::vector<float> lossbuf(static_cast<size_t>(steps), 0.0f);
+  float *dloss = nullptr;
+  MK(cudaMalloc(&dloss, static_cast<size_t>(steps) * sizeof(float)));
+  int rc = IMODEL_SWM_OK;
+  for (int64_t s = 0; s < steps && !rc; ++s) {
+    int nblk = 0;
+    rc = imodel::run_grad(P, P->dx, P->dt, P->dn, batch,
+                          imodel::splitmix(seed + static_cast<uint64_t>(P->step)), &nblk);
+    if (rc) break;
+    P->step += 1;
+    const float c1 = 1.0f - std::pow(b1, static_cast<float>(P->step));
+    const float c2 = 1.0f - std::pow(b2, static_cast<float>(P->step));
+    imodel::k_adam<<<(imodel::NPARAM + 255) / 256, 256, 0, P->stream>>>(P->p, P->g, P->m, P->v,
+                                                                        lr, b1, b2, eps, c1, c2);
+    cudaMemcpyAsync(dloss + s, P->g + imodel::NPARAM, sizeof(float), cudaMemcpyDeviceToDevice,
+                    P->stream);
+    rc = imodel::images(P);
+  }
+  if (!rc) {
+    cudaError_t e = cudaMemcpyAsync(lossbuf.data(), dloss, static_cast<size_t>(steps) * sizeof(float),
+                                    cudaMemcpyDeviceToHost, P->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
+    if (e != cudaSuccess) rc = imodel::fail(P, IMODEL_SWM_ECUDA, cudaGetErrorString(e));
+  }
+  cudaFree(dloss);
+  if (rc) return rc;
+  rc = imodel::check_err(P);
+  if (rc) return rc;
+  if (losses)
+    for (int64_t s = 0; s < steps; ++s) losses[s] = lossbuf[s] / static_cast<float>(batch);
+  return IMODEL_SWM_OK;
+}
+
+int imodel_mlp_destroy(void *mlp) {
+  Mlp *P = static_cast<Mlp *>(mlp);
+  if (!P) return IMODEL_SWM_OK;
+  if (P->stream) cudaStreamSynchronize(P->stream);
+  for (void *q : {static_cast<void *>(P->p), static_cast<void *>(P->m), static_cast<void *>(P->v),
+                  static_cast<void *>(P->g), static_cast<void *>(P->partials),
+                  static_cast<void *>(P->img), static_cast<void *>(P->d_err),
+                  static_cast<void *>(P->dx), static_cast<void *>(P->dt)})
+    if (q) cudaFree(q);
+  if (P->h_err) cudaFreeHost(P->h_err);
+  if (P->stream) cudaStreamDestroy(P->stream);
+  delete P;
+  return IMODEL_SWM_OK;
+}
+
+const char *imodel_mlp_last_error(void *mlp) {
+  Mlp *P = static_cast<Mlp *>(mlp);
+  return P ? P->err.c_str() : "NULL handle";
+}
+
+}  // extern "C"

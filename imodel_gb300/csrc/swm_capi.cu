@@ -273,6 +273,16 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
         (rc = upload(H, L.c_inva32, &M.c_inva32)) || (rc = upload(H, L.c_meta, &M.c_meta)) ||
         (rc = upload(H, L.e_vs, &M.e_vs)))
       return rc;
+    const int32_t *pk = nullptr;
+    const float *kd = nullptr;
+    const uint32_t *vs2 = nullptr;
+    if ((rc = upload(H, L.c_pk, &pk)) || (rc = upload(H, L.c_kd, &kd)) ||
+        (rc = upload(H, L.e_vs2, &vs2)))
+      return rc;
+    // cudaMalloc returns 256-byte aligned memory: safe to view as int4/float2/uint2
+    M.c_pk = reinterpret_cast<const int4 *>(pk);
+    M.c_kd = reinterpret_cast<const float2 *>(kd);
+    M.e_vs2 = reinterpret_cast<const uint2 *>(vs2);
   }
   const int32_t *cn2o = nullptr, *en2o = nullptr;
   if ((rc = upload(H, L.cell_n2o, &cn2o)) || (rc = upload(H, L.edge_n2o, &en2o))) return rc;

@@ -30,6 +30,9 @@ struct DevMesh {
   const int32_t *c_nb, *c_tr;
   const float *c_R32, *c_dg32, *c_inva32;
   const uint32_t *c_meta, *e_vs;
+  const int4 *c_pk;     // [6][nv] {edge, neighbour, triangle, kite fraction bits}
+  const float2 *c_kd;   // [6][nv] {KE weight, ttgout*d}
+  const uint2 *e_vs2;   // [ne] both cell words of an edge
 };
 
 // Launch configuration of the FP32 stage kernels, chosen by the autotuner.

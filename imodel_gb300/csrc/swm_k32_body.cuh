@@ -1,0 +1,187 @@
+// Per-entity bodies of the FP32 cell-centred TRSK stage (internal header).
+//
+// Shared by the single-run kernels (swm_k32.cu) and the ensemble kernel
+// (swm_ens.cu).  The index policy maps an entity to its slot in a state
+// array: one run stores entity i at i, an ensemble stores member m of entity
+// i at i*M + m (members fastest), so that the threads of a warp that share
+// an entity read its geometry once and the members' values contiguously.
+#pragma once
+#include "swm_common.cuh"
+
+namespace imodel {
+
+struct OneRun {
+  __device__ __forceinline__ int operator()(int i) const { return i; }
+};
+struct Member {
+  int M, m;
+  __device__ __forceinline__ int operator()(int i) const { return i * M + m; }
+};
+
+// Loads of fields that change during a run.  Separate launches see each
+// other's writes, so plain loads are fine there; inside the persistent
+// ensemble kernel another block may have rewritten the value since this SM
+// cached it, so those loads go through L2 (ld.global.cg), never through the
+// incoherent L1 / read-only path.
+struct LdPlain {
+  static __device__ __forceinline__ float ld(const float *p) { return *p; }
+};
+struct LdL2 {
+  static __device__ __forceinline__ float ld(const float *p) { return __ldcg(p); }
+};
+
+// ode_rk4 stage update (swm.f90:2647-2678) in FP32
+__device__ __forceinline__ float rk_stage32(int stage, float k, float yn, float *acc, float dt) {
+  if (stage == 0) {
+    *acc = k;
+    return yn + 0.5f * dt * k;
+  } else if (stage == 1) {
+    *acc = *acc + 2.0f * k;
+    return yn + 0.5f * dt * k;
+  } else if (stage == 2) {
+    *acc = *acc + 2.0f * k;
+    return yn + dt * k;
+  }
+  return yn + dt * (*acc + k) * (1.0f / 6.0f);
+}
+
+// q_t = (curl u / A + f) / h_t  (vort_tr + scalar_hx2tr + scalar_elem_divide)
+template <class Ix, class Ld = LdPlain>
+__device__ __forceinline__ void tri_body(const DevMesh &M, int t, Ix ix,
+                                         const float *__restrict__ hd,
+                                         const float *__restrict__ u, float *__restrict__ q_tr,
+                                         float h_ref, int pv_on, int *flags) {
+  const int nt = M.nt;
+  float eta = __ldg(&M.t_f32[t]);
+  float ht = 0.0f;
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    eta += __ldg(&M.t_circ32[s * nt + t]) * Ld::ld(u + ix(__ldg(&M.t_ed[s * nt + t])));
+    ht += __ldg(&M.t_kite32[s * nt + t]) * Ld::ld(hd + ix(__ldg(&M.t_v[s * nt + t])));
+  }
+  ht += h_ref;
+  float q = 0.0f;
+  if (pv_on) {
+    // scalar_elem_divide guard, swm_operators.f90:1604-1606
+    if (fabsf(ht) < 1.1920928955078125e-12f)
+      atomicOr(flags, 1);
+    else
+      q = eta / ht;
+  }
+  q_tr[ix(t)] = q;
+}
+
+// coriolis_ed (swm_operators.f90:1283-1308) sums, for edge e and each of its
+// two cells c, over the other edges k_j of c:
+//     F_k * (q_e + q_k)/2 * d_k * w_c(i_e, j) * ttgout_c(j) * tnrccw_c(i_e)
+// with w_c(i, j) = sum_{k=i}^{j-1} R_c(k) - 1/2 (calc_trisk_weights,
+// interpack.f90:4046-4095).  Every factor but q_e lives on cell c, so each
+// cell computes the contribution Z_c(i) of all its n edges at once from its n
+// kite fractions R_c; the edge kernel adds the two cells' Z and divides by
+// l_e.  The 10-entry stencil (40 B of indices and 40 B of weights per edge)
+// becomes n fractions per cell.
+template <int N>
+__device__ __forceinline__ void trsk_cell(const float (&G)[6], const float (&qs)[6],
+                                          const float (&R)[6], unsigned tneg, float (&Z)[6]) {
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    float c = 0.0f, acc = 0.0f;
+#pragma unroll
+    for (int s = 1; s < N; ++s) {
+      const int j = (i + s) % N;
+      c += R[(i + s - 1) % N];
+      acc += (c - 0.5f) * G[j] * (qs[i] + qs[j]);
+    }
+    const float z = 0.5f * acc;
+    Z[i] = ((tneg >> i) & 1u) ? -z : z;
+  }
+}
+
+// div F, K, Bernoulli potential, PV-flux contributions Z (cell-major
+// zflux[cell][6]) and the mass RK stage of cell i
+template <class Ix, class Ld = LdPlain>
+__device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
+                                          const float *__restrict__ hd,
+                                          const float *__restrict__ u,
+                                          const float *__restrict__ q_tr,
+                                          float *__restrict__ bern, float *__restrict__ zflux,
+                                          const float *__restrict__ yn, float *__restrict__ acc,
+                                          float *__restrict__ yout, float *__restrict__ tend,
+                                          int stage, float dt, float grav, float h_ref) {
+  const int nv = M.nv;
+  const uint32_t meta = __ldg(&M.c_meta[i]);
+  const int n = static_cast<int>(meta & 7u);
+  const unsigned tneg = meta >> 8;
+  int4 pk[6];
+  float2 kd[6];
+  // all slot records first (unused pentagon slots repeat slot 0 with zero
+  // weights), so that every load is in flight before the gathers
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    pk[j] = __ldg(&M.c_pk[j * nv + i]);
+    kd[j] = __ldg(&M.c_kd[j * nv + i]);
+  }
+  const float hi = Ld::ld(hd + ix(i));
+  float ue[6], hn[6], qt[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    ue[j] = Ld::ld(u + ix(pk[j].x));
+    hn[j] = Ld::ld(hd + ix(pk[j].y));
+    qt[j] = Ld::ld(q_tr + ix(pk[j].z));
+  }
+  float G[6], qs[6], R[6];
+  float div = 0.0f, ke = 0.0f;
+  const float qlast = n == 6 ? qt[5] : (n == 5 ? qt[4] : (n == 4 ? qt[3] : qt[2]));
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    // F_e = u_e h_e, h_e the two-cell average (scalar_hx2ed)
+    const float F = ue[j] * (h_ref + 0.5f * (hi + hn[j]));
+    G[j] = F * kd[j].y;
+    // q_e: edge j lies between triangles j-1 and j (scalar_tr2ed)
+    qs[j] = 0.5f * ((j == 0 ? qlast : qt[j - 1]) + qt[j]);
+    R[j] = __int_as_float(pk[j].w);
+    div += G[j];
+    ke += kd[j].x * (ue[j] * ue[j]);
+  }
+  bern[ix(i)] = grav * (hi + __ldg(&M.c_bt32[i])) + ke;
+  float Z[6];
+  if (n == 6)
+    trsk_cell<6>(G, qs, R, tneg, Z);
+  else if (n == 5)
+    trsk_cell<5>(G, qs, R, tneg, Z);
+  else if (n == 4)
+    trsk_cell<4>(G, qs, R, tneg, Z);
+  else
+    trsk_cell<3>(G, qs, R, tneg, Z);
+#pragma unroll
+  for (int j = 0; j < 6; ++j)
+    if (j < n) zflux[ix(6 * i + j)] = Z[j];
+  const float masseq = -div * __ldg(&M.c_inva32[i]);
+  if (stage < 0)
+    tend[ix(i)] = masseq;
+  else
+    yout[ix(i)] = rk_stage32(stage, masseq, Ld::ld(yn + ix(i)), acc + ix(i), dt);
+}
+
+// -grad B - (Z_c1 + Z_c2) / l_e and the momentum RK stage of edge e
+template <class Ix, class Ld = LdPlain>
+__device__ __forceinline__ void edge_body(const DevMesh &M, int e, Ix ix, uint2 w,
+                                          const float *__restrict__ bern,
+                                          const float *__restrict__ zflux,
+                                          const float *__restrict__ yn, float *__restrict__ acc,
+                                          float *__restrict__ yout, float *__restrict__ tend,
+                                          int stage, float dt, int mom_on, float erad) {
+  const int c1 = static_cast<int>(w.x & 0x0FFFFFFFu), c2 = static_cast<int>(w.y & 0x0FFFFFFFu);
+  const int s1 = static_cast<int>(w.x >> 28), s2 = static_cast<int>(w.y >> 28);
+  const float g = __ldg(&M.e_grad32[e]);  // 1 / (l_e a)
+  const float grad = (Ld::ld(bern + ix(c2)) - Ld::ld(bern + ix(c1))) * g;
+  const float q = (Ld::ld(zflux + ix(6 * c1 + s1)) + Ld::ld(zflux + ix(6 * c2 + s2))) * (g * erad);
+  float momeq = -grad - q;
+  if (!mom_on) momeq = 0.0f;
+  if (stage < 0)
+    tend[ix(e)] = momeq;
+  else
+    yout[ix(e)] = rk_stage32(stage, momeq, Ld::ld(yn + ix(e)), acc + ix(e), dt);
+}
+
+}  // namespace imodel

@@ -255,6 +255,31 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
     L.e_nst[i] = static_cast<int8_t>(ns);
   }
 
+  // packed cell slots and edge cell words for vector loads
+  L.c_pk.assign(kMaxNb * NV * 4, 0);
+  L.c_kd.assign(kMaxNb * NV * 2, 0.0f);
+  for (int i = 0; i < nv; ++i) {
+    const int n = L.c_nnb[i];
+    for (int j = 0; j < kMaxNb; ++j) {
+      const int src = j < n ? j : 0;  // padding repeats slot 0 ...
+      const size_t q = (static_cast<size_t>(j) * NV + i);
+      L.c_pk[4 * q + 0] = L.c_ed[src * NV + i];
+      L.c_pk[4 * q + 1] = L.c_nb[src * NV + i];
+      L.c_pk[4 * q + 2] = L.c_tr[src * NV + i];
+      float r = j < n ? L.c_R32[src * NV + i] : 0.0f;  // ... with zero weights
+      int32_t rb;
+      std::memcpy(&rb, &r, sizeof(rb));
+      L.c_pk[4 * q + 3] = rb;
+      L.c_kd[2 * q + 0] = j < n ? L.c_kew32[src * NV + i] : 0.0f;
+      L.c_kd[2 * q + 1] = j < n ? L.c_dg32[src * NV + i] : 0.0f;
+    }
+  }
+  L.e_vs2.resize(2 * NE);
+  for (size_t e = 0; e < NE; ++e) {
+    L.e_vs2[2 * e] = L.e_vs[e];
+    L.e_vs2[2 * e + 1] = L.e_vs[NE + e];
+  }
+
   // --- triangles ------------------------------------------------------
   L.t_ed.resize(3 * NT);
   L.t_v.resize(3 * NT);

@@ -52,6 +52,12 @@ struct Layout {
   std::vector<float> c_inva32;               // [nv] 1/(A*erad)
   std::vector<uint32_t> c_meta;              // [nv] nnb | tnrccw<0 bits << 8
   std::vector<uint32_t> e_vs;                // [2][ne] cell | slot << 28
+  // the same per-slot data packed for 16-byte loads, slot-major [6][nv]:
+  // {edge, neighbour, triangle, kite fraction bits} and {KE weight,
+  // ttgout*d}; unused slots of pentagons repeat slot 0 with zero weights
+  std::vector<int32_t> c_pk;                 // [6][nv][4]
+  std::vector<float> c_kd;                   // [6][nv][2]
+  std::vector<uint32_t> e_vs2;               // [ne][2] both cell words of an edge
 
   // edges [ne] and [2][ne]
   std::vector<int32_t> e_v;                  // [2][ne] cells (ed%v = edhx%sh)

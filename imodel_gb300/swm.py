@@ -256,6 +256,79 @@ class SWM:
         return self.lib.imodel_swm_stream(self._handle) or 0
 
 
+class Ensemble:
+    """Many FP32 instances on up to 8 grids, advanced by one persistent
+    launch (see imodel_swm_ensemble_* in include/imodel_swm.h)."""
+
+    def __init__(self, grids, members, testcase: int = 2, device: int = 0):
+        self.grids = list(grids)
+        self.members = [int(m) for m in members]
+        self.lib = _capi.swm_lib()
+        structs = (_capi.Mesh * len(self.grids))()
+        for k, g in enumerate(self.grids):
+            structs[k] = g.c_struct()
+        self._structs = structs
+        mem = np.ascontiguousarray(self.members, dtype=np.int32)
+        self._handle = ctypes.c_void_p()
+        rc = self.lib.imodel_swm_ensemble_create(structs, len(self.grids), _capi.as_i32p(mem),
+                                                 testcase, device, ctypes.byref(self._handle))
+        if rc != 0:
+            msg = self._last_error()
+            self.close()
+            raise SWMError(rc, msg)
+
+    def _last_error(self):
+        if not self._handle:
+            return ""
+        s = self.lib.imodel_swm_ensemble_last_error(self._handle)
+        return s.decode() if s else ""
+
+    def _check(self, rc):
+        if rc != 0:
+            raise SWMError(rc, self._last_error())
+
+    def close(self):
+        if getattr(self, "_handle", None):
+            self.lib.imodel_swm_ensemble_destroy(self._handle)
+            self._handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, grid: int, member: int, h, u):
+        h = np.ascontiguousarray(h, dtype=np.float64)
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        self._check(self.lib.imodel_swm_ensemble_set_state(self._handle, grid, member,
+                                                           _capi.as_f64p(h), _capi.as_f64p(u)))
+
+    def get_state(self, grid: int, member: int):
+        g = self.grids[grid]
+        h = np.empty(g.nv)
+        u = np.empty(g.ne)
+        self._check(self.lib.imodel_swm_ensemble_get_state(self._handle, grid, member,
+                                                           _capi.as_f64p(h), _capi.as_f64p(u)))
+        return h, u
+
+    def advance(self, dt, nsteps):
+        dt = np.ascontiguousarray(dt, dtype=np.float64)
+        ns = np.ascontiguousarray(nsteps, dtype=np.int32)
+        self._check(self.lib.imodel_swm_ensemble_advance(self._handle, _capi.as_f64p(dt),
+                                                         _capi.as_i32p(ns)))
+
+    def tune(self, dt, nsteps: int = 3) -> dict:
+        dt = np.ascontiguousarray(dt, dtype=np.float64)
+        c = np.zeros(2, dtype=np.int32)
+        self._check(self.lib.imodel_swm_ensemble_tune(self._handle, _capi.as_f64p(dt), nsteps,
+                                                      _capi.as_i32p(c)))
+        return {"block": int(c[0]), "blocks_per_sm": int(c[1])}
+
+    def stream(self) -> int:
+        return self.lib.imodel_swm_ensemble_stream(self._handle) or 0
+
+
 def ntime_for(maxtime_days: float, dt: float) -> int:
     """ntime = ceiling(maxtime/dt) (swm_data.f90:573)."""
     return int(math.ceil(maxtime_days * DAY2SEC / dt))

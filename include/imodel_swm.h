@@ -187,6 +187,31 @@ const char *imodel_swm_main_kernel(void *handle);
 /* The CUDA stream (cudaStream_t) all work of the handle is issued on. */
 void *imodel_swm_stream(void *handle);
 
+/* ---- ensembles ----------------------------------------------------------- *
+ * Many instances of the FP32 step on up to 8 grids (e.g. 64 members on one
+ * level and 16 on another) advanced together by ONE persistent cooperative
+ * launch.  Members of a grid share its geometry; their states are
+ * interleaved member-fastest.  Each grid keeps its own dt and step count; the
+ * grids' steps are spread evenly over the launch.  Member results equal the
+ * single-run FP32 path (variant 1) bit for bit.  No counterpart in the
+ * reference, which runs one instance per process. */
+int imodel_swm_ensemble_create(const imodel_swm_mesh *meshes, int32_t ngrids,
+                               const int32_t *members, int32_t testcase, int32_t device,
+                               void **ens);
+int imodel_swm_ensemble_set_state(void *ens, int32_t grid, int32_t member, const double *h,
+                                  const double *u);
+int imodel_swm_ensemble_get_state(void *ens, int32_t grid, int32_t member, double *h,
+                                  double *u);
+/* dt[ngrids] seconds and nsteps[ngrids] RK4 steps per grid, one launch. */
+int imodel_swm_ensemble_advance(void *ens, const double *dt, const int32_t *nsteps);
+/* Autotuner of the persistent launch: times nsteps steps per grid for each
+ * block size and blocks-per-SM count, keeps the fastest, restores the state.
+ * choice = {block size, blocks per SM}. */
+int imodel_swm_ensemble_tune(void *ens, const double *dt, int32_t nsteps, int32_t choice[2]);
+int imodel_swm_ensemble_destroy(void *ens);
+const char *imodel_swm_ensemble_last_error(void *ens);
+void *imodel_swm_ensemble_stream(void *ens);
+
 /* Area-weighted sums of one field with no device allocation.  No counterpart
  * in the reference: it is the compensated reduction behind
  * imodel_swm_diagnostics (sumf_areas / sumfsq_areas) for callers that cannot

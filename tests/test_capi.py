@@ -23,6 +23,10 @@ def test_header_lists_match_python_mirror():
     assert _declared("imodel_swm.h") == sorted(_capi.SWM_SYMBOLS)
 
 
+def test_mlp_header_matches_python_mirror():
+    assert _declared("imodel_mlp.h") == sorted(_capi.MLP_SYMBOLS)
+
+
 def test_mesh_library_exports():
     lib = _capi.mesh_lib()
     for name in _declared("imodel_mesh.h"):
@@ -34,7 +38,7 @@ def test_swm_library_exports():
     if not os.path.exists(path):
         pytest.skip("CUDA library not built (no nvcc)")
     lib = ctypes.CDLL(path)
-    for name in _declared("imodel_swm.h"):
+    for name in _declared("imodel_swm.h") + _declared("imodel_mlp.h"):
         assert hasattr(lib, name), name
 
 
