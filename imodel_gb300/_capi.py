@@ -201,9 +201,9 @@ def swm_lib() -> ctypes.CDLL:
         lib.imodel_mlp_set_params.argtypes = [vp, f32p, ctypes.c_int32]
         lib.imodel_mlp_get_params.argtypes = [vp, f32p, ctypes.c_int32]
         lib.imodel_mlp_forward.argtypes = [vp, u16p, ctypes.c_int64, f32p]
-        lib.imodel_mlp_grad.argtypes = [vp, u16p, f32p, ctypes.c_int64, ctypes.c_uint64,
+        lib.imodel_mlp_grad.argtypes = [vp, u16p, f32p, f32p, ctypes.c_int64, ctypes.c_uint64,
                                         ctypes.c_int64, f32p, ctypes.POINTER(ctypes.c_double)]
-        lib.imodel_mlp_load_dataset.argtypes = [vp, u16p, f32p, ctypes.c_int64]
+        lib.imodel_mlp_load_dataset.argtypes = [vp, u16p, f32p, f32p, ctypes.c_int64]
         lib.imodel_mlp_train.argtypes = [vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_float,
                                          ctypes.c_uint64, f32p]
         lib.imodel_mlp_destroy.argtypes = [vp]

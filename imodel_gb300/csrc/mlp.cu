@@ -32,6 +32,7 @@
 
 #include "imodel_mlp.h"
 #include "imodel_swm.h"
+#include "swm_common.cuh"
 #include "tc05.cuh"
 
 namespace imodel {
@@ -137,8 +138,34 @@ __global__ void k_make_images(const float *__restrict__ p, uint16_t *w1img, uint
 // dynamic shared memory: A1 8 KiB | B1 4 KiB | A2 16 KiB | B2 8 KiB
 constexpr int FWD_SMEM = 8192 + 4096 + 16384 + 8192;
 
-__global__ void __launch_bounds__(TM) k_mlp_forward(Weights W, const uint16_t *__restrict__ x,
-                                                     int64_t n, float *__restrict__ y, int *err) {
+// Inputs: rows of a BF16 array x[n][24]; output y[row].
+struct RowsIn {
+  const uint16_t *x;
+  struct Ctx {};
+  __device__ __forceinline__ Ctx stage(int64_t row, bool live, uint4 (&c)[4]) const {
+    c[0] = c[1] = c[2] = c[3] = make_uint4(0, 0, 0, 0);
+    if (live) {
+      const uint4 *src = reinterpret_cast<const uint4 *>(x + row * NIN);
+      c[0] = src[0];
+      c[1] = src[1];
+      c[2] = src[2];
+    }
+    return Ctx{};
+  }
+};
+struct RowsOut {
+  float *y;
+  template <class Ctx>
+  __device__ __forceinline__ void write(int64_t row, float v, const Ctx &) const {
+    y[row] = v;
+  }
+};
+
+// Forward over n rows in tiles of 128: Src stages a row's 24 BF16 inputs (as
+// four 16-byte chunks, the fourth zero), Dst consumes the network output.
+template <class Src, class Dst>
+__global__ void __launch_bounds__(TM) k_mlp_apply(Weights W, int64_t n, Src src, Dst dst,
+                                                   int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t *A1 = smem, *B1 = smem + 8192, *A2 = B1 + 4096, *B2 = A2 + 16384;
   __shared__ uint64_t mbar;
@@ -166,17 +193,11 @@ __global__ void __launch_bounds__(TM) k_mlp_forward(Weights W, const uint16_t *_
   bool ok = true;
   for (int64_t tile = blockIdx.x; ok && tile * TM < n; tile += gridDim.x) {
     const int64_t row = tile * TM + tid;
-    uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0, c2 = c0;
-    if (row < n) {
-      const uint4 *src = reinterpret_cast<const uint4 *>(x + row * NIN);
-      c0 = src[0];
-      c1 = src[1];
-      c2 = src[2];
-    }
-    *reinterpret_cast<uint4 *>(A1 + kmaj_off(tid, 0, K1)) = c0;
-    *reinterpret_cast<uint4 *>(A1 + kmaj_off(tid, 8, K1)) = c1;
-    *reinterpret_cast<uint4 *>(A1 + kmaj_off(tid, 16, K1)) = c2;
-    *reinterpret_cast<uint4 *>(A1 + kmaj_off(tid, 24, K1)) = make_uint4(0, 0, 0, 0);
+    const bool live = row < n;
+    uint4 c[4];
+    const typename Src::Ctx ctx = src.stage(row, live, c);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) *reinterpret_cast<uint4 *>(A1 + kmaj_off(tid, 8 * q, K1)) = c[q];
     fence_async_smem();
     sync_cta();
     if (tid == 0) {
@@ -213,13 +234,68 @@ __global__ void __launch_bounds__(TM) k_mlp_forward(Weights W, const uint16_t *_
       float acc = b3;
 #pragma unroll
       for (int j = 0; j < NH; ++j) acc += gelu(v[j] + sb2[j]) * sw3[j];
-      if (row < n) y[row] = acc;
+      if (live) dst.write(row, acc, ctx);
     }
     sync_cta();
   }
   sync_cta();
   if (warp == 0) tmem_dealloc(tmem, 128);
 }
+
+// ---- the learned correction inside the shallow-water step -------------------
+// Inputs of edge e: 10 stencil normal velocities times their TRSK signs,
+// divided by their RMS sigma, and 14 geometry numbers (BF16, 32 B per edge).
+struct EdgeIn {
+  const int32_t *lst;   // [10][ne] sign * (edge + 1), 0 = empty slot
+  const uint16_t *geo;  // [ne][16]
+  const float *u;
+  int64_t ne;
+  struct Ctx {
+    float sigma;
+  };
+  __device__ __forceinline__ Ctx stage(int64_t e, bool live, uint4 (&c)[4]) const {
+    float uv[10];
+    float ss = 0.0f;
+#pragma unroll
+    for (int s = 0; s < 10; ++s) {
+      const int v = live ? __ldg(&lst[s * ne + e]) : 0;
+      const int k = (v < 0 ? -v : v) - 1;
+      const float uk = v != 0 ? u[k] : 0.0f;
+      uv[s] = v < 0 ? -uk : uk;
+      ss += uv[s] * uv[s];
+    }
+    const float sigma = sqrtf(ss * 0.1f) + 1e-30f;
+    const float inv = 1.0f / sigma;
+    uint4 g0 = make_uint4(0, 0, 0, 0), g1 = g0;
+    if (live) {
+      const uint4 *gp = reinterpret_cast<const uint4 *>(geo + e * 16);
+      g0 = __ldg(gp);
+      g1 = __ldg(gp + 1);
+    }
+    c[0] = make_uint4(pack2(uv[0] * inv, uv[1] * inv), pack2(uv[2] * inv, uv[3] * inv),
+                      pack2(uv[4] * inv, uv[5] * inv), pack2(uv[6] * inv, uv[7] * inv));
+    c[1] = make_uint4(pack2(uv[8] * inv, uv[9] * inv), g0.x, g0.y, g0.z);
+    c[2] = make_uint4(g0.w, g1.x, g1.y, g1.z);
+    c[3] = make_uint4(0, 0, 0, 0);
+    return Ctx{sigma};
+  }
+};
+// corr[e] = q_e h_e sigma y: the PV flux of the predicted tangential error
+struct CorrOut {
+  const int32_t *e_sh;  // [2][ne] triangles
+  const uint2 *e_vs2;   // cell words
+  const float *q_tr, *hd;
+  float h_ref;
+  float *corr;
+  int64_t ne;
+  template <class Ctx>
+  __device__ __forceinline__ void write(int64_t e, float y, const Ctx &ctx) const {
+    const float q = 0.5f * (q_tr[e_sh[e]] + q_tr[e_sh[ne + e]]);
+    const uint2 w = e_vs2[e];
+    const float h = h_ref + 0.5f * (hd[w.x & 0x0FFFFFFFu] + hd[w.y & 0x0FFFFFFFu]);
+    corr[e] = q * h * ctx.sigma * y;
+  }
+};
 
 // ---- fused forward + backward over a batch ---------------------------------
 // dynamic shared memory: A1 8K | B1 4K | A2 16K | B2 8K | B2T 8K | A3 16K |
@@ -228,6 +304,7 @@ constexpr int TRN_SMEM = 8192 + 4096 + 16384 + 8192 + 8192 + 16384 + 32768 + 327
 
 __global__ void __launch_bounds__(TM, 1)
     k_mlp_train(Weights W, const uint16_t *__restrict__ x, const float *__restrict__ t,
+                const float *__restrict__ wts,
                 int64_t n, int64_t batch, uint64_t seed, float inv_batch,
                 float *__restrict__ partials, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -287,6 +364,7 @@ __global__ void __launch_bounds__(TM, 1)
       c[2] = src[2];
     }
     const float target = live ? t[row] : 0.0f;
+    const float wt = live ? (wts ? wts[row] : 1.0f) : 0.0f;  // sample weight
 #pragma unroll
     for (int q = 0; q < 3; ++q) *reinterpret_cast<uint4 *>(A1 + kmaj_off(tid, 8 * q, K1)) = c[q];
     *reinterpret_cast<uint4 *>(A1 + kmaj_off(tid, 24, K1)) = make_uint4(0, 0, 0, 0);
@@ -338,8 +416,8 @@ __global__ void __launch_bounds__(TM, 1)
         yv += h2[j] * sw3[j];
       }
       const float r = live ? yv - target : 0.0f;
-      const float dy = 2.0f * r * inv_batch;
-      float ls = warp_sum(r * r), sdy = warp_sum(dy);
+      const float dy = 2.0f * wt * r * inv_batch;
+      float ls = warp_sum(wt * r * r), sdy = warp_sum(dy);
       if (lane == 0) {
         atomicAdd(&sloss, ls);
         atomicAdd(&sdb3, sdy);
@@ -466,6 +544,7 @@ struct Mlp {
   // dataset
   uint16_t *dx = nullptr;
   float *dt = nullptr;
+  float *dw = nullptr;  // sample weights or NULL
   int64_t dn = 0;
   cudaStream_t stream = nullptr;
 };
@@ -510,11 +589,12 @@ int check_err(Mlp *P) {
   return IMODEL_SWM_OK;
 }
 
-int run_grad(Mlp *P, const uint16_t *x, const float *t, int64_t n, int64_t batch, uint64_t seed,
+int run_grad(Mlp *P, const uint16_t *x, const float *t, const float *w, int64_t n, int64_t batch,
+             uint64_t seed,
              int *nblk_out) {
   const int64_t ntiles = (batch + TM - 1) / TM;
   const int nblk = static_cast<int>(std::min<int64_t>(ntiles, P->sms));
-  k_mlp_train<<<nblk, TM, TRN_SMEM, P->stream>>>(weights(P), x, t, n, batch, seed,
+  k_mlp_train<<<nblk, TM, TRN_SMEM, P->stream>>>(weights(P), x, t, w, n, batch, seed,
                                                  1.0f / static_cast<float>(batch), P->partials,
                                                  P->d_err);
   MK(cudaGetLastError());
@@ -525,6 +605,38 @@ int run_grad(Mlp *P, const uint16_t *x, const float *t, int64_t n, int64_t batch
 }
 
 }  // namespace
+
+// ---- entry points used by the shallow-water handle (swm_capi.cu) -----------
+int learned_prepare(const float *params_host, LearnedDev *L, cudaStream_t s) {
+  if (cudaMalloc(&L->p, NPART * sizeof(float)) != cudaSuccess) return IMODEL_SWM_ENOMEM;
+  if (cudaMalloc(&L->img, (NH * K1 + 2 * NH * NH) * 2) != cudaSuccess) return IMODEL_SWM_ENOMEM;
+  if (cudaMemcpyAsync(L->p, params_host, NPARAM * sizeof(float), cudaMemcpyHostToDevice, s) !=
+      cudaSuccess)
+    return IMODEL_SWM_ECUDA;
+  k_make_images<<<(NH * NH + 255) / 256, 256, 0, s>>>(L->p, L->img, L->img + NH * K1,
+                                                      L->img + NH * K1 + NH * NH);
+  if (cudaGetLastError() != cudaSuccess) return IMODEL_SWM_ECUDA;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&L->sms, cudaDevAttrMultiProcessorCount, dev);
+  return IMODEL_SWM_OK;
+}
+
+void learned_launch(const DevMesh &M, const LearnedDev &L, const float *hd, const float *u,
+                    const float *q_tr, float h_ref, int *err, cudaStream_t s) {
+  Weights W;
+  W.w1img = L.img;
+  W.w2img = L.img + NH * K1;
+  W.w2timg = L.img + NH * K1 + NH * NH;
+  W.p = L.p;
+  const int64_t ne = M.ne;
+  const int64_t ntiles = (ne + TM - 1) / TM;
+  const int nblk = static_cast<int>(std::min<int64_t>(ntiles, 4LL * (L.sms > 0 ? L.sms : 1)));
+  EdgeIn in{L.lst, L.geo, u, ne};
+  CorrOut out{M.e_sh, M.e_vs2, q_tr, hd, h_ref, L.corr, ne};
+  k_mlp_apply<<<nblk, TM, FWD_SMEM, s>>>(W, ne, in, out, err);
+}
+
 }  // namespace imodel
 
 using imodel::Mlp;
@@ -543,8 +655,6 @@ int imodel_mlp_create(int32_t device, void **mlp) {
   MK(cudaSetDevice(device));
   MK(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
   MK(cudaDeviceGetAttribute(&P->sms, cudaDevAttrMultiProcessorCount, device));
-  MK(cudaFuncSetAttribute(imodel::k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                          imodel::FWD_SMEM));
   MK(cudaFuncSetAttribute(imodel::k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           imodel::TRN_SMEM));
   MK(cudaMalloc(&P->p, imodel::NPART * sizeof(float)));
@@ -599,8 +709,8 @@ int imodel_mlp_forward(void *mlp, const uint16_t *x, int64_t n, float *y) {
   if (e == cudaSuccess) {
     const int64_t ntiles = (n + imodel::TM - 1) / imodel::TM;
     const int nblk = static_cast<int>(std::min<int64_t>(ntiles, 4LL * P->sms));
-    imodel::k_mlp_forward<<<nblk, imodel::TM, imodel::FWD_SMEM, P->stream>>>(imodel::weights(P), dx,
-                                                                           n, dy, P->d_err);
+    imodel::k_mlp_apply<<<nblk, imodel::TM, imodel::FWD_SMEM, P->stream>>>(
+        imodel::weights(P), n, imodel::RowsIn{dx}, imodel::RowsOut{dy}, P->d_err);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess)
@@ -613,7 +723,8 @@ int imodel_mlp_forward(void *mlp, const uint16_t *x, int64_t n, float *y) {
   return imodel::check_err(P);
 }
 
-int imodel_mlp_grad(void *mlp, const uint16_t *x, const float *t, int64_t n, uint64_t seed,
+int imodel_mlp_grad(void *mlp, const uint16_t *x, const float *t, const float *w, int64_t n,
+                    uint64_t seed,
                     int64_t batch, float *grad, double *loss) {
   Mlp *P = static_cast<Mlp *>(mlp);
   if (!P || !x || !t || !grad || n <= 0 || batch <= 0) return IMODEL_SWM_EINVAL;
@@ -622,12 +733,17 @@ int imodel_mlp_grad(void *mlp, const uint16_t *x, const float *t, int64_t n, uin
   float *dt = nullptr;
   MK(cudaMalloc(&dx, static_cast<size_t>(n) * imodel::NIN * 2));
   MK(cudaMalloc(&dt, static_cast<size_t>(n) * sizeof(float)));
+  float *dwt = nullptr;
+  if (w) MK(cudaMalloc(&dwt, static_cast<size_t>(n) * sizeof(float)));
+  if (w)
+    MK(cudaMemcpyAsync(dwt, w, static_cast<size_t>(n) * sizeof(float), cudaMemcpyHostToDevice,
+                       P->stream));
   MK(cudaMemcpyAsync(dx, x, static_cast<size_t>(n) * imodel::NIN * 2, cudaMemcpyHostToDevice,
                      P->stream));
   MK(cudaMemcpyAsync(dt, t, static_cast<size_t>(n) * sizeof(float), cudaMemcpyHostToDevice,
                      P->stream));
   int nblk = 0;
-  int rc = imodel::run_grad(P, dx, dt, n, batch, seed, &nblk);
+  int rc = imodel::run_grad(P, dx, dt, dwt, n, batch, seed, &nblk);
   std::vector<float> g(imodel::NPART);
   if (!rc) {
     cudaError_t e = cudaMemcpyAsync(g.data(), P->g, imodel::NPART * sizeof(float),
@@ -637,6 +753,7 @@ int imodel_mlp_grad(void *mlp, const uint16_t *x, const float *t, int64_t n, uin
   }
   cudaFree(dx);
   cudaFree(dt);
+  if (dwt) cudaFree(dwt);
   if (rc) return rc;
   rc = imodel::check_err(P);
   if (rc) return rc;
@@ -645,17 +762,25 @@ int imodel_mlp_grad(void *mlp, const uint16_t *x, const float *t, int64_t n, uin
   return IMODEL_SWM_OK;
 }
 
-int imodel_mlp_load_dataset(void *mlp, const uint16_t *x, const float *t, int64_t n) {
+int imodel_mlp_load_dataset(void *mlp, const uint16_t *x, const float *t, const float *w,
+                            int64_t n) {
   Mlp *P = static_cast<Mlp *>(mlp);
   if (!P || !x || !t || n <= 0) return IMODEL_SWM_EINVAL;
   MK(cudaSetDevice(P->device));
   if (P->dx) cudaFree(P->dx);
   if (P->dt) cudaFree(P->dt);
+  if (P->dw) cudaFree(P->dw);
+  P->dw = nullptr;
   P->dx = nullptr;
   P->dt = nullptr;
   P->dn = 0;
   MK(cudaMalloc(&P->dx, static_cast<size_t>(n) * imodel::NIN * 2));
   MK(cudaMalloc(&P->dt, static_cast<size_t>(n) * sizeof(float)));
+  if (w) {
+    MK(cudaMalloc(&P->dw, static_cast<size_t>(n) * sizeof(float)));
+    MK(cudaMemcpyAsync(P->dw, w, static_cast<size_t>(n) * sizeof(float), cudaMemcpyHostToDevice,
+                       P->stream));
+  }
   MK(cudaMemcpyAsync(P->dx, x, static_cast<size_t>(n) * imodel::NIN * 2, cudaMemcpyHostToDevice,
                      P->stream));
   MK(cudaMemcpyAsync(P->dt, t, static_cast<size_t>(n) * sizeof(float), cudaMemcpyHostToDevice,
@@ -678,7 +803,7 @@ int imodel_mlp_train(void *mlp, int64_t steps, int64_t batch, float lr, uint64_t
   int rc = IMODEL_SWM_OK;
   for (int64_t s = 0; s < steps && !rc; ++s) {
     int nblk = 0;
-    rc = imodel::run_grad(P, P->dx, P->dt, P->dn, batch,
+    rc = imodel::run_grad(P, P->dx, P->dt, P->dw, P->dn, batch,
                           imodel::splitmix(seed + static_cast<uint64_t>(P->step)), &nblk);
     if (rc) break;
     P->step += 1;
@@ -712,7 +837,8 @@ int imodel_mlp_destroy(void *mlp) {
   for (void *q : {static_cast<void *>(P->p), static_cast<void *>(P->m), static_cast<void *>(P->v),
                   static_cast<void *>(P->g), static_cast<void *>(P->partials),
                   static_cast<void *>(P->img), static_cast<void *>(P->d_err),
-                  static_cast<void *>(P->dx), static_cast<void *>(P->dt)})
+                  static_cast<void *>(P->dx), static_cast<void *>(P->dt),
+                  static_cast<void *>(P->dw)})
     if (q) cudaFree(q);
   if (P->h_err) cudaFreeHost(P->h_err);
   if (P->stream) cudaStreamDestroy(P->stream);

@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "imodel_mlp.h"
 #include "imodel_swm.h"
 #include "swm_common.cuh"
 #include "swm_layout.h"
@@ -44,6 +45,13 @@ struct Handle {
   cudaGraphExec_t graph = nullptr;
   double graph_dt = 0.0;
   bool state_set = false;
+  // learned TRSK correction (FP32, cell-centred variant)
+  LearnedDev learned{};
+  bool learned_on = false;      // requested at create
+  bool learned_active = false;  // still applied (the drift guard may switch it off)
+  double drift_bound = 1e-3;
+  double te_ref = 0.0;
+  bool te_ref_set = false;
 };
 
 #define CK(call)                                                                  \
@@ -143,7 +151,11 @@ int ensure_graph(Handle *H, double dt) {
 // host FP64 arrays (reference order) -> device state yn, plus h_ed and the
 // "last stage input" ya, as after the reference's initial tendency call
 // (swm.f90:214)
-int load_state(Handle *H, const double *h, const double *u) {
+int learned_guard(Handle *H);
+
+// new_run: the state starts a new run (set_state), so the learned correction
+// is switched back on and its energy reference is taken again
+int load_state(Handle *H, const double *h, const double *u, bool new_run) {
   if (H->precision == IMODEL_SWM_FP32 && !H->href_fixed) {
     double s = 0.0, a = 0.0;
     for (int i = 0; i < H->nv; ++i) {
@@ -172,6 +184,18 @@ int load_state(Handle *H, const double *h, const double *u) {
   }
   CK(cudaGetLastError());
   H->state_set = true;
+  if (H->learned_on && (new_run || !H->te_ref_set)) {
+    if (!H->learned_active || H->W32.learned == nullptr) {
+      H->learned_active = true;
+      H->W32.learned = &H->learned;
+      if (H->graph) {
+        cudaGraphExecDestroy(H->graph);
+        H->graph = nullptr;
+      }
+    }
+    H->te_ref_set = false;
+    return learned_guard(H);
+  }
   return IMODEL_SWM_OK;
 }
 
@@ -204,6 +228,50 @@ int check_flags(Handle *H) {
   return IMODEL_SWM_OK;
 }
 
+// total energy of the current state (compensated FP64 integral)
+int total_energy(Handle *H, double *te) {
+  if (H->precision == IMODEL_SWM_FP64) {
+    auto &W = H->W64;
+    launch_diag<double>(H->M, W, W.yn_h, W.yn_u, W.ya_h, W.ya_u, H->d_scratch, H->d_result,
+                        H->stream);
+  } else {
+    auto &W = H->W32;
+    launch_diag<float>(H->M, W, W.yn_h, W.yn_u, W.ya_h, W.ya_u, H->d_scratch, H->d_result,
+                       H->stream);
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(H->h_result, H->d_result, sizeof(double) * kDiagQ, cudaMemcpyDeviceToHost,
+                     H->stream));
+  CK(cudaStreamSynchronize(H->stream));
+  *te = H->h_result[Q_PE] + H->h_result[Q_KE];
+  return IMODEL_SWM_OK;
+}
+
+// Fallback of the learned correction: once the relative drift of the total
+// energy since the state was set exceeds the bound, the plain TRSK scheme
+// takes over for the rest of the run.
+int learned_guard(Handle *H) {
+  if (!H->learned_active) return IMODEL_SWM_OK;
+  double te = 0.0;
+  int rc = total_energy(H, &te);
+  if (rc) return rc;
+  if (!H->te_ref_set) {
+    H->te_ref = te;
+    H->te_ref_set = true;
+    return IMODEL_SWM_OK;
+  }
+  const double drift = std::fabs(te - H->te_ref) / std::fabs(H->te_ref);
+  if (!(drift <= H->drift_bound)) {
+    H->learned_active = false;
+    H->W32.learned = nullptr;
+    if (H->graph) {
+      cudaGraphExecDestroy(H->graph);
+      H->graph = nullptr;
+    }
+  }
+  return IMODEL_SWM_OK;
+}
+
 int advance(Handle *H, double dt, int nsteps) {
   if (!H->state_set) return set_error(H, IMODEL_SWM_ESTATE, "no state set");
   if (nsteps < 0 || !(std::isfinite(dt))) return set_error(H, IMODEL_SWM_EINVAL, "bad dt or nsteps");
@@ -211,6 +279,29 @@ int advance(Handle *H, double dt, int nsteps) {
   int rc = ensure_graph(H, dt);
   if (rc) return rc;
   for (int k = 0; k < nsteps; ++k) CK(cudaGraphLaunch(H->graph, H->stream));
+  return learned_guard(H);
+}
+
+int setup_learned(Handle *H, const imodel_swm_mesh *m, const Layout &L, const imodel_swm_opts *o) {
+  if (H->precision != IMODEL_SWM_FP32)
+    return set_error(H, IMODEL_SWM_EINVAL, "the learned correction needs the FP32 path");
+  if (!o->mlp_weights || o->mlp_bytes != static_cast<size_t>(IMODEL_MLP_NPARAM) * sizeof(float))
+    return set_error(H, IMODEL_SWM_EINVAL, "mlp_weights must hold 5825 FP32 parameters");
+  LearnedLayout LL;
+  std::string msg = build_learned_layout(*m, L, LL);
+  if (!msg.empty()) return set_error(H, IMODEL_SWM_EINVAL, msg);
+  int rc;
+  if ((rc = upload(H, LL.lst, &H->learned.lst)) || (rc = upload(H, LL.geo, &H->learned.geo)) ||
+      (rc = dalloc(H, &H->learned.corr, static_cast<size_t>(L.ne))))
+    return rc;
+  rc = learned_prepare(static_cast<const float *>(o->mlp_weights), &H->learned, H->stream);
+  if (H->learned.p) H->allocs.push_back(H->learned.p);
+  if (H->learned.img) H->allocs.push_back(H->learned.img);
+  if (rc) return set_error(H, rc, "learned correction set-up failed");
+  H->drift_bound = o->drift_bound > 0 ? o->drift_bound : 1e-3;
+  H->learned_on = H->learned_active = true;
+  H->W32.learned = &H->learned;
+  H->W32.tune.variant = 1;
   return IMODEL_SWM_OK;
 }
 
@@ -220,8 +311,6 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
   H->device = o ? o->device : 0;
   if (H->precision != IMODEL_SWM_FP64 && H->precision != IMODEL_SWM_FP32)
     return set_error(H, IMODEL_SWM_EINVAL, "precision must be IMODEL_SWM_FP64 or IMODEL_SWM_FP32");
-  if (o && o->learned)
-    return set_error(H, IMODEL_SWM_EINVAL, "learned correction is not available in this build");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return set_error(H, IMODEL_SWM_ENODEV, "no CUDA device");
@@ -302,6 +391,7 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
     if ((rc = alloc_work(H, H->W32))) return rc;
     H->W32.h_ref = keep;
     if ((rc = dalloc(H, &H->W32.zflux, static_cast<size_t>(kMaxNb) * L.nv))) return rc;
+    if (o && o->learned && (rc = setup_learned(H, m, L, o))) return rc;
   }
   CK(cudaDeviceSynchronize());
   return IMODEL_SWM_OK;
@@ -353,7 +443,7 @@ int imodel_swm_step(void *handle, double *h_io, double *u_io, double dt, int32_t
   if (!H || !h_io || !u_io) return IMODEL_SWM_EINVAL;
   if (H->nv == 0) return imodel::set_error(H, IMODEL_SWM_ESTATE, "handle was not created");
   if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
-  int rc = imodel::load_state(H, h_io, u_io);
+  int rc = imodel::load_state(H, h_io, u_io, false);
   if (rc) return rc;
   rc = imodel::advance(H, dt, nsteps);
   if (rc) return rc;
@@ -367,7 +457,7 @@ int imodel_swm_set_state(void *handle, const double *h, const double *u) {
   if (!H || !h || !u) return IMODEL_SWM_EINVAL;
   if (H->nv == 0) return imodel::set_error(H, IMODEL_SWM_ESTATE, "handle was not created");
   if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
-  int rc = imodel::load_state(H, h, u);
+  int rc = imodel::load_state(H, h, u, true);
   if (rc) return rc;
   if (cudaStreamSynchronize(H->stream) != cudaSuccess)
     return imodel::set_error(H, IMODEL_SWM_ECUDA, "stream synchronize failed");
@@ -474,7 +564,7 @@ int imodel_swm_diagnostics(void *handle, imodel_swm_diag *out) {
   out->rms_div = std::sqrt(r[imodel::Q_ADIV2] / A);
   out->max_div = r[imodel::Q_MAXDIV];
   out->nan_found = r[imodel::Q_NAN] != 0.0 ? 1 : 0;
-  out->learned_active = 0;
+  out->learned_active = H->learned_active ? 1 : 0;
   return IMODEL_SWM_OK;
 }
 

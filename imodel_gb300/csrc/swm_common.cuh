@@ -44,9 +44,12 @@ struct Tune {
   int bs_tri = 256, bs_pre = 256, bs_cell = 256, bs_edge = 256;
 };
 
+struct LearnedDev;
+
 // Working fields of one handle, in the handle's precision T.
 template <class T>
 struct Work {
+  const LearnedDev *learned = nullptr;  // FP32 variant 1: learned correction on
   T *yn_h, *yn_u;    // state at t_n (advanced in place at the last stage)
   T *ya_h, *ya_u;    // stage inputs (ping)
   T *yb_h, *yb_u;    // stage inputs (pong)
@@ -73,6 +76,22 @@ void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
 void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
                     const float *u_in, float *h_out, float *u_out, int stage, float dt,
                     cudaStream_t s, cudaEvent_t *ev = nullptr);
+// The learned TRSK correction inside the FP32 step (mlp.cu): once per step,
+// after the first stage's PV, corr[e] = q_e h_e sigma_e y_e is formed from the
+// network output; the edge kernel adds it to the momentum tendency of every
+// stage of that step.
+struct LearnedDev {
+  float *p = nullptr;        // FP32 parameters
+  uint16_t *img = nullptr;   // BF16 weight images
+  const int32_t *lst = nullptr;
+  const uint16_t *geo = nullptr;
+  float *corr = nullptr;     // [ne]
+  int sms = 0;
+};
+int learned_prepare(const float *params_host, LearnedDev *L, cudaStream_t s);
+void learned_launch(const DevMesh &M, const LearnedDev &L, const float *hd, const float *u,
+                    const float *q_tr, float h_ref, int *err, cudaStream_t s);
+
 inline int launches_per_stage(int precision_fp32, int variant) {
   return (precision_fp32 && variant == 1) ? 3 : 4;
 }

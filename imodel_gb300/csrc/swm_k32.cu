@@ -117,19 +117,20 @@ __global__ void __launch_bounds__(512) k_edge32v2(DevMesh M, const float *__rest
                                                   float *__restrict__ acc,
                                                   float *__restrict__ yout,
                                                   float *__restrict__ tend, int stage, float dt,
-                                                  int mom_on, float erad) {
+                                                  int mom_on, float erad,
+                                                  const float *__restrict__ corr) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const int e0 = 2 * p;
   if (e0 >= M.ne) return;
   if (e0 + 1 < M.ne) {
     const uint4 w = __ldg(reinterpret_cast<const uint4 *>(M.e_vs2) + p);
     edge_body(M, e0, OneRun{}, make_uint2(w.x, w.y), bern, zflux, yn, acc, yout, tend, stage, dt,
-              mom_on, erad);
+              mom_on, erad, corr);
     edge_body(M, e0 + 1, OneRun{}, make_uint2(w.z, w.w), bern, zflux, yn, acc, yout, tend, stage,
-              dt, mom_on, erad);
+              dt, mom_on, erad, corr);
   } else {
     edge_body(M, e0, OneRun{}, __ldg(&M.e_vs2[e0]), bern, zflux, yn, acc, yout, tend, stage, dt,
-              mom_on, erad);
+              mom_on, erad, corr);
   }
 }
 
@@ -147,6 +148,9 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
                                                         W.flags);
   if (T.variant == 1) {
     if (ev) cudaEventRecord(ev[1], s);
+    // learned correction: formed once per step from the first stage's state
+    if (W.learned && stage <= 0)
+      learned_launch(M, *W.learned, h_in, u_in, W.q_tr, W.h_ref, W.flags, s);
     if (ev) cudaEventRecord(ev[2], s);
     k_cell32v2<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
         M, h_in, u_in, W.q_tr, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
@@ -154,7 +158,7 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
     if (ev) cudaEventRecord(ev[3], s);
     k_edge32v2<<<nblocks((M.ne + 1) / 2, T.bs_edge), T.bs_edge, 0, s>>>(
         M, W.bern, W.zflux, W.yn_u, W.acc_u, u_out, W.tend_u, stage, dt, W.mom_on,
-        static_cast<float>(M.erad));
+        static_cast<float>(M.erad), W.learned ? W.learned->corr : nullptr);
     if (ev) cudaEventRecord(ev[4], s);
     return;
   }

@@ -312,3 +312,66 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
 }
 
 }  // namespace imodel
+
+namespace imodel {
+
+uint16_t bf16_bits(float v) {
+  uint32_t b;
+  std::memcpy(&b, &v, sizeof(b));
+  if ((b & 0x7F800000u) == 0x7F800000u && (b & 0x007FFFFFu)) return static_cast<uint16_t>(b >> 16);
+  const uint64_t r = (static_cast<uint64_t>(b) + 0x7FFFu + ((b >> 16) & 1u)) >> 16;
+  return static_cast<uint16_t>(r & 0xFFFFu);
+}
+
+// Same inputs as imodel_gb300/learned.py (stencil, geometry_features): for
+// each edge and each of its two cells ed%v(1), ed%v(2), the cell's other
+// edges counter-clockwise from the edge (5 slots per cell, the sixth slot of
+// a pentagon empty), with sign ttgout_c(j) * tnrccw_c(i_e) and TRSK weight
+// trskw_c(i_e, j); geometry centred on a regular hexagonal grid and scaled:
+// 10 (l_e / mean l - 1), 10 (d_e / l_e - 1/sqrt 3), 10 (A_c / (l_e d_e) - 3/2)
+// for both cells and 20 (w - (r/n - 1/2)) for the 10 weights.
+std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, LearnedLayout &LL) {
+  const int ne = m.ne;
+  const size_t NE = ne;
+  LL.lst.assign(10 * NE, 0);
+  LL.geo.assign(16 * NE, 0);
+  double lmean = 0.0;
+  for (int e = 0; e < ne; ++e) lmean += m.ed_leng[e];
+  lmean /= ne;
+  for (int e = 0; e < ne; ++e) {
+    const int i = L.edge_o2n[e];
+    const double l = m.ed_leng[e], d = m.edhx_leng[e];
+    float g[14];
+    g[0] = static_cast<float>(10.0 * (l / lmean - 1.0));
+    g[1] = static_cast<float>(10.0 * (d / l - 1.0 / std::sqrt(3.0)));
+    for (int side = 0; side < 2; ++side) {
+      const int c = m.ed_v[2 * static_cast<size_t>(e) + side] - 1;
+      const int n = m.nnb[c];
+      g[2 + side] = static_cast<float>(10.0 * (m.hx_areag[c] / (l * d) - 1.5));
+      int slot = -1;
+      for (int j = 0; j < n; ++j)
+        if (m.v_ed[6 * static_cast<size_t>(c) + j] - 1 == e) slot = j;
+      if (slot < 0) return "edge missing from its cell's edge list";
+      for (int r = 1; r < 6; ++r) {
+        const int col = side * 5 + (r - 1);
+        float w = 0.0f;
+        if (r < n) {
+          const int j = (slot + r) % n;
+          const int k = m.v_ed[6 * static_cast<size_t>(c) + j] - 1;
+          const int s = m.hx_ttgout[6 * static_cast<size_t>(c) + j] *
+                        m.hx_tnrccw[6 * static_cast<size_t>(c) + slot];
+          LL.lst[col * NE + i] = (s < 0 ? -1 : 1) * (L.edge_o2n[k] + 1);
+          const double wreg = static_cast<double>(r) / n - 0.5;
+          w = static_cast<float>(
+              20.0 * (m.hx_trskw[36 * static_cast<size_t>(c) + 6 * static_cast<size_t>(j) + slot] -
+                      wreg));
+        }
+        g[4 + col] = w;
+      }
+    }
+    for (int q = 0; q < 14; ++q) LL.geo[16 * static_cast<size_t>(i) + q] = bf16_bits(g[q]);
+  }
+  return "";
+}
+
+}  // namespace imodel

@@ -88,4 +88,17 @@ struct Layout {
 // Builds the layout from a reference mesh; returns "" or an error message.
 std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L);
 
+// Inputs of the learned TRSK correction (imodel_gb300/learned.py), device
+// order: per edge the 10 stencil edges as sign * (index + 1) (0 = padding),
+// slot-major [10][ne], and the 14 geometry inputs as BF16 bit patterns,
+// [ne][16] (two zero pads, 32 bytes per edge).
+struct LearnedLayout {
+  std::vector<int32_t> lst;
+  std::vector<uint16_t> geo;
+};
+std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, LearnedLayout &LL);
+
+// float -> BF16 bit pattern, round to nearest, ties to even
+uint16_t bf16_bits(float v);
+
 }  // namespace imodel

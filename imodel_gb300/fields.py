@@ -102,6 +102,24 @@ class Spectral:
         return out
 
 
+    def eval_grad(self, lon, lat, chunk=262144):
+        """(d/dlat, d/dlon) of the field at points, in one pass."""
+        lon = np.asarray(lon, dtype=np.float64)
+        lat = np.asarray(lat, dtype=np.float64)
+        flat = np.empty(lon.size)
+        flon = np.empty(lon.size)
+        m = np.arange(self.lmax + 1, dtype=np.float64)
+        for s in range(0, lon.size, chunk):
+            la, lo = lat[s:s + chunk], lon[s:s + chunk]
+            Am, Bm = self.splA(la), self.splB(la)
+            dAm, dBm = self.splA(la, 1), self.splB(la, 1)
+            ml = np.outer(lo, m)
+            c, sn = np.cos(ml), np.sin(ml)
+            flat[s:s + chunk] = np.sum(dAm * c + dBm * sn, axis=1)
+            flon[s:s + chunk] = np.sum(m * (Bm * c - Am * sn), axis=1)
+        return flat, flon
+
+
 def gauss_grid(lmax: int):
     nlat = lmax + 3
     x, w = np.polynomial.legendre.leggauss(nlat)

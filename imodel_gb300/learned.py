@@ -11,8 +11,12 @@ reconstruction error from local inputs:
   ttgout_c(j) * tnrccw_c(i_e) (the local edge frame), ordered ccw from the
   edge in cell ed%v(1) (5 slots) then in cell ed%v(2) (5 slots), pentagon
   slots zero; divided by their RMS sigma,
-* 14 geometry numbers: l_e / mean l, d_e / l_e, A_c1 / (l_e d_e),
-  A_c2 / (l_e d_e), and the 10 TRSK weights w_c(i_e, j) of the slots above.
+* 14 geometry numbers, centred on their values for a regular hexagonal
+  grid and scaled so that BF16 keeps the grid-distortion signal:
+  10 (l_e / mean l - 1), 10 (d_e / l_e - 1/sqrt 3), 10 (A_c / (l_e d_e) - 3/2)
+  for both cells, and 20 (w_c(i_e, j) - w_reg) for the 10 TRSK weights of the
+  slots above, w_reg = r/n - 1/2 being the weight of slot r of a regular
+  n-gon.
 
 The network (24 -> 64 -> 64 -> 1, GELU, BF16 weights, FP32 accumulation)
 outputs the error divided by sigma, so the correction is linear in the
@@ -63,6 +67,16 @@ def stencil(grid: Grid):
     return idx, sgn, wts
 
 
+def regular_weights(grid: Grid):
+    """TRSK weight of each stencil slot on a regular n-gon: r/n - 1/2."""
+    wreg = np.zeros((grid.ne, NVEL))
+    for side in range(2):
+        n = grid.nnb[grid.ed_v[:, side] - 1].astype(np.float64)
+        for r in range(1, 6):
+            wreg[:, side * 5 + r - 1] = np.where(r < n, r / n - 0.5, 0.0)
+    return wreg
+
+
 def geometry_features(grid: Grid, wts=None):
     """The 14 per-edge geometry inputs [ne, 14] (float64)."""
     if wts is None:
@@ -72,11 +86,11 @@ def geometry_features(grid: Grid, wts=None):
     c1 = grid.ed_v[:, 0] - 1
     c2 = grid.ed_v[:, 1] - 1
     g = np.empty((grid.ne, NGEO))
-    g[:, 0] = l / l.mean()
-    g[:, 1] = d / l
-    g[:, 2] = grid.hx_areag[c1] / (l * d)
-    g[:, 3] = grid.hx_areag[c2] / (l * d)
-    g[:, 4:] = wts
+    g[:, 0] = 10.0 * (l / l.mean() - 1.0)
+    g[:, 1] = 10.0 * (d / l - 1.0 / np.sqrt(3.0))
+    g[:, 2] = 10.0 * (grid.hx_areag[c1] / (l * d) - 1.5)
+    g[:, 3] = 10.0 * (grid.hx_areag[c2] / (l * d) - 1.5)
+    g[:, 4:] = 20.0 * (wts - regular_weights(grid))
     return g
 
 
@@ -105,19 +119,34 @@ def velocity_sample(grid: Grid, lmax: int = 48, seed: int = 0, chi_fraction: flo
     elon = np.arctan2(grid.ed_c[:, 1], grid.ed_c[:, 0])
     elat = grid.ed_c_lat
     cosl = np.maximum(np.cos(elat), 1e-12)
-    ulon = -sp.eval(elon, elat, dlat=True) / ERAD
-    ulat = sp.eval(elon, elat, dlon=True) / (ERAD * cosl)
+    psi_lat, psi_lon = sp.eval_grad(elon, elat)
+    ulon = -psi_lat / ERAD
+    ulat = psi_lon / (ERAD * cosl)
     if chi_fraction > 0:
         ac, bc = fields.random_coeffs(lmax, seed + 7919, exponent)
         sc = fields.Spectral(ac, bc)
-        dl = sc.eval(elon, elat, dlon=True) / (ERAD * cosl)
-        dp = sc.eval(elon, elat, dlat=True) / ERAD
+        chi_lat, chi_lon = sc.eval_grad(elon, elat)
+        dl = chi_lon / (ERAD * cosl)
+        dp = chi_lat / ERAD
         k = chi_fraction * np.sqrt(ulon ** 2 + ulat ** 2).max() / np.sqrt(dl ** 2 + dp ** 2).max()
         ulon = ulon + k * dl
         ulat = ulat + k * dp
     scale = umax / np.sqrt(ulon ** 2 + ulat ** 2).max()
     v = convert_vec_sph2cart(ulon * scale, ulat * scale, grid.ed_c)
     return dot3(v, grid.ed_tg), dot3(v, grid.ed_nr)
+
+
+def init_params(seed: int = 0):
+    """Uniform Glorot initial parameters (layout of include/imodel_mlp.h),
+    zero biases."""
+    rng = np.random.default_rng(seed)
+    a1 = np.sqrt(6.0 / (NFEAT + HIDDEN))
+    a2 = np.sqrt(6.0 / (HIDDEN + HIDDEN))
+    a3 = np.sqrt(6.0 / (HIDDEN + 1))
+    return np.concatenate([
+        rng.uniform(-a1, a1, HIDDEN * NFEAT), np.zeros(HIDDEN),
+        rng.uniform(-a2, a2, HIDDEN * HIDDEN), np.zeros(HIDDEN),
+        rng.uniform(-a3, a3, HIDDEN), np.zeros(1)]).astype(np.float32)
 
 
 def to_bf16_bits(a):
@@ -185,21 +214,30 @@ class Mlp:
         self._check(self.lib.imodel_mlp_forward(self._h, self._u16p(xbits), n, self._f32p(y)))
         return y
 
-    def grad(self, xbits, t, batch=None, seed=0):
+    def grad(self, xbits, t, w=None, batch=None, seed=0):
         xbits = np.ascontiguousarray(xbits, dtype=np.uint16)
         t = np.ascontiguousarray(t, dtype=np.float32)
+        wp = None
+        if w is not None:
+            w = np.ascontiguousarray(w, dtype=np.float32)
+            wp = self._f32p(w)
         n = xbits.shape[0]
         g = np.empty(self.NPARAM, dtype=np.float32)
         loss = self._ct.c_double()
-        self._check(self.lib.imodel_mlp_grad(self._h, self._u16p(xbits), self._f32p(t), n, seed,
-                                             batch or n, self._f32p(g), self._ct.byref(loss)))
+        self._check(self.lib.imodel_mlp_grad(self._h, self._u16p(xbits), self._f32p(t), wp, n,
+                                             seed, batch or n, self._f32p(g),
+                                             self._ct.byref(loss)))
         return loss.value, g
 
-    def load_dataset(self, xbits, t):
+    def load_dataset(self, xbits, t, w=None):
         xbits = np.ascontiguousarray(xbits, dtype=np.uint16)
         t = np.ascontiguousarray(t, dtype=np.float32)
+        wp = None
+        if w is not None:
+            self._w = np.ascontiguousarray(w, dtype=np.float32)
+            wp = self._f32p(self._w)
         self._check(self.lib.imodel_mlp_load_dataset(self._h, self._u16p(xbits), self._f32p(t),
-                                                     xbits.shape[0]))
+                                                     wp, xbits.shape[0]))
 
     def train(self, steps, batch=65536, lr=1e-3, seed=1):
         losses = np.empty(steps, dtype=np.float32)
@@ -208,19 +246,39 @@ class Mlp:
         return losses
 
 
-def training_set(grid: Grid, seeds, lmax: int = 48, chi_fraction: float = 0.5):
-    """Inputs (BF16 bits [n, 24]) and normalised targets (error / sigma) of
-    TRSK's tangential reconstruction for seeded fields on one grid."""
+def training_set(grid: Grid, seeds, lmax: int = 48, chi_fraction: float = 0.5,
+                 mixtures: int = 0, mix_seed: int = 0):
+    """Inputs (BF16 bits [n, 24]), normalised targets (error / sigma) and
+    sample weights sigma^2 / mean(sigma^2) of TRSK's tangential
+    reconstruction for seeded fields on one grid.  With these weights the
+    loss is the mean squared error of the tangential velocity itself, so
+    near-stagnation edges (small sigma, where the stencil does not determine
+    the error) do not dominate the fit.
+
+    mixtures > 0 adds that many fields formed as random Gaussian combinations
+    of the sampled ones: a Gaussian mixture of random spherical-harmonic fields
+    is again such a field, and both the TRSK reconstruction and the exact
+    tangential component are linear in the velocity, so these samples are
+    exact and cost no spectral work."""
     st = stencil(grid)
     geo = geometry_features(grid, st[2])
-    xs, ts = [], []
-    for s in seeds:
-        u, ut = velocity_sample(grid, lmax=lmax, seed=s, chi_fraction=chi_fraction)
+    base = [velocity_sample(grid, lmax=lmax, seed=s, chi_fraction=chi_fraction) for s in seeds]
+    fields_uv = list(base)
+    if mixtures > 0:
+        rng = np.random.default_rng(mix_seed)
+        U = np.stack([b[0] for b in base])
+        UT = np.stack([b[1] for b in base])
+        for _ in range(mixtures):
+            a = rng.standard_normal(len(base)) / np.sqrt(len(base))
+            fields_uv.append((a @ U, a @ UT))
+    xs, ts, ws = [], [], []
+    for u, ut in fields_uv:
         utg = trsk_tangent_np(grid, u, st)
         x, sigma = features(grid, u, st, geo)
         xs.append(to_bf16_bits(x))
         ts.append(((ut - utg) / sigma).astype(np.float32))
-    return np.concatenate(xs), np.concatenate(ts)
+        ws.append((sigma * sigma / np.mean(sigma * sigma)).astype(np.float32))
+    return np.concatenate(xs), np.concatenate(ts), np.concatenate(ws)
 
 
 def corrected_tangent(grid: Grid, mlp: Mlp, u, st=None):

@@ -114,7 +114,8 @@ class SWM:
     """
 
     def __init__(self, grid: Grid, precision: str = "fp64", testcase: int = 2,
-                 bt=None, h_ref: float = 0.0, device: int = 0):
+                 bt=None, h_ref: float = 0.0, device: int = 0, learned_params=None,
+                 drift_bound: float = 0.0):
         self.grid = grid
         self.lib = _capi.swm_lib()
         self.precision = precision
@@ -128,6 +129,14 @@ class SWM:
             opts.bt = _capi.as_f64p(self._bt)
         opts.h_ref = h_ref
         opts.device = device
+        self._mlp = None
+        if learned_params is not None:
+            # learned TRSK correction (network parameters, see imodel_mlp.h)
+            self._mlp = np.ascontiguousarray(learned_params, dtype=np.float32)
+            opts.learned = 1
+            opts.mlp_weights = self._mlp.ctypes.data
+            opts.mlp_bytes = self._mlp.nbytes
+            opts.drift_bound = drift_bound
         self._handle = ctypes.c_void_p()
         rc = self.lib.imodel_swm_create(ctypes.byref(self._mesh), ctypes.byref(opts),
                                         ctypes.byref(self._handle))

@@ -27,13 +27,15 @@ int imodel_mlp_set_params(void *mlp, const float *params, int32_t n);
 int imodel_mlp_get_params(void *mlp, float *params, int32_t n);
 /* y[n] = network(x[n][24]); host arrays. */
 int imodel_mlp_forward(void *mlp, const uint16_t *x, int64_t n, float *y);
-/* Gradient of the mean squared error over one batch of `batch` rows of
- * (x, t): seed 0 takes rows 0..batch-1, any other seed draws rows with
- * replacement.  grad[5825]; *loss = mean squared error. */
-int imodel_mlp_grad(void *mlp, const uint16_t *x, const float *t, int64_t n, uint64_t seed,
-                    int64_t batch, float *grad, double *loss);
-/* Copies a training set (x[n][24], t[n]) to the device. */
-int imodel_mlp_load_dataset(void *mlp, const uint16_t *x, const float *t, int64_t n);
+/* Gradient of the weighted mean squared error sum_b w_b (y_b - t_b)^2 / batch
+ * over one batch of `batch` rows of (x, t, w) (w NULL: all weights 1):
+ * seed 0 takes rows 0..batch-1, any other seed draws rows with replacement.
+ * grad[5825]; *loss = the weighted mean squared error. */
+int imodel_mlp_grad(void *mlp, const uint16_t *x, const float *t, const float *w, int64_t n,
+                    uint64_t seed, int64_t batch, float *grad, double *loss);
+/* Copies a training set (x[n][24], t[n], optional weights w[n]) to the device. */
+int imodel_mlp_load_dataset(void *mlp, const uint16_t *x, const float *t, const float *w,
+                            int64_t n);
 /* `steps` Adam steps (beta 0.9/0.999, eps 1e-8) on random batches of the
  * loaded set; losses[steps] receives each batch's mean squared error. */
 int imodel_mlp_train(void *mlp, int64_t steps, int64_t batch, float lr, uint64_t seed,

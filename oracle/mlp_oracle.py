@@ -98,14 +98,16 @@ def forward(p, x):
     return y, {"xb": xb, "z1": z1, "h1b": h1b, "z2": z2, "h2": h2}
 
 
-def loss_and_grad(p, x, t):
-    """Mean squared error and its gradient (parameter-vector layout)."""
+def loss_and_grad(p, x, t, w=None):
+    """Weighted mean squared error sum w (y - t)^2 / n and its gradient
+    (parameter-vector layout); w None means all weights 1."""
     P = unpack(p)
     y, c = forward(p, x)
     n = x.shape[0]
+    w = np.ones(n) if w is None else np.asarray(w, dtype=np.float64)
     r = (y - t).astype(np.float64)
-    loss = float(np.mean(r * r))
-    dy = (2.0 * r / n).astype(np.float32)
+    loss = float(np.mean(w * r * r))
+    dy = (2.0 * w * r / n).astype(np.float32)
     g = {}
     g["w3"] = (c["h2"].astype(np.float64).T @ dy).astype(np.float32)
     g["b3"] = np.array([dy.sum(dtype=np.float64)], dtype=np.float32)

@@ -30,13 +30,14 @@ def test_forward_matches_oracle(n):
     assert np.mean(np.abs(y - yr)) < 1e-3 * np.mean(np.abs(yr)) + 1e-6
 
 
-@pytest.mark.parametrize("batch", [128, 300, 4096])
-def test_gradient_matches_oracle(batch):
+@pytest.mark.parametrize("batch,weighted", [(128, False), (300, True), (4096, True)])
+def test_gradient_matches_oracle(batch, weighted):
     xb, x, t = _rand_problem(batch, 2)
+    w = np.random.default_rng(8).uniform(0.1, 3.0, batch).astype(np.float32) if weighted else None
     p = mo.init_params(4)
     net = learned.Mlp(params=p)
-    loss, g = net.grad(xb, t, batch=batch, seed=0)
-    lr_, gr = mo.loss_and_grad(p, x, t)
+    loss, g = net.grad(xb, t, w=w, batch=batch, seed=0)
+    lr_, gr = mo.loss_and_grad(p, x, t, w)
     rel = np.linalg.norm(g - gr) / np.linalg.norm(gr)
     print(f"gradient batch={batch}: loss {loss:.6f} vs {lr_:.6f}, relative L2 {rel:.2e}")
     assert abs(loss - lr_) <= 1e-3 * lr_
@@ -63,14 +64,16 @@ def test_learned_correction_beats_plain_trsk(grid_at):
     """Trained on seeded fields of one grid, the network lowers TRSK's
     tangential-reconstruction error on unseen fields of the same grid."""
     g = grid_at(5)
-    x, t = learned.training_set(g, seeds=range(24), lmax=24)
+    # degree-12 fields resolved by ~14 cells per wavelength, as degree-48
+    # fields are on level 7
+    x, t, w = learned.training_set(g, seeds=range(24), lmax=12, mixtures=200)
     net = learned.Mlp(params=mo.init_params(0))
-    net.load_dataset(x, t)
-    losses = net.train(600, batch=16384, lr=2e-3, seed=3)
+    net.load_dataset(x, t, w)
+    losses = net.train(2000, batch=16384, lr=2e-3, seed=3)
     st = learned.stencil(g)
     gains = []
     for seed in (1000, 1001):
-        u, ut = learned.velocity_sample(g, lmax=24, seed=seed)
+        u, ut = learned.velocity_sample(g, lmax=12, seed=seed)
         plain = learned.trsk_tangent_np(g, u, st)
         corr = learned.corrected_tangent(g, net, u, st)
         e0 = np.sqrt(np.mean((plain - ut) ** 2) / np.mean(ut ** 2))
@@ -78,4 +81,4 @@ def test_learned_correction_beats_plain_trsk(grid_at):
         gains.append(e0 / e1)
         print(f"unseen field {seed}: TRSK rel L2 error {e0:.3e}, learned {e1:.3e}")
     print(f"training loss {losses[0]:.4f} -> {losses[-1]:.4f}")
-    assert min(gains) > 1.5
+    assert min(gains) > 2.0
