@@ -6,14 +6,18 @@ Workload: icosahedral level 9 (2,621,442 cells, 7,864,320 edges,
 synthetic state (Williamson case 2 steady flow), dt = 55 s.  One "step" is
 one RK4 time step of the whole grid.
 
-  value      cell-steps/s of the FP32 path with the state resident in HBM
-             (graph-replayed steps, CUDA events on the library's stream)
+  value      cell-steps/s of the FP32 path with the learned TRSK correction
+             (per-edge MLP evaluated once per step on the tensor cores),
+             state resident in HBM (graph-replayed steps, CUDA events on the
+             library's stream)
+  fp32_plain the same without the learned correction
   fp64       the same for the FP64 reference-order path
-  e2e        cell-steps/s through the C ABI call imodel_swm_step with
-             pinned host buffers: every step copies h and u (FP64) to the
-             device and back inside the timed region
-  roofline   the dominant kernel (edge kernel: grad B + TRSK PV flux +
-             momentum update) against the measured HBM copy bandwidth
+  e2e        cell-steps/s of the headline path through the C ABI call
+             imodel_swm_step with pinned host buffers: every step copies h
+             and u (FP64) to the device and back inside the timed region
+  roofline   the dominant stencil kernel against the measured HBM copy
+             bandwidth; mlp_roofline the network kernel against the
+             measured BF16 tensor throughput
   cpu_baseline  the CPU oracle (C++ restatement of the Fortran, OpenMP on
              all host threads) on a bounded sample of the same workload
 
@@ -278,13 +282,30 @@ def run_reference(args):
     return 0
 
 
-def config_dict(g, precision):
+def config_dict(g, path, weights=None):
+    learned = "off"
+    if path == "fp32l":
+        learned = ("per-edge MLP 24-64-64-1, BF16 tcgen05, once per step; weights " +
+                   (weights or "none"))
     return {"workload": f"icos-L{g.level} TRSK shallow-water RK4 step, trsk10/HTC/geo, "
                         f"dt={DT:g} s, Williamson case 2 state",
             "level": g.level, "cells": g.nv, "edges": g.ne, "triangles": g.nt,
-            "precision": precision, "learned_correction": "not built",
+            "precision": "fp64" if path == "fp64" else "fp32",
+            "learned_correction": learned,
             "l2": "inputs larger than L2 (state + geometry of several GB per step)",
             "parallelism": "replicas"}
+
+
+MLP_FLOP_PER_EDGE = 2 * (24 * 64 + 64 * 64 + 64)
+
+
+def load_tflops():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
 
 
 def main():
@@ -297,9 +318,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    # switches for profiler runs: time only the listed paths, skip the
-    # end-to-end and per-kernel passes
-    ap.add_argument("--precisions", default="fp64,fp32")
+    # switches for profiler runs: time only the listed paths (fp64, fp32 =
+    # plain FP32, fp32l = FP32 + learned correction), skip the end-to-end
+    # and per-kernel passes
+    ap.add_argument("--precisions", default="fp64,fp32,fp32l")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-kprof", action="store_true")
     ap.add_argument("--tuning", default="",
@@ -311,7 +333,7 @@ def main():
         return run_reference(args)
 
     ws, rank, local = dist_env()
-    from imodel_gb300 import _build, swm
+    from imodel_gb300 import _build, learned, swm
     from imodel_gb300.mesh import meshbuild
     _build.build_all()
     cr = Cudart()
@@ -320,13 +342,20 @@ def main():
 
     g = meshbuild(args.level)
     h, u = swm.initialize_fields_tc2(g)
+    params = learned.trained_params()
+    weights = "trained on icos-L7 (imodel_gb300/data/trsk_mlp_l7.npy)"
+    if params is None:
+        params = learned.init_params(0)
+        weights = "untrained (Glorot initial values, seed 0)"
     results = {}
-    precisions = [p for p in args.precisions.split(",") if p]
-    for precision in precisions:
-        m = swm.SWM(g, precision=precision, device=local)
+    paths = [p for p in args.precisions.split(",") if p]
+    headline = "fp32l" if "fp32l" in paths else "fp32"
+    for path in paths:
+        m = swm.SWM(g, precision="fp64" if path == "fp64" else "fp32", device=local,
+                    learned_params=params if path == "fp32l" else None)
         m.set_state(h, u)
         tuning = None
-        if precision == "fp32":
+        if path != "fp64":
             if args.tuning:
                 c = [int(x) for x in args.tuning.split(",")]
                 m.set_tuning(*c)
@@ -337,7 +366,7 @@ def main():
         m.advance(DT, args.warmup)
         cr.sync()
         ev0, ev1 = cr.event(), cr.event()
-        sampler = ClockSampler(local) if precision == "fp32" else None
+        sampler = ClockSampler(local) if path == headline else None
         D.barrier()
         cr.sync()
         if sampler:
@@ -352,11 +381,10 @@ def main():
         ms = D.max(ms)
         diag = m.diagnostics()
         prof = None if args.no_kprof else m.profile(DT, 3)
-        results[precision] = {"ms": ms, "clocks": clocks, "prof": prof, "diag": diag,
-                              "tuning": tuning,
-                              "launches": m.launch_count(args.steps),
-                              "main_kernel": m.main_kernel()}
-        if precision == "fp32" and not args.no_e2e:
+        results[path] = {"ms": ms, "clocks": clocks, "prof": prof, "diag": diag,
+                         "tuning": tuning, "launches": m.launch_count(args.steps),
+                         "main_kernel": m.main_kernel()}
+        if path == headline and not args.no_e2e:
             # e2e through the C ABI with pinned host buffers
             ph, hbuf = cr.pinned(g.nv)
             pu, ubuf = cr.pinned(g.ne)
@@ -380,34 +408,39 @@ def main():
             cr.lib.cudaFreeHost(pu)
         m.close()
 
-    if rank == 0 and not ("fp32" in results and "fp64" in results and "e2e" in results
-                          and results["fp32"]["prof"]):
+    full = ("fp64" in results and headline in results and "e2e" in results
+            and results[headline]["prof"])
+    if rank == 0 and not full:
         # profiler runs: a short line with the timed paths only
         print(json.dumps({k: {"ms_per_step": v["ms"] / args.steps} for k, v in results.items()
-                          if k in ("fp32", "fp64")}))
+                          if k in ("fp32", "fp32l", "fp64")}))
     elif rank == 0:
-        r32, r64 = results["fp32"], results["fp64"]
+        rh, r64 = results[headline], results["fp64"]
         total_cells = g.nv * ws
-        value = total_cells * args.steps / (r32["ms"] / 1000.0)
-        value64 = total_cells * args.steps / (r64["ms"] / 1000.0)
+
+        def rate(r):
+            return total_cells * args.steps / (r["ms"] / 1000.0)
+
         peak, peak_kind = load_peaks()
-        kb = kernel_bytes(g.nv, g.ne, g.nt, "fp32", r32["tuning"]["variant"])
-        dom = max(r32["prof"], key=r32["prof"].get)
-        achieved = kb[dom] / (r32["prof"][dom] / 1000.0) / 1e9
+        kb = kernel_bytes(g.nv, g.ne, g.nt, "fp32", rh["tuning"]["variant"])
+        prof = {k: v for k, v in rh["prof"].items() if k != "edge_pre" or kb["edge_pre"]}
+        dom = max(prof, key=prof.get)
+        achieved = kb[dom] / (prof[dom] / 1000.0) / 1e9
         step_bytes = 2000.0 * g.nv  # per-cell-step algorithmic bytes (FP32 model)
-        step_achieved = step_bytes / (r32["ms"] / args.steps / 1000.0) / 1e9
+        step_achieved = step_bytes / (rh["ms"] / args.steps / 1000.0) / 1e9
         e2e = results["e2e"]
+        kernel_ms = dict(prof)
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "metric": METRIC, "value": rate(rh), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": r32["ms"] / args.steps, "higher_is_better": True,
+            "ms_per_step": rh["ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: Williamson case 2 steady zonal flow on the grid (no dataset)",
-            "config": dict(config_dict(g, "fp32"), autotuned=r32["tuning"]),
-            "fp64": {"value": value64, "unit": UNIT, "ms_per_step": r64["ms"] / args.steps,
+            "config": dict(config_dict(g, headline, weights), autotuned=rh["tuning"]),
+            "fp64": {"value": rate(r64), "unit": UNIT, "ms_per_step": r64["ms"] / args.steps,
                      "kernel_ms": r64["prof"]},
-            "kernel_ms": r32["prof"],
-            "roofline": {"bound": "hbm", "kernel": kernel_names(r32["tuning"]["variant"])[dom],
+            "kernel_ms": kernel_ms,
+            "roofline": {"bound": "hbm", "kernel": kernel_names(rh["tuning"]["variant"])[dom],
                          "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": peak_kind, "traffic": None,
@@ -418,9 +451,26 @@ def main():
                     "h2d_bytes_per_step": 8 * (g.nv + g.ne),
                     "d2h_bytes_per_step": 8 * (g.nv + g.ne),
                     "path": "imodel_swm_step(nsteps=1) with pinned host FP64 h,u"},
-            "gpu_launches": r32["launches"],
-            "clocks": r32["clocks"],
+            "gpu_launches": rh["launches"],
+            "clocks": rh["clocks"],
         }
+        if "fp32" in results and headline != "fp32":
+            line["fp32_plain"] = {"value": rate(results["fp32"]), "unit": UNIT,
+                                  "ms_per_step": results["fp32"]["ms"] / args.steps,
+                                  "kernel_ms": results["fp32"]["prof"]}
+        if headline == "fp32l":
+            # the network runs once per step: the profile reports it per stage
+            mlp_ms = rh["prof"]["edge_pre"] * 4.0
+            kernel_ms["mlp"] = mlp_ms
+            kernel_ms.pop("edge_pre", None)
+            flop = MLP_FLOP_PER_EDGE * g.ne
+            tf, tf_kind = load_tflops()
+            ach = flop / (mlp_ms / 1000.0) / 1e12
+            line["mlp_roofline"] = {"bound": "tensor", "kernel": "k_mlp_apply<EdgeIn,CorrOut>",
+                                    "achieved": ach, "peak": tf, "unit": "TFLOP/s",
+                                    "frac": ach / tf, "peak_source": tf_kind,
+                                    "flop_per_launch": flop}
+            line["learned_active_after_run"] = bool(rh["diag"]["learned_active"])
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_sample(g, h, u, args.cpu_budget)
         print(json.dumps(line))

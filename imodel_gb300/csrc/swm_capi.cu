@@ -717,7 +717,8 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
   const int sizes[3] = {128, 256, 512};
   imodel::Tune best;
   float best_ms = 1e30f;
-  for (int v = 0; v < 2; ++v)
+  // the learned correction is wired into the cell-centred variant only
+  for (int v = H->learned_on ? 1 : 0; v < 2; ++v)
     for (int b : sizes) {
       imodel::Tune t;
       t.variant = v;
@@ -775,6 +776,9 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[5]) {
       return imodel::set_error(H, IMODEL_SWM_EINVAL, "block sizes must be 128, 256 or 512");
   if (choice[0] != 0 && choice[0] != 1)
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "variant must be 0 or 1");
+  if (H->learned_on && choice[0] != 1)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL,
+                             "the learned correction runs with the cell-centred variant (1) only");
   imodel::Tune t;
   t.variant = choice[0];
   t.bs_tri = choice[1];
@@ -795,6 +799,8 @@ int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count) {
   const int fp32 = H->precision == IMODEL_SWM_FP32;
   *count = static_cast<int64_t>(nsteps) * 4 *
            imodel::launches_per_stage(fp32, fp32 ? H->W32.tune.variant : 0);
+  // the learned correction adds one network launch per step while it is on
+  if (fp32 && H->W32.learned) *count += nsteps;
   return IMODEL_SWM_OK;
 }
 

@@ -1,0 +1,287 @@
+"""Accuracy and throughput runs of the shallow-water configurations.
+
+    python -m imodel_gb300.experiments <run> [--out result.json] [options]
+
+Runs (all on one GPU, seeded synthetic states from imodel_gb300.fields):
+
+  tc2        Williamson case 2 on icos level 5, dt 450 s, 5 days: FP64 and
+             FP32 error tables against the steady state (the reference's
+             swm_tests numbers).
+  balanced   icos level 8, dt 110 s, 10 days, balanced state (degree
+             1..64, l^-2 coefficients, max wind 40 m/s): FP32 and FP32 +
+             learned correction against the FP64 run of the same grid.
+  ensemble   64 members on level 6 (dt 225 s, seeds 0..63) and 16 on
+             level 7 (dt 110 s, seeds 100..115), degree <= 32, 5 days, in one
+             persistent launch; spot members checked against single runs.
+  mountains  level 8, dt 108 s, 10 days, balanced flow over 4 Gaussian
+             mountains: plain FP32 and FP32 + learned correction, each
+             against an FP64 run on level 9 (dt 54 s) restricted to the
+             level-8 cells.
+  fixed      level 9 (dt 54 s) FP64, FP32 and FP32 + learned, 10 days,
+             each against an FP64 run on level 10 (dt 27 s): h error and
+             cell-steps/s at equal error.
+  large      level 10, dt 28 s, 2 days, balanced state with an l^-3 energy
+             spectrum to degree 256 and max wind 60 m/s: FP32 + learned
+             against FP64.
+
+h of a coarser grid is compared with a finer grid's solution by index
+restriction: the icosahedral refinement keeps every node of level L as the
+first nv(L) nodes of level L+1.  Errors are area-weighted relative L2 and
+relative max norms, as error_calc (src/swm.f90:3492-3543).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import time
+
+import numpy as np
+
+DAY = 86400.0
+
+
+def _pool(workers: int = 0):
+    # started before any GPU work
+    return mp.get_context("spawn").Pool(workers or max(1, os.cpu_count() or 1))
+
+
+def rel_errors(x, ref, w):
+    d = x - ref
+    l2 = float(np.sqrt(np.sum(w * d * d) / np.sum(w * ref * ref)))
+    linf = float(np.max(np.abs(d)) / np.max(np.abs(ref)))
+    return {"l2": l2, "linf": linf}
+
+
+def _edge_w(g):
+    return g.ed_leng * g.edhx_leng / 2.0
+
+
+def run(grid, path, h, u, dt, nsteps, bt=None, params=None, chunk=0):
+    """One run on the GPU; returns the final state, timing and diagnostics.
+    path: "fp64", "fp32" or "fp32l" (FP32 + learned correction)."""
+    from . import swm
+    m = swm.SWM(grid, precision="fp64" if path == "fp64" else "fp32", bt=bt,
+                learned_params=params if path == "fp32l" else None)
+    try:
+        m.set_state(h, u)
+        if path != "fp64":
+            m.autotune(dt, 3)
+            m.set_state(h, u)
+        d0 = m.diagnostics()
+        chunk = chunk or nsteps
+        t0 = time.perf_counter()
+        done = 0
+        while done < nsteps:
+            k = min(chunk, nsteps - done)
+            m.advance(dt, k)
+            done += k
+        el = time.perf_counter() - t0
+        d1 = m.diagnostics()
+        hf, uf = m.get_state()
+    finally:
+        m.close()
+    rel = lambda k: (d1[k] - d0[k]) / abs(d0[k])  # noqa: E731
+    return {"h": hf, "u": uf, "seconds": el, "steps": nsteps,
+            "cell_steps_per_s": grid.nv * nsteps / el,
+            "mass_change": rel("mass"), "tenergy_change": rel("tenergy"),
+            "learned_active": bool(d1["learned_active"]), "nan": bool(d1["nan_found"])}
+
+
+def _summary(r, keep=("seconds", "steps", "cell_steps_per_s", "mass_change", "tenergy_change",
+                      "learned_active")):
+    return {k: r[k] for k in keep}
+
+
+def _params(args):
+    from . import learned
+    p = learned.trained_params()
+    if p is None:
+        raise SystemExit("no trained network: run imodel_gb300.train_learned first")
+    return p
+
+
+def exp_tc2(args, pool):
+    from . import swm
+    from .mesh import meshbuild
+    g = meshbuild(5)
+    out = {}
+    for prec in ("fp64", "fp32"):
+        out[prec] = swm.swm_tests(g, 450.0, 5.0, precision=prec)
+    return out
+
+
+def exp_balanced(args, pool):
+    from . import fields, swm
+    from .mesh import meshbuild
+    g = meshbuild(args.level or 8)
+    dt = args.dt or 110.0
+    n = swm.ntime_for(args.days or 10.0, dt)
+    h, u = fields.balanced_state(g, lmax=64, seed=0, evaluator=fields.PoolEvaluator(pool))
+    r64 = run(g, "fp64", h, u, dt, n)
+    out = {"level": g.level, "dt": dt, "steps": n, "fp64": _summary(r64)}
+    for path in ("fp32", "fp32l"):
+        r = run(g, path, h, u, dt, n, params=_params(args) if path == "fp32l" else None)
+        out[path] = dict(_summary(r), h_vs_fp64=rel_errors(r["h"], r64["h"], g.hx_areag),
+                         u_vs_fp64=rel_errors(r["u"], r64["u"], _edge_w(g)))
+    return out
+
+
+def _member_state(args):
+    level, seed = args
+    from . import fields
+    from .mesh import meshbuild
+    g = meshbuild(level, nthreads=1)
+    return fields.balanced_state(g, lmax=32, seed=seed)
+
+
+def exp_ensemble(args, pool):
+    from . import swm
+    from .mesh import meshbuild
+    levels, seeds = (6, 7), (list(range(64)), list(range(100, 116)))
+    dts = [225.0, 110.0]
+    days = args.days or 5.0
+    steps = [swm.ntime_for(days, dt) for dt in dts]
+    grids = [meshbuild(l) for l in levels]
+    states = [pool.map(_member_state, [(l, s) for s in ss]) for l, ss in zip(levels, seeds)]
+    ens = swm.Ensemble(grids, [len(s) for s in seeds])
+    try:
+        for k in range(2):
+            for j, (h, u) in enumerate(states[k]):
+                ens.set_state(k, j, h, u)
+        tune = ens.tune(dts, 3)
+        for k in range(2):
+            for j, (h, u) in enumerate(states[k]):
+                ens.set_state(k, j, h, u)
+        t0 = time.perf_counter()
+        ens.advance(dts, steps)
+        el = time.perf_counter() - t0
+        finals = {(k, j): ens.get_state(k, j) for k, j in ((0, 0), (0, 63), (1, 0), (1, 15))}
+    finally:
+        ens.close()
+    cells = sum(len(s) * g.nv * n for s, g, n in zip(seeds, grids, steps))
+    out = {"members": [len(s) for s in seeds], "levels": list(levels), "dt": dts,
+           "steps": steps, "seconds": el, "cell_steps_per_s": cells / el, "tuning": tune}
+    # spot members: single-instance FP32 and FP64 runs of the same states
+    single = [0.0, 0.0]
+    checks = []
+    for (k, j), (hf, uf) in finals.items():
+        g = grids[k]
+        h, u = states[k][j]
+        r32 = run(g, "fp32", h, u, dts[k], steps[k])
+        r64 = run(g, "fp64", h, u, dts[k], steps[k])
+        single[k] += r32["seconds"]
+        checks.append({"level": levels[k], "member": j,
+                       "h_vs_single_fp32": rel_errors(hf, r32["h"], g.hx_areag),
+                       "h_vs_fp64": rel_errors(hf, r64["h"], g.hx_areag),
+                       "u_vs_fp64": rel_errors(uf, r64["u"], _edge_w(g))})
+    out["checks"] = checks
+    # the same work as separate graph-launched single runs, from the spot
+    # members' timings (two per level)
+    out["separate_runs_estimate_s"] = (single[0] / 2.0) * len(seeds[0]) + \
+        (single[1] / 2.0) * len(seeds[1])
+    return out
+
+
+def _restrict_errors(r, ref, g):
+    return rel_errors(r["h"], ref["h"][: g.nv], g.hx_areag)
+
+
+def exp_mountains(args, pool):
+    from . import fields, swm
+    from .mesh import meshbuild
+    days = args.days or 10.0
+    gc, gf = meshbuild(8), meshbuild(9)
+    dtc, dtf = 108.0, 54.0
+    nc, nf = swm.ntime_for(days, dtc), swm.ntime_for(days, dtf)
+    ev = fields.PoolEvaluator(pool)
+    btc, btf = fields.gaussian_mountains(gc, seed=0), fields.gaussian_mountains(gf, seed=0)
+    hc, uc = fields.balanced_state(gc, lmax=64, seed=0, bt=btc, evaluator=ev)
+    hf, uf = fields.balanced_state(gf, lmax=64, seed=0, bt=btf, evaluator=ev)
+    ref = run(gf, "fp64", hf, uf, dtf, nf, bt=btf)
+    out = {"coarse": {"level": 8, "dt": dtc, "steps": nc},
+           "reference": dict(_summary(ref), level=9, dt=dtf, path="fp64")}
+    p = _params(args)
+    for path in ("fp64", "fp32", "fp32l"):
+        r = run(gc, path, hc, uc, dtc, nc, bt=btc, params=p)
+        # the topography is the same at the shared nodes: depth error =
+        # free-surface error
+        out[path] = dict(_summary(r), h_vs_l9_fp64=_restrict_errors(r, ref, gc))
+    return out
+
+
+def exp_fixed(args, pool):
+    from . import fields, swm
+    from .mesh import meshbuild
+    days = args.days or 10.0
+    lc = args.level or 9
+    gc, gf = meshbuild(lc), meshbuild(lc + 1)
+    dtc = args.dt or 54.0
+    dtf = dtc / 2.0
+    nc, nf = swm.ntime_for(days, dtc), swm.ntime_for(days, dtf)
+    ev = fields.PoolEvaluator(pool)
+    hc, uc = fields.balanced_state(gc, lmax=64, seed=0, evaluator=ev)
+    hf, uf = fields.balanced_state(gf, lmax=64, seed=0, evaluator=ev)
+    ref = run(gf, args.ref_precision, hf, uf, dtf, nf, chunk=2000)
+    out = {"coarse": {"level": lc, "dt": dtc, "steps": nc},
+           "reference": dict(_summary(ref), level=lc + 1, dt=dtf, path=args.ref_precision)}
+    p = _params(args)
+    for path in ("fp64", "fp32", "fp32l"):
+        r = run(gc, path, hc, uc, dtc, nc, params=p)
+        out[path] = dict(_summary(r), h_vs_ref=_restrict_errors(r, ref, gc))
+    out["speedup_fp32l_vs_fp64"] = (out["fp32l"]["cell_steps_per_s"] /
+                                    out["fp64"]["cell_steps_per_s"])
+    return out
+
+
+def exp_large(args, pool):
+    from . import fields, swm
+    from .mesh import meshbuild
+    g = meshbuild(10)
+    dt = 28.0
+    n = swm.ntime_for(args.days or 2.0, dt)
+    h, u = fields.balanced_state(g, lmax=256, seed=0, exponent=-3.0, umax=60.0,
+                                 evaluator=fields.PoolEvaluator(pool))
+    r64 = run(g, "fp64", h, u, dt, n, chunk=2000)
+    out = {"level": 10, "dt": dt, "steps": n, "fp64": _summary(r64)}
+    for path in ("fp32", "fp32l"):
+        r = run(g, path, h, u, dt, n, params=_params(args) if path == "fp32l" else None)
+        out[path] = dict(_summary(r), h_vs_fp64=rel_errors(r["h"], r64["h"], g.hx_areag),
+                         u_vs_fp64=rel_errors(r["u"], r64["u"], _edge_w(g)))
+    return out
+
+
+RUNS = {"tc2": exp_tc2, "balanced": exp_balanced, "ensemble": exp_ensemble,
+        "mountains": exp_mountains, "fixed": exp_fixed, "large": exp_large}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("runs", nargs="+", choices=sorted(RUNS))
+    ap.add_argument("--out", default="")
+    ap.add_argument("--days", type=float, default=0.0)
+    ap.add_argument("--level", type=int, default=0)
+    ap.add_argument("--dt", type=float, default=0.0)
+    ap.add_argument("--ref-precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--workers", type=int, default=0)
+    a = ap.parse_args(argv)
+    pool = _pool(a.workers)
+    results = {}
+    try:
+        for name in a.runs:
+            t0 = time.time()
+            results[name] = RUNS[name](a, pool)
+            results[name]["wall_s"] = time.time() - t0
+            print(json.dumps({name: results[name]}), flush=True)
+            if a.out:
+                with open(a.out, "w") as f:
+                    json.dump(results, f, indent=1)
+    finally:
+        pool.close()
+        pool.join()
+    return results
+
+
+if __name__ == "__main__":
+    main()

@@ -82,8 +82,9 @@ class Spectral:
         self.splA = CubicSpline(self.phi, A, axis=0)
         self.splB = CubicSpline(self.phi, B, axis=0)
 
-    def eval(self, lon, lat, dlat=False, dlon=False, chunk=262144):
+    def eval(self, lon, lat, dlat=False, dlon=False, chunk=0):
         """Field (or its latitude / longitude derivative) at points."""
+        chunk = chunk or max(4096, (1 << 24) // (self.lmax + 1))
         lon = np.asarray(lon, dtype=np.float64)
         lat = np.asarray(lat, dtype=np.float64)
         out = np.empty(lon.size)
@@ -171,28 +172,53 @@ def analyse_grid(f, lat, w, lon, lmax):
     return a, b
 
 
+def spectral_eval(a, b, lon, lat, mode: str = "f"):
+    """Synthesis at points: mode "f" (field), "dlat" or "dlon" (derivatives)."""
+    return Spectral(a, b).eval(lon, lat, dlat=mode == "dlat", dlon=mode == "dlon")
+
+
+def _eval_chunk(args):
+    a, b, lon, lat, mode = args
+    return spectral_eval(a, b, lon, lat, mode)
+
+
+class PoolEvaluator:
+    """spectral_eval split over a process pool by points (the same values as
+    the serial evaluation: every point is computed independently)."""
+
+    def __init__(self, pool, chunk: int = 1 << 20):
+        self.pool = pool
+        self.chunk = chunk
+
+    def __call__(self, a, b, lon, lat, mode="f"):
+        lon = np.asarray(lon, dtype=np.float64)
+        lat = np.asarray(lat, dtype=np.float64)
+        jobs = [(a, b, lon[s:s + self.chunk], lat[s:s + self.chunk], mode)
+                for s in range(0, lon.size, self.chunk)]
+        return np.concatenate(self.pool.map(_eval_chunk, jobs)) if jobs else np.empty(0)
+
+
 def balanced_state(grid: Grid, lmax: int = 64, seed: int = 0, exponent: float = -2.0,
                    umax: float = 40.0, gh0: float = 2.94e4, chi_fraction: float = 0.0,
-                   bt=None):
+                   bt=None, evaluator=None):
     """Seeded balanced (h, u) on the grid; see the module docstring.
 
     chi_fraction > 0 adds a divergent part grad(chi) whose coefficients are
     drawn with the same spectrum (seed + 1) and scaled to that fraction of
     the rotational part; the balance equation uses psi only.
     """
+    ev = evaluator or spectral_eval
     a, b = random_coeffs(lmax, seed, exponent)
-    sp = Spectral(a, b)
     elon = np.arctan2(grid.ed_c[:, 1], grid.ed_c[:, 0])
     elat = grid.ed_c_lat
     cosl = np.maximum(np.cos(elat), 1e-12)
     # u = k x grad psi : (u_lon, u_lat) = (-dpsi/dphi / a, dpsi/dlon / (a cos))
-    ulon = -sp.eval(elon, elat, dlat=True) / ERAD
-    ulat = sp.eval(elon, elat, dlon=True) / (ERAD * cosl)
+    ulon = -ev(a, b, elon, elat, "dlat") / ERAD
+    ulat = ev(a, b, elon, elat, "dlon") / (ERAD * cosl)
     if chi_fraction > 0:
         ac, bc = random_coeffs(lmax, seed + 1, exponent)
-        sc = Spectral(ac, bc)
-        dlon_c = sc.eval(elon, elat, dlon=True) / (ERAD * cosl)
-        dlat_c = sc.eval(elon, elat, dlat=True) / ERAD
+        dlon_c = ev(ac, bc, elon, elat, "dlon") / (ERAD * cosl)
+        dlat_c = ev(ac, bc, elon, elat, "dlat") / ERAD
         rot = np.sqrt(ulon ** 2 + ulat ** 2).max()
         div = np.sqrt(dlon_c ** 2 + dlat_c ** 2).max()
         k = chi_fraction * rot / max(div, 1e-300)
@@ -220,9 +246,8 @@ def balanced_state(grid: Grid, lmax: int = 64, seed: int = 0, exponent: float = 
     for l in range(1, lmax + 2):
         ha[l] = -ERAD ** 2 * ra[l] / (GRAV * l * (l + 1))
         hb[l] = -ERAD ** 2 * rb[l] / (GRAV * l * (l + 1))
-    hs = Spectral(ha, hb)
     vlon = np.arctan2(grid.v_p[:, 1], grid.v_p[:, 0])
-    h = gh0 / GRAV + scale * hs.eval(vlon, grid.v_lat)
+    h = gh0 / GRAV + scale * ev(ha, hb, vlon, grid.v_lat, "f")
     if bt is not None:
         h = h - bt
     return h, u

@@ -27,6 +27,8 @@ kernels that train and apply the network are in the CUDA library.
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 
 from . import fields
@@ -37,6 +39,7 @@ NVEL = 10
 NGEO = 14
 NFEAT = NVEL + NGEO
 HIDDEN = 64
+NPARAM = HIDDEN * NFEAT + HIDDEN + HIDDEN * HIDDEN + HIDDEN + HIDDEN + 1  # 5825
 
 
 def stencil(grid: Grid):
@@ -147,6 +150,21 @@ def init_params(seed: int = 0):
         rng.uniform(-a1, a1, HIDDEN * NFEAT), np.zeros(HIDDEN),
         rng.uniform(-a2, a2, HIDDEN * HIDDEN), np.zeros(HIDDEN),
         rng.uniform(-a3, a3, HIDDEN), np.zeros(1)]).astype(np.float32)
+
+
+TRAINED_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data",
+                            "trsk_mlp_l7.npy")
+
+
+def trained_params(path: str = TRAINED_PATH):
+    """Parameters trained by imodel_gb300.train_learned on icosahedral level 7
+    (256 seeded fields, degree <= 48); None when the file is absent."""
+    if not os.path.exists(path):
+        return None
+    p = np.load(path).astype(np.float32)
+    if p.shape != (NPARAM,):
+        raise ValueError(f"{path}: {p.shape} parameters, expected ({NPARAM},)")
+    return p
 
 
 def to_bf16_bits(a):

@@ -15,6 +15,7 @@ work.
 from __future__ import annotations
 
 import argparse
+import json
 import multiprocessing as mp
 import os
 import time
@@ -44,6 +45,28 @@ def build_training_set(level: int, seeds, lmax: int = 48, workers: int = 0):
     return tuple(np.concatenate([p[k] for p in parts]) for k in range(3))
 
 
+def evaluate(net, levels, lmax, seeds=(10**6 + 1, 10**6 + 2)):
+    """Relative L2 error of the tangential velocity, plain TRSK and corrected,
+    on fields the network has not seen, on each grid level."""
+    from imodel_gb300 import learned
+    from imodel_gb300.mesh import meshbuild
+    out = []
+    for level in levels:
+        g = meshbuild(level)
+        st = learned.stencil(g)
+        for seed in seeds:
+            u, ut = learned.velocity_sample(g, lmax=lmax, seed=seed)
+            plain = learned.trsk_tangent_np(g, u, st)
+            corr = learned.corrected_tangent(g, net, u, st)
+            e0 = float(np.sqrt(np.mean((plain - ut) ** 2) / np.mean(ut ** 2)))
+            e1 = float(np.sqrt(np.mean((corr - ut) ** 2) / np.mean(ut ** 2)))
+            out.append({"level": level, "seed": seed, "trsk": e0, "learned": e1,
+                        "gain": e0 / e1})
+            print(f"level {level} field {seed}: TRSK {e0:.3e} learned {e1:.3e} "
+                  f"gain {e0 / e1:.2f}", flush=True)
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--level", type=int, default=7)
@@ -69,6 +92,11 @@ def main(argv=None):
     print(f"trained {a.steps} Adam steps in {t2 - t1:.1f} s: loss {losses[:10].mean():.4f} -> "
           f"{losses[-10:].mean():.4f} (weighted target variance {np.mean(w * t * t):.4f})")
     p = net.get_params()
+    report = {"edges": int(x.shape[0]), "fields": a.fields, "level": a.level, "lmax": a.lmax,
+              "steps": a.steps, "batch": a.batch, "lr": a.lr, "train_s": t2 - t1,
+              "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-10:].mean()),
+              "eval": evaluate(net, [a.level, a.level + 1], a.lmax)}
+    print(json.dumps(report))
     if a.out:
         os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
         np.save(a.out, p)
