@@ -52,7 +52,13 @@ struct Handle {
   double drift_bound = 1e-3;
   double te_ref = 0.0;
   bool te_ref_set = false;
+  // state at the start of the current guard interval, restored when the
+  // interval ends past the drift bound (or with a non-finite energy)
+  float *ck_h = nullptr, *ck_u = nullptr;
 };
+
+// steps between two checks of the learned correction's energy drift
+constexpr int kGuardSteps = 32;
 
 #define CK(call)                                                                  \
   do {                                                                            \
@@ -151,7 +157,7 @@ int ensure_graph(Handle *H, double dt) {
 // host FP64 arrays (reference order) -> device state yn, plus h_ed and the
 // "last stage input" ya, as after the reference's initial tendency call
 // (swm.f90:214)
-int learned_guard(Handle *H);
+int learned_guard(Handle *H, bool *tripped = nullptr);
 
 // new_run: the state starts a new run (set_state), so the learned correction
 // is switched back on and its energy reference is taken again
@@ -248,9 +254,11 @@ int total_energy(Handle *H, double *te) {
 }
 
 // Fallback of the learned correction: once the relative drift of the total
-// energy since the state was set exceeds the bound, the plain TRSK scheme
-// takes over for the rest of the run.
-int learned_guard(Handle *H) {
+// energy since the state was set exceeds the bound (or the energy is not
+// finite), the plain TRSK scheme takes over for the rest of the run.
+// *tripped tells the caller that the guard switched the correction off.
+int learned_guard(Handle *H, bool *tripped) {
+  if (tripped) *tripped = false;
   if (!H->learned_active) return IMODEL_SWM_OK;
   double te = 0.0;
   int rc = total_energy(H, &te);
@@ -268,18 +276,51 @@ int learned_guard(Handle *H) {
       cudaGraphExecDestroy(H->graph);
       H->graph = nullptr;
     }
+    if (tripped) *tripped = true;
   }
   return IMODEL_SWM_OK;
 }
 
+int launch_steps(Handle *H, double dt, int nsteps) {
+  int rc = ensure_graph(H, dt);
+  if (rc) return rc;
+  for (int k = 0; k < nsteps; ++k) CK(cudaGraphLaunch(H->graph, H->stream));
+  return IMODEL_SWM_OK;
+}
+
+// With the learned correction on, the steps run in guard intervals: the
+// state is copied aside, the interval is stepped and the energy checked;
+// an interval that ends past the drift bound is rolled back and stepped
+// again with the plain scheme, so no corrected step that broke the bound
+// (or produced NaN) stays in the state.
 int advance(Handle *H, double dt, int nsteps) {
   if (!H->state_set) return set_error(H, IMODEL_SWM_ESTATE, "no state set");
   if (nsteps < 0 || !(std::isfinite(dt))) return set_error(H, IMODEL_SWM_EINVAL, "bad dt or nsteps");
   if (nsteps == 0) return IMODEL_SWM_OK;
-  int rc = ensure_graph(H, dt);
-  if (rc) return rc;
-  for (int k = 0; k < nsteps; ++k) CK(cudaGraphLaunch(H->graph, H->stream));
-  return learned_guard(H);
+  if (!H->learned_active) return launch_steps(H, dt, nsteps);
+  auto &W = H->W32;
+  const size_t bh = sizeof(float) * H->nv, bu = sizeof(float) * H->ne;
+  for (int done = 0; done < nsteps;) {
+    const int k = std::min(kGuardSteps, nsteps - done);
+    if (!H->learned_active) return launch_steps(H, dt, nsteps - done);
+    CK(cudaMemcpyAsync(H->ck_h, W.yn_h, bh, cudaMemcpyDeviceToDevice, H->stream));
+    CK(cudaMemcpyAsync(H->ck_u, W.yn_u, bu, cudaMemcpyDeviceToDevice, H->stream));
+    int rc = launch_steps(H, dt, k);
+    if (rc) return rc;
+    bool tripped = false;
+    if ((rc = learned_guard(H, &tripped))) return rc;
+    if (tripped) {
+      CK(cudaMemcpyAsync(W.yn_h, H->ck_h, bh, cudaMemcpyDeviceToDevice, H->stream));
+      CK(cudaMemcpyAsync(W.yn_u, H->ck_u, bu, cudaMemcpyDeviceToDevice, H->stream));
+      CK(cudaMemcpyAsync(W.ya_h, H->ck_h, bh, cudaMemcpyDeviceToDevice, H->stream));
+      CK(cudaMemcpyAsync(W.ya_u, H->ck_u, bu, cudaMemcpyDeviceToDevice, H->stream));
+      // flags raised by the rolled-back steps do not describe the state
+      CK(cudaMemsetAsync(H->d_flags, 0, sizeof(int), H->stream));
+      if ((rc = launch_steps(H, dt, k))) return rc;
+    }
+    done += k;
+  }
+  return IMODEL_SWM_OK;
 }
 
 int setup_learned(Handle *H, const imodel_swm_mesh *m, const Layout &L, const imodel_swm_opts *o) {
@@ -291,8 +332,12 @@ int setup_learned(Handle *H, const imodel_swm_mesh *m, const Layout &L, const im
   std::string msg = build_learned_layout(*m, L, LL);
   if (!msg.empty()) return set_error(H, IMODEL_SWM_EINVAL, msg);
   int rc;
+  H->learned.ne_pad = LL.ne_pad;
   if ((rc = upload(H, LL.lst, &H->learned.lst)) || (rc = upload(H, LL.geo, &H->learned.geo)) ||
-      (rc = dalloc(H, &H->learned.corr, static_cast<size_t>(L.ne))))
+      (rc = upload(H, LL.esh, &H->learned.esh)) || (rc = upload(H, LL.evs, &H->learned.evs)) ||
+      (rc = dalloc(H, &H->learned.corr, static_cast<size_t>(L.ne))) ||
+      (rc = dalloc(H, &H->ck_h, static_cast<size_t>(L.nv))) ||
+      (rc = dalloc(H, &H->ck_u, static_cast<size_t>(L.ne))))
     return rc;
   rc = learned_prepare(static_cast<const float *>(o->mlp_weights), &H->learned, H->stream);
   if (H->learned.p) H->allocs.push_back(H->learned.p);

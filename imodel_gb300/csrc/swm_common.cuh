@@ -83,8 +83,11 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
 struct LearnedDev {
   float *p = nullptr;        // FP32 parameters
   uint16_t *img = nullptr;   // BF16 weight images
-  const int32_t *lst = nullptr;
-  const uint16_t *geo = nullptr;
+  int64_t ne_pad = 0;        // edges rounded up to whole 128-edge tiles
+  const int32_t *lst = nullptr;   // [10][ne_pad]
+  const uint16_t *geo = nullptr;  // [ne_pad][16]
+  const int32_t *esh = nullptr;   // [2][ne_pad]
+  const uint32_t *evs = nullptr;  // [ne_pad][2]
   float *corr = nullptr;     // [ne]
   int sms = 0;
 };

@@ -28,9 +28,29 @@ namespace {
 
 constexpr int kMaxGrids = 8;
 
+// Division of 0 <= n < 2^31 by an invariant d >= 1 with one multiply-high
+// (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994, fig. 4.1): l = ceil(log2 d),
+// m = floor(2^32 (2^l - d) / d) + 1, n / d = (umulhi(m, n) + n) >> l; the sum
+// cannot overflow 32 bits for n < 2^31.
+struct FastDiv {
+  uint32_t m = 1, l = 0;
+  __device__ __forceinline__ int operator()(int n) const {
+    const uint32_t u = static_cast<uint32_t>(n);
+    return static_cast<int>((__umulhi(m, u) + u) >> l);
+  }
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+  FastDiv f;
+  while ((1ull << f.l) < d) ++f.l;
+  f.m = static_cast<uint32_t>(((1ull << 32) * ((1ull << f.l) - d)) / d + 1);
+  return f;
+}
+
 struct GridDev {
   DevMesh M;
   int members;
+  FastDiv per_member;  // entity index = item / members
   float h_ref;
   int nsteps;  // steps this launch
   float dt;
@@ -86,72 +106,60 @@ __device__ __forceinline__ bool steps_now(int s, int n, int S) {
   return (static_cast<long long>(s + 1) * n) / S > (static_cast<long long>(s) * n) / S;
 }
 
-__global__ void __launch_bounds__(512) k_ensemble(EnsArgs A) {
+// MINB = 1: registers as the compiler likes them; MINB = 2: capped at 64 per
+// thread for twice the resident warps (the tuner times both)
+template <int MINB>
+__global__ void __launch_bounds__(512, MINB) k_ensemble(EnsArgs A) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthr = gridDim.x * blockDim.x;
   for (int s = 0; s < A.macro_steps; ++s) {
     bool on[kMaxGrids];
-    long long ntri = 0, ncell = 0, nedge = 0;
-    for (int k = 0; k < A.ngrids; ++k) {
-      on[k] = steps_now(s, A.g[k].nsteps, A.macro_steps);
-      if (on[k]) {
-        ntri += static_cast<long long>(A.g[k].M.nt) * A.g[k].members;
-        ncell += static_cast<long long>(A.g[k].M.nv) * A.g[k].members;
-        nedge += static_cast<long long>(A.g[k].M.ne) * A.g[k].members;
-      }
-    }
+    for (int k = 0; k < A.ngrids; ++k) on[k] = steps_now(s, A.g[k].nsteps, A.macro_steps);
     for (int st = 0; st < 4; ++st) {
+      // Each phase walks the grids that step now; item r of a grid is
+      // entity r / members, member r % members (all counts < 2^31).
       // phase 1: potential vorticity at triangles
-      for (long long it = tid; it < ntri; it += nthr) {
-        long long r = it;
-        int k = 0;
-        for (; k < A.ngrids; ++k) {
-          if (!on[k]) continue;
-          const long long n = static_cast<long long>(A.g[k].M.nt) * A.g[k].members;
-          if (r < n) break;
-          r -= n;
-        }
+      for (int k = 0; k < A.ngrids; ++k) {
+        if (!on[k]) continue;
         const GridDev &G = A.g[k];
-        const int t = static_cast<int>(r / G.members), m = static_cast<int>(r % G.members);
         const float *hin = st == 0 ? G.yn_h : (st == 2 ? G.yb_h : G.ya_h);
         const float *uin = st == 0 ? G.yn_u : (st == 2 ? G.yb_u : G.ya_u);
-        tri_body<Member, LdL2>(G.M, t, Member{G.members, m}, hin, uin, G.q_tr, G.h_ref, A.pv_on, A.flags);
+        const int n = G.M.nt * G.members;
+        for (int r = tid; r < n; r += nthr) {
+          const int t = G.per_member(r), m = r - t * G.members;
+          tri_body<Member, LdL2>(G.M, t, Member{G.members, m}, hin, uin, G.q_tr, G.h_ref,
+                                 A.pv_on, A.flags);
+        }
       }
       if (!grid_barrier(A)) return;
       // phase 2: cells
-      for (long long it = tid; it < ncell; it += nthr) {
-        long long r = it;
-        int k = 0;
-        for (; k < A.ngrids; ++k) {
-          if (!on[k]) continue;
-          const long long n = static_cast<long long>(A.g[k].M.nv) * A.g[k].members;
-          if (r < n) break;
-          r -= n;
-        }
+      for (int k = 0; k < A.ngrids; ++k) {
+        if (!on[k]) continue;
         const GridDev &G = A.g[k];
-        const int i = static_cast<int>(r / G.members), m = static_cast<int>(r % G.members);
         const float *hin = st == 0 ? G.yn_h : (st == 2 ? G.yb_h : G.ya_h);
         const float *uin = st == 0 ? G.yn_u : (st == 2 ? G.yb_u : G.ya_u);
         float *hout = st == 0 ? G.ya_h : (st == 1 ? G.yb_h : (st == 2 ? G.ya_h : G.yn_h));
-        cell_body<Member, LdL2>(G.M, i, Member{G.members, m}, hin, uin, G.q_tr, G.bern, G.zflux, G.yn_h,
-                  G.acc_h, hout, nullptr, st, G.dt, static_cast<float>(G.M.grav), G.h_ref);
+        const int n = G.M.nv * G.members;
+        for (int r = tid; r < n; r += nthr) {
+          const int i = G.per_member(r), m = r - i * G.members;
+          cell_body<Member, LdL2>(G.M, i, Member{G.members, m}, hin, uin, G.q_tr, G.bern,
+                                  G.zflux, G.yn_h, G.acc_h, hout, nullptr, st, G.dt,
+                                  static_cast<float>(G.M.grav), G.h_ref);
+        }
       }
       if (!grid_barrier(A)) return;
       // phase 3: edges
-      for (long long it = tid; it < nedge; it += nthr) {
-        long long r = it;
-        int k = 0;
-        for (; k < A.ngrids; ++k) {
-          if (!on[k]) continue;
-          const long long n = static_cast<long long>(A.g[k].M.ne) * A.g[k].members;
-          if (r < n) break;
-          r -= n;
-        }
+      for (int k = 0; k < A.ngrids; ++k) {
+        if (!on[k]) continue;
         const GridDev &G = A.g[k];
-        const int e = static_cast<int>(r / G.members), m = static_cast<int>(r % G.members);
         float *uout = st == 0 ? G.ya_u : (st == 1 ? G.yb_u : (st == 2 ? G.ya_u : G.yn_u));
-        edge_body<Member, LdL2>(G.M, e, Member{G.members, m}, __ldg(&G.M.e_vs2[e]), G.bern, G.zflux, G.yn_u,
-                  G.acc_u, uout, nullptr, st, G.dt, A.mom_on, static_cast<float>(G.M.erad));
+        const int n = G.M.ne * G.members;
+        for (int r = tid; r < n; r += nthr) {
+          const int e = G.per_member(r), m = r - e * G.members;
+          edge_body<Member, LdL2>(G.M, e, Member{G.members, m}, __ldg(&G.M.e_vs2[e]), G.bern,
+                                  G.zflux, G.yn_u, G.acc_u, uout, nullptr, st, G.dt, A.mom_on,
+                                  static_cast<float>(G.M.erad));
+        }
       }
       if (!grid_barrier(A)) return;
     }
@@ -196,7 +204,7 @@ struct Ens {
   int *flags = nullptr;
   int *h_flags = nullptr;
   cudaStream_t stream = nullptr;
-  int block = 256, blocks_per_sm = 0;
+  int block = 256, blocks_per_sm = 0, variant = 0;
   bool any_state = false;
 };
 
@@ -286,6 +294,7 @@ int ens_create(Ens *E, const imodel_swm_mesh *meshes, int ngrids, const int32_t 
     G.edge_n2o = const_cast<int32_t *>(en2o);
     GridDev &W = G.dev;
     W.members = G.members;
+    W.per_member = make_fastdiv(static_cast<uint32_t>(G.members));
     float **bv[] = {&W.yn_h, &W.ya_h, &W.yb_h, &W.acc_h, &W.bern};
     for (float **b : bv)
       if ((rc = zalloc(E, b, static_cast<size_t>(L.nv) * M))) return rc;
@@ -314,7 +323,13 @@ int ens_flags(Ens *E) {
   return IMODEL_SWM_OK;
 }
 
-int ens_launch(Ens *E, const double *dt, const int32_t *nsteps, int block, int bps) {
+inline const void *ens_kernel(int variant) {
+  return variant == 1 ? reinterpret_cast<const void *>(k_ensemble<2>)
+                      : reinterpret_cast<const void *>(k_ensemble<1>);
+}
+
+int ens_launch(Ens *E, const double *dt, const int32_t *nsteps, int block, int bps,
+               int variant) {
   EnsArgs A;
   std::memset(&A, 0, sizeof(A));
   A.ngrids = E->ngrids;
@@ -338,12 +353,12 @@ int ens_launch(Ens *E, const double *dt, const int32_t *nsteps, int block, int b
   EK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   EK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
   if (!coop) return fail(E, IMODEL_SWM_ECUDA, "device does not support cooperative launch");
-  EK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_ensemble, block, 0));
+  EK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ens_kernel(variant), block, 0));
   if (occ < 1) return fail(E, IMODEL_SWM_ECUDA, "ensemble kernel does not fit an SM");
   const int per_sm = (bps > 0 && bps <= occ) ? bps : occ;
   EK(cudaMemsetAsync(E->bar, 0, 2 * sizeof(unsigned), E->stream));
   void *args[] = {&A};
-  EK(cudaLaunchCooperativeKernel(reinterpret_cast<void *>(k_ensemble), dim3(sms * per_sm),
+  EK(cudaLaunchCooperativeKernel(ens_kernel(variant), dim3(sms * per_sm),
                                  dim3(block), args, 0, E->stream));
   return IMODEL_SWM_OK;
 }
@@ -426,12 +441,12 @@ int imodel_swm_ensemble_advance(void *ens, const double *dt, const int32_t *nste
   if (!E || !dt || !nsteps) return IMODEL_SWM_EINVAL;
   if (!E->any_state) return imodel::fail(E, IMODEL_SWM_ESTATE, "no state set");
   if (cudaSetDevice(E->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
-  int rc = imodel::ens_launch(E, dt, nsteps, E->block, E->blocks_per_sm);
+  int rc = imodel::ens_launch(E, dt, nsteps, E->block, E->blocks_per_sm, E->variant);
   if (rc) return rc;
   return imodel::ens_flags(E);
 }
 
-int imodel_swm_ensemble_tune(void *ens, const double *dt, int32_t nsteps, int32_t choice[2]) {
+int imodel_swm_ensemble_tune(void *ens, const double *dt, int32_t nsteps, int32_t choice[3]) {
   Ens *E = static_cast<Ens *>(ens);
   if (!E || !dt || !choice || nsteps <= 0) return IMODEL_SWM_EINVAL;
   if (!E->any_state) return imodel::fail(E, IMODEL_SWM_ESTATE, "no state set");
@@ -461,28 +476,30 @@ int imodel_swm_ensemble_tune(void *ens, const double *dt, int32_t nsteps, int32_
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
-  int bb = E->block, bbps = E->blocks_per_sm;
+  int bb = E->block, bbps = E->blocks_per_sm, bv = E->variant;
   int rc = IMODEL_SWM_OK;
   const int blocks[3] = {128, 256, 512};
-  for (int b : blocks) {
-    int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, imodel::k_ensemble, b, 0);
-    for (int bps = occ; bps >= 1 && rc == IMODEL_SWM_OK; bps = bps > 1 ? bps / 2 : 0) {
-      cudaEventRecord(e0, E->stream);
-      rc = imodel::ens_launch(E, dt, ns.data(), b, bps);
-      cudaEventRecord(e1, E->stream);
-      if (rc) break;
-      rc = imodel::ens_flags(E);
-      float ms = 1e30f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      if (rc == IMODEL_SWM_OK && ms < best) {
-        best = ms;
-        bb = b;
-        bbps = bps;
+  for (int v = 0; v < 2 && rc == IMODEL_SWM_OK; ++v)
+    for (int b : blocks) {
+      int occ = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, imodel::ens_kernel(v), b, 0);
+      for (int bps = occ; bps >= 1 && rc == IMODEL_SWM_OK; bps = bps > 1 ? bps / 2 : 0) {
+        cudaEventRecord(e0, E->stream);
+        rc = imodel::ens_launch(E, dt, ns.data(), b, bps, v);
+        cudaEventRecord(e1, E->stream);
+        if (rc) break;
+        rc = imodel::ens_flags(E);
+        float ms = 1e30f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rc == IMODEL_SWM_OK && ms < best) {
+          best = ms;
+          bb = b;
+          bbps = bps;
+          bv = v;
+        }
+        if (bps == 1) break;
       }
-      if (bps == 1) break;
     }
-  }
   for (size_t q = 0; q < bufs.size(); ++q)
     cudaMemcpyAsync(bufs[q], saved[q], sizes[q], cudaMemcpyDeviceToDevice, E->stream);
   cudaStreamSynchronize(E->stream);
@@ -492,8 +509,10 @@ int imodel_swm_ensemble_tune(void *ens, const double *dt, int32_t nsteps, int32_
   if (rc) return rc;
   E->block = bb;
   E->blocks_per_sm = bbps;
+  E->variant = bv;
   choice[0] = bb;
   choice[1] = bbps;
+  choice[2] = bv;
   return IMODEL_SWM_OK;
 }
 

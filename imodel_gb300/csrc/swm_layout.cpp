@@ -332,9 +332,18 @@ uint16_t bf16_bits(float v) {
 // for both cells and 20 (w - (r/n - 1/2)) for the 10 weights.
 std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, LearnedLayout &LL) {
   const int ne = m.ne;
-  const size_t NE = ne;
+  const size_t NE = (static_cast<size_t>(ne) + 127) / 128 * 128;
+  LL.ne_pad = static_cast<int64_t>(NE);
   LL.lst.assign(10 * NE, 0);
   LL.geo.assign(16 * NE, 0);
+  LL.esh.assign(2 * NE, 0);
+  LL.evs.assign(2 * NE, 0);
+  for (size_t e = 0; e < static_cast<size_t>(ne); ++e) {
+    LL.esh[e] = L.e_sh[e];
+    LL.esh[NE + e] = L.e_sh[static_cast<size_t>(ne) + e];
+    LL.evs[2 * e] = L.e_vs2[2 * e];
+    LL.evs[2 * e + 1] = L.e_vs2[2 * e + 1];
+  }
   double lmean = 0.0;
   for (int e = 0; e < ne; ++e) lmean += m.ed_leng[e];
   lmean /= ne;

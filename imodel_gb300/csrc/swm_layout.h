@@ -92,9 +92,15 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L);
 // order: per edge the 10 stencil edges as sign * (index + 1) (0 = padding),
 // slot-major [10][ne], and the 14 geometry inputs as BF16 bit patterns,
 // [ne][16] (two zero pads, 32 bytes per edge).
+// Inputs of the learned correction, padded to ne_pad = ne rounded up to 128
+// edges so that every 128-edge tile is one bulk copy per array (padding:
+// empty stencil slots, zero geometry, triangle and cell 0).
 struct LearnedLayout {
-  std::vector<int32_t> lst;
-  std::vector<uint16_t> geo;
+  int64_t ne_pad = 0;
+  std::vector<int32_t> lst;   // [10][ne_pad] sign * (edge + 1), 0 = empty slot
+  std::vector<uint16_t> geo;  // [ne_pad][16] BF16 geometry inputs
+  std::vector<int32_t> esh;   // [2][ne_pad] triangles of the edge
+  std::vector<uint32_t> evs;  // [ne_pad][2] cell words of the edge
 };
 std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, LearnedLayout &LL);
 

@@ -70,13 +70,16 @@ def run(grid, path, h, u, dt, nsteps, bt=None, params=None, chunk=0):
             m.autotune(dt, 3)
             m.set_state(h, u)
         d0 = m.diagnostics()
-        chunk = chunk or nsteps
+        # the learned path reports when its drift guard switched it off
+        chunk = chunk or (256 if path == "fp32l" else nsteps)
         t0 = time.perf_counter()
-        done = 0
+        done, off_at = 0, None
         while done < nsteps:
             k = min(chunk, nsteps - done)
             m.advance(dt, k)
             done += k
+            if path == "fp32l" and off_at is None and not m.diagnostics()["learned_active"]:
+                off_at = done
         el = time.perf_counter() - t0
         d1 = m.diagnostics()
         hf, uf = m.get_state()
@@ -86,11 +89,12 @@ def run(grid, path, h, u, dt, nsteps, bt=None, params=None, chunk=0):
     return {"h": hf, "u": uf, "seconds": el, "steps": nsteps,
             "cell_steps_per_s": grid.nv * nsteps / el,
             "mass_change": rel("mass"), "tenergy_change": rel("tenergy"),
-            "learned_active": bool(d1["learned_active"]), "nan": bool(d1["nan_found"])}
+            "learned_active": bool(d1["learned_active"]), "nan": bool(d1["nan_found"]),
+            "learned_off_by_step": off_at}
 
 
 def _summary(r, keep=("seconds", "steps", "cell_steps_per_s", "mass_change", "tenergy_change",
-                      "learned_active")):
+                      "learned_active", "learned_off_by_step")):
     return {k: r[k] for k in keep}
 
 

@@ -39,6 +39,8 @@ NVEL = 10
 NGEO = 14
 NFEAT = NVEL + NGEO
 HIDDEN = 64
+# bound of the network output (error / sigma) applied in the step
+CORR_MAX = 0.5
 NPARAM = HIDDEN * NFEAT + HIDDEN + HIDDEN * HIDDEN + HIDDEN + HIDDEN + 1  # 5825
 
 
@@ -300,12 +302,14 @@ def training_set(grid: Grid, seeds, lmax: int = 48, chi_fraction: float = 0.5,
 
 
 def corrected_tangent(grid: Grid, mlp: Mlp, u, st=None):
-    """TRSK tangential velocity plus the network's predicted error."""
+    """TRSK tangential velocity plus the network's predicted error, clipped
+    to +-CORR_MAX sigma as in the step."""
     if st is None:
         st = stencil(grid)
     utg = trsk_tangent_np(grid, u, st)
     x, sigma = features(grid, u, st)
-    return utg + sigma * mlp.forward(to_bf16_bits(x)).astype(np.float64)
+    y = np.clip(mlp.forward(to_bf16_bits(x)).astype(np.float64), -CORR_MAX, CORR_MAX)
+    return utg + sigma * y
 
 
 def trsk_tangent_np(grid: Grid, u, st=None):

@@ -329,10 +329,10 @@ class Ensemble:
 
     def tune(self, dt, nsteps: int = 3) -> dict:
         dt = np.ascontiguousarray(dt, dtype=np.float64)
-        c = np.zeros(2, dtype=np.int32)
+        c = np.zeros(3, dtype=np.int32)
         self._check(self.lib.imodel_swm_ensemble_tune(self._handle, _capi.as_f64p(dt), nsteps,
                                                       _capi.as_i32p(c)))
-        return {"block": int(c[0]), "blocks_per_sm": int(c[1])}
+        return {"block": int(c[0]), "blocks_per_sm": int(c[1]), "variant": int(c[2])}
 
     def stream(self) -> int:
         return self.lib.imodel_swm_ensemble_stream(self._handle) or 0

@@ -205,9 +205,11 @@ int imodel_swm_ensemble_get_state(void *ens, int32_t grid, int32_t member, doubl
 /* dt[ngrids] seconds and nsteps[ngrids] RK4 steps per grid, one launch. */
 int imodel_swm_ensemble_advance(void *ens, const double *dt, const int32_t *nsteps);
 /* Autotuner of the persistent launch: times nsteps steps per grid for each
- * block size and blocks-per-SM count, keeps the fastest, restores the state.
- * choice = {block size, blocks per SM}. */
-int imodel_swm_ensemble_tune(void *ens, const double *dt, int32_t nsteps, int32_t choice[2]);
+ * kernel variant (0: registers unconstrained, 1: at most 64 registers per
+ * thread for more resident warps), block size and blocks-per-SM count, keeps
+ * the fastest, restores the state.
+ * choice = {block size, blocks per SM, variant}. */
+int imodel_swm_ensemble_tune(void *ens, const double *dt, int32_t nsteps, int32_t choice[3]);
 int imodel_swm_ensemble_destroy(void *ens);
 const char *imodel_swm_ensemble_last_error(void *ens);
 void *imodel_swm_ensemble_stream(void *ens);

@@ -1,7 +1,7 @@
 """CPU oracle of the learned TRSK correction network (test infrastructure).
 
 A numpy restatement of the network the CUDA kernels train and apply:
-24 -> 64 -> 64 -> 1 with GELU (erf form), BF16 inputs and weights for the two
+24 -> 64 -> 64 -> 1 with GELU (tanh form), BF16 inputs and weights for the two
 matrix products with FP32 accumulation, FP32 third layer, mean-squared-error
 loss and Adam.  The rounding points follow the kernels: the inputs x, the
 weights W1 and W2, the first hidden layer before the second product, and the
