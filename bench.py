@@ -325,8 +325,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-kprof", action="store_true")
     ap.add_argument("--tuning", default="",
-                    help="FP32 launch choice 'variant,bs_tri,bs_pre,bs_cell,bs_edge' "
-                         "instead of autotuning")
+                    help="FP32 launch choice 'variant,bs_tri,bs_pre,bs_cell,bs_edge"
+                         "[,mlp_gather]' instead of autotuning")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -359,7 +359,7 @@ def main():
             if args.tuning:
                 c = [int(x) for x in args.tuning.split(",")]
                 m.set_tuning(*c)
-                tuning = dict(zip(("variant", "bs_tri", "bs_pre", "bs_cell", "bs_edge"), c))
+                tuning = dict(zip(swm.TUNING_KEYS, c))
             else:
                 tuning = m.autotune(DT, 5)
         stream = m.stream()

@@ -112,14 +112,16 @@ __device__ __forceinline__ uint64_t f2fma(uint64_t a, uint64_t b, uint64_t c) {
   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
   return r;
 }
-// gelu of the pair z = (z0, z1) + (b0, b1), lane by lane as gelu() above
-__device__ __forceinline__ uint64_t gelu2(float z0, float z1, float b0, float b1) {
+// TWICE the gelu of the pair z = (z0, z1) + (b0, b1), lane by lane:
+// z + z tanh(u) = 2 gelu(z) exactly (the halving in gelu() is exact), so the
+// forward kernel halves the weights that multiply it instead (W2 and w3, also
+// exact) and saves one multiply per pair
+__device__ __forceinline__ uint64_t gelu2x2(float z0, float z1, float b0, float b1) {
   const uint64_t z = f2add(f2pk(z0, z1), f2pk(b0, b1));
   const uint64_t u = f2mul(f2fma(f2mul(z, z), f2pk(kGca, kGca), f2pk(kGc, kGc)), z);
   float u0, u1;
   f2upk(u, u0, u1);
-  const uint64_t hz = f2mul(z, f2pk(0.5f, 0.5f));
-  return f2fma(hz, f2pk(tanh_fast(u0), tanh_fast(u1)), hz);
+  return f2fma(z, f2pk(tanh_fast(u0), tanh_fast(u1)), z);
 }
 
 // row `r` of a K-major 16-bit operand with `kc` columns, from 64 FP32 values
@@ -513,14 +515,18 @@ int learned_prepare(const float *params_host, LearnedDev *L, cudaStream_t s) {
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&L->sms, cudaDevAttrMultiProcessorCount, dev);
-  if (cudaFuncSetAttribute(pipe::k_mlp_pipe<pipe::EdgeTask>,
+  if (cudaFuncSetAttribute(pipe::k_mlp_pipe<pipe::EdgeTask, 2>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, pipe::SMEM) != cudaSuccess ||
+      cudaFuncSetAttribute(pipe::k_mlp_pipe<pipe::EdgeTask, 3>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, pipe::SMEM) != cudaSuccess ||
+      cudaFuncSetAttribute(pipe::k_mlp_pipe<pipe::EdgeTask, 4>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, pipe::SMEM) != cudaSuccess)
     return IMODEL_SWM_ECUDA;
   return IMODEL_SWM_OK;
 }
 
 void learned_launch(const DevMesh &M, const LearnedDev &L, const float *hd, const float *u,
-                    const float *q_tr, float h_ref, int *err, cudaStream_t s) {
+                    const float *q_tr, float h_ref, int gather_groups, int *err, cudaStream_t s) {
   Weights W;
   W.w1img = L.img;
   W.w2img = L.img + NH * K1;
@@ -529,8 +535,13 @@ void learned_launch(const DevMesh &M, const LearnedDev &L, const float *hd, cons
   const int64_t ne = M.ne;
   const int64_t ntiles = (ne + TM - 1) / TM;
   const int nblk = static_cast<int>(std::min<int64_t>(ntiles, L.sms > 0 ? L.sms : 1));
-  pipe::EdgeTask task{L.lst, L.geo, L.esh, L.evs, L.ne_pad, u, q_tr, hd, h_ref, L.corr};
-  pipe::k_mlp_pipe<pipe::EdgeTask><<<nblk, pipe::THREADS, pipe::SMEM, s>>>(W, ne, task, err);
+  pipe::EdgeTask task{L.blocks, u, q_tr, hd, h_ref, L.corr};
+  if (gather_groups == 2)
+    pipe::k_mlp_pipe<pipe::EdgeTask, 2><<<nblk, pipe::THREADS, pipe::SMEM, s>>>(W, ne, task, err);
+  else if (gather_groups == 3)
+    pipe::k_mlp_pipe<pipe::EdgeTask, 3><<<nblk, pipe::THREADS, pipe::SMEM, s>>>(W, ne, task, err);
+  else
+    pipe::k_mlp_pipe<pipe::EdgeTask, 4><<<nblk, pipe::THREADS, pipe::SMEM, s>>>(W, ne, task, err);
 }
 
 }  // namespace imodel
@@ -553,7 +564,7 @@ int imodel_mlp_create(int32_t device, void **mlp) {
   MK(cudaDeviceGetAttribute(&P->sms, cudaDevAttrMultiProcessorCount, device));
   MK(cudaFuncSetAttribute(imodel::k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           imodel::TRN_SMEM));
-  MK(cudaFuncSetAttribute(imodel::pipe::k_mlp_pipe<imodel::pipe::RowsTask>,
+  MK(cudaFuncSetAttribute(imodel::pipe::k_mlp_pipe<imodel::pipe::RowsTask, 2>,
                           cudaFuncAttributeMaxDynamicSharedMemorySize, imodel::pipe::SMEM));
   MK(cudaMalloc(&P->p, imodel::NPART * sizeof(float)));
   MK(cudaMalloc(&P->m, imodel::NPART * sizeof(float)));
@@ -607,7 +618,8 @@ int imodel_mlp_forward(void *mlp, const uint16_t *x, int64_t n, float *y) {
   if (e == cudaSuccess) {
     const int64_t ntiles = (n + imodel::TM - 1) / imodel::TM;
     const int nblk = static_cast<int>(std::min<int64_t>(ntiles, P->sms));
-    imodel::pipe::k_mlp_pipe<imodel::pipe::RowsTask>
+    // rows need no gathers: two gather groups, four epilogue groups
+    imodel::pipe::k_mlp_pipe<imodel::pipe::RowsTask, 2>
         <<<nblk, imodel::pipe::THREADS, imodel::pipe::SMEM, P->stream>>>(
             imodel::weights(P), n, imodel::pipe::RowsTask{dx, dy}, P->d_err);
     e = cudaGetLastError();

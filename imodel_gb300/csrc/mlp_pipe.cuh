@@ -1,26 +1,32 @@
 // Pipelined forward pass of the per-edge MLP (internal header of mlp.cu).
 //
 // One persistent CTA per SM, warp-specialised:
-//   warps  0..15  four gather groups: each turns the prefetched index block of
+//   NG groups     gather groups (warps 0 .. 4 NG - 1): each turns the index block of
 //                 one tile of 128 rows into the tile's BF16 input operand
 //                 (the dependent gathers of velocities etc.) and one FP32
 //                 context value per row
-//   warps 16..23  two epilogue groups: TMEM -> registers, bias + GELU, the
+//   6 - NG groups epilogue groups: TMEM -> registers, bias + GELU, the
 //                 BF16 hidden layer back to shared memory, and after the
 //                 second product the final GELU . w3 + b3 and the output
+//                 (2 GELU is formed, with W2 and w3 halved: exact)
 //   warp  24      one thread runs an event loop that issues the bulk copies
 //                 (TMA, cp.async.bulk) of each tile's index block and the
 //                 tcgen05 MMAs of both layers
 // Shared memory holds NPF prefetched index blocks, NSTAGE input operands
 // (8 KiB each), NSLOT hidden-layer operands (16 KiB each); TMEM holds NSLOT
-// tiles in flight, 128 columns each: columns 0..63 the first layer's
-// accumulator, 64..127 the second's.  Every hand-off is an mbarrier; every
-// wait is bounded and gives up once any role has raised the CTA's abort flag,
-// so a stuck pipeline ends with an error flag, never a hang.
+// tiles in flight, SLOTW = 80 columns each.  The first product has N = 80:
+// columns 0..63 are the hidden units and column 64 carries the row's context
+// value through the tensor core (the gather writes it as a BF16 pair hi + lo
+// into the zero-padded input columns 24 and 25, and output row 64 of the
+// layer-1 operand holds ones there), so it needs no ring buffer of its own;
+// the second product overwrites columns 0..63 once the first epilogue has
+// read them.  Every hand-off is an mbarrier; every wait is bounded and gives
+// up once any role has raised the CTA's abort flag, so a stuck pipeline ends
+// with an error flag, never a hang.
 //
 // Tile i of this CTA (global tile blockIdx.x + i * gridDim.x) uses
-//   index block  i % NPF,   input stage  i % NSTAGE  (gather group i % NGATHER),
-//   TMEM slot    i % NSLOT  (epilogue group i % NEPI),  context entry i % NCTX.
+//   index block  i % NPF,   input stage  i % NSTAGE  (gather group i % NG),
+//   TMEM slot    i % NSLOT  (epilogue group i % NE).
 // Phase parities: the j-th completion of a barrier is awaited with parity
 // j & 1; a producer waiting for the consumer's (j-1)-th release waits with
 // parity (j & 1) ^ 1, which a fresh barrier satisfies at once for j = 0.
@@ -31,15 +37,20 @@ namespace pipe {
 
 using namespace tc05;
 
-constexpr int NGATHER = 4, NEPI = 2, NSTAGE = 8, NSLOT = 4, NCTX = 16, NPF = 4;
-constexpr int WARPS = NGATHER * 4 + NEPI * 4 + 1;
+// NGROUPS warp groups of 4 warps are split between gathering (NG) and the
+// epilogue (NGROUPS - NG); the split is a tuning choice (2, 3 or 4 gather
+// groups), the thread count and register budget are the same for all.
+constexpr int NGROUPS = 6, NSTAGE = 4, NSLOT = 6, NPF = 4;
+constexpr int N1 = 80, SLOTW = 80;  // layer-1 outputs: 64 hidden units, context, padding
+constexpr int WARPS = NGROUPS * 4 + 1;
 constexpr int THREADS = WARPS * 32;
 constexpr int PF_BYTES = 11264;  // largest index block of a task
-// dynamic shared memory: B1 4K | B2 8K | A1 ring 64K | A2 slots 64K | ctx 8K |
+// dynamic shared memory: B1 5K | B2 8K | A1 ring 32K | A2 slots 96K |
 // index blocks 44K
-constexpr int OFF_B1S = 0, OFF_B2S = 4096, OFF_A1S = 12288, OFF_A2S = OFF_A1S + NSTAGE * 8192,
-              OFF_CTX = OFF_A2S + NSLOT * 16384, OFF_PF = OFF_CTX + NCTX * 128 * 4,
+constexpr int OFF_B1S = 0, OFF_B2S = N1 * K1 * 2, OFF_A1S = OFF_B2S + 8192,
+              OFF_A2S = OFF_A1S + NSTAGE * 8192, OFF_PF = OFF_A2S + NSLOT * 16384,
               SMEM = OFF_PF + NPF * PF_BYTES;
+static_assert(NSLOT * SLOTW <= 512, "TMEM has 512 columns");
 static_assert(SMEM > 116 * 1024, "more than half of an SM's shared memory: one CTA per SM");
 static_assert(SMEM <= 220 * 1024, "fits the 227 KiB an SM offers one CTA");
 constexpr int ERR_PIPE = 16;
@@ -133,27 +144,44 @@ __device__ __forceinline__ void ld32(uint32_t taddr, float (&v)[32]) {
 //   float stage(row, live, idx, c[4])       the row's BF16 inputs -> c, returns
 //                                           the context value of the row
 //   void write(row, y, ctx)                 consumes the network output
-template <class Task>
+template <class Task, int NG>
 __global__ void __launch_bounds__(THREADS, 1)
     k_mlp_pipe(Weights W, int64_t n, Task task, int *err) {
+  constexpr int NE = NGROUPS - NG;
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ Bars bar;
   __shared__ uint32_t tslot;
   __shared__ int abort_flag;
   __shared__ __align__(16) float sb1[NH], sb2[NH], sw3[NH];
   uint8_t *B1s = smem + OFF_B1S, *B2s = smem + OFF_B2S;
-  float *ctx = reinterpret_cast<float *>(smem + OFF_CTX);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   volatile int *abort = &abort_flag;
 
+  // layer-1 operand: W1 (rows 0..63) and the context row 64 (ones in input
+  // columns 24 and 25), rows 65..79 zero
   for (int i = tid; i < 4096 / 16; i += THREADS)
     reinterpret_cast<uint4 *>(B1s)[i] = reinterpret_cast<const uint4 *>(W.w1img)[i];
-  for (int i = tid; i < 8192 / 16; i += THREADS)
-    reinterpret_cast<uint4 *>(B2s)[i] = reinterpret_cast<const uint4 *>(W.w2img)[i];
+  for (int i = 4096 / 16 + tid; i < N1 * K1 * 2 / 16; i += THREADS)
+    reinterpret_cast<uint4 *>(B1s)[i] = make_uint4(0, 0, 0, 0);
+  __syncthreads();
+  if (tid == 0) *reinterpret_cast<uint32_t *>(B1s + kmaj_off(64, 24, K1)) = pack2(1.0f, 1.0f);
+  // W2 and w3 halved (exact): they multiply 2 gelu, see gelu2x2
+  for (int i = tid; i < 8192 / 16; i += THREADS) {
+    uint4 q = reinterpret_cast<const uint4 *>(W.w2img)[i];
+    const __nv_bfloat162 h = __floats2bfloat162_rn(0.5f, 0.5f);
+    uint32_t *w = reinterpret_cast<uint32_t *>(&q);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      __nv_bfloat162 v = *reinterpret_cast<__nv_bfloat162 *>(&w[k]);
+      v = __hmul2(v, h);
+      w[k] = *reinterpret_cast<uint32_t *>(&v);
+    }
+    reinterpret_cast<uint4 *>(B2s)[i] = q;
+  }
   if (tid < NH) {
     sb1[tid] = W.p[OFF_B1 + tid];
     sb2[tid] = W.p[OFF_B2 + tid];
-    sw3[tid] = W.p[OFF_W3 + tid];
+    sw3[tid] = 0.5f * W.p[OFF_W3 + tid];
   }
   if (tid == 0) {
     abort_flag = 0;
@@ -183,10 +211,10 @@ __global__ void __launch_bounds__(THREADS, 1)
       blockIdx.x < ntiles ? static_cast<int>((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
   auto tile_of = [&](int i) { return blockIdx.x + static_cast<int64_t>(i) * gridDim.x; };
 
-  if (warp < NGATHER * 4) {
+  if (warp < NG * 4) {
     // ---- gather groups -----------------------------------------------------
     const int g = warp >> 2, r = tid & 127;
-    for (int i = g; i < ntile_cta; i += NGATHER) {
+    for (int i = g; i < ntile_cta; i += NG) {
       const int p = i % NPF, s = i % NSTAGE;
       if (!wait_warp(&bar.pf_full[p], (i / NPF) & 1, abort, err)) break;
       const auto idx = task.load_idx(smem + OFF_PF + p * PF_BYTES, r);
@@ -194,22 +222,24 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int64_t row = tile_of(i) * TM + r;
       uint4 c[4];
       const float cx = task.stage(row, row < n, idx, c);
+      // the context as hi + lo in input columns 24, 25 (16 significant bits)
+      const float hi = __bfloat162float(__float2bfloat16_rn(cx));
+      c[3] = make_uint4(pack2(hi, cx - hi), 0, 0, 0);
       if (!wait_warp(&bar.a1_empty[s], ((i / NSTAGE) & 1) ^ 1, abort, err)) break;
       uint8_t *A1 = smem + OFF_A1S + s * 8192;
 #pragma unroll
       for (int q = 0; q < 4; ++q) *reinterpret_cast<uint4 *>(A1 + kmaj_off(r, 8 * q, K1)) = c[q];
-      ctx[(i % NCTX) * 128 + r] = cx;
       fence_async_smem();
       arrive(&bar.a1_full[s]);
     }
-  } else if (warp < NGATHER * 4 + NEPI * 4) {
+  } else if (warp < NGROUPS * 4) {
     // ---- epilogue groups ---------------------------------------------------
-    const int e = (warp - NGATHER * 4) >> 2, r = tid & 127;
+    const int e = (warp - NG * 4) >> 2, r = tid & 127;
     const uint32_t lane_base = static_cast<uint32_t>((warp & 3) * 32) << 16;
-    for (int i = e; i < ntile_cta; i += NEPI) {
+    for (int i = e; i < ntile_cta; i += NE) {
       const int t = i % NSLOT;
       const uint32_t par = (i / NSLOT) & 1;
-      const uint32_t tcol = tmem + lane_base + t * 128;
+      const uint32_t tcol = tmem + lane_base + t * SLOTW;
       if (!wait_warp(&bar.acc1[t], par, abort, err)) break;
       fence_after_sync();
       uint8_t *A2 = smem + OFF_A2S + t * 16384;
@@ -223,10 +253,10 @@ __global__ void __launch_bounds__(THREADS, 1)
           const float4 bb = reinterpret_cast<const float4 *>(sb1)[8 * h + 2 * c8 + 1];
           const float *w = v + 8 * c8;
           float gv[8];
-          f2upk(gelu2(w[0], w[1], ba.x, ba.y), gv[0], gv[1]);
-          f2upk(gelu2(w[2], w[3], ba.z, ba.w), gv[2], gv[3]);
-          f2upk(gelu2(w[4], w[5], bb.x, bb.y), gv[4], gv[5]);
-          f2upk(gelu2(w[6], w[7], bb.z, bb.w), gv[6], gv[7]);
+          f2upk(gelu2x2(w[0], w[1], ba.x, ba.y), gv[0], gv[1]);
+          f2upk(gelu2x2(w[2], w[3], ba.z, ba.w), gv[2], gv[3]);
+          f2upk(gelu2x2(w[4], w[5], bb.x, bb.y), gv[4], gv[5]);
+          f2upk(gelu2x2(w[6], w[7], bb.z, bb.w), gv[6], gv[7]);
           uint4 q;
           q.x = pack2(gv[0], gv[1]);
           q.y = pack2(gv[2], gv[3]);
@@ -235,7 +265,12 @@ __global__ void __launch_bounds__(THREADS, 1)
           *reinterpret_cast<uint4 *>(A2 + kmaj_off(r, 32 * h + 8 * c8, NH)) = q;
         }
       }
+      float cv[16];
+      ld16(tcol + 64, cv);
+      wait_ld();
+      const float cx = cv[0];
       fence_async_smem();
+      fence_before_sync();
       arrive(&bar.a2_full[t]);
       if (!wait_warp(&bar.acc2[t], par, abort, err)) break;
       fence_after_sync();
@@ -244,19 +279,19 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         float v[32];
-        ld32(tcol + 64 + 32 * h, v);
+        ld32(tcol + 32 * h, v);
 #pragma unroll
         for (int c4 = 0; c4 < 8; ++c4) {
           const float4 bq = reinterpret_cast<const float4 *>(sb2)[8 * h + c4];
           const float4 wq = reinterpret_cast<const float4 *>(sw3)[8 * h + c4];
-          acc2 = f2fma(gelu2(v[4 * c4 + 0], v[4 * c4 + 1], bq.x, bq.y), f2pk(wq.x, wq.y), acc2);
-          acc2 = f2fma(gelu2(v[4 * c4 + 2], v[4 * c4 + 3], bq.z, bq.w), f2pk(wq.z, wq.w), acc2);
+          const float *w = v + 4 * c4;
+          acc2 = f2fma(gelu2x2(w[0], w[1], bq.x, bq.y), f2pk(wq.x, wq.y), acc2);
+          acc2 = f2fma(gelu2x2(w[2], w[3], bq.z, bq.w), f2pk(wq.z, wq.w), acc2);
         }
       }
       float acc_e, acc_o;
       f2upk(acc2, acc_e, acc_o);
       const float acc = b3 + (acc_e + acc_o);
-      const float cx = ctx[(i % NCTX) * 128 + r];
       fence_before_sync();
       arrive(&bar.tfree[t]);
       const int64_t row = tile_of(i) * TM + r;
@@ -269,7 +304,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     // its inputs are staged and its TMEM slot is free; the second layer of
     // tile i2 as soon as its hidden layer is in shared memory.  At most NSLOT
     // tiles are in TMEM at once.
-    const uint32_t id64 = idesc_bf16(TM, NH);
+    const uint32_t id80 = idesc_bf16(TM, N1), id64 = idesc_bf16(TM, NH);
     int ip = 0, i1 = 0, i2 = 0;
     for (long long idle = 0; i2 < ntile_cta;) {
       bool progress = false;
@@ -288,8 +323,8 @@ __global__ void __launch_bounds__(THREADS, 1)
         fence_after_sync();
         const uint32_t a1 = smem_u32(smem + OFF_A1S + s1 * 8192);
         for (int k = 0; k < K1 / 16; ++k)
-          mma(tmem + t * 128, smem_desc(a1 + 256 * k, 128, K1 * 16),
-              smem_desc(smem_u32(B1s) + 256 * k, 128, K1 * 16), id64, k);
+          mma(tmem + t * SLOTW, smem_desc(a1 + 256 * k, 128, K1 * 16),
+              smem_desc(smem_u32(B1s) + 256 * k, 128, K1 * 16), id80, k);
         commit(&bar.a1_empty[s1]);
         commit(&bar.acc1[t]);
         ++i1;
@@ -300,7 +335,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         fence_after_sync();
         const uint32_t a2 = smem_u32(smem + OFF_A2S + t * 16384);
         for (int k = 0; k < NH / 16; ++k)
-          mma(tmem + t * 128 + 64, smem_desc(a2 + 256 * k, 128, NH * 16),
+          mma(tmem + t * SLOTW, smem_desc(a2 + 256 * k, 128, NH * 16),
               smem_desc(smem_u32(B2s) + 256 * k, 128, NH * 16), id64, k);
         commit(&bar.acc2[t]);
         ++i2;
@@ -364,14 +399,11 @@ struct RowsTask {
 
 // the learned correction of the shallow-water step: inputs from the stencil
 // velocities and geometry of edge e; corr[e] = q_e h_e sigma_e clip(y).
-// Index arrays are padded to ne_pad (a multiple of 128 edges); the block of a
-// tile is lst [10][128] | geo [128][16] BF16 | esh [2][128] | evs [128][2].
+// The inputs of a tile are one 11,264-byte block (LearnedLayout in
+// swm_layout.h): lst [10][128] | geo [128][16] BF16 | esh [2][128] |
+// evs [128][2], fetched with a single bulk copy.
 struct EdgeTask {
-  const int32_t *lst;   // [10][ne_pad] sign * (edge + 1), 0 = empty slot
-  const uint16_t *geo;  // [ne_pad][16]
-  const int32_t *esh;   // [2][ne_pad] triangles
-  const uint32_t *evs;  // [ne_pad][2] cell words
-  int64_t ne_pad;
+  const uint8_t *blocks;  // [ntiles][PF_BYTES]
   const float *u, *q_tr, *hd;
   float h_ref;
   float *corr;
@@ -385,12 +417,7 @@ struct EdgeTask {
   __device__ __forceinline__ uint32_t pf_bytes(int64_t, int64_t) const { return PF_BYTES; }
   __device__ __forceinline__ void prefetch(int64_t tile, int64_t, uint8_t *dst,
                                            uint64_t *mbar) const {
-    const int64_t e0 = tile * TM;
-    for (int s = 0; s < 10; ++s) bulk_g2s(dst + B_LST + 512 * s, lst + s * ne_pad + e0, 512, mbar);
-    bulk_g2s(dst + B_GEO, geo + e0 * 16, 4096, mbar);
-    bulk_g2s(dst + B_ESH, esh + e0, 512, mbar);
-    bulk_g2s(dst + B_ESH + 512, esh + ne_pad + e0, 512, mbar);
-    bulk_g2s(dst + B_EVS, evs + 2 * e0, 1024, mbar);
+    bulk_g2s(dst, blocks + tile * PF_BYTES, PF_BYTES, mbar);
   }
   __device__ __forceinline__ Idx load_idx(const uint8_t *pf, int r) const {
     Idx d;

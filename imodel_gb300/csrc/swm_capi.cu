@@ -332,9 +332,7 @@ int setup_learned(Handle *H, const imodel_swm_mesh *m, const Layout &L, const im
   std::string msg = build_learned_layout(*m, L, LL);
   if (!msg.empty()) return set_error(H, IMODEL_SWM_EINVAL, msg);
   int rc;
-  H->learned.ne_pad = LL.ne_pad;
-  if ((rc = upload(H, LL.lst, &H->learned.lst)) || (rc = upload(H, LL.geo, &H->learned.geo)) ||
-      (rc = upload(H, LL.esh, &H->learned.esh)) || (rc = upload(H, LL.evs, &H->learned.evs)) ||
+  if ((rc = upload(H, LL.blocks, &H->learned.blocks)) ||
       (rc = dalloc(H, &H->learned.corr, static_cast<size_t>(L.ne))) ||
       (rc = dalloc(H, &H->ck_h, static_cast<size_t>(L.nv))) ||
       (rc = dalloc(H, &H->ck_u, static_cast<size_t>(L.ne))))
@@ -715,7 +713,7 @@ int imodel_swm_profile(void *handle, double dt, int32_t nsteps, double avg_ms[4]
   return imodel::check_flags(H);
 }
 
-int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[5]) {
+int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[6]) {
   Handle *H = static_cast<Handle *>(handle);
   if (!H || !choice || nsteps <= 0) return IMODEL_SWM_EINVAL;
   if (!H->state_set) return imodel::set_error(H, IMODEL_SWM_ESTATE, "no state set");
@@ -724,6 +722,7 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
     // the FP64 path has one variant; its launch shape is fixed
     choice[0] = 0;
     choice[1] = choice[2] = choice[3] = choice[4] = 256;
+    choice[5] = 0;
     return IMODEL_SWM_OK;
   }
   auto &W = H->W32;
@@ -790,6 +789,19 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
       }
     }
   }
+  // the learned-correction kernel's split of warps between gathering and
+  // the epilogue
+  if (H->learned_active)
+    for (int g = 2; g <= 4; ++g) {
+      if (best.mlp_gather == g) continue;
+      imodel::Tune t = best;
+      t.mlp_gather = g;
+      const float ms = trial(t);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = t;
+      }
+    }
   W.tune = best;
   if (H->graph) {
     cudaGraphExecDestroy(H->graph);
@@ -809,10 +821,11 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
   choice[2] = best.bs_pre;
   choice[3] = best.bs_cell;
   choice[4] = best.bs_edge;
+  choice[5] = H->learned_on ? best.mlp_gather : 0;
   return imodel::check_flags(H);
 }
 
-int imodel_swm_set_tuning(void *handle, const int32_t choice[5]) {
+int imodel_swm_set_tuning(void *handle, const int32_t choice[6]) {
   Handle *H = static_cast<Handle *>(handle);
   if (!H || !choice) return IMODEL_SWM_EINVAL;
   if (H->precision == IMODEL_SWM_FP64) return IMODEL_SWM_OK;
@@ -830,6 +843,11 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[5]) {
   t.bs_pre = choice[2];
   t.bs_cell = choice[3];
   t.bs_edge = choice[4];
+  if (H->learned_on) {
+    if (choice[5] < 2 || choice[5] > 4)
+      return imodel::set_error(H, IMODEL_SWM_EINVAL, "gather groups of the network: 2, 3 or 4");
+    t.mlp_gather = choice[5];
+  }
   H->W32.tune = t;
   if (H->graph) {
     cudaGraphExecDestroy(H->graph);

@@ -42,6 +42,7 @@ struct DevMesh {
 struct Tune {
   int variant = 1;
   int bs_tri = 256, bs_pre = 256, bs_cell = 256, bs_edge = 256;
+  int mlp_gather = 2;  // gather groups of the learned-correction kernel (2..4)
 };
 
 struct LearnedDev;
@@ -83,17 +84,14 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
 struct LearnedDev {
   float *p = nullptr;        // FP32 parameters
   uint16_t *img = nullptr;   // BF16 weight images
-  int64_t ne_pad = 0;        // edges rounded up to whole 128-edge tiles
-  const int32_t *lst = nullptr;   // [10][ne_pad]
-  const uint16_t *geo = nullptr;  // [ne_pad][16]
-  const int32_t *esh = nullptr;   // [2][ne_pad]
-  const uint32_t *evs = nullptr;  // [ne_pad][2]
+  // network inputs, one 11,264-byte block per 128-edge tile (LearnedLayout)
+  const uint8_t *blocks = nullptr;
   float *corr = nullptr;     // [ne]
   int sms = 0;
 };
 int learned_prepare(const float *params_host, LearnedDev *L, cudaStream_t s);
 void learned_launch(const DevMesh &M, const LearnedDev &L, const float *hd, const float *u,
-                    const float *q_tr, float h_ref, int *err, cudaStream_t s);
+                    const float *q_tr, float h_ref, int gather_groups, int *err, cudaStream_t s);
 
 inline int launches_per_stage(int precision_fp32, int variant) {
   return (precision_fp32 && variant == 1) ? 3 : 4;

@@ -150,7 +150,7 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
     if (ev) cudaEventRecord(ev[1], s);
     // learned correction: formed once per step from the first stage's state
     if (W.learned && stage <= 0)
-      learned_launch(M, *W.learned, h_in, u_in, W.q_tr, W.h_ref, W.flags, s);
+      learned_launch(M, *W.learned, h_in, u_in, W.q_tr, W.h_ref, T.mlp_gather, W.flags, s);
     if (ev) cudaEventRecord(ev[2], s);
     k_cell32v2<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
         M, h_in, u_in, W.q_tr, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,

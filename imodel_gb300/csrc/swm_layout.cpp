@@ -332,23 +332,30 @@ uint16_t bf16_bits(float v) {
 // for both cells and 20 (w - (r/n - 1/2)) for the 10 weights.
 std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, LearnedLayout &LL) {
   const int ne = m.ne;
-  const size_t NE = (static_cast<size_t>(ne) + 127) / 128 * 128;
-  LL.ne_pad = static_cast<int64_t>(NE);
-  LL.lst.assign(10 * NE, 0);
-  LL.geo.assign(16 * NE, 0);
-  LL.esh.assign(2 * NE, 0);
-  LL.evs.assign(2 * NE, 0);
-  for (size_t e = 0; e < static_cast<size_t>(ne); ++e) {
-    LL.esh[e] = L.e_sh[e];
-    LL.esh[NE + e] = L.e_sh[static_cast<size_t>(ne) + e];
-    LL.evs[2 * e] = L.e_vs2[2 * e];
-    LL.evs[2 * e + 1] = L.e_vs2[2 * e + 1];
+  constexpr int T = LearnedLayout::kTile;
+  LL.ntiles = (static_cast<int64_t>(ne) + T - 1) / T;
+  LL.blocks.assign(static_cast<size_t>(LL.ntiles) * LearnedLayout::kBlockBytes, 0);
+  // entry k of array `off` (element size `sz`) in the block of device edge i
+  auto at = [&](int64_t i, int off, int k, int sz) -> uint8_t * {
+    return LL.blocks.data() + (i / T) * LearnedLayout::kBlockBytes + off +
+           static_cast<size_t>(k) * sz;
+  };
+  auto put_i32 = [&](int64_t i, int off, int k, int32_t v) {
+    std::memcpy(at(i, off, k, 4), &v, 4);
+  };
+  for (int64_t i = 0; i < ne; ++i) {
+    const int64_t r = i % T;
+    put_i32(i, LearnedLayout::kEsh, static_cast<int>(r), L.e_sh[i]);
+    put_i32(i, LearnedLayout::kEsh, static_cast<int>(T + r), L.e_sh[static_cast<size_t>(ne) + i]);
+    const uint32_t w[2] = {L.e_vs2[2 * i], L.e_vs2[2 * i + 1]};
+    std::memcpy(at(i, LearnedLayout::kEvs, static_cast<int>(r), 8), w, 8);
   }
   double lmean = 0.0;
   for (int e = 0; e < ne; ++e) lmean += m.ed_leng[e];
   lmean /= ne;
   for (int e = 0; e < ne; ++e) {
     const int i = L.edge_o2n[e];
+    const int r = i % T;
     const double l = m.ed_leng[e], d = m.edhx_leng[e];
     float g[14];
     g[0] = static_cast<float>(10.0 * (l / lmean - 1.0));
@@ -361,16 +368,16 @@ std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, Lear
       for (int j = 0; j < n; ++j)
         if (m.v_ed[6 * static_cast<size_t>(c) + j] - 1 == e) slot = j;
       if (slot < 0) return "edge missing from its cell's edge list";
-      for (int r = 1; r < 6; ++r) {
-        const int col = side * 5 + (r - 1);
+      for (int q = 1; q < 6; ++q) {
+        const int col = side * 5 + (q - 1);
         float w = 0.0f;
-        if (r < n) {
-          const int j = (slot + r) % n;
+        if (q < n) {
+          const int j = (slot + q) % n;
           const int k = m.v_ed[6 * static_cast<size_t>(c) + j] - 1;
           const int s = m.hx_ttgout[6 * static_cast<size_t>(c) + j] *
                         m.hx_tnrccw[6 * static_cast<size_t>(c) + slot];
-          LL.lst[col * NE + i] = (s < 0 ? -1 : 1) * (L.edge_o2n[k] + 1);
-          const double wreg = static_cast<double>(r) / n - 0.5;
+          put_i32(i, LearnedLayout::kLst, col * T + r, (s < 0 ? -1 : 1) * (L.edge_o2n[k] + 1));
+          const double wreg = static_cast<double>(q) / n - 0.5;
           w = static_cast<float>(
               20.0 * (m.hx_trskw[36 * static_cast<size_t>(c) + 6 * static_cast<size_t>(j) + slot] -
                       wreg));
@@ -378,7 +385,10 @@ std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, Lear
         g[4 + col] = w;
       }
     }
-    for (int q = 0; q < 14; ++q) LL.geo[16 * static_cast<size_t>(i) + q] = bf16_bits(g[q]);
+    for (int q = 0; q < 14; ++q) {
+      const uint16_t b16 = bf16_bits(g[q]);
+      std::memcpy(at(i, LearnedLayout::kGeo, 16 * r + q, 2), &b16, 2);
+    }
   }
   return "";
 }

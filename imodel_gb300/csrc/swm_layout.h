@@ -92,15 +92,18 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L);
 // order: per edge the 10 stencil edges as sign * (index + 1) (0 = padding),
 // slot-major [10][ne], and the 14 geometry inputs as BF16 bit patterns,
 // [ne][16] (two zero pads, 32 bytes per edge).
-// Inputs of the learned correction, padded to ne_pad = ne rounded up to 128
-// edges so that every 128-edge tile is one bulk copy per array (padding:
-// empty stencil slots, zero geometry, triangle and cell 0).
+// Inputs of the learned correction, one 11,264-byte block per tile of 128
+// edges (ntiles = ceil(ne / 128); padding rows: empty stencil slots, zero
+// geometry, triangle and cell 0), so that a tile's inputs are one bulk copy:
+//   int32 lst[10][128]  sign * (edge + 1) of the stencil slots, 0 = empty
+//   bf16  geo[128][16]  geometry inputs (14 used)
+//   int32 esh[2][128]   the edge's triangles
+//   uint32 evs[128][2]  the edge's cell words
 struct LearnedLayout {
-  int64_t ne_pad = 0;
-  std::vector<int32_t> lst;   // [10][ne_pad] sign * (edge + 1), 0 = empty slot
-  std::vector<uint16_t> geo;  // [ne_pad][16] BF16 geometry inputs
-  std::vector<int32_t> esh;   // [2][ne_pad] triangles of the edge
-  std::vector<uint32_t> evs;  // [ne_pad][2] cell words of the edge
+  static constexpr int kTile = 128, kBlockBytes = 11264;
+  static constexpr int kLst = 0, kGeo = 5120, kEsh = 9216, kEvs = 10240;
+  int64_t ntiles = 0;
+  std::vector<uint8_t> blocks;  // [ntiles][kBlockBytes]
 };
 std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, LearnedLayout &LL);
 

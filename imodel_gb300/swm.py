@@ -106,6 +106,9 @@ def tc2_exact_operators(grid: Grid):
 # ---------------------------------------------------------------------------
 # the GB300 step behind the C ABI
 # ---------------------------------------------------------------------------
+TUNING_KEYS = ("variant", "bs_tri", "bs_pre", "bs_cell", "bs_edge", "mlp_gather")
+
+
 class SWM:
     """One grid's shallow-water step on the GPU (trsk10, HTC, geodesic areas).
 
@@ -244,13 +247,13 @@ class SWM:
     def autotune(self, dt: float, nsteps: int = 5) -> dict:
         """Times the FP32 fusion variants and block sizes on the current
         state, keeps the fastest, restores the state."""
-        c = np.zeros(5, dtype=np.int32)
+        c = np.zeros(6, dtype=np.int32)
         self._check(self.lib.imodel_swm_autotune(self._handle, dt, nsteps, _capi.as_i32p(c)))
-        return dict(zip(("variant", "bs_tri", "bs_pre", "bs_cell", "bs_edge"), c.tolist()))
+        return dict(zip(TUNING_KEYS, c.tolist()))
 
     def set_tuning(self, variant: int = 1, bs_tri: int = 256, bs_pre: int = 256,
-                   bs_cell: int = 256, bs_edge: int = 256):
-        c = np.array([variant, bs_tri, bs_pre, bs_cell, bs_edge], dtype=np.int32)
+                   bs_cell: int = 256, bs_edge: int = 256, mlp_gather: int = 2):
+        c = np.array([variant, bs_tri, bs_pre, bs_cell, bs_edge, mlp_gather], dtype=np.int32)
         self._check(self.lib.imodel_swm_set_tuning(self._handle, _capi.as_i32p(c)))
 
     def launch_count(self, nsteps: int) -> int:

@@ -168,12 +168,15 @@ int imodel_swm_advance(void *handle, double dt, int32_t nsteps);
 /* FP32 launch tuning (the project's autotuner): times nsteps graph-replayed
  * steps of every fusion variant and block size on the current state, keeps
  * the fastest and restores the state.  choice = {variant, block size of the
- * triangle, edge pre-pass, cell and edge kernels}; variant 0 uses the
- * 10-entry edge stencil, variant 1 the cell-centred TRSK sum.  The FP64 path
- * has a single configuration and returns it. */
-int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[5]);
+ * triangle, edge pre-pass, cell and edge kernels, gather groups of the
+ * learned-correction kernel}; variant 0 uses the 10-entry edge stencil,
+ * variant 1 the cell-centred TRSK sum; the last entry is 2, 3 or 4 with the
+ * learned correction on (its kernel has 6 warp groups, the rest run the
+ * epilogue) and 0 without it.  The FP64 path has a single configuration and
+ * returns it. */
+int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[6]);
 /* Applies a choice returned by imodel_swm_autotune (e.g. cached per grid). */
-int imodel_swm_set_tuning(void *handle, const int32_t choice[5]);
+int imodel_swm_set_tuning(void *handle, const int32_t choice[6]);
 /* Launches issued by one advance call for nsteps steps (kernels only). */
 int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count);
 /* Runs nsteps RK4 steps kernel by kernel (no graph) with CUDA events around
