@@ -298,6 +298,11 @@ def config_dict(g, path, weights=None):
 
 MLP_FLOP_PER_EDGE = 2 * (24 * 64 + 64 * 64 + 64)
 
+# DRAM bytes (read + write) per unit of a launch, from one ncu capture of the
+# kernel at icos level 8 (128.0 MB for 655,362 cells), scaled to the
+# benchmark's level by the number of cells, as the traffic grows with them.
+TRAFFIC_PER_CELL = {"k_cell32v2": 128.046e6 / 655362}
+
 
 def load_tflops():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -430,6 +435,8 @@ def main():
         step_achieved = step_bytes / (rh["ms"] / args.steps / 1000.0) / 1e9
         e2e = results["e2e"]
         kernel_ms = dict(prof)
+        kname = kernel_names(rh["tuning"]["variant"])[dom]
+        traffic = TRAFFIC_PER_CELL[kname] * g.nv if kname in TRAFFIC_PER_CELL else None
         line = {
             "metric": METRIC, "value": rate(rh), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup,
@@ -440,10 +447,11 @@ def main():
             "fp64": {"value": rate(r64), "unit": UNIT, "ms_per_step": r64["ms"] / args.steps,
                      "kernel_ms": r64["prof"]},
             "kernel_ms": kernel_ms,
-            "roofline": {"bound": "hbm", "kernel": kernel_names(rh["tuning"]["variant"])[dom],
+            "roofline": {"bound": "hbm", "kernel": kname,
                          "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "peak_source": peak_kind, "traffic": None,
+                         "peak_source": peak_kind, "traffic": traffic,
+                         "traffic_source": "ncu capture at icos level 8, scaled by cells",
                          "algorithmic_bytes_per_launch": kb[dom]},
             "step_roofline": {"bytes_per_cell_step": 2000.0, "achieved": step_achieved,
                               "peak": peak, "unit": "GB/s", "frac": step_achieved / peak},

@@ -239,11 +239,11 @@ int total_energy(Handle *H, double *te) {
   if (H->precision == IMODEL_SWM_FP64) {
     auto &W = H->W64;
     launch_diag<double>(H->M, W, W.yn_h, W.yn_u, W.ya_h, W.ya_u, H->d_scratch, H->d_result,
-                        H->stream);
+                        H->stream, true);
   } else {
     auto &W = H->W32;
     launch_diag<float>(H->M, W, W.yn_h, W.yn_u, W.ya_h, W.ya_u, H->d_scratch, H->d_result,
-                       H->stream);
+                       H->stream, true);
   }
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(H->h_result, H->d_result, sizeof(double) * kDiagQ, cudaMemcpyDeviceToHost,

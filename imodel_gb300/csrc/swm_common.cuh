@@ -112,16 +112,18 @@ void launch_scatter_out32(int n, const int32_t *n2o, const float *src, double *d
 // Compensated FP64 integrals.  Scratch: partial sums, 2 doubles per block
 // and quantity; result[kDiagQ] on the device.
 constexpr int kDiagQ = 12;
-constexpr int kRedBlocks = 304;   // 2 blocks per SM on 152 SMs
+constexpr int kRedBlocks = 608;   // 4 blocks per SM on 152 SMs
 constexpr int kRedThreads = 256;
 // result indices
 enum {
   Q_AREA = 0, Q_AH, Q_PE, Q_AHB, Q_AB2, Q_KE, Q_ENS, Q_ADIV2, Q_MAXDIV, Q_NAN,
   Q_SPARE0, Q_SPARE1
 };
+// energy_only: potential and kinetic energy only (the other entries are 0)
 template <class T>
 void launch_diag(const DevMesh &M, const Work<T> &W, const T *h, const T *u, const T *hs,
-                 const T *us, double *scratch, double *result, cudaStream_t s);
+                 const T *us, double *scratch, double *result, cudaStream_t s,
+                 bool energy_only = false);
 // error_calc partials: {sum A dif^2, sum A ref^2, max|dif|, max|ref|} for h
 // then for u.
 template <class T>

@@ -258,18 +258,34 @@ __global__ void k_finalize(const double *__restrict__ scratch, int nblk, int nq,
   }
 }
 
+// a / b for the diagnostics: FP64 division is slow on GB300's FP64 pipe, so
+// the reciprocal starts from the FP32 one (relative error < 2^-22) and takes
+// two Newton-Raphson steps r <- r (2 - b r), which square the error each
+// (< 2^-44, then below FP64 rounding); b must be a normal FP32-range number
+// (areas, depths)
+__device__ __forceinline__ double diag_div(double a, double b) {
+  double r = static_cast<double>(__frcp_rn(static_cast<float>(b)));
+  r = r * (2.0 - b * r);
+  r = r * (2.0 - b * r);
+  return a * r;
+}
+
 // calc_energies (swm.f90:2686-2752), sumf_areas (:3394), potential enstrophy,
-// RMS divergence of the last stage input (hs, us), NaN scan.
-template <class T>
+// RMS divergence of the last stage input (hs, us), NaN scan.  FULL = false
+// computes the two energies only (the learned correction's drift guard).
+// Each thread sums its few dozen terms in plain FP64 (relative error ~1e-14);
+// threads, warps, blocks and the grid are combined with Neumaier-compensated
+// sums.
+template <class T, bool FULL>
 __global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__restrict__ h,
                                                       const T *__restrict__ u,
                                                       const T *__restrict__ hs,
                                                       const T *__restrict__ us,
                                                       double h_ref,
                                                       double *__restrict__ scratch) {
-  KSum acc[kDiagQ];
+  double part[kDiagQ];
 #pragma unroll
-  for (int q = 0; q < kDiagQ; ++q) acc[q] = KSum{0.0, 0.0};
+  for (int q = 0; q < kDiagQ; ++q) part[q] = 0.0;
   const int stride = gridDim.x * blockDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const double g = M.grav, erad = M.erad;
@@ -280,11 +296,12 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__rest
     const double hi = static_cast<double>(h[i]) + h_ref;
     const double b = M.c_bt[i];
     if (!isfinite(hi)) nan = 1.0;
-    acc[Q_AREA].add(A);
-    acc[Q_AH].add(A * hi);
-    acc[Q_PE].add(A * g * hi * (hi * 0.5 + b));
-    acc[Q_AHB].add(A * (hi + b));
-    acc[Q_AB2].add(A * b * b);
+    part[Q_PE] += A * g * hi * (hi * 0.5 + b);
+    if (!FULL) continue;
+    part[Q_AREA] += A;
+    part[Q_AH] += A * hi;
+    part[Q_AHB] += A * (hi + b);
+    part[Q_AB2] += A * b * b;
     // div_hx(u) of the last stage input (diagnostic in tendency, :2570)
     const int n = M.c_nnb[i];
     double d = 0.0;
@@ -292,8 +309,8 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__rest
       const int e = M.c_ed[j * M.nv + i];
       d = d + static_cast<double>(us[e]) * M.c_sd[j * M.nv + i];
     }
-    d = d / A / erad;
-    acc[Q_ADIV2].add(A * (d * d));
+    d = diag_div(d, A * erad);
+    part[Q_ADIV2] += A * (d * d);
     maxdiv = fmax(maxdiv, fabs(d));
   }
   for (int e = tid; e < M.ne; e += stride) {
@@ -302,21 +319,24 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__rest
     // h_ed of the last stage input, as calc_energies uses (swm.f90:2738)
     const double he =
         (static_cast<double>(hs[M.e_v[e]]) + static_cast<double>(hs[M.e_v[M.ne + e]])) * 0.5 + h_ref;
-    acc[Q_KE].add(M.e_area[e] * he * (ue * ue));
+    part[Q_KE] += M.e_area[e] * he * (ue * ue);
   }
-  for (int t = tid; t < M.nt; t += stride) {
+  for (int t = tid; FULL && t < M.nt; t += stride) {
     double eta = 0.0, ht = 0.0;
     for (int s = 0; s < 3; ++s) {
       eta = eta + static_cast<double>(us[M.t_ed[s * M.nt + t]]) * M.t_lt[s * M.nt + t];
       ht = ht + M.t_kite[s * M.nt + t] * (static_cast<double>(hs[M.t_v[s * M.nt + t]]) + h_ref);
     }
     const double A = M.t_areag[t];
-    eta = eta / A / erad;
+    eta = diag_div(eta, A * erad);
     eta = eta + M.t_f[t];
-    ht = ht / A;
-    const double q = ht != 0.0 ? eta / ht : 0.0;
-    acc[Q_ENS].add(A * ht * (q * q) * 0.5);
+    ht = diag_div(ht, A);
+    const double q = ht != 0.0 ? diag_div(eta, ht) : 0.0;
+    part[Q_ENS] += A * ht * (q * q) * 0.5;
   }
+  KSum acc[kDiagQ];
+#pragma unroll
+  for (int q = 0; q < kDiagQ; ++q) acc[q] = KSum{part[q], 0.0};
   acc[Q_MAXDIV].s = maxdiv;
   acc[Q_NAN].s = nan;
   // max-type entries are reduced with max, not a sum: pre-reduce them
@@ -443,18 +463,23 @@ void launch_trsk_tangent(const DevMesh &M, const double *u, double *utg, cudaStr
 
 template <class T>
 void launch_diag(const DevMesh &M, const Work<T> &W, const T *h, const T *u, const T *hs,
-                 const T *us, double *scratch, double *result, cudaStream_t s) {
-  k_diag<T><<<kRedBlocks, kRedThreads, 0, s>>>(M, h, u, hs, us,
-                                                static_cast<double>(W.h_ref), scratch);
+                 const T *us, double *scratch, double *result, cudaStream_t s,
+                 bool energy_only) {
+  if (energy_only)
+    k_diag<T, false><<<kRedBlocks, kRedThreads, 0, s>>>(M, h, u, hs, us,
+                                                         static_cast<double>(W.h_ref), scratch);
+  else
+    k_diag<T, true><<<kRedBlocks, kRedThreads, 0, s>>>(M, h, u, hs, us,
+                                                        static_cast<double>(W.h_ref), scratch);
   const unsigned maxmask = (1u << Q_MAXDIV) | (1u << Q_NAN);
   k_finalize<<<kDiagQ, kRedThreads, 0, s>>>(scratch, kRedBlocks, kDiagQ, maxmask, result);
 }
 template void launch_diag<double>(const DevMesh &, const Work<double> &, const double *,
                                   const double *, const double *, const double *, double *,
-                                  double *, cudaStream_t);
+                                  double *, cudaStream_t, bool);
 template void launch_diag<float>(const DevMesh &, const Work<float> &, const float *,
                                  const float *, const float *, const float *, double *,
-                                 double *, cudaStream_t);
+                                 double *, cudaStream_t, bool);
 
 template <class T>
 void launch_errors(const DevMesh &M, const T *h, const T *u, double h_ref, const double *href,
