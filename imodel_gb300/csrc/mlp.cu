@@ -46,6 +46,7 @@ constexpr int OFF_W1 = 0, OFF_B1 = 1536, OFF_W2 = 1600, OFF_B2 = 5696, OFF_W3 = 
               OFF_B3 = 5824;
 constexpr int NPARAM = 5825;
 constexpr int NPART = NPARAM + 1;  // + loss
+static_assert(TM == 128, "four warps per training tile");
 constexpr int ERR_WAIT = 8;
 
 struct Weights {
@@ -208,7 +209,11 @@ __global__ void __launch_bounds__(TM, 1)
           *A3 = B2T + 8192, *AW = A3 + 16384, *BW = AW + 32768;
   __shared__ uint64_t mbar;
   __shared__ uint32_t tslot;
-  __shared__ float sb1[NH], sb2[NH], sw3[NH], sdw3[NH], sdb3, sloss;
+  __shared__ float sb1[NH], sb2[NH], sw3[NH];
+  // per-warp sums of dw3, db3 and the loss: each warp adds only to its own
+  // entries, and the warps are summed in a fixed order at the end, so the
+  // partial gradients do not depend on the order in which warps finish
+  __shared__ float sdw3[TM / 32][NH], sdb3[TM / 32], sloss[TM / 32];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (int i = tid; i < 4096 / 16; i += TM)
     reinterpret_cast<uint4 *>(B1)[i] = reinterpret_cast<const uint4 *>(W.w1img)[i];
@@ -222,11 +227,11 @@ __global__ void __launch_bounds__(TM, 1)
     sb1[tid] = W.p[OFF_B1 + tid];
     sb2[tid] = W.p[OFF_B2 + tid];
     sw3[tid] = W.p[OFF_W3 + tid];
-    sdw3[tid] = 0.0f;
+    for (int k = 0; k < TM / 32; ++k) sdw3[k][tid] = 0.0f;
   }
-  if (tid == 0) {
-    sdb3 = 0.0f;
-    sloss = 0.0f;
+  if (tid < TM / 32) {
+    sdb3[tid] = 0.0f;
+    sloss[tid] = 0.0f;
   }
   const float b3 = W.p[OFF_B3];
   __syncthreads();
@@ -315,13 +320,13 @@ __global__ void __launch_bounds__(TM, 1)
       const float dy = 2.0f * wt * r * inv_batch;
       float ls = warp_sum(wt * r * r), sdy = warp_sum(dy);
       if (lane == 0) {
-        atomicAdd(&sloss, ls);
-        atomicAdd(&sdb3, sdy);
+        sloss[warp] += ls;
+        sdb3[warp] += sdy;
       }
 #pragma unroll
       for (int j = 0; j < NH; ++j) {
         const float dw = warp_sum(h2[j] * dy);
-        if (lane == 0) atomicAdd(&sdw3[j], dw);
+        if (lane == 0) sdw3[warp][j] += dw;
         v[j] = dy * sw3[j] * gelu_grad(v[j]);  // dZ2
       }
       store_row64(A3, tid, v, NH);
@@ -397,10 +402,10 @@ __global__ void __launch_bounds__(TM, 1)
       for (int o = 0; o < NH; ++o) out[OFF_W1 + o * NIN + tid] = 0.0f;
   }
   __syncthreads();
-  if (tid < NH) out[OFF_W3 + tid] = sdw3[tid];
+  if (tid < NH) out[OFF_W3 + tid] = ((sdw3[0][tid] + sdw3[1][tid]) + sdw3[2][tid]) + sdw3[3][tid];
   if (tid == 0) {
-    out[OFF_B3] = sdb3;
-    out[NPARAM] = sloss;
+    out[OFF_B3] = ((sdb3[0] + sdb3[1]) + sdb3[2]) + sdb3[3];
+    out[NPARAM] = ((sloss[0] + sloss[1]) + sloss[2]) + sloss[3];
   }
   sync_cta();
   if (warp == 0) tmem_dealloc(tmem, 256);
