@@ -50,7 +50,7 @@ struct Handle {
   bool learned_on = false;      // requested at create
   bool learned_active = false;  // still applied (the drift guard may switch it off)
   double drift_bound = 1e-3;
-  double te_ref = 0.0;
+  double te_ref = 0.0, umax_ref = 0.0;
   bool te_ref_set = false;
   // state at the start of the current guard interval, restored when the
   // interval ends past the drift bound (or with a non-finite energy)
@@ -59,6 +59,10 @@ struct Handle {
 
 // steps between two checks of the learned correction's energy drift
 constexpr int kGuardSteps = 32;
+// the check also fails once max |u| exceeds this factor times its value when
+// the state was set: a mode growing at a few edges hardly moves the total
+// energy before it blows up
+constexpr double kUmaxGrowth = 1.5;
 
 #define CK(call)                                                                  \
   do {                                                                            \
@@ -234,8 +238,8 @@ int check_flags(Handle *H) {
   return IMODEL_SWM_OK;
 }
 
-// total energy of the current state (compensated FP64 integral)
-int total_energy(Handle *H, double *te) {
+// total energy of the current state (compensated FP64 integral) and max |u|
+int total_energy(Handle *H, double *te, double *umax) {
   if (H->precision == IMODEL_SWM_FP64) {
     auto &W = H->W64;
     launch_diag<double>(H->M, W, W.yn_h, W.yn_u, W.ya_h, W.ya_u, H->d_scratch, H->d_result,
@@ -250,6 +254,7 @@ int total_energy(Handle *H, double *te) {
                      H->stream));
   CK(cudaStreamSynchronize(H->stream));
   *te = H->h_result[Q_PE] + H->h_result[Q_KE];
+  *umax = H->h_result[Q_UMAX];
   return IMODEL_SWM_OK;
 }
 
@@ -260,16 +265,17 @@ int total_energy(Handle *H, double *te) {
 int learned_guard(Handle *H, bool *tripped) {
   if (tripped) *tripped = false;
   if (!H->learned_active) return IMODEL_SWM_OK;
-  double te = 0.0;
-  int rc = total_energy(H, &te);
+  double te = 0.0, umax = 0.0;
+  int rc = total_energy(H, &te, &umax);
   if (rc) return rc;
   if (!H->te_ref_set) {
     H->te_ref = te;
+    H->umax_ref = umax;
     H->te_ref_set = true;
     return IMODEL_SWM_OK;
   }
   const double drift = std::fabs(te - H->te_ref) / std::fabs(H->te_ref);
-  if (!(drift <= H->drift_bound)) {
+  if (!(drift <= H->drift_bound) || !(umax <= kUmaxGrowth * H->umax_ref)) {
     H->learned_active = false;
     H->W32.learned = nullptr;
     if (H->graph) {

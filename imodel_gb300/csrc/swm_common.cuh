@@ -117,7 +117,8 @@ constexpr int kRedThreads = 256;
 // result indices
 enum {
   Q_AREA = 0, Q_AH, Q_PE, Q_AHB, Q_AB2, Q_KE, Q_ENS, Q_ADIV2, Q_MAXDIV, Q_NAN,
-  Q_SPARE0, Q_SPARE1
+  Q_UMAX,  // max |u| over the edges
+  Q_SPARE1
 };
 // energy_only: potential and kinetic energy only (the other entries are 0)
 template <class T>

@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__rest
   const int stride = gridDim.x * blockDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const double g = M.grav, erad = M.erad;
-  double maxdiv = 0.0;
+  double maxdiv = 0.0, umax = 0.0;
   double nan = 0.0;
   for (int i = tid; i < M.nv; i += stride) {
     const double A = M.c_areag[i];
@@ -316,6 +316,7 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__rest
   for (int e = tid; e < M.ne; e += stride) {
     const double ue = static_cast<double>(u[e]);
     if (!isfinite(ue)) nan = 1.0;
+    umax = fmax(umax, fabs(ue));
     // h_ed of the last stage input, as calc_energies uses (swm.f90:2738)
     const double he =
         (static_cast<double>(hs[M.e_v[e]]) + static_cast<double>(hs[M.e_v[M.ne + e]])) * 0.5 + h_ref;
@@ -337,33 +338,26 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__rest
   KSum acc[kDiagQ];
 #pragma unroll
   for (int q = 0; q < kDiagQ; ++q) acc[q] = KSum{part[q], 0.0};
-  acc[Q_MAXDIV].s = maxdiv;
-  acc[Q_NAN].s = nan;
-  // max-type entries are reduced with max, not a sum: pre-reduce them
-  for (int off = 16; off > 0; off >>= 1) {
-    acc[Q_MAXDIV].s = fmax(acc[Q_MAXDIV].s, __shfl_down_sync(0xffffffffu, acc[Q_MAXDIV].s, off));
-    acc[Q_NAN].s = fmax(acc[Q_NAN].s, __shfl_down_sync(0xffffffffu, acc[Q_NAN].s, off));
-  }
-  __shared__ double smax[2][kRedThreads / 32];
+  // max-type entries are reduced with max, not a sum: pre-reduce them (their
+  // sums, all zero, are overwritten below)
+  const int kMaxQ[3] = {Q_MAXDIV, Q_NAN, Q_UMAX};
+  double mx[3] = {maxdiv, nan, umax};
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    for (int off = 16; off > 0; off >>= 1)
+      mx[k] = fmax(mx[k], __shfl_down_sync(0xffffffffu, mx[k], off));
+  __shared__ double smax[3][kRedThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) {
-    smax[0][warp] = acc[Q_MAXDIV].s;
-    smax[1][warp] = acc[Q_NAN].s;
-  }
+  if (lane == 0)
+    for (int k = 0; k < 3; ++k) smax[k][warp] = mx[k];
   __syncthreads();
-  double bmax = 0.0, bnan = 0.0;
-  for (int w = 0; w < kRedThreads / 32; ++w) {
-    bmax = fmax(bmax, smax[0][w]);
-    bnan = fmax(bnan, smax[1][w]);
-  }
-  acc[Q_MAXDIV] = KSum{0.0, 0.0};
-  acc[Q_NAN] = KSum{0.0, 0.0};
+  double bm[3] = {0.0, 0.0, 0.0};
+  for (int k = 0; k < 3; ++k)
+    for (int w = 0; w < kRedThreads / 32; ++w) bm[k] = fmax(bm[k], smax[k][w]);
   block_reduce_store<kDiagQ>(acc, scratch);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    scratch[(Q_MAXDIV * gridDim.x + blockIdx.x) * 2] = bmax;
-    scratch[(Q_NAN * gridDim.x + blockIdx.x) * 2] = bnan;
-  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 3; ++k) scratch[(kMaxQ[k] * gridDim.x + blockIdx.x) * 2] = bm[k];
 }
 
 // error_calc partials (swm.f90:3492-3543): weights A_i (cells) and l*d/2
@@ -471,7 +465,7 @@ void launch_diag(const DevMesh &M, const Work<T> &W, const T *h, const T *u, con
   else
     k_diag<T, true><<<kRedBlocks, kRedThreads, 0, s>>>(M, h, u, hs, us,
                                                         static_cast<double>(W.h_ref), scratch);
-  const unsigned maxmask = (1u << Q_MAXDIV) | (1u << Q_NAN);
+  const unsigned maxmask = (1u << Q_MAXDIV) | (1u << Q_NAN) | (1u << Q_UMAX);
   k_finalize<<<kDiagQ, kRedThreads, 0, s>>>(scratch, kRedBlocks, kDiagQ, maxmask, result);
 }
 template void launch_diag<double>(const DevMesh &, const Work<double> &, const double *,

@@ -102,10 +102,14 @@ typedef struct imodel_swm_opts {
                          0 selects the area mean of the first state set.   */
   int32_t device;     /* CUDA device ordinal                                */
   int32_t learned;    /* 1: add the learned TRSK correction (needs weights) */
-  const void *mlp_weights;  /* packed MLP parameters (see imodel_swm_mlp.h) */
+  const void *mlp_weights;  /* packed MLP parameters (see imodel_mlp.h)    */
   size_t mlp_bytes;
-  double drift_bound; /* |energy drift| above which the learned correction
-                         is switched off (0 = 1e-3)                       */
+  double drift_bound; /* relative total-energy drift above which the
+                         learned correction is switched off (0 = 1e-3); it
+                         is also switched off once max |u| exceeds 1.5x its
+                         value when the state was set.  Checked every 32
+                         steps; the interval that failed is stepped again
+                         with the plain scheme                           */
 } imodel_swm_opts;
 
 /* ---- diagnostics (swm.f90:293-322, :2686-2752, :3394-3440) ------------- */
@@ -196,8 +200,11 @@ void *imodel_swm_stream(void *handle);
  * launch.  Members of a grid share its geometry; their states are
  * interleaved member-fastest.  Each grid keeps its own dt and step count; the
  * grids' steps are spread evenly over the launch.  Member results equal the
- * single-run FP32 path (variant 1) bit for bit.  No counterpart in the
- * reference, which runs one instance per process. */
+ * single-run FP32 path (variant 1) bit for bit when both store h against the
+ * same reference depth (a grid's reference is the area mean of the first
+ * state set on it; other members differ from their own single runs at the
+ * 1e-7 level).  No counterpart in the reference, which runs one instance per
+ * process. */
 int imodel_swm_ensemble_create(const imodel_swm_mesh *meshes, int32_t ngrids,
                                const int32_t *members, int32_t testcase, int32_t device,
                                void **ens);
