@@ -98,11 +98,6 @@ __device__ __forceinline__ uint64_t f2pk(float lo, float hi) {
 __device__ __forceinline__ void f2upk(uint64_t r, float &lo, float &hi) {
   asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(r));
 }
-__device__ __forceinline__ uint64_t f2add(uint64_t a, uint64_t b) {
-  uint64_t r;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
 __device__ __forceinline__ uint64_t f2mul(uint64_t a, uint64_t b) {
   uint64_t r;
   asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
@@ -113,12 +108,12 @@ __device__ __forceinline__ uint64_t f2fma(uint64_t a, uint64_t b, uint64_t c) {
   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
   return r;
 }
-// TWICE the gelu of the pair z = (z0, z1) + (b0, b1), lane by lane:
+// TWICE the gelu of the pair z = (z0, z1), lane by lane:
 // z + z tanh(u) = 2 gelu(z) exactly (the halving in gelu() is exact), so the
 // forward kernel halves the weights that multiply it instead (W2 and w3, also
 // exact) and saves one multiply per pair
-__device__ __forceinline__ uint64_t gelu2x2(float z0, float z1, float b0, float b1) {
-  const uint64_t z = f2add(f2pk(z0, z1), f2pk(b0, b1));
+__device__ __forceinline__ uint64_t gelu2x2(float z0, float z1) {
+  const uint64_t z = f2pk(z0, z1);
   const uint64_t u = f2mul(f2fma(f2mul(z, z), f2pk(kGca, kGca), f2pk(kGc, kGc)), z);
   float u0, u1;
   f2upk(u, u0, u1);

@@ -5,7 +5,7 @@
 //                 one tile of 128 rows into the tile's BF16 input operand
 //                 (the dependent gathers of velocities etc.) and one FP32
 //                 context value per row
-//   6 - NG groups epilogue groups: TMEM -> registers, bias + GELU, the
+//   6 - NG groups epilogue groups: TMEM -> registers, GELU, the
 //                 BF16 hidden layer back to shared memory, and after the
 //                 second product the final GELU . w3 + b3 and the output
 //                 (2 GELU is formed, with W2 and w3 halved: exact)
@@ -13,7 +13,7 @@
 //                 (TMA, cp.async.bulk) of each tile's index block and the
 //                 tcgen05 MMAs of both layers
 // Shared memory holds NPF prefetched index blocks, NSTAGE input operands
-// (8 KiB each), NSLOT hidden-layer operands (16 KiB each); TMEM holds NSLOT
+// (8 KiB each), NSLOT hidden-layer operands (20 KiB each); TMEM holds NSLOT
 // tiles in flight, SLOTW = 80 columns each.  The first product has N = 80:
 // columns 0..63 are the hidden units and column 64 carries the row's context
 // value through the tensor core (the gather writes it as a BF16 pair hi + lo
@@ -42,13 +42,15 @@ using namespace tc05;
 // groups), the thread count and register budget are the same for all.
 constexpr int NGROUPS = 6, NSTAGE = 4, NSLOT = 6, NPF = 4;
 constexpr int N1 = 80, SLOTW = 80;  // layer-1 outputs: 64 hidden units, context, padding
+constexpr int K2 = 80;               // layer-2 inputs: 64 hidden units, two ones, padding
+constexpr int A2_BYTES = TM * K2 * 2;
 constexpr int WARPS = NGROUPS * 4 + 1;
 constexpr int THREADS = WARPS * 32;
 constexpr int PF_BYTES = 11264;  // largest index block of a task
-// dynamic shared memory: B1 5K | B2 8K | A1 ring 32K | A2 slots 96K |
+// dynamic shared memory: B1 5K | B2 10K | A1 ring 32K | A2 slots 120K |
 // index blocks 44K
-constexpr int OFF_B1S = 0, OFF_B2S = N1 * K1 * 2, OFF_A1S = OFF_B2S + 8192,
-              OFF_A2S = OFF_A1S + NSTAGE * 8192, OFF_PF = OFF_A2S + NSLOT * 16384,
+constexpr int OFF_B1S = 0, OFF_B2S = N1 * K1 * 2, OFF_A1S = OFF_B2S + NH * K2 * 2,
+              OFF_A2S = OFF_A1S + NSTAGE * 8192, OFF_PF = OFF_A2S + NSLOT * A2_BYTES,
               SMEM = OFF_PF + NPF * PF_BYTES;
 static_assert(NSLOT * SLOTW <= 512, "TMEM has 512 columns");
 static_assert(SMEM > 116 * 1024, "more than half of an SM's shared memory: one CTA per SM");
@@ -152,37 +154,50 @@ __global__ void __launch_bounds__(THREADS, 1)
   __shared__ Bars bar;
   __shared__ uint32_t tslot;
   __shared__ int abort_flag;
-  __shared__ __align__(16) float sb1[NH], sb2[NH], sw3[NH];
+  __shared__ __align__(16) float sw3[NH];
   uint8_t *B1s = smem + OFF_B1S, *B2s = smem + OFF_B2S;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   volatile int *abort = &abort_flag;
 
-  // layer-1 operand: W1 (rows 0..63) and the context row 64 (ones in input
-  // columns 24 and 25), rows 65..79 zero
+  // Operands that never change.  Input columns 24, 25 of a row hold its
+  // context as a BF16 pair hi + lo and columns 26, 27 hold ones; layer 1's
+  // operand B1 [80 outputs][32 inputs] is W1 in rows 0..63 with the bias b1
+  // as a pair hi + lo against the ones, and the context row 64 (ones against
+  // columns 24, 25).  Layer 2's operand B2 [64][80] is W2 / 2 (it multiplies
+  // 2 gelu, see gelu2x2; halving is exact) with the bias b2 as a pair against
+  // columns 64, 65 of the hidden-layer operand, which hold ones.  The biases
+  // thus enter the products with 16 significant bits.
   for (int i = tid; i < 4096 / 16; i += THREADS)
     reinterpret_cast<uint4 *>(B1s)[i] = reinterpret_cast<const uint4 *>(W.w1img)[i];
   for (int i = 4096 / 16 + tid; i < N1 * K1 * 2 / 16; i += THREADS)
     reinterpret_cast<uint4 *>(B1s)[i] = make_uint4(0, 0, 0, 0);
-  __syncthreads();
-  if (tid == 0) *reinterpret_cast<uint32_t *>(B1s + kmaj_off(64, 24, K1)) = pack2(1.0f, 1.0f);
-  // W2 and w3 halved (exact): they multiply 2 gelu, see gelu2x2
-  for (int i = tid; i < 8192 / 16; i += THREADS) {
-    uint4 q = reinterpret_cast<const uint4 *>(W.w2img)[i];
-    const __nv_bfloat162 h = __floats2bfloat162_rn(0.5f, 0.5f);
-    uint32_t *w = reinterpret_cast<uint32_t *>(&q);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      __nv_bfloat162 v = *reinterpret_cast<__nv_bfloat162 *>(&w[k]);
-      v = __hmul2(v, h);
-      w[k] = *reinterpret_cast<uint32_t *>(&v);
+  const uint16_t *w2 = W.w2img;
+  for (int i = tid; i < NH * K2; i += THREADS) {
+    const int o = i / K2, k = i % K2;
+    float v = 0.0f;
+    if (k < NH) {
+      v = 0.5f * __bfloat162float(__ushort_as_bfloat16(w2[kmaj_off(o, k, NH) / 2]));
+    } else if (k < NH + 2) {
+      const float b = W.p[OFF_B2 + o];
+      const float hi = __bfloat162float(__float2bfloat16_rn(b));
+      v = k == NH ? hi : b - hi;
     }
-    reinterpret_cast<uint4 *>(B2s)[i] = q;
+    *reinterpret_cast<uint16_t *>(B2s + kmaj_off(o, k, K2)) = bf16bits(v);
   }
+  for (int i = tid; i < NSLOT * TM; i += THREADS) {  // ones in hidden columns 64, 65
+    uint8_t *A2 = smem + OFF_A2S + (i / TM) * A2_BYTES;
+    const int r = i % TM;
+    *reinterpret_cast<uint4 *>(A2 + kmaj_off(r, NH, K2)) = make_uint4(pack2(1.0f, 1.0f), 0, 0, 0);
+    *reinterpret_cast<uint4 *>(A2 + kmaj_off(r, NH + 8, K2)) = make_uint4(0, 0, 0, 0);
+  }
+  __syncthreads();
   if (tid < NH) {
-    sb1[tid] = W.p[OFF_B1 + tid];
-    sb2[tid] = W.p[OFF_B2 + tid];
+    const float b = W.p[OFF_B1 + tid];
+    const float hi = __bfloat162float(__float2bfloat16_rn(b));
+    *reinterpret_cast<uint32_t *>(B1s + kmaj_off(tid, 26, K1)) = pack2(hi, b - hi);
     sw3[tid] = 0.5f * W.p[OFF_W3 + tid];
   }
+  if (tid == 0) *reinterpret_cast<uint32_t *>(B1s + kmaj_off(64, 24, K1)) = pack2(1.0f, 1.0f);
   if (tid == 0) {
     abort_flag = 0;
     for (int k = 0; k < NPF; ++k) {
@@ -222,9 +237,10 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int64_t row = tile_of(i) * TM + r;
       uint4 c[4];
       const float cx = task.stage(row, row < n, idx, c);
-      // the context as hi + lo in input columns 24, 25 (16 significant bits)
+      // the context as hi + lo in input columns 24, 25 (16 significant bits),
+      // ones in columns 26, 27 (the bias of layer 1)
       const float hi = __bfloat162float(__float2bfloat16_rn(cx));
-      c[3] = make_uint4(pack2(hi, cx - hi), 0, 0, 0);
+      c[3] = make_uint4(pack2(hi, cx - hi), pack2(1.0f, 1.0f), 0, 0);
       if (!wait_warp(&bar.a1_empty[s], ((i / NSTAGE) & 1) ^ 1, abort, err)) break;
       uint8_t *A1 = smem + OFF_A1S + s * 8192;
 #pragma unroll
@@ -242,27 +258,25 @@ __global__ void __launch_bounds__(THREADS, 1)
       const uint32_t tcol = tmem + lane_base + t * SLOTW;
       if (!wait_warp(&bar.acc1[t], par, abort, err)) break;
       fence_after_sync();
-      uint8_t *A2 = smem + OFF_A2S + t * 16384;
+      uint8_t *A2 = smem + OFF_A2S + t * A2_BYTES;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         float v[32];
         ld32(tcol + 32 * h, v);
 #pragma unroll
         for (int c8 = 0; c8 < 4; ++c8) {
-          const float4 ba = reinterpret_cast<const float4 *>(sb1)[8 * h + 2 * c8];
-          const float4 bb = reinterpret_cast<const float4 *>(sb1)[8 * h + 2 * c8 + 1];
           const float *w = v + 8 * c8;
           float gv[8];
-          f2upk(gelu2x2(w[0], w[1], ba.x, ba.y), gv[0], gv[1]);
-          f2upk(gelu2x2(w[2], w[3], ba.z, ba.w), gv[2], gv[3]);
-          f2upk(gelu2x2(w[4], w[5], bb.x, bb.y), gv[4], gv[5]);
-          f2upk(gelu2x2(w[6], w[7], bb.z, bb.w), gv[6], gv[7]);
+          f2upk(gelu2x2(w[0], w[1]), gv[0], gv[1]);
+          f2upk(gelu2x2(w[2], w[3]), gv[2], gv[3]);
+          f2upk(gelu2x2(w[4], w[5]), gv[4], gv[5]);
+          f2upk(gelu2x2(w[6], w[7]), gv[6], gv[7]);
           uint4 q;
           q.x = pack2(gv[0], gv[1]);
           q.y = pack2(gv[2], gv[3]);
           q.z = pack2(gv[4], gv[5]);
           q.w = pack2(gv[6], gv[7]);
-          *reinterpret_cast<uint4 *>(A2 + kmaj_off(r, 32 * h + 8 * c8, NH)) = q;
+          *reinterpret_cast<uint4 *>(A2 + kmaj_off(r, 32 * h + 8 * c8, K2)) = q;
         }
       }
       float cv[16];
@@ -282,11 +296,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         ld32(tcol + 32 * h, v);
 #pragma unroll
         for (int c4 = 0; c4 < 8; ++c4) {
-          const float4 bq = reinterpret_cast<const float4 *>(sb2)[8 * h + c4];
           const float4 wq = reinterpret_cast<const float4 *>(sw3)[8 * h + c4];
           const float *w = v + 4 * c4;
-          acc2 = f2fma(gelu2x2(w[0], w[1], bq.x, bq.y), f2pk(wq.x, wq.y), acc2);
-          acc2 = f2fma(gelu2x2(w[2], w[3], bq.z, bq.w), f2pk(wq.z, wq.w), acc2);
+          acc2 = f2fma(gelu2x2(w[0], w[1]), f2pk(wq.x, wq.y), acc2);
+          acc2 = f2fma(gelu2x2(w[2], w[3]), f2pk(wq.z, wq.w), acc2);
         }
       }
       float acc_e, acc_o;
@@ -333,10 +346,10 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (i2 < i1 && test_wait(&bar.a2_full[i2 % NSLOT], (i2 / NSLOT) & 1)) {
         const int t = i2 % NSLOT;
         fence_after_sync();
-        const uint32_t a2 = smem_u32(smem + OFF_A2S + t * 16384);
-        for (int k = 0; k < NH / 16; ++k)
-          mma(tmem + t * SLOTW, smem_desc(a2 + 256 * k, 128, NH * 16),
-              smem_desc(smem_u32(B2s) + 256 * k, 128, NH * 16), id64, k);
+        const uint32_t a2 = smem_u32(smem + OFF_A2S + t * A2_BYTES);
+        for (int k = 0; k < K2 / 16; ++k)
+          mma(tmem + t * SLOTW, smem_desc(a2 + 256 * k, 128, K2 * 16),
+              smem_desc(smem_u32(B2s) + 256 * k, 128, K2 * 16), id64, k);
         commit(&bar.acc2[t]);
         ++i2;
         progress = true;
