@@ -226,16 +226,28 @@ def exp_fixed(args, pool):
     nc, nf = swm.ntime_for(days, dtc), swm.ntime_for(days, dtf)
     ev = fields.PoolEvaluator(pool)
     hc, uc = fields.balanced_state(gc, lmax=64, seed=0, evaluator=ev)
-    hf, uf = fields.balanced_state(gf, lmax=64, seed=0, evaluator=ev)
-    ref = run(gf, args.ref_precision, hf, uf, dtf, nf, chunk=2000)
-    out = {"coarse": {"level": lc, "dt": dtc, "steps": nc},
-           "reference": dict(_summary(ref), level=lc + 1, dt=dtf, path=args.ref_precision)}
+    if args.load_ref:
+        # the fine run's h at the coarse nodes, saved by an earlier --save-ref
+        d = np.load(args.load_ref)
+        ref = {"h": d["h"]}
+        out = {"coarse": {"level": lc, "dt": dtc, "steps": nc},
+               "reference": {k: d[k].item() for k in d.files if k != "h"}}
+    else:
+        hf, uf = fields.balanced_state(gf, lmax=64, seed=0, evaluator=ev)
+        r = run(gf, args.ref_precision, hf, uf, dtf, nf, chunk=2000)
+        ref = {"h": r["h"][: gc.nv]}
+        out = {"coarse": {"level": lc, "dt": dtc, "steps": nc},
+               "reference": dict(_summary(r), level=lc + 1, dt=dtf, path=args.ref_precision)}
+        if args.save_ref:
+            np.savez(args.save_ref, h=ref["h"],
+                     **{k: np.array(v) for k, v in out["reference"].items() if v is not None})
     p = _params(args)
-    for path in ("fp64", "fp32", "fp32l"):
+    for path in [q for q in args.paths.split(",") if q]:
         r = run(gc, path, hc, uc, dtc, nc, params=p)
         out[path] = dict(_summary(r), h_vs_ref=_restrict_errors(r, ref, gc))
-    out["speedup_fp32l_vs_fp64"] = (out["fp32l"]["cell_steps_per_s"] /
-                                    out["fp64"]["cell_steps_per_s"])
+    if "fp32l" in out and "fp64" in out:
+        out["speedup_fp32l_vs_fp64"] = (out["fp32l"]["cell_steps_per_s"] /
+                                        out["fp64"]["cell_steps_per_s"])
     return out
 
 
@@ -269,6 +281,10 @@ def main(argv=None):
     ap.add_argument("--dt", type=float, default=0.0)
     ap.add_argument("--ref-precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--workers", type=int, default=0)
+    ap.add_argument("--paths", default="fp64,fp32,fp32l",
+                    help="coarse runs of 'fixed': fp64, fp32, fp32l (FP32 + learned)")
+    ap.add_argument("--save-ref", default="", help="'fixed': save the fine run's h (.npz)")
+    ap.add_argument("--load-ref", default="", help="'fixed': reuse a saved fine run")
     a = ap.parse_args(argv)
     pool = _pool(a.workers)
     results = {}
