@@ -474,7 +474,7 @@ def main():
             flop = MLP_FLOP_PER_EDGE * g.ne
             tf, tf_kind = load_tflops()
             ach = flop / (mlp_ms / 1000.0) / 1e12
-            line["mlp_roofline"] = {"bound": "tensor", "kernel": "k_mlp_apply<EdgeIn,CorrOut>",
+            line["mlp_roofline"] = {"bound": "tensor", "kernel": "k_mlp_pipe<EdgeTask>",
                                     "achieved": ach, "peak": tf, "unit": "TFLOP/s",
                                     "frac": ach / tf, "peak_source": tf_kind,
                                     "flop_per_launch": flop}
