@@ -291,13 +291,37 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__rest
   const double g = M.grav, erad = M.erad;
   double maxdiv = 0.0, umax = 0.0;
   double nan = 0.0;
-  for (int i = tid; i < M.nv; i += stride) {
+  if (!FULL) {
+    // energies for the learned correction's drift check: terms and each
+    // thread's few dozen-term sums in FP32 (the check compares with a value
+    // computed the same way, against a bound of 1e-3; FP64 operations are
+    // slow on this GPU), the thread sums merged in FP64
+    const float gf = static_cast<float>(g), hr = static_cast<float>(h_ref);
+    float pe = 0.0f, ke = 0.0f, um = 0.0f;
+    for (int i = tid; i < M.nv; i += stride) {
+      const float hi = static_cast<float>(h[i]) + hr;
+      if (!isfinite(hi)) nan = 1.0;
+      pe += static_cast<float>(M.c_areag[i]) * gf * hi *
+            (hi * 0.5f + static_cast<float>(M.c_bt[i]));
+    }
+    for (int e = tid; e < M.ne; e += stride) {
+      const float ue = static_cast<float>(u[e]);
+      if (!isfinite(ue)) nan = 1.0;
+      um = fmaxf(um, fabsf(ue));
+      const float he = (static_cast<float>(hs[M.e_v[e]]) +
+                        static_cast<float>(hs[M.e_v[M.ne + e]])) * 0.5f + hr;
+      ke += static_cast<float>(M.e_area[e]) * he * (ue * ue);
+    }
+    part[Q_PE] = pe;
+    part[Q_KE] = ke;
+    umax = um;
+  }
+  for (int i = tid; FULL && i < M.nv; i += stride) {
     const double A = M.c_areag[i];
     const double hi = static_cast<double>(h[i]) + h_ref;
     const double b = M.c_bt[i];
     if (!isfinite(hi)) nan = 1.0;
     part[Q_PE] += A * g * hi * (hi * 0.5 + b);
-    if (!FULL) continue;
     part[Q_AREA] += A;
     part[Q_AH] += A * hi;
     part[Q_AHB] += A * (hi + b);
@@ -313,7 +337,7 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__rest
     part[Q_ADIV2] += A * (d * d);
     maxdiv = fmax(maxdiv, fabs(d));
   }
-  for (int e = tid; e < M.ne; e += stride) {
+  for (int e = tid; FULL && e < M.ne; e += stride) {
     const double ue = static_cast<double>(u[e]);
     if (!isfinite(ue)) nan = 1.0;
     umax = fmax(umax, fabs(ue));
