@@ -411,6 +411,10 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
         (rc = upload(H, L.c_inva32, &M.c_inva32)) || (rc = upload(H, L.c_meta, &M.c_meta)) ||
         (rc = upload(H, L.e_vs, &M.e_vs)))
       return rc;
+    std::vector<float> c_area32(L.c_areag.begin(), L.c_areag.end());
+    std::vector<float> e_area32(L.e_area.begin(), L.e_area.end());
+    if ((rc = upload(H, c_area32, &M.c_area32)) || (rc = upload(H, e_area32, &M.e_area32)))
+      return rc;
     const int32_t *pk = nullptr;
     const float *kd = nullptr;
     const uint32_t *vs2 = nullptr;

@@ -29,6 +29,7 @@ struct DevMesh {
   // cell-centred TRSK variant (FP32)
   const int32_t *c_nb, *c_tr;
   const float *c_R32, *c_dg32, *c_inva32;
+  const float *c_area32, *e_area32;  // A_i and l_e d_e / 2 in FP32 (drift check)
   const uint32_t *c_meta, *e_vs;
   const int4 *c_pk;     // [6][nv] {edge, neighbour, triangle, kite fraction bits}
   const float2 *c_kd;   // [6][nv] {KE weight, ttgout*d}

@@ -296,13 +296,17 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__rest
     // thread's few dozen-term sums in FP32 (the check compares with a value
     // computed the same way, against a bound of 1e-3; FP64 operations are
     // slow on this GPU), the thread sums merged in FP64
+    // (FP32 handles read FP32 copies of the weights: even the conversions
+    // from FP64 would load the FP64 pipe)
+    constexpr bool f32 = sizeof(T) == sizeof(float);
     const float gf = static_cast<float>(g), hr = static_cast<float>(h_ref);
     float pe = 0.0f, ke = 0.0f, um = 0.0f;
     for (int i = tid; i < M.nv; i += stride) {
       const float hi = static_cast<float>(h[i]) + hr;
       if (!isfinite(hi)) nan = 1.0;
-      pe += static_cast<float>(M.c_areag[i]) * gf * hi *
-            (hi * 0.5f + static_cast<float>(M.c_bt[i]));
+      const float A = f32 ? M.c_area32[i] : static_cast<float>(M.c_areag[i]);
+      const float b = f32 ? M.c_bt32[i] : static_cast<float>(M.c_bt[i]);
+      pe += A * gf * hi * (hi * 0.5f + b);
     }
     for (int e = tid; e < M.ne; e += stride) {
       const float ue = static_cast<float>(u[e]);
@@ -310,7 +314,8 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__rest
       um = fmaxf(um, fabsf(ue));
       const float he = (static_cast<float>(hs[M.e_v[e]]) +
                         static_cast<float>(hs[M.e_v[M.ne + e]])) * 0.5f + hr;
-      ke += static_cast<float>(M.e_area[e]) * he * (ue * ue);
+      const float Ae = f32 ? M.e_area32[e] : static_cast<float>(M.e_area[e]);
+      ke += Ae * he * (ue * ue);
     }
     part[Q_PE] = pe;
     part[Q_KE] = ke;
