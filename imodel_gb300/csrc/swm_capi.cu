@@ -404,13 +404,19 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
   if (H->precision == IMODEL_SWM_FP32) {
     if ((rc = upload(H, L.c_div32, &M.c_div32)) || (rc = upload(H, L.c_kew32, &M.c_kew32)) ||
         (rc = upload(H, bt32, &M.c_bt32)) || (rc = upload(H, L.e_grad32, &M.e_grad32)) ||
-        (rc = upload(H, L.e_stc32, &M.e_stc32)) || (rc = upload(H, L.t_circ32, &M.t_circ32)) ||
-        (rc = upload(H, L.t_kite32, &M.t_kite32)) || (rc = upload(H, L.t_f32, &M.t_f32)) ||
+        (rc = upload(H, L.e_stc32, &M.e_stc32)) || (rc = upload(H, L.t_f32, &M.t_f32)) ||
         (rc = upload(H, L.c_nb, &M.c_nb)) || (rc = upload(H, L.c_tr, &M.c_tr)) ||
         (rc = upload(H, L.c_R32, &M.c_R32)) || (rc = upload(H, L.c_dg32, &M.c_dg32)) ||
         (rc = upload(H, L.c_inva32, &M.c_inva32)) || (rc = upload(H, L.c_meta, &M.c_meta)) ||
         (rc = upload(H, L.e_vs, &M.e_vs)))
       return rc;
+    const int32_t *ra = nullptr, *rb = nullptr, *rc32 = nullptr;
+    if ((rc = upload(H, L.t_recA, &ra)) || (rc = upload(H, L.t_recB, &rb)) ||
+        (rc = upload(H, L.t_recC, &rc32)))
+      return rc;
+    M.t_recA = reinterpret_cast<const int4 *>(ra);
+    M.t_recB = reinterpret_cast<const int4 *>(rb);
+    M.t_recC = reinterpret_cast<const float4 *>(rc32);
     std::vector<float> c_area32(L.c_areag.begin(), L.c_areag.end());
     std::vector<float> e_area32(L.e_area.begin(), L.e_area.end());
     if ((rc = upload(H, c_area32, &M.c_area32)) || (rc = upload(H, e_area32, &M.e_area32)))

@@ -25,7 +25,9 @@ struct DevMesh {
   // triangles
   const int32_t *t_ed, *t_v;
   const double *t_lt, *t_kite, *t_areag, *t_f;
-  const float *t_circ32, *t_kite32, *t_f32;
+  const float *t_f32;
+  const int4 *t_recA, *t_recB;  // [nt] packed triangle records (swm_layout.h)
+  const float4 *t_recC;
   // cell-centred TRSK variant (FP32)
   const int32_t *c_nb, *c_tr;
   const float *c_R32, *c_dg32, *c_inva32;

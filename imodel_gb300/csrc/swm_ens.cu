@@ -275,12 +275,18 @@ int ens_create(Ens *E, const imodel_swm_mesh *meshes, int ngrids, const int32_t 
     D.erad = L.erad;
     D.grav = L.grav;
     std::vector<float> bt32(L.nv, 0.0f);
+    const int32_t *ra = nullptr, *rb = nullptr, *rcc = nullptr;
+    if ((rc = up(E, L.t_recA, &ra)) || (rc = up(E, L.t_recB, &rb)) ||
+        (rc = up(E, L.t_recC, &rcc)))
+      return rc;
+    D.t_recA = reinterpret_cast<const int4 *>(ra);
+    D.t_recB = reinterpret_cast<const int4 *>(rb);
+    D.t_recC = reinterpret_cast<const float4 *>(rcc);
     const int32_t *pk = nullptr;
     const float *kd = nullptr;
     const uint32_t *vs2 = nullptr;
     const int32_t *cn2o = nullptr, *en2o = nullptr;
     if ((rc = up(E, L.t_ed, &D.t_ed)) || (rc = up(E, L.t_v, &D.t_v)) ||
-        (rc = up(E, L.t_circ32, &D.t_circ32)) || (rc = up(E, L.t_kite32, &D.t_kite32)) ||
         (rc = up(E, L.t_f32, &D.t_f32)) || (rc = up(E, L.c_meta, &D.c_meta)) ||
         (rc = up(E, L.c_inva32, &D.c_inva32)) || (rc = up(E, bt32, &D.c_bt32)) ||
         (rc = up(E, L.e_grad32, &D.e_grad32)) || (rc = up(E, L.c_pk, &pk)) ||

@@ -189,14 +189,14 @@ struct KSum {
 
 template <int NQ>
 __device__ void block_reduce_store(KSum (&acc)[NQ], double *__restrict__ scratch) {
-  // warp level
+  // warp level: plain sums of the sums and of the compensations (32 terms,
+  // error ~1e-15 relative; FP64 operations are slow on this GPU, and a
+  // Neumaier merge costs four times a plain add)
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     for (int off = 16; off > 0; off >>= 1) {
-      KSum o;
-      o.s = __shfl_down_sync(0xffffffffu, acc[q].s, off);
-      o.c = __shfl_down_sync(0xffffffffu, acc[q].c, off);
-      acc[q].merge(o);
+      acc[q].s += __shfl_down_sync(0xffffffffu, acc[q].s, off);
+      acc[q].c += __shfl_down_sync(0xffffffffu, acc[q].c, off);
     }
   }
   __shared__ double sh[kRedThreads / 32][NQ][2];
@@ -317,9 +317,37 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(DevMesh M, const T *__rest
       const float Ae = f32 ? M.e_area32[e] : static_cast<float>(M.e_area[e]);
       ke += Ae * he * (ue * ue);
     }
-    part[Q_PE] = pe;
-    part[Q_KE] = ke;
-    umax = um;
+    // warp sums in FP32, the block's warps in FP64; the other quantities'
+    // partials are zero
+    float ne = nan;
+    for (int off = 16; off > 0; off >>= 1) {
+      pe += __shfl_down_sync(0xffffffffu, pe, off);
+      ke += __shfl_down_sync(0xffffffffu, ke, off);
+      um = fmaxf(um, __shfl_down_sync(0xffffffffu, um, off));
+      ne = fmaxf(ne, __shfl_down_sync(0xffffffffu, ne, off));
+    }
+    __shared__ float se[4][kRedThreads / 32];
+    const int ln = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    if (ln == 0) {
+      se[0][wp] = pe;
+      se[1][wp] = ke;
+      se[2][wp] = um;
+      se[3][wp] = ne;
+    }
+    __syncthreads();
+    if (threadIdx.x < kDiagQ) {
+      const int q = threadIdx.x;
+      double v = 0.0;
+      for (int w = 0; w < kRedThreads / 32; ++w) {
+        if (q == Q_PE) v += static_cast<double>(se[0][w]);
+        if (q == Q_KE) v += static_cast<double>(se[1][w]);
+        if (q == Q_UMAX) v = fmax(v, static_cast<double>(se[2][w]));
+        if (q == Q_NAN) v = fmax(v, static_cast<double>(se[3][w]));
+      }
+      scratch[(q * gridDim.x + blockIdx.x) * 2] = v;
+      scratch[(q * gridDim.x + blockIdx.x) * 2 + 1] = 0.0;
+    }
+    return;
   }
   for (int i = tid; FULL && i < M.nv; i += stride) {
     const double A = M.c_areag[i];

@@ -308,6 +308,29 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
       L.t_kite32[s * NT + i] = static_cast<float>(m.tr_trhx_area[3 * static_cast<size_t>(t) + s] / A);
     }
   }
+  L.t_recA.resize(4 * NT);
+  L.t_recB.resize(4 * NT);
+  L.t_recC.resize(4 * NT);
+  auto bits = [](float f) {
+    int32_t b;
+    std::memcpy(&b, &f, sizeof(b));
+    return b;
+  };
+  for (size_t i = 0; i < NT; ++i) {
+    int32_t *a = &L.t_recA[4 * i], *b = &L.t_recB[4 * i], *c = &L.t_recC[4 * i];
+    a[0] = L.t_ed[i];
+    a[1] = L.t_ed[NT + i];
+    a[2] = L.t_ed[2 * NT + i];
+    a[3] = L.t_v[i];
+    b[0] = L.t_v[NT + i];
+    b[1] = L.t_v[2 * NT + i];
+    b[2] = bits(L.t_circ32[i]);
+    b[3] = bits(L.t_circ32[NT + i]);
+    c[0] = bits(L.t_circ32[2 * NT + i]);
+    c[1] = bits(L.t_kite32[i]);
+    c[2] = bits(L.t_kite32[NT + i]);
+    c[3] = bits(L.t_kite32[2 * NT + i]);
+  }
   return "";
 }
 

@@ -77,6 +77,10 @@ struct Layout {
   std::vector<double> t_kite;                // tr%trhx_area
   std::vector<double> t_areag;               // [nt]
   std::vector<double> t_f;                   // [nt] 2*omega*sin(lat_c)
+  // a triangle's FP32 stage inputs as three 16-byte records, [nt] each:
+  //   A {edge 0, edge 1, edge 2, cell 0}  B {cell 1, cell 2, circ 0, circ 1}
+  //   C {circ 2, kite 0, kite 1, kite 2}  (circ, kite: FP32 bit patterns)
+  std::vector<int32_t> t_recA, t_recB, t_recC;
   std::vector<float> t_circ32;               // l*tg/(A*erad)
   std::vector<float> t_kite32;               // kite/A
   std::vector<float> t_f32;
