@@ -109,8 +109,21 @@ __global__ void __launch_bounds__(512) k_cell32v2(DevMesh M, const float *__rest
   cell_body(M, i, OneRun{}, hd, u, q_tr, bern, zflux, yn, acc, yout, tend, stage, dt, grav, h_ref);
 }
 
-// two consecutive edges per thread: one 16-byte load of their cell words and
-// twice the independent loads in flight
+// the momentum tendency of edge e (edge_body's arithmetic): -grad B -
+// (Z_c1 + Z_c2) / l_e, plus the learned correction term
+__device__ __forceinline__ float edge_momeq(uint32_t wa, uint32_t wb, float g,
+                                           const float *__restrict__ bern,
+                                           const float *__restrict__ zflux, float erad) {
+  const int c1 = static_cast<int>(wa & 0x0FFFFFFFu), c2 = static_cast<int>(wb & 0x0FFFFFFFu);
+  const int s1 = static_cast<int>(wa >> 28), s2 = static_cast<int>(wb >> 28);
+  const float grad = (bern[c2] - bern[c1]) * g;
+  const float q = (zflux[6 * c1 + s1] + zflux[6 * c2 + s2]) * (g * erad);
+  return -grad - q;
+}
+
+// two consecutive edges per thread: one 16-byte load of their cell words,
+// 8-byte loads and stores of their per-edge values, and twice the
+// independent gathers in flight
 __global__ void __launch_bounds__(512) k_edge32v2(DevMesh M, const float *__restrict__ bern,
                                                   const float *__restrict__ zflux,
                                                   const float *__restrict__ yn,
@@ -124,10 +137,27 @@ __global__ void __launch_bounds__(512) k_edge32v2(DevMesh M, const float *__rest
   if (e0 >= M.ne) return;
   if (e0 + 1 < M.ne) {
     const uint4 w = __ldg(reinterpret_cast<const uint4 *>(M.e_vs2) + p);
-    edge_body(M, e0, OneRun{}, make_uint2(w.x, w.y), bern, zflux, yn, acc, yout, tend, stage, dt,
-              mom_on, erad, corr);
-    edge_body(M, e0 + 1, OneRun{}, make_uint2(w.z, w.w), bern, zflux, yn, acc, yout, tend, stage,
-              dt, mom_on, erad, corr);
+    const float2 g = __ldg(reinterpret_cast<const float2 *>(M.e_grad32) + p);
+    float m0 = edge_momeq(w.x, w.y, g.x, bern, zflux, erad);
+    float m1 = edge_momeq(w.z, w.w, g.y, bern, zflux, erad);
+    // learned correction of the PV flux (frozen over the RK step)
+    if (corr) {
+      const float2 c = reinterpret_cast<const float2 *>(corr)[p];
+      m0 += c.x;
+      m1 += c.y;
+    }
+    if (!mom_on) m0 = m1 = 0.0f;
+    if (stage < 0) {
+      reinterpret_cast<float2 *>(tend)[p] = make_float2(m0, m1);
+    } else {
+      const float2 y = reinterpret_cast<const float2 *>(yn)[p];
+      // stage 0 only writes the accumulator
+      float2 a = stage == 0 ? make_float2(0.0f, 0.0f) : reinterpret_cast<float2 *>(acc)[p];
+      const float o0 = rk_stage32(stage, m0, y.x, &a.x, dt);
+      const float o1 = rk_stage32(stage, m1, y.y, &a.y, dt);
+      if (stage < 3) reinterpret_cast<float2 *>(acc)[p] = a;
+      reinterpret_cast<float2 *>(yout)[p] = make_float2(o0, o1);
+    }
   } else {
     edge_body(M, e0, OneRun{}, __ldg(&M.e_vs2[e0]), bern, zflux, yn, acc, yout, tend, stage, dt,
               mom_on, erad, corr);
