@@ -224,38 +224,45 @@ __device__ void block_reduce_store(KSum (&acc)[NQ], double *__restrict__ scratch
 // one block: quantity q summed over nblk partials; "max" quantities use max
 __global__ void k_finalize(const double *__restrict__ scratch, int nblk, int nq,
                            unsigned maxmask, double *__restrict__ result) {
+  // one block per quantity; the partials are combined as a tree (a few
+  // dependent compensated merges per thread, then 5 shuffle levels per warp
+  // and 3 across the warps) rather than by one thread in a row: FP64
+  // operations have a long latency on this GPU
   const int q = blockIdx.x;
   if (q >= nq) return;
-  __shared__ double ss[kRedThreads], sc[kRedThreads];
+  static_assert(kRedThreads == 256, "8 warps per block");
+  __shared__ double ss[8], sc[8];
   const bool is_max = (maxmask >> q) & 1u;
   KSum a{0.0, 0.0};
-  double m = 0.0;
   for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
     const double s = scratch[(q * nblk + b) * 2], c = scratch[(q * nblk + b) * 2 + 1];
     if (is_max) {
-      m = fmax(m, s);
+      a.s = fmax(a.s, s);
     } else {
       KSum o{s, c};
       a.merge(o);
     }
   }
-  ss[threadIdx.x] = is_max ? m : a.s;
-  sc[threadIdx.x] = is_max ? 0.0 : a.c;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    if (is_max) {
-      double r = 0.0;
-      for (int t = 0; t < blockDim.x; ++t) r = fmax(r, ss[t]);
-      result[q] = r;
-    } else {
-      KSum r{0.0, 0.0};
-      for (int t = 0; t < blockDim.x; ++t) {
-        KSum o{ss[t], sc[t]};
-        r.merge(o);
-      }
-      result[q] = r.s + r.c;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int level = 0; level < 2; ++level) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      KSum o{__shfl_down_sync(0xffffffffu, a.s, off), __shfl_down_sync(0xffffffffu, a.c, off)};
+      if (is_max)
+        a.s = fmax(a.s, o.s);
+      else
+        a.merge(o);
     }
+    if (level == 1) break;
+    if (lane == 0) {
+      ss[warp] = a.s;
+      sc[warp] = a.c;
+    }
+    __syncthreads();
+    if (warp != 0) return;
+    a = lane < 8 ? KSum{ss[lane], sc[lane]} : KSum{0.0, 0.0};
   }
+  if (threadIdx.x == 0) result[q] = is_max ? a.s : a.s + a.c;
 }
 
 // a / b for the diagnostics: FP64 division is slow on GB300's FP64 pipe, so
