@@ -3,6 +3,7 @@
 // A handle owns the device copy of the mesh layout, the state buffers of
 // classic RK4 and one CUDA stream.  One RK4 step is 4 stages x 4 kernels;
 // it is captured once into a CUDA graph per time step length and replayed.
+#include <cuda.h>  // pointer-attribute types only; the driver call is resolved at run time
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -33,6 +34,9 @@ struct Handle {
   DevMesh M{};
   std::vector<void *> allocs;
   int32_t *d_cell_n2o = nullptr, *d_edge_n2o = nullptr;
+  int32_t *d_cell_o2n = nullptr, *d_edge_o2n = nullptr;
+  // cuPointerGetAttribute, for the extent of a caller's page-locked array
+  CUresult (*range_attr)(void *, CUpointer_attribute, CUdeviceptr) = nullptr;
   double *d_stage_h = nullptr, *d_stage_u = nullptr;  // FP64, reference order
   double *d_ref_h = nullptr, *d_ref_u = nullptr;      // FP64, device order
   double *d_scratch = nullptr, *d_result = nullptr;
@@ -158,6 +162,30 @@ int ensure_graph(Handle *H, double dt) {
   return IMODEL_SWM_OK;
 }
 
+// A device address of a caller's host array of `bytes` bytes when the array
+// lies wholly inside page-locked memory known to CUDA (cudaMallocHost,
+// cudaHostAlloc, cudaHostRegister) and mapped for this handle's device;
+// nullptr otherwise, and the array then goes through cudaMemcpyAsync.  The
+// extent check keeps a kernel from reaching past the caller's allocation.
+void *host_view(Handle *H, const void *p, size_t bytes) {
+  if (!H->range_attr || !p) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer || a.device != H->device) return nullptr;
+  CUdeviceptr start = 0;
+  size_t size = 0;
+  const CUdeviceptr q = reinterpret_cast<CUdeviceptr>(p);
+  if (H->range_attr(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, q) != CUDA_SUCCESS ||
+      H->range_attr(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, q) != CUDA_SUCCESS)
+    return nullptr;
+  if (q < start || q - start > size || bytes > size - (q - start)) return nullptr;
+  // the device address keeps p's offset inside the allocation
+  return static_cast<char *>(a.devicePointer);
+}
+
 // host FP64 arrays (reference order) -> device state yn, plus h_ed and the
 // "last stage input" ya, as after the reference's initial tendency call
 // (swm.f90:214)
@@ -177,15 +205,31 @@ int load_state(Handle *H, const double *h, const double *u, bool new_run) {
     H->h_ref = static_cast<double>(H->W32.h_ref);
     H->href_fixed = true;
   }
-  CK(cudaMemcpyAsync(H->d_stage_h, h, sizeof(double) * H->nv, cudaMemcpyHostToDevice, H->stream));
-  CK(cudaMemcpyAsync(H->d_stage_u, u, sizeof(double) * H->ne, cudaMemcpyHostToDevice, H->stream));
-  if (H->precision == IMODEL_SWM_FP64) {
+  const double *hz = static_cast<const double *>(host_view(H, h, sizeof(double) * H->nv));
+  const double *uz = static_cast<const double *>(host_view(H, u, sizeof(double) * H->ne));
+  if (hz && uz) {
+    // page-locked arrays: one kernel per array reads them over the host link
+    // in order and writes yn and ya in device order (no staging copy)
+    if (H->precision == IMODEL_SWM_FP64) {
+      Work<double> &W = H->W64;
+      launch_load_host(H->nv, H->d_cell_o2n, hz, W.yn_h, W.ya_h, 0.0, H->stream);
+      launch_load_host(H->ne, H->d_edge_o2n, uz, W.yn_u, W.ya_u, 0.0, H->stream);
+    } else {
+      Work<float> &W = H->W32;
+      launch_load_host(H->nv, H->d_cell_o2n, hz, W.yn_h, W.ya_h, H->h_ref, H->stream);
+      launch_load_host(H->ne, H->d_edge_o2n, uz, W.yn_u, W.ya_u, 0.0, H->stream);
+    }
+  } else if (H->precision == IMODEL_SWM_FP64) {
+    CK(cudaMemcpyAsync(H->d_stage_h, h, sizeof(double) * H->nv, cudaMemcpyHostToDevice, H->stream));
+    CK(cudaMemcpyAsync(H->d_stage_u, u, sizeof(double) * H->ne, cudaMemcpyHostToDevice, H->stream));
     Work<double> &W = H->W64;
     launch_gather_in(H->nv, H->d_cell_n2o, H->d_stage_h, W.yn_h, 0.0, H->stream);
     launch_gather_in(H->ne, H->d_edge_n2o, H->d_stage_u, W.yn_u, 0.0, H->stream);
     CK(cudaMemcpyAsync(W.ya_h, W.yn_h, sizeof(double) * H->nv, cudaMemcpyDeviceToDevice, H->stream));
     CK(cudaMemcpyAsync(W.ya_u, W.yn_u, sizeof(double) * H->ne, cudaMemcpyDeviceToDevice, H->stream));
   } else {
+    CK(cudaMemcpyAsync(H->d_stage_h, h, sizeof(double) * H->nv, cudaMemcpyHostToDevice, H->stream));
+    CK(cudaMemcpyAsync(H->d_stage_u, u, sizeof(double) * H->ne, cudaMemcpyHostToDevice, H->stream));
     Work<float> &W = H->W32;
     launch_gather_in32(H->nv, H->d_cell_n2o, H->d_stage_h, W.yn_h, H->h_ref, H->stream);
     launch_gather_in32(H->ne, H->d_edge_n2o, H->d_stage_u, W.yn_u, 0.0, H->stream);
@@ -210,6 +254,21 @@ int load_state(Handle *H, const double *h, const double *u, bool new_run) {
 }
 
 int store_state(Handle *H, double *h, double *u) {
+  double *hz = static_cast<double *>(host_view(H, h, sizeof(double) * H->nv));
+  double *uz = static_cast<double *>(host_view(H, u, sizeof(double) * H->ne));
+  if (hz && uz) {
+    // page-locked arrays: written in order over the host link by the
+    // kernels that undo the permutation (no staging copy)
+    if (H->precision == IMODEL_SWM_FP64) {
+      launch_store_host(H->nv, H->d_cell_o2n, H->W64.yn_h, hz, 0.0, H->d_flags, H->stream);
+      launch_store_host(H->ne, H->d_edge_o2n, H->W64.yn_u, uz, 0.0, H->d_flags, H->stream);
+    } else {
+      launch_store_host(H->nv, H->d_cell_o2n, H->W32.yn_h, hz, H->h_ref, H->d_flags, H->stream);
+      launch_store_host(H->ne, H->d_edge_o2n, H->W32.yn_u, uz, 0.0, H->d_flags, H->stream);
+    }
+    CK(cudaGetLastError());
+    return IMODEL_SWM_OK;
+  }
   if (H->precision == IMODEL_SWM_FP64) {
     launch_scatter_out(H->nv, H->d_cell_n2o, H->W64.yn_h, H->d_stage_h, 0.0, H->d_flags, H->stream);
     launch_scatter_out(H->ne, H->d_edge_n2o, H->W64.yn_u, H->d_stage_u, 0.0, H->d_flags, H->stream);
@@ -436,6 +495,19 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
   if ((rc = upload(H, L.cell_n2o, &cn2o)) || (rc = upload(H, L.edge_n2o, &en2o))) return rc;
   H->d_cell_n2o = const_cast<int32_t *>(cn2o);
   H->d_edge_n2o = const_cast<int32_t *>(en2o);
+  const int32_t *co2n = nullptr, *eo2n = nullptr;
+  if ((rc = upload(H, L.cell_o2n, &co2n)) || (rc = upload(H, L.edge_o2n, &eo2n))) return rc;
+  H->d_cell_o2n = const_cast<int32_t *>(co2n);
+  H->d_edge_o2n = const_cast<int32_t *>(eo2n);
+  {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult qr;
+    if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &fn, 12000, cudaEnableDefault,
+                                         &qr) == cudaSuccess &&
+        qr == cudaDriverEntryPointSuccess)
+      H->range_attr = reinterpret_cast<CUresult (*)(void *, CUpointer_attribute, CUdeviceptr)>(fn);
+    cudaGetLastError();
+  }
   if ((rc = dalloc(H, &H->d_stage_h, L.nv)) || (rc = dalloc(H, &H->d_stage_u, L.ne)) ||
       (rc = dalloc(H, &H->d_ref_h, L.nv)) || (rc = dalloc(H, &H->d_ref_u, L.ne)) ||
       (rc = dalloc(H, &H->d_scratch, static_cast<size_t>(2) * kRedBlocks * 16)) ||

@@ -156,6 +156,32 @@ __global__ void k_scatter_out(int n, const int32_t *__restrict__ n2o, const T *_
   }
 }
 
+// j runs over the reference order, so that the host array is read (or
+// written) in order; the device side takes the permutation
+template <class T>
+__global__ void k_load_host(int n, const int32_t *__restrict__ o2n,
+                            const double *__restrict__ src, T *__restrict__ yn,
+                            T *__restrict__ ya, double shift) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) {
+    const T v = static_cast<T>(src[j] - shift);
+    const int i = o2n[j];
+    yn[i] = v;
+    ya[i] = v;
+  }
+}
+
+template <class T>
+__global__ void k_store_host(int n, const int32_t *__restrict__ o2n, const T *__restrict__ src,
+                             double *__restrict__ dst, double shift, int *flags) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) {
+    const double v = static_cast<double>(src[o2n[j]]) + shift;
+    dst[j] = v;
+    if (!isfinite(v)) atomicOr(flags, 2);
+  }
+}
+
 // vecrecon_trsk_tg, interpack.f90:3852-3976 (var%pos == 6)
 __global__ void k_trsk_tangent(DevMesh M, const double *__restrict__ u, double *__restrict__ utg) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -514,6 +540,25 @@ void launch_scatter_out32(int n, const int32_t *n2o, const float *src, double *d
                           double shift, int *flags, cudaStream_t s) {
   k_scatter_out<float><<<nblocks(n, 256), 256, 0, s>>>(n, n2o, src, dst, shift, flags);
 }
+
+template <class T>
+void launch_load_host(int n, const int32_t *o2n, const double *src, T *yn, T *ya, double shift,
+                      cudaStream_t s) {
+  k_load_host<T><<<nblocks(n, 256), 256, 0, s>>>(n, o2n, src, yn, ya, shift);
+}
+template <class T>
+void launch_store_host(int n, const int32_t *o2n, const T *src, double *dst, double shift,
+                       int *flags, cudaStream_t s) {
+  k_store_host<T><<<nblocks(n, 256), 256, 0, s>>>(n, o2n, src, dst, shift, flags);
+}
+template void launch_load_host<double>(int, const int32_t *, const double *, double *, double *,
+                                       double, cudaStream_t);
+template void launch_load_host<float>(int, const int32_t *, const double *, float *, float *,
+                                      double, cudaStream_t);
+template void launch_store_host<double>(int, const int32_t *, const double *, double *, double,
+                                        int *, cudaStream_t);
+template void launch_store_host<float>(int, const int32_t *, const float *, double *, double,
+                                       int *, cudaStream_t);
 
 void launch_trsk_tangent(const DevMesh &M, const double *u, double *utg, cudaStream_t s) {
   k_trsk_tangent<<<nblocks(M.ne, 256), 256, 0, s>>>(M, u, utg);
