@@ -59,6 +59,11 @@ struct Handle {
   // state at the start of the current guard interval, restored when the
   // interval ends past the drift bound (or with a non-finite energy)
   float *ck_h = nullptr, *ck_u = nullptr;
+  bool ck_fresh = false;  // ck holds yn (written by the page-locked load)
+  // a second stream for the energy check, which runs beside the write-back
+  // of the state in imodel_swm_step
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_steps = nullptr, ev_side = nullptr;
 };
 
 // steps between two checks of the learned correction's energy drift
@@ -210,14 +215,20 @@ int load_state(Handle *H, const double *h, const double *u, bool new_run) {
   if (hz && uz) {
     // page-locked arrays: one kernel per array reads them over the host link
     // in order and writes yn and ya in device order (no staging copy)
+    // (and, with the learned correction on, the guard's checkpoint)
     if (H->precision == IMODEL_SWM_FP64) {
       Work<double> &W = H->W64;
-      launch_load_host(H->nv, H->d_cell_o2n, hz, W.yn_h, W.ya_h, 0.0, H->stream);
-      launch_load_host(H->ne, H->d_edge_o2n, uz, W.yn_u, W.ya_u, 0.0, H->stream);
+      launch_load_host<double>(H->nv, H->d_cell_o2n, hz, W.yn_h, W.ya_h, nullptr, 0.0, H->stream);
+      launch_load_host<double>(H->ne, H->d_edge_o2n, uz, W.yn_u, W.ya_u, nullptr, 0.0, H->stream);
+      H->ck_fresh = false;
     } else {
       Work<float> &W = H->W32;
-      launch_load_host(H->nv, H->d_cell_o2n, hz, W.yn_h, W.ya_h, H->h_ref, H->stream);
-      launch_load_host(H->ne, H->d_edge_o2n, uz, W.yn_u, W.ya_u, 0.0, H->stream);
+      const bool ck = H->learned_on;
+      launch_load_host(H->nv, H->d_cell_o2n, hz, W.yn_h, W.ya_h, ck ? H->ck_h : nullptr,
+                       H->h_ref, H->stream);
+      launch_load_host(H->ne, H->d_edge_o2n, uz, W.yn_u, W.ya_u, ck ? H->ck_u : nullptr, 0.0,
+                       H->stream);
+      H->ck_fresh = ck;
     }
   } else if (H->precision == IMODEL_SWM_FP64) {
     CK(cudaMemcpyAsync(H->d_stage_h, h, sizeof(double) * H->nv, cudaMemcpyHostToDevice, H->stream));
@@ -236,6 +247,7 @@ int load_state(Handle *H, const double *h, const double *u, bool new_run) {
     CK(cudaMemcpyAsync(W.ya_h, W.yn_h, sizeof(float) * H->nv, cudaMemcpyDeviceToDevice, H->stream));
     CK(cudaMemcpyAsync(W.ya_u, W.yn_u, sizeof(float) * H->ne, cudaMemcpyDeviceToDevice, H->stream));
   }
+  if (!(hz && uz)) H->ck_fresh = false;
   CK(cudaGetLastError());
   H->state_set = true;
   if (H->learned_on && (new_run || !H->te_ref_set)) {
@@ -284,12 +296,17 @@ int store_state(Handle *H, double *h, double *u) {
   return IMODEL_SWM_OK;
 }
 
-// reads and clears the device flags; maps them to a status
-int check_flags(Handle *H) {
+// reads and clears the device flags (synchronising the stream)
+int read_flags(Handle *H, int *f) {
   CK(cudaMemcpyAsync(H->h_flags, H->d_flags, sizeof(int), cudaMemcpyDeviceToHost, H->stream));
   CK(cudaMemsetAsync(H->d_flags, 0, sizeof(int), H->stream));
   CK(cudaStreamSynchronize(H->stream));
-  const int f = *H->h_flags;
+  *f = *H->h_flags;
+  return IMODEL_SWM_OK;
+}
+
+// maps device flags to a status
+int flags_status(Handle *H, int f) {
   if (f & 1)
     return set_error(H, IMODEL_SWM_EDIVZERO,
                      "division by zero in PV (|h_tr| < eps/1e5), as scalar_elem_divide stops");
@@ -297,20 +314,33 @@ int check_flags(Handle *H) {
   return IMODEL_SWM_OK;
 }
 
+int check_flags(Handle *H) {
+  int f = 0;
+  const int rc = read_flags(H, &f);
+  return rc ? rc : flags_status(H, f);
+}
+
 // total energy of the current state (compensated FP64 integral) and max |u|
-int total_energy(Handle *H, double *te, double *umax) {
+// enqueues it on stream s, with the read-back into h_result
+int enqueue_energy(Handle *H, cudaStream_t s) {
   if (H->precision == IMODEL_SWM_FP64) {
     auto &W = H->W64;
-    launch_diag<double>(H->M, W, W.yn_h, W.yn_u, W.ya_h, W.ya_u, H->d_scratch, H->d_result,
-                        H->stream, true);
+    launch_diag<double>(H->M, W, W.yn_h, W.yn_u, W.ya_h, W.ya_u, H->d_scratch, H->d_result, s,
+                        true);
   } else {
     auto &W = H->W32;
-    launch_diag<float>(H->M, W, W.yn_h, W.yn_u, W.ya_h, W.ya_u, H->d_scratch, H->d_result,
-                       H->stream, true);
+    launch_diag<float>(H->M, W, W.yn_h, W.yn_u, W.ya_h, W.ya_u, H->d_scratch, H->d_result, s,
+                       true);
   }
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(H->h_result, H->d_result, sizeof(double) * kDiagQ, cudaMemcpyDeviceToHost,
-                     H->stream));
+                     s));
+  return IMODEL_SWM_OK;
+}
+
+int total_energy(Handle *H, double *te, double *umax) {
+  int rc = enqueue_energy(H, H->stream);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(H->stream));
   *te = H->h_result[Q_PE] + H->h_result[Q_KE];
   *umax = H->h_result[Q_UMAX];
@@ -321,35 +351,66 @@ int total_energy(Handle *H, double *te, double *umax) {
 // energy since the state was set exceeds the bound (or the energy is not
 // finite), the plain TRSK scheme takes over for the rest of the run.
 // *tripped tells the caller that the guard switched the correction off.
+// the decision on a measured energy and max |u|; true when it switched the
+// correction off
+bool guard_decide(Handle *H, double te, double umax) {
+  if (!H->te_ref_set) {
+    H->te_ref = te;
+    H->umax_ref = umax;
+    H->te_ref_set = true;
+    return false;
+  }
+  const double drift = std::fabs(te - H->te_ref) / std::fabs(H->te_ref);
+  if (drift <= H->drift_bound && umax <= kUmaxGrowth * H->umax_ref) return false;
+  H->learned_active = false;
+  H->W32.learned = nullptr;
+  if (H->graph) {
+    cudaGraphExecDestroy(H->graph);
+    H->graph = nullptr;
+  }
+  return true;
+}
+
 int learned_guard(Handle *H, bool *tripped) {
   if (tripped) *tripped = false;
   if (!H->learned_active) return IMODEL_SWM_OK;
   double te = 0.0, umax = 0.0;
   int rc = total_energy(H, &te, &umax);
   if (rc) return rc;
-  if (!H->te_ref_set) {
-    H->te_ref = te;
-    H->umax_ref = umax;
-    H->te_ref_set = true;
-    return IMODEL_SWM_OK;
-  }
-  const double drift = std::fabs(te - H->te_ref) / std::fabs(H->te_ref);
-  if (!(drift <= H->drift_bound) || !(umax <= kUmaxGrowth * H->umax_ref)) {
-    H->learned_active = false;
-    H->W32.learned = nullptr;
-    if (H->graph) {
-      cudaGraphExecDestroy(H->graph);
-      H->graph = nullptr;
-    }
-    if (tripped) *tripped = true;
-  }
+  const bool t = guard_decide(H, te, umax);
+  if (tripped) *tripped = t;
   return IMODEL_SWM_OK;
 }
 
 int launch_steps(Handle *H, double dt, int nsteps) {
   int rc = ensure_graph(H, dt);
   if (rc) return rc;
+  H->ck_fresh = false;
   for (int k = 0; k < nsteps; ++k) CK(cudaGraphLaunch(H->graph, H->stream));
+  return IMODEL_SWM_OK;
+}
+
+// copies the state aside at the start of a guard interval (unless the
+// page-locked load already wrote the copy)
+int save_checkpoint(Handle *H) {
+  if (H->ck_fresh) return IMODEL_SWM_OK;
+  auto &W = H->W32;
+  CK(cudaMemcpyAsync(H->ck_h, W.yn_h, sizeof(float) * H->nv, cudaMemcpyDeviceToDevice, H->stream));
+  CK(cudaMemcpyAsync(H->ck_u, W.yn_u, sizeof(float) * H->ne, cudaMemcpyDeviceToDevice, H->stream));
+  H->ck_fresh = true;
+  return IMODEL_SWM_OK;
+}
+
+// back to the state at the start of the interval
+int roll_back(Handle *H) {
+  auto &W = H->W32;
+  const size_t bh = sizeof(float) * H->nv, bu = sizeof(float) * H->ne;
+  CK(cudaMemcpyAsync(W.yn_h, H->ck_h, bh, cudaMemcpyDeviceToDevice, H->stream));
+  CK(cudaMemcpyAsync(W.yn_u, H->ck_u, bu, cudaMemcpyDeviceToDevice, H->stream));
+  CK(cudaMemcpyAsync(W.ya_h, H->ck_h, bh, cudaMemcpyDeviceToDevice, H->stream));
+  CK(cudaMemcpyAsync(W.ya_u, H->ck_u, bu, cudaMemcpyDeviceToDevice, H->stream));
+  // flags raised by the rolled-back steps do not describe the state
+  CK(cudaMemsetAsync(H->d_flags, 0, sizeof(int), H->stream));
   return IMODEL_SWM_OK;
 }
 
@@ -363,29 +424,52 @@ int advance(Handle *H, double dt, int nsteps) {
   if (nsteps < 0 || !(std::isfinite(dt))) return set_error(H, IMODEL_SWM_EINVAL, "bad dt or nsteps");
   if (nsteps == 0) return IMODEL_SWM_OK;
   if (!H->learned_active) return launch_steps(H, dt, nsteps);
-  auto &W = H->W32;
-  const size_t bh = sizeof(float) * H->nv, bu = sizeof(float) * H->ne;
   for (int done = 0; done < nsteps;) {
     const int k = std::min(kGuardSteps, nsteps - done);
     if (!H->learned_active) return launch_steps(H, dt, nsteps - done);
-    CK(cudaMemcpyAsync(H->ck_h, W.yn_h, bh, cudaMemcpyDeviceToDevice, H->stream));
-    CK(cudaMemcpyAsync(H->ck_u, W.yn_u, bu, cudaMemcpyDeviceToDevice, H->stream));
-    int rc = launch_steps(H, dt, k);
+    int rc = save_checkpoint(H);
     if (rc) return rc;
+    if ((rc = launch_steps(H, dt, k))) return rc;
     bool tripped = false;
     if ((rc = learned_guard(H, &tripped))) return rc;
     if (tripped) {
-      CK(cudaMemcpyAsync(W.yn_h, H->ck_h, bh, cudaMemcpyDeviceToDevice, H->stream));
-      CK(cudaMemcpyAsync(W.yn_u, H->ck_u, bu, cudaMemcpyDeviceToDevice, H->stream));
-      CK(cudaMemcpyAsync(W.ya_h, H->ck_h, bh, cudaMemcpyDeviceToDevice, H->stream));
-      CK(cudaMemcpyAsync(W.ya_u, H->ck_u, bu, cudaMemcpyDeviceToDevice, H->stream));
-      // flags raised by the rolled-back steps do not describe the state
-      CK(cudaMemsetAsync(H->d_flags, 0, sizeof(int), H->stream));
+      if ((rc = roll_back(H))) return rc;
       if ((rc = launch_steps(H, dt, k))) return rc;
     }
     done += k;
   }
   return IMODEL_SWM_OK;
+}
+
+// imodel_swm_step with host arrays.  With the learned correction on and at
+// most one guard interval of steps, the energy check runs on the second
+// stream while the state is written back, and one synchronisation serves
+// the check and the flags; a failed check rolls the interval back, steps it
+// with the plain scheme and writes the state back again.
+int step_host(Handle *H, double *h, double *u, double dt, int nsteps) {
+  int rc = load_state(H, h, u, false);
+  if (rc) return rc;
+  const bool overlap = H->learned_active && H->te_ref_set && H->side && nsteps > 0 &&
+                       nsteps <= kGuardSteps && std::isfinite(dt);
+  if (!overlap) {
+    if ((rc = advance(H, dt, nsteps)) || (rc = store_state(H, h, u))) return rc;
+    return check_flags(H);
+  }
+  if ((rc = save_checkpoint(H)) || (rc = launch_steps(H, dt, nsteps))) return rc;
+  CK(cudaEventRecord(H->ev_steps, H->stream));
+  CK(cudaStreamWaitEvent(H->side, H->ev_steps, 0));
+  if ((rc = enqueue_energy(H, H->side))) return rc;
+  CK(cudaEventRecord(H->ev_side, H->side));
+  if ((rc = store_state(H, h, u))) return rc;
+  CK(cudaStreamWaitEvent(H->stream, H->ev_side, 0));
+  int f = 0;
+  if ((rc = read_flags(H, &f))) return rc;
+  const double te = H->h_result[Q_PE] + H->h_result[Q_KE];
+  if (!guard_decide(H, te, H->h_result[Q_UMAX])) return flags_status(H, f);
+  if ((rc = roll_back(H)) || (rc = launch_steps(H, dt, nsteps)) ||
+      (rc = store_state(H, h, u)))
+    return rc;
+  return check_flags(H);
 }
 
 int setup_learned(Handle *H, const imodel_swm_mesh *m, const Layout &L, const imodel_swm_opts *o) {
@@ -402,6 +486,9 @@ int setup_learned(Handle *H, const imodel_swm_mesh *m, const Layout &L, const im
       (rc = dalloc(H, &H->ck_h, static_cast<size_t>(L.nv))) ||
       (rc = dalloc(H, &H->ck_u, static_cast<size_t>(L.ne))))
     return rc;
+  CK(cudaStreamCreateWithFlags(&H->side, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&H->ev_steps, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&H->ev_side, cudaEventDisableTiming));
   rc = learned_prepare(static_cast<const float *>(o->mlp_weights), &H->learned, H->stream);
   if (H->learned.p) H->allocs.push_back(H->learned.p);
   if (H->learned.img) H->allocs.push_back(H->learned.img);
@@ -535,6 +622,10 @@ void destroy(Handle *H) {
   for (void *p : H->allocs) cudaFree(p);
   if (H->h_flags) cudaFreeHost(H->h_flags);
   if (H->h_result) cudaFreeHost(H->h_result);
+  if (H->side) cudaStreamSynchronize(H->side);
+  if (H->ev_steps) cudaEventDestroy(H->ev_steps);
+  if (H->ev_side) cudaEventDestroy(H->ev_side);
+  if (H->side) cudaStreamDestroy(H->side);
   if (H->stream) cudaStreamDestroy(H->stream);
   delete H;
 }
@@ -574,13 +665,7 @@ int imodel_swm_step(void *handle, double *h_io, double *u_io, double dt, int32_t
   if (!H || !h_io || !u_io) return IMODEL_SWM_EINVAL;
   if (H->nv == 0) return imodel::set_error(H, IMODEL_SWM_ESTATE, "handle was not created");
   if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
-  int rc = imodel::load_state(H, h_io, u_io, false);
-  if (rc) return rc;
-  rc = imodel::advance(H, dt, nsteps);
-  if (rc) return rc;
-  rc = imodel::store_state(H, h_io, u_io);
-  if (rc) return rc;
-  return imodel::check_flags(H);
+  return imodel::step_host(H, h_io, u_io, dt, nsteps);
 }
 
 int imodel_swm_set_state(void *handle, const double *h, const double *u) {

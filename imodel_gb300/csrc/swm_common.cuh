@@ -112,10 +112,11 @@ void launch_scatter_out32(int n, const int32_t *n2o, const float *src, double *d
                           double shift, int *flags, cudaStream_t s);
 // the same conversions straight between a page-locked host array (reference
 // order, read or written in order over the host link) and the device state:
-// load writes both yn and ya, store raises bit 1 of *flags on NaN/Inf
+// load writes yn, ya and (when not NULL) ck; store raises bit 1 of *flags on
+// NaN/Inf
 template <class T>
-void launch_load_host(int n, const int32_t *o2n, const double *src, T *yn, T *ya, double shift,
-                      cudaStream_t s);
+void launch_load_host(int n, const int32_t *o2n, const double *src, T *yn, T *ya, T *ck,
+                      double shift, cudaStream_t s);
 template <class T>
 void launch_store_host(int n, const int32_t *o2n, const T *src, double *dst, double shift,
                        int *flags, cudaStream_t s);

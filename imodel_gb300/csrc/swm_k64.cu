@@ -161,13 +161,14 @@ __global__ void k_scatter_out(int n, const int32_t *__restrict__ n2o, const T *_
 template <class T>
 __global__ void k_load_host(int n, const int32_t *__restrict__ o2n,
                             const double *__restrict__ src, T *__restrict__ yn,
-                            T *__restrict__ ya, double shift) {
+                            T *__restrict__ ya, T *__restrict__ ck, double shift) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < n) {
     const T v = static_cast<T>(src[j] - shift);
     const int i = o2n[j];
     yn[i] = v;
     ya[i] = v;
+    if (ck) ck[i] = v;
   }
 }
 
@@ -542,9 +543,9 @@ void launch_scatter_out32(int n, const int32_t *n2o, const float *src, double *d
 }
 
 template <class T>
-void launch_load_host(int n, const int32_t *o2n, const double *src, T *yn, T *ya, double shift,
-                      cudaStream_t s) {
-  k_load_host<T><<<nblocks(n, 256), 256, 0, s>>>(n, o2n, src, yn, ya, shift);
+void launch_load_host(int n, const int32_t *o2n, const double *src, T *yn, T *ya, T *ck,
+                      double shift, cudaStream_t s) {
+  k_load_host<T><<<nblocks(n, 256), 256, 0, s>>>(n, o2n, src, yn, ya, ck, shift);
 }
 template <class T>
 void launch_store_host(int n, const int32_t *o2n, const T *src, double *dst, double shift,
@@ -552,9 +553,9 @@ void launch_store_host(int n, const int32_t *o2n, const T *src, double *dst, dou
   k_store_host<T><<<nblocks(n, 256), 256, 0, s>>>(n, o2n, src, dst, shift, flags);
 }
 template void launch_load_host<double>(int, const int32_t *, const double *, double *, double *,
-                                       double, cudaStream_t);
+                                       double *, double, cudaStream_t);
 template void launch_load_host<float>(int, const int32_t *, const double *, float *, float *,
-                                      double, cudaStream_t);
+                                      float *, double, cudaStream_t);
 template void launch_store_host<double>(int, const int32_t *, const double *, double *, double,
                                         int *, cudaStream_t);
 template void launch_store_host<float>(int, const int32_t *, const float *, double *, double,

@@ -100,3 +100,67 @@ def test_pinned_nan_is_reported(grid_at):
         hb.free()
         ub.free()
         m.close()
+
+
+def _pinned_pair(rt, h, u):
+    hb, ub = Pinned(rt, h.size), Pinned(rt, u.size)
+    hb.a[:] = h
+    ub.a[:] = u
+    return hb, ub
+
+
+def test_pinned_learned_steps_match_advance(grid_at):
+    """With the learned correction, imodel_swm_step on page-locked arrays runs
+    the energy check beside the write-back; the states equal those of
+    set_state + advance + get_state, which check after each call too."""
+    from imodel_gb300 import fields, learned
+    g = grid_at(5)
+    h, u = fields.balanced_state(g, lmax=24, seed=5)
+    p = learned.trained_params()
+    assert p is not None
+    a = SWM(g, "fp32", learned_params=p)
+    b = SWM(g, "fp32", learned_params=p)
+    rt = _cudart()
+    hb, ub = _pinned_pair(rt, h, u)
+    try:
+        a.set_state(h, u)
+        for _ in range(3):
+            a.advance(450.0, 1)
+            assert b.lib.imodel_swm_step(b.handle, hb.ptr(), ub.ptr(), 450.0, 1) == 0
+        ha, ua = a.get_state()
+        assert np.array_equal(hb.a, ha) and np.array_equal(ub.a, ua)
+        assert a.diagnostics()["learned_active"] == 1
+        assert b.diagnostics()["learned_active"] == 1
+    finally:
+        hb.free()
+        ub.free()
+        a.close()
+        b.close()
+
+
+def test_pinned_learned_trip_rolls_back(grid_at):
+    """A step that breaks the drift bound inside imodel_swm_step on
+    page-locked arrays is rolled back and stepped with the plain scheme."""
+    from imodel_gb300 import fields
+    from oracle import mlp_oracle as mo
+    g = grid_at(4)
+    h, u = fields.balanced_state(g, lmax=16, seed=3)
+    p = mo.init_params(9) * 50.0
+    p[-1] = 30.0
+    a = SWM(g, "fp32", learned_params=p, drift_bound=1e-12)
+    b = SWM(g, "fp32")
+    b.set_tuning(variant=1)
+    rt = _cudart()
+    hb, ub = _pinned_pair(rt, h, u)
+    try:
+        hc, uc = h, u
+        for _ in range(3):
+            assert a.lib.imodel_swm_step(a.handle, hb.ptr(), ub.ptr(), 900.0, 1) == 0
+            hc, uc = b.ode_rk4(hc, uc, 900.0, 1)
+        assert a.diagnostics()["learned_active"] == 0
+        assert np.array_equal(hb.a, hc) and np.array_equal(ub.a, uc)
+    finally:
+        hb.free()
+        ub.free()
+        a.close()
+        b.close()
