@@ -137,7 +137,11 @@ int imodel_swm_create(const imodel_swm_mesh *m, const imodel_swm_opts *o,
 /* Runs nsteps classic RK4 steps (swm.f90:2600-2683) of length dt seconds.
  * h_io[nv] and u_io[ne] (host, FP64, reference ordering) are read on entry
  * and overwritten with the state after nsteps steps.  nsteps > 1 replays a
- * CUDA graph of one step. */
+ * CUDA graph of one step.  Arrays in page-locked memory (cudaMallocHost,
+ * cudaHostRegister) that wholly cover nv and ne values are read and written
+ * in place by the library's kernels over the host link; pageable arrays are
+ * copied through a staging buffer (slower).  The same holds for
+ * imodel_swm_set_state and imodel_swm_get_state. */
 int imodel_swm_step(void *handle, double *h_io, double *u_io, double dt,
                     int32_t nsteps);
 
