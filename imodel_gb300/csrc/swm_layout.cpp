@@ -9,23 +9,41 @@
 namespace imodel {
 namespace {
 
-// Cells are numbered in latitude bands half a mean cell spacing tall,
-// south to north, by longitude within a band (alternating east- and
-// westward, so that consecutive bands join): every neighbour of a cell then
-// lies within a few bands, and its rank within a few thousand of the cell's
-// (at most 6.3e3 at icos level 9, 1.3e4 at level 10).  Edges and triangles
-// are numbered by the sum of their cells' ranks, so edge e sits near
-// 3/2 (c1 + c2) and triangle t near 2/3 (v1 + v2 + v3): a cell's edges lie
-// within about 1.5 times that bound of 3 i, its triangles of 2 i.
-uint64_t band_key(const double *p, double band_h) {
-  const double lat = std::atan2(p[2], std::hypot(p[0], p[1]));
-  const double lon = std::atan2(p[1], p[0]);
-  const uint64_t band = static_cast<uint64_t>(std::floor((lat + 0.5 * M_PI) / band_h));
-  double f = (lon + M_PI) / (2.0 * M_PI);
-  f = std::min(std::max(f, 0.0), 1.0);
-  uint64_t q = static_cast<uint64_t>(f * 4294967295.0);
-  if (band & 1u) q = 4294967295ull - q;
-  return (band << 32) | q;
+// 3-D Hilbert index of integer coordinates (b bits each), following the
+// transpose formulation published by J. Skilling, "Programming the Hilbert
+// curve", AIP Conf. Proc. 707 (2004).
+uint64_t hilbert3(uint32_t x0, uint32_t x1, uint32_t x2, int b) {
+  uint32_t X[3] = {x0, x1, x2};
+  const uint32_t M = 1u << (b - 1);
+  for (uint32_t Q = M; Q > 1; Q >>= 1) {
+    const uint32_t P = Q - 1;
+    for (int i = 0; i < 3; ++i) {
+      if (X[i] & Q) {
+        X[0] ^= P;
+      } else {
+        uint32_t t = (X[0] ^ X[i]) & P;
+        X[0] ^= t;
+        X[i] ^= t;
+      }
+    }
+  }
+  for (int i = 1; i < 3; ++i) X[i] ^= X[i - 1];
+  uint32_t t = 0;
+  for (uint32_t Q = M; Q > 1; Q >>= 1)
+    if (X[2] & Q) t ^= Q - 1;
+  for (int i = 0; i < 3; ++i) X[i] ^= t;
+  uint64_t key = 0;
+  for (int bit = b - 1; bit >= 0; --bit)
+    for (int i = 0; i < 3; ++i) key = (key << 1) | ((X[i] >> bit) & 1u);
+  return key;
+}
+
+uint32_t quant(double x, int b) {
+  const double s = static_cast<double>((1u << b) - 1);
+  double q = (x + 1.0) * 0.5 * s + 0.5;
+  if (q < 0) q = 0;
+  if (q > s) q = s;
+  return static_cast<uint32_t>(q);
 }
 
 template <class Key>
@@ -85,8 +103,11 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
   // --- orderings ------------------------------------------------------
   {
     std::vector<uint64_t> key(nv);
-    const double band_h = 0.5 * std::sqrt(4.0 * M_PI / nv);
-    for (int i = 0; i < nv; ++i) key[i] = band_key(m.v_p + 3 * static_cast<size_t>(i), band_h);
+    const int b = 20;
+    for (int i = 0; i < nv; ++i) {
+      const double *p = m.v_p + 3 * static_cast<size_t>(i);
+      key[i] = hilbert3(quant(p[0], b), quant(p[1], b), quant(p[2], b), b);
+    }
     sort_perm(L.cell_n2o, L.cell_o2n, key);
   }
   {
@@ -94,7 +115,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
     for (int e = 0; e < ne; ++e) {
       uint64_t a = static_cast<uint64_t>(L.cell_o2n[m.ed_v[2 * static_cast<size_t>(e)] - 1]);
       uint64_t c = static_cast<uint64_t>(L.cell_o2n[m.ed_v[2 * static_cast<size_t>(e) + 1] - 1]);
-      key[e] = ((a + c) << 32) | std::min(a, c);
+      key[e] = (std::min(a, c) << 32) | std::max(a, c);
     }
     sort_perm(L.edge_n2o, L.edge_o2n, key);
   }
@@ -104,7 +125,8 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
       uint64_t v[3];
       for (int s = 0; s < 3; ++s)
         v[s] = static_cast<uint64_t>(L.cell_o2n[m.tr_v[3 * static_cast<size_t>(t) + s] - 1]);
-      key[t] = ((v[0] + v[1] + v[2]) << 32) | std::min(v[0], std::min(v[1], v[2]));
+      std::sort(v, v + 3);
+      key[t] = (v[0] << 42) | (v[1] << 21) | (v[2] & 0x1FFFFF);
     }
     sort_perm(L.tri_n2o, L.tri_o2n, key);
   }

@@ -1,10 +1,9 @@
 // Device data layout of the TRSK shallow-water step (internal header).
 //
-// Cells are renumbered in thin latitude bands (by longitude within a band);
-// edges and triangles by the sum of their cells' new numbers, so that the
-// entities one thread block touches sit in a few contiguous runs of HBM and
-// every index a stencil record holds lies within a bounded distance of the
-// record's own position.  All per-entity lists are
+// Cells are renumbered along a 3-D Hilbert curve through their positions on
+// the sphere; edges are renumbered by their lower-numbered cell and
+// triangles by their lowest vertex, so that the entities one thread block
+// touches sit in a few contiguous runs of HBM.  All per-entity lists are
 // padded to a fixed width and stored slot-major (slot j of entity i at
 // [j * n + i]) so that a warp reading slot j of 32 consecutive entities
 // issues one coalesced request.
