@@ -126,7 +126,9 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
       for (int s = 0; s < 3; ++s)
         v[s] = static_cast<uint64_t>(L.cell_o2n[m.tr_v[3 * static_cast<size_t>(t) + s] - 1]);
       std::sort(v, v + 3);
-      key[t] = (v[0] << 42) | (v[1] << 21) | (v[2] & 0x1FFFFF);
+      // (lowest, middle) vertex; the sort is stable, so the two triangles
+      // of an edge keep the reference's order (no overflow below 2^32 cells)
+      key[t] = (v[0] << 32) | v[1];
     }
     sort_perm(L.tri_n2o, L.tri_o2n, key);
   }
