@@ -36,12 +36,27 @@ struct DevMesh {
   const int4 *c_pk;     // [6][nv] {edge, neighbour, triangle, kite fraction bits}
   const float2 *c_kd;   // [6][nv] {KE weight, ttgout*d}
   const uint2 *e_vs2;   // [ne] both cell words of an edge
+  // the same records with 16-bit indices against per-warp bases (variant 2;
+  // swm_layout.h): cells {KE weight, ttgout*d, R, edge | neighbour << 16}
+  // [6][nv], triangle offsets of slot pairs [3][nv], warp bases {edge,
+  // neighbour, triangle, usable}; triangles {e0|e1, e2|c0, c1|c2, circ 0},
+  // {circ 1, circ 2, kite 0, kite 1}, {kite 2, f} [nt], warp bases {edge,
+  // cell (-1: use the 32-bit records)}
+  const float4 *c_rec;
+  const uint32_t *c_toff;
+  const int4 *c_wb;
+  const uint4 *t_c16A;
+  const float4 *t_c16B;
+  const float2 *t_c16C;
+  const int2 *t_wb;
 };
 
 // Launch configuration of the FP32 stage kernels, chosen by the autotuner.
 //   variant 0: triangle -> edge pre-pass -> cell -> edge (10-entry stencil)
 //   variant 1: triangle -> cell (cell-centred TRSK, writes the PV flux
 //              contribution of each cell edge) -> edge (sums two cells)
+//   variant 2: variant 1 reading the triangle and cell records with 16-bit
+//              indices (36 B less per cell and 12 B less per triangle)
 struct Tune {
   int variant = 1;
   int bs_tri = 256, bs_pre = 256, bs_cell = 256, bs_edge = 256;
@@ -97,7 +112,7 @@ void learned_launch(const DevMesh &M, const LearnedDev &L, const float *hd, cons
                     const float *q_tr, float h_ref, int gather_groups, int *err, cudaStream_t s);
 
 inline int launches_per_stage(int precision_fp32, int variant) {
-  return (precision_fp32 && variant == 1) ? 3 : 4;
+  return (precision_fp32 && variant >= 1) ? 3 : 4;
 }
 
 // reference order <-> device order, with precision conversion

@@ -121,6 +121,31 @@ __device__ __forceinline__ float edge_momeq(uint32_t wa, uint32_t wb, float g,
   return -grad - q;
 }
 
+// ---- variant 2: the same kernels on records with 16-bit indices ---------
+__global__ void __launch_bounds__(512) k_tri32c(DevMesh M, const float *__restrict__ hd,
+                                                const float *__restrict__ u,
+                                                float *__restrict__ q_tr, float h_ref,
+                                                int pv_on, int *flags) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= M.nt) return;
+  tri_body16(M, t, hd, u, q_tr, h_ref, pv_on, flags);
+}
+
+__global__ void __launch_bounds__(512) k_cell32c(DevMesh M, const float *__restrict__ hd,
+                                                 const float *__restrict__ u,
+                                                 const float *__restrict__ q_tr,
+                                                 float *__restrict__ bern,
+                                                 float *__restrict__ zflux,
+                                                 const float *__restrict__ yn,
+                                                 float *__restrict__ acc,
+                                                 float *__restrict__ yout,
+                                                 float *__restrict__ tend, int stage, float dt,
+                                                 float grav, float h_ref) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M.nv) return;
+  cell_body16(M, i, hd, u, q_tr, bern, zflux, yn, acc, yout, tend, stage, dt, grav, h_ref);
+}
+
 // two consecutive edges per thread: one 16-byte load of their cell words,
 // 8-byte loads and stores of their per-edge values, and twice the
 // independent gathers in flight
@@ -174,17 +199,26 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
   const Tune &T = W.tune;
   const float grav = static_cast<float>(M.grav);
   if (ev) cudaEventRecord(ev[0], s);
-  k_tri32<<<nblocks(M.nt, T.bs_tri), T.bs_tri, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ref, W.pv_on,
-                                                        W.flags);
-  if (T.variant == 1) {
+  if (T.variant == 2)
+    k_tri32c<<<nblocks(M.nt, T.bs_tri), T.bs_tri, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ref,
+                                                           W.pv_on, W.flags);
+  else
+    k_tri32<<<nblocks(M.nt, T.bs_tri), T.bs_tri, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ref,
+                                                          W.pv_on, W.flags);
+  if (T.variant >= 1) {
     if (ev) cudaEventRecord(ev[1], s);
     // learned correction: formed once per step from the first stage's state
     if (W.learned && stage <= 0)
       learned_launch(M, *W.learned, h_in, u_in, W.q_tr, W.h_ref, T.mlp_gather, W.flags, s);
     if (ev) cudaEventRecord(ev[2], s);
-    k_cell32v2<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
-        M, h_in, u_in, W.q_tr, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
-        grav, W.h_ref);
+    if (T.variant == 2)
+      k_cell32c<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
+          M, h_in, u_in, W.q_tr, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
+          grav, W.h_ref);
+    else
+      k_cell32v2<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
+          M, h_in, u_in, W.q_tr, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
+          grav, W.h_ref);
     if (ev) cudaEventRecord(ev[3], s);
     k_edge32v2<<<nblocks((M.ne + 1) / 2, T.bs_edge), T.bs_edge, 0, s>>>(
         M, W.bern, W.zflux, W.yn_u, W.acc_u, u_out, W.tend_u, stage, dt, W.mom_on,

@@ -46,19 +46,15 @@ __device__ __forceinline__ float rk_stage32(int stage, float k, float yn, float 
 }
 
 // q_t = (curl u / A + f) / h_t  (vort_tr + scalar_hx2tr + scalar_elem_divide)
-template <class Ix, class Ld = LdPlain>
-__device__ __forceinline__ void tri_body(const DevMesh &M, int t, Ix ix,
-                                         const float *__restrict__ hd,
+// from a triangle's decoded record: edges, cells, circulation and kite
+// coefficients, Coriolis parameter; the sums run in slot order 0, 1, 2
+template <class Ix, class Ld>
+__device__ __forceinline__ void tri_core(int t, Ix ix, const int (&ed)[3], const int (&cv)[3],
+                                         const float (&circ)[3], const float (&kite)[3],
+                                         float f, const float *__restrict__ hd,
                                          const float *__restrict__ u, float *__restrict__ q_tr,
                                          float h_ref, int pv_on, int *flags) {
-  // three 16-byte records instead of 12 scalar streams (fewer load
-  // instructions in flight per SM); the sums run in slot order 0, 1, 2
-  const int4 a = __ldg(&M.t_recA[t]), b = __ldg(&M.t_recB[t]);
-  const float4 c = __ldg(&M.t_recC[t]);
-  const int ed[3] = {a.x, a.y, a.z}, cv[3] = {a.w, b.x, b.y};
-  const float circ[3] = {__int_as_float(b.z), __int_as_float(b.w), c.x};
-  const float kite[3] = {c.y, c.z, c.w};
-  float eta = __ldg(&M.t_f32[t]);
+  float eta = f;
   float ht = 0.0f;
 #pragma unroll
   for (int s = 0; s < 3; ++s) {
@@ -75,6 +71,47 @@ __device__ __forceinline__ void tri_body(const DevMesh &M, int t, Ix ix,
       q = eta / ht;
   }
   q_tr[ix(t)] = q;
+}
+
+template <class Ix, class Ld = LdPlain>
+__device__ __forceinline__ void tri_body(const DevMesh &M, int t, Ix ix,
+                                         const float *__restrict__ hd,
+                                         const float *__restrict__ u, float *__restrict__ q_tr,
+                                         float h_ref, int pv_on, int *flags) {
+  // three 16-byte records instead of 12 scalar streams (fewer load
+  // instructions in flight per SM)
+  const int4 a = __ldg(&M.t_recA[t]), b = __ldg(&M.t_recB[t]);
+  const float4 c = __ldg(&M.t_recC[t]);
+  const int ed[3] = {a.x, a.y, a.z}, cv[3] = {a.w, b.x, b.y};
+  const float circ[3] = {__int_as_float(b.z), __int_as_float(b.w), c.x};
+  const float kite[3] = {c.y, c.z, c.w};
+  tri_core<Ix, Ld>(t, ix, ed, cv, circ, kite, __ldg(&M.t_f32[t]), hd, u, q_tr, h_ref, pv_on,
+                   flags);
+}
+
+// the same from 40-byte records with 16-bit indices (single runs): a warp of
+// 32 triangles shares one base per index kind (t_wb); a warp whose indices
+// span more than 65,536 reads the 32-bit records instead (warp-uniform branch)
+__device__ __forceinline__ void tri_body16(const DevMesh &M, int t, const float *__restrict__ hd,
+                                           const float *__restrict__ u,
+                                           float *__restrict__ q_tr, float h_ref, int pv_on,
+                                           int *flags) {
+  const int2 wb = __ldg(&M.t_wb[t >> 5]);
+  if (wb.y < 0) {
+    tri_body(M, t, OneRun{}, hd, u, q_tr, h_ref, pv_on, flags);
+    return;
+  }
+  const uint4 a = __ldg(&M.t_c16A[t]);
+  const float4 b = __ldg(&M.t_c16B[t]);
+  const float2 c = __ldg(&M.t_c16C[t]);
+  const int ed[3] = {wb.x + static_cast<int>(a.x & 0xFFFFu), wb.x + static_cast<int>(a.x >> 16),
+                     wb.x + static_cast<int>(a.y & 0xFFFFu)};
+  const int cv[3] = {wb.y + static_cast<int>(a.y >> 16), wb.y + static_cast<int>(a.z & 0xFFFFu),
+                     wb.y + static_cast<int>(a.z >> 16)};
+  const float circ[3] = {__uint_as_float(a.w), b.x, b.y};
+  const float kite[3] = {b.z, b.w, c.x};
+  tri_core<OneRun, LdPlain>(t, OneRun{}, ed, cv, circ, kite, c.y, hd, u, q_tr, h_ref, pv_on,
+                            flags);
 }
 
 // coriolis_ed (swm_operators.f90:1283-1308) sums, for edge e and each of its
@@ -104,38 +141,32 @@ __device__ __forceinline__ void trsk_cell(const float (&G)[6], const float (&qs)
 }
 
 // div F, K, Bernoulli potential, PV-flux contributions Z (cell-major
-// zflux[cell][6]) and the mass RK stage of cell i
-template <class Ix, class Ld = LdPlain>
-__device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
-                                          const float *__restrict__ hd,
+// zflux[cell][6]) and the mass RK stage of cell i, from its decoded slot
+// records: edge, neighbour, triangle, kite fraction R and {KE weight,
+// ttgout*d} of each slot (unused pentagon slots repeat slot 0 with zero
+// weights)
+template <class Ix, class Ld>
+__device__ __forceinline__ void cell_core(const DevMesh &M, int i, Ix ix, uint32_t meta,
+                                          const int (&ed)[6], const int (&nb)[6],
+                                          const int (&tr)[6], const float (&R)[6],
+                                          const float2 (&kd)[6], const float *__restrict__ hd,
                                           const float *__restrict__ u,
                                           const float *__restrict__ q_tr,
                                           float *__restrict__ bern, float *__restrict__ zflux,
                                           const float *__restrict__ yn, float *__restrict__ acc,
                                           float *__restrict__ yout, float *__restrict__ tend,
                                           int stage, float dt, float grav, float h_ref) {
-  const int nv = M.nv;
-  const uint32_t meta = __ldg(&M.c_meta[i]);
   const int n = static_cast<int>(meta & 7u);
   const unsigned tneg = meta >> 8;
-  int4 pk[6];
-  float2 kd[6];
-  // all slot records first (unused pentagon slots repeat slot 0 with zero
-  // weights), so that every load is in flight before the gathers
-#pragma unroll
-  for (int j = 0; j < 6; ++j) {
-    pk[j] = __ldg(&M.c_pk[j * nv + i]);
-    kd[j] = __ldg(&M.c_kd[j * nv + i]);
-  }
   const float hi = Ld::ld(hd + ix(i));
   float ue[6], hn[6], qt[6];
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
-    ue[j] = Ld::ld(u + ix(pk[j].x));
-    hn[j] = Ld::ld(hd + ix(pk[j].y));
-    qt[j] = Ld::ld(q_tr + ix(pk[j].z));
+    ue[j] = Ld::ld(u + ix(ed[j]));
+    hn[j] = Ld::ld(hd + ix(nb[j]));
+    qt[j] = Ld::ld(q_tr + ix(tr[j]));
   }
-  float G[6], qs[6], R[6];
+  float G[6], qs[6];
   float div = 0.0f, ke = 0.0f;
   const float qlast = n == 6 ? qt[5] : (n == 5 ? qt[4] : (n == 4 ? qt[3] : qt[2]));
 #pragma unroll
@@ -145,7 +176,6 @@ __device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
     G[j] = F * kd[j].y;
     // q_e: edge j lies between triangles j-1 and j (scalar_tr2ed)
     qs[j] = 0.5f * ((j == 0 ? qlast : qt[j - 1]) + qt[j]);
-    R[j] = __int_as_float(pk[j].w);
     div += G[j];
     ke += kd[j].x * (ue[j] * ue[j]);
   }
@@ -167,6 +197,78 @@ __device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
     tend[ix(i)] = masseq;
   else
     yout[ix(i)] = rk_stage32(stage, masseq, Ld::ld(yn + ix(i)), acc + ix(i), dt);
+}
+
+template <class Ix, class Ld = LdPlain>
+__device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
+                                          const float *__restrict__ hd,
+                                          const float *__restrict__ u,
+                                          const float *__restrict__ q_tr,
+                                          float *__restrict__ bern, float *__restrict__ zflux,
+                                          const float *__restrict__ yn, float *__restrict__ acc,
+                                          float *__restrict__ yout, float *__restrict__ tend,
+                                          int stage, float dt, float grav, float h_ref) {
+  const int nv = M.nv;
+  const uint32_t meta = __ldg(&M.c_meta[i]);
+  int ed[6], nb[6], tr[6];
+  float R[6];
+  float2 kd[6];
+  // all slot records first, so that every load is in flight before the
+  // gathers
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const int4 pk = __ldg(&M.c_pk[j * nv + i]);
+    kd[j] = __ldg(&M.c_kd[j * nv + i]);
+    ed[j] = pk.x;
+    nb[j] = pk.y;
+    tr[j] = pk.z;
+    R[j] = __int_as_float(pk.w);
+  }
+  cell_core<Ix, Ld>(M, i, ix, meta, ed, nb, tr, R, kd, hd, u, q_tr, bern, zflux, yn, acc, yout,
+                    tend, stage, dt, grav, h_ref);
+}
+
+// the same from 16-byte slot records {KE weight, ttgout*d, R, edge and
+// neighbour offsets} plus the triangle offsets of slot pairs (single runs):
+// a warp of 32 cells shares one base per index kind (c_wb); a warp whose
+// indices span more than 65,536 reads the 32-bit records instead
+// (warp-uniform branch)
+__device__ __forceinline__ void cell_body16(const DevMesh &M, int i,
+                                            const float *__restrict__ hd,
+                                            const float *__restrict__ u,
+                                            const float *__restrict__ q_tr,
+                                            float *__restrict__ bern, float *__restrict__ zflux,
+                                            const float *__restrict__ yn, float *__restrict__ acc,
+                                            float *__restrict__ yout, float *__restrict__ tend,
+                                            int stage, float dt, float grav, float h_ref) {
+  const int4 wb = __ldg(&M.c_wb[i >> 5]);
+  if (!wb.w) {
+    cell_body(M, i, OneRun{}, hd, u, q_tr, bern, zflux, yn, acc, yout, tend, stage, dt, grav,
+              h_ref);
+    return;
+  }
+  const int nv = M.nv;
+  const uint32_t meta = __ldg(&M.c_meta[i]);
+  float4 rec[6];
+  uint32_t tp[3];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) rec[j] = __ldg(&M.c_rec[j * nv + i]);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) tp[k] = __ldg(&M.c_toff[k * nv + i]);
+  int ed[6], nb[6], tr[6];
+  float R[6];
+  float2 kd[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const uint32_t w = __float_as_uint(rec[j].w);
+    ed[j] = wb.x + static_cast<int>(w & 0xFFFFu);
+    nb[j] = wb.y + static_cast<int>(w >> 16);
+    tr[j] = wb.z + static_cast<int>((tp[j >> 1] >> (16 * (j & 1))) & 0xFFFFu);
+    R[j] = rec[j].z;
+    kd[j] = make_float2(rec[j].x, rec[j].y);
+  }
+  cell_core<OneRun, LdPlain>(M, i, OneRun{}, meta, ed, nb, tr, R, kd, hd, u, q_tr, bern, zflux,
+                             yn, acc, yout, tend, stage, dt, grav, h_ref);
 }
 
 // -grad B - (Z_c1 + Z_c2) / l_e and the momentum RK stage of edge e

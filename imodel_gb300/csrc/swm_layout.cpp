@@ -2,6 +2,7 @@
 #include "swm_layout.h"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -281,6 +282,45 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
     L.e_vs2[2 * e] = L.e_vs[e];
     L.e_vs2[2 * e + 1] = L.e_vs[NE + e];
   }
+  {
+    // 16-bit cell records: bases per warp of 32 cells
+    const size_t nw = (NV + 31) / 32;
+    L.c_rec.assign(kMaxNb * NV * 4, 0u);
+    L.c_toff.assign(3 * NV, 0u);
+    L.c_wb.assign(4 * nw, 0);
+    auto fbits = [](float f) {
+      uint32_t b;
+      std::memcpy(&b, &f, sizeof(b));
+      return b;
+    };
+    for (size_t w = 0; w < nw; ++w) {
+      const size_t i0 = 32 * w, i1 = std::min(NV, i0 + 32);
+      int32_t lo[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, hi[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+      for (size_t i = i0; i < i1; ++i)
+        for (int j = 0; j < kMaxNb; ++j)
+          for (int k = 0; k < 3; ++k) {
+            const int32_t v = L.c_pk[4 * (j * NV + i) + k];
+            lo[k] = std::min(lo[k], v);
+            hi[k] = std::max(hi[k], v);
+          }
+      bool ok = true;
+      for (int k = 0; k < 3; ++k) ok = ok && static_cast<int64_t>(hi[k]) - lo[k] <= 0xFFFF;
+      for (int k = 0; k < 3; ++k) L.c_wb[4 * w + k] = ok ? lo[k] : 0;
+      L.c_wb[4 * w + 3] = ok ? 1 : 0;
+      for (size_t i = i0; i < i1; ++i)
+        for (int j = 0; j < kMaxNb; ++j) {
+          const size_t q = j * NV + i;
+          uint32_t off[3] = {0u, 0u, 0u};
+          if (ok)
+            for (int k = 0; k < 3; ++k) off[k] = static_cast<uint32_t>(L.c_pk[4 * q + k] - lo[k]);
+          L.c_rec[4 * q + 0] = fbits(L.c_kd[2 * q + 0]);
+          L.c_rec[4 * q + 1] = fbits(L.c_kd[2 * q + 1]);
+          L.c_rec[4 * q + 2] = static_cast<uint32_t>(L.c_pk[4 * q + 3]);
+          L.c_rec[4 * q + 3] = off[0] | (off[1] << 16);
+          L.c_toff[(j / 2) * NV + i] |= off[2] << (16 * (j % 2));
+        }
+    }
+  }
 
   // --- triangles ------------------------------------------------------
   L.t_ed.resize(3 * NT);
@@ -332,6 +372,49 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
     c[1] = bits(L.t_kite32[i]);
     c[2] = bits(L.t_kite32[NT + i]);
     c[3] = bits(L.t_kite32[2 * NT + i]);
+  }
+  {
+    // 16-bit triangle records: bases per warp of 32 triangles
+    const size_t nw = (NT + 31) / 32;
+    L.t_c16A.assign(4 * NT, 0u);
+    L.t_c16B.assign(4 * NT, 0.0f);
+    L.t_c16C.assign(2 * NT, 0.0f);
+    L.t_wb.assign(2 * nw, 0);
+    for (size_t w = 0; w < nw; ++w) {
+      const size_t t0 = 32 * w, t1 = std::min(NT, t0 + 32);
+      int32_t lo[2] = {INT32_MAX, INT32_MAX}, hi[2] = {INT32_MIN, INT32_MIN};
+      for (size_t t = t0; t < t1; ++t)
+        for (int s = 0; s < 3; ++s) {
+          lo[0] = std::min(lo[0], L.t_ed[s * NT + t]);
+          hi[0] = std::max(hi[0], L.t_ed[s * NT + t]);
+          lo[1] = std::min(lo[1], L.t_v[s * NT + t]);
+          hi[1] = std::max(hi[1], L.t_v[s * NT + t]);
+        }
+      const bool ok = static_cast<int64_t>(hi[0]) - lo[0] <= 0xFFFF &&
+                      static_cast<int64_t>(hi[1]) - lo[1] <= 0xFFFF;
+      L.t_wb[2 * w] = ok ? lo[0] : 0;
+      L.t_wb[2 * w + 1] = ok ? lo[1] : -1;
+      for (size_t t = t0; t < t1; ++t) {
+        uint32_t oe[3] = {0u, 0u, 0u}, ov[3] = {0u, 0u, 0u};
+        if (ok)
+          for (int s = 0; s < 3; ++s) {
+            oe[s] = static_cast<uint32_t>(L.t_ed[s * NT + t] - lo[0]);
+            ov[s] = static_cast<uint32_t>(L.t_v[s * NT + t] - lo[1]);
+          }
+        uint32_t *a = &L.t_c16A[4 * t];
+        a[0] = oe[0] | (oe[1] << 16);
+        a[1] = oe[2] | (ov[0] << 16);
+        a[2] = ov[1] | (ov[2] << 16);
+        a[3] = static_cast<uint32_t>(bits(L.t_circ32[t]));
+        float *b = &L.t_c16B[4 * t];
+        b[0] = L.t_circ32[NT + t];
+        b[1] = L.t_circ32[2 * NT + t];
+        b[2] = L.t_kite32[t];
+        b[3] = L.t_kite32[NT + t];
+        L.t_c16C[2 * t] = L.t_kite32[2 * NT + t];
+        L.t_c16C[2 * t + 1] = L.t_f32[t];
+      }
+    }
   }
   return "";
 }

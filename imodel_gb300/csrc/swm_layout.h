@@ -58,6 +58,15 @@ struct Layout {
   std::vector<int32_t> c_pk;                 // [6][nv][4]
   std::vector<float> c_kd;                   // [6][nv][2]
   std::vector<uint32_t> e_vs2;               // [ne][2] both cell words of an edge
+  // the cell records with 16-bit indices: per warp of 32 cells one base per
+  // index kind, c_wb [nwarps][4] = {edge, neighbour, triangle, usable}
+  // (usable = 0 when the warp's indices of some kind span more than 65,536);
+  // c_rec [6][nv][4] = {KE weight, ttgout*d, R, (edge - base) |
+  // (neighbour - base) << 16} as bits, c_toff [3][nv] = offsets of the
+  // triangles of slots 2k and 2k+1
+  std::vector<uint32_t> c_rec;
+  std::vector<uint32_t> c_toff;
+  std::vector<int32_t> c_wb;
 
   // edges [ne] and [2][ne]
   std::vector<int32_t> e_v;                  // [2][ne] cells (ed%v = edhx%sh)
@@ -81,6 +90,13 @@ struct Layout {
   //   A {edge 0, edge 1, edge 2, cell 0}  B {cell 1, cell 2, circ 0, circ 1}
   //   C {circ 2, kite 0, kite 1, kite 2}  (circ, kite: FP32 bit patterns)
   std::vector<int32_t> t_recA, t_recB, t_recC;
+  // the same with 16-bit indices against per-warp bases t_wb [nwarps][2] =
+  // {edge, cell} (cell = -1: the warp keeps the 32-bit records):
+  //   A {e0 | e1 << 16, e2 | c0 << 16, c1 | c2 << 16, circ 0}
+  //   B {circ 1, circ 2, kite 0, kite 1}  C {kite 2, f}
+  std::vector<uint32_t> t_c16A;
+  std::vector<float> t_c16B, t_c16C;
+  std::vector<int32_t> t_wb;
   std::vector<float> t_circ32;               // l*tg/(A*erad)
   std::vector<float> t_kite32;               // kite/A
   std::vector<float> t_f32;
