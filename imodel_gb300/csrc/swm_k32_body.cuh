@@ -91,23 +91,34 @@ __device__ __forceinline__ void tri_body(const DevMesh &M, int t, Ix ix,
 
 // the same from 40-byte records with 16-bit indices (single runs): a warp of
 // 32 triangles shares one base per index kind (t_wb); a warp whose indices
-// span more than 65,536 reads the 32-bit records instead (warp-uniform branch)
+// span more than 65,536 takes its indices from the 32-bit records instead
+// (warp-uniform branch).  The records and the bases are loaded together, so
+// that the gathers wait for one round trip, as with the 32-bit records.
 __device__ __forceinline__ void tri_body16(const DevMesh &M, int t, const float *__restrict__ hd,
                                            const float *__restrict__ u,
                                            float *__restrict__ q_tr, float h_ref, int pv_on,
                                            int *flags) {
   const int2 wb = __ldg(&M.t_wb[t >> 5]);
-  if (wb.y < 0) {
-    tri_body(M, t, OneRun{}, hd, u, q_tr, h_ref, pv_on, flags);
-    return;
-  }
   const uint4 a = __ldg(&M.t_c16A[t]);
   const float4 b = __ldg(&M.t_c16B[t]);
   const float2 c = __ldg(&M.t_c16C[t]);
-  const int ed[3] = {wb.x + static_cast<int>(a.x & 0xFFFFu), wb.x + static_cast<int>(a.x >> 16),
-                     wb.x + static_cast<int>(a.y & 0xFFFFu)};
-  const int cv[3] = {wb.y + static_cast<int>(a.y >> 16), wb.y + static_cast<int>(a.z & 0xFFFFu),
-                     wb.y + static_cast<int>(a.z >> 16)};
+  int ed[3], cv[3];
+  if (wb.y >= 0) {
+    ed[0] = wb.x + static_cast<int>(a.x & 0xFFFFu);
+    ed[1] = wb.x + static_cast<int>(a.x >> 16);
+    ed[2] = wb.x + static_cast<int>(a.y & 0xFFFFu);
+    cv[0] = wb.y + static_cast<int>(a.y >> 16);
+    cv[1] = wb.y + static_cast<int>(a.z & 0xFFFFu);
+    cv[2] = wb.y + static_cast<int>(a.z >> 16);
+  } else {
+    const int4 ra = __ldg(&M.t_recA[t]), rb = __ldg(&M.t_recB[t]);
+    ed[0] = ra.x;
+    ed[1] = ra.y;
+    ed[2] = ra.z;
+    cv[0] = ra.w;
+    cv[1] = rb.x;
+    cv[2] = rb.y;
+  }
   const float circ[3] = {__uint_as_float(a.w), b.x, b.y};
   const float kite[3] = {b.z, b.w, c.x};
   tri_core<OneRun, LdPlain>(t, OneRun{}, ed, cv, circ, kite, c.y, hd, u, q_tr, h_ref, pv_on,
@@ -231,8 +242,8 @@ __device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
 // the same from 16-byte slot records {KE weight, ttgout*d, R, edge and
 // neighbour offsets} plus the triangle offsets of slot pairs (single runs):
 // a warp of 32 cells shares one base per index kind (c_wb); a warp whose
-// indices span more than 65,536 reads the 32-bit records instead
-// (warp-uniform branch)
+// indices span more than 65,536 takes its indices from the 32-bit records
+// instead (warp-uniform branch).  Records and bases are loaded together.
 __device__ __forceinline__ void cell_body16(const DevMesh &M, int i,
                                             const float *__restrict__ hd,
                                             const float *__restrict__ u,
@@ -241,13 +252,8 @@ __device__ __forceinline__ void cell_body16(const DevMesh &M, int i,
                                             const float *__restrict__ yn, float *__restrict__ acc,
                                             float *__restrict__ yout, float *__restrict__ tend,
                                             int stage, float dt, float grav, float h_ref) {
-  const int4 wb = __ldg(&M.c_wb[i >> 5]);
-  if (!wb.w) {
-    cell_body(M, i, OneRun{}, hd, u, q_tr, bern, zflux, yn, acc, yout, tend, stage, dt, grav,
-              h_ref);
-    return;
-  }
   const int nv = M.nv;
+  const int4 wb = __ldg(&M.c_wb[i >> 5]);
   const uint32_t meta = __ldg(&M.c_meta[i]);
   float4 rec[6];
   uint32_t tp[3];
@@ -260,12 +266,25 @@ __device__ __forceinline__ void cell_body16(const DevMesh &M, int i,
   float2 kd[6];
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
-    const uint32_t w = __float_as_uint(rec[j].w);
-    ed[j] = wb.x + static_cast<int>(w & 0xFFFFu);
-    nb[j] = wb.y + static_cast<int>(w >> 16);
-    tr[j] = wb.z + static_cast<int>((tp[j >> 1] >> (16 * (j & 1))) & 0xFFFFu);
     R[j] = rec[j].z;
     kd[j] = make_float2(rec[j].x, rec[j].y);
+  }
+  if (wb.w) {
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      const uint32_t w = __float_as_uint(rec[j].w);
+      ed[j] = wb.x + static_cast<int>(w & 0xFFFFu);
+      nb[j] = wb.y + static_cast<int>(w >> 16);
+      tr[j] = wb.z + static_cast<int>((tp[j >> 1] >> (16 * (j & 1))) & 0xFFFFu);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      const int4 pk = __ldg(&M.c_pk[j * nv + i]);
+      ed[j] = pk.x;
+      nb[j] = pk.y;
+      tr[j] = pk.z;
+    }
   }
   cell_core<OneRun, LdPlain>(M, i, OneRun{}, meta, ed, nb, tr, R, kd, hd, u, q_tr, bern, zflux,
                              yn, acc, yout, tend, stage, dt, grav, h_ref);
