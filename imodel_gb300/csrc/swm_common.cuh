@@ -57,6 +57,8 @@ struct DevMesh {
 //              contribution of each cell edge) -> edge (sums two cells)
 //   variant 2: variant 1 reading the triangle and cell records with 16-bit
 //              indices (36 B less per cell and 12 B less per triangle)
+//   variant 3: variant 2 with a persistent cell kernel that prefetches the
+//              next cell's records into shared memory (block size 128)
 struct Tune {
   int variant = 1;
   int bs_tri = 256, bs_pre = 256, bs_cell = 256, bs_edge = 256;

@@ -146,6 +146,122 @@ __global__ void __launch_bounds__(512) k_cell32c(DevMesh M, const float *__restr
   cell_body16(M, i, hd, u, q_tr, bern, zflux, yn, acc, yout, tend, stage, dt, grav, h_ref);
 }
 
+// ---- variant 3: persistent cell kernel, records prefetched -------------
+// Each thread walks its cells with a grid stride and copies the next cell's
+// records and own values into shared memory (cp.async) while it gathers and
+// computes the current one, so that only the gathers (mostly L2 hits) wait
+// on memory.  A thread reads back only what it copied itself, except the
+// warp's index bases, which lane 0 copies.
+constexpr int kPB = 128;  // threads per block
+struct CellPre {
+  float4 rec[6][kPB];   // 16-bit slot records
+  uint32_t toff[3][kPB];
+  uint32_t meta[kPB];
+  float own[5][kPB];    // h deviation, b, 1/(A a), y_n, RK accumulator
+  int4 wb[kPB / 32];    // warp bases
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_addr(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+__global__ void __launch_bounds__(kPB) k_cell32p(DevMesh M, const float *__restrict__ hd,
+                                                 const float *__restrict__ u,
+                                                 const float *__restrict__ q_tr,
+                                                 float *__restrict__ bern,
+                                                 float *__restrict__ zflux,
+                                                 const float *__restrict__ yn,
+                                                 float *__restrict__ acc,
+                                                 float *__restrict__ yout,
+                                                 float *__restrict__ tend, int stage, float dt,
+                                                 float grav, float h_ref) {
+  __shared__ CellPre buf[2];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nv = M.nv;
+  const int stride = gridDim.x * kPB;
+  // copies of cell c (every address checked against nv) as one group
+  auto issue = [&](CellPre &B, int c) {
+    if (c < nv) {
+#pragma unroll
+      for (int j = 0; j < 6; ++j) cp_async16(&B.rec[j][tid], &M.c_rec[j * nv + c]);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) cp_async4(&B.toff[k][tid], &M.c_toff[k * nv + c]);
+      cp_async4(&B.meta[tid], &M.c_meta[c]);
+      cp_async4(&B.own[0][tid], hd + c);
+      cp_async4(&B.own[1][tid], &M.c_bt32[c]);
+      cp_async4(&B.own[2][tid], &M.c_inva32[c]);
+      if (stage >= 0) cp_async4(&B.own[3][tid], yn + c);
+      if (stage >= 1) cp_async4(&B.own[4][tid], acc + c);
+      if (lane == 0) cp_async16(&B.wb[warp], &M.c_wb[c >> 5]);
+    }
+    cp_async_commit();
+  };
+  int base = blockIdx.x * kPB;
+  issue(buf[0], base + tid);
+  // the trip count is uniform over a warp (its first cell decides)
+  for (int it = 0; base + 32 * warp < nv; ++it, base += stride) {
+    const int i = base + tid;
+    CellPre &cur = buf[it & 1];
+    __syncwarp();  // every lane is done with the buffer refilled next
+    issue(buf[(it + 1) & 1], i + stride);
+    cp_async_wait<1>();
+    __syncwarp();  // lane 0's copy of the warp bases
+    if (i < nv) {
+      const int4 wb = cur.wb[warp];
+      int ed[6], nb[6], tr[6];
+      float R[6];
+      float2 kd[6];
+      float4 rec[6];
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        rec[j] = cur.rec[j][tid];
+        R[j] = rec[j].z;
+        kd[j] = make_float2(rec[j].x, rec[j].y);
+      }
+      if (wb.w) {
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+          const uint32_t w = __float_as_uint(rec[j].w);
+          const uint32_t tp = cur.toff[j >> 1][tid];
+          ed[j] = wb.x + static_cast<int>(w & 0xFFFFu);
+          nb[j] = wb.y + static_cast<int>(w >> 16);
+          tr[j] = wb.z + static_cast<int>((tp >> (16 * (j & 1))) & 0xFFFFu);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+          const int4 pk = __ldg(&M.c_pk[j * nv + i]);
+          ed[j] = pk.x;
+          nb[j] = pk.y;
+          tr[j] = pk.z;
+        }
+      }
+      cell_core<OneRun, LdPlain>(i, OneRun{}, cur.meta[tid], ed, nb, tr, R, kd, cur.own[0][tid],
+                                 cur.own[1][tid], cur.own[2][tid],
+                                 stage >= 0 ? cur.own[3][tid] : 0.0f,
+                                 stage >= 1 ? cur.own[4][tid] : 0.0f, hd, u, q_tr, bern, zflux,
+                                 acc, yout, tend, stage, dt, grav, h_ref);
+    }
+  }
+  // no copy may still be writing this block's shared memory when it exits
+  cp_async_wait<0>();
+}
+
 // two consecutive edges per thread: one 16-byte load of their cell words,
 // 8-byte loads and stores of their per-edge values, and twice the
 // independent gathers in flight
@@ -191,6 +307,22 @@ __global__ void __launch_bounds__(512) k_edge32v2(DevMesh M, const float *__rest
 
 inline int nblocks(int n, int t) { return (n + t - 1) / t; }
 
+// persistent grid of the prefetching cell kernel: the resident blocks of
+// every SM (measured once), at most one block per 128 cells
+int cell32p_grid(int nv) {
+  static int per_sm = 0, sms = 0;
+  if (per_sm == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cell32p, kPB, 0);
+    if (per_sm < 1) per_sm = 1;
+    if (sms < 1) sms = 1;
+  }
+  const int g = per_sm * sms, need = nblocks(nv, kPB);
+  return g < need ? g : need;
+}
+
 }  // namespace
 
 void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
@@ -199,7 +331,7 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
   const Tune &T = W.tune;
   const float grav = static_cast<float>(M.grav);
   if (ev) cudaEventRecord(ev[0], s);
-  if (T.variant == 2)
+  if (T.variant >= 2)
     k_tri32c<<<nblocks(M.nt, T.bs_tri), T.bs_tri, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ref,
                                                            W.pv_on, W.flags);
   else
@@ -211,7 +343,11 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
     if (W.learned && stage <= 0)
       learned_launch(M, *W.learned, h_in, u_in, W.q_tr, W.h_ref, T.mlp_gather, W.flags, s);
     if (ev) cudaEventRecord(ev[2], s);
-    if (T.variant == 2)
+    if (T.variant == 3)
+      k_cell32p<<<cell32p_grid(M.nv), kPB, 0, s>>>(M, h_in, u_in, W.q_tr, W.bern, W.zflux,
+                                                  W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
+                                                  grav, W.h_ref);
+    else if (T.variant == 2)
       k_cell32c<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
           M, h_in, u_in, W.q_tr, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
           grav, W.h_ref);

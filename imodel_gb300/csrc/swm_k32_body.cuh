@@ -157,19 +157,21 @@ __device__ __forceinline__ void trsk_cell(const float (&G)[6], const float (&qs)
 // ttgout*d} of each slot (unused pentagon slots repeat slot 0 with zero
 // weights)
 template <class Ix, class Ld>
-__device__ __forceinline__ void cell_core(const DevMesh &M, int i, Ix ix, uint32_t meta,
+// The cell's own values come in as arguments: h (deviation) hi, b bt,
+// 1/(A a) inva, y_n ynv and the RK accumulator accv (read for stages 1-3).
+__device__ __forceinline__ void cell_core(int i, Ix ix, uint32_t meta,
                                           const int (&ed)[6], const int (&nb)[6],
                                           const int (&tr)[6], const float (&R)[6],
-                                          const float2 (&kd)[6], const float *__restrict__ hd,
+                                          const float2 (&kd)[6], float hi, float bt, float inva,
+                                          float ynv, float accv, const float *__restrict__ hd,
                                           const float *__restrict__ u,
                                           const float *__restrict__ q_tr,
                                           float *__restrict__ bern, float *__restrict__ zflux,
-                                          const float *__restrict__ yn, float *__restrict__ acc,
-                                          float *__restrict__ yout, float *__restrict__ tend,
-                                          int stage, float dt, float grav, float h_ref) {
+                                          float *__restrict__ acc, float *__restrict__ yout,
+                                          float *__restrict__ tend, int stage, float dt,
+                                          float grav, float h_ref) {
   const int n = static_cast<int>(meta & 7u);
   const unsigned tneg = meta >> 8;
-  const float hi = Ld::ld(hd + ix(i));
   float ue[6], hn[6], qt[6];
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
@@ -190,7 +192,7 @@ __device__ __forceinline__ void cell_core(const DevMesh &M, int i, Ix ix, uint32
     div += G[j];
     ke += kd[j].x * (ue[j] * ue[j]);
   }
-  bern[ix(i)] = grav * (hi + __ldg(&M.c_bt32[i])) + ke;
+  bern[ix(i)] = grav * (hi + bt) + ke;
   float Z[6];
   if (n == 6)
     trsk_cell<6>(G, qs, R, tneg, Z);
@@ -203,11 +205,28 @@ __device__ __forceinline__ void cell_core(const DevMesh &M, int i, Ix ix, uint32
 #pragma unroll
   for (int j = 0; j < 6; ++j)
     if (j < n) zflux[ix(6 * i + j)] = Z[j];
-  const float masseq = -div * __ldg(&M.c_inva32[i]);
-  if (stage < 0)
+  const float masseq = -div * inva;
+  if (stage < 0) {
     tend[ix(i)] = masseq;
-  else
-    yout[ix(i)] = rk_stage32(stage, masseq, Ld::ld(yn + ix(i)), acc + ix(i), dt);
+  } else {
+    float a = accv;
+    yout[ix(i)] = rk_stage32(stage, masseq, ynv, &a, dt);
+    if (stage < 3) acc[ix(i)] = a;
+  }
+}
+
+// the cell's own values from global memory
+template <class Ix, class Ld>
+__device__ __forceinline__ void cell_own(const DevMesh &M, int i, Ix ix,
+                                         const float *__restrict__ hd,
+                                         const float *__restrict__ yn,
+                                         const float *__restrict__ acc, int stage, float &hi,
+                                         float &bt, float &inva, float &ynv, float &accv) {
+  hi = Ld::ld(hd + ix(i));
+  bt = __ldg(&M.c_bt32[i]);
+  inva = __ldg(&M.c_inva32[i]);
+  ynv = stage >= 0 ? Ld::ld(yn + ix(i)) : 0.0f;
+  accv = stage >= 1 ? Ld::ld(acc + ix(i)) : 0.0f;
 }
 
 template <class Ix, class Ld = LdPlain>
@@ -235,8 +254,10 @@ __device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
     tr[j] = pk.z;
     R[j] = __int_as_float(pk.w);
   }
-  cell_core<Ix, Ld>(M, i, ix, meta, ed, nb, tr, R, kd, hd, u, q_tr, bern, zflux, yn, acc, yout,
-                    tend, stage, dt, grav, h_ref);
+  float hi, bt, inva, ynv, accv;
+  cell_own<Ix, Ld>(M, i, ix, hd, yn, acc, stage, hi, bt, inva, ynv, accv);
+  cell_core<Ix, Ld>(i, ix, meta, ed, nb, tr, R, kd, hi, bt, inva, ynv, accv, hd, u, q_tr, bern,
+                    zflux, acc, yout, tend, stage, dt, grav, h_ref);
 }
 
 // the same from 16-byte slot records {KE weight, ttgout*d, R, edge and
@@ -286,8 +307,10 @@ __device__ __forceinline__ void cell_body16(const DevMesh &M, int i,
       tr[j] = pk.z;
     }
   }
-  cell_core<OneRun, LdPlain>(M, i, OneRun{}, meta, ed, nb, tr, R, kd, hd, u, q_tr, bern, zflux,
-                             yn, acc, yout, tend, stage, dt, grav, h_ref);
+  float hi, bt, inva, ynv, accv;
+  cell_own<OneRun, LdPlain>(M, i, OneRun{}, hd, yn, acc, stage, hi, bt, inva, ynv, accv);
+  cell_core<OneRun, LdPlain>(i, OneRun{}, meta, ed, nb, tr, R, kd, hi, bt, inva, ynv, accv, hd,
+                             u, q_tr, bern, zflux, acc, yout, tend, stage, dt, grav, h_ref);
 }
 
 // -grad B - (Z_c1 + Z_c2) / l_e and the momentum RK stage of edge e
