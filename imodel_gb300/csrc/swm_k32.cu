@@ -146,20 +146,29 @@ __global__ void __launch_bounds__(512) k_cell32c(DevMesh M, const float *__restr
   cell_body16(M, i, hd, u, q_tr, bern, zflux, yn, acc, yout, tend, stage, dt, grav, h_ref);
 }
 
-// ---- variant 3: persistent cell kernel, records prefetched -------------
-// Each thread walks its cells with a grid stride and copies the next cell's
-// records and own values into shared memory (cp.async) while it gathers and
-// computes the current one, so that only the gathers (mostly L2 hits) wait
-// on memory.  A thread reads back only what it copied itself, except the
-// warp's index bases, which lane 0 copies.
+// ---- variant 3: persistent cell kernel, software-pipelined -------------
+// Each thread walks its cells with a grid stride in a three-stage pipeline
+// through shared memory: while it computes cell k, the records of cell k+2
+// (16-bit slot records, meta, own values, warp bases) and the 18 gathered
+// values of cell k+1 (u, neighbour h, q at the triangles) are in flight as
+// cp.async copies.  A thread reads back only what it copied itself, except
+// the warp's index bases, which lane 0 copies.
 constexpr int kPB = 128;  // threads per block
-struct CellPre {
+struct CellRec {
   float4 rec[6][kPB];   // 16-bit slot records
   uint32_t toff[3][kPB];
   uint32_t meta[kPB];
   float own[5][kPB];    // h deviation, b, 1/(A a), y_n, RK accumulator
   int4 wb[kPB / 32];    // warp bases
 };
+struct CellGather {
+  float ue[6][kPB], hn[6][kPB], qt[6][kPB];
+};
+struct CellPipe {
+  CellRec r[2];
+  CellGather g[2];
+};
+constexpr size_t kCellPipeBytes = sizeof(CellPipe);
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -190,12 +199,13 @@ __global__ void __launch_bounds__(kPB) k_cell32p(DevMesh M, const float *__restr
                                                  float *__restrict__ yout,
                                                  float *__restrict__ tend, int stage, float dt,
                                                  float grav, float h_ref) {
-  __shared__ CellPre buf[2];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  CellPipe &P = *reinterpret_cast<CellPipe *>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nv = M.nv;
   const int stride = gridDim.x * kPB;
-  // copies of cell c (every address checked against nv) as one group
-  auto issue = [&](CellPre &B, int c) {
+  // stage 1: the records of cell c (every address checked against nv)
+  auto issue_rec = [&](CellRec &B, int c) {
     if (c < nv) {
 #pragma unroll
       for (int j = 0; j < 6; ++j) cp_async16(&B.rec[j][tid], &M.c_rec[j * nv + c]);
@@ -211,51 +221,73 @@ __global__ void __launch_bounds__(kPB) k_cell32p(DevMesh M, const float *__restr
     }
     cp_async_commit();
   };
-  int base = blockIdx.x * kPB;
-  issue(buf[0], base + tid);
-  // the trip count is uniform over a warp (its first cell decides)
-  for (int it = 0; base + 32 * warp < nv; ++it, base += stride) {
-    const int i = base + tid;
-    CellPre &cur = buf[it & 1];
-    __syncwarp();  // every lane is done with the buffer refilled next
-    issue(buf[(it + 1) & 1], i + stride);
-    cp_async_wait<1>();
-    __syncwarp();  // lane 0's copy of the warp bases
-    if (i < nv) {
-      const int4 wb = cur.wb[warp];
-      int ed[6], nb[6], tr[6];
-      float R[6];
-      float2 kd[6];
-      float4 rec[6];
+  // stage 2: decode cell c's indices from its records, copy its gathers
+  auto issue_gather = [&](const CellRec &B, CellGather &G, int c) {
+    if (c < nv) {
+      const int4 wb = B.wb[warp];
 #pragma unroll
       for (int j = 0; j < 6; ++j) {
-        rec[j] = cur.rec[j][tid];
-        R[j] = rec[j].z;
-        kd[j] = make_float2(rec[j].x, rec[j].y);
-      }
-      if (wb.w) {
-#pragma unroll
-        for (int j = 0; j < 6; ++j) {
-          const uint32_t w = __float_as_uint(rec[j].w);
-          const uint32_t tp = cur.toff[j >> 1][tid];
-          ed[j] = wb.x + static_cast<int>(w & 0xFFFFu);
-          nb[j] = wb.y + static_cast<int>(w >> 16);
-          tr[j] = wb.z + static_cast<int>((tp >> (16 * (j & 1))) & 0xFFFFu);
+        int e, n, t;
+        if (wb.w) {
+          const uint32_t w = __float_as_uint(B.rec[j][tid].w);
+          const uint32_t tp = B.toff[j >> 1][tid];
+          e = wb.x + static_cast<int>(w & 0xFFFFu);
+          n = wb.y + static_cast<int>(w >> 16);
+          t = wb.z + static_cast<int>((tp >> (16 * (j & 1))) & 0xFFFFu);
+        } else {
+          const int4 pk = __ldg(&M.c_pk[j * nv + c]);
+          e = pk.x;
+          n = pk.y;
+          t = pk.z;
         }
-      } else {
-#pragma unroll
-        for (int j = 0; j < 6; ++j) {
-          const int4 pk = __ldg(&M.c_pk[j * nv + i]);
-          ed[j] = pk.x;
-          nb[j] = pk.y;
-          tr[j] = pk.z;
-        }
+        cp_async4(&G.ue[j][tid], u + e);
+        cp_async4(&G.hn[j][tid], hd + n);
+        cp_async4(&G.qt[j][tid], q_tr + t);
       }
-      cell_core<OneRun, LdPlain>(i, OneRun{}, cur.meta[tid], ed, nb, tr, R, kd, cur.own[0][tid],
-                                 cur.own[1][tid], cur.own[2][tid],
-                                 stage >= 0 ? cur.own[3][tid] : 0.0f,
-                                 stage >= 1 ? cur.own[4][tid] : 0.0f, hd, u, q_tr, bern, zflux,
-                                 acc, yout, tend, stage, dt, grav, h_ref);
+    }
+    cp_async_commit();
+  };
+  int base = blockIdx.x * kPB;
+  // prologue: records of cells 0 and 1 in flight, gathers of cell 0
+  issue_rec(P.r[0], base + tid);
+  issue_rec(P.r[1], base + stride + tid);
+  cp_async_wait<1>();
+  __syncwarp();
+  issue_gather(P.r[0], P.g[0], base + tid);
+  // the trip count is uniform over a warp (its first cell decides); at the
+  // top of iteration k the copies of records k+1 and gathers k are pending
+  for (int k = 0; base + 32 * warp < nv; ++k, base += stride) {
+    const int i = base + tid;
+    CellRec &rk = P.r[k & 1];
+    // cell k's record values into registers: its buffer takes cell k+2
+    const uint32_t meta = rk.meta[tid];
+    float R[6];
+    float2 kd[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      const float4 r = rk.rec[j][tid];
+      R[j] = r.z;
+      kd[j] = make_float2(r.x, r.y);
+    }
+    const float hi = rk.own[0][tid], bt = rk.own[1][tid], inva = rk.own[2][tid];
+    const float ynv = stage >= 0 ? rk.own[3][tid] : 0.0f;
+    const float accv = stage >= 1 ? rk.own[4][tid] : 0.0f;
+    __syncwarp();  // every lane is done with the warp bases of this buffer
+    issue_rec(rk, i + 2 * stride);
+    cp_async_wait<1>();  // records k+1 and gathers k are in
+    __syncwarp();        // lane 0's copy of the warp bases of k+1
+    issue_gather(P.r[(k + 1) & 1], P.g[(k + 1) & 1], i + stride);
+    if (i < nv) {
+      const CellGather &gk = P.g[k & 1];
+      float ue[6], hn[6], qt[6];
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        ue[j] = gk.ue[j][tid];
+        hn[j] = gk.hn[j][tid];
+        qt[j] = gk.qt[j][tid];
+      }
+      cell_math(i, meta, R, kd, ue, hn, qt, hi, bt, inva, ynv, accv, bern, zflux, acc, yout,
+                tend, stage, dt, grav, h_ref);
     }
   }
   // no copy may still be writing this block's shared memory when it exits
@@ -315,7 +347,9 @@ int cell32p_grid(int nv) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cell32p, kPB, 0);
+    cudaFuncSetAttribute(k_cell32p, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(kCellPipeBytes));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cell32p, kPB, kCellPipeBytes);
     if (per_sm < 1) per_sm = 1;
     if (sms < 1) sms = 1;
   }
@@ -344,7 +378,7 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
       learned_launch(M, *W.learned, h_in, u_in, W.q_tr, W.h_ref, T.mlp_gather, W.flags, s);
     if (ev) cudaEventRecord(ev[2], s);
     if (T.variant == 3)
-      k_cell32p<<<cell32p_grid(M.nv), kPB, 0, s>>>(M, h_in, u_in, W.q_tr, W.bern, W.zflux,
+      k_cell32p<<<cell32p_grid(M.nv), kPB, kCellPipeBytes, s>>>(M, h_in, u_in, W.q_tr, W.bern, W.zflux,
                                                   W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
                                                   grav, W.h_ref);
     else if (T.variant == 2)

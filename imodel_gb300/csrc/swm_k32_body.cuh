@@ -151,34 +151,20 @@ __device__ __forceinline__ void trsk_cell(const float (&G)[6], const float (&qs)
   }
 }
 
-// div F, K, Bernoulli potential, PV-flux contributions Z (cell-major
-// zflux[cell][6]) and the mass RK stage of cell i, from its decoded slot
-// records: edge, neighbour, triangle, kite fraction R and {KE weight,
-// ttgout*d} of each slot (unused pentagon slots repeat slot 0 with zero
-// weights)
-template <class Ix, class Ld>
-// The cell's own values come in as arguments: h (deviation) hi, b bt,
-// 1/(A a) inva, y_n ynv and the RK accumulator accv (read for stages 1-3).
-__device__ __forceinline__ void cell_core(int i, Ix ix, uint32_t meta,
-                                          const int (&ed)[6], const int (&nb)[6],
-                                          const int (&tr)[6], const float (&R)[6],
-                                          const float2 (&kd)[6], float hi, float bt, float inva,
-                                          float ynv, float accv, const float *__restrict__ hd,
-                                          const float *__restrict__ u,
-                                          const float *__restrict__ q_tr,
+// the arithmetic of one cell from its gathered values: div F, K, the
+// Bernoulli potential, the PV-flux contributions Z (cell-major zflux) and
+// the mass RK stage
+template <class Ix = OneRun>
+__device__ __forceinline__ void cell_math(int i, uint32_t meta, const float (&R)[6],
+                                          const float2 (&kd)[6], const float (&ue)[6],
+                                          const float (&hn)[6], const float (&qt)[6], float hi,
+                                          float bt, float inva, float ynv, float accv,
                                           float *__restrict__ bern, float *__restrict__ zflux,
                                           float *__restrict__ acc, float *__restrict__ yout,
                                           float *__restrict__ tend, int stage, float dt,
-                                          float grav, float h_ref) {
+                                          float grav, float h_ref, Ix ix = Ix{}) {
   const int n = static_cast<int>(meta & 7u);
   const unsigned tneg = meta >> 8;
-  float ue[6], hn[6], qt[6];
-#pragma unroll
-  for (int j = 0; j < 6; ++j) {
-    ue[j] = Ld::ld(u + ix(ed[j]));
-    hn[j] = Ld::ld(hd + ix(nb[j]));
-    qt[j] = Ld::ld(q_tr + ix(tr[j]));
-  }
   float G[6], qs[6];
   float div = 0.0f, ke = 0.0f;
   const float qlast = n == 6 ? qt[5] : (n == 5 ? qt[4] : (n == 4 ? qt[3] : qt[2]));
@@ -213,6 +199,36 @@ __device__ __forceinline__ void cell_core(int i, Ix ix, uint32_t meta,
     yout[ix(i)] = rk_stage32(stage, masseq, ynv, &a, dt);
     if (stage < 3) acc[ix(i)] = a;
   }
+}
+
+// div F, K, Bernoulli potential, PV-flux contributions Z (cell-major
+// zflux[cell][6]) and the mass RK stage of cell i, from its decoded slot
+// records: edge, neighbour, triangle, kite fraction R and {KE weight,
+// ttgout*d} of each slot (unused pentagon slots repeat slot 0 with zero
+// weights), gathering its neighbours' values.  The cell's own values come in
+// as arguments: h (deviation) hi, b bt, 1/(A a) inva, y_n ynv and the RK
+// accumulator accv (read for stages 1-3).
+template <class Ix, class Ld>
+__device__ __forceinline__ void cell_core(int i, Ix ix, uint32_t meta,
+                                          const int (&ed)[6], const int (&nb)[6],
+                                          const int (&tr)[6], const float (&R)[6],
+                                          const float2 (&kd)[6], float hi, float bt, float inva,
+                                          float ynv, float accv, const float *__restrict__ hd,
+                                          const float *__restrict__ u,
+                                          const float *__restrict__ q_tr,
+                                          float *__restrict__ bern, float *__restrict__ zflux,
+                                          float *__restrict__ acc, float *__restrict__ yout,
+                                          float *__restrict__ tend, int stage, float dt,
+                                          float grav, float h_ref) {
+  float ue[6], hn[6], qt[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    ue[j] = Ld::ld(u + ix(ed[j]));
+    hn[j] = Ld::ld(hd + ix(nb[j]));
+    qt[j] = Ld::ld(q_tr + ix(tr[j]));
+  }
+  cell_math(i, meta, R, kd, ue, hn, qt, hi, bt, inva, ynv, accv, bern, zflux, acc, yout, tend,
+            stage, dt, grav, h_ref, ix);
 }
 
 // the cell's own values from global memory
