@@ -187,19 +187,15 @@ def kernel_bytes(nv, ne, nt, precision, variant=0):
     # triangle: f, 3 circulation coefs, 3 edge idx, 3 kite coefs, 3 cell idx,
     # q out; gathers u and h
     tri = nt * (w + 3 * w + 3 * 4 + 3 * w + 3 * 4 + w) + ne * w + nv * w
-    if precision == "fp32" and variant in (1, 2, 3):
+    if precision == "fp32" and variant in (1, 2):
+        if variant == 2:
+            # the triangle record: 40 bytes (6 16-bit indices, f in the
+            # record), 8 bytes of bases per warp of 32 triangles
+            tri = nt * (40 + 8 / 32 + w) + ne * w + nv * w
         # cell: meta, 1/(A a), b, 6 slots x (edge, neighbour, triangle idx,
         # kite fraction, KE weight, ttgout*d); h, y_n, acc r/w, y_out, B out,
         # 6 PV-flux contributions out; gathers u and q
-        slots = 6 * 24
-        if variant >= 2:
-            # 16-byte slot records with 16-bit edge and neighbour offsets, 2-byte
-            # triangle offsets, 16 bytes of bases per warp of 32 cells; the
-            # triangle record: 40 bytes (6 16-bit indices, f in the record),
-            # 8 bytes of bases per warp of 32 triangles
-            slots = 6 * 16 + 6 * 2 + 16 / 32
-            tri = nt * (40 + 8 / 32 + w) + ne * w + nv * w
-        cell = nv * (4 + 4 + 4 + slots + 4 + 4 + 8 + 4 + 4 + 6 * 4) + ne * w + nt * w
+        cell = nv * (4 + 4 + 4 + 6 * 24 + 4 + 4 + 8 + 4 + 4 + 6 * 4) + ne * w + nt * w
         # edge: 2 cell words, 1/(l a), y_n, acc r/w, y_out; gathers B and
         # the cells' PV-flux contributions
         edge = ne * (8 + 4 + 4 + 8 + 4) + nv * 4 + nv * 6 * 4
@@ -215,9 +211,9 @@ def kernel_bytes(nv, ne, nt, precision, variant=0):
 
 
 def kernel_names(variant):
-    if variant >= 2:
-        return {"triangle": "k_tri32c", "edge_pre": "",
-                "cell": "k_cell32p" if variant == 3 else "k_cell32c", "edge": "k_edge32v2"}
+    if variant == 2:
+        return {"triangle": "k_tri32c", "edge_pre": "", "cell": "k_cell32v2",
+                "edge": "k_edge32v2"}
     v2 = "v2" if variant == 1 else ""
     return {"triangle": "k_tri32", "edge_pre": "k_edge_pre32", "cell": "k_cell32" + v2,
             "edge": "k_edge32" + v2}

@@ -577,16 +577,12 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
     M.c_pk = reinterpret_cast<const int4 *>(pk);
     M.c_kd = reinterpret_cast<const float2 *>(kd);
     M.e_vs2 = reinterpret_cast<const uint2 *>(vs2);
-    const uint32_t *crec = nullptr, *ta = nullptr;
-    const int32_t *cwb = nullptr, *twb = nullptr;
+    const uint32_t *ta = nullptr;
+    const int32_t *twb = nullptr;
     const float *tb = nullptr, *tc = nullptr;
-    if ((rc = upload(H, L.c_rec, &crec)) || (rc = upload(H, L.c_toff, &M.c_toff)) ||
-        (rc = upload(H, L.c_wb, &cwb)) || (rc = upload(H, L.t_c16A, &ta)) ||
-        (rc = upload(H, L.t_c16B, &tb)) || (rc = upload(H, L.t_c16C, &tc)) ||
-        (rc = upload(H, L.t_wb, &twb)))
+    if ((rc = upload(H, L.t_c16A, &ta)) || (rc = upload(H, L.t_c16B, &tb)) ||
+        (rc = upload(H, L.t_c16C, &tc)) || (rc = upload(H, L.t_wb, &twb)))
       return rc;
-    M.c_rec = reinterpret_cast<const float4 *>(crec);
-    M.c_wb = reinterpret_cast<const int4 *>(cwb);
     M.t_c16A = reinterpret_cast<const uint4 *>(ta);
     M.t_c16B = reinterpret_cast<const float4 *>(tb);
     M.t_c16C = reinterpret_cast<const float2 *>(tc);
@@ -949,7 +945,7 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
   imodel::Tune best;
   float best_ms = 1e30f;
   // the learned correction is wired into the cell-centred variants only
-  for (int v = H->learned_on ? 1 : 0; v <= 3; ++v)
+  for (int v = H->learned_on ? 1 : 0; v <= 2; ++v)
     for (int b : sizes) {
       imodel::Tune t;
       t.variant = v;
@@ -1019,11 +1015,11 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[6]) {
   for (int k = 1; k < 5; ++k)
     if (choice[k] != 128 && choice[k] != 256 && choice[k] != 512)
       return imodel::set_error(H, IMODEL_SWM_EINVAL, "block sizes must be 128, 256 or 512");
-  if (choice[0] < 0 || choice[0] > 3)
-    return imodel::set_error(H, IMODEL_SWM_EINVAL, "variant must be 0, 1, 2 or 3");
+  if (choice[0] < 0 || choice[0] > 2)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "variant must be 0, 1 or 2");
   if (H->learned_on && choice[0] == 0)
     return imodel::set_error(H, IMODEL_SWM_EINVAL,
-                             "the learned correction runs with the cell-centred variants (1-3) only");
+                             "the learned correction runs with the cell-centred variants (1, 2) only");
   imodel::Tune t;
   t.variant = choice[0];
   t.bs_tri = choice[1];
@@ -1059,7 +1055,7 @@ const char *imodel_swm_main_kernel(void *handle) {
   if (!H) return "";
   if (H->precision == IMODEL_SWM_FP64) return "k_edge64";
   const int v = H->W32.tune.variant;
-  return v == 3 ? "k_cell32p" : v == 2 ? "k_cell32c" : (v == 1 ? "k_cell32v2" : "k_edge32");
+  return v >= 1 ? "k_cell32v2" : "k_edge32";
 }
 
 void *imodel_swm_stream(void *handle) {

@@ -36,15 +36,10 @@ struct DevMesh {
   const int4 *c_pk;     // [6][nv] {edge, neighbour, triangle, kite fraction bits}
   const float2 *c_kd;   // [6][nv] {KE weight, ttgout*d}
   const uint2 *e_vs2;   // [ne] both cell words of an edge
-  // the same records with 16-bit indices against per-warp bases (variant 2;
-  // swm_layout.h): cells {KE weight, ttgout*d, R, edge | neighbour << 16}
-  // [6][nv], triangle offsets of slot pairs [3][nv], warp bases {edge,
-  // neighbour, triangle, usable}; triangles {e0|e1, e2|c0, c1|c2, circ 0},
-  // {circ 1, circ 2, kite 0, kite 1}, {kite 2, f} [nt], warp bases {edge,
-  // cell (-1: use the 32-bit records)}
-  const float4 *c_rec;
-  const uint32_t *c_toff;
-  const int4 *c_wb;
+  // the triangle records with 16-bit indices against per-warp bases
+  // (variant 2; swm_layout.h): {e0|e1, e2|c0, c1|c2, circ 0}, {circ 1,
+  // circ 2, kite 0, kite 1}, {kite 2, f} [nt], warp bases {edge, cell (-1:
+  // use the 32-bit records)}
   const uint4 *t_c16A;
   const float4 *t_c16B;
   const float2 *t_c16C;
@@ -55,10 +50,8 @@ struct DevMesh {
 //   variant 0: triangle -> edge pre-pass -> cell -> edge (10-entry stencil)
 //   variant 1: triangle -> cell (cell-centred TRSK, writes the PV flux
 //              contribution of each cell edge) -> edge (sums two cells)
-//   variant 2: variant 1 reading the triangle and cell records with 16-bit
-//              indices (36 B less per cell and 12 B less per triangle)
-//   variant 3: variant 2 with a persistent cell kernel that prefetches the
-//              next cell's records into shared memory (block size 128)
+//   variant 2: variant 1 reading the triangle records with 16-bit indices
+//              (40 instead of 52 bytes per triangle)
 struct Tune {
   int variant = 1;
   int bs_tri = 256, bs_pre = 256, bs_cell = 256, bs_edge = 256;
@@ -70,7 +63,7 @@ struct LearnedDev;
 // Working fields of one handle, in the handle's precision T.
 template <class T>
 struct Work {
-  const LearnedDev *learned = nullptr;  // FP32 variant 1: learned correction on
+  const LearnedDev *learned = nullptr;  // FP32 variants 1, 2: learned correction on
   T *yn_h, *yn_u;    // state at t_n (advanced in place at the last stage)
   T *ya_h, *ya_u;    // stage inputs (ping)
   T *yb_h, *yb_u;    // stage inputs (pong)
@@ -79,7 +72,7 @@ struct Work {
   T *h_ed, *uh, *q_ed;  // [ne]
   T *bern;           // [nv] g (h + b) + K
   T *tend_h, *tend_u;   // tendency outputs (tendency-only evaluations)
-  T *zflux;          // [6][nv] cell-centred PV flux of each cell edge (variant 1)
+  T *zflux;          // [6][nv] cell-centred PV flux of each cell edge (variants 1, 2)
   Tune tune;
   int *flags;        // bit 0: PV division by ~0
   T h_ref;           // FP32: h is stored as h - h_ref

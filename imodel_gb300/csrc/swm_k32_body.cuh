@@ -276,59 +276,6 @@ __device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
                     zflux, acc, yout, tend, stage, dt, grav, h_ref);
 }
 
-// the same from 16-byte slot records {KE weight, ttgout*d, R, edge and
-// neighbour offsets} plus the triangle offsets of slot pairs (single runs):
-// a warp of 32 cells shares one base per index kind (c_wb); a warp whose
-// indices span more than 65,536 takes its indices from the 32-bit records
-// instead (warp-uniform branch).  Records and bases are loaded together.
-__device__ __forceinline__ void cell_body16(const DevMesh &M, int i,
-                                            const float *__restrict__ hd,
-                                            const float *__restrict__ u,
-                                            const float *__restrict__ q_tr,
-                                            float *__restrict__ bern, float *__restrict__ zflux,
-                                            const float *__restrict__ yn, float *__restrict__ acc,
-                                            float *__restrict__ yout, float *__restrict__ tend,
-                                            int stage, float dt, float grav, float h_ref) {
-  const int nv = M.nv;
-  const int4 wb = __ldg(&M.c_wb[i >> 5]);
-  const uint32_t meta = __ldg(&M.c_meta[i]);
-  float4 rec[6];
-  uint32_t tp[3];
-#pragma unroll
-  for (int j = 0; j < 6; ++j) rec[j] = __ldg(&M.c_rec[j * nv + i]);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) tp[k] = __ldg(&M.c_toff[k * nv + i]);
-  int ed[6], nb[6], tr[6];
-  float R[6];
-  float2 kd[6];
-#pragma unroll
-  for (int j = 0; j < 6; ++j) {
-    R[j] = rec[j].z;
-    kd[j] = make_float2(rec[j].x, rec[j].y);
-  }
-  if (wb.w) {
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-      const uint32_t w = __float_as_uint(rec[j].w);
-      ed[j] = wb.x + static_cast<int>(w & 0xFFFFu);
-      nb[j] = wb.y + static_cast<int>(w >> 16);
-      tr[j] = wb.z + static_cast<int>((tp[j >> 1] >> (16 * (j & 1))) & 0xFFFFu);
-    }
-  } else {
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-      const int4 pk = __ldg(&M.c_pk[j * nv + i]);
-      ed[j] = pk.x;
-      nb[j] = pk.y;
-      tr[j] = pk.z;
-    }
-  }
-  float hi, bt, inva, ynv, accv;
-  cell_own<OneRun, LdPlain>(M, i, OneRun{}, hd, yn, acc, stage, hi, bt, inva, ynv, accv);
-  cell_core<OneRun, LdPlain>(i, OneRun{}, meta, ed, nb, tr, R, kd, hi, bt, inva, ynv, accv, hd,
-                             u, q_tr, bern, zflux, acc, yout, tend, stage, dt, grav, h_ref);
-}
-
 // -grad B - (Z_c1 + Z_c2) / l_e and the momentum RK stage of edge e
 template <class Ix, class Ld = LdPlain>
 __device__ __forceinline__ void edge_body(const DevMesh &M, int e, Ix ix, uint2 w,

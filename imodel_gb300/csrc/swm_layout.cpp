@@ -282,45 +282,6 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
     L.e_vs2[2 * e] = L.e_vs[e];
     L.e_vs2[2 * e + 1] = L.e_vs[NE + e];
   }
-  {
-    // 16-bit cell records: bases per warp of 32 cells
-    const size_t nw = (NV + 31) / 32;
-    L.c_rec.assign(kMaxNb * NV * 4, 0u);
-    L.c_toff.assign(3 * NV, 0u);
-    L.c_wb.assign(4 * nw, 0);
-    auto fbits = [](float f) {
-      uint32_t b;
-      std::memcpy(&b, &f, sizeof(b));
-      return b;
-    };
-    for (size_t w = 0; w < nw; ++w) {
-      const size_t i0 = 32 * w, i1 = std::min(NV, i0 + 32);
-      int32_t lo[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, hi[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
-      for (size_t i = i0; i < i1; ++i)
-        for (int j = 0; j < kMaxNb; ++j)
-          for (int k = 0; k < 3; ++k) {
-            const int32_t v = L.c_pk[4 * (j * NV + i) + k];
-            lo[k] = std::min(lo[k], v);
-            hi[k] = std::max(hi[k], v);
-          }
-      bool ok = true;
-      for (int k = 0; k < 3; ++k) ok = ok && static_cast<int64_t>(hi[k]) - lo[k] <= 0xFFFF;
-      for (int k = 0; k < 3; ++k) L.c_wb[4 * w + k] = ok ? lo[k] : 0;
-      L.c_wb[4 * w + 3] = ok ? 1 : 0;
-      for (size_t i = i0; i < i1; ++i)
-        for (int j = 0; j < kMaxNb; ++j) {
-          const size_t q = j * NV + i;
-          uint32_t off[3] = {0u, 0u, 0u};
-          if (ok)
-            for (int k = 0; k < 3; ++k) off[k] = static_cast<uint32_t>(L.c_pk[4 * q + k] - lo[k]);
-          L.c_rec[4 * q + 0] = fbits(L.c_kd[2 * q + 0]);
-          L.c_rec[4 * q + 1] = fbits(L.c_kd[2 * q + 1]);
-          L.c_rec[4 * q + 2] = static_cast<uint32_t>(L.c_pk[4 * q + 3]);
-          L.c_rec[4 * q + 3] = off[0] | (off[1] << 16);
-          L.c_toff[(j / 2) * NV + i] |= off[2] << (16 * (j % 2));
-        }
-    }
-  }
 
   // --- triangles ------------------------------------------------------
   L.t_ed.resize(3 * NT);

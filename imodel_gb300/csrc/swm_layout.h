@@ -58,15 +58,6 @@ struct Layout {
   std::vector<int32_t> c_pk;                 // [6][nv][4]
   std::vector<float> c_kd;                   // [6][nv][2]
   std::vector<uint32_t> e_vs2;               // [ne][2] both cell words of an edge
-  // the cell records with 16-bit indices: per warp of 32 cells one base per
-  // index kind, c_wb [nwarps][4] = {edge, neighbour, triangle, usable}
-  // (usable = 0 when the warp's indices of some kind span more than 65,536);
-  // c_rec [6][nv][4] = {KE weight, ttgout*d, R, (edge - base) |
-  // (neighbour - base) << 16} as bits, c_toff [3][nv] = offsets of the
-  // triangles of slots 2k and 2k+1
-  std::vector<uint32_t> c_rec;
-  std::vector<uint32_t> c_toff;
-  std::vector<int32_t> c_wb;
 
   // edges [ne] and [2][ne]
   std::vector<int32_t> e_v;                  // [2][ne] cells (ed%v = edhx%sh)

@@ -178,7 +178,9 @@ int imodel_swm_advance(void *handle, double dt, int32_t nsteps);
  * the fastest and restores the state.  choice = {variant, block size of the
  * triangle, edge pre-pass, cell and edge kernels, gather groups of the
  * learned-correction kernel}; variant 0 uses the 10-entry edge stencil,
- * variant 1 the cell-centred TRSK sum; the last entry is 2, 3 or 4 with the
+ * variant 1 the cell-centred TRSK sum, variant 2 the same with triangle
+ * records holding 16-bit indices (bit-identical results); the last entry is
+ * 2, 3 or 4 with the
  * learned correction on (its kernel has 6 warp groups, the rest run the
  * epilogue) and 0 without it.  The FP64 path has a single configuration and
  * returns it. */

@@ -152,7 +152,7 @@ def test_fp32_error_against_fp64(grid_at):
     assert eh < disc / 100
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("variant", [0, 1, 2])
 def test_fp32_variants_against_fp64(grid_at, variant):
     """The FP32 fusion variants (edge stencil, cell-centred TRSK, the latter
     on 16-bit records) stay within FP32 round-off of the FP64 oracle over 5
@@ -184,16 +184,15 @@ def test_fp32_block_sizes_do_not_change_results(grid_at):
         assert np.array_equal(o[0], out[0][0]) and np.array_equal(o[1], out[0][1])
 
 
-def test_fp32_16bit_records_equal_32bit(grid_at):
-    """Variant 2 reads the same triangle and cell records with 16-bit indices
-    against per-warp bases (warps whose indices span more than 65,536 keep the
-    32-bit records), variant 3 prefetches them through shared memory in a
-    persistent cell kernel: the same arithmetic, so the states equal variant
-    1's bit for bit.  Level 7 has warps of both kinds."""
+def test_fp32_16bit_triangle_records_equal_32bit(grid_at):
+    """Variant 2 reads the same triangle records with 16-bit indices against
+    per-warp bases (warps whose indices span more than 65,536 keep the 32-bit
+    records): the same arithmetic, so the states equal variant 1's bit for
+    bit.  Level 7 has warps of both kinds."""
     g = grid_at(7)
     h, u = fields.balanced_state(g, lmax=32, seed=11)
     out = []
-    for v in (1, 2, 3):
+    for v in (1, 2):
         m = SWM(g, "fp32")
         m.set_tuning(variant=v, bs_tri=256, bs_pre=256, bs_cell=128, bs_edge=256)
         out.append(m.ode_rk4(h, u, 225.0, 6) + m.tendency(h, u))
@@ -207,7 +206,7 @@ def test_autotune_keeps_state(grid_at):
     m = SWM(g, "fp32")
     m.set_state(h, u)
     choice = m.autotune(225.0, 3)
-    assert choice["variant"] in (0, 1, 2, 3)
+    assert choice["variant"] in (0, 1, 2)
     h1, u1 = m.get_state()
     np.testing.assert_allclose(h1, h, rtol=0, atol=1e-3)   # FP32 storage of h - h_ref
     np.testing.assert_allclose(u1, u, rtol=0, atol=1e-5)
