@@ -58,12 +58,12 @@ def _edge_w(g):
     return g.ed_leng * g.edhx_leng / 2.0
 
 
-def run(grid, path, h, u, dt, nsteps, bt=None, params=None, chunk=0):
+def run(grid, path, h, u, dt, nsteps, bt=None, params=None, chunk=0, testcase=2):
     """One run on the GPU; returns the final state, timing and diagnostics.
     path: "fp64", "fp32" or "fp32l" (FP32 + learned correction)."""
     from . import swm
     m = swm.SWM(grid, precision="fp64" if path == "fp64" else "fp32", bt=bt,
-                learned_params=params if path == "fp32l" else None)
+                learned_params=params if path == "fp32l" else None, testcase=testcase)
     try:
         m.set_state(h, u)
         if path != "fp64":
@@ -85,7 +85,7 @@ def run(grid, path, h, u, dt, nsteps, bt=None, params=None, chunk=0):
         hf, uf = m.get_state()
     finally:
         m.close()
-    rel = lambda k: (d1[k] - d0[k]) / abs(d0[k])  # noqa: E731
+    rel = lambda k: (d1[k] - d0[k]) / abs(d0[k]) if d0[k] else d1[k] - d0[k]  # noqa: E731
     return {"h": hf, "u": uf, "seconds": el, "steps": nsteps,
             "cell_steps_per_s": grid.nv * nsteps / el,
             "mass_change": rel("mass"), "tenergy_change": rel("tenergy"),
@@ -268,7 +268,41 @@ def exp_large(args, pool):
     return out
 
 
-RUNS = {"tc2": exp_tc2, "balanced": exp_balanced, "ensemble": exp_ensemble,
+def exp_williamson(args, pool):
+    """Cases 1, 5 and 6 of the reference (imodel_gb300/testcases.py) at one
+    level (default 7), time steps scaled from level 5 (900, 300 and 225 s)
+    by the grid spacing.  Case 1 (cosine bell, one 12-day rotation) against
+    its initial state, the exact solution; cases 5 (15 days) and 6 (14 days)
+    FP32 and FP32 + learned against FP64, with mass and energy changes."""
+    from . import swm, testcases
+    from .mesh import meshbuild
+    lvl = args.level or 7
+    g = meshbuild(lvl)
+    scale = 2.0 ** (5 - lvl)
+    out = {"level": lvl}
+    for case, dt5, days in ((1, 900.0, 12.0), (5, 300.0, 15.0), (6, 225.0, 14.0)):
+        dt = dt5 * scale
+        n = swm.ntime_for(days, dt)
+        h, u, bt = testcases.initialize_fields(g, case)
+        btp = bt if np.any(bt != 0) else None
+        res = {"dt": dt, "steps": n, "days": days}
+        r64 = run(g, "fp64", h, u, dt, n, bt=btp, testcase=case)
+        res["fp64"] = _summary(r64)
+        paths = ("fp32",) if case < 2 else ("fp32", "fp32l")
+        for path in paths:
+            r = run(g, path, h, u, dt, n, bt=btp, testcase=case,
+                    params=_params(args) if path == "fp32l" else None)
+            res[path] = dict(_summary(r), h_vs_fp64=rel_errors(r["h"], r64["h"], g.hx_areag),
+                             u_vs_fp64=rel_errors(r["u"], r64["u"], _edge_w(g)))
+            if case == 1:
+                res[path]["h_vs_exact"] = rel_errors(r["h"], h, g.hx_areag)
+        if case == 1:
+            res["fp64"]["h_vs_exact"] = rel_errors(r64["h"], h, g.hx_areag)
+        out[f"case{case}"] = res
+    return out
+
+
+RUNS = {"tc2": exp_tc2, "williamson": exp_williamson, "balanced": exp_balanced, "ensemble": exp_ensemble,
         "mountains": exp_mountains, "fixed": exp_fixed, "large": exp_large}
 
 

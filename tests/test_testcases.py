@@ -1,0 +1,81 @@
+"""Initial states of test cases 0, 1, 5 and 6 (imodel_gb300/testcases.py)
+and the truncation error of the discrete tendency against the analytic
+case-6 tendency, computed by the oracle (the GPU FP64 path equals the oracle
+bit for bit, tests/test_gpu_testcases.py)."""
+import numpy as np
+import pytest
+
+import oracle
+from imodel_gb300 import testcases as tc
+from imodel_gb300.mesh import ERAD
+
+
+def rel_l2(a, b, w):
+    return float(np.sqrt(np.sum(w * (a - b) ** 2) / np.sum(w * b ** 2)))
+
+
+def test_case0_and_case1_fields(grid_at):
+    g = grid_at(5)
+    h, u, bt = tc.initialize_fields(g, 0)
+    assert np.all(u == 0) and np.all(bt == 0)
+    assert abs(h.max() - 1.0) < 1e-2 and abs(h.min() + 1.0) < 1e-2
+    h, u, bt = tc.initialize_fields(g, 1)
+    lon, lat = tc.lonlat(g.v_p)
+    r = ERAD * tc.arclen(g.v_p, tc.sph2cart(0.0, 0.0))
+    assert np.all(h[r >= ERAD / 3.0] == 0.0)
+    assert 990.0 < h.max() <= 1000.0
+    # solid-body rotation: u = u0 cos(lat) e_lon . tg, at most u0 (with the
+    # reference's pi, built from a float32 literal)
+    assert np.abs(u).max() <= 2.0 * tc.PI * ERAD / (12 * 86400.0) + 1e-9
+
+
+def test_case5_mountain(grid_at):
+    g = grid_at(6)
+    h, u, bt = tc.initialize_fields(g, 5)
+    k = np.argmax(bt)
+    lon, _ = tc.lonlat(g.v_p)
+    assert abs(lon[k] + np.pi / 2) < 0.05 and abs(g.v_lat[k] - np.pi / 6) < 0.05
+    assert 1800.0 < bt.max() <= 2000.0 and bt.min() == 0.0
+    # the free surface h + b is the zonal-flow surface, unaffected by the cone
+    s = np.sin(g.v_lat)
+    h_ct = (ERAD * 7.292e-5 * 20.0 + 200.0) / 9.80616
+    np.testing.assert_allclose(h + bt, 5960.0 - h_ct * s * s, rtol=0, atol=1e-9)
+
+
+def test_case6_fields_match_analytic_wave(grid_at):
+    g = grid_at(5)
+    h, u, bt = tc.initialize_fields(g, 6)
+    # wave pattern: h varies with 4 lon periods along a latitude circle
+    lon, _ = tc.lonlat(g.v_p)
+    band = np.abs(g.v_lat - np.radians(30.0)) < 0.03
+    c = np.corrcoef(h[band], np.cos(4 * lon[band]))[0, 1]
+    assert c > 0.99
+    assert h.min() == 8000.0 and h.max() < 11000.0  # h0 at the poles
+
+
+def test_case6_truncation_error_converges(grid_at):
+    """masseq converges at first order or better in L2 on these grids; the
+    TRSK momentum tendency converges slowly in L2 (its maximum error does not
+    converge on grids without optimisation, a known property of TRSK on
+    icosahedral grids)."""
+    oracle.build()
+    em, eu = [], []
+    for level in (3, 4, 5, 6):
+        g = grid_at(level)
+        h, u, _ = tc.initialize_fields(g, 6)
+        mex, uex = tc.tc6_exact_tendency(g)
+        m, mo = oracle.Oracle(g, 6).tendency(h, u)
+        em.append(rel_l2(m, mex, g.hx_areag))
+        eu.append(rel_l2(mo, uex, g.ed_leng * g.edhx_leng))
+    print("case 6 truncation error, levels 3-6: masseq", ["%.3e" % x for x in em],
+          "momeq", ["%.3e" % x for x in eu])
+    for a, b in zip(em, em[1:]):
+        assert a / b > 1.8
+    for a, b in zip(eu, eu[1:]):
+        assert a / b > 1.2
+    assert em[-1] < 0.1 and eu[-1] < 0.3
+
+
+def test_unknown_case_is_refused(grid_at):
+    with pytest.raises(ValueError):
+        tc.initialize_fields(grid_at(2), 21)
