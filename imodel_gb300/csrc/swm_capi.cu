@@ -55,6 +55,7 @@ struct Handle {
   bool learned_active = false;  // still applied (the drift guard may switch it off)
   double drift_bound = 1e-3;
   double te_ref = 0.0, umax_ref = 0.0;
+  double umax_last = 0.0;  // max |u| at the start of the current guard interval
   bool te_ref_set = false;
   // state at the start of the current guard interval, restored when the
   // interval ends past the drift bound (or with a non-finite energy)
@@ -68,10 +69,13 @@ struct Handle {
 
 // steps between two checks of the learned correction's energy drift
 constexpr int kGuardSteps = 32;
-// the check also fails once max |u| exceeds this factor times its value when
-// the state was set: a mode growing at a few edges hardly moves the total
-// energy before it blows up
-constexpr double kUmaxGrowth = 1.5;
+// the check also fails when max |u| grows by more than this factor within one
+// interval, or exceeds kUmaxCap times its value when the state was set: a
+// mode growing at a few edges hardly moves the total energy before it blows
+// up.  Flows change max |u| far more slowly: 7.4 % per 256 steps at most in
+// case 5 (flow over a mountain), whose max |u| doubles over 15 days.
+constexpr double kUmaxStep = 1.1;
+constexpr double kUmaxCap = 3.0;
 
 #define CK(call)                                                                  \
   do {                                                                            \
@@ -356,12 +360,16 @@ int total_energy(Handle *H, double *te, double *umax) {
 bool guard_decide(Handle *H, double te, double umax) {
   if (!H->te_ref_set) {
     H->te_ref = te;
-    H->umax_ref = umax;
+    H->umax_ref = H->umax_last = umax;
     H->te_ref_set = true;
     return false;
   }
   const double drift = std::fabs(te - H->te_ref) / std::fabs(H->te_ref);
-  if (drift <= H->drift_bound && umax <= kUmaxGrowth * H->umax_ref) return false;
+  if (drift <= H->drift_bound && umax <= kUmaxStep * H->umax_last &&
+      umax <= kUmaxCap * H->umax_ref) {
+    H->umax_last = umax;
+    return false;
+  }
   H->learned_active = false;
   H->W32.learned = nullptr;
   if (H->graph) {

@@ -106,10 +106,11 @@ typedef struct imodel_swm_opts {
   size_t mlp_bytes;
   double drift_bound; /* relative total-energy drift above which the
                          learned correction is switched off (0 = 1e-3); it
-                         is also switched off once max |u| exceeds 1.5x its
-                         value when the state was set.  Checked every 32
-                         steps; the interval that failed is stepped again
-                         with the plain scheme                           */
+                         is also switched off when max |u| grows by more
+                         than 10 % within one check interval or exceeds 3x
+                         its value when the state was set.  Checked every
+                         32 steps; the interval that failed is stepped
+                         again with the plain scheme                     */
 } imodel_swm_opts;
 
 /* ---- diagnostics (swm.f90:293-322, :2686-2752, :3394-3440) ------------- */
