@@ -315,6 +315,12 @@ int flags_status(Handle *H, int f) {
     return set_error(H, IMODEL_SWM_EDIVZERO,
                      "division by zero in PV (|h_tr| < eps/1e5), as scalar_elem_divide stops");
   if (f & 2) return set_error(H, IMODEL_SWM_EBLOWUP, "state holds NaN or Inf");
+  // bits 8 and 16: a bounded wait of the learned-correction network kernel
+  // ran out (mlp.cu, mlp_pipe.cuh); the kernel returned without finishing
+  // its tiles, so the correction of that step is incomplete
+  if (f & (8 | 16))
+    return set_error(H, IMODEL_SWM_ECUDA,
+                     "the learned-correction kernel's pipeline gave up on a bounded wait");
   return IMODEL_SWM_OK;
 }
 
