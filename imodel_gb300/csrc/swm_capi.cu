@@ -61,6 +61,9 @@ struct Handle {
   // interval ends past the drift bound (or with a non-finite energy)
   float *ck_h = nullptr, *ck_u = nullptr;
   bool ck_fresh = false;  // ck holds yn (written by the page-locked load)
+  // the mesh gave ed%nr, which the diffusion terms' tangential gradient needs
+  bool dif_ok = false;
+  double *d_kt64 = nullptr;  // [nt] FP64 K_tr scratch of an FP32 handle
   // a second stream for the energy check, which runs beside the write-back
   // of the state in imodel_swm_step
   cudaStream_t side = nullptr;
@@ -559,7 +562,8 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
       (rc = upload(H, L.e_stw, &M.e_stw)) || (rc = upload(H, L.t_ed, &M.t_ed)) ||
       (rc = upload(H, L.t_v, &M.t_v)) || (rc = upload(H, L.t_lt, &M.t_lt)) ||
       (rc = upload(H, L.t_kite, &M.t_kite)) || (rc = upload(H, L.t_areag, &M.t_areag)) ||
-      (rc = upload(H, L.t_f, &M.t_f)))
+      (rc = upload(H, L.t_f, &M.t_f)) || (rc = upload(H, L.e_sgtg, &M.e_sgtg)) ||
+      (rc = upload(H, L.e_gtg32, &M.e_gtg32)))
     return rc;
   if (H->precision == IMODEL_SWM_FP32) {
     if ((rc = upload(H, L.c_div32, &M.c_div32)) || (rc = upload(H, L.c_kew32, &M.c_kew32)) ||
@@ -604,6 +608,7 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
   }
   const int32_t *cn2o = nullptr, *en2o = nullptr;
   if ((rc = upload(H, L.cell_n2o, &cn2o)) || (rc = upload(H, L.edge_n2o, &en2o))) return rc;
+  H->dif_ok = m->ed_nr != nullptr;
   H->d_cell_n2o = const_cast<int32_t *>(cn2o);
   H->d_edge_n2o = const_cast<int32_t *>(en2o);
   const int32_t *co2n = nullptr, *eo2n = nullptr;
@@ -654,6 +659,37 @@ void destroy(Handle *H) {
   delete H;
 }
 
+// the coefficients and work arrays of the (hyper)diffusion terms
+template <class T>
+int setup_diffusion(Handle *H, Work<T> &W, double k2, double k4) {
+  Diffusion<T> &D = W.dif;
+  D.k2 = k2 > 0;
+  D.k4 = k4 > 0;
+  D.on = D.k2 || D.k4;
+  if (!D.on) return IMODEL_SWM_OK;
+  int rc;
+  if (!D.kt && ((rc = dalloc(H, &D.kt, H->nt)) || (rc = dalloc(H, &D.coefdiv, H->nv)) ||
+                (rc = dalloc(H, &D.coefvort, H->nt)) || (rc = dalloc(H, &D.lap, H->ne)) ||
+                (rc = dalloc(H, &D.lap2, H->ne))))
+    return rc;
+  double *kt64 = nullptr;
+  float *kt32 = nullptr;
+  if (sizeof(T) == sizeof(double)) {
+    kt64 = reinterpret_cast<double *>(D.kt);
+  } else {
+    if (!H->d_kt64 && (rc = dalloc(H, &H->d_kt64, H->nt))) return rc;
+    kt64 = H->d_kt64;
+    kt32 = reinterpret_cast<float *>(D.kt);
+  }
+  // swm.f90:169-205, "const": K at the cells, hx2tr(K) at the triangles;
+  // hyperdiffusion applies the Laplacian twice with sqrt(K4) and
+  // sqrt(hx2tr(K4)), and then also replaces the Laplacian's coefficients
+  D.kc = static_cast<T>(D.k4 ? std::sqrt(k4) : k2);
+  launch_hx2tr_const(H->M, D.k4 ? k4 : k2, D.k4, kt64, kt32, H->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(H->stream));
+  return IMODEL_SWM_OK;
+}
 }  // namespace
 }  // namespace imodel
 
@@ -1053,12 +1089,33 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[6]) {
   return IMODEL_SWM_OK;
 }
 
+int imodel_swm_set_diffusion(void *handle, double k2, double k4) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H) return IMODEL_SWM_EINVAL;
+  if (H->nv == 0) return imodel::set_error(H, IMODEL_SWM_ESTATE, "handle was not created");
+  if (!(k2 >= 0) || !(k4 >= 0) || !std::isfinite(k2) || !std::isfinite(k4))
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "diffusion coefficients must be finite and >= 0");
+  if ((k2 > 0 || k4 > 0) && !H->dif_ok)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "the diffusion terms need the mesh's ed_nr");
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  const int rc = H->precision == IMODEL_SWM_FP64 ? imodel::setup_diffusion(H, H->W64, k2, k4)
+                                                 : imodel::setup_diffusion(H, H->W32, k2, k4);
+  if (rc) return rc;
+  if (H->graph) {
+    cudaGraphExecDestroy(H->graph);
+    H->graph = nullptr;
+  }
+  return IMODEL_SWM_OK;
+}
+
 int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count) {
   Handle *H = static_cast<Handle *>(handle);
   if (!H || !count || nsteps < 0) return IMODEL_SWM_EINVAL;
   const int fp32 = H->precision == IMODEL_SWM_FP32;
+  const bool on = fp32 ? H->W32.dif.on : H->W64.dif.on;
+  const bool k4 = fp32 ? H->W32.dif.k4 : H->W64.dif.k4;
   *count = static_cast<int64_t>(nsteps) * 4 *
-           imodel::launches_per_stage(fp32, fp32 ? H->W32.tune.variant : 0);
+           imodel::launches_per_stage(fp32, fp32 ? H->W32.tune.variant : 0, on ? (k4 ? 2 : 1) : 0);
   // the learned correction adds one network launch per step while it is on
   if (fp32 && H->W32.learned) *count += nsteps;
   return IMODEL_SWM_OK;

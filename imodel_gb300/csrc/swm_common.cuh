@@ -18,6 +18,8 @@ struct DevMesh {
   const int32_t *e_v, *e_sh;
   const double *e_leng, *e_dleng, *e_kew, *e_area;
   const float *e_grad32;
+  const double *e_sgtg;   // [ne] sign of grad_ed_tg (swm_layout.h)
+  const float *e_gtg32;   // [ne] sign / (edhx%leng erad)
   const int8_t *e_nst;
   const int32_t *e_stk;
   const double *e_stw;
@@ -60,6 +62,21 @@ struct Tune {
 
 struct LearnedDev;
 
+// Laplacian diffusion and hyperdiffusion of the momentum (diffusion_ed,
+// hyperdiffusion_ed, swm_operators.f90:855-975; coefficients swm.f90:169-205,
+// "const" branch).  lap = grad_ed(K div x) - grad_ed_tg(K_tr zeta(x)) for
+// x = u, and for x = lap with hyperdiffusion; the momentum tendency gains
+// + lap (K2 > 0) and - lap2 (K4 > 0), in that order.
+template <class T>
+struct Diffusion {
+  bool on = false, k2 = false, k4 = false;
+  T kc = T(0);              // coefficient at cells: K2, or sqrt(K4)
+  T *kt = nullptr;          // [nt] at triangles: hx2tr(K2), or sqrt(hx2tr(K4))
+  T *coefdiv = nullptr;     // [nv] K div x
+  T *coefvort = nullptr;    // [nt] K_tr zeta(x)
+  T *lap = nullptr, *lap2 = nullptr;  // [ne]
+};
+
 // Working fields of one handle, in the handle's precision T.
 template <class T>
 struct Work {
@@ -73,6 +90,7 @@ struct Work {
   T *bern;           // [nv] g (h + b) + K
   T *tend_h, *tend_u;   // tendency outputs (tendency-only evaluations)
   T *zflux;          // [6][nv] cell-centred PV flux of each cell edge (variants 1, 2)
+  Diffusion<T> dif;
   Tune tune;
   int *flags;        // bit 0: PV division by ~0
   T h_ref;           // FP32: h is stored as h - h_ref
@@ -106,9 +124,15 @@ int learned_prepare(const float *params_host, LearnedDev *L, cudaStream_t s);
 void learned_launch(const DevMesh &M, const LearnedDev &L, const float *hd, const float *u,
                     const float *q_tr, float h_ref, int gather_groups, int *err, cudaStream_t s);
 
-inline int launches_per_stage(int precision_fp32, int variant) {
-  return (precision_fp32 && variant >= 1) ? 3 : 4;
+inline int launches_per_stage(int precision_fp32, int variant, int dif_passes = 0) {
+  return ((precision_fp32 && variant >= 1) ? 3 : 4) + 2 * dif_passes;
 }
+// K_tr of a constant coefficient: scalar_hx2tr (kite-area weights, FP64),
+// then sqrt with take_sqrt (hyperdiffusion), into kt64 and, when not NULL,
+// its FP32 rounding kt32
+void launch_hx2tr_const(const DevMesh &M, double k, bool take_sqrt, double *kt64, float *kt32,
+                        cudaStream_t s);
+
 
 // reference order <-> device order, with precision conversion
 void launch_gather_in(int n, const int32_t *n2o, const double *src, double *dst, double shift,

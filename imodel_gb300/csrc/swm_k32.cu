@@ -73,7 +73,8 @@ __global__ void __launch_bounds__(512) k_edge32(DevMesh M, const float *__restri
                                                 float *__restrict__ acc,
                                                 float *__restrict__ yout,
                                                 float *__restrict__ tend, int stage, float dt,
-                                                int mom_on) {
+                                                int mom_on, const float *__restrict__ dif1,
+                                                const float *__restrict__ dif2) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const int ne = M.ne;
   if (e >= ne) return;
@@ -86,11 +87,55 @@ __global__ void __launch_bounds__(512) k_edge32(DevMesh M, const float *__restri
     q += __ldg(&M.e_stc32[s * ne + e]) * uh[k] * (qe + q_ed[k]);
   }
   float momeq = -g - q;
+  if (dif1) momeq += dif1[e];
+  if (dif2) momeq -= dif2[e];
   if (!mom_on) momeq = 0.0f;
   if (stage < 0)
     tend[e] = momeq;
   else
     yout[e] = rk_stage32(stage, momeq, yn[e], acc + e, dt);
+}
+
+// ---- diffusion and hyperdiffusion (diffusion_ed, swm_operators.f90:855-975)
+// coefdiv = K div x at the cells (blocks [0, nbc)), coefvort = K_tr zeta(x)
+// at the triangles (the blocks after), with the folded FP32 coefficients of
+// div_hx and rel_vort_tr
+__global__ void __launch_bounds__(256) k_difcv32(DevMesh M, const float *__restrict__ x,
+                                                 float kc, const float *__restrict__ kt,
+                                                 float *__restrict__ coefdiv,
+                                                 float *__restrict__ coefvort, int nbc) {
+  if (static_cast<int>(blockIdx.x) < nbc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nv = M.nv;
+    if (i >= nv) return;
+    const int n = M.c_nnb[i];
+    float d = 0.0f;
+    for (int j = 0; j < n; ++j) d += x[__ldg(&M.c_ed[j * nv + i])] * __ldg(&M.c_div32[j * nv + i]);
+    coefdiv[i] = kc * d;
+  } else {
+    const int t = (blockIdx.x - nbc) * blockDim.x + threadIdx.x;
+    if (t >= M.nt) return;
+    const int4 a = __ldg(&M.t_recA[t]), b = __ldg(&M.t_recB[t]);
+    const float4 c = __ldg(&M.t_recC[t]);
+    float z = __int_as_float(b.z) * x[a.x];
+    z += __int_as_float(b.w) * x[a.y];
+    z += c.x * x[a.z];
+    coefvort[t] = __ldg(&kt[t]) * z;
+  }
+}
+
+// lap = grad_ed(coefdiv) - grad_ed_tg(coefvort)
+__global__ void __launch_bounds__(256) k_diflap32(DevMesh M, const float *__restrict__ coefdiv,
+                                                  const float *__restrict__ coefvort,
+                                                  float *__restrict__ lap) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ne = M.ne;
+  if (e >= ne) return;
+  const float g = (coefdiv[__ldg(&M.e_v[ne + e])] - coefdiv[__ldg(&M.e_v[e])]) *
+                  __ldg(&M.e_grad32[e]);
+  const float gt = (coefvort[__ldg(&M.e_sh[ne + e])] - coefvort[__ldg(&M.e_sh[e])]) *
+                   __ldg(&M.e_gtg32[e]);
+  lap[e] = g - gt;
 }
 
 // ---- cell-centred TRSK (variant 1), bodies in swm_k32_body.cuh ------------
@@ -141,7 +186,9 @@ __global__ void __launch_bounds__(512) k_edge32v2(DevMesh M, const float *__rest
                                                   float *__restrict__ yout,
                                                   float *__restrict__ tend, int stage, float dt,
                                                   int mom_on, float erad,
-                                                  const float *__restrict__ corr) {
+                                                  const float *__restrict__ corr,
+                                                  const float *__restrict__ dif1,
+                                                  const float *__restrict__ dif2) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const int e0 = 2 * p;
   if (e0 >= M.ne) return;
@@ -155,6 +202,17 @@ __global__ void __launch_bounds__(512) k_edge32v2(DevMesh M, const float *__rest
       const float2 c = reinterpret_cast<const float2 *>(corr)[p];
       m0 += c.x;
       m1 += c.y;
+    }
+    // diffusion, then hyperdiffusion
+    if (dif1) {
+      const float2 d = reinterpret_cast<const float2 *>(dif1)[p];
+      m0 += d.x;
+      m1 += d.y;
+    }
+    if (dif2) {
+      const float2 d = reinterpret_cast<const float2 *>(dif2)[p];
+      m0 -= d.x;
+      m1 -= d.y;
     }
     if (!mom_on) m0 = m1 = 0.0f;
     if (stage < 0) {
@@ -170,7 +228,7 @@ __global__ void __launch_bounds__(512) k_edge32v2(DevMesh M, const float *__rest
     }
   } else {
     edge_body(M, e0, OneRun{}, __ldg(&M.e_vs2[e0]), bern, zflux, yn, acc, yout, tend, stage, dt,
-              mom_on, erad, corr);
+              mom_on, erad, corr, dif1, dif2);
   }
 }
 
@@ -184,6 +242,17 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
   const Tune &T = W.tune;
   const float grav = static_cast<float>(M.grav);
   if (ev) cudaEventRecord(ev[0], s);
+  const Diffusion<float> &D = W.dif;
+  if (D.on) {
+    const int nbc = nblocks(M.nv, 256), nbt = nblocks(M.nt, 256);
+    k_difcv32<<<nbc + nbt, 256, 0, s>>>(M, u_in, D.kc, D.kt, D.coefdiv, D.coefvort, nbc);
+    k_diflap32<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap);
+    if (D.k4) {
+      k_difcv32<<<nbc + nbt, 256, 0, s>>>(M, D.lap, D.kc, D.kt, D.coefdiv, D.coefvort, nbc);
+      k_diflap32<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap2);
+    }
+  }
+  const float *dif1 = D.k2 ? D.lap : nullptr, *dif2 = D.k4 ? D.lap2 : nullptr;
   if (T.variant == 2)
     k_tri32c<<<nblocks(M.nt, T.bs_tri), T.bs_tri, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ref,
                                                            W.pv_on, W.flags);
@@ -202,7 +271,7 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
     if (ev) cudaEventRecord(ev[3], s);
     k_edge32v2<<<nblocks((M.ne + 1) / 2, T.bs_edge), T.bs_edge, 0, s>>>(
         M, W.bern, W.zflux, W.yn_u, W.acc_u, u_out, W.tend_u, stage, dt, W.mom_on,
-        static_cast<float>(M.erad), W.learned ? W.learned->corr : nullptr);
+        static_cast<float>(M.erad), W.learned ? W.learned->corr : nullptr, dif1, dif2);
     if (ev) cudaEventRecord(ev[4], s);
     return;
   }
@@ -216,7 +285,7 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
   if (ev) cudaEventRecord(ev[3], s);
   k_edge32<<<nblocks(M.ne, T.bs_edge), T.bs_edge, 0, s>>>(M, W.bern, W.uh, W.q_ed, W.yn_u,
                                                            W.acc_u, u_out, W.tend_u, stage, dt,
-                                                           W.mom_on);
+                                                           W.mom_on, dif1, dif2);
   if (ev) cudaEventRecord(ev[4], s);
 }
 

@@ -284,7 +284,9 @@ __device__ __forceinline__ void edge_body(const DevMesh &M, int e, Ix ix, uint2 
                                           const float *__restrict__ yn, float *__restrict__ acc,
                                           float *__restrict__ yout, float *__restrict__ tend,
                                           int stage, float dt, int mom_on, float erad,
-                                          const float *__restrict__ corr = nullptr) {
+                                          const float *__restrict__ corr = nullptr,
+                                          const float *__restrict__ dif1 = nullptr,
+                                          const float *__restrict__ dif2 = nullptr) {
   const int c1 = static_cast<int>(w.x & 0x0FFFFFFFu), c2 = static_cast<int>(w.y & 0x0FFFFFFFu);
   const int s1 = static_cast<int>(w.x >> 28), s2 = static_cast<int>(w.y >> 28);
   const float g = __ldg(&M.e_grad32[e]);  // 1 / (l_e a)
@@ -293,6 +295,9 @@ __device__ __forceinline__ void edge_body(const DevMesh &M, int e, Ix ix, uint2 
   float momeq = -grad - q;
   // learned correction of the PV flux (frozen over the RK step)
   if (corr) momeq += corr[ix(e)];
+  // diffusion, then hyperdiffusion
+  if (dif1) momeq += dif1[ix(e)];
+  if (dif2) momeq -= dif2[ix(e)];
   if (!mom_on) momeq = 0.0f;
   if (stage < 0)
     tend[ix(e)] = momeq;

@@ -113,7 +113,9 @@ __global__ void __launch_bounds__(256) k_edge64(DevMesh M, const double *__restr
                                                 double *__restrict__ acc,
                                                 double *__restrict__ yout,
                                                 double *__restrict__ tend, int stage,
-                                                double dt, int mom_on) {
+                                                double dt, int mom_on,
+                                                const double *__restrict__ dif1,
+                                                const double *__restrict__ dif2) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const int ne = M.ne;
   if (e >= ne) return;
@@ -130,11 +132,74 @@ __global__ void __launch_bounds__(256) k_edge64(DevMesh M, const double *__restr
   }
   q = q / l;
   double momeq = -g - q;
+  // diffusion, then hyperdiffusion (swm.f90:2578-2589)
+  if (dif1) momeq = momeq + dif1[e];
+  if (dif2) momeq = momeq - dif2[e];
   if (!mom_on) momeq = 0.0;
   if (stage < 0)
     tend[e] = momeq;
   else
     yout[e] = rk_stage(stage, momeq, yn[e], acc + e, dt);
+}
+
+// diffusion_ed (swm_operators.f90:855-895), first half: coefdiv = K
+// div_hx(x) at the cells (blocks [0, nbc)), coefvort = K_tr rel_vort_tr(x)
+// at the triangles (the blocks after), HTC branches of div_hx (:613-661) and
+// rel_vort_tr (:780-827)
+__global__ void __launch_bounds__(256) k_difcv64(DevMesh M, const double *__restrict__ x,
+                                                 double kc, const double *__restrict__ kt,
+                                                 double *__restrict__ coefdiv,
+                                                 double *__restrict__ coefvort, int nbc) {
+  if (static_cast<int>(blockIdx.x) < nbc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nv = M.nv;
+    if (i >= nv) return;
+    const int n = M.c_nnb[i];
+    double d = 0.0;
+    for (int j = 0; j < n; ++j) d = d + x[M.c_ed[j * nv + i]] * M.c_sd[j * nv + i];
+    const double divx = d / M.c_areag[i] / M.erad;
+    coefdiv[i] = kc * divx;
+  } else {
+    const int t = (blockIdx.x - nbc) * blockDim.x + threadIdx.x;
+    const int nt = M.nt;
+    if (t >= nt) return;
+    double z = 0.0;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) z = z + x[M.t_ed[s * nt + t]] * M.t_lt[s * nt + t];
+    z = z / M.t_areag[t] / M.erad;
+    coefvort[t] = kt[t] * z;
+  }
+}
+
+// second half: lap = grad_ed(coefdiv) - grad_ed_tg(coefvort) (grad_ed
+// :511-548, grad_ed_tg :738-777, HTC)
+__global__ void __launch_bounds__(256) k_diflap64(DevMesh M, const double *__restrict__ coefdiv,
+                                                  const double *__restrict__ coefvort,
+                                                  double *__restrict__ lap) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ne = M.ne;
+  if (e >= ne) return;
+  double g = coefdiv[M.e_v[ne + e]] - coefdiv[M.e_v[e]];
+  g = g / M.e_leng[e] / M.erad;
+  double gt = M.e_sgtg[e] * (coefvort[M.e_sh[ne + e]] - coefvort[M.e_sh[e]]);
+  gt = gt / (M.e_dleng[e] * M.erad);
+  lap[e] = g - gt;
+}
+
+// scalar_hx2tr (:258-263) of a constant k, then sqrt for hyperdiffusion
+// (swm.f90:183-204)
+__global__ void k_hx2tr_const(DevMesh M, double k, int take_sqrt, double *__restrict__ kt64,
+                              float *__restrict__ kt32) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = M.nt;
+  if (t >= nt) return;
+  double f = 0.0;
+#pragma unroll
+  for (int s = 0; s < 3; ++s) f = f + M.t_kite[s * nt + t] * k;
+  f = f / M.t_areag[t];
+  if (take_sqrt) f = sqrt(f);
+  kt64[t] = f;
+  if (kt32) kt32[t] = static_cast<float>(f);
 }
 
 template <class T>
@@ -513,6 +578,16 @@ void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
                     const double *u_in, double *h_out, double *u_out, int stage, double dt,
                     cudaStream_t s, cudaEvent_t *ev) {
   if (ev) cudaEventRecord(ev[0], s);
+  const Diffusion<double> &D = W.dif;
+  if (D.on) {
+    const int nbc = nblocks(M.nv, 256), nbt = nblocks(M.nt, 256);
+    k_difcv64<<<nbc + nbt, 256, 0, s>>>(M, u_in, D.kc, D.kt, D.coefdiv, D.coefvort, nbc);
+    k_diflap64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap);
+    if (D.k4) {
+      k_difcv64<<<nbc + nbt, 256, 0, s>>>(M, D.lap, D.kc, D.kt, D.coefdiv, D.coefvort, nbc);
+      k_diflap64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap2);
+    }
+  }
   k_tri64<<<nblocks(M.nt, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.pv_on, W.flags);
   if (ev) cudaEventRecord(ev[1], s);
   k_edge_pre64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ed, W.uh, W.q_ed);
@@ -521,8 +596,14 @@ void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
                                                h_out, W.tend_h, stage, dt);
   if (ev) cudaEventRecord(ev[3], s);
   k_edge64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, W.bern, W.uh, W.q_ed, W.yn_u, W.acc_u, u_out,
-                                               W.tend_u, stage, dt, W.mom_on);
+                                               W.tend_u, stage, dt, W.mom_on,
+                                               D.k2 ? D.lap : nullptr, D.k4 ? D.lap2 : nullptr);
   if (ev) cudaEventRecord(ev[4], s);
+}
+
+void launch_hx2tr_const(const DevMesh &M, double k, bool take_sqrt, double *kt64, float *kt32,
+                        cudaStream_t s) {
+  k_hx2tr_const<<<nblocks(M.nt, 256), 256, 0, s>>>(M, k, take_sqrt ? 1 : 0, kt64, kt32);
 }
 
 void launch_gather_in(int n, const int32_t *n2o, const double *src, double *dst, double shift,

@@ -209,6 +209,8 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
   L.e_kew.resize(NE);
   L.e_area.resize(NE);
   L.e_grad32.resize(NE);
+  L.e_sgtg.resize(NE);
+  L.e_gtg32.resize(NE);
   L.e_nst.assign(NE, 0);
   L.e_stk.assign(kMaxSt * NE, 0);
   L.e_stw.assign(kMaxSt * NE, 0.0);
@@ -226,6 +228,33 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
     L.e_kew[i] = 0.25 * l * d;
     L.e_area[i] = l * d * 0.5;
     L.e_grad32[i] = static_cast<float>(1.0 / (l * m.erad));
+    L.e_sgtg[i] = 0.0;  // 0 without ed%nr: the diffusion terms are then refused
+    L.e_gtg32[i] = 0.0f;
+    if (m.ed_nr) {
+      // circumcentre directions of the edge's two triangles: the unit
+      // normal of the plane through the vertices, on their side of the
+      // origin (only the sign of nr . (c2 - c1) is used, and on a Delaunay
+      // mesh c2 - c1 runs along the Voronoi edge, parallel to nr)
+      double c[2][3];
+      for (int s = 0; s < 2; ++s) {
+        const int t = m.ed_sh[2 * static_cast<size_t>(e) + s] - 1;
+        const double *p[3];
+        for (int k = 0; k < 3; ++k) p[k] = m.v_p + 3 * static_cast<size_t>(m.tr_v[3 * static_cast<size_t>(t) + k] - 1);
+        const double a[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
+        const double b[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
+        double x[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+        const double side = x[0] * (p[0][0] + p[1][0] + p[2][0]) + x[1] * (p[0][1] + p[1][1] + p[2][1]) +
+                            x[2] * (p[0][2] + p[1][2] + p[2][2]);
+        const double nrm = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+        for (int k = 0; k < 3; ++k) c[s][k] = (side < 0 ? -x[k] : x[k]) / nrm;
+      }
+      const double *nr = m.ed_nr + 3 * static_cast<size_t>(e);
+      const double dot = nr[0] * (c[1][0] - c[0][0]) + nr[1] * (c[1][1] - c[0][1]) +
+                         nr[2] * (c[1][2] - c[0][2]);
+      const double sg = dot < 0 ? -1.0 : 1.0;  // dsign(1, x): +1 for x = +-0
+      L.e_sgtg[i] = sg;
+      L.e_gtg32[i] = static_cast<float>(sg / (d * m.erad));
+    }
     // TRSK stencil, coriolis_ed order: cell ed%v(1) then ed%v(2), each in
     // its ccw edge order, the edge's own slot (zero weight) left out.
     int ns = 0;

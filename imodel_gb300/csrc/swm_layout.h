@@ -66,6 +66,11 @@ struct Layout {
   std::vector<double> e_dleng;               // edhx%leng
   std::vector<double> e_kew;                 // 0.25*l*d (KE weight, FP64)
   std::vector<float> e_grad32;               // 1/(l*erad)
+  // grad_ed_tg (swm_operators.f90:738-777, HTC): sign of ed%nr . (c2 - c1)
+  // for the circumcentres c1, c2 of ed%sh(1), ed%sh(2), and the FP32 factor
+  // sign / (edhx%leng * erad); used by the (hyper)diffusion terms
+  std::vector<double> e_sgtg;
+  std::vector<float> e_gtg32;
   std::vector<int8_t> e_nst;                 // stencil length
   std::vector<int32_t> e_stk;                // [kMaxSt][ne] stencil edges
   std::vector<double> e_stw;                 // [kMaxSt][ne] trskw * signcor

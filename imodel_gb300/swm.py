@@ -211,6 +211,12 @@ class SWM:
     def advance(self, dt: float, nsteps: int):
         self._check(self.lib.imodel_swm_advance(self._handle, dt, nsteps))
 
+    def set_diffusion(self, k2: float = 0.0, k4: float = 0.0):
+        """Laplacian diffusion K2_max (m^2/s) and hyperdiffusion K4_max
+        (m^4/s) of the momentum, constant coefficients (swm.f90:169-205,
+        swm_operators.f90:855-975); 0 switches a term off."""
+        self._check(self.lib.imodel_swm_set_diffusion(self._handle, k2, k4))
+
     def diagnostics(self) -> dict:
         """sumf_areas + calc_energies + RMS divergence of the current state."""
         d = _capi.Diag()

@@ -188,6 +188,15 @@ int imodel_swm_advance(void *handle, double dt, int32_t nsteps);
 int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[6]);
 /* Applies a choice returned by imodel_swm_autotune (e.g. cached per grid). */
 int imodel_swm_set_tuning(void *handle, const int32_t choice[6]);
+/* Laplacian diffusion (K2_max) and hyperdiffusion (K4_max) of the momentum
+ * with constant coefficients ("const" branch of swm.f90:169-205), in m^2/s
+ * and m^4/s; 0 switches a term off.  The momentum tendency gains
+ * + grad(K div u) - grad_tg(K_tr zeta) (diffusion_ed,
+ * swm_operators.f90:855-895) and, with K4 > 0, minus the same operator
+ * applied twice with sqrt(K4) (hyperdiffusion_ed, :930-975; the Laplacian
+ * term then also uses sqrt(K4), as the reference's coefficients do).  Needs
+ * the mesh's ed_nr.  May be called at any time; applies from the next step. */
+int imodel_swm_set_diffusion(void *handle, double k2, double k4);
 /* Launches issued by one advance call for nsteps steps (kernels only). */
 int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count);
 /* Runs nsteps RK4 steps kernel by kernel (no graph) with CUDA events around

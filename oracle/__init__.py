@@ -61,6 +61,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_trsk_weights.argtypes = [ctypes.POINTER(Mesh), f64p]
         L.oracle_tc2.argtypes = [ctypes.POINTER(Mesh), f64p, f64p]
         L.oracle_field.argtypes = [vp, ctypes.c_int32, f64p]
+        L.oracle_set_diffusion.argtypes = [vp, ctypes.c_double, ctypes.c_double]
         _lib = L
     return _lib
 
@@ -78,7 +79,8 @@ FIELDS = {"h_ed": (0, "ne"), "uh": (1, "ne"), "eta": (2, "nt"), "h_tr": (3, "nt"
 class Oracle:
     """The reference's swm_tests state machine on the CPU, for one grid."""
 
-    def __init__(self, grid, testcase: int = 2, bt=None, nthreads: int = 0):
+    def __init__(self, grid, testcase: int = 2, bt=None, nthreads: int = 0, k2: float = 0.0,
+                 k4: float = 0.0):
         self.grid = grid
         self._mesh = grid.c_struct()
         self._bt = None if bt is None else np.ascontiguousarray(bt, dtype=np.float64)
@@ -86,6 +88,9 @@ class Oracle:
         self.nthreads = n
         self._h = lib().oracle_create(ctypes.byref(self._mesh), testcase,
                                       None if self._bt is None else _p(self._bt), n)
+        if k2 or k4:
+            if lib().oracle_set_diffusion(self._h, k2, k4):
+                raise ValueError("bad diffusion coefficients")
 
     def __del__(self):
         if getattr(self, "_h", None):

@@ -32,6 +32,11 @@ struct Oracle {
   std::vector<double> h_ed, uh, eta, h_tr, eta_ed, q_tr, q_ed, divuh, ke, hbt, ghbK, grad,
       uhq, divu, zeta, vhx;
   std::vector<double> massf[4], momf[4], h_tmp, u_tmp;
+  // diffusion_ed / hyperdiffusion_ed with constant coefficients
+  bool k2_on = false, k4_on = false;
+  double dif_hx = 0.0;                 // dif_coef_hx (constant)
+  std::vector<double> dif_tr, sgtg;    // dif_coef_tr [nt]; grad_ed_tg signcor [ne]
+  std::vector<double> coefdiv, coefvort, lapu, lap_lapu, div_lap, vort_lap;
 };
 
 #define I6(i, j) (static_cast<size_t>(i) * 6 + (j))
@@ -41,6 +46,29 @@ inline int getedindexonhx(const imodel_swm_mesh &m, int ed, int cell) {
   for (int i = 0; i < m.nnb[cell]; ++i)
     if (m.v_ed[I6(cell, i)] - 1 == ed) return i + 1;
   return 0;
+}
+
+// diffusion_ed (swm_operators.f90:855-895): coef*div and coef*vort
+// (scalar_elem_product), grad_ed of the first (:511-548, HTC), grad_ed_tg of
+// the second (:738-777, HTC), lap = difference
+void diffusion(Oracle &o, const double *div, const double *vort, double *lap) {
+  const imodel_swm_mesh &m = o.m;
+  const int nv = m.nv, ne = m.ne, nt = m.nt;
+  const double erad = m.erad;
+  const int nth = o.nthreads;
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int i = 0; i < nv; ++i) o.coefdiv[i] = o.dif_hx * div[i];
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int k = 0; k < nt; ++k) o.coefvort[k] = o.dif_tr[k] * vort[k];
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l) {
+    double g = o.coefdiv[m.ed_v[2 * l + 1] - 1] - o.coefdiv[m.ed_v[2 * l] - 1];
+    g = g / m.ed_leng[l] / erad;
+    const int k1 = m.ed_sh[2 * l] - 1, k2 = m.ed_sh[2 * l + 1] - 1;
+    double gt = o.sgtg[l] * (o.coefvort[k2] - o.coefvort[k1]);
+    gt = gt / (m.edhx_leng[l] * erad);
+    lap[l] = g - gt;
+  }
 }
 
 // tendency, swm.f90:2416-2598
@@ -220,6 +248,42 @@ int tendency(Oracle &o, const double *h, const double *u, double *masseq, double
     o.zeta[k] = z / m.tr_areag[k] / erad;
   }
 
+  // Diffusion (swm.f90:2578-2581), hyperdiffusion (:2586-2589)
+  if (o.k2_on || o.k4_on) {
+    // diffusion_ed (swm_operators.f90:855-895) of u, from divu and zeta
+    diffusion(o, o.divu.data(), o.zeta.data(), o.lapu.data());
+    if (o.k2_on) {
+#pragma omp parallel for schedule(static) num_threads(nth)
+      for (int l = 0; l < ne; ++l) momeq[l] = momeq[l] + o.lapu[l];
+    }
+    if (o.k4_on) {
+      // hyperdiffusion_ed (:930-975): div_hx and rel_vort_tr of lapu, then
+      // diffusion_ed of them
+#pragma omp parallel for schedule(static) num_threads(nth)
+      for (int i = 0; i < nv; ++i) {
+        double d = 0.0;
+        for (int j = 0; j < m.nnb[i]; ++j) {
+          int l = m.v_ed[I6(i, j)] - 1;
+          double signcor = static_cast<double>(m.hx_ttgout[I6(i, j)]);
+          d = d + signcor * o.lapu[l] * m.edhx_leng[l];
+        }
+        o.div_lap[i] = d / m.hx_areag[i] / erad;
+      }
+#pragma omp parallel for schedule(static) num_threads(nth)
+      for (int k = 0; k < nt; ++k) {
+        double z = 0.0;
+        for (int l = 0; l < 3; ++l) {
+          int ed = m.tr_ed[3 * k + l] - 1;
+          z = z + o.lapu[ed] * m.ed_leng[ed] * static_cast<double>(m.tr_tg[3 * k + l]);
+        }
+        o.vort_lap[k] = z / m.tr_areag[k] / erad;
+      }
+      diffusion(o, o.div_lap.data(), o.vort_lap.data(), o.lap_lapu.data());
+#pragma omp parallel for schedule(static) num_threads(nth)
+      for (int l = 0; l < ne; ++l) momeq[l] = momeq[l] - o.lap_lapu[l];
+    }
+  }
+
   if (o.testcase <= 1) {
     for (int l = 0; l < ne; ++l) momeq[l] = 0.0;
   }
@@ -325,6 +389,63 @@ void *oracle_create(const imodel_swm_mesh *m, int32_t testcase, const double *bt
 }
 
 void oracle_destroy(void *o) { delete static_cast<Oracle *>(o); }
+
+// coefficients as swm.f90:169-205 sets them for diffus = hyperdiffus =
+// "const"; the sign of grad_ed_tg from the triangles' circumcentres
+// (trcircumc: the unit normal of the vertices' plane, on their side)
+int oracle_set_diffusion(void *p, double k2, double k4) {
+  Oracle &o = *static_cast<Oracle *>(p);
+  const imodel_swm_mesh &m = o.m;
+  if (!(k2 >= 0) || !(k4 >= 0)) return IMODEL_SWM_EINVAL;
+  o.k2_on = k2 > 0;
+  o.k4_on = k4 > 0;
+  if (!o.k2_on && !o.k4_on) return IMODEL_SWM_OK;
+  if (!m.ed_nr || !m.v_p) return IMODEL_SWM_EINVAL;
+  const size_t nv = m.nv, ne = m.ne, nt = m.nt;
+  // scalar_hx2tr of the constant coefficient (:258-263)
+  const double kc = o.k4_on ? k4 : k2;
+  o.dif_tr.assign(nt, 0.0);
+  for (size_t k = 0; k < nt; ++k) {
+    double f = 0.0;
+    for (int i = 0; i < 3; ++i) f = f + m.tr_trhx_area[3 * k + i] * kc;
+    o.dif_tr[k] = f / m.tr_areag[k];
+  }
+  o.dif_hx = kc;
+  if (o.k4_on) {
+    o.dif_hx = std::sqrt(o.dif_hx);
+    for (size_t k = 0; k < nt; ++k) o.dif_tr[k] = std::sqrt(o.dif_tr[k]);
+  }
+  std::vector<double> cc(3 * nt);
+  for (size_t k = 0; k < nt; ++k) {
+    const double *p0 = m.v_p + 3 * static_cast<size_t>(m.tr_v[3 * k] - 1);
+    const double *p1 = m.v_p + 3 * static_cast<size_t>(m.tr_v[3 * k + 1] - 1);
+    const double *p2 = m.v_p + 3 * static_cast<size_t>(m.tr_v[3 * k + 2] - 1);
+    double a[3], b[3], x[3];
+    for (int i = 0; i < 3; ++i) {
+      a[i] = p1[i] - p0[i];
+      b[i] = p2[i] - p0[i];
+    }
+    x[0] = a[1] * b[2] - a[2] * b[1];
+    x[1] = a[2] * b[0] - a[0] * b[2];
+    x[2] = a[0] * b[1] - a[1] * b[0];
+    const double side = x[0] * (p0[0] + p1[0] + p2[0]) + x[1] * (p0[1] + p1[1] + p2[1]) +
+                        x[2] * (p0[2] + p1[2] + p2[2]);
+    const double n = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]) * (side < 0 ? -1.0 : 1.0);
+    for (int i = 0; i < 3; ++i) cc[3 * k + i] = x[i] / n;
+  }
+  o.sgtg.assign(ne, 0.0);
+  for (size_t l = 0; l < ne; ++l) {
+    const double *c1 = &cc[3 * static_cast<size_t>(m.ed_sh[2 * l] - 1)];
+    const double *c2 = &cc[3 * static_cast<size_t>(m.ed_sh[2 * l + 1] - 1)];
+    const double *nr = m.ed_nr + 3 * l;
+    const double d = nr[0] * (c2[0] - c1[0]) + nr[1] * (c2[1] - c1[1]) + nr[2] * (c2[2] - c1[2]);
+    o.sgtg[l] = std::copysign(1.0, d);
+  }
+  for (auto *v : {&o.lapu, &o.lap_lapu}) v->assign(ne, 0.0);
+  for (auto *v : {&o.coefvort, &o.vort_lap}) v->assign(nt, 0.0);
+  for (auto *v : {&o.coefdiv, &o.div_lap}) v->assign(nv, 0.0);
+  return IMODEL_SWM_OK;
+}
 
 int oracle_tendency(void *p, const double *h, const double *u, double *masseq, double *momeq) {
   return tendency(*static_cast<Oracle *>(p), h, u, masseq, momeq);

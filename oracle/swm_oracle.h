@@ -20,6 +20,9 @@ extern "C" {
 void *oracle_create(const imodel_swm_mesh *m, int32_t testcase, const double *bt,
                     int32_t nthreads);
 void oracle_destroy(void *o);
+/* Laplacian diffusion / hyperdiffusion with constant coefficients (m^2/s,
+ * m^4/s; 0 = off), swm.f90:169-205 and swm_operators.f90:855-975 */
+int oracle_set_diffusion(void *o, double k2, double k4);
 int oracle_tendency(void *o, const double *h, const double *u, double *masseq,
                     double *momeq);
 int oracle_rk4(void *o, const double *h, const double *u, double *h_new, double *u_new,
