@@ -1115,7 +1115,7 @@ int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count) {
   const bool on = fp32 ? H->W32.dif.on : H->W64.dif.on;
   const bool k4 = fp32 ? H->W32.dif.k4 : H->W64.dif.k4;
   *count = static_cast<int64_t>(nsteps) * 4 *
-           imodel::launches_per_stage(fp32, fp32 ? H->W32.tune.variant : 0, on ? (k4 ? 2 : 1) : 0);
+           imodel::launches_per_stage(fp32, fp32 ? H->W32.tune.variant : 0, on, k4);
   // the learned correction adds one network launch per step while it is on
   if (fp32 && H->W32.learned) *count += nsteps;
   return IMODEL_SWM_OK;

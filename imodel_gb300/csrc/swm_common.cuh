@@ -124,8 +124,14 @@ int learned_prepare(const float *params_host, LearnedDev *L, cudaStream_t s);
 void learned_launch(const DevMesh &M, const LearnedDev &L, const float *hd, const float *u,
                     const float *q_tr, float h_ref, int gather_groups, int *err, cudaStream_t s);
 
-inline int launches_per_stage(int precision_fp32, int variant, int dif_passes = 0) {
-  return ((precision_fp32 && variant >= 1) ? 3 : 4) + 2 * dif_passes;
+// kernel launches of one RK stage; with diffusion on, the edge gradients
+// (1 launch, 3 with hyperdiffusion) and, for FP32 variant 0, a first pass of
+// K div u and K_tr zeta (1 launch)
+inline int launches_per_stage(int precision_fp32, int variant, bool dif_on = false,
+                              bool dif_k4 = false) {
+  int n = (precision_fp32 && variant >= 1) ? 3 : 4;
+  if (dif_on) n += (dif_k4 ? 3 : 1) + ((precision_fp32 && variant == 0) ? 1 : 0);
+  return n;
 }
 // K_tr of a constant coefficient: scalar_hx2tr (kite-area weights, FP64),
 // then sqrt with take_sqrt (hyperdiffusion), into kt64 and, when not NULL,

@@ -14,10 +14,12 @@ namespace {
 __global__ void __launch_bounds__(512) k_tri32(DevMesh M, const float *__restrict__ hd,
                                                const float *__restrict__ u,
                                                float *__restrict__ q_tr, float h_ref,
-                                               int pv_on, int *flags) {
+                                               int pv_on, int *flags,
+                                               const float *__restrict__ kt,
+                                               float *__restrict__ coefvort) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= M.nt) return;
-  tri_body(M, t, OneRun{}, hd, u, q_tr, h_ref, pv_on, flags);
+  tri_body(M, t, OneRun{}, hd, u, q_tr, h_ref, pv_on, flags, kt, coefvort);
 }
 
 // h_e (deviation), flux F_e = u_e (h_ref + h_e), q_e
@@ -148,20 +150,24 @@ __global__ void __launch_bounds__(512) k_cell32v2(DevMesh M, const float *__rest
                                                   float *__restrict__ acc,
                                                   float *__restrict__ yout,
                                                   float *__restrict__ tend, int stage, float dt,
-                                                  float grav, float h_ref) {
+                                                  float grav, float h_ref, float kc,
+                                                  float *__restrict__ coefdiv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= M.nv) return;
-  cell_body(M, i, OneRun{}, hd, u, q_tr, bern, zflux, yn, acc, yout, tend, stage, dt, grav, h_ref);
+  cell_body(M, i, OneRun{}, hd, u, q_tr, bern, zflux, yn, acc, yout, tend, stage, dt, grav, h_ref,
+            kc, coefdiv);
 }
 
 // ---- variant 2: the triangle kernel on records with 16-bit indices -------
 __global__ void __launch_bounds__(512) k_tri32c(DevMesh M, const float *__restrict__ hd,
                                                 const float *__restrict__ u,
                                                 float *__restrict__ q_tr, float h_ref,
-                                                int pv_on, int *flags) {
+                                                int pv_on, int *flags,
+                                                const float *__restrict__ kt,
+                                                float *__restrict__ coefvort) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= M.nt) return;
-  tri_body16(M, t, hd, u, q_tr, h_ref, pv_on, flags);
+  tri_body16(M, t, hd, u, q_tr, h_ref, pv_on, flags, kt, coefvort);
 }
 
 // the momentum tendency of edge e (edge_body's arithmetic): -grad B -
@@ -243,22 +249,27 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
   const float grav = static_cast<float>(M.grav);
   if (ev) cudaEventRecord(ev[0], s);
   const Diffusion<float> &D = W.dif;
-  if (D.on) {
-    const int nbc = nblocks(M.nv, 256), nbt = nblocks(M.nt, 256);
-    k_difcv32<<<nbc + nbt, 256, 0, s>>>(M, u_in, D.kc, D.kt, D.coefdiv, D.coefvort, nbc);
+  const float *dif1 = D.k2 ? D.lap : nullptr, *dif2 = D.k4 ? D.lap2 : nullptr;
+  const int nbc = nblocks(M.nv, 256), nbt = nblocks(M.nt, 256);
+  // the edge gradients of the diffusion (and the second application of
+  // hyperdiffusion) once K div u and K_tr zeta are written
+  auto diffusion_tail = [&]() {
+    if (!D.on) return;
     k_diflap32<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap);
     if (D.k4) {
       k_difcv32<<<nbc + nbt, 256, 0, s>>>(M, D.lap, D.kc, D.kt, D.coefdiv, D.coefvort, nbc);
       k_diflap32<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap2);
     }
-  }
-  const float *dif1 = D.k2 ? D.lap : nullptr, *dif2 = D.k4 ? D.lap2 : nullptr;
+  };
+  if (T.variant == 0 && D.on)  // variant 0: K div u and K_tr zeta in their own pass
+    k_difcv32<<<nbc + nbt, 256, 0, s>>>(M, u_in, D.kc, D.kt, D.coefdiv, D.coefvort, nbc);
+  float *cvort = (T.variant >= 1 && D.on) ? D.coefvort : nullptr;
   if (T.variant == 2)
     k_tri32c<<<nblocks(M.nt, T.bs_tri), T.bs_tri, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ref,
-                                                           W.pv_on, W.flags);
+                                                           W.pv_on, W.flags, D.kt, cvort);
   else
     k_tri32<<<nblocks(M.nt, T.bs_tri), T.bs_tri, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ref,
-                                                          W.pv_on, W.flags);
+                                                          W.pv_on, W.flags, D.kt, cvort);
   if (T.variant >= 1) {
     if (ev) cudaEventRecord(ev[1], s);
     // learned correction: formed once per step from the first stage's state
@@ -267,7 +278,8 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
     if (ev) cudaEventRecord(ev[2], s);
     k_cell32v2<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
         M, h_in, u_in, W.q_tr, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
-        grav, W.h_ref);
+        grav, W.h_ref, D.kc, D.on ? D.coefdiv : nullptr);
+    diffusion_tail();
     if (ev) cudaEventRecord(ev[3], s);
     k_edge32v2<<<nblocks((M.ne + 1) / 2, T.bs_edge), T.bs_edge, 0, s>>>(
         M, W.bern, W.zflux, W.yn_u, W.acc_u, u_out, W.tend_u, stage, dt, W.mom_on,
@@ -282,6 +294,7 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
   k_cell32<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(M, h_in, u_in, W.uh, W.bern, W.yn_h,
                                                            W.acc_h, h_out, W.tend_h, stage, dt,
                                                            grav);
+  diffusion_tail();
   if (ev) cudaEventRecord(ev[3], s);
   k_edge32<<<nblocks(M.ne, T.bs_edge), T.bs_edge, 0, s>>>(M, W.bern, W.uh, W.q_ed, W.yn_u,
                                                            W.acc_u, u_out, W.tend_u, stage, dt,

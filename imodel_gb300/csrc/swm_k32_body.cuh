@@ -53,14 +53,20 @@ __device__ __forceinline__ void tri_core(int t, Ix ix, const int (&ed)[3], const
                                          const float (&circ)[3], const float (&kite)[3],
                                          float f, const float *__restrict__ hd,
                                          const float *__restrict__ u, float *__restrict__ q_tr,
-                                         float h_ref, int pv_on, int *flags) {
+                                         float h_ref, int pv_on, int *flags,
+                                         const float *__restrict__ kt = nullptr,
+                                         float *__restrict__ coefvort = nullptr) {
   float eta = f;
-  float ht = 0.0f;
+  float ht = 0.0f, z = 0.0f;
 #pragma unroll
   for (int s = 0; s < 3; ++s) {
-    eta += circ[s] * Ld::ld(u + ix(ed[s]));
+    const float us = Ld::ld(u + ix(ed[s]));
+    eta += circ[s] * us;
+    z += circ[s] * us;
     ht += kite[s] * Ld::ld(hd + ix(cv[s]));
   }
+  // with diffusion on: K_tr times the relative vorticity
+  if (coefvort) coefvort[ix(t)] = kt[t] * z;
   ht += h_ref;
   float q = 0.0f;
   if (pv_on) {
@@ -77,7 +83,9 @@ template <class Ix, class Ld = LdPlain>
 __device__ __forceinline__ void tri_body(const DevMesh &M, int t, Ix ix,
                                          const float *__restrict__ hd,
                                          const float *__restrict__ u, float *__restrict__ q_tr,
-                                         float h_ref, int pv_on, int *flags) {
+                                         float h_ref, int pv_on, int *flags,
+                                         const float *__restrict__ kt = nullptr,
+                                         float *__restrict__ coefvort = nullptr) {
   // three 16-byte records instead of 12 scalar streams (fewer load
   // instructions in flight per SM)
   const int4 a = __ldg(&M.t_recA[t]), b = __ldg(&M.t_recB[t]);
@@ -86,7 +94,7 @@ __device__ __forceinline__ void tri_body(const DevMesh &M, int t, Ix ix,
   const float circ[3] = {__int_as_float(b.z), __int_as_float(b.w), c.x};
   const float kite[3] = {c.y, c.z, c.w};
   tri_core<Ix, Ld>(t, ix, ed, cv, circ, kite, __ldg(&M.t_f32[t]), hd, u, q_tr, h_ref, pv_on,
-                   flags);
+                   flags, kt, coefvort);
 }
 
 // the same from 40-byte records with 16-bit indices (single runs): a warp of
@@ -97,7 +105,8 @@ __device__ __forceinline__ void tri_body(const DevMesh &M, int t, Ix ix,
 __device__ __forceinline__ void tri_body16(const DevMesh &M, int t, const float *__restrict__ hd,
                                            const float *__restrict__ u,
                                            float *__restrict__ q_tr, float h_ref, int pv_on,
-                                           int *flags) {
+                                           int *flags, const float *__restrict__ kt,
+                                           float *__restrict__ coefvort) {
   const int2 wb = __ldg(&M.t_wb[t >> 5]);
   const uint4 a = __ldg(&M.t_c16A[t]);
   const float4 b = __ldg(&M.t_c16B[t]);
@@ -122,7 +131,7 @@ __device__ __forceinline__ void tri_body16(const DevMesh &M, int t, const float 
   const float circ[3] = {__uint_as_float(a.w), b.x, b.y};
   const float kite[3] = {b.z, b.w, c.x};
   tri_core<OneRun, LdPlain>(t, OneRun{}, ed, cv, circ, kite, c.y, hd, u, q_tr, h_ref, pv_on,
-                            flags);
+                            flags, kt, coefvort);
 }
 
 // coriolis_ed (swm_operators.f90:1283-1308) sums, for edge e and each of its
@@ -162,11 +171,12 @@ __device__ __forceinline__ void cell_math(int i, uint32_t meta, const float (&R)
                                           float *__restrict__ bern, float *__restrict__ zflux,
                                           float *__restrict__ acc, float *__restrict__ yout,
                                           float *__restrict__ tend, int stage, float dt,
-                                          float grav, float h_ref, Ix ix = Ix{}) {
+                                          float grav, float h_ref, Ix ix = Ix{}, float kc = 0.0f,
+                                          float *__restrict__ coefdiv = nullptr) {
   const int n = static_cast<int>(meta & 7u);
   const unsigned tneg = meta >> 8;
   float G[6], qs[6];
-  float div = 0.0f, ke = 0.0f;
+  float div = 0.0f, ke = 0.0f, du = 0.0f;
   const float qlast = n == 6 ? qt[5] : (n == 5 ? qt[4] : (n == 4 ? qt[3] : qt[2]));
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
@@ -177,7 +187,10 @@ __device__ __forceinline__ void cell_math(int i, uint32_t meta, const float (&R)
     qs[j] = 0.5f * ((j == 0 ? qlast : qt[j - 1]) + qt[j]);
     div += G[j];
     ke += kd[j].x * (ue[j] * ue[j]);
+    du += ue[j] * kd[j].y;
   }
+  // with diffusion on: K times the divergence of u
+  if (coefdiv) coefdiv[ix(i)] = kc * (du * inva);
   bern[ix(i)] = grav * (hi + bt) + ke;
   float Z[6];
   if (n == 6)
@@ -219,7 +232,8 @@ __device__ __forceinline__ void cell_core(int i, Ix ix, uint32_t meta,
                                           float *__restrict__ bern, float *__restrict__ zflux,
                                           float *__restrict__ acc, float *__restrict__ yout,
                                           float *__restrict__ tend, int stage, float dt,
-                                          float grav, float h_ref) {
+                                          float grav, float h_ref, float kc = 0.0f,
+                                          float *__restrict__ coefdiv = nullptr) {
   float ue[6], hn[6], qt[6];
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
@@ -228,7 +242,7 @@ __device__ __forceinline__ void cell_core(int i, Ix ix, uint32_t meta,
     qt[j] = Ld::ld(q_tr + ix(tr[j]));
   }
   cell_math(i, meta, R, kd, ue, hn, qt, hi, bt, inva, ynv, accv, bern, zflux, acc, yout, tend,
-            stage, dt, grav, h_ref, ix);
+            stage, dt, grav, h_ref, ix, kc, coefdiv);
 }
 
 // the cell's own values from global memory
@@ -253,7 +267,8 @@ __device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
                                           float *__restrict__ bern, float *__restrict__ zflux,
                                           const float *__restrict__ yn, float *__restrict__ acc,
                                           float *__restrict__ yout, float *__restrict__ tend,
-                                          int stage, float dt, float grav, float h_ref) {
+                                          int stage, float dt, float grav, float h_ref,
+                                          float kc = 0.0f, float *__restrict__ coefdiv = nullptr) {
   const int nv = M.nv;
   const uint32_t meta = __ldg(&M.c_meta[i]);
   int ed[6], nb[6], tr[6];
@@ -273,7 +288,7 @@ __device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
   float hi, bt, inva, ynv, accv;
   cell_own<Ix, Ld>(M, i, ix, hd, yn, acc, stage, hi, bt, inva, ynv, accv);
   cell_core<Ix, Ld>(i, ix, meta, ed, nb, tr, R, kd, hi, bt, inva, ynv, accv, hd, u, q_tr, bern,
-                    zflux, acc, yout, tend, stage, dt, grav, h_ref);
+                    zflux, acc, yout, tend, stage, dt, grav, h_ref, kc, coefdiv);
 }
 
 // -grad B - (Z_c1 + Z_c2) / l_e and the momentum RK stage of edge e

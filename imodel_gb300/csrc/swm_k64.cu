@@ -33,7 +33,8 @@ __device__ __forceinline__ T rk_stage(int stage, T k, T yn, T *acc, T dt) {
 __global__ void __launch_bounds__(256) k_tri64(DevMesh M, const double *__restrict__ h,
                                                const double *__restrict__ u,
                                                double *__restrict__ q_tr, int pv_on,
-                                               int *flags) {
+                                               int *flags, const double *__restrict__ kt,
+                                               double *__restrict__ coefvort) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = M.nt;
   if (t >= nt) return;
@@ -42,6 +43,9 @@ __global__ void __launch_bounds__(256) k_tri64(DevMesh M, const double *__restri
   for (int s = 0; s < 3; ++s) e = e + u[M.t_ed[s * nt + t]] * M.t_lt[s * nt + t];
   const double A = M.t_areag[t];
   e = e / A / M.erad;
+  // with diffusion on: rel_vort_tr(u) (:780-827) is this sum before f is
+  // added; diffusion_ed's K_tr zeta
+  if (coefvort) coefvort[t] = kt[t] * e;
   e = e + M.t_f[t];
   double ht = 0.0;
 #pragma unroll
@@ -83,18 +87,22 @@ __global__ void __launch_bounds__(256) k_cell64(DevMesh M, const double *__restr
                                                 double *__restrict__ acc,
                                                 double *__restrict__ yout,
                                                 double *__restrict__ tend, int stage,
-                                                double dt) {
+                                                double dt, double kc,
+                                                double *__restrict__ coefdiv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int nv = M.nv;
   if (i >= nv) return;
   const int n = M.c_nnb[i];
-  double d = 0.0, k = 0.0;
+  double d = 0.0, k = 0.0, du = 0.0;
   for (int j = 0; j < n; ++j) {
     const int e = M.c_ed[j * nv + i];
     d = d + uh[e] * M.c_sd[j * nv + i];
     const double ue = u[e];
     k = k + M.e_kew[e] * (ue * ue);
+    if (coefdiv) du = du + ue * M.c_sd[j * nv + i];
   }
+  // with diffusion on: div_hx(u) (:613-661), diffusion_ed's K div u
+  if (coefdiv) coefdiv[i] = kc * (du / M.c_areag[i] / M.erad);
   const double divuh = d / M.c_areag[i] / M.erad;
   const double ke = k / M.c_cellarea[i];
   bern[i] = M.grav * (h[i] + M.c_bt[i]) + ke;
@@ -578,22 +586,26 @@ void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
                     const double *u_in, double *h_out, double *u_out, int stage, double dt,
                     cudaStream_t s, cudaEvent_t *ev) {
   if (ev) cudaEventRecord(ev[0], s);
+  // diffusion: the triangle and cell kernels also write K_tr zeta(u) and
+  // K div u; the edge gradients follow them (and, with hyperdiffusion, the
+  // second application), before the edge kernel
   const Diffusion<double> &D = W.dif;
-  if (D.on) {
-    const int nbc = nblocks(M.nv, 256), nbt = nblocks(M.nt, 256);
-    k_difcv64<<<nbc + nbt, 256, 0, s>>>(M, u_in, D.kc, D.kt, D.coefdiv, D.coefvort, nbc);
-    k_diflap64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap);
-    if (D.k4) {
-      k_difcv64<<<nbc + nbt, 256, 0, s>>>(M, D.lap, D.kc, D.kt, D.coefdiv, D.coefvort, nbc);
-      k_diflap64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap2);
-    }
-  }
-  k_tri64<<<nblocks(M.nt, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.pv_on, W.flags);
+  k_tri64<<<nblocks(M.nt, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.pv_on, W.flags, D.kt,
+                                              D.on ? D.coefvort : nullptr);
   if (ev) cudaEventRecord(ev[1], s);
   k_edge_pre64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ed, W.uh, W.q_ed);
   if (ev) cudaEventRecord(ev[2], s);
   k_cell64<<<nblocks(M.nv, 256), 256, 0, s>>>(M, h_in, u_in, W.uh, W.bern, W.yn_h, W.acc_h,
-                                               h_out, W.tend_h, stage, dt);
+                                               h_out, W.tend_h, stage, dt, D.kc,
+                                               D.on ? D.coefdiv : nullptr);
+  if (D.on) {
+    k_diflap64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap);
+    if (D.k4) {
+      const int nbc = nblocks(M.nv, 256), nbt = nblocks(M.nt, 256);
+      k_difcv64<<<nbc + nbt, 256, 0, s>>>(M, D.lap, D.kc, D.kt, D.coefdiv, D.coefvort, nbc);
+      k_diflap64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap2);
+    }
+  }
   if (ev) cudaEventRecord(ev[3], s);
   k_edge64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, W.bern, W.uh, W.q_ed, W.yn_u, W.acc_u, u_out,
                                                W.tend_u, stage, dt, W.mom_on,
