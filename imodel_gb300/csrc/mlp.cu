@@ -515,9 +515,7 @@ int learned_prepare(const float *params_host, LearnedDev *L, cudaStream_t s) {
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&L->sms, cudaDevAttrMultiProcessorCount, dev);
-  if (cudaFuncSetAttribute(pipe::k_mlp_pipe<pipe::EdgeTask, 1>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, pipe::SMEM) != cudaSuccess ||
-      cudaFuncSetAttribute(pipe::k_mlp_pipe<pipe::EdgeTask, 2>,
+  if (cudaFuncSetAttribute(pipe::k_mlp_pipe<pipe::EdgeTask, 2>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, pipe::SMEM) != cudaSuccess ||
       cudaFuncSetAttribute(pipe::k_mlp_pipe<pipe::EdgeTask, 3>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, pipe::SMEM) != cudaSuccess ||
@@ -538,9 +536,7 @@ void learned_launch(const DevMesh &M, const LearnedDev &L, const float *hd, cons
   const int64_t ntiles = (ne + TM - 1) / TM;
   const int nblk = static_cast<int>(std::min<int64_t>(ntiles, L.sms > 0 ? L.sms : 1));
   pipe::EdgeTask task{L.blocks, u, q_tr, hd, h_ref, L.corr};
-  if (gather_groups == 1)
-    pipe::k_mlp_pipe<pipe::EdgeTask, 1><<<nblk, pipe::THREADS, pipe::SMEM, s>>>(W, ne, task, err);
-  else if (gather_groups == 2)
+  if (gather_groups == 2)
     pipe::k_mlp_pipe<pipe::EdgeTask, 2><<<nblk, pipe::THREADS, pipe::SMEM, s>>>(W, ne, task, err);
   else if (gather_groups == 3)
     pipe::k_mlp_pipe<pipe::EdgeTask, 3><<<nblk, pipe::THREADS, pipe::SMEM, s>>>(W, ne, task, err);

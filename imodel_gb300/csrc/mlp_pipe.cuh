@@ -38,7 +38,7 @@ namespace pipe {
 using namespace tc05;
 
 // NGROUPS warp groups of 4 warps are split between gathering (NG) and the
-// epilogue (NGROUPS - NG); the split is a tuning choice (1 to 4 gather
+// epilogue (NGROUPS - NG); the split is a tuning choice (2, 3 or 4 gather
 // groups), the thread count and register budget are the same for all.
 constexpr int NGROUPS = 6, NSTAGE = 4, NSLOT = 6, NPF = 4;
 constexpr int N1 = 80, SLOTW = 80;  // layer-1 outputs: 64 hidden units, context, padding

@@ -1025,7 +1025,7 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
   // the learned-correction kernel's split of warps between gathering and
   // the epilogue
   if (H->learned_active)
-    for (int g = 1; g <= 4; ++g) {
+    for (int g = 2; g <= 4; ++g) {
       if (best.mlp_gather == g) continue;
       imodel::Tune t = best;
       t.mlp_gather = g;
@@ -1077,8 +1077,8 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[6]) {
   t.bs_cell = choice[3];
   t.bs_edge = choice[4];
   if (H->learned_on) {
-    if (choice[5] < 1 || choice[5] > 4)
-      return imodel::set_error(H, IMODEL_SWM_EINVAL, "gather groups of the network: 1 to 4");
+    if (choice[5] < 2 || choice[5] > 4)
+      return imodel::set_error(H, IMODEL_SWM_EINVAL, "gather groups of the network: 2, 3 or 4");
     t.mlp_gather = choice[5];
   }
   H->W32.tune = t;

@@ -57,7 +57,7 @@ struct DevMesh {
 struct Tune {
   int variant = 1;
   int bs_tri = 256, bs_pre = 256, bs_cell = 256, bs_edge = 256;
-  int mlp_gather = 2;  // gather groups of the learned-correction kernel (1..4)
+  int mlp_gather = 2;  // gather groups of the learned-correction kernel (2..4)
 };
 
 struct LearnedDev;

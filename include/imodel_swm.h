@@ -181,7 +181,7 @@ int imodel_swm_advance(void *handle, double dt, int32_t nsteps);
  * learned-correction kernel}; variant 0 uses the 10-entry edge stencil,
  * variant 1 the cell-centred TRSK sum, variant 2 the same with triangle
  * records holding 16-bit indices (bit-identical results); the last entry is
- * 1 to 4 with the
+ * 2, 3 or 4 with the
  * learned correction on (its kernel has 6 warp groups, the rest run the
  * epilogue) and 0 without it.  The FP64 path has a single configuration and
  * returns it. */
