@@ -82,3 +82,21 @@ def test_guard_rolls_back_the_interval(grid_at):
     hb, ub = b.ode_rk4(h, u, 900.0, 40)
     assert a.diagnostics()["learned_active"] == 0
     assert np.array_equal(ha, hb) and np.array_equal(ua, ub)
+
+
+def test_gather_group_splits_give_identical_steps(grid_at):
+    """The network kernel's split of warps between gathering and the
+    epilogue (2 to 4 gather groups) changes the schedule, not the
+    arithmetic: the steps agree bit for bit."""
+    from imodel_gb300 import learned as lrn
+    g = grid_at(5)
+    h, u = fields.balanced_state(g, lmax=24, seed=9)
+    p = lrn.trained_params()
+    assert p is not None
+    out = []
+    for ng in (2, 3, 4):
+        m = SWM(g, "fp32", learned_params=p)
+        m.set_tuning(variant=2, mlp_gather=ng)
+        out.append(m.ode_rk4(h, u, 450.0, 4))
+    for hh, uu in out[1:]:
+        assert np.array_equal(hh, out[0][0]) and np.array_equal(uu, out[0][1])
