@@ -269,18 +269,20 @@ def exp_large(args, pool):
 
 
 def exp_williamson(args, pool):
-    """Cases 1, 5 and 6 of the reference (imodel_gb300/testcases.py) at one
-    level (default 7), time steps scaled from level 5 (900, 300 and 225 s)
-    by the grid spacing.  Case 1 (cosine bell, one 12-day rotation) against
-    its initial state, the exact solution; cases 5 (15 days) and 6 (14 days)
-    FP32 and FP32 + learned against FP64, with mass and energy changes."""
+    """Cases 1, 5, 6 and 21 of the reference (imodel_gb300/testcases.py) at
+    one level (default 7), time steps scaled from level 5 (900, 300, 225 and
+    225 s) by the grid spacing.  Case 1 (cosine bell, one 12-day rotation)
+    against its initial state, the exact solution; cases 5 (15 days), 6 (14
+    days) and 21 (Galewsky jet, 6 days) FP32 and FP32 + learned against
+    FP64, with mass and energy changes."""
     from . import swm, testcases
     from .mesh import meshbuild
     lvl = args.level or 7
     g = meshbuild(lvl)
     scale = 2.0 ** (5 - lvl)
     out = {"level": lvl}
-    for case, dt5, days in ((1, 900.0, 12.0), (5, 300.0, 15.0), (6, 225.0, 14.0)):
+    for case, dt5, days in ((1, 900.0, 12.0), (5, 300.0, 15.0), (6, 225.0, 14.0),
+                            (21, 225.0, 6.0)):
         dt = dt5 * scale
         n = swm.ntime_for(days, dt)
         h, u, bt = testcases.initialize_fields(g, case)

@@ -2,7 +2,7 @@
 
 ``initialize_fields`` (src/swm.f90:1134-2380) fills h, u and the bottom
 topography for a test-case number.  Case 2 lives in ``swm.py``; this module
-adds the cases that need nothing but closed-form fields:
+adds:
 
 * 0 -- time-discretisation check: h = cos(lon) cos^2(lat), u = 0
   (swm.f90:1135-1146);
@@ -11,7 +11,10 @@ adds the cases that need nothing but closed-form fields:
 * 5 -- zonal flow over an isolated conical mountain (Williamson et al.
   1992, case 5; swm.f90:1327-1423);
 * 6 -- Rossby-Haurwitz wave of wavenumber 4 (Williamson case 6;
-  swm.f90:1426-1620, height ``h_tc6`` at :2392-2413).
+  swm.f90:1426-1620, height ``h_tc6`` at :2392-2413);
+* 21, 22, 23 -- the Galewsky et al. (2004) barotropic jet with its height
+  perturbation (21), without it (22, a steady balanced jet), and the
+  200 m/s jet with the perturbation (23) (swm.f90:1646-1810).
 
 Every field is returned in the grid's (reference) ordering; u is the normal
 component along ``ed%tg`` at the triangle-edge midpoint ``ed%c``, as the
@@ -199,11 +202,74 @@ def tc6_exact_tendency(grid: Grid):
     return masseq, momeq
 
 
-CASES = {0: tc0, 1: tc1, 2: None, 5: tc5, 6: tc6}
+# ---- cases 21, 22, 23 -----------------------------------------------------
+def galewsky(grid: Grid, testcase: int = 21):
+    """Galewsky, Scott and Polvani (2004) barotropic jet, as the reference sets
+    it up (swm.f90:1646-1810, after J. Thuburn): the zonal jet u(lat) =
+    umax/en exp(1 / ((lat - lat0)(lat - lat1))) between lat0 = pi/7 and
+    lat1 = pi/2 - lat0 (case 23: umax 200 m/s, else 80 m/s); the balanced
+    height tabulated on 4 floor(sqrt(nv)) latitude intervals by the trapezoid
+    rule on d(gh)/dlat = -a u (f + tan(lat) u / a), shifted to a 10 km mean
+    depth and interpolated to the cells (cubic Lagrange, linear in the end
+    intervals); cases 21 and 23 add the 120 m height bump at (0, pi/4)."""
+    u00 = 200.0 if testcase == 23 else 80.0
+    lat0 = PI / 7.0
+    lat1 = PI / 2.0 - lat0
+    en = np.exp(-4.0 / (lat1 - lat0) ** 2)
+    umen = u00 / en
+
+    def jet(lat):
+        den = (lat - lat0) * (lat - lat1)
+        with np.errstate(divide="ignore", over="ignore"):
+            return np.where(den < 0.0, umen * np.exp(1.0 / np.where(den < 0.0, den, -1.0)), 0.0)
+
+    # REAL(mesh%nv) is a default (single-precision) real
+    nygg = 4 * int(np.floor(np.sqrt(np.float32(grid.nv))))
+    dygg = PI / nygg
+    hgg = np.zeros(nygg + 1)
+    totarea = totvol = 0.0
+    for j in range(2, nygg + 1):
+        l1 = (j - 2) * dygg - PIO2
+        l2 = (j - 1) * dygg - PIO2
+        u1, u2 = float(jet(l1)), float(jet(l2))
+        u1 = u1 * (2.0 * OMEGA * np.sin(l1) + np.tan(l1) * u1 / ERAD)
+        u2 = u2 * (2.0 * OMEGA * np.sin(l2) + np.tan(l2) * u2 / ERAD)
+        hgg[j - 1] = hgg[j - 2] - ERAD * 0.5 * (u1 + u2) * dygg
+        totarea = totarea + np.cos(l2) * dygg
+        totvol = totvol + hgg[j - 1] * np.cos(l2) * dygg
+    hgg[nygg] = hgg[nygg - 1]
+    totvol = totvol / (totarea * GRAV)
+    hgg = (hgg + (1.0e4 - totvol) * GRAV) * GRAVI
+
+    l1 = grid.v_lat + PIO2
+    jy = np.floor(l1 / dygg).astype(np.int64) + 1          # 1-based interval
+    beta = (l1 - (jy - 1) * dygg) / dygg
+    g = lambda k: hgg[np.clip(k - 1, 0, nygg)]            # noqa: E731  hgg(k), 1-based
+    lin = (1.0 - beta) * g(jy) + beta * g(jy + 1)
+    c1 = -beta * (beta - 1.0) * (beta - 2.0) / 6.0
+    c2 = 0.5 * (beta + 1.0) * (beta - 1.0) * (beta - 2.0)
+    c3 = -0.5 * (beta + 1.0) * beta * (beta - 2.0)
+    c4 = (beta + 1.0) * beta * (beta - 1.0) / 6.0
+    cub = c1 * g(jy - 1) + c2 * g(jy) + c3 * g(jy + 1) + c4 * g(jy + 2)
+    h = np.where((jy == 1) | (jy == nygg), lin, cub)
+
+    u = _edge_u(grid, jet(grid.ed_c_lat), 0.0)
+
+    if testcase in (21, 23):
+        hpert, alpha, bet = 120.0, 1.0 / 3.0, 1.0 / 15.0
+        lat2 = 0.5 * PIO2
+        lon, _ = lonlat(grid.v_p)
+        h = h + hpert * np.cos(grid.v_lat) * np.exp(-(lon / alpha) ** 2) \
+            * np.exp(-((lat2 - grid.v_lat) / bet) ** 2)
+    return h, u, np.zeros(grid.nv)
+
+
+CASES = {0: tc0, 1: tc1, 2: None, 5: tc5, 6: tc6,
+         21: galewsky, 22: lambda g: galewsky(g, 22), 23: lambda g: galewsky(g, 23)}
 
 
 def initialize_fields(grid: Grid, testcase: int):
-    """(h[nv], u[ne], bt[nv]) of a test case (0, 1, 2, 5 or 6)."""
+    """(h[nv], u[ne], bt[nv]) of a test case (0, 1, 2, 5, 6, 21, 22, 23)."""
     if testcase == 2:
         h, u = initialize_fields_tc2(grid)
         return h, u, np.zeros(grid.nv)

@@ -1,4 +1,4 @@
-"""The step from the states of test cases 1, 5 and 6: the FP64 GPU path
+"""The step from the states of test cases 1, 5, 6 and 21: the FP64 GPU path
 equals the oracle bit for bit (case 5 with its topography, case 1 with the
 momentum equation and PV off), the FP32 path stays within FP32 round-off."""
 import numpy as np
@@ -11,7 +11,7 @@ from imodel_gb300.swm import SWM
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("case,dt", [(1, 900.0), (5, 600.0), (6, 600.0)])
+@pytest.mark.parametrize("case,dt", [(1, 900.0), (5, 600.0), (6, 600.0), (21, 600.0)])
 def test_fp64_equals_oracle(grid_at, case, dt):
     g = grid_at(5)
     h, u, bt = tc.initialize_fields(g, case)
@@ -21,7 +21,7 @@ def test_fp64_equals_oracle(grid_at, case, dt):
     assert np.array_equal(hg, hr) and np.array_equal(ug, ur)
 
 
-@pytest.mark.parametrize("case,dt", [(1, 900.0), (5, 600.0), (6, 600.0)])
+@pytest.mark.parametrize("case,dt", [(1, 900.0), (5, 600.0), (6, 600.0), (21, 600.0)])
 def test_fp32_close_to_oracle(grid_at, case, dt):
     g = grid_at(5)
     h, u, bt = tc.initialize_fields(g, case)

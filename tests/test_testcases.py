@@ -78,4 +78,28 @@ def test_case6_truncation_error_converges(grid_at):
 
 def test_unknown_case_is_refused(grid_at):
     with pytest.raises(ValueError):
-        tc.initialize_fields(grid_at(2), 21)
+        tc.initialize_fields(grid_at(2), 56)
+
+
+def test_galewsky_jet(grid_at):
+    """Cases 21-23: 10 km mean depth, the jet's maximum at 45 degrees, the
+    height bump only in 21 and 23, and case 22 (no bump) in balance: its
+    discrete momentum tendency is small beside the pressure gradient it
+    balances."""
+    g = grid_at(6)
+    A = g.hx_areag
+    h22, u22, _ = tc.initialize_fields(g, 22)
+    h21, u21, _ = tc.initialize_fields(g, 21)
+    h23, u23, _ = tc.initialize_fields(g, 23)
+    assert abs(np.sum(A * h22) / np.sum(A) - 1.0e4) < 1.0
+    assert 79.0 < np.abs(u22).max() <= 80.0 and 198.0 < np.abs(u23).max() <= 200.0
+    assert np.array_equal(u21, u22)
+    bump = h21 - h22
+    k = np.argmax(bump)
+    lon, _ = tc.lonlat(g.v_p)
+    assert 100.0 < bump.max() <= 120.0 and abs(lon[k]) < 0.1 and abs(g.v_lat[k] - np.pi / 4) < 0.1
+    oracle.build()
+    o = oracle.Oracle(g, 22)
+    m, mo = o.tendency(h22, u22)
+    grad = o.field("grad_ghbK")
+    assert np.sqrt(np.mean(mo ** 2)) < 0.05 * np.sqrt(np.mean(grad ** 2))
