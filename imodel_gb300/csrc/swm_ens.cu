@@ -50,8 +50,7 @@ inline FastDiv make_fastdiv(uint32_t d) {
 struct GridDev {
   DevMesh M;
   int members;
-  int groups;          // members / MPT: items per entity
-  FastDiv per_group;   // entity index = item / groups
+  FastDiv per_member;  // entity index = item / members
   float h_ref;
   int nsteps;  // steps this launch
   float dt;
@@ -108,12 +107,8 @@ __device__ __forceinline__ bool steps_now(int s, int n, int S) {
 }
 
 // MINB = 1: registers as the compiler likes them; MINB = 2: capped at 64 per
-// thread for twice the resident warps.  MPT: members per thread -- a thread
-// runs the per-member body for MPT consecutive members of one entity, so the
-// copies share the entity's geometry loads and put MPT members' loads in
-// flight at once (each member's arithmetic is the single-run code).  The
-// tuner times the variants.
-template <int MINB, int MPT>
+// thread for twice the resident warps (the tuner times both)
+template <int MINB>
 __global__ void __launch_bounds__(512, MINB) k_ensemble(EnsArgs A) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthr = gridDim.x * blockDim.x;
@@ -129,13 +124,11 @@ __global__ void __launch_bounds__(512, MINB) k_ensemble(EnsArgs A) {
         const GridDev &G = A.g[k];
         const float *hin = st == 0 ? G.yn_h : (st == 2 ? G.yb_h : G.ya_h);
         const float *uin = st == 0 ? G.yn_u : (st == 2 ? G.yb_u : G.ya_u);
-        const int n = G.M.nt * G.groups;
+        const int n = G.M.nt * G.members;
         for (int r = tid; r < n; r += nthr) {
-          const int t = G.per_group(r), m0 = (r - t * G.groups) * MPT;
-#pragma unroll
-          for (int j = 0; j < MPT; ++j)
-            tri_body<Member, LdL2>(G.M, t, Member{G.members, m0 + j}, hin, uin, G.q_tr, G.h_ref,
-                                   A.pv_on, A.flags);
+          const int t = G.per_member(r), m = r - t * G.members;
+          tri_body<Member, LdL2>(G.M, t, Member{G.members, m}, hin, uin, G.q_tr, G.h_ref,
+                                 A.pv_on, A.flags);
         }
       }
       if (!grid_barrier(A)) return;
@@ -146,14 +139,12 @@ __global__ void __launch_bounds__(512, MINB) k_ensemble(EnsArgs A) {
         const float *hin = st == 0 ? G.yn_h : (st == 2 ? G.yb_h : G.ya_h);
         const float *uin = st == 0 ? G.yn_u : (st == 2 ? G.yb_u : G.ya_u);
         float *hout = st == 0 ? G.ya_h : (st == 1 ? G.yb_h : (st == 2 ? G.ya_h : G.yn_h));
-        const int n = G.M.nv * G.groups;
+        const int n = G.M.nv * G.members;
         for (int r = tid; r < n; r += nthr) {
-          const int i = G.per_group(r), m0 = (r - i * G.groups) * MPT;
-#pragma unroll
-          for (int j = 0; j < MPT; ++j)
-            cell_body<Member, LdL2>(G.M, i, Member{G.members, m0 + j}, hin, uin, G.q_tr, G.bern,
-                                    G.zflux, G.yn_h, G.acc_h, hout, nullptr, st, G.dt,
-                                    static_cast<float>(G.M.grav), G.h_ref);
+          const int i = G.per_member(r), m = r - i * G.members;
+          cell_body<Member, LdL2>(G.M, i, Member{G.members, m}, hin, uin, G.q_tr, G.bern,
+                                  G.zflux, G.yn_h, G.acc_h, hout, nullptr, st, G.dt,
+                                  static_cast<float>(G.M.grav), G.h_ref);
         }
       }
       if (!grid_barrier(A)) return;
@@ -162,15 +153,12 @@ __global__ void __launch_bounds__(512, MINB) k_ensemble(EnsArgs A) {
         if (!on[k]) continue;
         const GridDev &G = A.g[k];
         float *uout = st == 0 ? G.ya_u : (st == 1 ? G.yb_u : (st == 2 ? G.ya_u : G.yn_u));
-        const int n = G.M.ne * G.groups;
+        const int n = G.M.ne * G.members;
         for (int r = tid; r < n; r += nthr) {
-          const int e = G.per_group(r), m0 = (r - e * G.groups) * MPT;
-          const uint2 w = __ldg(&G.M.e_vs2[e]);
-#pragma unroll
-          for (int j = 0; j < MPT; ++j)
-            edge_body<Member, LdL2>(G.M, e, Member{G.members, m0 + j}, w, G.bern, G.zflux,
-                                    G.yn_u, G.acc_u, uout, nullptr, st, G.dt, A.mom_on,
-                                    static_cast<float>(G.M.erad));
+          const int e = G.per_member(r), m = r - e * G.members;
+          edge_body<Member, LdL2>(G.M, e, Member{G.members, m}, __ldg(&G.M.e_vs2[e]), G.bern,
+                                  G.zflux, G.yn_u, G.acc_u, uout, nullptr, st, G.dt, A.mom_on,
+                                  static_cast<float>(G.M.erad));
         }
       }
       if (!grid_barrier(A)) return;
@@ -312,8 +300,7 @@ int ens_create(Ens *E, const imodel_swm_mesh *meshes, int ngrids, const int32_t 
     G.edge_n2o = const_cast<int32_t *>(en2o);
     GridDev &W = G.dev;
     W.members = G.members;
-    W.groups = G.members;
-    W.per_group = make_fastdiv(static_cast<uint32_t>(G.members));
+    W.per_member = make_fastdiv(static_cast<uint32_t>(G.members));
     float **bv[] = {&W.yn_h, &W.ya_h, &W.yb_h, &W.acc_h, &W.bern};
     for (float **b : bv)
       if ((rc = zalloc(E, b, static_cast<size_t>(L.nv) * M))) return rc;
@@ -342,24 +329,9 @@ int ens_flags(Ens *E) {
   return IMODEL_SWM_OK;
 }
 
-// variants: 0 = (MINB 1, 1 member per thread), 1 = (2, 1), 2 = (1, 2),
-// 3 = (1, 4)
-constexpr int kEnsVariants = 4;
-inline int ens_mpt(int variant) { return variant == 2 ? 2 : (variant == 3 ? 4 : 1); }
 inline const void *ens_kernel(int variant) {
-  switch (variant) {
-    case 1: return reinterpret_cast<const void *>(k_ensemble<2, 1>);
-    case 2: return reinterpret_cast<const void *>(k_ensemble<1, 2>);
-    case 3: return reinterpret_cast<const void *>(k_ensemble<1, 4>);
-    default: return reinterpret_cast<const void *>(k_ensemble<1, 1>);
-  }
-}
-// every grid's member count divisible by the variant's members per thread
-inline bool ens_variant_fits(const Ens *E, int variant) {
-  const int mpt = ens_mpt(variant);
-  for (int k = 0; k < E->ngrids; ++k)
-    if (E->g[k].members % mpt) return false;
-  return true;
+  return variant == 1 ? reinterpret_cast<const void *>(k_ensemble<2>)
+                      : reinterpret_cast<const void *>(k_ensemble<1>);
 }
 
 int ens_launch(Ens *E, const double *dt, const int32_t *nsteps, int block, int bps,
@@ -379,13 +351,6 @@ int ens_launch(Ens *E, const double *dt, const int32_t *nsteps, int block, int b
     S = std::max(S, static_cast<int>(nsteps[k]));
   }
   if (S == 0) return IMODEL_SWM_OK;
-  if (variant < 0 || variant >= kEnsVariants || !ens_variant_fits(E, variant))
-    return fail(E, IMODEL_SWM_EINVAL, "ensemble variant does not fit the member counts");
-  const int mpt = ens_mpt(variant);
-  for (int k = 0; k < E->ngrids; ++k) {
-    A.g[k].groups = A.g[k].members / mpt;
-    A.g[k].per_group = make_fastdiv(static_cast<uint32_t>(A.g[k].groups));
-  }
   A.macro_steps = S;
   A.bar_count = E->bar;
   A.bar_gen = E->bar + 1;
@@ -520,8 +485,7 @@ int imodel_swm_ensemble_tune(void *ens, const double *dt, int32_t nsteps, int32_
   int bb = E->block, bbps = E->blocks_per_sm, bv = E->variant;
   int rc = IMODEL_SWM_OK;
   const int blocks[3] = {128, 256, 512};
-  for (int v = 0; v < imodel::kEnsVariants && rc == IMODEL_SWM_OK; ++v) {
-    if (!imodel::ens_variant_fits(E, v)) continue;
+  for (int v = 0; v < 2 && rc == IMODEL_SWM_OK; ++v)
     for (int b : blocks) {
       int occ = 0;
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, imodel::ens_kernel(v), b, 0);
@@ -542,7 +506,6 @@ int imodel_swm_ensemble_tune(void *ens, const double *dt, int32_t nsteps, int32_
         if (bps == 1) break;
       }
     }
-  }
   for (size_t q = 0; q < bufs.size(); ++q)
     cudaMemcpyAsync(bufs[q], saved[q], sizes[q], cudaMemcpyDeviceToDevice, E->stream);
   cudaStreamSynchronize(E->stream);

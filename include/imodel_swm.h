@@ -232,9 +232,8 @@ int imodel_swm_ensemble_get_state(void *ens, int32_t grid, int32_t member, doubl
 int imodel_swm_ensemble_advance(void *ens, const double *dt, const int32_t *nsteps);
 /* Autotuner of the persistent launch: times nsteps steps per grid for each
  * kernel variant (0: registers unconstrained, 1: at most 64 registers per
- * thread for more resident warps, 2 and 3: 2 and 4 consecutive members of
- * an entity per thread, tried when every grid's member count is a multiple),
- * block size and blocks-per-SM count, keeps the fastest, restores the state.
+ * thread for more resident warps), block size and blocks-per-SM count, keeps
+ * the fastest, restores the state.
  * choice = {block size, blocks per SM, variant}. */
 int imodel_swm_ensemble_tune(void *ens, const double *dt, int32_t nsteps, int32_t choice[3]);
 int imodel_swm_ensemble_destroy(void *ens);
