@@ -309,7 +309,7 @@ MLP_FLOP_PER_EDGE = 2 * (24 * 64 + 64 * 64 + 64)
 # kernel at icos level 8 (128.0 MB for 655,362 cells), scaled to the
 # benchmark's level by the number of cells, as the traffic grows with them.
 # DRAM bytes per cell of one launch (ncu at icos level 8, an RK stage that
-# reads the accumulator; profiles/k_cell32v2_icosL8_fp32.md)
+# reads the accumulator)
 TRAFFIC_PER_CELL = {"k_cell32v2": 133.779e6 / 655362}
 
 
