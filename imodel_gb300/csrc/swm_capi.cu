@@ -632,6 +632,8 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
   CK(cudaMallocHost(&H->h_flags, sizeof(int)));
   CK(cudaMallocHost(&H->h_result, 16 * sizeof(double)));
   if (H->precision == IMODEL_SWM_FP64) {
+    if (o && o->learned)
+      return set_error(H, IMODEL_SWM_EINVAL, "the learned correction needs the FP32 path");
     if ((rc = alloc_work(H, H->W64))) return rc;
   } else {
     const float keep = H->W32.h_ref;
