@@ -153,14 +153,20 @@ def dist_env():
 
 
 class Dist:
-    def __init__(self, device):
+    """The ranks of a torchrun launch: one replica per GPU (NCCL); the
+    barrier around the timed region and the maximum of the ranks' times.
+    backend="gloo" runs the same on CPU tensors (multi-process tests)."""
+
+    def __init__(self, device, backend: str = "nccl"):
         self.ws, self.rank, self.local = dist_env()
         self.torch = None
+        self.dev = "cuda" if backend == "nccl" else "cpu"
         if self.ws > 1:
             import torch
             import torch.distributed as dist
-            torch.cuda.set_device(device)
-            dist.init_process_group("nccl")
+            if backend == "nccl":
+                torch.cuda.set_device(device)
+            dist.init_process_group(backend)
             self.torch, self.dist = torch, dist
 
     def barrier(self):
@@ -170,7 +176,7 @@ class Dist:
     def max(self, x: float) -> float:
         if self.torch is None:
             return x
-        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda")
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=self.dev)
         self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
         return float(t.item())
 
