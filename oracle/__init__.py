@@ -73,7 +73,8 @@ def _p(a):
 FIELDS = {"h_ed": (0, "ne"), "uh": (1, "ne"), "eta": (2, "nt"), "h_tr": (3, "nt"),
           "q_tr": (4, "nt"), "q_ed": (5, "ne"), "divuh": (6, "nv"), "ke": (7, "nv"),
           "ghbK": (8, "nv"), "grad_ghbK": (9, "ne"), "uhq_perp": (10, "ne"),
-          "divu": (11, "nv"), "zeta": (12, "nt"), "eta_ed": (13, "ne")}
+          "divu": (11, "nv"), "zeta": (12, "nt"), "eta_ed": (13, "ne"),
+          "lapu": (14, "ne"), "lap_lapu": (15, "ne")}
 
 
 class Oracle:

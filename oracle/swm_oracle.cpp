@@ -643,8 +643,11 @@ int oracle_field(void *p, int32_t which, double *out) {
     case 11: v = &o.divu; break;
     case 12: v = &o.zeta; break;
     case 13: v = &o.eta_ed; break;
+    case 14: v = &o.lapu; break;       // with diffusion on
+    case 15: v = &o.lap_lapu; break;   // with hyperdiffusion on
     default: return IMODEL_SWM_EINVAL;
   }
+  if (v->empty()) return IMODEL_SWM_ESTATE;
   std::memcpy(out, v->data(), v->size() * sizeof(double));
   return IMODEL_SWM_OK;
 }
