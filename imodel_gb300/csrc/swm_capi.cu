@@ -609,6 +609,12 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
   const int32_t *cn2o = nullptr, *en2o = nullptr;
   if ((rc = upload(H, L.cell_n2o, &cn2o)) || (rc = upload(H, L.edge_n2o, &en2o))) return rc;
   H->dif_ok = m->ed_nr != nullptr;
+  // the APVM reconstructions (FP64 step) read the edge, triangle and cell points
+  if (H->precision == IMODEL_SWM_FP64 && !L.t_c.empty()) {
+    if ((rc = upload(H, L.e_c, &M.e_c)) || (rc = upload(H, L.t_c, &M.t_c)) ||
+        (rc = upload(H, L.c_p, &M.c_p)))
+      return rc;
+  }
   H->d_cell_n2o = const_cast<int32_t *>(cn2o);
   H->d_edge_n2o = const_cast<int32_t *>(en2o);
   const int32_t *co2n = nullptr, *eo2n = nullptr;
@@ -690,6 +696,20 @@ int setup_diffusion(Handle *H, Work<T> &W, double k2, double k4) {
   launch_hx2tr_const(H->M, D.k4 ? k4 : k2, D.k4, kt64, kt32, H->stream);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(H->stream));
+  return IMODEL_SWM_OK;
+}
+// the anticipated potential vorticity method (apvm, swm_operators.f90:
+// 1465-1543) with parameter pvspar and the run's time step dt: the
+// tendency reads dt from the module (swm.f90:2558), not from the stage
+int setup_apvm(Handle *H, Work<double> &W, double pvspar, double dt) {
+  Apvm<double> &A = W.apvm;
+  A.on = pvspar > 0;
+  if (!A.on) return IMODEL_SWM_OK;
+  int rc;
+  if (!A.qg && ((rc = dalloc(H, &A.qg, 3 * static_cast<size_t>(H->nt))) ||
+                (rc = dalloc(H, &A.vhx, 3 * static_cast<size_t>(H->nv)))))
+    return rc;
+  A.coef = pvspar * dt;
   return IMODEL_SWM_OK;
 }
 }  // namespace
@@ -1110,6 +1130,28 @@ int imodel_swm_set_diffusion(void *handle, double k2, double k4) {
   return IMODEL_SWM_OK;
 }
 
+int imodel_swm_set_apvm(void *handle, double pvspar, double dt) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H) return IMODEL_SWM_EINVAL;
+  if (H->nv == 0) return imodel::set_error(H, IMODEL_SWM_ESTATE, "handle was not created");
+  if (!(pvspar >= 0) || !std::isfinite(pvspar))
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "pvspar must be finite and >= 0");
+  if (pvspar > 0 && (!(dt > 0) || !std::isfinite(dt)))
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "apvm needs a finite dt > 0");
+  if (pvspar > 0 && H->precision != IMODEL_SWM_FP64)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "apvm is built for the FP64 step only");
+  if (pvspar > 0 && !H->M.t_c)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "apvm needs the mesh's ed_nr and ed_c");
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  const int rc = imodel::setup_apvm(H, H->W64, pvspar, dt);
+  if (rc) return rc;
+  if (H->graph) {
+    cudaGraphExecDestroy(H->graph);
+    H->graph = nullptr;
+  }
+  return IMODEL_SWM_OK;
+}
+
 int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count) {
   Handle *H = static_cast<Handle *>(handle);
   if (!H || !count || nsteps < 0) return IMODEL_SWM_EINVAL;
@@ -1117,7 +1159,8 @@ int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count) {
   const bool on = fp32 ? H->W32.dif.on : H->W64.dif.on;
   const bool k4 = fp32 ? H->W32.dif.k4 : H->W64.dif.k4;
   *count = static_cast<int64_t>(nsteps) * 4 *
-           imodel::launches_per_stage(fp32, fp32 ? H->W32.tune.variant : 0, on, k4);
+           imodel::launches_per_stage(fp32, fp32 ? H->W32.tune.variant : 0, on, k4,
+                                      !fp32 && H->W64.apvm.on);
   // the learned correction adds one network launch per step while it is on
   if (fp32 && H->W32.learned) *count += nsteps;
   return IMODEL_SWM_OK;

@@ -46,6 +46,9 @@ struct DevMesh {
   const float4 *t_c16B;
   const float2 *t_c16C;
   const int2 *t_wb;
+  // points for the APVM reconstructions (FP64, [3][n], NULL without
+  // ed%nr): ed%c%p, tr%c%p (circumcentre), v%p
+  const double *e_c, *t_c, *c_p;
 };
 
 // Launch configuration of the FP32 stage kernels, chosen by the autotuner.
@@ -77,6 +80,16 @@ struct Diffusion {
   T *lap = nullptr, *lap2 = nullptr;  // [ne]
 };
 
+// The anticipated potential vorticity method, apvm (swm_operators.f90:
+// 1465-1543): q_ed -= pvspar dt (grad q(t1) + grad q(t2)) . (v(c1) + v(c2)).
+template <class T>
+struct Apvm {
+  bool on = false;
+  T coef = T(0);          // pvspar * dt
+  T *qg = nullptr;        // [3][nt] Perot reconstruction of grad_tr2ed(q_tr)
+  T *vhx = nullptr;       // [3][nv] Perot reconstruction of u at the cells
+};
+
 // Working fields of one handle, in the handle's precision T.
 template <class T>
 struct Work {
@@ -91,6 +104,7 @@ struct Work {
   T *tend_h, *tend_u;   // tendency outputs (tendency-only evaluations)
   T *zflux;          // [6][nv] cell-centred PV flux of each cell edge (variants 1, 2)
   Diffusion<T> dif;
+  Apvm<T> apvm;
   Tune tune;
   int *flags;        // bit 0: PV division by ~0
   T h_ref;           // FP32: h is stored as h - h_ref
@@ -128,9 +142,10 @@ void learned_launch(const DevMesh &M, const LearnedDev &L, const float *hd, cons
 // (1 launch, 3 with hyperdiffusion) and, for FP32 variant 0, a first pass of
 // K div u and K_tr zeta (1 launch)
 inline int launches_per_stage(int precision_fp32, int variant, bool dif_on = false,
-                              bool dif_k4 = false) {
+                              bool dif_k4 = false, bool apvm_on = false) {
   int n = (precision_fp32 && variant >= 1) ? 3 : 4;
   if (dif_on) n += (dif_k4 ? 3 : 1) + ((precision_fp32 && variant == 0) ? 1 : 0);
+  if (apvm_on) n += 1;
   return n;
 }
 // K_tr of a constant coefficient: scalar_hx2tr (kite-area weights, FP64),

@@ -61,20 +61,107 @@ __global__ void __launch_bounds__(256) k_tri64(DevMesh M, const double *__restri
   q_tr[t] = q;
 }
 
-// scalar_hx2ed (:89-97), scalar_elem_product (:1546), scalar_tr2ed (:124)
+// proj_vec_sphere (smeshpack.f90:4419-4433): v - (v . p) p / |p|
+__device__ __forceinline__ void proj_sphere(double &v0, double &v1, double &v2, double p0,
+                                            double p1, double p2) {
+  const double vp = v0 * p0 + v1 * p1 + v2 * p2;
+  const double np = sqrt(p0 * p0 + p1 * p1 + p2 * p2);
+  v0 = v0 - vp * p0 / np;
+  v1 = v1 - vp * p1 / np;
+  v2 = v2 - vp * p2 / np;
+}
+
+// The two reconstructions apvm (:1465-1543) reads.  Blocks [0, nbt): the
+// PV gradient at the triangles, vector_edtr2tr_perot (:408-452) of
+// grad_tr2ed(q_tr) (:1427-1463), each edge's gradient formed where it is
+// used; dsign(1, tr%nr) = -tr%tg (smeshpack.f90:853-859), the sign of t_lt.
+// The blocks after: the velocity at the cells, vector_edhx2hx_perot
+// (:454-509, HTC, hx%areag); ttgout is the sign of c_sd.
+__global__ void __launch_bounds__(256) k_apvm64(DevMesh M, const double *__restrict__ q_tr,
+                                                const double *__restrict__ u,
+                                                double *__restrict__ qg,
+                                                double *__restrict__ vhx, int nbt) {
+  const int ne = M.ne;
+  if (static_cast<int>(blockIdx.x) < nbt) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nt = M.nt;
+    if (t >= nt) return;
+    const double c0 = M.t_c[t], c1 = M.t_c[nt + t], c2 = M.t_c[2 * nt + t];
+    double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const int ed = M.t_ed[s * nt + t];
+      double g = M.e_sgtg[ed] * (q_tr[M.e_sh[ne + ed]] - q_tr[M.e_sh[ed]]);
+      g = g / M.e_dleng[ed] / M.erad;
+      const double sg = (M.t_lt[s * nt + t] < 0.0 ? 1.0 : -1.0) * g;
+      const double l = M.e_leng[ed];
+      v0 = v0 + sg * (M.e_c[ed] - c0) * l;
+      v1 = v1 + sg * (M.e_c[ne + ed] - c1) * l;
+      v2 = v2 + sg * (M.e_c[2 * ne + ed] - c2) * l;
+    }
+    const double A = M.t_areag[t];
+    v0 = v0 / A;
+    v1 = v1 / A;
+    v2 = v2 / A;
+    proj_sphere(v0, v1, v2, c0, c1, c2);
+    qg[t] = v0;
+    qg[nt + t] = v1;
+    qg[2 * nt + t] = v2;
+  } else {
+    const int i = (blockIdx.x - nbt) * blockDim.x + threadIdx.x;
+    const int nv = M.nv;
+    if (i >= nv) return;
+    const double p0 = M.c_p[i], p1 = M.c_p[nv + i], p2 = M.c_p[2 * nv + i];
+    double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+    const int n = M.c_nnb[i];
+    for (int j = 0; j < n; ++j) {
+      const int ed = M.c_ed[j * nv + i];
+      const double su = (M.c_sd[j * nv + i] < 0.0 ? -1.0 : 1.0) * u[ed];
+      const double d = M.e_dleng[ed];
+      v0 = v0 + su * (M.e_c[ed] - p0) * d;
+      v1 = v1 + su * (M.e_c[ne + ed] - p1) * d;
+      v2 = v2 + su * (M.e_c[2 * ne + ed] - p2) * d;
+    }
+    const double A = M.c_areag[i];
+    v0 = v0 / A;
+    v1 = v1 / A;
+    v2 = v2 / A;
+    proj_sphere(v0, v1, v2, p0, p1, p2);
+    vhx[i] = v0;
+    vhx[nv + i] = v1;
+    vhx[2 * nv + i] = v2;
+  }
+}
+
+// scalar_hx2ed (:89-97), scalar_elem_product (:1546), scalar_tr2ed (:124);
+// with qg != NULL the apvm correction of q_ed (:1495-1502), coef = pvspar dt
 __global__ void __launch_bounds__(256) k_edge_pre64(DevMesh M, const double *__restrict__ h,
                                                     const double *__restrict__ u,
                                                     const double *__restrict__ q_tr,
                                                     double *__restrict__ h_ed,
                                                     double *__restrict__ uh,
-                                                    double *__restrict__ q_ed) {
+                                                    double *__restrict__ q_ed,
+                                                    const double *__restrict__ qg,
+                                                    const double *__restrict__ vhx,
+                                                    double coef) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const int ne = M.ne;
   if (e >= ne) return;
   const double he = (h[M.e_v[e]] + h[M.e_v[ne + e]]) * 0.5;
   h_ed[e] = he;
   uh[e] = u[e] * he;
-  q_ed[e] = 0.5 * (q_tr[M.e_sh[e]] + q_tr[M.e_sh[ne + e]]);
+  const int t1 = M.e_sh[e], t2 = M.e_sh[ne + e];
+  double q = 0.5 * (q_tr[t1] + q_tr[t2]);
+  if (qg) {
+    const int nt = M.nt, nv = M.nv;
+    const int c1 = M.e_v[e], c2 = M.e_v[ne + e];
+    const double a0 = qg[t1] + qg[t2], a1 = qg[nt + t1] + qg[nt + t2],
+                 a2 = qg[2 * nt + t1] + qg[2 * nt + t2];
+    const double b0 = vhx[c1] + vhx[c2], b1 = vhx[nv + c1] + vhx[nv + c2],
+                 b2 = vhx[2 * nv + c1] + vhx[2 * nv + c2];
+    q = q - coef * (a0 * b0 + a1 * b1 + a2 * b2);
+  }
+  q_ed[e] = q;
 }
 
 // div_hx(uh) (:613-661), kinetic_energy_hx trsk (:1162-1171), Bernoulli
@@ -593,7 +680,13 @@ void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
   k_tri64<<<nblocks(M.nt, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.pv_on, W.flags, D.kt,
                                               D.on ? D.coefvort : nullptr);
   if (ev) cudaEventRecord(ev[1], s);
-  k_edge_pre64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ed, W.uh, W.q_ed);
+  const Apvm<double> &A = W.apvm;
+  if (A.on) {
+    const int nbt = nblocks(M.nt, 256);
+    k_apvm64<<<nbt + nblocks(M.nv, 256), 256, 0, s>>>(M, W.q_tr, u_in, A.qg, A.vhx, nbt);
+  }
+  k_edge_pre64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ed, W.uh, W.q_ed,
+                                                   A.on ? A.qg : nullptr, A.vhx, A.coef);
   if (ev) cudaEventRecord(ev[2], s);
   k_cell64<<<nblocks(M.nv, 256), 256, 0, s>>>(M, h_in, u_in, W.uh, W.bern, W.yn_h, W.acc_h,
                                                h_out, W.tend_h, stage, dt, D.kc,

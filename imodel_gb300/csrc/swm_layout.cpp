@@ -58,6 +58,23 @@ void sort_perm(std::vector<int32_t> &n2o, std::vector<int32_t> &o2n, const std::
   for (size_t i = 0; i < n; ++i) o2n[n2o[i]] = static_cast<int32_t>(i);
 }
 
+// tr%c%p of triangle t (0-based): the unit normal of the plane through its
+// vertices, on their side of the origin -- the direction of the spherical
+// circumcentre.  The oracle evaluates the same expressions.
+void circumcentre(const imodel_swm_mesh &m, int t, double c[3]) {
+  const double *p[3];
+  for (int k = 0; k < 3; ++k)
+    p[k] = m.v_p + 3 * static_cast<size_t>(m.tr_v[3 * static_cast<size_t>(t) + k] - 1);
+  const double a[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
+  const double b[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
+  const double x[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2],
+                       a[0] * b[1] - a[1] * b[0]};
+  const double side = x[0] * (p[0][0] + p[1][0] + p[2][0]) +
+                      x[1] * (p[0][1] + p[1][1] + p[2][1]) + x[2] * (p[0][2] + p[1][2] + p[2][2]);
+  const double nrm = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+  for (int k = 0; k < 3; ++k) c[k] = (side < 0 ? -x[k] : x[k]) / nrm;
+}
+
 }  // namespace
 
 std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) {
@@ -231,23 +248,11 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
     L.e_sgtg[i] = 0.0;  // 0 without ed%nr: the diffusion terms are then refused
     L.e_gtg32[i] = 0.0f;
     if (m.ed_nr) {
-      // circumcentre directions of the edge's two triangles: the unit
-      // normal of the plane through the vertices, on their side of the
-      // origin (only the sign of nr . (c2 - c1) is used, and on a Delaunay
-      // mesh c2 - c1 runs along the Voronoi edge, parallel to nr)
+      // circumcentre directions of the edge's two triangles (only the sign
+      // of nr . (c2 - c1) is used, and on a Delaunay mesh c2 - c1 runs
+      // along the Voronoi edge, parallel to nr)
       double c[2][3];
-      for (int s = 0; s < 2; ++s) {
-        const int t = m.ed_sh[2 * static_cast<size_t>(e) + s] - 1;
-        const double *p[3];
-        for (int k = 0; k < 3; ++k) p[k] = m.v_p + 3 * static_cast<size_t>(m.tr_v[3 * static_cast<size_t>(t) + k] - 1);
-        const double a[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
-        const double b[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
-        double x[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
-        const double side = x[0] * (p[0][0] + p[1][0] + p[2][0]) + x[1] * (p[0][1] + p[1][1] + p[2][1]) +
-                            x[2] * (p[0][2] + p[1][2] + p[2][2]);
-        const double nrm = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
-        for (int k = 0; k < 3; ++k) c[s][k] = (side < 0 ? -x[k] : x[k]) / nrm;
-      }
+      for (int s = 0; s < 2; ++s) circumcentre(m, m.ed_sh[2 * static_cast<size_t>(e) + s] - 1, c[s]);
       const double *nr = m.ed_nr + 3 * static_cast<size_t>(e);
       const double dot = nr[0] * (c[1][0] - c[0][0]) + nr[1] * (c[1][1] - c[0][1]) +
                          nr[2] * (c[1][2] - c[0][2]);
@@ -339,6 +344,22 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
       L.t_circ32[s * NT + i] = static_cast<float>(m.ed_leng[e] * tg / (A * m.erad));
       L.t_kite32[s * NT + i] = static_cast<float>(m.tr_trhx_area[3 * static_cast<size_t>(t) + s] / A);
     }
+  }
+
+  // --- APVM points (need ed%nr for grad_tr2ed's sign) --------------------
+  if (m.ed_nr && m.ed_c) {
+    L.t_c.resize(3 * NT);
+    L.e_c.resize(3 * NE);
+    L.c_p.resize(3 * NV);
+    for (int i = 0; i < nt; ++i) {
+      double c[3];
+      circumcentre(m, L.tri_n2o[i], c);
+      for (int k = 0; k < 3; ++k) L.t_c[k * NT + i] = c[k];
+    }
+    for (int i = 0; i < ne; ++i)
+      for (int k = 0; k < 3; ++k) L.e_c[k * NE + i] = m.ed_c[3 * static_cast<size_t>(L.edge_n2o[i]) + k];
+    for (int i = 0; i < nv; ++i)
+      for (int k = 0; k < 3; ++k) L.c_p[k * NV + i] = m.v_p[3 * static_cast<size_t>(L.cell_n2o[i]) + k];
   }
   L.t_recA.resize(4 * NT);
   L.t_recB.resize(4 * NT);

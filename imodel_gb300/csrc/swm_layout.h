@@ -82,6 +82,9 @@ struct Layout {
   std::vector<double> t_kite;                // tr%trhx_area
   std::vector<double> t_areag;               // [nt]
   std::vector<double> t_f;                   // [nt] 2*omega*sin(lat_c)
+  // APVM points, [3][n] in device order, empty without ed%nr: ed%c%p, the
+  // circumcentre direction of each triangle (circumcentre()), v%p
+  std::vector<double> e_c, t_c, c_p;
   // a triangle's FP32 stage inputs as three 16-byte records, [nt] each:
   //   A {edge 0, edge 1, edge 2, cell 0}  B {cell 1, cell 2, circ 0, circ 1}
   //   C {circ 2, kite 0, kite 1, kite 2}  (circ, kite: FP32 bit patterns)

@@ -217,6 +217,11 @@ class SWM:
         swm_operators.f90:855-975); 0 switches a term off."""
         self._check(self.lib.imodel_swm_set_diffusion(self._handle, k2, k4))
 
+    def set_apvm(self, pvspar: float, dt: float):
+        """pv_stab = "apvm" (swm_operators.f90:1465-1543) with parameter
+        pvspar (0 = off) and the run's time step dt; FP64 handles only."""
+        self._check(self.lib.imodel_swm_set_apvm(self._handle, pvspar, dt))
+
     def diagnostics(self) -> dict:
         """sumf_areas + calc_energies + RMS divergence of the current state."""
         d = _capi.Diag()

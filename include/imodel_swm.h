@@ -197,6 +197,16 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[6]);
  * term then also uses sqrt(K4), as the reference's coefficients do).  Needs
  * the mesh's ed_nr.  May be called at any time; applies from the next step. */
 int imodel_swm_set_diffusion(void *handle, double k2, double k4);
+/* PV stabilisation pv_stab = "apvm" (swm.par; swm_data.f90:548) with
+ * parameter pvspar (0 switches it off): before the Coriolis term each edge's
+ * PV becomes q_ed - pvspar dt (grad q(t1) + grad q(t2)) . (v(c1) + v(c2)),
+ * grad q the Perot reconstruction at the triangles of grad_tr2ed(q_tr) and v
+ * that of u at the cells (apvm, swm_operators.f90:1465-1543; called at
+ * swm.f90:2557-2559).  dt is the run's time step, which the reference's
+ * tendency reads from its module: pass the dt the steps use.  FP64 handles
+ * only (IMODEL_SWM_EINVAL for FP32); needs the mesh's ed_nr and ed_c.  May be
+ * called at any time; applies from the next step. */
+int imodel_swm_set_apvm(void *handle, double pvspar, double dt);
 /* Launches issued by one advance call for nsteps steps (kernels only). */
 int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count);
 /* Runs nsteps RK4 steps kernel by kernel (no graph) with CUDA events around

@@ -62,6 +62,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_tc2.argtypes = [ctypes.POINTER(Mesh), f64p, f64p]
         L.oracle_field.argtypes = [vp, ctypes.c_int32, f64p]
         L.oracle_set_diffusion.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+        L.oracle_set_apvm.argtypes = [vp, ctypes.c_double, ctypes.c_double]
         _lib = L
     return _lib
 
@@ -74,14 +75,14 @@ FIELDS = {"h_ed": (0, "ne"), "uh": (1, "ne"), "eta": (2, "nt"), "h_tr": (3, "nt"
           "q_tr": (4, "nt"), "q_ed": (5, "ne"), "divuh": (6, "nv"), "ke": (7, "nv"),
           "ghbK": (8, "nv"), "grad_ghbK": (9, "ne"), "uhq_perp": (10, "ne"),
           "divu": (11, "nv"), "zeta": (12, "nt"), "eta_ed": (13, "ne"),
-          "lapu": (14, "ne"), "lap_lapu": (15, "ne")}
+          "lapu": (14, "ne"), "lap_lapu": (15, "ne"), "q_grad_ed": (16, "ne")}
 
 
 class Oracle:
     """The reference's swm_tests state machine on the CPU, for one grid."""
 
     def __init__(self, grid, testcase: int = 2, bt=None, nthreads: int = 0, k2: float = 0.0,
-                 k4: float = 0.0):
+                 k4: float = 0.0, pvspar: float = 0.0, dt: float = 0.0):
         self.grid = grid
         self._mesh = grid.c_struct()
         self._bt = None if bt is None else np.ascontiguousarray(bt, dtype=np.float64)
@@ -92,6 +93,9 @@ class Oracle:
         if k2 or k4:
             if lib().oracle_set_diffusion(self._h, k2, k4):
                 raise ValueError("bad diffusion coefficients")
+        if pvspar:
+            if lib().oracle_set_apvm(self._h, pvspar, dt):
+                raise ValueError("bad apvm parameter or time step")
 
     def __del__(self):
         if getattr(self, "_h", None):

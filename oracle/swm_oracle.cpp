@@ -37,6 +37,11 @@ struct Oracle {
   double dif_hx = 0.0;                 // dif_coef_hx (constant)
   std::vector<double> dif_tr, sgtg;    // dif_coef_tr [nt]; grad_ed_tg signcor [ne]
   std::vector<double> coefdiv, coefvort, lapu, lap_lapu, div_lap, vort_lap;
+  // apvm (swm_operators.f90:1465-1543): pv_stab = "apvm", pvspar, the run's dt
+  bool apvm_on = false;
+  double pvspar = 0.0, apvm_dt = 0.0;
+  std::vector<double> cc;              // tr%c%p [nt][3]
+  std::vector<double> q_grad_ed, q_grad_tr;   // [ne], [nt][3]
 };
 
 #define I6(i, j) (static_cast<size_t>(i) * 6 + (j))
@@ -160,6 +165,51 @@ int tendency(Oracle &o, const double *h, const double *u, double *masseq, double
     o.vhx[3 * static_cast<size_t>(i)] = v0 - vp * p[0] / np;
     o.vhx[3 * static_cast<size_t>(i) + 1] = v1 - vp * p[1] / np;
     o.vhx[3 * static_cast<size_t>(i) + 2] = v2 - vp * p[2] / np;
+  }
+
+  if (o.apvm_on) {
+    // grad_tr2ed(q_tr -> q_grad_ed) (swm_operators.f90:1427-1463)
+#pragma omp parallel for schedule(static) num_threads(nth)
+    for (int l = 0; l < ne; ++l) {
+      const int k1 = m.ed_sh[2 * l] - 1, k2 = m.ed_sh[2 * l + 1] - 1;
+      o.q_grad_ed[l] = o.sgtg[l] * (o.q_tr[k2] - o.q_tr[k1]) / m.edhx_leng[l] / erad;
+    }
+    // vector_edtr2tr_perot(q_grad_ed -> q_grad_tr) (:408-452);
+    // dsign(1, tr%nr) with tr%nr = -tr%tg (smeshpack.f90:853-859)
+#pragma omp parallel for schedule(static) num_threads(nth)
+    for (int k = 0; k < nt; ++k) {
+      const double *c = &o.cc[3 * static_cast<size_t>(k)];
+      double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+      for (int l = 0; l < 3; ++l) {
+        const int ed = m.tr_ed[3 * k + l] - 1;
+        const double signcor = -static_cast<double>(m.tr_tg[3 * k + l]);
+        const double *ec = m.ed_c + 3 * static_cast<size_t>(ed);
+        const double s = signcor * o.q_grad_ed[ed];
+        v0 = v0 + s * (ec[0] - c[0]) * m.ed_leng[ed];
+        v1 = v1 + s * (ec[1] - c[1]) * m.ed_leng[ed];
+        v2 = v2 + s * (ec[2] - c[2]) * m.ed_leng[ed];
+      }
+      v0 = v0 / m.tr_areag[k];
+      v1 = v1 / m.tr_areag[k];
+      v2 = v2 / m.tr_areag[k];
+      // proj_vec_sphere (smeshpack.f90:4419-4433)
+      const double vp = v0 * c[0] + v1 * c[1] + v2 * c[2];
+      const double nc = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+      o.q_grad_tr[3 * static_cast<size_t>(k)] = v0 - vp * c[0] / nc;
+      o.q_grad_tr[3 * static_cast<size_t>(k) + 1] = v1 - vp * c[1] / nc;
+      o.q_grad_tr[3 * static_cast<size_t>(k) + 2] = v2 - vp * c[2] / nc;
+    }
+    // apvm: q_ed = q_ed - pvspar*dt*(g(sh1) + g(sh2)) . (v(v1) + v(v2))
+#pragma omp parallel for schedule(static) num_threads(nth)
+    for (int l = 0; l < ne; ++l) {
+      const double *g1 = &o.q_grad_tr[3 * static_cast<size_t>(m.ed_sh[2 * l] - 1)];
+      const double *g2 = &o.q_grad_tr[3 * static_cast<size_t>(m.ed_sh[2 * l + 1] - 1)];
+      const double *w1 = &o.vhx[3 * static_cast<size_t>(m.ed_v[2 * l] - 1)];
+      const double *w2 = &o.vhx[3 * static_cast<size_t>(m.ed_v[2 * l + 1] - 1)];
+      double d = 0.0;
+      for (int k = 0; k < 3; ++k) d = d + (g1[k] + g2[k]) * (w1[k] + w2[k]);
+      o.q_ed[l] = o.q_ed[l] - o.pvspar * o.apvm_dt * d;
+    }
   }
 
   // div_hx(uh -> divuh) (swm_operators.f90:613-661), HTC: signcor = ttgout
@@ -390,32 +440,14 @@ void *oracle_create(const imodel_swm_mesh *m, int32_t testcase, const double *bt
 
 void oracle_destroy(void *o) { delete static_cast<Oracle *>(o); }
 
-// coefficients as swm.f90:169-205 sets them for diffus = hyperdiffus =
-// "const"; the sign of grad_ed_tg from the triangles' circumcentres
-// (trcircumc: the unit normal of the vertices' plane, on their side)
-int oracle_set_diffusion(void *p, double k2, double k4) {
-  Oracle &o = *static_cast<Oracle *>(p);
+// tr%c%p as the unit normal of the triangle's vertex plane, on their side,
+// and grad_ed_tg's / grad_tr2ed's sign of ed%nr . (c2 - c1)
+void circumcentres_and_signs(Oracle &o) {
   const imodel_swm_mesh &m = o.m;
-  if (!(k2 >= 0) || !(k4 >= 0)) return IMODEL_SWM_EINVAL;
-  o.k2_on = k2 > 0;
-  o.k4_on = k4 > 0;
-  if (!o.k2_on && !o.k4_on) return IMODEL_SWM_OK;
-  if (!m.ed_nr || !m.v_p) return IMODEL_SWM_EINVAL;
-  const size_t nv = m.nv, ne = m.ne, nt = m.nt;
-  // scalar_hx2tr of the constant coefficient (:258-263)
-  const double kc = o.k4_on ? k4 : k2;
-  o.dif_tr.assign(nt, 0.0);
-  for (size_t k = 0; k < nt; ++k) {
-    double f = 0.0;
-    for (int i = 0; i < 3; ++i) f = f + m.tr_trhx_area[3 * k + i] * kc;
-    o.dif_tr[k] = f / m.tr_areag[k];
-  }
-  o.dif_hx = kc;
-  if (o.k4_on) {
-    o.dif_hx = std::sqrt(o.dif_hx);
-    for (size_t k = 0; k < nt; ++k) o.dif_tr[k] = std::sqrt(o.dif_tr[k]);
-  }
-  std::vector<double> cc(3 * nt);
+  const size_t ne = m.ne, nt = m.nt;
+  if (!o.sgtg.empty()) return;
+  std::vector<double> &cc = o.cc;
+  cc.assign(3 * nt, 0.0);
   for (size_t k = 0; k < nt; ++k) {
     const double *p0 = m.v_p + 3 * static_cast<size_t>(m.tr_v[3 * k] - 1);
     const double *p1 = m.v_p + 3 * static_cast<size_t>(m.tr_v[3 * k + 1] - 1);
@@ -441,9 +473,55 @@ int oracle_set_diffusion(void *p, double k2, double k4) {
     const double d = nr[0] * (c2[0] - c1[0]) + nr[1] * (c2[1] - c1[1]) + nr[2] * (c2[2] - c1[2]);
     o.sgtg[l] = std::copysign(1.0, d);
   }
+}
+
+// coefficients as swm.f90:169-205 sets them for diffus = hyperdiffus =
+// "const"; the sign of grad_ed_tg from the triangles' circumcentres
+// (trcircumc: the unit normal of the vertices' plane, on their side)
+int oracle_set_diffusion(void *p, double k2, double k4) {
+  Oracle &o = *static_cast<Oracle *>(p);
+  const imodel_swm_mesh &m = o.m;
+  if (!(k2 >= 0) || !(k4 >= 0)) return IMODEL_SWM_EINVAL;
+  o.k2_on = k2 > 0;
+  o.k4_on = k4 > 0;
+  if (!o.k2_on && !o.k4_on) return IMODEL_SWM_OK;
+  if (!m.ed_nr || !m.v_p) return IMODEL_SWM_EINVAL;
+  const size_t nv = m.nv, ne = m.ne, nt = m.nt;
+  // scalar_hx2tr of the constant coefficient (:258-263)
+  const double kc = o.k4_on ? k4 : k2;
+  o.dif_tr.assign(nt, 0.0);
+  for (size_t k = 0; k < nt; ++k) {
+    double f = 0.0;
+    for (int i = 0; i < 3; ++i) f = f + m.tr_trhx_area[3 * k + i] * kc;
+    o.dif_tr[k] = f / m.tr_areag[k];
+  }
+  o.dif_hx = kc;
+  if (o.k4_on) {
+    o.dif_hx = std::sqrt(o.dif_hx);
+    for (size_t k = 0; k < nt; ++k) o.dif_tr[k] = std::sqrt(o.dif_tr[k]);
+  }
+  circumcentres_and_signs(o);
   for (auto *v : {&o.lapu, &o.lap_lapu}) v->assign(ne, 0.0);
   for (auto *v : {&o.coefvort, &o.vort_lap}) v->assign(nt, 0.0);
   for (auto *v : {&o.coefdiv, &o.div_lap}) v->assign(nv, 0.0);
+  return IMODEL_SWM_OK;
+}
+
+int oracle_set_apvm(void *p, double pvspar, double dt) {
+  Oracle &o = *static_cast<Oracle *>(p);
+  const imodel_swm_mesh &m = o.m;
+  if (!(pvspar >= 0) || !std::isfinite(pvspar)) return IMODEL_SWM_EINVAL;
+  o.apvm_on = pvspar > 0;
+  if (!o.apvm_on) return IMODEL_SWM_OK;
+  if (!(dt > 0) || !std::isfinite(dt) || !m.ed_nr || !m.ed_c || !m.v_p) {
+    o.apvm_on = false;
+    return IMODEL_SWM_EINVAL;
+  }
+  o.pvspar = pvspar;
+  o.apvm_dt = dt;
+  circumcentres_and_signs(o);
+  o.q_grad_ed.assign(m.ne, 0.0);
+  o.q_grad_tr.assign(3 * static_cast<size_t>(m.nt), 0.0);
   return IMODEL_SWM_OK;
 }
 
@@ -645,6 +723,7 @@ int oracle_field(void *p, int32_t which, double *out) {
     case 13: v = &o.eta_ed; break;
     case 14: v = &o.lapu; break;       // with diffusion on
     case 15: v = &o.lap_lapu; break;   // with hyperdiffusion on
+    case 16: v = &o.q_grad_ed; break;  // with apvm on
     default: return IMODEL_SWM_EINVAL;
   }
   if (v->empty()) return IMODEL_SWM_ESTATE;

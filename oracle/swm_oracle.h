@@ -23,6 +23,9 @@ void oracle_destroy(void *o);
 /* Laplacian diffusion / hyperdiffusion with constant coefficients (m^2/s,
  * m^4/s; 0 = off), swm.f90:169-205 and swm_operators.f90:855-975 */
 int oracle_set_diffusion(void *o, double k2, double k4);
+/* pv_stab = "apvm" with parameter pvspar (0 = off) and the run's time step
+ * dt, swm_operators.f90:1465-1543 */
+int oracle_set_apvm(void *o, double pvspar, double dt);
 int oracle_tendency(void *o, const double *h, const double *u, double *masseq,
                     double *momeq);
 int oracle_rk4(void *o, const double *h, const double *u, double *h_new, double *u_new,

@@ -1,0 +1,74 @@
+"""The anticipated potential vorticity method on the GPU
+(imodel_swm_set_apvm): the FP64 step equals the oracle bit for bit,
+tendency and RK4 steps, alone and with diffusion; it costs one launch per
+stage; it switches off again; FP32 handles refuse it."""
+import numpy as np
+import pytest
+
+import oracle
+from imodel_gb300 import _capi, fields, swm
+from imodel_gb300.swm import SWM, SWMError
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("level,state", [(3, "tc2"), (4, "balanced"), (5, "balanced")])
+def test_fp64_equals_oracle(grid_at, level, state):
+    g = grid_at(level)
+    if state == "tc2":
+        h, u = swm.initialize_fields_tc2(g)
+    else:
+        h, u = fields.balanced_state(g, lmax=12, seed=11)
+    dt = 600.0
+    m = SWM(g, "fp64")
+    m.set_apvm(0.5, dt)
+    o = oracle.Oracle(g, 2, pvspar=0.5, dt=dt)
+    mg, ug = m.tendency(h, u)
+    mr, ur = o.tendency(h, u)
+    assert np.array_equal(mg, mr) and np.array_equal(ug, ur)
+    hg, ug = m.ode_rk4(h, u, dt, 8)
+    hr, ur = o.run(h, u, dt, 8)
+    assert np.array_equal(hg, hr) and np.array_equal(ug, ur)
+    # the correction changed the step
+    hp, up = oracle.Oracle(g, 2).run(h, u, dt, 8)
+    assert not np.array_equal(up, ur)
+
+
+def test_fp64_with_diffusion_equals_oracle(grid_at):
+    g = grid_at(4)
+    h, u = fields.balanced_state(g, lmax=12, seed=12)
+    m = SWM(g, "fp64")
+    m.set_apvm(1.0, 600.0)
+    m.set_diffusion(1.0e5, 1.0e13)
+    o = oracle.Oracle(g, 2, k2=1.0e5, k4=1.0e13, pvspar=1.0, dt=600.0)
+    hg, ug = m.ode_rk4(h, u, 600.0, 6)
+    hr, ur = o.run(h, u, 600.0, 6)
+    assert np.array_equal(hg, hr) and np.array_equal(ug, ur)
+
+
+def test_launch_count_and_switching_off(grid_at):
+    g = grid_at(4)
+    h, u = fields.balanced_state(g, lmax=12, seed=13)
+    a = SWM(g, "fp64")
+    n0 = a.launch_count(1)
+    a.set_apvm(0.5, 600.0)
+    assert a.launch_count(1) == n0 + 4
+    a.set_apvm(0.0, 600.0)
+    assert a.launch_count(1) == n0
+    ha, ua = a.ode_rk4(h, u, 600.0, 4)
+    hb, ub = SWM(g, "fp64").ode_rk4(h, u, 600.0, 4)
+    assert np.array_equal(ha, hb) and np.array_equal(ua, ub)
+
+
+def test_refusals(grid_at):
+    g = grid_at(3)
+    m = SWM(g, "fp32")
+    with pytest.raises(SWMError) as ei:
+        m.set_apvm(0.5, 600.0)
+    assert ei.value.code == _capi.EINVAL
+    m.set_apvm(0.0, 600.0)              # off is accepted everywhere
+    d = SWM(g, "fp64")
+    for pv, dt in ((-0.5, 600.0), (float("nan"), 600.0), (0.5, 0.0), (0.5, float("inf"))):
+        with pytest.raises(SWMError) as ei:
+            d.set_apvm(pv, dt)
+        assert ei.value.code == _capi.EINVAL
