@@ -615,6 +615,11 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
         (rc = upload(H, L.c_p, &M.c_p)))
       return rc;
   }
+  if (H->precision == IMODEL_SWM_FP32 && !L.t_apw32.empty()) {
+    if ((rc = upload(H, L.t_apw32, &M.t_apw32)) || (rc = upload(H, L.t_cc32, &M.t_cc32)) ||
+        (rc = upload(H, L.c_apw32, &M.c_apw32)) || (rc = upload(H, L.c_p32, &M.c_p32)))
+      return rc;
+  }
   H->d_cell_n2o = const_cast<int32_t *>(cn2o);
   H->d_edge_n2o = const_cast<int32_t *>(en2o);
   const int32_t *co2n = nullptr, *eo2n = nullptr;
@@ -701,15 +706,16 @@ int setup_diffusion(Handle *H, Work<T> &W, double k2, double k4) {
 // the anticipated potential vorticity method (apvm, swm_operators.f90:
 // 1465-1543) with parameter pvspar and the run's time step dt: the
 // tendency reads dt from the module (swm.f90:2558), not from the stage
-int setup_apvm(Handle *H, Work<double> &W, double pvspar, double dt) {
-  Apvm<double> &A = W.apvm;
+template <class T>
+int setup_apvm(Handle *H, Work<T> &W, double pvspar, double dt) {
+  Apvm<T> &A = W.apvm;
   A.on = pvspar > 0;
   if (!A.on) return IMODEL_SWM_OK;
   int rc;
   if (!A.qg && ((rc = dalloc(H, &A.qg, 3 * static_cast<size_t>(H->nt))) ||
                 (rc = dalloc(H, &A.vhx, 3 * static_cast<size_t>(H->nv)))))
     return rc;
-  A.coef = pvspar * dt;
+  A.coef = static_cast<T>(pvspar * dt);
   return IMODEL_SWM_OK;
 }
 }  // namespace
@@ -1017,7 +1023,8 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
   imodel::Tune best;
   float best_ms = 1e30f;
   // the learned correction is wired into the cell-centred variants only
-  for (int v = H->learned_on ? 1 : 0; v <= 2; ++v)
+  // and APVM into the edge pre-pass of variant 0
+  for (int v = H->learned_on ? 1 : 0; v <= (H->W32.apvm.on ? 0 : 2); ++v)
     for (int b : sizes) {
       imodel::Tune t;
       t.variant = v;
@@ -1092,6 +1099,8 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[6]) {
   if (H->learned_on && choice[0] == 0)
     return imodel::set_error(H, IMODEL_SWM_EINVAL,
                              "the learned correction runs with the cell-centred variants (1, 2) only");
+  if (H->W32.apvm.on && choice[0] != 0)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "apvm runs with variant 0 only");
   imodel::Tune t;
   t.variant = choice[0];
   t.bs_tri = choice[1];
@@ -1138,13 +1147,18 @@ int imodel_swm_set_apvm(void *handle, double pvspar, double dt) {
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "pvspar must be finite and >= 0");
   if (pvspar > 0 && (!(dt > 0) || !std::isfinite(dt)))
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "apvm needs a finite dt > 0");
-  if (pvspar > 0 && H->precision != IMODEL_SWM_FP64)
-    return imodel::set_error(H, IMODEL_SWM_EINVAL, "apvm is built for the FP64 step only");
-  if (pvspar > 0 && !H->M.t_c)
+  const bool fp32 = H->precision == IMODEL_SWM_FP32;
+  if (pvspar > 0 && !(fp32 ? H->M.t_apw32 != nullptr : H->M.t_c != nullptr))
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "apvm needs the mesh's ed_nr and ed_c");
+  if (pvspar > 0 && H->learned_on)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL,
+                             "apvm runs with FP32 variant 0, the learned correction with 1 and 2");
   if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
-  const int rc = imodel::setup_apvm(H, H->W64, pvspar, dt);
+  const int rc = fp32 ? imodel::setup_apvm(H, H->W32, pvspar, dt)
+                      : imodel::setup_apvm(H, H->W64, pvspar, dt);
   if (rc) return rc;
+  // FP32: the correction is applied in the edge pre-pass of variant 0
+  if (fp32 && pvspar > 0) H->W32.tune.variant = 0;
   if (H->graph) {
     cudaGraphExecDestroy(H->graph);
     H->graph = nullptr;
@@ -1160,7 +1174,7 @@ int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count) {
   const bool k4 = fp32 ? H->W32.dif.k4 : H->W64.dif.k4;
   *count = static_cast<int64_t>(nsteps) * 4 *
            imodel::launches_per_stage(fp32, fp32 ? H->W32.tune.variant : 0, on, k4,
-                                      !fp32 && H->W64.apvm.on);
+                                      fp32 ? H->W32.apvm.on : H->W64.apvm.on);
   // the learned correction adds one network launch per step while it is on
   if (fp32 && H->W32.learned) *count += nsteps;
   return IMODEL_SWM_OK;

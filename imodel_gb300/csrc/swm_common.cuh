@@ -49,6 +49,8 @@ struct DevMesh {
   // points for the APVM reconstructions (FP64, [3][n], NULL without
   // ed%nr): ed%c%p, tr%c%p (circumcentre), v%p
   const double *e_c, *t_c, *c_p;
+  // the FP32 step's APVM weights and projection vectors (swm_layout.h)
+  const float *t_apw32, *t_cc32, *c_apw32, *c_p32;
 };
 
 // Launch configuration of the FP32 stage kernels, chosen by the autotuner.

@@ -28,14 +28,81 @@ __global__ void __launch_bounds__(512) k_edge_pre32(DevMesh M, const float *__re
                                                     const float *__restrict__ q_tr,
                                                     float *__restrict__ h_ed,
                                                     float *__restrict__ uh,
-                                                    float *__restrict__ q_ed, float h_ref) {
+                                                    float *__restrict__ q_ed, float h_ref,
+                                                    const float *__restrict__ qg,
+                                                    const float *__restrict__ vhx,
+                                                    float coef) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const int ne = M.ne;
   if (e >= ne) return;
-  const float he = 0.5f * (hd[__ldg(&M.e_v[e])] + hd[__ldg(&M.e_v[ne + e])]);
+  const int c1 = __ldg(&M.e_v[e]), c2 = __ldg(&M.e_v[ne + e]);
+  const float he = 0.5f * (hd[c1] + hd[c2]);
   h_ed[e] = he;
   uh[e] = u[e] * (h_ref + he);
-  q_ed[e] = 0.5f * (q_tr[__ldg(&M.e_sh[e])] + q_tr[__ldg(&M.e_sh[ne + e])]);
+  const int t1 = __ldg(&M.e_sh[e]), t2 = __ldg(&M.e_sh[ne + e]);
+  float q = 0.5f * (q_tr[t1] + q_tr[t2]);
+  if (qg) {
+    // apvm (swm_operators.f90:1495-1502), coef = pvspar dt
+    const int nt = M.nt, nv = M.nv;
+    float d = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      d += (qg[k * nt + t1] + qg[k * nt + t2]) * (vhx[k * nv + c1] + vhx[k * nv + c2]);
+    q -= coef * d;
+  }
+  q_ed[e] = q;
+}
+
+// The two reconstructions apvm reads, in FP32 with the layout's weights
+// (swm_layout.h): blocks [0, nbt) the PV gradient at the triangles,
+// vector_edtr2tr_perot (:408-452) of grad_tr2ed(q_tr) (:1427-1463); the
+// blocks after the velocity at the cells, vector_edhx2hx_perot (:454-509);
+// each then projected on the tangent plane of its unit point.
+__global__ void __launch_bounds__(256) k_apvm32(DevMesh M, const float *__restrict__ q_tr,
+                                                const float *__restrict__ u,
+                                                float *__restrict__ qg,
+                                                float *__restrict__ vhx, int nbt) {
+  const int ne = M.ne;
+  float v[3] = {0.0f, 0.0f, 0.0f}, p[3];
+  int n, i, stride;
+  float *out;
+  if (static_cast<int>(blockIdx.x) < nbt) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nt = M.nt;
+    if (t >= nt) return;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const int ed = __ldg(&M.t_ed[s * nt + t]);
+      const float g = __ldg(&M.e_gtg32[ed]) *
+                      (q_tr[__ldg(&M.e_sh[ne + ed])] - q_tr[__ldg(&M.e_sh[ed])]);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) v[k] = fmaf(g, __ldg(&M.t_apw32[(3 * s + k) * nt + t]), v[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) p[k] = __ldg(&M.t_cc32[k * nt + t]);
+    i = t;
+    stride = nt;
+    out = qg;
+  } else {
+    const int c = (blockIdx.x - nbt) * blockDim.x + threadIdx.x;
+    const int nv = M.nv;
+    if (c >= nv) return;
+    n = M.c_nnb[c];
+    for (int j = 0; j < n; ++j) {
+      const float ue = u[__ldg(&M.c_ed[j * nv + c])];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) v[k] = fmaf(ue, __ldg(&M.c_apw32[(3 * j + k) * nv + c]), v[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) p[k] = __ldg(&M.c_p32[k * nv + c]);
+    i = c;
+    stride = nv;
+    out = vhx;
+  }
+  // proj_vec_sphere (smeshpack.f90:4419-4433) with |p| = 1
+  const float vp = v[0] * p[0] + v[1] * p[1] + v[2] * p[2];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) out[k * stride + i] = v[k] - vp * p[k];
 }
 
 // -div F, K, Bernoulli potential g (h - h_ref + b) + K, mass RK stage
@@ -288,8 +355,15 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
     return;
   }
   if (ev) cudaEventRecord(ev[1], s);
+  const Apvm<float> &A = W.apvm;
+  if (A.on) {
+    const int nbt = nblocks(M.nt, 256);
+    k_apvm32<<<nbt + nblocks(M.nv, 256), 256, 0, s>>>(M, W.q_tr, u_in, A.qg, A.vhx, nbt);
+  }
   k_edge_pre32<<<nblocks(M.ne, T.bs_pre), T.bs_pre, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ed, W.uh,
-                                                             W.q_ed, W.h_ref);
+                                                             W.q_ed, W.h_ref,
+                                                             A.on ? A.qg : nullptr, A.vhx,
+                                                             A.coef);
   if (ev) cudaEventRecord(ev[2], s);
   k_cell32<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(M, h_in, u_in, W.uh, W.bern, W.yn_h,
                                                            W.acc_h, h_out, W.tend_h, stage, dt,

@@ -360,6 +360,34 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
       for (int k = 0; k < 3; ++k) L.e_c[k * NE + i] = m.ed_c[3 * static_cast<size_t>(L.edge_n2o[i]) + k];
     for (int i = 0; i < nv; ++i)
       for (int k = 0; k < 3; ++k) L.c_p[k * NV + i] = m.v_p[3 * static_cast<size_t>(L.cell_n2o[i]) + k];
+    L.t_apw32.assign(9 * NT, 0.0f);
+    L.t_cc32.assign(3 * NT, 0.0f);
+    for (int i = 0; i < nt; ++i) {
+      const int t = L.tri_n2o[i];
+      for (int s = 0; s < 3; ++s) {
+        const int e = m.tr_ed[3 * static_cast<size_t>(t) + s] - 1;
+        const double sg = -static_cast<double>(m.tr_tg[3 * static_cast<size_t>(t) + s]);
+        for (int k = 0; k < 3; ++k) {
+          const double d = m.ed_c[3 * static_cast<size_t>(e) + k] - L.t_c[k * NT + i];
+          L.t_apw32[(3 * s + k) * NT + i] = static_cast<float>(sg * d * m.ed_leng[e] / m.tr_areag[t]);
+        }
+      }
+      for (int k = 0; k < 3; ++k) L.t_cc32[k * NT + i] = static_cast<float>(L.t_c[k * NT + i]);
+    }
+    L.c_apw32.assign(18 * NV, 0.0f);
+    L.c_p32.assign(3 * NV, 0.0f);
+    for (int i = 0; i < nv; ++i) {
+      const int c = L.cell_n2o[i];
+      for (int j = 0; j < m.nnb[c]; ++j) {
+        const int e = m.v_ed[6 * static_cast<size_t>(c) + j] - 1;
+        const double sg = static_cast<double>(m.hx_ttgout[6 * static_cast<size_t>(c) + j]);
+        for (int k = 0; k < 3; ++k) {
+          const double d = m.ed_c[3 * static_cast<size_t>(e) + k] - L.c_p[k * NV + i];
+          L.c_apw32[(3 * j + k) * NV + i] = static_cast<float>(sg * d * m.edhx_leng[e] / m.hx_areag[c]);
+        }
+      }
+      for (int k = 0; k < 3; ++k) L.c_p32[k * NV + i] = static_cast<float>(L.c_p[k * NV + i]);
+    }
   }
   L.t_recA.resize(4 * NT);
   L.t_recB.resize(4 * NT);

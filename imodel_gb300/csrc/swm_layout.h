@@ -85,6 +85,12 @@ struct Layout {
   // APVM points, [3][n] in device order, empty without ed%nr: ed%c%p, the
   // circumcentre direction of each triangle (circumcentre()), v%p
   std::vector<double> e_c, t_c, c_p;
+  // the FP32 step's APVM weights: per triangle slot s and component k,
+  // t_apw32[(3s+k)][nt] = -tr%tg (ed%c%p - tr%c%p)_k ed%leng / tr%areag,
+  // per cell slot j, c_apw32[(3j+k)][nv] = ttgout (ed%c%p - v%p)_k
+  // edhx%leng / hx%areag (0 in a pentagon's sixth slot); the unit vectors
+  // t_cc32 [3][nt] and c_p32 [3][nv] for the tangent-plane projections
+  std::vector<float> t_apw32, t_cc32, c_apw32, c_p32;
   // a triangle's FP32 stage inputs as three 16-byte records, [nt] each:
   //   A {edge 0, edge 1, edge 2, cell 0}  B {cell 1, cell 2, circ 0, circ 1}
   //   C {circ 2, kite 0, kite 1, kite 2}  (circ, kite: FP32 bit patterns)

@@ -1,7 +1,9 @@
 """The anticipated potential vorticity method on the GPU
 (imodel_swm_set_apvm): the FP64 step equals the oracle bit for bit,
-tendency and RK4 steps, alone and with diffusion; it costs one launch per
-stage; it switches off again; FP32 handles refuse it."""
+tendency and RK4 steps, alone and with diffusion; the FP32 step (variant 0)
+stays within FP32 round-off of it; it costs one launch per stage; it
+switches off again; the learned correction and the cell-centred variants
+exclude it."""
 import numpy as np
 import pytest
 
@@ -60,13 +62,38 @@ def test_launch_count_and_switching_off(grid_at):
     assert np.array_equal(ha, hb) and np.array_equal(ua, ub)
 
 
+def test_fp32_close_to_oracle(grid_at):
+    g = grid_at(5)
+    h, u = fields.balanced_state(g, lmax=16, seed=7)
+    m = SWM(g, "fp32")
+    m.set_apvm(0.5, 450.0)
+    assert m.launch_count(1) == 4 * 5          # variant 0 and the reconstructions
+    hg, ug = m.ode_rk4(h, u, 450.0, 24)
+    hr, ur = oracle.Oracle(g, 2, pvspar=0.5, dt=450.0).run(h, u, 450.0, 24)
+    hp, up = oracle.Oracle(g, 2).run(h, u, 450.0, 24)
+    w = g.ed_leng * g.edhx_leng
+    rel_h = lambda a, b: np.sqrt(np.sum(g.hx_areag * (a - b) ** 2) / np.sum(g.hx_areag * b ** 2))
+    rel_u = lambda a, b: np.sqrt(np.sum(w * (a - b) ** 2) / np.sum(w * b ** 2))
+    eh, eu = rel_h(hg, hr), rel_u(ug, ur)
+    assert eh < 1e-6 and eu < 1e-5, (eh, eu)
+    # the correction itself is far above that (1.4e-4 in h, 3.9e-3 in u)
+    assert rel_h(hg, hp) > 50 * eh and rel_u(ug, up) > 50 * eu
+
+
 def test_refusals(grid_at):
+    from imodel_gb300 import learned
     g = grid_at(3)
     m = SWM(g, "fp32")
-    with pytest.raises(SWMError) as ei:
-        m.set_apvm(0.5, 600.0)
+    m.set_apvm(0.5, 600.0)
+    with pytest.raises(SWMError) as ei:  # the cell-centred variants have no pre-pass
+        m.set_tuning(variant=1)
     assert ei.value.code == _capi.EINVAL
-    m.set_apvm(0.0, 600.0)              # off is accepted everywhere
+    m.set_apvm(0.0, 600.0)              # off again: every variant is open
+    m.set_tuning(variant=2)
+    n = SWM(g, "fp32", learned_params=learned.trained_params())
+    with pytest.raises(SWMError) as ei:
+        n.set_apvm(0.5, 600.0)
+    assert ei.value.code == _capi.EINVAL
     d = SWM(g, "fp64")
     for pv, dt in ((-0.5, 600.0), (float("nan"), 600.0), (0.5, 0.0), (0.5, float("inf"))):
         with pytest.raises(SWMError) as ei:
