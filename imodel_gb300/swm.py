@@ -219,7 +219,8 @@ class SWM:
 
     def set_apvm(self, pvspar: float, dt: float):
         """pv_stab = "apvm" (swm_operators.f90:1465-1543) with parameter
-        pvspar (0 = off) and the run's time step dt; FP64 handles only."""
+        pvspar (0 = off) and the run's time step dt; moves an FP32 handle
+        to stencil variant 0."""
         self._check(self.lib.imodel_swm_set_apvm(self._handle, pvspar, dt))
 
     def diagnostics(self) -> dict:

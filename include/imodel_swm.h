@@ -203,9 +203,11 @@ int imodel_swm_set_diffusion(void *handle, double k2, double k4);
  * grad q the Perot reconstruction at the triangles of grad_tr2ed(q_tr) and v
  * that of u at the cells (apvm, swm_operators.f90:1465-1543; called at
  * swm.f90:2557-2559).  dt is the run's time step, which the reference's
- * tendency reads from its module: pass the dt the steps use.  FP64 handles
- * only (IMODEL_SWM_EINVAL for FP32); needs the mesh's ed_nr and ed_c.  May be
- * called at any time; applies from the next step. */
+ * tendency reads from its module: pass the dt the steps use.  FP32 handles
+ * move to stencil variant 0 (the correction sits in its edge pre-pass);
+ * set_tuning then refuses variants 1 and 2, and a handle with the learned
+ * correction refuses APVM (IMODEL_SWM_EINVAL).  Needs the mesh's ed_nr and
+ * ed_c.  May be called at any time; applies from the next step. */
 int imodel_swm_set_apvm(void *handle, double pvspar, double dt);
 /* Launches issued by one advance call for nsteps steps (kernels only). */
 int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count);
