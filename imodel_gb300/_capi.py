@@ -102,7 +102,7 @@ SWM_SYMBOLS = [
     "imodel_swm_destroy", "imodel_swm_last_error", "imodel_swm_set_state",
     "imodel_swm_get_state", "imodel_swm_advance", "imodel_swm_profile",
     "imodel_swm_autotune", "imodel_swm_set_tuning", "imodel_swm_set_diffusion",
-    "imodel_swm_set_apvm", "imodel_swm_launch_count",
+    "imodel_swm_set_diffusion_fields", "imodel_swm_set_apvm", "imodel_swm_launch_count",
     "imodel_swm_main_kernel", "imodel_swm_stream", "imodel_swm_weighted_sums_noalloc",
     "imodel_swm_ensemble_create", "imodel_swm_ensemble_set_state",
     "imodel_swm_ensemble_get_state", "imodel_swm_ensemble_advance", "imodel_swm_ensemble_tune",
@@ -174,6 +174,7 @@ def swm_lib() -> ctypes.CDLL:
         lib.imodel_swm_advance.argtypes = [vp, ctypes.c_double, ctypes.c_int32]
         lib.imodel_swm_set_diffusion.argtypes = [vp, ctypes.c_double, ctypes.c_double]
         lib.imodel_swm_set_apvm.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+        lib.imodel_swm_set_diffusion_fields.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
         lib.imodel_swm_profile.argtypes = [vp, ctypes.c_double, ctypes.c_int32, c_f64p]
         lib.imodel_swm_autotune.argtypes = [vp, ctypes.c_double, ctypes.c_int32, c_i32p]
         lib.imodel_swm_set_tuning.argtypes = [vp, c_i32p]

@@ -64,6 +64,8 @@ struct Handle {
   // the mesh gave ed%nr, which the diffusion terms' tangential gradient needs
   bool dif_ok = false;
   double *d_kt64 = nullptr;  // [nt] FP64 K_tr scratch of an FP32 handle
+  double *d_kc64 = nullptr;  // [nv] FP64 K scratch of an FP32 handle
+  double *d_kf = nullptr;    // [2][nv] coefficient fields: reference order, device order
   // a second stream for the energy check, which runs beside the write-back
   // of the state in imodel_swm_step
   cudaStream_t side = nullptr;
@@ -672,33 +674,48 @@ void destroy(Handle *H) {
   delete H;
 }
 
-// the coefficients and work arrays of the (hyper)diffusion terms
+// The coefficients and work arrays of the (hyper)diffusion terms: constant
+// k2 / k4, or, with kf2 / kf4 (host, reference cell order) not NULL, those
+// per-cell fields (the "align" and "diam" branches).
 template <class T>
-int setup_diffusion(Handle *H, Work<T> &W, double k2, double k4) {
+int setup_diffusion(Handle *H, Work<T> &W, double k2, double k4, const double *kf2,
+                    const double *kf4) {
   Diffusion<T> &D = W.dif;
-  D.k2 = k2 > 0;
-  D.k4 = k4 > 0;
+  D.k2 = k2 > 0 || kf2;
+  D.k4 = k4 > 0 || kf4;
   D.on = D.k2 || D.k4;
   if (!D.on) return IMODEL_SWM_OK;
   int rc;
-  if (!D.kt && ((rc = dalloc(H, &D.kt, H->nt)) || (rc = dalloc(H, &D.coefdiv, H->nv)) ||
-                (rc = dalloc(H, &D.coefvort, H->nt)) || (rc = dalloc(H, &D.lap, H->ne)) ||
-                (rc = dalloc(H, &D.lap2, H->ne))))
+  if (!D.kt && ((rc = dalloc(H, &D.kt, H->nt)) || (rc = dalloc(H, &D.kcv, H->nv)) ||
+                (rc = dalloc(H, &D.coefdiv, H->nv)) || (rc = dalloc(H, &D.coefvort, H->nt)) ||
+                (rc = dalloc(H, &D.lap, H->ne)) || (rc = dalloc(H, &D.lap2, H->ne))))
     return rc;
-  double *kt64 = nullptr;
-  float *kt32 = nullptr;
+  double *kt64 = nullptr, *kc64 = nullptr;
+  float *kt32 = nullptr, *kc32 = nullptr;
   if (sizeof(T) == sizeof(double)) {
     kt64 = reinterpret_cast<double *>(D.kt);
+    kc64 = reinterpret_cast<double *>(D.kcv);
   } else {
-    if (!H->d_kt64 && (rc = dalloc(H, &H->d_kt64, H->nt))) return rc;
+    if (!H->d_kt64 && ((rc = dalloc(H, &H->d_kt64, H->nt)) || (rc = dalloc(H, &H->d_kc64, H->nv))))
+      return rc;
     kt64 = H->d_kt64;
+    kc64 = H->d_kc64;
     kt32 = reinterpret_cast<float *>(D.kt);
+    kc32 = reinterpret_cast<float *>(D.kcv);
   }
-  // swm.f90:169-205, "const": K at the cells, hx2tr(K) at the triangles;
+  // swm.f90:169-205: K at the cells, hx2tr(K) at the triangles;
   // hyperdiffusion applies the Laplacian twice with sqrt(K4) and
   // sqrt(hx2tr(K4)), and then also replaces the Laplacian's coefficients
-  D.kc = static_cast<T>(D.k4 ? std::sqrt(k4) : k2);
-  launch_hx2tr_const(H->M, D.k4 ? k4 : k2, D.k4, kt64, kt32, H->stream);
+  const double *kf = D.k4 ? kf4 : kf2;
+  double *kf_dev = nullptr;
+  if (kf) {
+    const size_t nv = static_cast<size_t>(H->nv);
+    if (!H->d_kf && (rc = dalloc(H, &H->d_kf, 2 * nv))) return rc;
+    CK(cudaMemcpyAsync(H->d_kf, kf, nv * sizeof(double), cudaMemcpyHostToDevice, H->stream));
+    launch_gather_in(H->nv, H->d_cell_n2o, H->d_kf, H->d_kf + nv, 0.0, H->stream);
+    kf_dev = H->d_kf + nv;
+  }
+  launch_dif_coefs(H->M, kf_dev, D.k4 ? k4 : k2, D.k4, kc64, kc32, kt64, kt32, H->stream);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(H->stream));
   return IMODEL_SWM_OK;
@@ -1129,8 +1146,33 @@ int imodel_swm_set_diffusion(void *handle, double k2, double k4) {
   if ((k2 > 0 || k4 > 0) && !H->dif_ok)
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "the diffusion terms need the mesh's ed_nr");
   if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
-  const int rc = H->precision == IMODEL_SWM_FP64 ? imodel::setup_diffusion(H, H->W64, k2, k4)
-                                                 : imodel::setup_diffusion(H, H->W32, k2, k4);
+  const int rc = H->precision == IMODEL_SWM_FP64
+                     ? imodel::setup_diffusion(H, H->W64, k2, k4, nullptr, nullptr)
+                     : imodel::setup_diffusion(H, H->W32, k2, k4, nullptr, nullptr);
+  if (rc) return rc;
+  if (H->graph) {
+    cudaGraphExecDestroy(H->graph);
+    H->graph = nullptr;
+  }
+  return IMODEL_SWM_OK;
+}
+
+int imodel_swm_set_diffusion_fields(void *handle, const double *k2_hx, const double *k4_hx) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H) return IMODEL_SWM_EINVAL;
+  if (H->nv == 0) return imodel::set_error(H, IMODEL_SWM_ESTATE, "handle was not created");
+  for (const double *f : {k2_hx, k4_hx})
+    if (f)
+      for (int i = 0; i < H->nv; ++i)
+        if (!(f[i] >= 0) || !std::isfinite(f[i]))
+          return imodel::set_error(H, IMODEL_SWM_EINVAL,
+                                   "diffusion coefficient fields must be finite and >= 0");
+  if ((k2_hx || k4_hx) && !H->dif_ok)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "the diffusion terms need the mesh's ed_nr");
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  const int rc = H->precision == IMODEL_SWM_FP64
+                     ? imodel::setup_diffusion(H, H->W64, 0.0, 0.0, k2_hx, k4_hx)
+                     : imodel::setup_diffusion(H, H->W32, 0.0, 0.0, k2_hx, k4_hx);
   if (rc) return rc;
   if (H->graph) {
     cudaGraphExecDestroy(H->graph);

@@ -75,7 +75,7 @@ struct LearnedDev;
 template <class T>
 struct Diffusion {
   bool on = false, k2 = false, k4 = false;
-  T kc = T(0);              // coefficient at cells: K2, or sqrt(K4)
+  T *kcv = nullptr;         // [nv] at the cells: K2, or sqrt(K4)
   T *kt = nullptr;          // [nt] at triangles: hx2tr(K2), or sqrt(hx2tr(K4))
   T *coefdiv = nullptr;     // [nv] K div x
   T *coefvort = nullptr;    // [nt] K_tr zeta(x)
@@ -150,11 +150,12 @@ inline int launches_per_stage(int precision_fp32, int variant, bool dif_on = fal
   if (apvm_on) n += 1;
   return n;
 }
-// K_tr of a constant coefficient: scalar_hx2tr (kite-area weights, FP64),
-// then sqrt with take_sqrt (hyperdiffusion), into kt64 and, when not NULL,
-// its FP32 rounding kt32
-void launch_hx2tr_const(const DevMesh &M, double k, bool take_sqrt, double *kt64, float *kt32,
-                        cudaStream_t s);
+// The diffusion coefficients from the cell field kf (device order, FP64;
+// NULL: the constant k): kc64 = kf at the cells and kt64 = scalar_hx2tr(kf)
+// (kite-area weights) at the triangles, each then sqrt with take_sqrt
+// (hyperdiffusion); kc32 / kt32, when not NULL, their FP32 roundings
+void launch_dif_coefs(const DevMesh &M, const double *kf, double k, bool take_sqrt, double *kc64,
+                      float *kc32, double *kt64, float *kt32, cudaStream_t s);
 
 
 // reference order <-> device order, with precision conversion

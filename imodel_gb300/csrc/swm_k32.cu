@@ -170,7 +170,8 @@ __global__ void __launch_bounds__(512) k_edge32(DevMesh M, const float *__restri
 // at the triangles (the blocks after), with the folded FP32 coefficients of
 // div_hx and rel_vort_tr
 __global__ void __launch_bounds__(256) k_difcv32(DevMesh M, const float *__restrict__ x,
-                                                 float kc, const float *__restrict__ kt,
+                                                 const float *__restrict__ kcv,
+                                                 const float *__restrict__ kt,
                                                  float *__restrict__ coefdiv,
                                                  float *__restrict__ coefvort, int nbc) {
   if (static_cast<int>(blockIdx.x) < nbc) {
@@ -180,7 +181,7 @@ __global__ void __launch_bounds__(256) k_difcv32(DevMesh M, const float *__restr
     const int n = M.c_nnb[i];
     float d = 0.0f;
     for (int j = 0; j < n; ++j) d += x[__ldg(&M.c_ed[j * nv + i])] * __ldg(&M.c_div32[j * nv + i]);
-    coefdiv[i] = kc * d;
+    coefdiv[i] = kcv[i] * d;
   } else {
     const int t = (blockIdx.x - nbc) * blockDim.x + threadIdx.x;
     if (t >= M.nt) return;
@@ -217,12 +218,13 @@ __global__ void __launch_bounds__(512) k_cell32v2(DevMesh M, const float *__rest
                                                   float *__restrict__ acc,
                                                   float *__restrict__ yout,
                                                   float *__restrict__ tend, int stage, float dt,
-                                                  float grav, float h_ref, float kc,
+                                                  float grav, float h_ref,
+                                                  const float *__restrict__ kcv,
                                                   float *__restrict__ coefdiv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= M.nv) return;
   cell_body(M, i, OneRun{}, hd, u, q_tr, bern, zflux, yn, acc, yout, tend, stage, dt, grav, h_ref,
-            kc, coefdiv);
+            kcv, coefdiv);
 }
 
 // ---- variant 2: the triangle kernel on records with 16-bit indices -------
@@ -324,12 +326,12 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
     if (!D.on) return;
     k_diflap32<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap);
     if (D.k4) {
-      k_difcv32<<<nbc + nbt, 256, 0, s>>>(M, D.lap, D.kc, D.kt, D.coefdiv, D.coefvort, nbc);
+      k_difcv32<<<nbc + nbt, 256, 0, s>>>(M, D.lap, D.kcv, D.kt, D.coefdiv, D.coefvort, nbc);
       k_diflap32<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap2);
     }
   };
   if (T.variant == 0 && D.on)  // variant 0: K div u and K_tr zeta in their own pass
-    k_difcv32<<<nbc + nbt, 256, 0, s>>>(M, u_in, D.kc, D.kt, D.coefdiv, D.coefvort, nbc);
+    k_difcv32<<<nbc + nbt, 256, 0, s>>>(M, u_in, D.kcv, D.kt, D.coefdiv, D.coefvort, nbc);
   float *cvort = (T.variant >= 1 && D.on) ? D.coefvort : nullptr;
   if (T.variant == 2)
     k_tri32c<<<nblocks(M.nt, T.bs_tri), T.bs_tri, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ref,
@@ -345,7 +347,7 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
     if (ev) cudaEventRecord(ev[2], s);
     k_cell32v2<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
         M, h_in, u_in, W.q_tr, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
-        grav, W.h_ref, D.kc, D.on ? D.coefdiv : nullptr);
+        grav, W.h_ref, D.kcv, D.on ? D.coefdiv : nullptr);
     diffusion_tail();
     if (ev) cudaEventRecord(ev[3], s);
     k_edge32v2<<<nblocks((M.ne + 1) / 2, T.bs_edge), T.bs_edge, 0, s>>>(

@@ -171,7 +171,8 @@ __device__ __forceinline__ void cell_math(int i, uint32_t meta, const float (&R)
                                           float *__restrict__ bern, float *__restrict__ zflux,
                                           float *__restrict__ acc, float *__restrict__ yout,
                                           float *__restrict__ tend, int stage, float dt,
-                                          float grav, float h_ref, Ix ix = Ix{}, float kc = 0.0f,
+                                          float grav, float h_ref, Ix ix = Ix{},
+                                          const float *__restrict__ kcv = nullptr,
                                           float *__restrict__ coefdiv = nullptr) {
   const int n = static_cast<int>(meta & 7u);
   const unsigned tneg = meta >> 8;
@@ -190,7 +191,7 @@ __device__ __forceinline__ void cell_math(int i, uint32_t meta, const float (&R)
     du += ue[j] * kd[j].y;
   }
   // with diffusion on: K times the divergence of u
-  if (coefdiv) coefdiv[ix(i)] = kc * (du * inva);
+  if (coefdiv) coefdiv[ix(i)] = kcv[ix(i)] * (du * inva);
   bern[ix(i)] = grav * (hi + bt) + ke;
   float Z[6];
   if (n == 6)
@@ -232,7 +233,7 @@ __device__ __forceinline__ void cell_core(int i, Ix ix, uint32_t meta,
                                           float *__restrict__ bern, float *__restrict__ zflux,
                                           float *__restrict__ acc, float *__restrict__ yout,
                                           float *__restrict__ tend, int stage, float dt,
-                                          float grav, float h_ref, float kc = 0.0f,
+                                          float grav, float h_ref, const float *__restrict__ kcv = nullptr,
                                           float *__restrict__ coefdiv = nullptr) {
   float ue[6], hn[6], qt[6];
 #pragma unroll
@@ -242,7 +243,7 @@ __device__ __forceinline__ void cell_core(int i, Ix ix, uint32_t meta,
     qt[j] = Ld::ld(q_tr + ix(tr[j]));
   }
   cell_math(i, meta, R, kd, ue, hn, qt, hi, bt, inva, ynv, accv, bern, zflux, acc, yout, tend,
-            stage, dt, grav, h_ref, ix, kc, coefdiv);
+            stage, dt, grav, h_ref, ix, kcv, coefdiv);
 }
 
 // the cell's own values from global memory
@@ -268,7 +269,8 @@ __device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
                                           const float *__restrict__ yn, float *__restrict__ acc,
                                           float *__restrict__ yout, float *__restrict__ tend,
                                           int stage, float dt, float grav, float h_ref,
-                                          float kc = 0.0f, float *__restrict__ coefdiv = nullptr) {
+                                          const float *__restrict__ kcv = nullptr,
+                                          float *__restrict__ coefdiv = nullptr) {
   const int nv = M.nv;
   const uint32_t meta = __ldg(&M.c_meta[i]);
   int ed[6], nb[6], tr[6];
@@ -288,7 +290,7 @@ __device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
   float hi, bt, inva, ynv, accv;
   cell_own<Ix, Ld>(M, i, ix, hd, yn, acc, stage, hi, bt, inva, ynv, accv);
   cell_core<Ix, Ld>(i, ix, meta, ed, nb, tr, R, kd, hi, bt, inva, ynv, accv, hd, u, q_tr, bern,
-                    zflux, acc, yout, tend, stage, dt, grav, h_ref, kc, coefdiv);
+                    zflux, acc, yout, tend, stage, dt, grav, h_ref, kcv, coefdiv);
 }
 
 // -grad B - (Z_c1 + Z_c2) / l_e and the momentum RK stage of edge e

@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(256) k_cell64(DevMesh M, const double *__restr
                                                 double *__restrict__ acc,
                                                 double *__restrict__ yout,
                                                 double *__restrict__ tend, int stage,
-                                                double dt, double kc,
+                                                double dt, const double *__restrict__ kcv,
                                                 double *__restrict__ coefdiv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int nv = M.nv;
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(256) k_cell64(DevMesh M, const double *__restr
     if (coefdiv) du = du + ue * M.c_sd[j * nv + i];
   }
   // with diffusion on: div_hx(u) (:613-661), diffusion_ed's K div u
-  if (coefdiv) coefdiv[i] = kc * (du / M.c_areag[i] / M.erad);
+  if (coefdiv) coefdiv[i] = kcv[i] * (du / M.c_areag[i] / M.erad);
   const double divuh = d / M.c_areag[i] / M.erad;
   const double ke = k / M.c_cellarea[i];
   bern[i] = M.grav * (h[i] + M.c_bt[i]) + ke;
@@ -242,7 +242,8 @@ __global__ void __launch_bounds__(256) k_edge64(DevMesh M, const double *__restr
 // at the triangles (the blocks after), HTC branches of div_hx (:613-661) and
 // rel_vort_tr (:780-827)
 __global__ void __launch_bounds__(256) k_difcv64(DevMesh M, const double *__restrict__ x,
-                                                 double kc, const double *__restrict__ kt,
+                                                 const double *__restrict__ kcv,
+                                                 const double *__restrict__ kt,
                                                  double *__restrict__ coefdiv,
                                                  double *__restrict__ coefvort, int nbc) {
   if (static_cast<int>(blockIdx.x) < nbc) {
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(256) k_difcv64(DevMesh M, const double *__rest
     double d = 0.0;
     for (int j = 0; j < n; ++j) d = d + x[M.c_ed[j * nv + i]] * M.c_sd[j * nv + i];
     const double divx = d / M.c_areag[i] / M.erad;
-    coefdiv[i] = kc * divx;
+    coefdiv[i] = kcv[i] * divx;
   } else {
     const int t = (blockIdx.x - nbc) * blockDim.x + threadIdx.x;
     const int nt = M.nt;
@@ -281,20 +282,31 @@ __global__ void __launch_bounds__(256) k_diflap64(DevMesh M, const double *__res
   lap[e] = g - gt;
 }
 
-// scalar_hx2tr (:258-263) of a constant k, then sqrt for hyperdiffusion
-// (swm.f90:183-204)
-__global__ void k_hx2tr_const(DevMesh M, double k, int take_sqrt, double *__restrict__ kt64,
-                              float *__restrict__ kt32) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nt = M.nt;
-  if (t >= nt) return;
-  double f = 0.0;
+// the coefficients swm.f90:169-205 sets: at the cells the coefficient field
+// kf (device order; NULL: the constant k), at the triangles its
+// scalar_hx2tr (:258-263); both then sqrt for hyperdiffusion
+__global__ void k_dif_coefs(DevMesh M, const double *__restrict__ kf, double k, int take_sqrt,
+                            double *__restrict__ kc64, float *__restrict__ kc32,
+                            double *__restrict__ kt64, float *__restrict__ kt32, int nbc) {
+  if (static_cast<int>(blockIdx.x) < nbc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M.nv) return;
+    double f = kf ? kf[i] : k;
+    if (take_sqrt) f = sqrt(f);
+    kc64[i] = f;
+    if (kc32) kc32[i] = static_cast<float>(f);
+  } else {
+    const int t = (blockIdx.x - nbc) * blockDim.x + threadIdx.x;
+    const int nt = M.nt;
+    if (t >= nt) return;
+    double f = 0.0;
 #pragma unroll
-  for (int s = 0; s < 3; ++s) f = f + M.t_kite[s * nt + t] * k;
-  f = f / M.t_areag[t];
-  if (take_sqrt) f = sqrt(f);
-  kt64[t] = f;
-  if (kt32) kt32[t] = static_cast<float>(f);
+    for (int s = 0; s < 3; ++s) f = f + M.t_kite[s * nt + t] * (kf ? kf[M.t_v[s * nt + t]] : k);
+    f = f / M.t_areag[t];
+    if (take_sqrt) f = sqrt(f);
+    kt64[t] = f;
+    if (kt32) kt32[t] = static_cast<float>(f);
+  }
 }
 
 template <class T>
@@ -689,13 +701,13 @@ void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
                                                    A.on ? A.qg : nullptr, A.vhx, A.coef);
   if (ev) cudaEventRecord(ev[2], s);
   k_cell64<<<nblocks(M.nv, 256), 256, 0, s>>>(M, h_in, u_in, W.uh, W.bern, W.yn_h, W.acc_h,
-                                               h_out, W.tend_h, stage, dt, D.kc,
+                                               h_out, W.tend_h, stage, dt, D.kcv,
                                                D.on ? D.coefdiv : nullptr);
   if (D.on) {
     k_diflap64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap);
     if (D.k4) {
       const int nbc = nblocks(M.nv, 256), nbt = nblocks(M.nt, 256);
-      k_difcv64<<<nbc + nbt, 256, 0, s>>>(M, D.lap, D.kc, D.kt, D.coefdiv, D.coefvort, nbc);
+      k_difcv64<<<nbc + nbt, 256, 0, s>>>(M, D.lap, D.kcv, D.kt, D.coefdiv, D.coefvort, nbc);
       k_diflap64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap2);
     }
   }
@@ -706,9 +718,11 @@ void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
   if (ev) cudaEventRecord(ev[4], s);
 }
 
-void launch_hx2tr_const(const DevMesh &M, double k, bool take_sqrt, double *kt64, float *kt32,
-                        cudaStream_t s) {
-  k_hx2tr_const<<<nblocks(M.nt, 256), 256, 0, s>>>(M, k, take_sqrt ? 1 : 0, kt64, kt32);
+void launch_dif_coefs(const DevMesh &M, const double *kf, double k, bool take_sqrt, double *kc64,
+                      float *kc32, double *kt64, float *kt32, cudaStream_t s) {
+  const int nbc = nblocks(M.nv, 256);
+  k_dif_coefs<<<nbc + nblocks(M.nt, 256), 256, 0, s>>>(M, kf, k, take_sqrt ? 1 : 0, kc64, kc32,
+                                                        kt64, kt32, nbc);
 }
 
 void launch_gather_in(int n, const int32_t *n2o, const double *src, double *dst, double shift,

@@ -217,6 +217,18 @@ class SWM:
         swm_operators.f90:855-975); 0 switches a term off."""
         self._check(self.lib.imodel_swm_set_diffusion(self._handle, k2, k4))
 
+    def set_diffusion_fields(self, k2_hx=None, k4_hx=None):
+        """Diffusion / hyperdiffusion with per-cell coefficient fields (nv
+        values, the "align" / "diam" branches; see imodel_gb300.difcoef);
+        None switches a term off."""
+        a = [None if f is None else np.ascontiguousarray(f, dtype=np.float64)
+             for f in (k2_hx, k4_hx)]
+        for f in a:
+            if f is not None and f.shape != (self.grid.nv,):
+                raise ValueError("a coefficient field has one value per cell")
+        p = [None if f is None else f.ctypes.data for f in a]
+        self._check(self.lib.imodel_swm_set_diffusion_fields(self._handle, p[0], p[1]))
+
     def set_apvm(self, pvspar: float, dt: float):
         """pv_stab = "apvm" (swm_operators.f90:1465-1543) with parameter
         pvspar (0 = off) and the run's time step dt; moves an FP32 handle

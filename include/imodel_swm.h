@@ -197,6 +197,13 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[6]);
  * term then also uses sqrt(K4), as the reference's coefficients do).  Needs
  * the mesh's ed_nr.  May be called at any time; applies from the next step. */
 int imodel_swm_set_diffusion(void *handle, double k2, double k4);
+/* The same terms with per-cell coefficient fields (nv values in the mesh's
+ * cell order, m^2/s and m^4/s; NULL switches a term off), as the "align" and
+ * "diam" branches of swm.f90:169-205 form them (alignment_coef,
+ * diameter_coef, swm_operators.f90:977-1069): K_tr is the kite-weighted
+ * scalar_hx2tr of the field, and with k4_hx both coefficients are the square
+ * roots.  Values must be finite and >= 0. */
+int imodel_swm_set_diffusion_fields(void *handle, const double *k2_hx, const double *k4_hx);
 /* PV stabilisation pv_stab = "apvm" (swm.par; swm_data.f90:548) with
  * parameter pvspar (0 switches it off): before the Coriolis term each edge's
  * PV becomes q_ed - pvspar dt (grad q(t1) + grad q(t2)) . (v(c1) + v(c2)),

@@ -63,6 +63,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_field.argtypes = [vp, ctypes.c_int32, f64p]
         L.oracle_set_diffusion.argtypes = [vp, ctypes.c_double, ctypes.c_double]
         L.oracle_set_apvm.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+        L.oracle_set_diffusion_fields.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -82,7 +83,8 @@ class Oracle:
     """The reference's swm_tests state machine on the CPU, for one grid."""
 
     def __init__(self, grid, testcase: int = 2, bt=None, nthreads: int = 0, k2: float = 0.0,
-                 k4: float = 0.0, pvspar: float = 0.0, dt: float = 0.0):
+                 k4: float = 0.0, pvspar: float = 0.0, dt: float = 0.0, k2_hx=None,
+                 k4_hx=None):
         self.grid = grid
         self._mesh = grid.c_struct()
         self._bt = None if bt is None else np.ascontiguousarray(bt, dtype=np.float64)
@@ -93,6 +95,12 @@ class Oracle:
         if k2 or k4:
             if lib().oracle_set_diffusion(self._h, k2, k4):
                 raise ValueError("bad diffusion coefficients")
+        if k2_hx is not None or k4_hx is not None:
+            self._kf = [None if f is None else np.ascontiguousarray(f, dtype=np.float64)
+                        for f in (k2_hx, k4_hx)]
+            p = [None if f is None else f.ctypes.data for f in self._kf]
+            if lib().oracle_set_diffusion_fields(self._h, p[0], p[1]):
+                raise ValueError("bad diffusion coefficient fields")
         if pvspar:
             if lib().oracle_set_apvm(self._h, pvspar, dt):
                 raise ValueError("bad apvm parameter or time step")

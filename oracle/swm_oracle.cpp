@@ -34,7 +34,7 @@ struct Oracle {
   std::vector<double> massf[4], momf[4], h_tmp, u_tmp;
   // diffusion_ed / hyperdiffusion_ed with constant coefficients
   bool k2_on = false, k4_on = false;
-  double dif_hx = 0.0;                 // dif_coef_hx (constant)
+  std::vector<double> dif_hx;          // dif_coef_hx [nv]
   std::vector<double> dif_tr, sgtg;    // dif_coef_tr [nt]; grad_ed_tg signcor [ne]
   std::vector<double> coefdiv, coefvort, lapu, lap_lapu, div_lap, vort_lap;
   // apvm (swm_operators.f90:1465-1543): pv_stab = "apvm", pvspar, the run's dt
@@ -62,7 +62,7 @@ void diffusion(Oracle &o, const double *div, const double *vort, double *lap) {
   const double erad = m.erad;
   const int nth = o.nthreads;
 #pragma omp parallel for schedule(static) num_threads(nth)
-  for (int i = 0; i < nv; ++i) o.coefdiv[i] = o.dif_hx * div[i];
+  for (int i = 0; i < nv; ++i) o.coefdiv[i] = o.dif_hx[i] * div[i];
 #pragma omp parallel for schedule(static) num_threads(nth)
   for (int k = 0; k < nt; ++k) o.coefvort[k] = o.dif_tr[k] * vort[k];
 #pragma omp parallel for schedule(static) num_threads(nth)
@@ -475,29 +475,30 @@ void circumcentres_and_signs(Oracle &o) {
   }
 }
 
-// coefficients as swm.f90:169-205 sets them for diffus = hyperdiffus =
-// "const"; the sign of grad_ed_tg from the triangles' circumcentres
-// (trcircumc: the unit normal of the vertices' plane, on their side)
-int oracle_set_diffusion(void *p, double k2, double k4) {
-  Oracle &o = *static_cast<Oracle *>(p);
+// coefficients as swm.f90:169-205 sets them: kf2 / kf4 (the "align" /
+// "diam" fields, [nv]) or, where NULL, the constants k2 / k4 ("const"); the
+// sign of grad_ed_tg from the triangles' circumcentres (trcircumc: the unit
+// normal of the vertices' plane, on their side)
+static int set_diffusion(Oracle &o, double k2, double k4, const double *kf2, const double *kf4) {
   const imodel_swm_mesh &m = o.m;
   if (!(k2 >= 0) || !(k4 >= 0)) return IMODEL_SWM_EINVAL;
-  o.k2_on = k2 > 0;
-  o.k4_on = k4 > 0;
+  o.k2_on = k2 > 0 || kf2;
+  o.k4_on = k4 > 0 || kf4;
   if (!o.k2_on && !o.k4_on) return IMODEL_SWM_OK;
   if (!m.ed_nr || !m.v_p) return IMODEL_SWM_EINVAL;
   const size_t nv = m.nv, ne = m.ne, nt = m.nt;
-  // scalar_hx2tr of the constant coefficient (:258-263)
-  const double kc = o.k4_on ? k4 : k2;
+  const double *kf = o.k4_on ? kf4 : kf2;
+  o.dif_hx.assign(nv, o.k4_on ? k4 : k2);
+  if (kf) o.dif_hx.assign(kf, kf + nv);
+  // scalar_hx2tr of the coefficient (:258-263)
   o.dif_tr.assign(nt, 0.0);
   for (size_t k = 0; k < nt; ++k) {
     double f = 0.0;
-    for (int i = 0; i < 3; ++i) f = f + m.tr_trhx_area[3 * k + i] * kc;
+    for (int i = 0; i < 3; ++i) f = f + m.tr_trhx_area[3 * k + i] * o.dif_hx[m.tr_v[3 * k + i] - 1];
     o.dif_tr[k] = f / m.tr_areag[k];
   }
-  o.dif_hx = kc;
   if (o.k4_on) {
-    o.dif_hx = std::sqrt(o.dif_hx);
+    for (size_t i = 0; i < nv; ++i) o.dif_hx[i] = std::sqrt(o.dif_hx[i]);
     for (size_t k = 0; k < nt; ++k) o.dif_tr[k] = std::sqrt(o.dif_tr[k]);
   }
   circumcentres_and_signs(o);
@@ -505,6 +506,19 @@ int oracle_set_diffusion(void *p, double k2, double k4) {
   for (auto *v : {&o.coefvort, &o.vort_lap}) v->assign(nt, 0.0);
   for (auto *v : {&o.coefdiv, &o.div_lap}) v->assign(nv, 0.0);
   return IMODEL_SWM_OK;
+}
+
+int oracle_set_diffusion(void *p, double k2, double k4) {
+  return set_diffusion(*static_cast<Oracle *>(p), k2, k4, nullptr, nullptr);
+}
+
+int oracle_set_diffusion_fields(void *p, const double *k2_hx, const double *k4_hx) {
+  Oracle &o = *static_cast<Oracle *>(p);
+  for (const double *f : {k2_hx, k4_hx})
+    if (f)
+      for (int i = 0; i < o.m.nv; ++i)
+        if (!(f[i] >= 0) || !std::isfinite(f[i])) return IMODEL_SWM_EINVAL;
+  return set_diffusion(o, 0.0, 0.0, k2_hx, k4_hx);
 }
 
 int oracle_set_apvm(void *p, double pvspar, double dt) {

@@ -23,6 +23,9 @@ void oracle_destroy(void *o);
 /* Laplacian diffusion / hyperdiffusion with constant coefficients (m^2/s,
  * m^4/s; 0 = off), swm.f90:169-205 and swm_operators.f90:855-975 */
 int oracle_set_diffusion(void *o, double k2, double k4);
+/* the same with per-cell coefficient fields [nv] (NULL: term off), the
+ * "align" / "diam" branches of swm.f90:169-205 */
+int oracle_set_diffusion_fields(void *o, const double *k2_hx, const double *k4_hx);
 /* pv_stab = "apvm" with parameter pvspar (0 = off) and the run's time step
  * dt, swm_operators.f90:1465-1543 */
 int oracle_set_apvm(void *o, double pvspar, double dt);
