@@ -347,6 +347,9 @@ def main():
     ap.add_argument("--tuning", default="",
                     help="FP32 launch choice 'variant,bs_tri,bs_pre,bs_cell,bs_edge"
                          "[,mlp_gather]' instead of autotuning")
+    ap.add_argument("--apvm", type=float, default=0.0,
+                    help="pv_stab = apvm with this pvspar on the fp64 and fp32 paths "
+                         "(FP32 then runs stencil variant 0)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -374,6 +377,8 @@ def main():
         m = swm.SWM(g, precision="fp64" if path == "fp64" else "fp32", device=local,
                     learned_params=params if path == "fp32l" else None)
         m.set_state(h, u)
+        if args.apvm > 0 and path != "fp32l":
+            m.set_apvm(args.apvm, DT)
         tuning = None
         if path != "fp64":
             if args.tuning:
@@ -458,7 +463,8 @@ def main():
             "ms_per_step": rh["ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: Williamson case 2 steady zonal flow on the grid (no dataset)",
-            "config": dict(config_dict(g, headline, weights), autotuned=rh["tuning"]),
+            "config": dict(config_dict(g, headline, weights), autotuned=rh["tuning"],
+                           **({"apvm_pvspar": args.apvm} if args.apvm > 0 else {})),
             "fp64": {"value": rate(r64), "unit": UNIT, "ms_per_step": r64["ms"] / args.steps,
                      "kernel_ms": r64["prof"]},
             "kernel_ms": kernel_ms,
