@@ -264,12 +264,93 @@ def galewsky(grid: Grid, testcase: int = 21):
     return h, u, np.zeros(grid.nv)
 
 
+# ---- cases 56, 57: Matsuno equatorial waves ------------------------------
+MATSUNO_H0 = 30.0
+MATSUNO_N = 1
+MATSUNO_K = 5.0
+MATSUNO_AM = float(np.float32(0.00001))   # a default-real literal
+
+
+def matsuno_parameters(testcase: int):
+    """parameters_matsuno (swm_matsuno.f90): frequency w of the n = 1,
+    k = 5 wave -- the largest root of the cubic dispersion relation for the
+    inertia-gravity wave (56), the smallest in magnitude, sign flipped, for
+    the Rossby wave (57) -- and the coefficients of its Hermite-function
+    structure.  The square roots of (n+1)/2 and n/2 are taken in single
+    precision, as the reference's real() conversions do."""
+    if testcase not in (56, 57):
+        raise ValueError("Matsuno cases are 56 (inertia-gravity) and 57 (Rossby)")
+    a, g, h0, n = ERAD, GRAV, MATSUNO_H0, MATSUNO_N
+    eps = (2.0 * OMEGA * a) ** 2 / (g * h0)
+    ks = MATSUNO_K / a
+    d0 = 3.0 * (g * h0 * ks * ks + 2.0 * OMEGA * np.sqrt(g * h0) * (2.0 * n + 1.0) / a)
+    d4 = -54.0 * OMEGA * g * h0 * ks / a
+    w_nk = np.empty(3)
+    for j in (1, 2, 3):
+        d = np.sqrt(complex(d4 ** 2 - 4.0 * d0 ** 3))
+        d = (d + d4) * 0.5
+        d = d ** (1.0 / 3.0)
+        d = d * np.exp((2.0 * PI * j / 3.0) * 1j)
+        w_nk[j - 1] = -np.real(d + d0 / d) / 3.0
+    w = w_nk.max() if testcase == 56 else -np.abs(w_nk).min()
+    c1 = eps ** 0.25 / a
+    c2 = g * h0 * eps ** 0.25 / ((w * w - g * h0 * ks * ks) * a) / 1j
+    s1 = float(np.sqrt(np.float32((n + 1.0) * 0.5)))
+    s0 = float(np.sqrt(np.float32(n * 0.5)))
+    coef = np.array([c1,
+                     c2 * (-s1 * (w / np.sqrt(g * h0) + ks)),
+                     c2 * (-s0 * (w / np.sqrt(g * h0) - ks)),
+                     c2 * (-s1 * (w + np.sqrt(g * h0) * ks)),
+                     c2 * (s0 * (w - np.sqrt(g * h0) * ks))], dtype=np.complex128)
+    return w, ks, coef
+
+
+def hermite(x, n: int):
+    """Normalised Hermite function without its Gaussian (swm_matsuno.f90,
+    Hermite): H_0 = pi^(-1/4), H_(i+1) = x sqrt(2/(i+1)) H_i - sqrt(i/(i+1))
+    H_(i-1), the last square root in single precision."""
+    hm = np.zeros_like(x)
+    hc = np.full_like(x, 1.0 / PI ** 0.25)
+    for i in range(n):
+        r = float(np.sqrt(np.float32(np.float32(i) / np.float32(i + 1))))
+        hm, hc = hc, x * np.sqrt(2.0 / (i + 1)) * hc - r * hm
+    return hc
+
+
+def _matsuno_vbar(lat, coef):
+    y = lat * ERAD
+    yy = np.real(coef[0]) * y
+    gauss = np.exp(-0.5 * yy ** 2)
+    n = MATSUNO_N
+    return [MATSUNO_AM * hermite(yy, k) * gauss for k in (n - 1, n, n + 1)]
+
+
+def matsuno_fields(grid: Grid, testcase: int, t: float = 0.0):
+    """exact_matsuno (swm_matsuno.f90): the wave's h at the cells and its
+    velocity along ed%tg at the edge midpoints at time t (s)."""
+    w, ks, coef = matsuno_parameters(testcase)
+    vm, v0, vp = _matsuno_vbar(grid.v_lat, coef)
+    phase = np.exp((ks * grid.v_lon * ERAD - w * t) * 1j)
+    h = np.real((coef[3] * vp + coef[4] * vm) * phase) / GRAV + MATSUNO_H0
+    vm, v0, vp = _matsuno_vbar(grid.ed_c_lat, coef)
+    phase = np.exp((ks * grid.ed_c_lon * ERAD - w * t) * 1j)
+    ue = np.real((coef[1] * vp + coef[2] * vm) * phase)
+    ve = np.real(v0 * phase)
+    return h, _edge_u(grid, ue, ve)
+
+
+def matsuno(grid: Grid, testcase: int):
+    h, u = matsuno_fields(grid, testcase, 0.0)
+    return h, u, np.zeros(grid.nv)
+
+
 CASES = {0: tc0, 1: tc1, 2: None, 5: tc5, 6: tc6,
-         21: galewsky, 22: lambda g: galewsky(g, 22), 23: lambda g: galewsky(g, 23)}
+         21: galewsky, 22: lambda g: galewsky(g, 22), 23: lambda g: galewsky(g, 23),
+         56: lambda g: matsuno(g, 56), 57: lambda g: matsuno(g, 57)}
 
 
 def initialize_fields(grid: Grid, testcase: int):
-    """(h[nv], u[ne], bt[nv]) of a test case (0, 1, 2, 5, 6, 21, 22, 23)."""
+    """(h[nv], u[ne], bt[nv]) of a test case (0, 1, 2, 5, 6, 21-23, 56, 57)."""
     if testcase == 2:
         h, u = initialize_fields_tc2(grid)
         return h, u, np.zeros(grid.nv)

@@ -11,7 +11,8 @@ from imodel_gb300.swm import SWM
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("case,dt", [(1, 900.0), (5, 600.0), (6, 600.0), (21, 600.0)])
+@pytest.mark.parametrize("case,dt", [(1, 900.0), (5, 600.0), (6, 600.0), (21, 600.0), (56, 300.0),
+                                     (57, 1800.0)])
 def test_fp64_equals_oracle(grid_at, case, dt):
     g = grid_at(5)
     h, u, bt = tc.initialize_fields(g, case)
@@ -21,7 +22,8 @@ def test_fp64_equals_oracle(grid_at, case, dt):
     assert np.array_equal(hg, hr) and np.array_equal(ug, ur)
 
 
-@pytest.mark.parametrize("case,dt", [(1, 900.0), (5, 600.0), (6, 600.0), (21, 600.0)])
+@pytest.mark.parametrize("case,dt", [(1, 900.0), (5, 600.0), (6, 600.0), (21, 600.0), (56, 300.0),
+                                     (57, 1800.0)])
 def test_fp32_close_to_oracle(grid_at, case, dt):
     g = grid_at(5)
     h, u, bt = tc.initialize_fields(g, case)

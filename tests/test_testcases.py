@@ -78,7 +78,58 @@ def test_case6_truncation_error_converges(grid_at):
 
 def test_unknown_case_is_refused(grid_at):
     with pytest.raises(ValueError):
-        tc.initialize_fields(grid_at(2), 56)
+        tc.initialize_fields(grid_at(2), 58)
+    with pytest.raises(ValueError):
+        tc.matsuno_parameters(2)
+
+
+def test_matsuno_dispersion_relation():
+    """Cases 56/57 (swm_matsuno.f90): the three frequencies solve the
+    equatorial beta-plane cubic w^3 - (c^2 k^2 + beta c (2n+1)) w - beta c^2
+    k = 0; the inertia-gravity wave takes the largest, the Rossby wave the
+    smallest in magnitude, with the periods the reference's analysis uses
+    (1.9 and 18.5 days)."""
+    c = np.sqrt(tc.GRAV * tc.MATSUNO_H0)
+    beta = 2.0 * tc.OMEGA / tc.ERAD
+    k = tc.MATSUNO_K / tc.ERAD
+    n = tc.MATSUNO_N
+    A, B = c * c * k * k + beta * c * (2 * n + 1), beta * c * c * k
+    w56 = tc.matsuno_parameters(56)[0]
+    w57 = tc.matsuno_parameters(57)[0]
+    for w in (w56, w57):     # the Rossby root is negative: w = -min |w_nk| is that root
+        # Cardano's form loses a few digits to cancellation on the small root
+        assert abs(w ** 3 - A * w - B) < 1e-5 * (A * abs(w) + B)
+    assert w56 > 0 and w57 < 0
+    assert abs(2 * np.pi / w56 / tc.DAY2SEC - 1.9) < 0.05
+    assert abs(2 * np.pi / -w57 / tc.DAY2SEC - 18.5) < 0.05
+
+
+def test_hermite_functions_are_orthonormal():
+    x = np.linspace(-12.0, 12.0, 24001)
+    dx = x[1] - x[0]
+    hs = [tc.hermite(x, n) for n in range(4)]
+    for i in range(4):
+        for j in range(4):
+            v = np.sum(hs[i] * hs[j] * np.exp(-x * x)) * dx
+            assert abs(v - (1.0 if i == j else 0.0)) < 1e-6
+
+
+@pytest.mark.parametrize("case,dt", [(56, 300.0), (57, 1800.0)])
+def test_matsuno_wave_propagates(grid_at, case, dt):
+    """A quarter period in the oracle at levels 4 and 5: h stays close to the
+    travelling exact wave (persistence would be 141 % off) and the error
+    falls with resolution."""
+    w = tc.matsuno_parameters(case)[0]
+    n = int(round(2 * np.pi / abs(w) / 4 / dt))
+    err = []
+    for level in (4, 5):
+        g = grid_at(level)
+        h0, u0, _ = tc.initialize_fields(g, case)
+        h, _ = oracle.Oracle(g, case).run(h0, u0, dt, n)
+        he, _ = tc.matsuno_fields(g, case, n * dt)
+        a = g.hx_areag
+        err.append(np.sqrt(np.sum(a * (h - he) ** 2) / np.sum(a * (he - tc.MATSUNO_H0) ** 2)))
+    assert err[0] < 0.1 and err[1] < 0.7 * err[0]
 
 
 def test_galewsky_jet(grid_at):
