@@ -730,7 +730,8 @@ int setup_apvm(Handle *H, Work<T> &W, double pvspar, double dt) {
   if (!A.on) return IMODEL_SWM_OK;
   int rc;
   if (!A.qg && ((rc = dalloc(H, &A.qg, 3 * static_cast<size_t>(H->nt))) ||
-                (rc = dalloc(H, &A.vhx, 3 * static_cast<size_t>(H->nv)))))
+                (rc = dalloc(H, &A.vhx, 3 * static_cast<size_t>(H->nv))) ||
+                (rc = dalloc(H, &A.qge, static_cast<size_t>(H->ne)))))
     return rc;
   A.coef = static_cast<T>(pvspar * dt);
   return IMODEL_SWM_OK;

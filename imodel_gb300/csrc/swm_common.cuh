@@ -90,6 +90,7 @@ struct Apvm {
   T coef = T(0);          // pvspar * dt
   T *qg = nullptr;        // [3][nt] Perot reconstruction of grad_tr2ed(q_tr)
   T *vhx = nullptr;       // [3][nv] Perot reconstruction of u at the cells
+  T *qge = nullptr;       // [ne] grad_tr2ed(q_tr) (FP64 step)
 };
 
 // Working fields of one handle, in the handle's precision T.
@@ -147,7 +148,7 @@ inline int launches_per_stage(int precision_fp32, int variant, bool dif_on = fal
                               bool dif_k4 = false, bool apvm_on = false) {
   int n = (precision_fp32 && variant >= 1) ? 3 : 4;
   if (dif_on) n += (dif_k4 ? 3 : 1) + ((precision_fp32 && variant == 0) ? 1 : 0);
-  if (apvm_on) n += 1;
+  if (apvm_on) n += precision_fp32 ? 1 : 2;
   return n;
 }
 // The diffusion coefficients from the cell field kf (device order, FP64;

@@ -71,13 +71,22 @@ __device__ __forceinline__ void proj_sphere(double &v0, double &v1, double &v2, 
   v2 = v2 - vp * p2 / np;
 }
 
+// grad_tr2ed(q_tr) (:1427-1463), the PV gradient across each edge
+__global__ void __launch_bounds__(256) k_qgrad64(DevMesh M, const double *__restrict__ q_tr,
+                                                 double *__restrict__ qge) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ne = M.ne;
+  if (e >= ne) return;
+  double g = M.e_sgtg[e] * (q_tr[M.e_sh[ne + e]] - q_tr[M.e_sh[e]]);
+  qge[e] = g / M.e_dleng[e] / M.erad;
+}
+
 // The two reconstructions apvm (:1465-1543) reads.  Blocks [0, nbt): the
-// PV gradient at the triangles, vector_edtr2tr_perot (:408-452) of
-// grad_tr2ed(q_tr) (:1427-1463), each edge's gradient formed where it is
-// used; dsign(1, tr%nr) = -tr%tg (smeshpack.f90:853-859), the sign of t_lt.
+// PV gradient at the triangles, vector_edtr2tr_perot (:408-452) of qge;
+// dsign(1, tr%nr) = -tr%tg (smeshpack.f90:853-859), the sign of t_lt.
 // The blocks after: the velocity at the cells, vector_edhx2hx_perot
 // (:454-509, HTC, hx%areag); ttgout is the sign of c_sd.
-__global__ void __launch_bounds__(256) k_apvm64(DevMesh M, const double *__restrict__ q_tr,
+__global__ void __launch_bounds__(256) k_apvm64(DevMesh M, const double *__restrict__ qge,
                                                 const double *__restrict__ u,
                                                 double *__restrict__ qg,
                                                 double *__restrict__ vhx, int nbt) {
@@ -91,9 +100,7 @@ __global__ void __launch_bounds__(256) k_apvm64(DevMesh M, const double *__restr
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
       const int ed = M.t_ed[s * nt + t];
-      double g = M.e_sgtg[ed] * (q_tr[M.e_sh[ne + ed]] - q_tr[M.e_sh[ed]]);
-      g = g / M.e_dleng[ed] / M.erad;
-      const double sg = (M.t_lt[s * nt + t] < 0.0 ? 1.0 : -1.0) * g;
+      const double sg = (M.t_lt[s * nt + t] < 0.0 ? 1.0 : -1.0) * qge[ed];
       const double l = M.e_leng[ed];
       v0 = v0 + sg * (M.e_c[ed] - c0) * l;
       v1 = v1 + sg * (M.e_c[ne + ed] - c1) * l;
@@ -695,7 +702,8 @@ void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
   const Apvm<double> &A = W.apvm;
   if (A.on) {
     const int nbt = nblocks(M.nt, 256);
-    k_apvm64<<<nbt + nblocks(M.nv, 256), 256, 0, s>>>(M, W.q_tr, u_in, A.qg, A.vhx, nbt);
+    k_qgrad64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, W.q_tr, A.qge);
+    k_apvm64<<<nbt + nblocks(M.nv, 256), 256, 0, s>>>(M, A.qge, u_in, A.qg, A.vhx, nbt);
   }
   k_edge_pre64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ed, W.uh, W.q_ed,
                                                    A.on ? A.qg : nullptr, A.vhx, A.coef);

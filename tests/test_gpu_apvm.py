@@ -54,7 +54,7 @@ def test_launch_count_and_switching_off(grid_at):
     a = SWM(g, "fp64")
     n0 = a.launch_count(1)
     a.set_apvm(0.5, 600.0)
-    assert a.launch_count(1) == n0 + 4
+    assert a.launch_count(1) == n0 + 8      # edge gradients, reconstructions
     a.set_apvm(0.0, 600.0)
     assert a.launch_count(1) == n0
     ha, ua = a.ode_rk4(h, u, 600.0, 4)
