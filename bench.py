@@ -2,22 +2,30 @@
 """Throughput of the GB300 TRSK shallow-water step (cell-steps/s).
 
 Workload: icosahedral level 9 (2,621,442 cells, 7,864,320 edges,
-5,242,880 triangles), classic RK4, trsk10 / HTC / geodesic areas, seeded
-synthetic state (Williamson case 2 steady flow), dt = 55 s.  One "step" is
-one RK4 time step of the whole grid.
+5,242,880 triangles), classic RK4, trsk10 / HTC / geodesic areas, dt = 55 s,
+from a seeded balanced state (streamfunction of real spherical harmonics of
+degree 1..64 with N(0,1) coefficients times l^-2, seed 0, scaled to a
+40 m/s maximum wind; h from linear balance, mean g h = 2.94e4; flat
+bottom).  One "step" is one RK4 time step of the whole grid.
 
   value      cell-steps/s of the FP32 path with the learned TRSK correction
              (per-edge MLP evaluated once per step on the tensor cores),
              state resident in HBM (graph-replayed steps, CUDA events on the
              library's stream)
   fp32_plain the same without the learned correction
-  fp64       the same for the FP64 reference-order path
+  fp64       the same for the FP64 reference-order path, with its own
+             end-to-end figure
   e2e        cell-steps/s of the headline path through the C ABI call
              imodel_swm_step with pinned host buffers: every step copies h
              and u (FP64) to the device and back inside the timed region
+  error_vs_fp64  relative L2 and max-norm differences of the FP32 and
+             FP32 + learned states from the FP64 state after the same steps
+             from the same start
   roofline   the dominant stencil kernel against the measured HBM copy
              bandwidth; mlp_roofline the network kernel against the
-             measured BF16 tensor throughput
+             measured BF16 tensor throughput; step_roofline the whole step
+             with the layout's own bytes per cell-step beside the 2000 B
+             model
   cpu_baseline  the CPU oracle (C++ restatement of the Fortran, OpenMP on
              all host threads) on a bounded sample of the same workload
 
@@ -46,6 +54,30 @@ METRIC = "SWM cell-steps/s at icos-L9, plain FP64 vs FP32+learned at fixed error
 UNIT = "cell-steps/s"
 LEVEL = 9
 DT = 55.0
+# the seeded balanced state of the workload
+STATE = {"lmax": 64, "seed": 0, "exponent": -2.0, "umax": 40.0, "gh0": 2.94e4}
+STATE_NAME = ("seeded balanced state (SH degree 1..64, l^-2, seed 0, max wind 40 m/s, "
+              "mean gh 2.94e4)")
+
+
+def bench_state(g, workers: int = 0):
+    """The workload's initial (h, u): the spectral synthesis at every cell
+    and edge is split over a spawn process pool (started before any GPU
+    work in this process)."""
+    import multiprocessing as mp
+    from imodel_gb300 import fields
+    n = workers or max(1, os.cpu_count() or 1)
+    with mp.get_context("spawn").Pool(n) as pool:
+        return fields.balanced_state(g, evaluator=fields.PoolEvaluator(pool, chunk=1 << 18),
+                                     **STATE)
+
+
+def rel_errors(x, ref, w):
+    """Relative L2 (weighted as error_calc weights cells and edges) and
+    max-norm difference of x from ref."""
+    d = np.asarray(x, dtype=np.float64) - ref
+    return {"l2": float(np.sqrt(np.sum(w * d * d) / np.sum(w * ref * ref))),
+            "linf": float(np.max(np.abs(d)) / np.max(np.abs(ref)))}
 
 
 # ---------------------------------------------------------------------------
@@ -236,8 +268,8 @@ def load_peaks():
 
 
 def cpu_baseline_sample(grid, h, u, budget_s=15.0, nthreads=0):
-    """Times the CPU oracle on whole RK4 steps of the same grid until about
-    budget_s seconds have passed."""
+    """Times the CPU oracle on whole RK4 steps of the same grid and state
+    until about budget_s seconds have passed."""
     import oracle
     nthreads = nthreads or (os.cpu_count() or 1)
     o = oracle.Oracle(grid, 2, nthreads=nthreads)
@@ -251,21 +283,21 @@ def cpu_baseline_sample(grid, h, u, budget_s=15.0, nthreads=0):
         if el >= budget_s or steps >= 1000:
             break
     return {"value": grid.nv * steps / el, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{steps} RK4 steps of icos-L{grid.level} ({grid.nv} cells) in {el:.1f} s, "
-                      f"C++ oracle, OpenMP {nthreads} threads"}
+            "sample": f"{steps} RK4 steps of icos-L{grid.level} ({grid.nv} cells) from the "
+                      f"workload's state in {el:.1f} s, C++ oracle, OpenMP {nthreads} threads"}
 
 
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    from imodel_gb300 import _build, swm
+    from imodel_gb300 import _build
     from imodel_gb300.mesh import meshbuild
     import oracle
     _build.build_mesh_lib()
     oracle.build()
     g = meshbuild(args.level)
-    h, u = swm.initialize_fields_tc2(g)
+    h, u = bench_state(g)
     nth = os.cpu_count() or 1
     o = oracle.Oracle(g, 2, nthreads=nth)
     hh, uu = h, u
@@ -285,7 +317,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
             "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * el / steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (Williamson case 2 state)",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic: " + STATE_NAME,
             "config": config_dict(g, "fp64"),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
                              "sample": sample},
@@ -301,7 +333,7 @@ def config_dict(g, path, weights=None):
         learned = ("per-edge MLP 24-64-64-1, BF16 tcgen05, once per step; weights " +
                    (weights or "none"))
     return {"workload": f"icos-L{g.level} TRSK shallow-water RK4 step, trsk10/HTC/geo, "
-                        f"dt={DT:g} s, Williamson case 2 state",
+                        f"dt={DT:g} s, {STATE_NAME}",
             "level": g.level, "cells": g.nv, "edges": g.ne, "triangles": g.nt,
             "precision": "fp64" if path == "fp64" else "fp32",
             "learned_correction": learned,
@@ -326,6 +358,14 @@ def load_tflops():
             return float(json.load(f)["bf16_tflops"]), "measured"
     except (OSError, KeyError, ValueError):
         return 1900.0, "fallback"
+
+
+def mlp_bytes(nv, ne, nt):
+    """Algorithmic bytes of one launch of the learned-correction kernel: the
+    11,264-byte index block of every 128-edge tile, u, q_tr and h gathered
+    (each element counted once) and the correction written."""
+    tiles = (ne + 127) // 128
+    return tiles * 11264 + ne * 4 + nt * 4 + nv * 4 + ne * 4
 
 
 def main():
@@ -359,12 +399,14 @@ def main():
     from imodel_gb300 import _build, learned, swm
     from imodel_gb300.mesh import meshbuild
     _build.build_all()
+    g = meshbuild(args.level)
+    # the state is computed by a process pool before this process touches
+    # the GPU
+    h, u = bench_state(g, max(1, (os.cpu_count() or 1) // max(ws, 1)))
     cr = Cudart()
     assert cr.lib.cudaSetDevice(local) == 0
     D = Dist(local)
 
-    g = meshbuild(args.level)
-    h, u = swm.initialize_fields_tc2(g)
     params = learned.trained_params()
     weights = "trained on icos-L7 (imodel_gb300/data/trsk_mlp_l7.npy)"
     if params is None:
@@ -405,11 +447,13 @@ def main():
         D.barrier()
         ms = D.max(ms)
         diag = m.diagnostics()
+        # the state after warmup + steps steps from the common start
+        hf, uf = m.get_state()
         prof = None if args.no_kprof else m.profile(DT, 3)
         results[path] = {"ms": ms, "clocks": clocks, "prof": prof, "diag": diag,
                          "tuning": tuning, "launches": m.launch_count(args.steps),
-                         "main_kernel": m.main_kernel()}
-        if path == headline and not args.no_e2e:
+                         "main_kernel": m.main_kernel(), "h": hf, "u": uf}
+        if (path == headline or path == "fp64") and not args.no_e2e:
             # e2e through the C ABI with pinned host buffers
             ph, hbuf = cr.pinned(g.nv)
             pu, ubuf = cr.pinned(g.ne)
@@ -428,12 +472,12 @@ def main():
             el = time.perf_counter() - t0
             D.barrier()
             el = D.max(el)
-            results["e2e"] = {"s": el, "steps": args.e2e_steps}
+            results[path]["e2e"] = {"s": el, "steps": args.e2e_steps}
             cr.lib.cudaFreeHost(ph)
             cr.lib.cudaFreeHost(pu)
         m.close()
 
-    full = ("fp64" in results and headline in results and "e2e" in results
+    full = ("fp64" in results and headline in results and "e2e" in results[headline]
             and results[headline]["prof"])
     if rank == 0 and not full:
         # profiler runs: a short line with the timed paths only
@@ -446,27 +490,53 @@ def main():
         def rate(r):
             return total_cells * args.steps / (r["ms"] / 1000.0)
 
+        def e2e_line(r):
+            e = r["e2e"]
+            return {"value": total_cells * e["steps"] / e["s"], "unit": UNIT,
+                    "h2d_bytes_per_step": 8 * (g.nv + g.ne),
+                    "d2h_bytes_per_step": 8 * (g.nv + g.ne),
+                    "path": "imodel_swm_step(nsteps=1) with pinned host FP64 h,u"}
+
         peak, peak_kind = load_peaks()
-        kb = kernel_bytes(g.nv, g.ne, g.nt, "fp32", rh["tuning"]["variant"])
+        variant = rh["tuning"]["variant"]
+        kb = kernel_bytes(g.nv, g.ne, g.nt, "fp32", variant)
         prof = {k: v for k, v in rh["prof"].items() if k != "edge_pre" or kb["edge_pre"]}
         dom = max(prof, key=prof.get)
+        if headline == "fp32l":
+            # the profile's edge_pre slot is the network, once per step
+            stencil = {k: v for k, v in prof.items() if k != "edge_pre"}
+            dom = max(stencil, key=stencil.get)
         achieved = kb[dom] / (prof[dom] / 1000.0) / 1e9
-        step_bytes = 2000.0 * g.nv  # per-cell-step algorithmic bytes (FP32 model)
-        step_achieved = step_bytes / (rh["ms"] / args.steps / 1000.0) / 1e9
-        e2e = results["e2e"]
+        # whole-step bytes: the 2000 B/cell-step model and this layout's own
+        # (four stages of the stencil kernels, plus the network once per step)
+        layout_step = 4 * sum(kb.values())
+        if headline == "fp32l":
+            layout_step += mlp_bytes(g.nv, g.ne, g.nt)
+        sec_step = rh["ms"] / args.steps / 1000.0
         kernel_ms = dict(prof)
-        kname = kernel_names(rh["tuning"]["variant"])[dom]
+        kname = kernel_names(variant)[dom]
         traffic = TRAFFIC_PER_CELL[kname] * g.nv if kname in TRAFFIC_PER_CELL else None
+        wc, we = g.hx_areag, g.ed_leng * g.edhx_leng / 2.0
+        err = {}
+        for p in ("fp32", "fp32l"):
+            if p in results:
+                err[p] = {"h": rel_errors(results[p]["h"], r64["h"], wc),
+                          "u": rel_errors(results[p]["u"], r64["u"], we)}
+        err["steps"] = args.warmup + args.steps
+        err["days"] = (args.warmup + args.steps) * DT / 86400.0
+        err["reference"] = "the FP64 path's state after the same steps from the same start"
         line = {
             "metric": METRIC, "value": rate(rh), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": rh["ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic: Williamson case 2 steady zonal flow on the grid (no dataset)",
+            "data": "synthetic: " + STATE_NAME + " (no dataset)",
             "config": dict(config_dict(g, headline, weights), autotuned=rh["tuning"],
                            **({"apvm_pvspar": args.apvm} if args.apvm > 0 else {})),
+            "error_vs_fp64": err,
             "fp64": {"value": rate(r64), "unit": UNIT, "ms_per_step": r64["ms"] / args.steps,
-                     "kernel_ms": r64["prof"]},
+                     "kernel_ms": r64["prof"], "dtype": "f64",
+                     **({"e2e": e2e_line(r64)} if "e2e" in r64 else {})},
             "kernel_ms": kernel_ms,
             "roofline": {"bound": "hbm", "kernel": kname,
                          "achieved": achieved,
@@ -474,12 +544,13 @@ def main():
                          "peak_source": peak_kind, "traffic": traffic,
                          "traffic_source": "ncu capture at icos level 8, scaled by cells",
                          "algorithmic_bytes_per_launch": kb[dom]},
-            "step_roofline": {"bytes_per_cell_step": 2000.0, "achieved": step_achieved,
-                              "peak": peak, "unit": "GB/s", "frac": step_achieved / peak},
-            "e2e": {"value": total_cells * e2e["steps"] / e2e["s"], "unit": UNIT,
-                    "h2d_bytes_per_step": 8 * (g.nv + g.ne),
-                    "d2h_bytes_per_step": 8 * (g.nv + g.ne),
-                    "path": "imodel_swm_step(nsteps=1) with pinned host FP64 h,u"},
+            "step_roofline": {
+                "bytes_per_cell_step_model": 2000.0,
+                "achieved_model": 2000.0 * g.nv / sec_step / 1e9,
+                "bytes_per_cell_step_layout": layout_step / g.nv,
+                "achieved": layout_step / sec_step / 1e9,
+                "peak": peak, "unit": "GB/s", "frac": layout_step / sec_step / 1e9 / peak},
+            "e2e": e2e_line(rh),
             "gpu_launches": rh["launches"],
             "clocks": rh["clocks"],
         }
@@ -495,10 +566,15 @@ def main():
             flop = MLP_FLOP_PER_EDGE * g.ne
             tf, tf_kind = load_tflops()
             ach = flop / (mlp_ms / 1000.0) / 1e12
-            line["mlp_roofline"] = {"bound": "tensor", "kernel": "k_mlp_pipe<EdgeTask>",
-                                    "achieved": ach, "peak": tf, "unit": "TFLOP/s",
-                                    "frac": ach / tf, "peak_source": tf_kind,
-                                    "flop_per_launch": flop}
+            mb = mlp_bytes(g.nv, g.ne, g.nt)
+            line["mlp_roofline"] = {"bound": "hbm", "kernel": "k_mlp_pipe<EdgeTask>",
+                                    "achieved": mb / (mlp_ms / 1000.0) / 1e9, "peak": peak,
+                                    "unit": "GB/s",
+                                    "frac": mb / (mlp_ms / 1000.0) / 1e9 / peak,
+                                    "algorithmic_bytes_per_launch": mb,
+                                    "tensor": {"achieved": ach, "peak": tf, "unit": "TFLOP/s",
+                                               "frac": ach / tf, "peak_source": tf_kind,
+                                               "flop_per_launch": flop}}
             line["learned_active_after_run"] = bool(rh["diag"]["learned_active"])
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_sample(g, h, u, args.cpu_budget)

@@ -6,6 +6,7 @@
 #include <cuda.h>  // pointer-attribute types only; the driver call is resolved at run time
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -105,9 +106,20 @@ int upload(Handle *H, const std::vector<V> &v, const V **dst) {
   return IMODEL_SWM_OK;
 }
 
+// host-side allocation-failure injection for tests: when > 0, the
+// allocation that brings the count to zero fails as if the device were full
+std::atomic<int> g_fail_alloc_after{0};
+
 template <class T>
 int dalloc(Handle *H, T **p, size_t n) {
   void *q = nullptr;
+  int after = g_fail_alloc_after.load();
+  while (after > 0 && !g_fail_alloc_after.compare_exchange_weak(after, after - 1)) {
+  }
+  if (after == 1) {
+    H->err = "cudaMalloc: out of memory (injected by imodel_swm_test_fail_alloc)";
+    return IMODEL_SWM_ENOMEM;
+  }
   CK(cudaMalloc(&q, (n > 0 ? n : 1) * sizeof(T)));
   H->allocs.push_back(q);
   CK(cudaMemset(q, 0, (n > 0 ? n : 1) * sizeof(T)));
@@ -681,14 +693,20 @@ template <class T>
 int setup_diffusion(Handle *H, Work<T> &W, double k2, double k4, const double *kf2,
                     const double *kf4) {
   Diffusion<T> &D = W.dif;
-  D.k2 = k2 > 0 || kf2;
-  D.k4 = k4 > 0 || kf4;
-  D.on = D.k2 || D.k4;
-  if (!D.on) return IMODEL_SWM_OK;
+  // the terms stay off until every buffer and coefficient is in place: a
+  // failure below leaves the handle stepping without diffusion
+  D.on = false;
+  const bool k2on = k2 > 0 || kf2, k4on = k4 > 0 || kf4;
+  if (!k2on && !k4on) {
+    D.k2 = D.k4 = false;
+    return IMODEL_SWM_OK;
+  }
   int rc;
-  if (!D.kt && ((rc = dalloc(H, &D.kt, H->nt)) || (rc = dalloc(H, &D.kcv, H->nv)) ||
-                (rc = dalloc(H, &D.coefdiv, H->nv)) || (rc = dalloc(H, &D.coefvort, H->nt)) ||
-                (rc = dalloc(H, &D.lap, H->ne)) || (rc = dalloc(H, &D.lap2, H->ne))))
+  // each buffer on its own, so that a call after a failed one completes the set
+  if ((!D.kt && (rc = dalloc(H, &D.kt, H->nt))) || (!D.kcv && (rc = dalloc(H, &D.kcv, H->nv))) ||
+      (!D.coefdiv && (rc = dalloc(H, &D.coefdiv, H->nv))) ||
+      (!D.coefvort && (rc = dalloc(H, &D.coefvort, H->nt))) ||
+      (!D.lap && (rc = dalloc(H, &D.lap, H->ne))) || (!D.lap2 && (rc = dalloc(H, &D.lap2, H->ne))))
     return rc;
   double *kt64 = nullptr, *kc64 = nullptr;
   float *kt32 = nullptr, *kc32 = nullptr;
@@ -696,7 +714,8 @@ int setup_diffusion(Handle *H, Work<T> &W, double k2, double k4, const double *k
     kt64 = reinterpret_cast<double *>(D.kt);
     kc64 = reinterpret_cast<double *>(D.kcv);
   } else {
-    if (!H->d_kt64 && ((rc = dalloc(H, &H->d_kt64, H->nt)) || (rc = dalloc(H, &H->d_kc64, H->nv))))
+    if ((!H->d_kt64 && (rc = dalloc(H, &H->d_kt64, H->nt))) ||
+        (!H->d_kc64 && (rc = dalloc(H, &H->d_kc64, H->nv))))
       return rc;
     kt64 = H->d_kt64;
     kc64 = H->d_kc64;
@@ -706,7 +725,7 @@ int setup_diffusion(Handle *H, Work<T> &W, double k2, double k4, const double *k
   // swm.f90:169-205: K at the cells, hx2tr(K) at the triangles;
   // hyperdiffusion applies the Laplacian twice with sqrt(K4) and
   // sqrt(hx2tr(K4)), and then also replaces the Laplacian's coefficients
-  const double *kf = D.k4 ? kf4 : kf2;
+  const double *kf = k4on ? kf4 : kf2;
   double *kf_dev = nullptr;
   if (kf) {
     const size_t nv = static_cast<size_t>(H->nv);
@@ -715,9 +734,12 @@ int setup_diffusion(Handle *H, Work<T> &W, double k2, double k4, const double *k
     launch_gather_in(H->nv, H->d_cell_n2o, H->d_kf, H->d_kf + nv, 0.0, H->stream);
     kf_dev = H->d_kf + nv;
   }
-  launch_dif_coefs(H->M, kf_dev, D.k4 ? k4 : k2, D.k4, kc64, kc32, kt64, kt32, H->stream);
+  launch_dif_coefs(H->M, kf_dev, k4on ? k4 : k2, k4on, kc64, kc32, kt64, kt32, H->stream);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(H->stream));
+  D.k2 = k2on;
+  D.k4 = k4on;
+  D.on = true;
   return IMODEL_SWM_OK;
 }
 // the anticipated potential vorticity method (apvm, swm_operators.f90:
@@ -726,14 +748,17 @@ int setup_diffusion(Handle *H, Work<T> &W, double k2, double k4, const double *k
 template <class T>
 int setup_apvm(Handle *H, Work<T> &W, double pvspar, double dt) {
   Apvm<T> &A = W.apvm;
-  A.on = pvspar > 0;
-  if (!A.on) return IMODEL_SWM_OK;
+  // off until all three buffers exist: a failed allocation leaves the handle
+  // stepping without APVM instead of launching through a null buffer
+  A.on = false;
+  if (!(pvspar > 0)) return IMODEL_SWM_OK;
   int rc;
-  if (!A.qg && ((rc = dalloc(H, &A.qg, 3 * static_cast<size_t>(H->nt))) ||
-                (rc = dalloc(H, &A.vhx, 3 * static_cast<size_t>(H->nv))) ||
-                (rc = dalloc(H, &A.qge, static_cast<size_t>(H->ne)))))
+  if ((!A.qg && (rc = dalloc(H, &A.qg, 3 * static_cast<size_t>(H->nt)))) ||
+      (!A.vhx && (rc = dalloc(H, &A.vhx, 3 * static_cast<size_t>(H->nv)))) ||
+      (!A.qge && (rc = dalloc(H, &A.qge, static_cast<size_t>(H->ne)))))
     return rc;
   A.coef = static_cast<T>(pvspar * dt);
+  A.on = true;
   return IMODEL_SWM_OK;
 }
 }  // namespace
@@ -1150,12 +1175,13 @@ int imodel_swm_set_diffusion(void *handle, double k2, double k4) {
   const int rc = H->precision == IMODEL_SWM_FP64
                      ? imodel::setup_diffusion(H, H->W64, k2, k4, nullptr, nullptr)
                      : imodel::setup_diffusion(H, H->W32, k2, k4, nullptr, nullptr);
-  if (rc) return rc;
+  // the captured step no longer matches the options, whether or not the
+  // set-up succeeded (a failure leaves the terms off)
   if (H->graph) {
     cudaGraphExecDestroy(H->graph);
     H->graph = nullptr;
   }
-  return IMODEL_SWM_OK;
+  return rc;
 }
 
 int imodel_swm_set_diffusion_fields(void *handle, const double *k2_hx, const double *k4_hx) {
@@ -1174,11 +1200,16 @@ int imodel_swm_set_diffusion_fields(void *handle, const double *k2_hx, const dou
   const int rc = H->precision == IMODEL_SWM_FP64
                      ? imodel::setup_diffusion(H, H->W64, 0.0, 0.0, k2_hx, k4_hx)
                      : imodel::setup_diffusion(H, H->W32, 0.0, 0.0, k2_hx, k4_hx);
-  if (rc) return rc;
   if (H->graph) {
     cudaGraphExecDestroy(H->graph);
     H->graph = nullptr;
   }
+  return rc;
+}
+
+int imodel_swm_test_fail_alloc(int32_t after) {
+  if (after < 0) return IMODEL_SWM_EINVAL;
+  imodel::g_fail_alloc_after.store(after);
   return IMODEL_SWM_OK;
 }
 
@@ -1199,14 +1230,13 @@ int imodel_swm_set_apvm(void *handle, double pvspar, double dt) {
   if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
   const int rc = fp32 ? imodel::setup_apvm(H, H->W32, pvspar, dt)
                       : imodel::setup_apvm(H, H->W64, pvspar, dt);
-  if (rc) return rc;
   // FP32: the correction is applied in the edge pre-pass of variant 0
-  if (fp32 && pvspar > 0) H->W32.tune.variant = 0;
+  if (!rc && fp32 && pvspar > 0) H->W32.tune.variant = 0;
   if (H->graph) {
     cudaGraphExecDestroy(H->graph);
     H->graph = nullptr;
   }
-  return IMODEL_SWM_OK;
+  return rc;
 }
 
 int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count) {

@@ -5,6 +5,7 @@
 // file-scope __device__ array instead of a buffer the caller's handle
 // allocated.  Compiled with --fmad=false: the compensation terms rely on each
 // product being rounded on its own.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -26,6 +27,12 @@ constexpr int kMaxDevices = 64;
 // exits.  Each launch overwrites every partial it later reads, so nothing in
 // it has to start at zero; it keeps the last call's partials.
 __device__ __align__(256) double g_partials[kQ * kMaxBlocks * 2];
+
+// max that keeps a NaN: fmax alone returns the other operand when one is NaN,
+// so a field holding NaN would report a finite maximum
+__device__ __forceinline__ double nanmax(double a, double b) {
+  return (a != a || b != b) ? a + b : fmax(a, b);
+}
 
 struct KSum {
   double s, c;
@@ -57,7 +64,7 @@ __global__ void __launch_bounds__(kThreads) k_wsum_partials(const double *__rest
       a[0].add(wi);
       a[1].add(wi * fi);
       a[2].add(wi * (fi * fi));
-      mx = fmax(mx, fabs(fi));
+      mx = nanmax(mx, fabs(fi));
     }
   }
   for (int off = 16; off > 0; off >>= 1) {
@@ -66,7 +73,7 @@ __global__ void __launch_bounds__(kThreads) k_wsum_partials(const double *__rest
       const double oc = __shfl_down_sync(0xffffffffu, a[q].c, off);
       a[q].merge(os, oc);
     }
-    mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    mx = nanmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
   }
   __shared__ double sh[kThreads / 32][kQ][2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -87,7 +94,7 @@ __global__ void __launch_bounds__(kThreads) k_wsum_partials(const double *__rest
       if (q < 3)
         t.merge(sh[wv][q][0], sh[wv][q][1]);
       else
-        m = fmax(m, sh[wv][q][0]);
+        m = nanmax(m, sh[wv][q][0]);
     }
     const size_t slot = (static_cast<size_t>(q) * kMaxBlocks + blockIdx.x) * 2;
     partials[slot] = q < 3 ? t.s : m;
@@ -107,7 +114,7 @@ __global__ void __launch_bounds__(kThreads) k_wsum_final(const double *__restric
     if (q < 3)
       a.merge(partials[slot], partials[slot + 1]);
     else
-      m = fmax(m, partials[slot]);
+      m = nanmax(m, partials[slot]);
   }
   ss[threadIdx.x] = q < 3 ? a.s : m;
   sc[threadIdx.x] = q < 3 ? a.c : 0.0;
@@ -119,15 +126,35 @@ __global__ void __launch_bounds__(kThreads) k_wsum_final(const double *__restric
       out[q] = r.s + r.c;
     } else {
       double r = 0.0;
-      for (int t = 0; t < kThreads; ++t) r = fmax(r, ss[t]);
+      for (int t = 0; t < kThreads; ++t) r = nanmax(r, ss[t]);
       out[q] = r;
     }
   }
 }
 
-// device address of g_partials, looked up once per device
-double *g_partials_addr[kMaxDevices] = {};
+// device address of g_partials per device, with the context it was looked up
+// in: a caller that makes another context current on the device (or resets
+// the device) gets the address looked up again
+struct PartialsAddr {
+  CUcontext ctx;
+  double *addr;
+};
+PartialsAddr g_partials_addr[kMaxDevices] = {};
 std::mutex g_partials_mu;
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult qr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &qr) !=
+            cudaSuccess ||
+        qr != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(p);
+  }();
+  return fn;
+}
 
 }  // namespace
 
@@ -138,22 +165,41 @@ extern "C" int imodel_swm_weighted_sums_noalloc(const double *w, const double *f
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess) return IMODEL_SWM_ENODEV;
   if (dev < 0 || dev >= kMaxDevices) return IMODEL_SWM_EINVAL;
+  // the current context (null before the runtime first touches the device;
+  // cudaGetSymbolAddress below then makes the primary context current)
+  CtxGetCurrentFn get_ctx = ctx_get_current();
+  CUcontext ctx = nullptr;
+  if (get_ctx && get_ctx(&ctx) != CUDA_SUCCESS) return IMODEL_SWM_ECUDA;
   double *partials = nullptr;
   {
-    // first call on this device: host code may not use g_partials itself (it
-    // names a host-side stand-in), so ask the runtime for its device address
+    // first call on this device (or in this context): host code may not use
+    // g_partials itself (it names a host-side stand-in), so ask the runtime
+    // for its device address
     std::lock_guard<std::mutex> lock(g_partials_mu);
-    if (!g_partials_addr[dev]) {
+    PartialsAddr &slot = g_partials_addr[dev];
+    if (!slot.addr || (ctx && slot.ctx != ctx)) {
       void *p = nullptr;
       if (cudaGetSymbolAddress(&p, g_partials) != cudaSuccess || !p) return IMODEL_SWM_ECUDA;
-      g_partials_addr[dev] = static_cast<double *>(p);
+      if (get_ctx && !ctx && get_ctx(&ctx) != CUDA_SUCCESS) return IMODEL_SWM_ECUDA;
+      slot.addr = static_cast<double *>(p);
+      slot.ctx = ctx;
     }
-    partials = g_partials_addr[dev];
+    partials = slot.addr;
   }
   const int nblk = static_cast<int>((n + static_cast<int64_t>(kThreads) * kItems - 1) /
                                     (static_cast<int64_t>(kThreads) * kItems));
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  k_wsum_partials<<<nblk, kThreads, 0, s>>>(w, f, n, partials);
-  k_wsum_final<<<kQ, kThreads, 0, s>>>(partials, nblk, out);
-  return cudaGetLastError() == cudaSuccess ? IMODEL_SWM_OK : IMODEL_SWM_ECUDA;
+  // launched through cudaLaunchKernel so that each launch's own status is
+  // returned: cudaGetLastError would also report (and clear) an error the
+  // caller left pending before this call
+  void *a1[] = {&w, &f, &n, &partials};
+  if (cudaLaunchKernel(reinterpret_cast<const void *>(k_wsum_partials), dim3(nblk),
+                       dim3(kThreads), a1, 0, s) != cudaSuccess)
+    return IMODEL_SWM_ECUDA;
+  int nb = nblk;
+  void *a2[] = {&partials, &nb, &out};
+  if (cudaLaunchKernel(reinterpret_cast<const void *>(k_wsum_final), dim3(kQ), dim3(kThreads), a2,
+                       0, s) != cudaSuccess)
+    return IMODEL_SWM_ECUDA;
+  return IMODEL_SWM_OK;
 }

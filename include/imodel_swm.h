@@ -216,6 +216,12 @@ int imodel_swm_set_diffusion_fields(void *handle, const double *k2_hx, const dou
  * correction refuses APVM (IMODEL_SWM_EINVAL).  Needs the mesh's ed_nr and
  * ed_c.  May be called at any time; applies from the next step. */
 int imodel_swm_set_apvm(void *handle, double pvspar, double dt);
+/* Test hook with no counterpart in the reference: when after > 0, the
+ * after-th device allocation made by any handle from now on fails with
+ * IMODEL_SWM_ENOMEM as if the device were full (0 switches the injection
+ * off).  It lets tests check that a failed set-up (set_apvm,
+ * set_diffusion*) leaves the handle stepping correctly without the option. */
+int imodel_swm_test_fail_alloc(int32_t after);
 /* Launches issued by one advance call for nsteps steps (kernels only). */
 int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count);
 /* Runs nsteps RK4 steps kernel by kernel (no graph) with CUDA events around
@@ -263,23 +269,26 @@ void *imodel_swm_ensemble_stream(void *ens);
  * in the reference: it is the compensated reduction behind
  * imodel_swm_diagnostics (sumf_areas / sumfsq_areas) for callers that cannot
  * call cudaMalloc -- a host whose device memory is all handed out by another
- * runtime's pool, code running inside a CUDA stream capture (where an
- * allocation would break the capture), or a plugin that may only touch the
- * buffers its caller gives it.  Instead of a handle's buffer it uses a
- * 256 KiB block-partials array built into the library (every GPU that loads
- * the library keeps it until the process exits).
+ * runtime's pool, or a plugin that may only touch the buffers its caller
+ * gives it.  Instead of a handle's buffer it uses a 256 KiB block-partials
+ * array built into the library (every GPU that loads the library keeps it
+ * until the process exits).
  *
  * w, f: device arrays of n doubles (weights, field); out: device array of 4
  * doubles receiving {sum w, sum w*f, sum w*f^2, max |f|}, the sums
- * Neumaier-compensated.  stream: a cudaStream_t (NULL = legacy default
- * stream); the call only enqueues work, out is valid once the stream reaches
- * it.  n may be at most 33,554,432 (4096 blocks x 256 threads x 32 elements);
- * a longer input returns IMODEL_SWM_ETOOBIG and launches nothing.  Runs on the
- * current device.  Its first call on a device looks up the array's device
- * address (cudaGetSymbolAddress), so make that first call before any stream
- * capture.  All calls share the one array: calls whose work overlaps on the
- * GPU (different streams, or different host threads on one device) race and
- * must be serialised by the caller. */
+ * Neumaier-compensated; a NaN in f makes the maximum NaN as well as the sums.
+ * stream: a cudaStream_t (NULL = legacy default stream); the call only
+ * enqueues work, out is valid once the stream reaches it.  n may be at most
+ * 33,554,432 (4096 blocks x 256 threads x 32 elements); a longer input
+ * returns IMODEL_SWM_ETOOBIG and launches nothing.  Runs on the current
+ * device.  Its first call on a device (and its first call after another
+ * context was made current there) looks up the array's device address
+ * (cudaGetSymbolAddress) before it launches anything.  All calls share the
+ * one array, and each call overwrites the partials it reads: calls whose work
+ * overlaps on the GPU (different streams, or different host threads on one
+ * device) race and must be serialised by the caller.  IMODEL_SWM_ECUDA
+ * reports a failed launch of this call only; an error the caller left
+ * pending in the runtime is neither reported nor cleared. */
 int imodel_swm_weighted_sums_noalloc(const double *w, const double *f, int64_t n, double *out,
                                      void *stream);
 

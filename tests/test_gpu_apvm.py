@@ -99,3 +99,51 @@ def test_refusals(grid_at):
         with pytest.raises(SWMError) as ei:
             d.set_apvm(pv, dt)
         assert ei.value.code == _capi.EINVAL
+
+
+@pytest.mark.parametrize("fail_at", [1, 2, 3])
+def test_failed_allocation_leaves_apvm_off(grid_at, fail_at):
+    """An allocation that fails inside set_apvm (injected on the host) returns
+    ENOMEM and leaves APVM off: the next steps equal the plain oracle's, and a
+    later set_apvm completes the buffers and equals the APVM oracle."""
+    g = grid_at(4)
+    h, u = fields.balanced_state(g, lmax=12, seed=14)
+    dt = 600.0
+    m = SWM(g, "fp64")
+    lib = _capi.swm_lib()
+    assert lib.imodel_swm_test_fail_alloc(fail_at) == 0
+    try:
+        with pytest.raises(SWMError) as e:
+            m.set_apvm(0.5, dt)
+        assert e.value.code == _capi.ENOMEM
+    finally:
+        lib.imodel_swm_test_fail_alloc(0)
+    hg, ug = m.ode_rk4(h, u, dt, 3)
+    hr, ur = oracle.Oracle(g, 2).run(h, u, dt, 3)
+    assert np.array_equal(hg, hr) and np.array_equal(ug, ur)
+    m.set_apvm(0.5, dt)
+    hg, ug = m.ode_rk4(h, u, dt, 3)
+    hr, ur = oracle.Oracle(g, 2, pvspar=0.5, dt=dt).run(h, u, dt, 3)
+    assert np.array_equal(hg, hr) and np.array_equal(ug, ur)
+
+
+def test_failed_allocation_leaves_diffusion_off(grid_at):
+    g = grid_at(4)
+    h, u = fields.balanced_state(g, lmax=12, seed=15)
+    dt = 600.0
+    m = SWM(g, "fp64")
+    lib = _capi.swm_lib()
+    assert lib.imodel_swm_test_fail_alloc(4) == 0
+    try:
+        with pytest.raises(SWMError) as e:
+            m.set_diffusion(1.0e5, 0.0)
+        assert e.value.code == _capi.ENOMEM
+    finally:
+        lib.imodel_swm_test_fail_alloc(0)
+    hg, ug = m.ode_rk4(h, u, dt, 2)
+    hr, ur = oracle.Oracle(g, 2).run(h, u, dt, 2)
+    assert np.array_equal(hg, hr) and np.array_equal(ug, ur)
+    m.set_diffusion(1.0e5, 0.0)
+    hg, ug = m.ode_rk4(h, u, dt, 2)
+    hr, ur = oracle.Oracle(g, 2, k2=1.0e5).run(h, u, dt, 2)
+    assert np.array_equal(hg, hr) and np.array_equal(ug, ur)

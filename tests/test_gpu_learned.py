@@ -26,7 +26,9 @@ def test_forward_matches_oracle(n):
     yr, _ = mo.forward(p, x)
     err = np.max(np.abs(y - yr)) / np.max(np.abs(yr))
     print(f"forward n={n}: max |y - y_oracle| / max |y| = {err:.2e}")
-    assert err < 1e-2
+    # measured 2.1e-4 (n = 128) and 3.4e-4 (n = 1000) on a GB300: the
+    # tensor cores and the oracle sum the FP32 products in different orders
+    assert err < 3e-3
     assert np.mean(np.abs(y - yr)) < 1e-3 * np.mean(np.abs(yr)) + 1e-6
 
 
@@ -40,12 +42,14 @@ def test_gradient_matches_oracle(batch, weighted):
     lr_, gr = mo.loss_and_grad(p, x, t, w)
     rel = np.linalg.norm(g - gr) / np.linalg.norm(gr)
     print(f"gradient batch={batch}: loss {loss:.6f} vs {lr_:.6f}, relative L2 {rel:.2e}")
-    assert abs(loss - lr_) <= 1e-3 * lr_
-    assert rel < 1e-2
+    assert abs(loss - lr_) <= 1e-4 * lr_
+    # measured 4.1e-4, 1.7e-4, 6.3e-5 for the three batches on a GB300
+    assert rel < 4e-3
     P, G = mo.unpack(g), mo.unpack(gr)
     for name in ("W1", "b1", "W2", "b2", "w3", "b3"):
         r = np.linalg.norm(P[name] - G[name]) / (np.linalg.norm(G[name]) + 1e-30)
-        assert r < 2e-2, (name, r)
+        print(f"  {name}: relative L2 {r:.2e}")
+        assert r < 8e-3, (name, r)
 
 
 def test_adam_training_reduces_loss():

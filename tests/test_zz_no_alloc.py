@@ -1,8 +1,8 @@
 """The allocation-free weighted sums against the allocating diagnostics.
 
 imodel_swm_weighted_sums_noalloc serves callers that cannot call cudaMalloc
-(a host whose device memory belongs to another runtime's pool, code inside a
-CUDA stream capture, a plugin restricted to its caller's buffers): its block
+(a host whose device memory belongs to another runtime's pool, a plugin
+restricted to its caller's buffers): its block
 partials live in a fixed array built into the library.  Here it is called
 through the C ABI on device arrays and must agree with what
 imodel_swm_diagnostics and imodel_swm_errors (which reduce into a buffer
@@ -77,6 +77,29 @@ def test_noalloc_sums_match_diagnostics(grid_at):
             assert abs(pe - d["penergy"]) <= RTOL * abs(d["penergy"]), (call, pe, d["penergy"])
             assert abs(l2 - e["error2_h"]) <= RTOL * e["error2_h"], (call, l2, e["error2_h"])
             assert fmax == e["errormax_h"], (call, fmax, e["errormax_h"])
+    finally:
+        for p in (w, f, out):
+            rt.cudaFree(p)
+
+
+def test_noalloc_max_keeps_nan(grid_at):
+    """A NaN in the field makes the maximum NaN too (not a finite value)."""
+    g = grid_at(4)
+    lib = _capi.swm_lib()
+    rt = _cudart()
+    f_host = np.linspace(-2.0, 3.0, g.nv)
+    f_host[g.nv // 3] = np.nan
+    w = _device_copy(rt, np.ascontiguousarray(g.hx_areag, dtype=np.float64))
+    f = _device_copy(rt, f_host)
+    out = ctypes.c_void_p()
+    assert rt.cudaMalloc(ctypes.byref(out), 32) == 0
+    host = np.zeros(4)
+    try:
+        assert lib.imodel_swm_weighted_sums_noalloc(w, f, g.nv, out, None) == 0
+        assert rt.cudaDeviceSynchronize() == 0
+        assert rt.cudaMemcpy(host.ctypes.data, out, 32, D2H) == 0
+        assert abs(host[0] - 4 * np.pi) < 1e-12
+        assert np.isnan(host[1]) and np.isnan(host[3])
     finally:
         for p in (w, f, out):
             rt.cudaFree(p)
