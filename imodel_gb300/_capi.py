@@ -28,6 +28,9 @@ ETOOBIG = 8
 
 FP64 = 0
 FP32 = 1
+# method wrappers (swm_data.f90:446-507); "dtred" is mtdwrapper "none" with
+# coriolis_reconmtd = dtred
+SCHEMES = {"trsk10": 0, "pxt16": 1, "gass18": 2, "dtred": 3}
 
 STATUS_NAMES = {
     OK: "OK", EINVAL: "EINVAL", ECUDA: "ECUDA", EBLOWUP: "EBLOWUP",
@@ -73,6 +76,7 @@ class Opts(ctypes.Structure):
         ("bt", c_f64p), ("h_ref", ctypes.c_double), ("device", ctypes.c_int32),
         ("learned", ctypes.c_int32), ("mlp_weights", ctypes.c_void_p),
         ("mlp_bytes", ctypes.c_size_t), ("drift_bound", ctypes.c_double),
+        ("scheme", ctypes.c_int32),
     ]
 
 

@@ -542,8 +542,13 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
     return set_error(H, IMODEL_SWM_ENODEV, "no CUDA device");
   if (H->device < 0 || H->device >= ndev) return set_error(H, IMODEL_SWM_EINVAL, "bad device ordinal");
   CK(cudaSetDevice(H->device));
+  const int scheme = o ? o->scheme : IMODEL_SWM_TRSK10;
+  if (scheme < IMODEL_SWM_TRSK10 || scheme > IMODEL_SWM_DTRED)
+    return set_error(H, IMODEL_SWM_EINVAL, "unknown scheme");
+  if (scheme != IMODEL_SWM_TRSK10 && H->precision != IMODEL_SWM_FP64)
+    return set_error(H, IMODEL_SWM_EINVAL, "the pxt16, gass18 and dtred schemes run on FP64 handles");
   Layout L;
-  std::string msg = build_layout(*m, o ? o->bt : nullptr, L);
+  std::string msg = build_layout(*m, o ? o->bt : nullptr, L, scheme);
   if (!msg.empty()) return set_error(H, IMODEL_SWM_EINVAL, msg);
   H->nv = L.nv;
   H->ne = L.ne;
@@ -629,6 +634,11 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
         (rc = upload(H, L.c_p, &M.c_p)))
       return rc;
   }
+  // the other method wrappers' geometry (empty vectors upload as NULL)
+  if ((rc = upload(H, L.t_bary, &M.t_bary)) || (rc = upload(H, L.e_dist, &M.e_dist)) ||
+      (rc = upload(H, L.t_edarea, &M.t_edarea)) || (rc = upload(H, L.e_nr, &M.e_nr)) ||
+      (rc = upload(H, L.e_stq, &M.e_stq)))
+    return rc;
   if (H->precision == IMODEL_SWM_FP32 && !L.t_apw32.empty()) {
     if ((rc = upload(H, L.t_apw32, &M.t_apw32)) || (rc = upload(H, L.t_cc32, &M.t_cc32)) ||
         (rc = upload(H, L.c_apw32, &M.c_apw32)) || (rc = upload(H, L.c_p32, &M.c_p32)))
@@ -660,6 +670,12 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
     if (o && o->learned)
       return set_error(H, IMODEL_SWM_EINVAL, "the learned correction needs the FP32 path");
     if ((rc = alloc_work(H, H->W64))) return rc;
+    H->W64.scheme = scheme;
+    if (scheme == IMODEL_SWM_GASS18 &&
+        ((rc = dalloc(H, &H->W64.eta_t, L.nt)) || (rc = dalloc(H, &H->W64.h_trs, L.nt))))
+      return rc;
+    if (scheme == IMODEL_SWM_DTRED && (rc = dalloc(H, &H->W64.vhq, 3 * static_cast<size_t>(L.nt))))
+      return rc;
   } else {
     const float keep = H->W32.h_ref;
     if ((rc = alloc_work(H, H->W32))) return rc;
@@ -1247,7 +1263,8 @@ int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count) {
   const bool k4 = fp32 ? H->W32.dif.k4 : H->W64.dif.k4;
   *count = static_cast<int64_t>(nsteps) * 4 *
            imodel::launches_per_stage(fp32, fp32 ? H->W32.tune.variant : 0, on, k4,
-                                      fp32 ? H->W32.apvm.on : H->W64.apvm.on);
+                                      fp32 ? H->W32.apvm.on : H->W64.apvm.on,
+                                      fp32 ? 0 : H->W64.scheme);
   // the learned correction adds one network launch per step while it is on
   if (fp32 && H->W32.learned) *count += nsteps;
   return IMODEL_SWM_OK;
@@ -1256,7 +1273,9 @@ int imodel_swm_launch_count(void *handle, int32_t nsteps, int64_t *count) {
 const char *imodel_swm_main_kernel(void *handle) {
   Handle *H = static_cast<Handle *>(handle);
   if (!H) return "";
-  if (H->precision == IMODEL_SWM_FP64) return "k_edge64";
+  if (H->precision == IMODEL_SWM_FP64)
+    return H->W64.scheme == IMODEL_SWM_PXT16 || H->W64.scheme == IMODEL_SWM_DTRED ? "k_edge64r"
+                                                                                  : "k_edge64";
   const int v = H->W32.tune.variant;
   return v >= 1 ? "k_cell32v2" : "k_edge32";
 }

@@ -51,6 +51,12 @@ struct DevMesh {
   const double *e_c, *t_c, *c_p;
   // the FP32 step's APVM weights and projection vectors (swm_layout.h)
   const float *t_apw32, *t_cc32, *c_apw32, *c_p32;
+  // geometry of the pxt16, gass18 and dtred method wrappers (FP64, NULL
+  // for trsk10; swm_layout.h): barycentric weights [3][nt], circumcentre
+  // distances [2][ne], edge areas [3][nt], connecting edges [10][ne], ed%nr
+  // [3][ne]
+  const double *t_bary, *e_dist, *t_edarea, *e_nr;
+  const int32_t *e_stq;
 };
 
 // Launch configuration of the FP32 stage kernels, chosen by the autotuner.
@@ -110,6 +116,10 @@ struct Work {
   Apvm<T> apvm;
   Tune tune;
   int *flags;        // bit 0: PV division by ~0
+  // method wrapper (IMODEL_SWM_TRSK10 ... IMODEL_SWM_DTRED; FP64 handles)
+  int scheme = 0;
+  T *eta_t = nullptr, *h_trs = nullptr;  // [nt] gass18: eta and h_tr for the rhombus PV
+  T *vhq = nullptr;                      // [3][nt] dtred: Perot reconstruction of uh, times q
   T h_ref;           // FP32: h is stored as h - h_ref
   int pv_on;         // testcase >= 2: q = eta / h_tr, else q = 0
   int mom_on;        // testcase >= 2: momentum tendency kept, else zeroed
@@ -145,8 +155,9 @@ void learned_launch(const DevMesh &M, const LearnedDev &L, const float *hd, cons
 // (1 launch, 3 with hyperdiffusion) and, for FP32 variant 0, a first pass of
 // K div u and K_tr zeta (1 launch)
 inline int launches_per_stage(int precision_fp32, int variant, bool dif_on = false,
-                              bool dif_k4 = false, bool apvm_on = false) {
+                              bool dif_k4 = false, bool apvm_on = false, int scheme = 0) {
   int n = (precision_fp32 && variant >= 1) ? 3 : 4;
+  if (scheme == 3) n += 1;  // dtred: the triangle reconstruction of uh q
   if (dif_on) n += (dif_k4 ? 3 : 1) + ((precision_fp32 && variant == 0) ? 1 : 0);
   if (apvm_on) n += precision_fp32 ? 1 : 2;
   return n;

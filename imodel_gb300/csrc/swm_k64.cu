@@ -5,6 +5,7 @@
 // below is rounded on its own, as in the Fortran built without contraction,
 // so that the FP64 step reproduces the reference arithmetic of
 // src/swm.f90:2416-2683 and src/swm_operators.f90 bit for bit.
+#include "imodel_swm.h"
 #include "swm_common.cuh"
 
 namespace imodel {
@@ -29,12 +30,18 @@ __device__ __forceinline__ T rk_stage(int stage, T k, T yn, T *acc, T dt) {
   return yn + dt * (*acc + k) / T(6);
 }
 
-// vort_tr (:551-611) + scalar_hx2tr (:229-284) + scalar_elem_divide (:1579)
+// vort_tr (:551-611) + scalar_hx2tr (:229-284) + scalar_elem_divide (:1579);
+// the depth at the triangle by the scheme's interpolation (swm.f90:2459-2464):
+// kite areas (trsk), barycentric weights of the circumcentre (bary, pxt16) or
+// scalar_edtr2trcc of h_ed (:286-343, gass18, which also keeps eta and h_tr
+// for the rhombus PV)
 __global__ void __launch_bounds__(256) k_tri64(DevMesh M, const double *__restrict__ h,
                                                const double *__restrict__ u,
                                                double *__restrict__ q_tr, int pv_on,
                                                int *flags, const double *__restrict__ kt,
-                                               double *__restrict__ coefvort) {
+                                               double *__restrict__ coefvort, int scheme,
+                                               double *__restrict__ eta_t,
+                                               double *__restrict__ h_trs) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = M.nt;
   if (t >= nt) return;
@@ -48,9 +55,25 @@ __global__ void __launch_bounds__(256) k_tri64(DevMesh M, const double *__restri
   if (coefvort) coefvort[t] = kt[t] * e;
   e = e + M.t_f[t];
   double ht = 0.0;
+  if (scheme == IMODEL_SWM_PXT16) {
 #pragma unroll
-  for (int s = 0; s < 3; ++s) ht = ht + M.t_kite[s * nt + t] * h[M.t_v[s * nt + t]];
-  ht = ht / A;
+    for (int s = 0; s < 3; ++s) ht = ht + M.t_bary[s * nt + t] * h[M.t_v[s * nt + t]];
+  } else if (scheme == IMODEL_SWM_GASS18) {
+    const int ne = M.ne;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const int ed = M.t_ed[s * nt + t];
+      const double he = (h[M.e_v[ed]] + h[M.e_v[ne + ed]]) * 0.5;
+      ht = ht + M.t_edarea[s * nt + t] * he;
+    }
+    ht = ht / A;
+    eta_t[t] = e;
+    h_trs[t] = ht;
+  } else {
+#pragma unroll
+    for (int s = 0; s < 3; ++s) ht = ht + M.t_kite[s * nt + t] * h[M.t_v[s * nt + t]];
+    ht = ht / A;
+  }
   double q = 0.0;
   if (pv_on) {
     if (fabs(ht) < kEps / 100000.0)
@@ -140,8 +163,11 @@ __global__ void __launch_bounds__(256) k_apvm64(DevMesh M, const double *__restr
   }
 }
 
-// scalar_hx2ed (:89-97), scalar_elem_product (:1546), scalar_tr2ed (:124);
-// with qg != NULL the apvm correction of q_ed (:1495-1502), coef = pvspar dt
+// scalar_hx2ed (:89-97), scalar_elem_product (:1546), scalar_tr2ed (:124-176:
+// the plain average for trsk, circumcentre-distance weights for bary) or,
+// for gass18, scalar_elem_divide of the rhombus averages of eta and h_tr
+// (swm.f90:2475-2480); with qg != NULL the apvm correction of q_ed
+// (:1495-1502), coef = pvspar dt
 __global__ void __launch_bounds__(256) k_edge_pre64(DevMesh M, const double *__restrict__ h,
                                                     const double *__restrict__ u,
                                                     const double *__restrict__ q_tr,
@@ -150,7 +176,10 @@ __global__ void __launch_bounds__(256) k_edge_pre64(DevMesh M, const double *__r
                                                     double *__restrict__ q_ed,
                                                     const double *__restrict__ qg,
                                                     const double *__restrict__ vhx,
-                                                    double coef) {
+                                                    double coef, int scheme,
+                                                    const double *__restrict__ eta_t,
+                                                    const double *__restrict__ h_trs,
+                                                    int pv_on, int *flags) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const int ne = M.ne;
   if (e >= ne) return;
@@ -158,7 +187,24 @@ __global__ void __launch_bounds__(256) k_edge_pre64(DevMesh M, const double *__r
   h_ed[e] = he;
   uh[e] = u[e] * he;
   const int t1 = M.e_sh[e], t2 = M.e_sh[ne + e];
-  double q = 0.5 * (q_tr[t1] + q_tr[t2]);
+  double q;
+  if (scheme == IMODEL_SWM_PXT16) {
+    const double d1 = M.e_dist[e], d2 = M.e_dist[ne + e];
+    q = (d2 * q_tr[t1] + d1 * q_tr[t2]) / (d1 + d2);
+  } else if (scheme == IMODEL_SWM_GASS18) {
+    const double a1 = M.t_areag[t1], a2 = M.t_areag[t2];
+    const double eta_ed = (a1 * eta_t[t1] + a2 * eta_t[t2]) / (a1 + a2);
+    const double h_rhb = (a1 * h_trs[t1] + a2 * h_trs[t2]) / (a1 + a2);
+    q = 0.0;
+    if (pv_on) {
+      if (fabs(h_rhb) < kEps / 100000.0)
+        atomicOr(flags, 1);
+      else
+        q = eta_ed / h_rhb;
+    }
+  } else {
+    q = 0.5 * (q_tr[t1] + q_tr[t2]);
+  }
   if (qg) {
     const int nt = M.nt, nv = M.nv;
     const int c1 = M.e_v[e], c2 = M.e_v[ne + e];
@@ -182,7 +228,7 @@ __global__ void __launch_bounds__(256) k_cell64(DevMesh M, const double *__restr
                                                 double *__restrict__ yout,
                                                 double *__restrict__ tend, int stage,
                                                 double dt, const double *__restrict__ kcv,
-                                                double *__restrict__ coefdiv) {
+                                                double *__restrict__ coefdiv, int perot_ke) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int nv = M.nv;
   if (i >= nv) return;
@@ -198,7 +244,30 @@ __global__ void __launch_bounds__(256) k_cell64(DevMesh M, const double *__restr
   // with diffusion on: div_hx(u) (:613-661), diffusion_ed's K div u
   if (coefdiv) coefdiv[i] = kcv[i] * (du / M.c_areag[i] / M.erad);
   const double divuh = d / M.c_areag[i] / M.erad;
-  const double ke = k / M.c_cellarea[i];
+  double ke;
+  if (perot_ke) {
+    // kinetic_energy_hx, perhx branch (:1172-1173): half the squared
+    // vector_edhx2hx_perot (:454-509, HTC) of u
+    const int ne = M.ne;
+    const double p0 = M.c_p[i], p1 = M.c_p[nv + i], p2 = M.c_p[2 * nv + i];
+    double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+    for (int j = 0; j < n; ++j) {
+      const int ed = M.c_ed[j * nv + i];
+      const double su = (M.c_sd[j * nv + i] < 0.0 ? -1.0 : 1.0) * u[ed];
+      const double dl = M.e_dleng[ed];
+      v0 = v0 + su * (M.e_c[ed] - p0) * dl;
+      v1 = v1 + su * (M.e_c[ne + ed] - p1) * dl;
+      v2 = v2 + su * (M.e_c[2 * ne + ed] - p2) * dl;
+    }
+    const double A = M.c_areag[i];
+    v0 = v0 / A;
+    v1 = v1 / A;
+    v2 = v2 / A;
+    proj_sphere(v0, v1, v2, p0, p1, p2);
+    ke = (v0 * v0 + v1 * v1 + v2 * v2) / 2.0;
+  } else {
+    ke = k / M.c_cellarea[i];
+  }
   bern[i] = M.grav * (h[i] + M.c_bt[i]) + ke;
   const double masseq = -divuh;
   if (stage < 0)
@@ -217,7 +286,8 @@ __global__ void __launch_bounds__(256) k_edge64(DevMesh M, const double *__restr
                                                 double *__restrict__ tend, int stage,
                                                 double dt, int mom_on,
                                                 const double *__restrict__ dif1,
-                                                const double *__restrict__ dif2) {
+                                                const double *__restrict__ dif2,
+                                                const int32_t *__restrict__ stq) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const int ne = M.ne;
   if (e >= ne) return;
@@ -229,12 +299,116 @@ __global__ void __launch_bounds__(256) k_edge64(DevMesh M, const double *__restr
   double q = 0.0;
   for (int s = 0; s < ns; ++s) {
     const int k = M.e_stk[s * ne + e];
-    const double qtmp = 0.5 * (qe + q_ed[k]);
+    // gass18 (:1378-1410): the PV of the edge connecting e and k when there
+    // is one (stq != NULL), else the TRSK average
+    const int c3 = stq ? stq[s * ne + e] : -1;
+    const double qtmp = c3 >= 0 ? q_ed[c3] : 0.5 * (qe + q_ed[k]);
     q = q + uh[k] * qtmp * M.e_dleng[k] * M.e_stw[s * ne + e];
   }
   q = q / l;
   double momeq = -g - q;
   // diffusion, then hyperdiffusion (swm.f90:2578-2589)
+  if (dif1) momeq = momeq + dif1[e];
+  if (dif2) momeq = momeq - dif2[e];
+  if (!mom_on) momeq = 0.0;
+  if (stage < 0)
+    tend[e] = momeq;
+  else
+    yout[e] = rk_stage(stage, momeq, yn[e], acc + e, dt);
+}
+
+// dtred: vector_edhx2tr_perot (:345-406, HTC) of uh at the triangle
+// circumcentres, cross(tr%c, v) / tr%areag, times q_tr (vector_elem_product,
+// :1617-1649); signcor = dsign(1, tr%tg) is the sign of t_lt
+__global__ void __launch_bounds__(256) k_vhq64(DevMesh M, const double *__restrict__ uh,
+                                               const double *__restrict__ q_tr,
+                                               double *__restrict__ vhq) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = M.nt, ne = M.ne;
+  if (t >= nt) return;
+  const double c0 = M.t_c[t], c1 = M.t_c[nt + t], c2 = M.t_c[2 * nt + t];
+  double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    const int ed = M.t_ed[s * nt + t];
+    const double su = (M.t_lt[s * nt + t] < 0.0 ? -1.0 : 1.0) * uh[ed];
+    const double l = M.e_leng[ed];
+    v0 = v0 + su * (M.e_c[ed] - c0) * l;
+    v1 = v1 + su * (M.e_c[ne + ed] - c1) * l;
+    v2 = v2 + su * (M.e_c[2 * ne + ed] - c2) * l;
+  }
+  const double w0 = c1 * v2 - c2 * v1, w1 = c2 * v0 - c0 * v2, w2 = c0 * v1 - c1 * v0;
+  const double A = M.t_areag[t], q = q_tr[t];
+  vhq[t] = w0 / A * q;
+  vhq[nt + t] = w1 / A * q;
+  vhq[2 * nt + t] = w2 / A * q;
+}
+
+// grad_ed (:511-548) + coriolis_ed's dtred (:1310-1329) or pered
+// (:1330-1377) branch, HTC, and the momentum RK stage
+__global__ void __launch_bounds__(256) k_edge64r(DevMesh M, const double *__restrict__ bern,
+                                                 const double *__restrict__ uh,
+                                                 const double *__restrict__ q_ed,
+                                                 const double *__restrict__ vhq,
+                                                 const double *__restrict__ yn,
+                                                 double *__restrict__ acc,
+                                                 double *__restrict__ yout,
+                                                 double *__restrict__ tend, int stage,
+                                                 double dt, int mom_on,
+                                                 const double *__restrict__ dif1,
+                                                 const double *__restrict__ dif2, int scheme) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ne = M.ne, nv = M.nv, nt = M.nt;
+  if (e >= ne) return;
+  const double l = M.e_leng[e];
+  double g = bern[M.e_v[ne + e]] - bern[M.e_v[e]];
+  g = g / l / M.erad;
+  double v0, v1, v2;
+  if (scheme == IMODEL_SWM_DTRED) {
+    // the dual-triangle reconstructions of the edge's two triangles,
+    // weighted by the other triangle's circumcentre distance
+    const int k1 = M.e_sh[e], k2 = M.e_sh[ne + e];
+    const double d1 = M.e_dist[e], d2 = M.e_dist[ne + e];
+    v0 = (d2 * vhq[k1] + d1 * vhq[k2]) / (d1 + d2);
+    v1 = (d2 * vhq[nt + k1] + d1 * vhq[nt + k2]) / (d1 + d2);
+    v2 = (d2 * vhq[2 * nt + k1] + d1 * vhq[2 * nt + k2]) / (d1 + d2);
+  } else {
+    // pered: at each of the edge's cells the Perot reconstruction of
+    // uh (q_e + q_k) / 2 over the cell's edges, projected on the tangent
+    // plane; their average
+    const double qe = q_ed[e];
+    double vc[2][3];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const int c = M.e_v[i * ne + e];
+      const double p0 = M.c_p[c], p1 = M.c_p[nv + c], p2 = M.c_p[2 * nv + c];
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+      const int n = M.c_nnb[c];
+      for (int j = 0; j < n; ++j) {
+        const int l2 = M.c_ed[j * nv + c];
+        const double qtmp = 0.5 * (qe + q_ed[l2]);
+        const double f = (M.c_sd[j * nv + c] < 0.0 ? -1.0 : 1.0) * uh[l2] * qtmp;
+        const double d = M.e_dleng[l2];
+        a0 = a0 + f * (M.e_c[l2] - p0) * d;
+        a1 = a1 + f * (M.e_c[ne + l2] - p1) * d;
+        a2 = a2 + f * (M.e_c[2 * ne + l2] - p2) * d;
+      }
+      const double A = M.c_areag[c];
+      a0 = a0 / A;
+      a1 = a1 / A;
+      a2 = a2 / A;
+      proj_sphere(a0, a1, a2, p0, p1, p2);
+      vc[i][0] = a0;
+      vc[i][1] = a1;
+      vc[i][2] = a2;
+    }
+    v0 = 0.5 * vc[0][0] + 0.5 * vc[1][0];
+    v1 = 0.5 * vc[0][1] + 0.5 * vc[1][1];
+    v2 = 0.5 * vc[0][2] + 0.5 * vc[1][2];
+  }
+  proj_sphere(v0, v1, v2, M.e_c[e], M.e_c[ne + e], M.e_c[2 * ne + e]);
+  const double q = -(v0 * M.e_nr[e] + v1 * M.e_nr[ne + e] + v2 * M.e_nr[2 * ne + e]);
+  double momeq = -g - q;
   if (dif1) momeq = momeq + dif1[e];
   if (dif2) momeq = momeq - dif2[e];
   if (!mom_on) momeq = 0.0;
@@ -696,8 +870,10 @@ void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
   // K div u; the edge gradients follow them (and, with hyperdiffusion, the
   // second application), before the edge kernel
   const Diffusion<double> &D = W.dif;
+  const int sch = W.scheme;
   k_tri64<<<nblocks(M.nt, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.pv_on, W.flags, D.kt,
-                                              D.on ? D.coefvort : nullptr);
+                                              D.on ? D.coefvort : nullptr, sch, W.eta_t,
+                                              W.h_trs);
   if (ev) cudaEventRecord(ev[1], s);
   const Apvm<double> &A = W.apvm;
   if (A.on) {
@@ -706,11 +882,15 @@ void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
     k_apvm64<<<nbt + nblocks(M.nv, 256), 256, 0, s>>>(M, A.qge, u_in, A.qg, A.vhx, nbt);
   }
   k_edge_pre64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ed, W.uh, W.q_ed,
-                                                   A.on ? A.qg : nullptr, A.vhx, A.coef);
+                                                   A.on ? A.qg : nullptr, A.vhx, A.coef, sch,
+                                                   W.eta_t, W.h_trs, W.pv_on, W.flags);
+  if (sch == IMODEL_SWM_DTRED)
+    k_vhq64<<<nblocks(M.nt, 256), 256, 0, s>>>(M, W.uh, W.q_tr, W.vhq);
   if (ev) cudaEventRecord(ev[2], s);
   k_cell64<<<nblocks(M.nv, 256), 256, 0, s>>>(M, h_in, u_in, W.uh, W.bern, W.yn_h, W.acc_h,
                                                h_out, W.tend_h, stage, dt, D.kcv,
-                                               D.on ? D.coefdiv : nullptr);
+                                               D.on ? D.coefdiv : nullptr,
+                                               sch == IMODEL_SWM_PXT16 ? 1 : 0);
   if (D.on) {
     k_diflap64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, D.coefdiv, D.coefvort, D.lap);
     if (D.k4) {
@@ -720,9 +900,16 @@ void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
     }
   }
   if (ev) cudaEventRecord(ev[3], s);
-  k_edge64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, W.bern, W.uh, W.q_ed, W.yn_u, W.acc_u, u_out,
-                                               W.tend_u, stage, dt, W.mom_on,
-                                               D.k2 ? D.lap : nullptr, D.k4 ? D.lap2 : nullptr);
+  if (sch == IMODEL_SWM_PXT16 || sch == IMODEL_SWM_DTRED)
+    k_edge64r<<<nblocks(M.ne, 256), 256, 0, s>>>(M, W.bern, W.uh, W.q_ed, W.vhq, W.yn_u, W.acc_u,
+                                                  u_out, W.tend_u, stage, dt, W.mom_on,
+                                                  D.k2 ? D.lap : nullptr,
+                                                  D.k4 ? D.lap2 : nullptr, sch);
+  else
+    k_edge64<<<nblocks(M.ne, 256), 256, 0, s>>>(M, W.bern, W.uh, W.q_ed, W.yn_u, W.acc_u, u_out,
+                                                 W.tend_u, stage, dt, W.mom_on,
+                                                 D.k2 ? D.lap : nullptr, D.k4 ? D.lap2 : nullptr,
+                                                 sch == IMODEL_SWM_GASS18 ? M.e_stq : nullptr);
   if (ev) cudaEventRecord(ev[4], s);
 }
 

@@ -75,9 +75,85 @@ void circumcentre(const imodel_swm_mesh &m, int t, double c[3]) {
   for (int k = 0; k < 3; ++k) c[k] = (side < 0 ? -x[k] : x[k]) / nrm;
 }
 
+// spherical geometry as smeshpack.f90 evaluates it (no contraction: this
+// file is compiled with -ffp-contract=off)
+double dot3(const double *a, const double *b) {
+  double s = a[0] * b[0];
+  s = s + a[1] * b[1];
+  s = s + a[2] * b[2];
+  return s;
+}
+// det(p1, p2, p3) = cross_product(p1, p2) . p3 (smeshpack.f90:6560-6595)
+double det3(const double *p1, const double *p2, const double *p3) {
+  const double c[3] = {p1[1] * p2[2] - p1[2] * p2[1], p1[2] * p2[0] - p1[0] * p2[2],
+                       p1[0] * p2[1] - p1[1] * p2[0]};
+  return dot3(c, p3);
+}
+// arclen (smeshpack.f90:4624-4657; pi from the default-real literal of
+// constants.f90:31)
+double arclen(const double *p, const double *q) {
+  const double s[3] = {p[0] + q[0], p[1] + q[1], p[2] + q[2]};
+  const double d = dot3(s, s);
+  if (d == 0.0) return 4.0 * static_cast<double>(0.78539816339744830961566f);
+  if (d >= 4.0) return 0.0;
+  return 2.0 * std::atan(std::sqrt((4.0 - d) / d));
+}
+// sphtriarea, L'Huilier's theorem (smeshpack.f90:4710-4762; the degeneracy
+// tolerance eps/100 with eps = epsilon(1.))
+double sphtriarea(const double *p1, const double *p2, const double *p3) {
+  const double tol = static_cast<double>(1.1920928955078125e-07f) / 100.0;
+  auto dist = [](const double *a, const double *b) {
+    const double d[3] = {a[0] - b[0], a[1] - b[1], a[2] - b[2]};
+    return std::sqrt(dot3(d, d));
+  };
+  if (dist(p1, p2) < tol || dist(p2, p3) < tol || dist(p1, p3) < tol) return 0.0;
+  const double a = arclen(p1, p2), b = arclen(p2, p3), c = arclen(p3, p1);
+  const double s = (a + b + c) / 2.0;
+  double t = std::tan(s / 2.0) * std::tan((s - a) / 2.0);
+  t = t * std::tan((s - b) / 2.0);
+  t = t * std::tan((s - c) / 2.0);
+  if (t < 0.0) return 0.0;
+  return 4.0 * std::atan(std::sqrt(t));
+}
+
+// The edge whose PV the gass Coriolis term uses for stencil edge ed2 of edge
+// ed1 (0-based, reference numbering): the third edge of a triangle holding
+// both, else an edge joining a triangle of ed2's dual edge to a triangle
+// holding ed1; -1 when ed1 == ed2 or they are further apart (the TRSK
+// average is then used).  Restates getedgeintriangle and
+// gethxedgeconnection, smeshpack.f90:4127-4244.
+int edge_connection(const imodel_swm_mesh &m, int ed1, int ed2) {
+  if (ed1 == ed2) return -1;
+  auto tri_ed = [&](int t, int i) { return m.tr_ed[3 * static_cast<size_t>(t) + i] - 1; };
+  auto tri_of = [&](int e, int s) { return m.ed_sh[2 * static_cast<size_t>(e) + s] - 1; };
+  const int tr1 = tri_of(ed1, 0), tr2 = tri_of(ed1, 1);
+  int tr = -1;
+  for (int i = 0; i < 3 && tr < 0; ++i) {
+    if (ed2 == tri_ed(tr1, i))
+      tr = tr1;
+    else if (ed2 == tri_ed(tr2, i))
+      tr = tr2;
+  }
+  if (tr >= 0)
+    for (int i = 0; i < 3; ++i)
+      if (tri_ed(tr, i) != ed1 && tri_ed(tr, i) != ed2) return tri_ed(tr, i);
+  for (int j = 0; j < 2; ++j) {
+    const int trj = tri_of(ed2, j);
+    for (int i = 0; i < 3; ++i) {
+      const int edtmp = tri_ed(trj, i);
+      if (edtmp == ed2) continue;
+      const int a = tri_of(edtmp, 0);
+      const int other = a == trj ? tri_of(edtmp, 1) : a;
+      for (int k = 0; k < 3; ++k)
+        if (ed1 == tri_ed(other, k)) return edtmp;
+    }
+  }
+  return -1;
+}
+
 }  // namespace
 
-std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) {
+std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, int scheme) {
   const int nv = m.nv, ne = m.ne, nt = m.nt;
   if (nv < 4 || ne < 6 || nt < 4) return "mesh sizes too small";
   if (!m.nnb || !m.v_ed || !m.v_tr || !m.hx_ttgout || !m.hx_tnrccw || !m.hx_areag ||
@@ -232,6 +308,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
   L.e_stk.assign(kMaxSt * NE, 0);
   L.e_stw.assign(kMaxSt * NE, 0.0);
   L.e_stc32.assign(kMaxSt * NE, 0.0f);
+  if (scheme == IMODEL_SWM_GASS18) L.e_stq.assign(kMaxSt * NE, -1);
   L.e_vs.assign(2 * NE, 0u);
   for (int i = 0; i < ne; ++i) {
     const int e = L.edge_n2o[i];
@@ -284,6 +361,10 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
                      m.hx_tnrccw[6 * static_cast<size_t>(node) + edcelli]);
         const double w = m.hx_trskw[36 * static_cast<size_t>(node) + 6 * static_cast<size_t>(j) + edcelli];
         L.e_stk[ns * NE + i] = L.edge_o2n[k];
+        if (scheme == IMODEL_SWM_GASS18) {
+          const int c3 = edge_connection(m, e, k);
+          L.e_stq[ns * NE + i] = c3 < 0 ? -1 : L.edge_o2n[c3];
+        }
         L.e_stw[ns * NE + i] = w * sc;
         L.e_stc32[ns * NE + i] = static_cast<float>(0.5 * w * sc * m.edhx_leng[k] / l);
         ++ns;
@@ -388,6 +469,54 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L) 
       }
       for (int k = 0; k < 3; ++k) L.c_p32[k * NV + i] = static_cast<float>(L.c_p[k * NV + i]);
     }
+  }
+  // --- geometry of the pxt16, gass18 and dtred branches -------------------
+  if (scheme != IMODEL_SWM_TRSK10) {
+    if (scheme < IMODEL_SWM_TRSK10 || scheme > IMODEL_SWM_DTRED) return "unknown scheme";
+    if (!m.ed_nr || !m.ed_c) return "the pxt16, gass18 and dtred schemes need ed_nr and ed_c";
+    if (scheme == IMODEL_SWM_PXT16) {
+      L.t_bary.resize(3 * NT);
+      for (int i = 0; i < nt; ++i) {
+        const int t = L.tri_n2o[i];
+        const double pc[3] = {L.t_c[i], L.t_c[NT + i], L.t_c[2 * NT + i]};
+        const double *p[3];
+        for (int k = 0; k < 3; ++k)
+          p[k] = m.v_p + 3 * static_cast<size_t>(m.tr_v[3 * static_cast<size_t>(t) + k] - 1);
+        const double b[3] = {std::fabs(det3(pc, p[1], p[2])), std::fabs(det3(pc, p[2], p[0])),
+                             std::fabs(det3(pc, p[0], p[1]))};
+        double area = b[0];
+        area = area + b[1];
+        area = area + b[2];
+        for (int k = 0; k < 3; ++k) L.t_bary[k * NT + i] = b[k] / area;
+      }
+    }
+    if (scheme == IMODEL_SWM_PXT16 || scheme == IMODEL_SWM_DTRED) {
+      L.e_dist.resize(2 * NE);
+      for (int i = 0; i < ne; ++i) {
+        const int e = L.edge_n2o[i];
+        for (int s = 0; s < 2; ++s) {
+          const int ti = L.e_sh[s * NE + i];
+          const double c[3] = {L.t_c[ti], L.t_c[NT + ti], L.t_c[2 * NT + ti]};
+          L.e_dist[s * NE + i] = arclen(m.ed_c + 3 * static_cast<size_t>(e), c);
+        }
+      }
+    }
+    if (scheme == IMODEL_SWM_GASS18) {
+      L.t_edarea.resize(3 * NT);
+      for (int i = 0; i < nt; ++i) {
+        const int t = L.tri_n2o[i];
+        const double pc[3] = {L.t_c[i], L.t_c[NT + i], L.t_c[2 * NT + i]};
+        for (int s = 0; s < 3; ++s) {
+          const int e = m.tr_ed[3 * static_cast<size_t>(t) + s] - 1;
+          L.t_edarea[s * NT + i] =
+              sphtriarea(pc, m.v_p + 3 * static_cast<size_t>(m.ed_v[2 * static_cast<size_t>(e)] - 1),
+                         m.v_p + 3 * static_cast<size_t>(m.ed_v[2 * static_cast<size_t>(e) + 1] - 1));
+        }
+      }
+    }
+    L.e_nr.resize(3 * NE);
+    for (int i = 0; i < ne; ++i)
+      for (int k = 0; k < 3; ++k) L.e_nr[k * NE + i] = m.ed_nr[3 * static_cast<size_t>(L.edge_n2o[i]) + k];
   }
   L.t_recA.resize(4 * NT);
   L.t_recB.resize(4 * NT);

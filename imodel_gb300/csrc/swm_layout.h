@@ -108,10 +108,27 @@ struct Layout {
 
   // per-edge reference-ordered weight for edge integrals: l*d*0.5
   std::vector<double> e_area;
+
+  // the geometry of the other method wrappers (FP64, device order; empty for
+  // trsk10), as initialize_gridprop precomputes it (swm.f90:1005-1028):
+  //   t_bary  [3][nt] tr%c%b, barycentric coordinates of the circumcentre
+  //           (bar_coord_tr, smeshpack.f90:5200-5245; pxt16)
+  //   e_dist  [2][ne] arclen(ed%c, tr(ed%sh(i))%c) (scalar_tr2ed's bary
+  //           weights, pxt16; the dtred interpolation)
+  //   t_edarea [3][nt] sphtriarea(tr%c, the end cells of triangle edge s)
+  //           (scalar_edtr2trcc, geodesic areas; gass18)
+  //   e_stq   [kMaxSt][ne] per TRSK stencil slot the connecting edge
+  //           gethxedgeconnection(e, k) (smeshpack.f90:4174-4244) whose PV the
+  //           gass Coriolis term takes, or -1 for the TRSK average (gass18)
+  //   e_nr    [3][ne] ed%nr (pered, dtred)
+  std::vector<double> t_bary, e_dist, t_edarea, e_nr;
+  std::vector<int32_t> e_stq;
 };
 
 // Builds the layout from a reference mesh; returns "" or an error message.
-std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L);
+// scheme (IMODEL_SWM_TRSK10 ... IMODEL_SWM_DTRED) selects the extra geometry.
+std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L,
+                         int scheme = IMODEL_SWM_TRSK10);
 
 // Inputs of the learned TRSK correction (imodel_gb300/learned.py), device
 // order: per edge the 10 stencil edges as sign * (index + 1) (0 = padding),

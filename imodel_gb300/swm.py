@@ -114,11 +114,14 @@ class SWM:
 
     precision: "fp64" reproduces the reference's FP64 operation order;
     "fp32" runs FP32 state and operators with FP64 integrals.
+    scheme: the method wrapper of swm.par, "trsk10", "pxt16", "gass18", or
+    "dtred" (trsk10 with the dtred Coriolis reconstruction); the last three
+    on "fp64" handles.
     """
 
     def __init__(self, grid: Grid, precision: str = "fp64", testcase: int = 2,
                  bt=None, h_ref: float = 0.0, device: int = 0, learned_params=None,
-                 drift_bound: float = 0.0):
+                 drift_bound: float = 0.0, scheme: str = "trsk10"):
         self.grid = grid
         self.lib = _capi.swm_lib()
         self.precision = precision
@@ -132,6 +135,8 @@ class SWM:
             opts.bt = _capi.as_f64p(self._bt)
         opts.h_ref = h_ref
         opts.device = device
+        opts.scheme = _capi.SCHEMES[scheme]
+        self.scheme = scheme
         self._mlp = None
         if learned_params is not None:
             # learned TRSK correction (network parameters, see imodel_mlp.h)

@@ -57,6 +57,17 @@ extern "C" {
 #define IMODEL_SWM_FP64 0 /* reference operation order, FP64 everywhere      */
 #define IMODEL_SWM_FP32 1 /* FP32 state and operators, FP64 integrals        */
 
+/* ---- method wrappers (swm.par's mtdwrapper, swm_data.f90:446-507) ------ */
+#define IMODEL_SWM_TRSK10 0 /* trsk interpolation, TRSK Coriolis and K      */
+#define IMODEL_SWM_PXT16 1  /* bary interpolation (scalar_hx2tr, tr2ed),
+                               pered Coriolis, Perot K (perhx)            */
+#define IMODEL_SWM_GASS18 2 /* gass: h_tr from the edges (scalar_edtr2trcc),
+                               rhombus PV q_ed, Coriolis with the PV of the
+                               connecting edge, TRSK K                    */
+#define IMODEL_SWM_DTRED 3  /* mtdwrapper "none" with trsk interpolation and
+                               K and coriolis_reconmtd "dtred" (dual
+                               triangle Perot reconstruction)             */
+
 /* ---- mesh (copied from grid_structure) --------------------------------- */
 typedef struct imodel_swm_mesh {
   int32_t nv, ne, nt;
@@ -92,7 +103,7 @@ typedef struct imodel_swm_mesh {
   double erad, grav, omega;
 } imodel_swm_mesh;
 
-/* ---- options (par/swm.par subset for the trsk10/HTC/geo path) ---------- */
+/* ---- options (par/swm.par subset for the HTC/geo path) ----------------- */
 typedef struct imodel_swm_opts {
   int32_t precision;  /* IMODEL_SWM_FP64 or IMODEL_SWM_FP32                 */
   int32_t testcase;   /* reference testcase number: q_tr=0 if <2 and momeq=0
@@ -111,6 +122,10 @@ typedef struct imodel_swm_opts {
                          its value when the state was set.  Checked every
                          32 steps; the interval that failed is stepped
                          again with the plain scheme                     */
+  int32_t scheme;     /* IMODEL_SWM_TRSK10 (0) ... IMODEL_SWM_DTRED; the
+                         other wrappers need the mesh's ed_nr and ed_c and
+                         run on FP64 handles (an FP32 handle, the learned
+                         correction or an ensemble takes trsk10 only)   */
 } imodel_swm_opts;
 
 /* ---- diagnostics (swm.f90:293-322, :2686-2752, :3394-3440) ------------- */

@@ -63,6 +63,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_field.argtypes = [vp, ctypes.c_int32, f64p]
         L.oracle_set_diffusion.argtypes = [vp, ctypes.c_double, ctypes.c_double]
         L.oracle_set_apvm.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+        L.oracle_set_scheme.argtypes = [vp, ctypes.c_int32]
         L.oracle_set_diffusion_fields.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
         _lib = L
     return _lib
@@ -76,7 +77,12 @@ FIELDS = {"h_ed": (0, "ne"), "uh": (1, "ne"), "eta": (2, "nt"), "h_tr": (3, "nt"
           "q_tr": (4, "nt"), "q_ed": (5, "ne"), "divuh": (6, "nv"), "ke": (7, "nv"),
           "ghbK": (8, "nv"), "grad_ghbK": (9, "ne"), "uhq_perp": (10, "ne"),
           "divu": (11, "nv"), "zeta": (12, "nt"), "eta_ed": (13, "ne"),
-          "lapu": (14, "ne"), "lap_lapu": (15, "ne"), "q_grad_ed": (16, "ne")}
+          "lapu": (14, "ne"), "lap_lapu": (15, "ne"), "q_grad_ed": (16, "ne"),
+          "h_rhb": (17, "ne"), "vhq_tr": (18, "nt3"), "v_hx": (19, "nv3")}
+
+# method wrappers of swm.par (swm_data.f90:446-507); "dtred" is trsk10 with
+# coriolis_reconmtd = dtred (mtdwrapper "none")
+SCHEMES = {"trsk10": 0, "pxt16": 1, "gass18": 2, "dtred": 3}
 
 
 class Oracle:
@@ -84,7 +90,7 @@ class Oracle:
 
     def __init__(self, grid, testcase: int = 2, bt=None, nthreads: int = 0, k2: float = 0.0,
                  k4: float = 0.0, pvspar: float = 0.0, dt: float = 0.0, k2_hx=None,
-                 k4_hx=None):
+                 k4_hx=None, scheme: str = "trsk10"):
         self.grid = grid
         self._mesh = grid.c_struct()
         self._bt = None if bt is None else np.ascontiguousarray(bt, dtype=np.float64)
@@ -92,6 +98,9 @@ class Oracle:
         self.nthreads = n
         self._h = lib().oracle_create(ctypes.byref(self._mesh), testcase,
                                       None if self._bt is None else _p(self._bt), n)
+        if scheme != "trsk10":
+            if lib().oracle_set_scheme(self._h, SCHEMES[scheme]):
+                raise ValueError(f"bad scheme {scheme!r} (or the mesh lacks ed_nr / ed_c)")
         if k2 or k4:
             if lib().oracle_set_diffusion(self._h, k2, k4):
                 raise ValueError("bad diffusion coefficients")
@@ -163,8 +172,12 @@ class Oracle:
 
     def field(self, name: str):
         which, cnt = FIELDS[name]
-        out = np.zeros(getattr(self.grid, cnt))
-        lib().oracle_field(self._h, which, _p(out))
+        if cnt.endswith("3"):
+            out = np.zeros((getattr(self.grid, cnt[:2]), 3))
+        else:
+            out = np.zeros(getattr(self.grid, cnt))
+        if lib().oracle_field(self._h, which, _p(out)):
+            raise RuntimeError(f"oracle field {name!r} not available")
         return out
 
 

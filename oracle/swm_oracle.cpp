@@ -3,8 +3,9 @@
 // TEST INFRASTRUCTURE ONLY: the correctness oracle for the GB300 kernels and
 // the CPU baseline timed beside them.  Nothing in the product links this.
 //
-// It follows the Fortran loop by loop for the branches the trsk10 wrapper,
-// HTC staggering and geodesic areas select (swm_data.f90:446-507), with the
+// It follows the Fortran loop by loop for the branches the trsk10, pxt16 and
+// gass18 wrappers (and the dtred Coriolis reconstruction), HTC staggering and
+// geodesic areas select (swm_data.f90:446-507), with the
 // same per-entity accumulation order and one OpenMP parallel loop per
 // operator, like the reference's `!$omp parallel do schedule(static)`.
 // Build with -ffp-contract=off so no multiply-add is fused.
@@ -42,6 +43,15 @@ struct Oracle {
   double pvspar = 0.0, apvm_dt = 0.0;
   std::vector<double> cc;              // tr%c%p [nt][3]
   std::vector<double> q_grad_ed, q_grad_tr;   // [ne], [nt][3]
+  // method wrapper (swm_data.f90:446-507): 0 trsk10, 1 pxt16, 2 gass18,
+  // 3 trsk10 with the dtred Coriolis reconstruction (mtdwrapper "none")
+  int scheme = 0;
+  std::vector<double> bary;            // tr%c%b [nt][3] (pxt16)
+  std::vector<double> dist;            // arclen(ed%c, tr(sh(i))%c) [ne][2] (pxt16, dtred)
+  std::vector<double> edarea;          // sphtriarea(tr%c, ed%v) [nt][3] (gass18)
+  std::vector<int> conn;               // gethxedgeconnection(l, k) per TRSK term [ne][12]
+  std::vector<double> h_rhb, vhq_tr;   // [ne] (gass18), [nt][3] (dtred)
+  std::vector<double> h_trk;           // kite-weighted h_tr of the last call (diagnostics)
 };
 
 #define I6(i, j) (static_cast<size_t>(i) * 6 + (j))
@@ -51,6 +61,94 @@ inline int getedindexonhx(const imodel_swm_mesh &m, int ed, int cell) {
   for (int i = 0; i < m.nnb[cell]; ++i)
     if (m.v_ed[I6(cell, i)] - 1 == ed) return i + 1;
   return 0;
+}
+
+// ---- spherical geometry of smeshpack.f90, as the scheme set-up uses it ----
+inline double dot3(const double *a, const double *b) {
+  double s = a[0] * b[0];
+  s = s + a[1] * b[1];
+  s = s + a[2] * b[2];
+  return s;
+}
+// cross_product, smeshpack.f90:6560-6578
+inline void cross3(const double *a, const double *b, double *c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+// det, smeshpack.f90:6580-6595
+inline double det3(const double *p1, const double *p2, const double *p3) {
+  double c[3];
+  cross3(p1, p2, c);
+  return dot3(c, p3);
+}
+// arclen, smeshpack.f90:4624-4657
+inline double arclen(const double *p, const double *q) {
+  const double s[3] = {p[0] + q[0], p[1] + q[1], p[2] + q[2]};
+  const double d = dot3(s, s);
+  if (d == 0.0) return kPi;
+  if (d >= 4.0) return 0.0;
+  return 2.0 * std::atan(std::sqrt((4.0 - d) / d));
+}
+inline double norm3(const double *p) { return std::sqrt(dot3(p, p)); }
+// sphtriarea (L'Huilier), smeshpack.f90:4710-4762
+double sphtriarea(const double *p1, const double *p2, const double *p3) {
+  const double d12[3] = {p1[0] - p2[0], p1[1] - p2[1], p1[2] - p2[2]};
+  const double d23[3] = {p2[0] - p3[0], p2[1] - p3[1], p2[2] - p3[2]};
+  const double d13[3] = {p1[0] - p3[0], p1[1] - p3[1], p1[2] - p3[2]};
+  const double tol = kEps / 100.0;
+  if (norm3(d12) < tol || norm3(d23) < tol || norm3(d13) < tol) return 0.0;
+  const double a = arclen(p1, p2), b = arclen(p2, p3), c = arclen(p3, p1);
+  const double s = (a + b + c) / 2.0;
+  double t = std::tan(s / 2.0) * std::tan((s - a) / 2.0);
+  t = t * std::tan((s - b) / 2.0);
+  t = t * std::tan((s - c) / 2.0);
+  if (t < 0.0) return 0.0;
+  return 4.0 * std::atan(std::sqrt(t));
+}
+// proj_vec_sphere, smeshpack.f90:4419-4433: v - (v . p) p / |p|
+inline void proj_sphere(double *v, const double *p) {
+  const double vp = dot3(v, p);
+  const double np = norm3(p);
+  for (int k = 0; k < 3; ++k) v[k] = v[k] - vp * p[k] / np;
+}
+
+// getedgeintriangle + gethxedgeconnection, smeshpack.f90:4127-4244 (0-based
+// edges; 0-based third edge, -1 for "equal" (the reference's 0) and -2 for
+// "not connected" (its -1))
+int edge_connection(const imodel_swm_mesh &m, int ed1, int ed2) {
+  if (ed1 == ed2) return -1;
+  const int tr1 = m.ed_sh[2 * ed1] - 1, tr2 = m.ed_sh[2 * ed1 + 1] - 1;
+  int tr = -1;
+  for (int i = 0; i < 3; ++i) {
+    if (ed2 == m.tr_ed[3 * tr1 + i] - 1) {
+      tr = tr1;
+      break;
+    }
+    if (ed2 == m.tr_ed[3 * tr2 + i] - 1) {
+      tr = tr2;
+      break;
+    }
+  }
+  if (tr >= 0) {
+    for (int i = 0; i < 3; ++i) {
+      const int ed = m.tr_ed[3 * tr + i] - 1;
+      if (ed != ed1 && ed != ed2) return ed;
+    }
+  }
+  // edhx(edref)%v = ed(edref)%sh: the triangles at the ends of ed2's dual edge
+  for (int j = 0; j < 2; ++j) {
+    const int trj = m.ed_sh[2 * ed2 + j] - 1;
+    for (int i = 0; i < 3; ++i) {
+      const int edtmp = m.tr_ed[3 * trj + i] - 1;
+      if (edtmp == ed2) continue;
+      const int a = m.ed_sh[2 * edtmp] - 1, b = m.ed_sh[2 * edtmp + 1] - 1;
+      const int other = a == trj ? b : a;
+      for (int l = 0; l < 3; ++l)
+        if (ed1 == m.tr_ed[3 * other + l] - 1) return edtmp;
+    }
+  }
+  return -2;
 }
 
 // diffusion_ed (swm_operators.f90:855-895): coef*div and coef*vort
@@ -73,6 +171,28 @@ void diffusion(Oracle &o, const double *div, const double *vort, double *lap) {
     double gt = o.sgtg[l] * (o.coefvort[k2] - o.coefvort[k1]);
     gt = gt / (m.edhx_leng[l] * erad);
     lap[l] = g - gt;
+  }
+}
+
+// scalar_tr2ed (swm_operators.f90:124-176), HTC: the plain average for
+// trsk interpolation, rhombus (triangle-area) weights for gass, and
+// circumcentre-distance weights for bary
+void tr2ed(Oracle &o, const double *ftr, double *fed) {
+  const imodel_swm_mesh &m = o.m;
+  const int ne = m.ne;
+  const int nth = o.nthreads;
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l) {
+    const int k1 = m.ed_sh[2 * l] - 1, k2 = m.ed_sh[2 * l + 1] - 1;
+    if (o.scheme == 0 || o.scheme == 3) {
+      fed[l] = 0.5 * (ftr[k1] + ftr[k2]);
+    } else if (o.scheme == 2) {
+      const double a1 = m.tr_areag[k1], a2 = m.tr_areag[k2];
+      fed[l] = (a1 * ftr[k1] + a2 * ftr[k2]) / (a1 + a2);
+    } else {
+      const double d1 = o.dist[2 * static_cast<size_t>(l)], d2 = o.dist[2 * static_cast<size_t>(l) + 1];
+      fed[l] = (d2 * ftr[k1] + d1 * ftr[k2]) / (d1 + d2);
+    }
   }
 }
 
@@ -109,18 +229,33 @@ int tendency(Oracle &o, const double *h, const double *u, double *masseq, double
     o.eta[k] = e;
   }
 
-  // scalar_hx2tr (swm_operators.f90:258-263), trsk branch
+  // depth at the triangles (swm.f90:2459-2464): scalar_hx2tr
+  // (swm_operators.f90:229-284), trsk branch (kite areas) or bary branch
+  // (barycentric coordinates of the circumcentre); gass: scalar_edtr2trcc
+  // (:286-343, geodesic areas) of h_ed, and its rhombus average h_rhb
 #pragma omp parallel for schedule(static) num_threads(nth)
   for (int k = 0; k < nt; ++k) {
     double f = 0.0;
     for (int i = 0; i < 3; ++i) f = f + m.tr_trhx_area[3 * k + i] * h[m.tr_v[3 * k + i] - 1];
-    o.h_tr[k] = f / m.tr_areag[k];
+    f = f / m.tr_areag[k];
+    if (o.scheme == 0 || o.scheme == 3) {
+      o.h_tr[k] = f;
+    } else {
+      o.h_trk[k] = f;
+      double g = 0.0;
+      if (o.scheme == 1) {
+        for (int i = 0; i < 3; ++i) g = g + o.bary[3 * k + i] * h[m.tr_v[3 * k + i] - 1];
+      } else {
+        for (int i = 0; i < 3; ++i) g = g + o.edarea[3 * k + i] * o.h_ed[m.tr_ed[3 * k + i] - 1];
+        g = g / m.tr_areag[k];
+      }
+      o.h_tr[k] = g;
+    }
   }
+  if (o.scheme == 2) tr2ed(o, o.h_tr.data(), o.h_rhb.data());
 
-  // scalar_tr2ed(eta -> eta_ed) (swm_operators.f90:140-176)
-#pragma omp parallel for schedule(static) num_threads(nth)
-  for (int l = 0; l < ne; ++l)
-    o.eta_ed[l] = 0.5 * (o.eta[m.ed_sh[2 * l] - 1] + o.eta[m.ed_sh[2 * l + 1] - 1]);
+  // scalar_tr2ed(eta -> eta_ed) (swm_operators.f90:124-176)
+  tr2ed(o, o.eta.data(), o.eta_ed.data());
 
   // scalar_elem_divide (swm_operators.f90:1579-1615)
   int divzero = 0;
@@ -137,10 +272,45 @@ int tendency(Oracle &o, const double *h, const double *u, double *masseq, double
   }
   if (divzero) return IMODEL_SWM_EDIVZERO;
 
-  // scalar_tr2ed(q_tr -> q_ed)
+  // PV at the edges (swm.f90:2475-2480): scalar_tr2ed(q_tr), or for gass
+  // scalar_elem_divide(eta_ed, h_rhb) with its division guard
+  if (o.scheme == 2) {
+    if (o.testcase < 2) {
+      for (int l = 0; l < ne; ++l) o.q_ed[l] = 0.0;
+    } else {
+#pragma omp parallel for schedule(static) num_threads(nth) reduction(+ : divzero)
+      for (int l = 0; l < ne; ++l) {
+        if (std::fabs(o.h_rhb[l]) < kEps / 100000.0)
+          divzero += 1;
+        else
+          o.q_ed[l] = o.eta_ed[l] / o.h_rhb[l];
+      }
+    }
+    if (divzero) return IMODEL_SWM_EDIVZERO;
+  } else {
+    tr2ed(o, o.q_tr.data(), o.q_ed.data());
+  }
+
+  // dtred: vector_edhx2tr_perot(uh -> vhq_tr) (swm_operators.f90:345-406,
+  // HTC), times q_tr (vector_elem_product, :1617-1649)
+  if (o.scheme == 3) {
 #pragma omp parallel for schedule(static) num_threads(nth)
-  for (int l = 0; l < ne; ++l)
-    o.q_ed[l] = 0.5 * (o.q_tr[m.ed_sh[2 * l] - 1] + o.q_tr[m.ed_sh[2 * l + 1] - 1]);
+    for (int k = 0; k < nt; ++k) {
+      const double *c = &o.cc[3 * static_cast<size_t>(k)];
+      double v[3] = {0.0, 0.0, 0.0};
+      for (int l = 0; l < 3; ++l) {
+        const int ed = m.tr_ed[3 * k + l] - 1;
+        const double signcor = std::copysign(1.0, static_cast<double>(m.tr_tg[3 * k + l]));
+        const double *ec = m.ed_c + 3 * static_cast<size_t>(ed);
+        for (int i = 0; i < 3; ++i)
+          v[i] = v[i] + signcor * o.uh[ed] * (ec[i] - c[i]) * m.ed_leng[ed];
+      }
+      double w[3];
+      cross3(c, v, w);
+      for (int i = 0; i < 3; ++i)
+        o.vhq_tr[3 * static_cast<size_t>(k) + i] = w[i] / m.tr_areag[k] * o.q_tr[k];
+    }
+  }
 
   // vector_edhx2hx_perot(u -> v_hx) (swm_operators.f90:454-509): computed by
   // the reference on every call although trsk10 never reads it.
@@ -226,9 +396,15 @@ int tendency(Oracle &o, const double *h, const double *u, double *masseq, double
 #pragma omp parallel for schedule(static) num_threads(nth)
   for (int i = 0; i < nv; ++i) masseq[i] = -o.divuh[i];
 
-  // kinetic_energy_hx, trsk branch (swm_operators.f90:1162-1171)
+  // kinetic_energy_hx (swm_operators.f90:1132-1217): perhx branch for
+  // pxt16 (half the squared Perot velocity), trsk branch otherwise
 #pragma omp parallel for schedule(static) num_threads(nth)
   for (int i = 0; i < nv; ++i) {
+    if (o.scheme == 1) {
+      const double *v = &o.vhx[3 * static_cast<size_t>(i)];
+      o.ke[i] = dot3(v, v) / 2.0;
+      continue;
+    }
     double k = 0.0, cell_area = 0.0;
     for (int l = 0; l < m.nnb[i]; ++l) {
       int ed = m.v_ed[I6(i, l)] - 1;
@@ -255,9 +431,46 @@ int tendency(Oracle &o, const double *h, const double *u, double *masseq, double
     momeq[l] = -g;
   }
 
-  // coriolis_ed, TRSK branch (swm_operators.f90:1283-1308)
+  // coriolis_ed (swm_operators.f90:1219-1414), HTC: TRSK branch (:1283-1308),
+  // its gass variant with the PV of the connecting edge (:1378-1410), the
+  // dtred branch (:1310-1329) and the pered branch (:1330-1377)
 #pragma omp parallel for schedule(static) num_threads(nth)
   for (int l = 0; l < ne; ++l) {
+    if (o.scheme == 3) {
+      const int k1 = m.ed_sh[2 * l] - 1, k2 = m.ed_sh[2 * l + 1] - 1;
+      const double d1 = o.dist[2 * static_cast<size_t>(l)], d2 = o.dist[2 * static_cast<size_t>(l) + 1];
+      double v[3];
+      for (int i = 0; i < 3; ++i)
+        v[i] = (d2 * o.vhq_tr[3 * static_cast<size_t>(k1) + i] +
+                d1 * o.vhq_tr[3 * static_cast<size_t>(k2) + i]) / (d1 + d2);
+      proj_sphere(v, m.ed_c + 3 * static_cast<size_t>(l));
+      o.uhq[l] = -dot3(v, m.ed_nr + 3 * static_cast<size_t>(l));
+      continue;
+    }
+    if (o.scheme == 1) {
+      double vc[2][3];
+      for (int i = 0; i < 2; ++i) {
+        const int node = m.ed_v[2 * l + i] - 1;
+        const double *p = m.v_p + 3 * static_cast<size_t>(node);
+        double v[3] = {0.0, 0.0, 0.0};
+        for (int j = 0; j < m.nnb[node]; ++j) {
+          const int l2 = m.v_ed[I6(node, j)] - 1;
+          const double qtmp = 0.5 * (o.q_ed[l] + o.q_ed[l2]);
+          const double signcor = static_cast<double>(m.hx_ttgout[I6(node, j)]);
+          const double *ec = m.ed_c + 3 * static_cast<size_t>(l2);
+          for (int k = 0; k < 3; ++k)
+            v[k] = v[k] + signcor * o.uh[l2] * qtmp * (ec[k] - p[k]) * m.edhx_leng[l2];
+        }
+        for (int k = 0; k < 3; ++k) v[k] = v[k] / m.hx_areag[node];
+        proj_sphere(v, p);
+        for (int k = 0; k < 3; ++k) vc[i][k] = v[k];
+      }
+      double v[3];
+      for (int k = 0; k < 3; ++k) v[k] = 0.5 * vc[0][k] + 0.5 * vc[1][k];
+      proj_sphere(v, m.ed_c + 3 * static_cast<size_t>(l));
+      o.uhq[l] = -dot3(v, m.ed_nr + 3 * static_cast<size_t>(l));
+      continue;
+    }
     double q = 0.0;
     for (int i = 0; i < 2; ++i) {
       int node = m.ed_v[2 * l + i] - 1;
@@ -267,6 +480,10 @@ int tendency(Oracle &o, const double *h, const double *u, double *masseq, double
         double signcor = std::copysign(
             1.0, 1.0 * m.hx_ttgout[I6(node, j)] * m.hx_tnrccw[I6(node, edcelli - 1)]);
         double qtmp = 0.5 * (o.q_ed[l] + o.q_ed[k]);
+        if (o.scheme == 2) {
+          const int ed3 = o.conn[12 * static_cast<size_t>(l) + 6 * i + j];
+          if (ed3 >= 0) qtmp = o.q_ed[ed3];
+        }
         double w = m.hx_trskw[static_cast<size_t>(node) * 36 + static_cast<size_t>(j) * 6 +
                               (edcelli - 1)];
         q = q + o.uh[k] * qtmp * m.edhx_leng[k] * w * signcor;
@@ -539,6 +756,68 @@ int oracle_set_apvm(void *p, double pvspar, double dt) {
   return IMODEL_SWM_OK;
 }
 
+// the method wrapper of swm.par (swm_data.f90:446-507) and the geometry its
+// branches read, as initialize_gridprop precomputes it (swm.f90:1005-1028):
+// tr%c%b = bar_coord_tr(tr%c%p) (smeshpack.f90:5200-5245) for pxt16, the
+// circumcentre distances of scalar_tr2ed's bary branch and of dtred, the
+// kite-free edge areas of scalar_edtr2trcc and the edge connections of the
+// gass Coriolis term
+int oracle_set_scheme(void *p, int32_t scheme) {
+  Oracle &o = *static_cast<Oracle *>(p);
+  const imodel_swm_mesh &m = o.m;
+  if (scheme < 0 || scheme > 3) return IMODEL_SWM_EINVAL;
+  if (scheme != 0 && (!m.ed_nr || !m.ed_c || !m.v_p)) return IMODEL_SWM_EINVAL;
+  o.scheme = scheme;
+  if (scheme == 0) return IMODEL_SWM_OK;
+  const size_t nv = m.nv, ne = m.ne, nt = m.nt;
+  (void)nv;
+  circumcentres_and_signs(o);
+  o.h_trk.assign(nt, 0.0);
+  if (scheme == 1) {
+    o.bary.assign(3 * nt, 0.0);
+    for (size_t k = 0; k < nt; ++k) {
+      const double *pc = &o.cc[3 * k];
+      const double *p1 = m.v_p + 3 * static_cast<size_t>(m.tr_v[3 * k] - 1);
+      const double *p2 = m.v_p + 3 * static_cast<size_t>(m.tr_v[3 * k + 1] - 1);
+      const double *p3 = m.v_p + 3 * static_cast<size_t>(m.tr_v[3 * k + 2] - 1);
+      double b[3] = {std::fabs(det3(pc, p2, p3)), std::fabs(det3(pc, p3, p1)),
+                     std::fabs(det3(pc, p1, p2))};
+      double area = b[0];
+      area = area + b[1];
+      area = area + b[2];
+      for (int i = 0; i < 3; ++i) o.bary[3 * k + i] = b[i] / area;
+    }
+  }
+  if (scheme == 1 || scheme == 3) {
+    o.dist.assign(2 * ne, 0.0);
+    for (size_t l = 0; l < ne; ++l)
+      for (int i = 0; i < 2; ++i)
+        o.dist[2 * l + i] =
+            arclen(m.ed_c + 3 * l, &o.cc[3 * static_cast<size_t>(m.ed_sh[2 * l + i] - 1)]);
+  }
+  if (scheme == 2) {
+    o.edarea.assign(3 * nt, 0.0);
+    for (size_t k = 0; k < nt; ++k)
+      for (int i = 0; i < 3; ++i) {
+        const int ed = m.tr_ed[3 * k + i] - 1;
+        o.edarea[3 * k + i] =
+            sphtriarea(&o.cc[3 * k], m.v_p + 3 * static_cast<size_t>(m.ed_v[2 * ed] - 1),
+                       m.v_p + 3 * static_cast<size_t>(m.ed_v[2 * ed + 1] - 1));
+      }
+    o.h_rhb.assign(ne, 0.0);
+    o.conn.assign(12 * ne, -2);
+    for (size_t l = 0; l < ne; ++l)
+      for (int i = 0; i < 2; ++i) {
+        const int node = m.ed_v[2 * l + i] - 1;
+        for (int j = 0; j < m.nnb[node]; ++j)
+          o.conn[12 * l + 6 * i + j] =
+              edge_connection(m, static_cast<int>(l), m.v_ed[I6(node, j)] - 1);
+      }
+  }
+  if (scheme == 3) o.vhq_tr.assign(3 * nt, 0.0);
+  return IMODEL_SWM_OK;
+}
+
 int oracle_tendency(void *p, const double *h, const double *u, double *masseq, double *momeq) {
   return tendency(*static_cast<Oracle *>(p), h, u, masseq, momeq);
 }
@@ -586,8 +865,18 @@ int oracle_diagnostics(void *p, const double *h, const double *u, imodel_swm_dia
   out->kenergy = ke;
   out->tenergy = pe + ke;
   out->availenergy = out->tenergy - unavail;
+  // potential enstrophy with the kite-weighted depth at the triangles, whatever
+  // the scheme's own h_tr
   double ens = 0.0;
-  for (int k = 0; k < m.nt; ++k) ens = ens + m.tr_areag[k] * o.h_tr[k] * (o.q_tr[k] * o.q_tr[k]) * 0.5;
+  if (o.scheme == 0 || o.scheme == 3) {
+    for (int k = 0; k < m.nt; ++k) ens = ens + m.tr_areag[k] * o.h_tr[k] * (o.q_tr[k] * o.q_tr[k]) * 0.5;
+  } else {
+    for (int k = 0; k < m.nt; ++k) {
+      const double ht = o.h_trk[k];
+      const double q = ht != 0.0 ? o.eta[k] / ht : 0.0;
+      ens = ens + m.tr_areag[k] * ht * (q * q) * 0.5;
+    }
+  }
   out->pot_enstrophy = ens;
   out->rms_div = std::sqrt(sumfsq_areas(m, o.divu.data(), 0));
   double mx = 0.0;
@@ -738,6 +1027,9 @@ int oracle_field(void *p, int32_t which, double *out) {
     case 14: v = &o.lapu; break;       // with diffusion on
     case 15: v = &o.lap_lapu; break;   // with hyperdiffusion on
     case 16: v = &o.q_grad_ed; break;  // with apvm on
+    case 17: v = &o.h_rhb; break;      // gass18
+    case 18: v = &o.vhq_tr; break;     // dtred [nt][3]
+    case 19: v = &o.vhx; break;        // Perot velocity at the cells [nv][3]
     default: return IMODEL_SWM_EINVAL;
   }
   if (v->empty()) return IMODEL_SWM_ESTATE;

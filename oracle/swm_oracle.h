@@ -29,6 +29,9 @@ int oracle_set_diffusion_fields(void *o, const double *k2_hx, const double *k4_h
 /* pv_stab = "apvm" with parameter pvspar (0 = off) and the run's time step
  * dt, swm_operators.f90:1465-1543 */
 int oracle_set_apvm(void *o, double pvspar, double dt);
+/* method wrapper: 0 trsk10, 1 pxt16, 2 gass18, 3 trsk10 with the dtred
+ * Coriolis reconstruction (swm_data.f90:446-507) */
+int oracle_set_scheme(void *o, int32_t scheme);
 int oracle_tendency(void *o, const double *h, const double *u, double *masseq,
                     double *momeq);
 int oracle_rk4(void *o, const double *h, const double *u, double *h_new, double *u_new,
@@ -42,7 +45,8 @@ int oracle_trsk_weights(const imodel_swm_mesh *m, double *trskw);
 int oracle_tc2(const imodel_swm_mesh *m, double *h, double *u);
 /* copy an intermediate field of the last tendency call:
  * 0 h_ed, 1 uh, 2 eta, 3 h_tr, 4 q_tr, 5 q_ed, 6 divuh, 7 ke, 8 ghbK,
- * 9 grad_ghbK, 10 uhq_perp, 11 divu, 12 zeta, 13 eta_ed */
+ * 9 grad_ghbK, 10 uhq_perp, 11 divu, 12 zeta, 13 eta_ed, 14 lapu, 15 lap_lapu,
+ * 16 q_grad_ed, 17 h_rhb, 18 vhq_tr [nt][3], 19 v_hx [nv][3] */
 int oracle_field(void *o, int32_t which, double *out);
 
 #ifdef __cplusplus

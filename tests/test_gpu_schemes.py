@@ -1,0 +1,111 @@
+"""The pxt16, gass18 and dtred method wrappers on the GPU (FP64 handles)
+against the CPU oracle: tendencies and RK4 runs bit for bit, alone and with
+APVM and diffusion; the options an FP32 handle or a mesh without ed_nr
+cannot take are refused."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+from imodel_gb300 import _capi, fields, swm
+from imodel_gb300.swm import SWM, SWMError
+
+pytestmark = pytest.mark.gpu
+
+SCHEMES = ("pxt16", "gass18", "dtred")
+
+
+@pytest.mark.parametrize("scheme", SCHEMES)
+@pytest.mark.parametrize("level", [2, 4, 5])
+def test_tendency_bitwise(grid_at, scheme, level):
+    g = grid_at(level)
+    h, u = swm.initialize_fields_tc2(g)
+    rng = np.random.default_rng(level)
+    h = h + rng.normal(0, 5.0, g.nv)   # unbalanced: all terms active
+    u = u + rng.normal(0, 2.0, g.ne)
+    m = SWM(g, "fp64", scheme=scheme)
+    mg, ug = m.tendency(h, u)
+    mr, ur = oracle.Oracle(g, 2, scheme=scheme).tendency(h, u)
+    assert np.array_equal(mg, mr), np.max(np.abs(mg - mr))
+    assert np.array_equal(ug, ur), np.max(np.abs(ug - ur))
+    m.close()
+
+
+@pytest.mark.parametrize("scheme", SCHEMES)
+def test_balanced_state_run_bitwise(grid_at, scheme):
+    """160 RK4 steps (1.7 days) of a seeded balanced state at level 4."""
+    g = grid_at(4)
+    h, u = fields.balanced_state(g, lmax=16, seed=21)
+    m = SWM(g, "fp64", scheme=scheme)
+    m.set_state(h, u)
+    m.advance(900.0, 160)
+    hg, ug = m.get_state()
+    d = m.diagnostics()
+    m.close()
+    o = oracle.Oracle(g, 2, scheme=scheme)
+    hr, ur = o.run(h, u, 900.0, 160)
+    assert np.array_equal(hg, hr) and np.array_equal(ug, ur), (
+        np.max(np.abs(hg - hr)), np.max(np.abs(ug - ur)))
+    o.tendency(hr, ur)
+    # the diagnostics come from the last stage input in both
+    mass0 = float(np.sum(g.hx_areag * h) / np.sum(g.hx_areag))
+    assert abs(d["mass"] - mass0) <= 1e-13 * mass0
+
+
+@pytest.mark.parametrize("scheme", SCHEMES)
+def test_with_apvm_and_diffusion_bitwise(grid_at, scheme):
+    g = grid_at(4)
+    h, u = fields.balanced_state(g, lmax=12, seed=22)
+    dt = 600.0
+    m = SWM(g, "fp64", scheme=scheme)
+    m.set_apvm(0.5, dt)
+    m.set_diffusion(1.0e5, 1.0e13)
+    o = oracle.Oracle(g, 2, scheme=scheme, pvspar=0.5, dt=dt, k2=1.0e5, k4=1.0e13)
+    hg, ug = m.ode_rk4(h, u, dt, 6)
+    hr, ur = o.run(h, u, dt, 6)
+    assert np.array_equal(hg, hr) and np.array_equal(ug, ur)
+    m.close()
+
+
+def test_launch_counts(grid_at):
+    g = grid_at(3)
+    base = SWM(g, "fp64").launch_count(1)
+    assert SWM(g, "fp64", scheme="pxt16").launch_count(1) == base
+    assert SWM(g, "fp64", scheme="gass18").launch_count(1) == base
+    assert SWM(g, "fp64", scheme="dtred").launch_count(1) == base + 4
+
+
+def test_refusals(grid_at):
+    g = grid_at(3)
+    with pytest.raises(SWMError) as e:
+        SWM(g, "fp32", scheme="pxt16")
+    assert e.value.code == _capi.EINVAL
+    # a mesh without ed_nr cannot feed pered / dtred / the circumcentres
+    mesh = _capi.Mesh.from_buffer_copy(g.c_struct())  # the grid's own struct stays intact
+    mesh.ed_nr = None
+    opts = _capi.Opts()
+    opts.precision = _capi.FP64
+    opts.testcase = 2
+    opts.scheme = _capi.SCHEMES["gass18"]
+    h = ctypes.c_void_p()
+    lib = _capi.swm_lib()
+    rc = lib.imodel_swm_create(ctypes.byref(mesh), ctypes.byref(opts),
+                               ctypes.byref(h))
+    assert rc == _capi.EINVAL
+    lib.imodel_swm_destroy(h)
+    opts.scheme = 9
+    rc = lib.imodel_swm_create(ctypes.byref(g.c_struct()), ctypes.byref(opts),
+                               ctypes.byref(h))
+    assert rc == _capi.EINVAL
+    lib.imodel_swm_destroy(h)
+
+
+def test_gass_divide_guard(grid_at):
+    """An all-zero depth trips scalar_elem_divide's guard (swm_operators.f90:
+    1604-1606) in the triangle PV and the rhombus PV alike."""
+    g = grid_at(2)
+    m = SWM(g, "fp64", scheme="gass18")
+    with pytest.raises(SWMError) as e:
+        m.tendency(np.zeros(g.nv), np.zeros(g.ne))
+    assert e.value.code == _capi.EDIVZERO
