@@ -76,7 +76,7 @@ class Opts(ctypes.Structure):
         ("bt", c_f64p), ("h_ref", ctypes.c_double), ("device", ctypes.c_int32),
         ("learned", ctypes.c_int32), ("mlp_weights", ctypes.c_void_p),
         ("mlp_bytes", ctypes.c_size_t), ("drift_bound", ctypes.c_double),
-        ("scheme", ctypes.c_int32),
+        ("scheme", ctypes.c_int32), ("fsphere", ctypes.c_int32), ("fcte", ctypes.c_double),
     ]
 
 

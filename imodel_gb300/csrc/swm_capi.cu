@@ -547,8 +547,13 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
     return set_error(H, IMODEL_SWM_EINVAL, "unknown scheme");
   if (scheme != IMODEL_SWM_TRSK10 && H->precision != IMODEL_SWM_FP64)
     return set_error(H, IMODEL_SWM_EINVAL, "the pxt16, gass18 and dtred schemes run on FP64 handles");
+  const int fsphere = o ? o->fsphere : 0;
+  const double fcte = o ? o->fcte : 0.0;
+  if (fsphere != 0 && fsphere != 2)
+    return set_error(H, IMODEL_SWM_EINVAL, "fsphere must be 0 (f = 2 Omega sin lat) or 2 (f = fcte)");
+  if (fsphere == 2 && !std::isfinite(fcte)) return set_error(H, IMODEL_SWM_EINVAL, "fcte must be finite");
   Layout L;
-  std::string msg = build_layout(*m, o ? o->bt : nullptr, L, scheme);
+  std::string msg = build_layout(*m, o ? o->bt : nullptr, L, scheme, fsphere, fcte);
   if (!msg.empty()) return set_error(H, IMODEL_SWM_EINVAL, msg);
   H->nv = L.nv;
   H->ne = L.ne;

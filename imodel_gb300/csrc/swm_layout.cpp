@@ -153,7 +153,8 @@ int edge_connection(const imodel_swm_mesh &m, int ed1, int ed2) {
 
 }  // namespace
 
-std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, int scheme) {
+std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, int scheme,
+                         int fsphere, double fcte) {
   const int nv = m.nv, ne = m.ne, nt = m.nt;
   if (nv < 4 || ne < 6 || nt < 4) return "mesh sizes too small";
   if (!m.nnb || !m.v_ed || !m.v_tr || !m.hx_ttgout || !m.hx_tnrccw || !m.hx_areag ||
@@ -412,7 +413,9 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
     const int t = L.tri_n2o[i];
     const double A = m.tr_areag[t];
     L.t_areag[i] = A;
-    L.t_f[i] = 2.0 * m.omega * std::sin(m.tr_c_lat[t]);
+    // vort_tr's Coriolis parameter (swm_operators.f90:592-601): 2.*Omega*
+    // dsin(lat) (fsphere 0) or the constant fcte (fsphere 2)
+    L.t_f[i] = fsphere == 2 ? fcte : 2.0 * m.omega * std::sin(m.tr_c_lat[t]);
     L.t_f32[i] = static_cast<float>(L.t_f[i]);
     for (int s = 0; s < 3; ++s) {
       const int e = m.tr_ed[3 * static_cast<size_t>(t) + s] - 1;

@@ -126,9 +126,10 @@ struct Layout {
 };
 
 // Builds the layout from a reference mesh; returns "" or an error message.
-// scheme (IMODEL_SWM_TRSK10 ... IMODEL_SWM_DTRED) selects the extra geometry.
+// scheme (IMODEL_SWM_TRSK10 ... IMODEL_SWM_DTRED) selects the extra geometry;
+// fsphere = 2 sets f = fcte at every triangle instead of 2 Omega sin(lat).
 std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L,
-                         int scheme = IMODEL_SWM_TRSK10);
+                         int scheme = IMODEL_SWM_TRSK10, int fsphere = 0, double fcte = 0.0);
 
 // Inputs of the learned TRSK correction (imodel_gb300/learned.py), device
 // order: per edge the 10 stencil edges as sign * (index + 1) (0 = padding),

@@ -116,12 +116,14 @@ class SWM:
     "fp32" runs FP32 state and operators with FP64 integrals.
     scheme: the method wrapper of swm.par, "trsk10", "pxt16", "gass18", or
     "dtred" (trsk10 with the dtred Coriolis reconstruction); the last three
-    on "fp64" handles.
+    on "fp64" handles.  fsphere = 2 replaces f = 2 Omega sin(lat) by the
+    constant fcte (the f-sphere of test cases 33, 35, 40-42).
     """
 
     def __init__(self, grid: Grid, precision: str = "fp64", testcase: int = 2,
                  bt=None, h_ref: float = 0.0, device: int = 0, learned_params=None,
-                 drift_bound: float = 0.0, scheme: str = "trsk10"):
+                 drift_bound: float = 0.0, scheme: str = "trsk10", fsphere: int = 0,
+                 fcte: float = 0.0):
         self.grid = grid
         self.lib = _capi.swm_lib()
         self.precision = precision
@@ -137,6 +139,8 @@ class SWM:
         opts.device = device
         opts.scheme = _capi.SCHEMES[scheme]
         self.scheme = scheme
+        opts.fsphere = fsphere
+        opts.fcte = fcte
         self._mlp = None
         if learned_params is not None:
             # learned TRSK correction (network parameters, see imodel_mlp.h)

@@ -14,7 +14,14 @@ adds:
   swm.f90:1426-1620, height ``h_tc6`` at :2392-2413);
 * 21, 22, 23 -- the Galewsky et al. (2004) barotropic jet with its height
   perturbation (21), without it (22, a steady balanced jet), and the
-  200 m/s jet with the perturbation (23) (swm.f90:1646-1810).
+  200 m/s jet with the perturbation (23) (swm.f90:1646-1810); 52 and 53 the
+  same jet in the southern hemisphere, without and with a perturbation;
+* 32-35 -- the Hollingsworth-instability cases: a thin layer over a bottom
+  carrying case 2's balanced height (swm.f90:1918-2068);
+* 40-43 -- localised steady states on an f-sphere, two of them rotated
+  (swm.f90:2070-2371);
+* 51 -- case 5's flow as a thin layer over a Gaussian hill (:1380-1398);
+* 56, 57 -- Matsuno's equatorial waves.
 
 Every field is returned in the grid's (reference) ordering; u is the normal
 component along ``ed%tg`` at the triangle-edge midpoint ``ed%c``, as the
@@ -38,7 +45,26 @@ from .swm import convert_vec_sph2cart, dot3, initialize_fields_tc2
 
 GRAVI = 1.0 / GRAV
 PIO2 = PI / 2.0
+DEG2RAD = PI / 180.0                   # constants.f90, pi/180._r8
 EPS = float(np.finfo(np.float32).eps)  # constants.f90:45, epsilon(1.)
+HOLLGW = 2.0                           # swm.par's Hollingsworth layer depth (par/swm.par:29)
+
+
+def ipow(x, n: int):
+    """x**n for an integer n as the Fortran run time evaluates it: square
+    and multiply, low bits first (not pow(), whose rounding differs)."""
+    x = np.asarray(x, dtype=np.float64)
+    result = np.ones_like(x)
+    base = x.copy()
+    u = int(n)
+    while True:
+        if u & 1:
+            result = result * base
+        u >>= 1
+        if not u:
+            break
+        base = base * base
+    return result
 
 
 def lonlat(p):
@@ -212,9 +238,13 @@ def galewsky(grid: Grid, testcase: int = 21):
     rule on d(gh)/dlat = -a u (f + tan(lat) u / a), shifted to a 10 km mean
     depth and interpolated to the cells (cubic Lagrange, linear in the end
     intervals); cases 21 and 23 add the 120 m height bump at (0, pi/4)."""
-    u00 = 200.0 if testcase == 23 else 80.0
-    lat0 = PI / 7.0
-    lat1 = PI / 2.0 - lat0
+    if testcase in (52, 53):
+        # the jet in the southern hemisphere between 5 and 45 degrees south
+        u00, lat0, lat1 = 80.0, -5.0 * DEG2RAD, -45.0 * DEG2RAD
+    else:
+        u00 = 200.0 if testcase == 23 else 80.0
+        lat0 = PI / 7.0
+        lat1 = PI / 2.0 - lat0
     en = np.exp(-4.0 / (lat1 - lat0) ** 2)
     umen = u00 / en
 
@@ -255,13 +285,143 @@ def galewsky(grid: Grid, testcase: int = 21):
 
     u = _edge_u(grid, jet(grid.ed_c_lat), 0.0)
 
-    if testcase in (21, 23):
+    if testcase in (21, 23, 53):
         hpert, alpha, bet = 120.0, 1.0 / 3.0, 1.0 / 15.0
-        lat2 = 0.5 * PIO2
+        lat2 = -25.0 * DEG2RAD if testcase == 53 else 0.5 * PIO2
         lon, _ = lonlat(grid.v_p)
+        if testcase == 53:
+            lon = lon + 120.0 * DEG2RAD
         h = h + hpert * np.cos(grid.v_lat) * np.exp(-(lon / alpha) ** 2) \
             * np.exp(-((lat2 - grid.v_lat) / bet) ** 2)
     return h, u, np.zeros(grid.nv)
+
+
+# ---- case 51 ----------------------------------------------------------------
+def tc51(grid: Grid, hollgw: float = HOLLGW):
+    """Case 5's zonal flow as a thin layer (the Hollingsworth depth) over a
+    bottom that carries the balanced case-5 height plus a 20 m Gaussian hill
+    at (-pi/2, pi/6) (swm.f90:1380-1398); the layer thins by the hill's
+    height so that the free surface stays balanced."""
+    u0, h0 = 20.0, 5960.0
+    h_ct = (ERAD * OMEGA * u0 + (u0 * u0) / 2.0) * GRAVI
+    lon0, lat0, rmax = -PI * 0.5, PI / 6.0, PI / 9.0
+    p0 = sph2cart(lon0, lat0)
+    d = grid.v_p - p0
+    r = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
+    rmaxc = 2 * (1 - np.cos(rmax))
+    c04 = float(np.float32(0.4))   # -0.4 is a default-real literal
+    hill = 20.0 * np.exp(-c04 * r ** 2 / rmaxc ** 2)
+    bt = (h0 - h_ct * np.sin(grid.v_lat) ** 2) + hill
+    h = hollgw - hill
+    u = _edge_u(grid, u0 * np.cos(grid.ed_c_lat), 0.0)
+    return h, u, bt
+
+
+# ---- cases 32-35: the Hollingsworth instability ---------------------------
+def hollingsworth(grid: Grid, testcase: int = 32, hollgw: float = HOLLGW):
+    """A thin layer of depth hollgw riding on a bottom that carries case 2's
+    balanced height (swm.f90:1918-2068): 32 and 34 in the rotating frame,
+    33 and 35 on an f = 0 sphere (f-sphere, fcte = 0) with the matching
+    balance (u0^2/2 only).  34 and 35 start from the same states as 32 and
+    33.  Their time loop's linear analysis (swm.f90:251-281: a forcing, a
+    perturbation of cell 18, and a rescaling of the departure to 1e-6 of u)
+    is not built: at the first step the forcing cancels the departure in u
+    to rounding -- exactly, on the grids tried -- and the rescaling factor
+    1e-6 / error2_u is then infinite."""
+    if testcase not in (32, 33, 34, 35):
+        raise ValueError("Hollingsworth cases are 32-35")
+    if not hollgw > EPS:
+        raise ValueError("the Hollingsworth cases need a positive layer depth")
+    u0 = 2.0 * PI * ERAD / (12.0 * DAY2SEC)
+    h0 = 2.94e4 * GRAVI
+    if testcase in (33, 35):
+        h_ct = ((u0 * u0) / 2.0) * GRAVI
+    else:
+        h_ct = (ERAD * OMEGA * u0 + (u0 * u0) / 2.0) * GRAVI
+    bt = h0 - h_ct * np.sin(grid.v_lat) ** 2
+    # fsphere = 2 subtracts (erad / grav) fcte sin(lat), with fcte = 0
+    h = np.full(grid.nv, float(hollgw))
+    u = _edge_u(grid, u0 * np.cos(grid.ed_c_lat), 0.0)
+    return h, u, bt
+
+
+# ---- cases 40-43: localised steady states ---------------------------------
+def _rotation(lon0: float, lat0: float):
+    """Rmat of swm.f90:2146-2156: takes (lon0, lat0) to the north pole."""
+    R = np.zeros((3, 3))
+    R[0, 0] = np.sin(lat0) * np.cos(lon0)
+    R[0, 1] = np.sin(lat0) * np.sin(lon0)
+    R[0, 2] = -np.cos(lat0)
+    R[1, 0] = -np.sin(lon0)
+    R[1, 1] = np.cos(lon0)
+    R[2, 0] = np.cos(lat0) * np.cos(lon0)
+    R[2, 1] = np.cos(lat0) * np.sin(lon0)
+    R[2, 2] = np.sin(lat0)
+    return R
+
+
+def _matvec(R, p):
+    """matmul(R, p) for points p[..., 3], each component summed in order."""
+    p = np.asarray(p, dtype=np.float64)
+    out = np.empty_like(p)
+    for i in range(3):
+        s = R[i, 0] * p[..., 0]
+        s = s + R[i, 1] * p[..., 1]
+        s = s + R[i, 2] * p[..., 2]
+        out[..., i] = s
+    return out
+
+
+def localised(grid: Grid, testcase: int = 40):
+    """Steady localised states on an f-sphere (swm.f90:2070-2331):
+
+    * 40 -- h = h0 (2 - sin(lat)^n), u = u0 sin(lat)^k cos(lat), k = 120,
+      n = 2k + 2, h0 = 10^4 / g, u0 = sqrt(n h0 g), f = 0;
+    * 41 -- the same with h0 = 10^5 / g, rotated so that its peak sits at
+      (1, 3) degrees;
+    * 42 -- k = 160 with f = 1.4584e-4 s^-1, rotated: the northern cap in
+      cyclogeostrophic balance u^2 + F u + C = 0, the rest at rest;
+    * 43 -- a 20 m/s easterly equatorial jet exp(-50 lat^2) over h = 100 m
+      (not balanced: the reference's "play toy")."""
+    if testcase == 43:
+        umen = -20.0 / 1.0
+        u = _edge_u(grid, umen * np.exp(-(grid.ed_c_lat - 0.0) ** 2 * 50.0), 0.0)
+        return np.full(grid.nv, 100.0), u, np.zeros(grid.nv)
+    if testcase == 40:
+        h0, k = 10000 * GRAVI, 120
+    elif testcase == 41:
+        h0, k = 100000 * GRAVI, 120
+    elif testcase == 42:
+        h0, k = 100000 * GRAVI, 160
+    else:
+        raise ValueError("localised cases are 40-43")
+    n = k * 2 + 2
+    u0 = np.sqrt(n * h0 * GRAV)
+    if testcase == 40:
+        h = h0 * (2 - ipow(np.sin(grid.v_lat), n))
+        lat = grid.ed_c_lat
+        u = _edge_u(grid, u0 * ipow(np.sin(lat), k) * np.cos(lat), 0.0)
+        return h, u, np.zeros(grid.nv)
+    R = _rotation(1 * DEG2RAD, 3 * DEG2RAD)
+    _, vlat = lonlat(_matvec(R, grid.v_p))
+    if testcase == 41:
+        h = h0 * (2 - ipow(np.sin(vlat), n))
+    else:
+        h = np.where(vlat > 0, h0 * (2 - ipow(np.sin(vlat), n)), 2.0 * h0)
+    pe = _matvec(R, grid.ed_c)
+    _, elat = lonlat(pe)
+    if testcase == 41:
+        ut = u0 * ipow(np.sin(elat), k) * np.cos(elat)
+    else:
+        fcte = 1.4584e-4
+        with np.errstate(divide="ignore", invalid="ignore"):
+            F = np.where(np.abs(elat) > EPS, ERAD * fcte * np.cos(elat) / np.sin(elat), 0.0)
+        C = -GRAV * h0 * n * ipow(np.sin(elat), n - 2) * ipow(np.cos(elat), 2)
+        with np.errstate(invalid="ignore"):
+            ut = np.where(elat > 0, (-F + np.sqrt(F * F - 4 * C)) / 2, 0.0)
+    v = convert_vec_sph2cart(ut, 0.0, pe)
+    v = _matvec(R.T, v)
+    return h, dot3(v, grid.ed_tg), np.zeros(grid.nv)
 
 
 # ---- cases 56, 57: Matsuno equatorial waves ------------------------------
@@ -346,14 +506,41 @@ def matsuno(grid: Grid, testcase: int):
 
 CASES = {0: tc0, 1: tc1, 2: None, 5: tc5, 6: tc6,
          21: galewsky, 22: lambda g: galewsky(g, 22), 23: lambda g: galewsky(g, 23),
+         32: hollingsworth, 33: lambda g: hollingsworth(g, 33),
+         34: lambda g: hollingsworth(g, 34), 35: lambda g: hollingsworth(g, 35),
+         40: localised, 41: lambda g: localised(g, 41), 42: lambda g: localised(g, 42),
+         43: lambda g: localised(g, 43), 51: tc51,
+         52: lambda g: galewsky(g, 52), 53: lambda g: galewsky(g, 53),
          56: lambda g: matsuno(g, 56), 57: lambda g: matsuno(g, 57)}
+
+# cases whose vort_tr runs on an f-sphere (fsphere = 2, constant fcte)
+F_SPHERE = {33: 0.0, 35: 0.0, 40: 0.0, 41: 0.0, 42: 1.4584e-4}
+
+# cases that need input data the reference does not ship: 24 reads a
+# day-5 ENDGame state from its output directory (swm.f90:1812-1916), 60 the
+# ETOPO elevation data of the Andes (refinter.f90:381-469); 11 and 12 are
+# the linearised equations of the normal-mode analysis, not a time step
+UNAVAILABLE = {24: "needs a day-5 ENDGame GLW state file",
+               60: "needs the ETOPO elevation data",
+               11: "linearised normal-mode equations", 12: "linearised normal-mode equations"}
+
+
+def case_options(testcase: int) -> dict:
+    """Keyword options of swm.SWM and oracle.Oracle a test case needs
+    (testcase number for the momentum switch; the f-sphere)."""
+    opts = {"testcase": testcase}
+    if testcase in F_SPHERE:
+        opts.update(fsphere=2, fcte=F_SPHERE[testcase])
+    return opts
 
 
 def initialize_fields(grid: Grid, testcase: int):
-    """(h[nv], u[ne], bt[nv]) of a test case (0, 1, 2, 5, 6, 21-23, 56, 57)."""
+    """(h[nv], u[ne], bt[nv]) of a test case (see CASES)."""
     if testcase == 2:
         h, u = initialize_fields_tc2(grid)
         return h, u, np.zeros(grid.nv)
+    if testcase in UNAVAILABLE:
+        raise ValueError(f"test case {testcase}: {UNAVAILABLE[testcase]}")
     if testcase not in CASES:
         raise ValueError(f"test case {testcase} is not built (cases: {sorted(CASES)})")
     return CASES[testcase](grid)

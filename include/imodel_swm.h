@@ -126,6 +126,13 @@ typedef struct imodel_swm_opts {
                          other wrappers need the mesh's ed_nr and ed_c and
                          run on FP64 handles (an FP32 handle, the learned
                          correction or an ensemble takes trsk10 only)   */
+  int32_t fsphere;    /* Coriolis parameter of vort_tr (swm_operators.f90:
+                         551-611): 0 f = 2 Omega sin(lat) at the triangle
+                         circumcentres; 2 the constant fcte (f-sphere, test
+                         cases 33, 35, 40-42).  The linearised branch 1 of
+                         the normal-mode cases is not a time step and is
+                         refused                                         */
+  double fcte;        /* f for fsphere = 2 (s^-1)                          */
 } imodel_swm_opts;
 
 /* ---- diagnostics (swm.f90:293-322, :2686-2752, :3394-3440) ------------- */

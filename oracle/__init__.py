@@ -64,6 +64,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_set_diffusion.argtypes = [vp, ctypes.c_double, ctypes.c_double]
         L.oracle_set_apvm.argtypes = [vp, ctypes.c_double, ctypes.c_double]
         L.oracle_set_scheme.argtypes = [vp, ctypes.c_int32]
+        L.oracle_set_fcor.argtypes = [vp, ctypes.c_int32, ctypes.c_double]
         L.oracle_set_diffusion_fields.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
         _lib = L
     return _lib
@@ -90,7 +91,7 @@ class Oracle:
 
     def __init__(self, grid, testcase: int = 2, bt=None, nthreads: int = 0, k2: float = 0.0,
                  k4: float = 0.0, pvspar: float = 0.0, dt: float = 0.0, k2_hx=None,
-                 k4_hx=None, scheme: str = "trsk10"):
+                 k4_hx=None, scheme: str = "trsk10", fsphere: int = 0, fcte: float = 0.0):
         self.grid = grid
         self._mesh = grid.c_struct()
         self._bt = None if bt is None else np.ascontiguousarray(bt, dtype=np.float64)
@@ -98,6 +99,9 @@ class Oracle:
         self.nthreads = n
         self._h = lib().oracle_create(ctypes.byref(self._mesh), testcase,
                                       None if self._bt is None else _p(self._bt), n)
+        if fsphere:
+            if lib().oracle_set_fcor(self._h, fsphere, fcte):
+                raise ValueError("fsphere must be 0 or 2")
         if scheme != "trsk10":
             if lib().oracle_set_scheme(self._h, SCHEMES[scheme]):
                 raise ValueError(f"bad scheme {scheme!r} (or the mesh lacks ed_nr / ed_c)")

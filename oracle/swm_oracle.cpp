@@ -738,6 +738,16 @@ int oracle_set_diffusion_fields(void *p, const double *k2_hx, const double *k4_h
   return set_diffusion(o, 0.0, 0.0, k2_hx, k4_hx);
 }
 
+// vort_tr's Coriolis parameter (swm_operators.f90:592-601): fsphere 0
+// 2.*Omega*dsin(lat), fsphere 2 the constant fcte
+int oracle_set_fcor(void *p, int32_t fsphere, double fcte) {
+  Oracle &o = *static_cast<Oracle *>(p);
+  if (fsphere != 0 && fsphere != 2) return IMODEL_SWM_EINVAL;
+  for (int k = 0; k < o.m.nt; ++k)
+    o.fcor[k] = fsphere == 2 ? fcte : 2.0 * o.m.omega * std::sin(o.m.tr_c_lat[k]);
+  return IMODEL_SWM_OK;
+}
+
 int oracle_set_apvm(void *p, double pvspar, double dt) {
   Oracle &o = *static_cast<Oracle *>(p);
   const imodel_swm_mesh &m = o.m;

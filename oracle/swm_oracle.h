@@ -29,6 +29,9 @@ int oracle_set_diffusion_fields(void *o, const double *k2_hx, const double *k4_h
 /* pv_stab = "apvm" with parameter pvspar (0 = off) and the run's time step
  * dt, swm_operators.f90:1465-1543 */
 int oracle_set_apvm(void *o, double pvspar, double dt);
+/* Coriolis parameter: fsphere 0 (2 Omega sin lat) or 2 (constant fcte),
+ * vort_tr, swm_operators.f90:592-601 */
+int oracle_set_fcor(void *o, int32_t fsphere, double fcte);
 /* method wrapper: 0 trsk10, 1 pxt16, 2 gass18, 3 trsk10 with the dtred
  * Coriolis reconstruction (swm_data.f90:446-507) */
 int oracle_set_scheme(void *o, int32_t scheme);

@@ -156,3 +156,76 @@ def test_galewsky_jet(grid_at):
     m, mo = o.tendency(h22, u22)
     grad = o.field("grad_ghbK")
     assert np.sqrt(np.mean(mo ** 2)) < 0.05 * np.sqrt(np.mean(grad ** 2))
+
+
+def test_localised_steady_states_converge(grid_at):
+    """Cases 40-42 are steady states of the continuous equations on an
+    f-sphere: the discrete momentum tendency, relative to the height
+    gradient it balances, falls with resolution."""
+    for case in (40, 41, 42):
+        res = []
+        for L in (4, 5, 6):
+            g = grid_at(L)
+            h, u, bt = tc.initialize_fields(g, case)
+            o = oracle.Oracle(g, bt=bt, **tc.case_options(case))
+            _, mo = o.tendency(h, u)
+            res.append(np.abs(mo).max() / np.abs(o.field("grad_ghbK")).max())
+        assert res[0] > res[1] > res[2], (case, res)
+
+
+def test_f_sphere_option_sets_constant_f(grid_at):
+    """fsphere = 2 adds the constant fcte to the relative vorticity in place
+    of 2 Omega sin(lat) (vort_tr, swm_operators.f90:592-601)."""
+    g = grid_at(3)
+    h, u, bt = tc.initialize_fields(g, 42)
+    a = oracle.Oracle(g, 42, fsphere=2, fcte=1.4584e-4)
+    b = oracle.Oracle(g, 42, fsphere=2, fcte=0.0)
+    a.tendency(h, u)
+    b.tendency(h, u)
+    np.testing.assert_allclose(a.field("eta") - b.field("eta"), 1.4584e-4, rtol=1e-9, atol=0)
+    np.testing.assert_allclose(b.field("eta"), b.field("zeta"), rtol=1e-13, atol=1e-20)
+
+
+def test_southern_jet_and_its_bump(grid_at):
+    g = grid_at(6)
+    h52, u52, _ = tc.initialize_fields(g, 52)
+    h53, u53, _ = tc.initialize_fields(g, 53)
+    assert np.array_equal(u52, u53)
+    # the jet lies between 45 and 5 degrees south and peaks at 80 m/s
+    lat = np.degrees(g.ed_c_lat)
+    assert np.all(np.abs(u52[(lat > -4.9) | (lat < -45.1)]) < 1e-12)
+    assert 75.0 < np.abs(u52).max() <= 80.0
+    # 53 adds the 120 m bump centred at (-120, -25) degrees
+    d = h53 - h52
+    k = np.argmax(d)
+    lon, _ = tc.lonlat(g.v_p)
+    assert 100.0 < d.max() <= 120.0
+    assert abs(np.degrees(lon[k]) + 120.0) < 3.0 and abs(np.degrees(g.v_lat[k]) + 25.0) < 3.0
+
+
+def test_hollingsworth_and_case51_layers(grid_at):
+    g = grid_at(5)
+    s = np.sin(g.v_lat)
+    u0 = 2.0 * tc.PI * ERAD / (12 * 86400.0)
+    for case in (32, 33):
+        h, u, bt = tc.initialize_fields(g, case)
+        assert np.all(h == tc.HOLLGW)
+        # a divergence-free zonal flow: the mass tendency is truncation error
+        # only, far below the scale h u0 / a of its terms
+        o = oracle.Oracle(g, bt=bt, **tc.case_options(case))
+        m, _ = o.tendency(h, u)
+        assert np.abs(m).max() < 1e-2 * tc.HOLLGW * u0 / ERAD
+    h32, _, b32 = tc.initialize_fields(g, 32)
+    h33, _, b33 = tc.initialize_fields(g, 33)
+    assert np.all(b33 >= b32)   # the f = 0 balance needs a smaller pole-equator drop
+    h, u, bt = tc.tc51(g, hollgw=50.0)
+    h_ct = (ERAD * 7.292e-5 * 20.0 + 200.0) / 9.80616
+    np.testing.assert_allclose(h + bt, 50.0 + 5960.0 - h_ct * s * s, rtol=0, atol=1e-9)
+    assert 49.0 - 20.0 < h.min() < 31.0
+
+
+def test_unavailable_cases_are_named():
+    with pytest.raises(ValueError, match="ENDGame"):
+        tc.initialize_fields(None, 24)
+    with pytest.raises(ValueError, match="ETOPO"):
+        tc.initialize_fields(None, 60)
