@@ -8,10 +8,13 @@ degree 1..64 with N(0,1) coefficients times l^-2, seed 0, scaled to a
 40 m/s maximum wind; h from linear balance, mean g h = 2.94e4; flat
 bottom).  One "step" is one RK4 time step of the whole grid.
 
-  value      cell-steps/s of the FP32 path with the learned TRSK correction
-             (per-edge MLP evaluated once per step on the tensor cores),
-             state resident in HBM (graph-replayed steps, CUDA events on the
-             library's stream)
+  value      cell-steps/s of the FP32 path with the learned TRSK weights
+             (a per-kite-slot MLP, evaluated once on the tensor cores when
+             the handle is created, corrects the kite fractions TRSK builds
+             its weights from), state resident in HBM (graph-replayed
+             steps, CUDA events on the library's stream)
+  fp32_step_net  the FP32 path with the per-step learned correction (a
+             per-edge MLP on the stencil velocities, once per step)
   fp32_plain the same without the learned correction
   fp64       the same for the FP64 reference-order path, with its own
              end-to-end figure
@@ -20,10 +23,11 @@ bottom).  One "step" is one RK4 time step of the whole grid.
              and u (FP64) to the device and back inside the timed region
   error_vs_fp64  relative L2 and max-norm differences of the FP32 and
              FP32 + learned states from the FP64 state after the same steps
-             from the same start
+             from the same start (the learned schemes differ from TRSK by
+             design: their accuracy is measured against finer runs)
   roofline   the dominant stencil kernel against the measured HBM copy
-             bandwidth; mlp_roofline the network kernel against the
-             measured BF16 tensor throughput; step_roofline the whole step
+             bandwidth; mlp_roofline the per-step network kernel against HBM
+             and the measured BF16 tensor throughput; step_roofline the whole step
              with the layout's own bytes per cell-step beside the 2000 B
              model
   cpu_baseline  the CPU oracle (C++ restatement of the Fortran, OpenMP on
@@ -330,7 +334,11 @@ def run_reference(args):
 def config_dict(g, path, weights=None):
     learned = "off"
     if path == "fp32l":
-        learned = ("per-edge MLP 24-64-64-1, BF16 tcgen05, once per step; weights " +
+        learned = ("learned TRSK weights: per-kite-slot MLP 24-64-64-1 (BF16, tcgen05) "
+                   "corrects the kite fractions once at create, TRSK weights rebuilt; "
+                   "parameters " + (weights or "none"))
+    elif path == "fp32n":
+        learned = ("per-edge MLP 24-64-64-1, BF16 tcgen05, once per step; parameters " +
                    (weights or "none"))
     return {"workload": f"icos-L{g.level} TRSK shallow-water RK4 step, trsk10/HTC/geo, "
                         f"dt={DT:g} s, {STATE_NAME}",
@@ -381,7 +389,7 @@ def main():
     # switches for profiler runs: time only the listed paths (fp64, fp32 =
     # plain FP32, fp32l = FP32 + learned correction), skip the end-to-end
     # and per-kernel passes
-    ap.add_argument("--precisions", default="fp64,fp32,fp32l")
+    ap.add_argument("--precisions", default="fp64,fp32,fp32l,fp32n")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-kprof", action="store_true")
     ap.add_argument("--tuning", default="",
@@ -407,19 +415,26 @@ def main():
     assert cr.lib.cudaSetDevice(local) == 0
     D = Dist(local)
 
-    params = learned.trained_params()
-    weights = "trained on icos-L7 (imodel_gb300/data/trsk_mlp_l7.npy)"
-    if params is None:
-        params = learned.init_params(0)
-        weights = "untrained (Glorot initial values, seed 0)"
+    from imodel_gb300 import learned_weights
+    params_n = learned.trained_params()
+    weights_n = "trained on icos-L7 (imodel_gb300/data/trsk_mlp_l7.npy)"
+    if params_n is None:
+        params_n = learned.init_params(0)
+        weights_n = "untrained (Glorot initial values, seed 0)"
+    params_w = learned_weights.trained_params()
+    weights_w = "trained on icos-L5 and L6 (imodel_gb300/data/trsk_kite_mlp.npy)"
+    if params_w is None:
+        params_w = learned.init_params(0)
+        weights_w = "untrained (Glorot initial values, seed 0)"
     results = {}
     paths = [p for p in args.precisions.split(",") if p]
     headline = "fp32l" if "fp32l" in paths else "fp32"
     for path in paths:
         m = swm.SWM(g, precision="fp64" if path == "fp64" else "fp32", device=local,
-                    learned_params=params if path == "fp32l" else None)
+                    learned_params=params_n if path == "fp32n" else None,
+                    learned_weights=params_w if path == "fp32l" else None)
         m.set_state(h, u)
-        if args.apvm > 0 and path != "fp32l":
+        if args.apvm > 0 and path not in ("fp32l", "fp32n"):
             m.set_apvm(args.apvm, DT)
         tuning = None
         if path != "fp64":
@@ -482,7 +497,7 @@ def main():
     if rank == 0 and not full:
         # profiler runs: a short line with the timed paths only
         print(json.dumps({k: {"ms_per_step": v["ms"] / args.steps} for k, v in results.items()
-                          if k in ("fp32", "fp32l", "fp64")}))
+                          if k in ("fp32", "fp32l", "fp32n", "fp64")}))
     elif rank == 0:
         rh, r64 = results[headline], results["fp64"]
         total_cells = g.nv * ws
@@ -502,23 +517,17 @@ def main():
         kb = kernel_bytes(g.nv, g.ne, g.nt, "fp32", variant)
         prof = {k: v for k, v in rh["prof"].items() if k != "edge_pre" or kb["edge_pre"]}
         dom = max(prof, key=prof.get)
-        if headline == "fp32l":
-            # the profile's edge_pre slot is the network, once per step
-            stencil = {k: v for k, v in prof.items() if k != "edge_pre"}
-            dom = max(stencil, key=stencil.get)
         achieved = kb[dom] / (prof[dom] / 1000.0) / 1e9
         # whole-step bytes: the 2000 B/cell-step model and this layout's own
-        # (four stages of the stencil kernels, plus the network once per step)
+        # (four stages of the stencil kernels; the learned weights add none)
         layout_step = 4 * sum(kb.values())
-        if headline == "fp32l":
-            layout_step += mlp_bytes(g.nv, g.ne, g.nt)
         sec_step = rh["ms"] / args.steps / 1000.0
         kernel_ms = dict(prof)
         kname = kernel_names(variant)[dom]
         traffic = TRAFFIC_PER_CELL[kname] * g.nv if kname in TRAFFIC_PER_CELL else None
         wc, we = g.hx_areag, g.ed_leng * g.edhx_leng / 2.0
         err = {}
-        for p in ("fp32", "fp32l"):
+        for p in ("fp32", "fp32l", "fp32n"):
             if p in results:
                 err[p] = {"h": rel_errors(results[p]["h"], r64["h"], wc),
                           "u": rel_errors(results[p]["u"], r64["u"], we)}
@@ -531,7 +540,8 @@ def main():
             "ms_per_step": rh["ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: " + STATE_NAME + " (no dataset)",
-            "config": dict(config_dict(g, headline, weights), autotuned=rh["tuning"],
+            "config": dict(config_dict(g, headline, weights_w if headline == "fp32l" else None),
+                           autotuned=rh["tuning"],
                            **({"apvm_pvspar": args.apvm} if args.apvm > 0 else {})),
             "error_vs_fp64": err,
             "fp64": {"value": rate(r64), "unit": UNIT, "ms_per_step": r64["ms"] / args.steps,
@@ -559,10 +569,18 @@ def main():
                                   "ms_per_step": results["fp32"]["ms"] / args.steps,
                                   "kernel_ms": results["fp32"]["prof"]}
         if headline == "fp32l":
-            # the network runs once per step: the profile reports it per stage
-            mlp_ms = rh["prof"]["edge_pre"] * 4.0
-            kernel_ms["mlp"] = mlp_ms
-            kernel_ms.pop("edge_pre", None)
+            line["learned_active_after_run"] = bool(rh["diag"]["learned_active"])
+        if "fp32n" in results and results["fp32n"]["prof"]:
+            # the per-step network: the profile reports it in the edge_pre
+            # slot, per stage; it runs once per step
+            rn = results["fp32n"]
+            nk = dict(rn["prof"])
+            mlp_ms = nk.pop("edge_pre") * 4.0
+            nk["mlp"] = mlp_ms
+            line["fp32_step_net"] = {
+                "value": rate(rn), "unit": UNIT, "ms_per_step": rn["ms"] / args.steps,
+                "kernel_ms": nk, "learned_active_after_run": bool(rn["diag"]["learned_active"]),
+                "config": config_dict(g, "fp32n", weights_n)["learned_correction"]}
             flop = MLP_FLOP_PER_EDGE * g.ne
             tf, tf_kind = load_tflops()
             ach = flop / (mlp_ms / 1000.0) / 1e12
@@ -575,7 +593,6 @@ def main():
                                     "tensor": {"achieved": ach, "peak": tf, "unit": "TFLOP/s",
                                                "frac": ach / tf, "peak_source": tf_kind,
                                                "flop_per_launch": flop}}
-            line["learned_active_after_run"] = bool(rh["diag"]["learned_active"])
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_sample(g, h, u, args.cpu_budget)
         print(json.dumps(line))

@@ -50,10 +50,22 @@ struct Handle {
   cudaGraphExec_t graph = nullptr;
   double graph_dt = 0.0;
   bool state_set = false;
-  // learned TRSK correction (FP32, cell-centred variant)
+  // learned TRSK correction: mode 1 the per-step network (FP32, cell-centred
+  // variant), mode 2 the learned TRSK weights (kite fractions corrected once
+  // at create)
   LearnedDev learned{};
-  bool learned_on = false;      // requested at create
+  int learned_mode = 0;
+  bool learned_on = false;      // a guarded learned correction (FP32 handles)
   bool learned_active = false;  // still applied (the drift guard may switch it off)
+  // mode 2: the weight-dependent device arrays of the learned and of the
+  // plain scheme (the guard's fallback), and host copies of the learned
+  // kite fractions and weights (reference layout) for export
+  struct WeightSet {
+    const double *e_stw = nullptr;
+    const float *e_stc32 = nullptr, *c_R32 = nullptr;
+    const int4 *c_pk = nullptr;
+  } w_learned, w_plain;
+  std::vector<double> kite_hxtr, kite_trskw;
   double drift_bound = 1e-3;
   double te_ref = 0.0, umax_ref = 0.0;
   double umax_last = 0.0;  // max |u| at the start of the current guard interval
@@ -219,6 +231,24 @@ int learned_guard(Handle *H, bool *tripped = nullptr);
 
 // new_run: the state starts a new run (set_state), so the learned correction
 // is switched back on and its energy reference is taken again
+// the learned correction on or off: mode 1 launches the network inside the
+// step, mode 2 points the step at the learned or the plain TRSK weights
+void learned_switch(Handle *H, bool on) {
+  if (H->learned_mode == 1) {
+    H->W32.learned = on ? &H->learned : nullptr;
+  } else if (H->learned_mode == 2) {
+    const Handle::WeightSet &w = on ? H->w_learned : H->w_plain;
+    H->M.e_stw = w.e_stw;
+    H->M.e_stc32 = w.e_stc32;
+    H->M.c_R32 = w.c_R32;
+    H->M.c_pk = w.c_pk;
+  }
+  if (H->graph) {
+    cudaGraphExecDestroy(H->graph);
+    H->graph = nullptr;
+  }
+}
+
 int load_state(Handle *H, const double *h, const double *u, bool new_run) {
   if (H->precision == IMODEL_SWM_FP32 && !H->href_fixed) {
     double s = 0.0, a = 0.0;
@@ -272,13 +302,9 @@ int load_state(Handle *H, const double *h, const double *u, bool new_run) {
   CK(cudaGetLastError());
   H->state_set = true;
   if (H->learned_on && (new_run || !H->te_ref_set)) {
-    if (!H->learned_active || H->W32.learned == nullptr) {
+    if (!H->learned_active) {
       H->learned_active = true;
-      H->W32.learned = &H->learned;
-      if (H->graph) {
-        cudaGraphExecDestroy(H->graph);
-        H->graph = nullptr;
-      }
+      learned_switch(H, true);
     }
     H->te_ref_set = false;
     return learned_guard(H);
@@ -394,11 +420,7 @@ bool guard_decide(Handle *H, double te, double umax) {
     return false;
   }
   H->learned_active = false;
-  H->W32.learned = nullptr;
-  if (H->graph) {
-    cudaGraphExecDestroy(H->graph);
-    H->graph = nullptr;
-  }
+  learned_switch(H, false);
   return true;
 }
 
@@ -526,8 +548,42 @@ int setup_learned(Handle *H, const imodel_swm_mesh *m, const Layout &L, const im
   if (rc) return set_error(H, rc, "learned correction set-up failed");
   H->drift_bound = o->drift_bound > 0 ? o->drift_bound : 1e-3;
   H->learned_on = H->learned_active = true;
+  H->learned_mode = 1;
   H->W32.learned = &H->learned;
   H->W32.tune.variant = 1;
+  return IMODEL_SWM_OK;
+}
+
+// Learned TRSK weights (opts.learned = 2): the network corrects every kite
+// fraction from local geometry once (imodel_gb300/learned_weights.py); the
+// weights are rebuilt from the corrected fractions.  On success *m2 views
+// the caller's mesh with H->kite_hxtr / H->kite_trskw in place of
+// hx_hxtr_area / hx_trskw.
+int learned_weights(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o,
+                    imodel_swm_mesh *m2) {
+  if (!o->mlp_weights || o->mlp_bytes != static_cast<size_t>(IMODEL_MLP_NPARAM) * sizeof(float))
+    return set_error(H, IMODEL_SWM_EINVAL, "mlp_weights must hold 5825 FP32 parameters");
+  KiteInputs K;
+  std::string msg = build_kite_inputs(*m, K);
+  if (!msg.empty()) return set_error(H, IMODEL_SWM_EINVAL, msg);
+  const int64_t n = static_cast<int64_t>(K.cell.size());
+  std::vector<float> y(static_cast<size_t>(n));
+  void *net = nullptr;
+  int rc = imodel_mlp_create(H->device, &net);
+  if (!rc) rc = imodel_mlp_set_params(net, static_cast<const float *>(o->mlp_weights),
+                                      IMODEL_MLP_NPARAM);
+  if (!rc) rc = imodel_mlp_forward(net, K.x.data(), n, y.data());
+  if (rc) {
+    const char *e = net ? imodel_mlp_last_error(net) : "";
+    std::string what = std::string("learned weights: network evaluation failed: ") + (e ? e : "");
+    if (net) imodel_mlp_destroy(net);
+    return set_error(H, rc, what);
+  }
+  imodel_mlp_destroy(net);
+  apply_kite_outputs(*m, K, y.data(), H->kite_hxtr, H->kite_trskw);
+  *m2 = *m;
+  m2->hx_hxtr_area = H->kite_hxtr.data();
+  m2->hx_trskw = H->kite_trskw.data();
   return IMODEL_SWM_OK;
 }
 
@@ -552,8 +608,22 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
   if (fsphere != 0 && fsphere != 2)
     return set_error(H, IMODEL_SWM_EINVAL, "fsphere must be 0 (f = 2 Omega sin lat) or 2 (f = fcte)");
   if (fsphere == 2 && !std::isfinite(fcte)) return set_error(H, IMODEL_SWM_EINVAL, "fcte must be finite");
+  const int lmode = o ? o->learned : 0;
+  if (lmode < 0 || lmode > 2)
+    return set_error(H, IMODEL_SWM_EINVAL,
+                     "learned must be 0, 1 (per-step network) or 2 (learned weights)");
+  if (lmode == 2 && scheme != IMODEL_SWM_TRSK10)
+    return set_error(H, IMODEL_SWM_EINVAL, "the learned weights correct trsk10 only");
+  imodel_swm_mesh mk{};
+  const imodel_swm_mesh *mesh = m;
+  if (lmode == 2) {
+    const int rc0 = learned_weights(H, m, o, &mk);
+    if (rc0) return rc0;
+    mesh = &mk;
+    H->learned_mode = 2;
+  }
   Layout L;
-  std::string msg = build_layout(*m, o ? o->bt : nullptr, L, scheme, fsphere, fcte);
+  std::string msg = build_layout(*mesh, o ? o->bt : nullptr, L, scheme, fsphere, fcte);
   if (!msg.empty()) return set_error(H, IMODEL_SWM_EINVAL, msg);
   H->nv = L.nv;
   H->ne = L.ne;
@@ -672,8 +742,8 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
   CK(cudaMallocHost(&H->h_flags, sizeof(int)));
   CK(cudaMallocHost(&H->h_result, 16 * sizeof(double)));
   if (H->precision == IMODEL_SWM_FP64) {
-    if (o && o->learned)
-      return set_error(H, IMODEL_SWM_EINVAL, "the learned correction needs the FP32 path");
+    if (o && o->learned == 1)
+      return set_error(H, IMODEL_SWM_EINVAL, "the per-step learned correction needs the FP32 path");
     if ((rc = alloc_work(H, H->W64))) return rc;
     H->W64.scheme = scheme;
     if (scheme == IMODEL_SWM_GASS18 &&
@@ -686,7 +756,30 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
     if ((rc = alloc_work(H, H->W32))) return rc;
     H->W32.h_ref = keep;
     if ((rc = dalloc(H, &H->W32.zflux, static_cast<size_t>(kMaxNb) * L.nv))) return rc;
-    if (o && o->learned && (rc = setup_learned(H, m, L, o))) return rc;
+    if (o && o->learned == 1 && (rc = setup_learned(H, m, L, o))) return rc;
+  }
+  if (H->learned_mode == 2) {
+    H->w_learned = {M.e_stw, M.e_stc32, M.c_R32, M.c_pk};
+    if (H->precision == IMODEL_SWM_FP32) {
+      // the guard's fallback: the plain scheme's weight-dependent arrays
+      Layout Lp;
+      msg = build_layout(*m, o ? o->bt : nullptr, Lp, scheme, fsphere, fcte);
+      if (!msg.empty()) return set_error(H, IMODEL_SWM_EINVAL, msg);
+      const int32_t *pk = nullptr;
+      if ((rc = upload(H, Lp.e_stw, &H->w_plain.e_stw)) ||
+          (rc = upload(H, Lp.e_stc32, &H->w_plain.e_stc32)) ||
+          (rc = upload(H, Lp.c_R32, &H->w_plain.c_R32)) || (rc = upload(H, Lp.c_pk, &pk)))
+        return rc;
+      H->w_plain.c_pk = reinterpret_cast<const int4 *>(pk);
+      if ((rc = dalloc(H, &H->ck_h, static_cast<size_t>(L.nv))) ||
+          (rc = dalloc(H, &H->ck_u, static_cast<size_t>(L.ne))))
+        return rc;
+      CK(cudaStreamCreateWithFlags(&H->side, cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&H->ev_steps, cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&H->ev_side, cudaEventDisableTiming));
+      H->drift_bound = o->drift_bound > 0 ? o->drift_bound : 1e-3;
+      H->learned_on = H->learned_active = true;
+    }
   }
   CK(cudaDeviceSynchronize());
   return IMODEL_SWM_OK;
@@ -932,7 +1025,9 @@ int imodel_swm_diagnostics(void *handle, imodel_swm_diag *out) {
   out->rms_div = std::sqrt(r[imodel::Q_ADIV2] / A);
   out->max_div = r[imodel::Q_MAXDIV];
   out->nan_found = r[imodel::Q_NAN] != 0.0 ? 1 : 0;
-  out->learned_active = H->learned_active ? 1 : 0;
+  // an FP64 handle with learned weights has no guard: they stay applied
+  out->learned_active =
+      (H->learned_active || (H->learned_mode == 2 && !H->learned_on)) ? 1 : 0;
   return IMODEL_SWM_OK;
 }
 
@@ -1088,7 +1183,7 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
   float best_ms = 1e30f;
   // the learned correction is wired into the cell-centred variants only
   // and APVM into the edge pre-pass of variant 0
-  for (int v = H->learned_on ? 1 : 0; v <= (H->W32.apvm.on ? 0 : 2); ++v)
+  for (int v = H->learned_mode == 1 ? 1 : 0; v <= (H->W32.apvm.on ? 0 : 2); ++v)
     for (int b : sizes) {
       imodel::Tune t;
       t.variant = v;
@@ -1117,7 +1212,7 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
   }
   // the learned-correction kernel's split of warps between gathering and
   // the epilogue
-  if (H->learned_active)
+  if (H->learned_active && H->learned_mode == 1)
     for (int g = 2; g <= 4; ++g) {
       if (best.mlp_gather == g) continue;
       imodel::Tune t = best;
@@ -1147,7 +1242,7 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
   choice[2] = best.bs_pre;
   choice[3] = best.bs_cell;
   choice[4] = best.bs_edge;
-  choice[5] = H->learned_on ? best.mlp_gather : 0;
+  choice[5] = H->learned_mode == 1 ? best.mlp_gather : 0;
   return imodel::check_flags(H);
 }
 
@@ -1160,7 +1255,7 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[6]) {
       return imodel::set_error(H, IMODEL_SWM_EINVAL, "block sizes must be 128, 256 or 512");
   if (choice[0] < 0 || choice[0] > 2)
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "variant must be 0, 1 or 2");
-  if (H->learned_on && choice[0] == 0)
+  if (H->learned_mode == 1 && choice[0] == 0)
     return imodel::set_error(H, IMODEL_SWM_EINVAL,
                              "the learned correction runs with the cell-centred variants (1, 2) only");
   if (H->W32.apvm.on && choice[0] != 0)
@@ -1171,7 +1266,7 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[6]) {
   t.bs_pre = choice[2];
   t.bs_cell = choice[3];
   t.bs_edge = choice[4];
-  if (H->learned_on) {
+  if (H->learned_mode == 1) {
     if (choice[5] < 2 || choice[5] > 4)
       return imodel::set_error(H, IMODEL_SWM_EINVAL, "gather groups of the network: 2, 3 or 4");
     t.mlp_gather = choice[5];
@@ -1228,6 +1323,16 @@ int imodel_swm_set_diffusion_fields(void *handle, const double *k2_hx, const dou
   return rc;
 }
 
+int imodel_swm_learned_weights(void *handle, double *hxtr_area, double *trskw) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H || !hxtr_area || !trskw) return IMODEL_SWM_EINVAL;
+  if (H->learned_mode != 2)
+    return imodel::set_error(H, IMODEL_SWM_ESTATE, "the handle was not created with learned weights");
+  std::memcpy(hxtr_area, H->kite_hxtr.data(), sizeof(double) * H->kite_hxtr.size());
+  std::memcpy(trskw, H->kite_trskw.data(), sizeof(double) * H->kite_trskw.size());
+  return IMODEL_SWM_OK;
+}
+
 int imodel_swm_test_fail_alloc(int32_t after) {
   if (after < 0) return IMODEL_SWM_EINVAL;
   imodel::g_fail_alloc_after.store(after);
@@ -1245,7 +1350,7 @@ int imodel_swm_set_apvm(void *handle, double pvspar, double dt) {
   const bool fp32 = H->precision == IMODEL_SWM_FP32;
   if (pvspar > 0 && !(fp32 ? H->M.t_apw32 != nullptr : H->M.t_c != nullptr))
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "apvm needs the mesh's ed_nr and ed_c");
-  if (pvspar > 0 && H->learned_on)
+  if (pvspar > 0 && H->learned_mode == 1)
     return imodel::set_error(H, IMODEL_SWM_EINVAL,
                              "apvm runs with FP32 variant 0, the learned correction with 1 and 2");
   if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;

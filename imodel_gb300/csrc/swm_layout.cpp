@@ -672,4 +672,108 @@ std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, Lear
   return "";
 }
 
+// ---- learned TRSK weights ----------------------------------------------------
+std::string build_kite_inputs(const imodel_swm_mesh &m, KiteInputs &K) {
+  const int nv = m.nv;
+  if (!m.v_p || !m.v_tr || !m.tr_v || !m.hx_hxtr_area)
+    return "the learned weights need v_p, v_tr and tr_v";
+  size_t nrow = 0;
+  for (int c = 0; c < nv; ++c) nrow += static_cast<size_t>(m.nnb[c]);
+  K.x.assign(nrow * 24, 0);
+  K.cell.resize(nrow);
+  K.slot.resize(nrow);
+  // row of (c, j): slot-major, the cells with nnb > j in order
+  std::vector<size_t> next(6, 0);
+  {
+    size_t acc = 0;
+    for (int j = 0; j < 6; ++j) {
+      next[j] = acc;
+      for (int c = 0; c < nv; ++c) acc += m.nnb[c] > j ? 1 : 0;
+    }
+  }
+  auto tangent = [](const double *v, const double *p, double *t) {
+    const double vp = dot3(v, p);
+    for (int k = 0; k < 3; ++k) t[k] = v[k] - vp * p[k];
+  };
+  static const int kDj[6] = {0, -1, 1, -2, 2, 3};
+  for (int c = 0; c < nv; ++c) {
+    const int n = m.nnb[c];
+    const double *P = m.v_p + 3 * static_cast<size_t>(c);
+    const double sA = std::sqrt(m.hx_areag[c]);
+    const double *R = m.hx_hxtr_area + 6 * static_cast<size_t>(c);
+    double T[6][3], Tt[6][3], r[6], V[3] = {0.0, 0.0, 0.0};
+    double sum_d = 0.0, sum_l = 0.0, sum_r = 0.0;
+    int ed[6];
+    for (int j = 0; j < n; ++j) {
+      circumcentre(m, m.v_tr[6 * static_cast<size_t>(c) + j] - 1, T[j]);
+      for (int k = 0; k < 3; ++k) V[k] += T[j][k];
+      tangent(T[j], P, Tt[j]);
+      r[j] = std::sqrt(dot3(Tt[j], Tt[j]));
+      ed[j] = m.v_ed[6 * static_cast<size_t>(c) + j] - 1;
+      sum_d += m.edhx_leng[ed[j]];
+      sum_l += m.ed_leng[ed[j]];
+      sum_r += r[j];
+    }
+    for (int k = 0; k < 3; ++k) V[k] /= n;
+    double O[3];
+    tangent(V, P, O);
+    const double mean_d = sum_d / n, mean_l = sum_l / n, mean_r = sum_r / n;
+    for (int j = 0; j < n; ++j) {
+      double f[24] = {};
+      for (int q = 0; q < 6; ++q) f[q] = 10.0 * (R[((j + kDj[q]) % n + n) % n] - 1.0 / n);
+      f[6] = n == 5 ? 1.0 : 0.0;
+      const double dn = std::sqrt(dot3(Tt[j], Tt[j]));
+      const double D[3] = {Tt[j][0] / dn, Tt[j][1] / dn, Tt[j][2] / dn};
+      const double Q[3] = {P[1] * D[2] - P[2] * D[1], P[2] * D[0] - P[0] * D[2],
+                           P[0] * D[1] - P[1] * D[0]};
+      f[7] = 10.0 * dot3(O, D) / sA;
+      f[8] = 10.0 * dot3(O, Q) / sA;
+      const int e0 = ed[j], e1 = ed[(j + 1) % n];
+      f[9] = 10.0 * (m.edhx_leng[e0] / mean_d - 1.0);
+      f[10] = 10.0 * (m.edhx_leng[e1] / mean_d - 1.0);
+      f[11] = 10.0 * (m.ed_leng[e0] / mean_l - 1.0);
+      f[12] = 10.0 * (m.ed_leng[e1] / mean_l - 1.0);
+      f[13] = 10.0 * (r[j] / mean_r - 1.0);
+      const size_t row = next[j]++;
+      for (int q = 0; q < 24; ++q) K.x[24 * row + q] = bf16_bits(static_cast<float>(f[q]));
+      K.cell[row] = c;
+      K.slot[row] = static_cast<int8_t>(j);
+    }
+  }
+  return "";
+}
+
+void apply_kite_outputs(const imodel_swm_mesh &m, const KiteInputs &K, const float *y,
+                        std::vector<double> &hxtr, std::vector<double> &trskw) {
+  const int nv = m.nv;
+  std::vector<double> dR(6 * static_cast<size_t>(nv), 0.0);
+  for (size_t r = 0; r < K.cell.size(); ++r)
+    dR[6 * static_cast<size_t>(K.cell[r]) + K.slot[r]] = 0.1 * static_cast<double>(y[r]);
+  hxtr.assign(m.hx_hxtr_area, m.hx_hxtr_area + 6 * static_cast<size_t>(nv));
+  trskw.assign(36 * static_cast<size_t>(nv), 0.0);
+  for (int c = 0; c < nv; ++c) {
+    const int n = m.nnb[c];
+    double *R = hxtr.data() + 6 * static_cast<size_t>(c);
+    const double *d = dR.data() + 6 * static_cast<size_t>(c);
+    double mean = 0.0;
+    for (int j = 0; j < n; ++j) mean += d[j];
+    mean /= n;
+    for (int j = 0; j < n; ++j) R[j] += d[j] - mean;
+    // calc_trisk_weights: w(i, j) = sum_{k=i}^{j-1} R(k) - 1/2, cyclic
+    double *w = trskw.data() + 36 * static_cast<size_t>(c);
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        if (i == j) continue;
+        double s = 0.0;
+        if (j < i) {
+          for (int k = i; k < n; ++k) s = s + R[k];
+          for (int k = 0; k < j; ++k) s = s + R[k];
+        } else {
+          for (int k = i; k < j; ++k) s = s + R[k];
+        }
+        w[6 * j + i] = s - 0.5;
+      }
+  }
+}
+
 }  // namespace imodel

@@ -58,27 +58,37 @@ def _edge_w(g):
     return g.ed_leng * g.edhx_leng / 2.0
 
 
-def run(grid, path, h, u, dt, nsteps, bt=None, params=None, chunk=0, testcase=2):
+def run(grid, path, h, u, dt, nsteps, bt=None, params=None, chunk=0, testcase=2, wparams=None):
     """One run on the GPU; returns the final state, timing and diagnostics.
-    path: "fp64", "fp32" or "fp32l" (FP32 + learned correction)."""
+    path: "fp64", "fp32", "fp32l" (FP32 + the per-step learned correction,
+    parameters `params`), "fp32w" / "fp64w" (the learned TRSK weights,
+    parameters `wparams`)."""
     from . import swm
-    m = swm.SWM(grid, precision="fp64" if path == "fp64" else "fp32", bt=bt,
-                learned_params=params if path == "fp32l" else None, testcase=testcase)
+    if path in ("fp32w", "fp64w") and wparams is None:
+        from . import learned_weights
+        wparams = learned_weights.trained_params()
+        if wparams is None:
+            raise SystemExit("no trained weights network: run imodel_gb300.train_learned_weights")
+    m = swm.SWM(grid, precision="fp64" if path.startswith("fp64") else "fp32", bt=bt,
+                learned_params=params if path == "fp32l" else None,
+                learned_weights=wparams if path in ("fp32w", "fp64w") else None,
+                testcase=testcase)
     try:
         m.set_state(h, u)
-        if path != "fp64":
+        if not path.startswith("fp64"):
             m.autotune(dt, 3)
             m.set_state(h, u)
         d0 = m.diagnostics()
         # the learned path reports when its drift guard switched it off
-        chunk = chunk or (256 if path == "fp32l" else nsteps)
+        guarded = path in ("fp32l", "fp32w")
+        chunk = chunk or (256 if guarded else nsteps)
         t0 = time.perf_counter()
         done, off_at = 0, None
         while done < nsteps:
             k = min(chunk, nsteps - done)
             m.advance(dt, k)
             done += k
-            if path == "fp32l" and off_at is None and not m.diagnostics()["learned_active"]:
+            if guarded and off_at is None and not m.diagnostics()["learned_active"]:
                 off_at = done
         el = time.perf_counter() - t0
         d1 = m.diagnostics()
@@ -241,13 +251,15 @@ def exp_fixed(args, pool):
         if args.save_ref:
             np.savez(args.save_ref, h=ref["h"],
                      **{k: np.array(v) for k, v in out["reference"].items() if v is not None})
-    p = _params(args)
-    for path in [q for q in args.paths.split(",") if q]:
+    paths = [q for q in args.paths.split(",") if q]
+    p = _params(args) if "fp32l" in paths else None
+    for path in paths:
         r = run(gc, path, hc, uc, dtc, nc, params=p)
         out[path] = dict(_summary(r), h_vs_ref=_restrict_errors(r, ref, gc))
-    if "fp32l" in out and "fp64" in out:
-        out["speedup_fp32l_vs_fp64"] = (out["fp32l"]["cell_steps_per_s"] /
-                                        out["fp64"]["cell_steps_per_s"])
+    for q in ("fp32l", "fp32w"):
+        if q in out and "fp64" in out:
+            out[f"speedup_{q}_vs_fp64"] = (out[q]["cell_steps_per_s"] /
+                                           out["fp64"]["cell_steps_per_s"])
     return out
 
 
@@ -317,8 +329,9 @@ def main(argv=None):
     ap.add_argument("--dt", type=float, default=0.0)
     ap.add_argument("--ref-precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--workers", type=int, default=0)
-    ap.add_argument("--paths", default="fp64,fp32,fp32l",
-                    help="coarse runs of 'fixed': fp64, fp32, fp32l (FP32 + learned)")
+    ap.add_argument("--paths", default="fp64,fp32,fp32w",
+                    help="coarse runs of 'fixed': fp64, fp32, fp32w (FP32 + learned TRSK "
+                         "weights), fp64w, fp32l (FP32 + per-step learned correction)")
     ap.add_argument("--save-ref", default="", help="'fixed': save the fine run's h (.npz)")
     ap.add_argument("--load-ref", default="", help="'fixed': reuse a saved fine run")
     a = ap.parse_args(argv)

@@ -118,12 +118,15 @@ class SWM:
     "dtred" (trsk10 with the dtred Coriolis reconstruction); the last three
     on "fp64" handles.  fsphere = 2 replaces f = 2 Omega sin(lat) by the
     constant fcte (the f-sphere of test cases 33, 35, 40-42).
+    learned_params: the per-step learned correction (FP32); learned_weights:
+    network parameters of the learned TRSK weights (imodel_gb300.
+    learned_weights), applied once at creation.
     """
 
     def __init__(self, grid: Grid, precision: str = "fp64", testcase: int = 2,
                  bt=None, h_ref: float = 0.0, device: int = 0, learned_params=None,
                  drift_bound: float = 0.0, scheme: str = "trsk10", fsphere: int = 0,
-                 fcte: float = 0.0):
+                 fcte: float = 0.0, learned_weights=None):
         self.grid = grid
         self.lib = _capi.swm_lib()
         self.precision = precision
@@ -142,10 +145,15 @@ class SWM:
         opts.fsphere = fsphere
         opts.fcte = fcte
         self._mlp = None
-        if learned_params is not None:
-            # learned TRSK correction (network parameters, see imodel_mlp.h)
-            self._mlp = np.ascontiguousarray(learned_params, dtype=np.float32)
-            opts.learned = 1
+        if learned_params is not None and learned_weights is not None:
+            raise ValueError("learned_params (per-step network) and learned_weights exclude "
+                             "each other")
+        if learned_params is not None or learned_weights is not None:
+            # learned TRSK correction (network parameters, see imodel_mlp.h):
+            # mode 1 the per-step network, mode 2 the learned TRSK weights
+            p = learned_params if learned_params is not None else learned_weights
+            self._mlp = np.ascontiguousarray(p, dtype=np.float32)
+            opts.learned = 1 if learned_params is not None else 2
             opts.mlp_weights = self._mlp.ctypes.data
             opts.mlp_bytes = self._mlp.nbytes
             opts.drift_bound = drift_bound
@@ -243,6 +251,16 @@ class SWM:
         pvspar (0 = off) and the run's time step dt; moves an FP32 handle
         to stencil variant 0."""
         self._check(self.lib.imodel_swm_set_apvm(self._handle, pvspar, dt))
+
+    def learned_weights(self):
+        """(hxtr_area[nv, 6], trskw[nv, 6, 6]) of a handle created with
+        learned_weights: the corrected kite fractions and the TRSK weights
+        the step uses (trskw(i, j) at [c, j, i])."""
+        R = np.zeros((self.grid.nv, 6))
+        w = np.zeros((self.grid.nv, 6, 6))
+        self._check(self.lib.imodel_swm_learned_weights(self._handle, _capi.as_f64p(R),
+                                                        _capi.as_f64p(w)))
+        return R, w
 
     def diagnostics(self) -> dict:
         """sumf_areas + calc_energies + RMS divergence of the current state."""

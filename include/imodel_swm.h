@@ -112,7 +112,15 @@ typedef struct imodel_swm_opts {
   double h_ref;       /* FP32 mode: h is stored as h - h_ref in FP32.
                          0 selects the area mean of the first state set.   */
   int32_t device;     /* CUDA device ordinal                                */
-  int32_t learned;    /* 1: add the learned TRSK correction (needs weights) */
+  int32_t learned;    /* 0 off; 1 the per-step learned correction of the
+                         TRSK reconstruction (FP32 handles; the network runs
+                         once per step on the stencil velocities); 2 learned
+                         TRSK weights: at create the network corrects each
+                         cell's kite fractions from local geometry and the
+                         TRSK weights are rebuilt from them, so the scheme
+                         keeps TRSK's structure and a step costs a plain
+                         step (trsk10; FP32 handles guarded as below, FP64
+                         handles unguarded)                                */
   const void *mlp_weights;  /* packed MLP parameters (see imodel_mlp.h)    */
   size_t mlp_bytes;
   double drift_bound; /* relative total-energy drift above which the
@@ -238,6 +246,13 @@ int imodel_swm_set_diffusion_fields(void *handle, const double *k2_hx, const dou
  * correction refuses APVM (IMODEL_SWM_EINVAL).  Needs the mesh's ed_nr and
  * ed_c.  May be called at any time; applies from the next step. */
 int imodel_swm_set_apvm(void *handle, double pvspar, double dt);
+/* The kite fractions hxtr_area[nv][6] and TRSK weights trskw[nv][6][6]
+ * (trskw(i, j) at [c][j][i], the mesh's layout) a handle created with
+ * learned = 2 steps with: the reference's hx%hxtr_area corrected by the
+ * network, and calc_trisk_weights (interpack.f90:3978-4098) of them.  A host
+ * that puts them into its grid_structure runs the same scheme on the CPU.
+ * IMODEL_SWM_ESTATE for other handles.  No counterpart in the reference. */
+int imodel_swm_learned_weights(void *handle, double *hxtr_area, double *trskw);
 /* Test hook with no counterpart in the reference: when after > 0, the
  * after-th device allocation made by any handle from now on fails with
  * IMODEL_SWM_ENOMEM as if the device were full (0 switches the injection
