@@ -89,6 +89,8 @@ def build_swm_lib(force: bool = False) -> str:
         "swm_capi.cu": [],
         "swm_ens.cu": [],
         "mlp.cu": [],
+        # moist shallow-water model: reference operation order, no contraction
+        "swm_moist.cu": ["--fmad=false"],
         # allocation-free weighted sums: compensated summation, no contraction
         "swm_noalloc.cu": ["--fmad=false"],
     }

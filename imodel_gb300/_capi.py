@@ -112,6 +112,7 @@ SWM_SYMBOLS = [
     "imodel_swm_main_kernel", "imodel_swm_stream", "imodel_swm_weighted_sums_noalloc",
     "imodel_swm_ensemble_create", "imodel_swm_ensemble_set_state",
     "imodel_swm_ensemble_get_state", "imodel_swm_ensemble_advance", "imodel_swm_ensemble_tune",
+    "imodel_swm_ensemble_test_stall",
     "imodel_swm_ensemble_destroy", "imodel_swm_ensemble_last_error",
     "imodel_swm_ensemble_stream",
 ]
@@ -121,6 +122,19 @@ MLP_SYMBOLS = [
     "imodel_mlp_forward", "imodel_mlp_grad", "imodel_mlp_load_dataset", "imodel_mlp_train",
     "imodel_mlp_destroy", "imodel_mlp_last_error",
 ]
+
+MOIST_SYMBOLS = [
+    "imodel_moist_create", "imodel_moist_set_state", "imodel_moist_advance",
+    "imodel_moist_get_state", "imodel_moist_destroy", "imodel_moist_last_error",
+]
+
+
+class MoistOpts(ctypes.Structure):
+    """struct imodel_moist_opts."""
+
+    _fields_ = [("testcase", ctypes.c_int32), ("bt", c_f64p), ("theta", c_f64p),
+                ("q0", ctypes.c_double), ("device", ctypes.c_int32)]
+
 
 _libs: dict = {}
 
@@ -202,6 +216,7 @@ def swm_lib() -> ctypes.CDLL:
                                                       c_f64p, c_f64p]
         lib.imodel_swm_ensemble_advance.argtypes = [vp, c_f64p, c_i32p]
         lib.imodel_swm_ensemble_tune.argtypes = [vp, c_f64p, ctypes.c_int32, c_i32p]
+        lib.imodel_swm_ensemble_test_stall.argtypes = [vp, ctypes.c_int32, ctypes.c_int64]
         lib.imodel_swm_ensemble_destroy.argtypes = [vp]
         lib.imodel_swm_ensemble_last_error.argtypes = [vp]
         lib.imodel_swm_ensemble_last_error.restype = ctypes.c_char_p
@@ -221,6 +236,15 @@ def swm_lib() -> ctypes.CDLL:
         lib.imodel_mlp_destroy.argtypes = [vp]
         lib.imodel_mlp_last_error.argtypes = [vp]
         lib.imodel_mlp_last_error.restype = ctypes.c_char_p
+        f64pp = ctypes.POINTER(c_f64p)
+        lib.imodel_moist_create.argtypes = [ctypes.POINTER(Mesh), ctypes.POINTER(MoistOpts),
+                                            ctypes.POINTER(vp)]
+        lib.imodel_moist_set_state.argtypes = [vp, f64pp, c_f64p, c_f64p, c_f64p]
+        lib.imodel_moist_advance.argtypes = [vp, ctypes.c_double, ctypes.c_int32]
+        lib.imodel_moist_get_state.argtypes = [vp, f64pp]
+        lib.imodel_moist_destroy.argtypes = [vp]
+        lib.imodel_moist_last_error.argtypes = [vp]
+        lib.imodel_moist_last_error.restype = ctypes.c_char_p
         lib._typed = True
     return lib
 

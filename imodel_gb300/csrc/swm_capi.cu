@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "imodel_mlp.h"
+#include "imodel_moist.h"
 #include "imodel_swm.h"
 #include "swm_common.cuh"
 #include "swm_layout.h"
@@ -1404,6 +1405,201 @@ const char *imodel_swm_last_error(void *handle) {
   Handle *H = static_cast<Handle *>(handle);
   if (!H) return "NULL handle";
   return H->err.c_str();
+}
+
+}  // extern "C"
+
+// ---- the moist shallow-water model ---------------------------------------------
+namespace {
+struct Moist {
+  Handle *H = nullptr;  // the FP64 shallow-water handle: geometry, h and u
+  int testcase = 0;
+  double q0 = 0.0;
+  double *th = nullptr, *ex20 = nullptr, *qv = nullptr, *qc = nullptr, *qr = nullptr;
+  double *q[5][4] = {};  // per tracer: y_n, two stage buffers, RK accumulator
+  double *uphi = nullptr;
+  bool state_set = false;
+};
+
+// host array (reference order, nv or ne values) -> device array (device order)
+int moist_in(Handle *H, const double *src, double *dst, bool edges) {
+  const int n = edges ? H->ne : H->nv;
+  double *stage = edges ? H->d_stage_u : H->d_stage_h;
+  CK(cudaMemcpyAsync(stage, src, sizeof(double) * n, cudaMemcpyHostToDevice, H->stream));
+  imodel::launch_gather_in(n, edges ? H->d_edge_n2o : H->d_cell_n2o, stage, dst, 0.0, H->stream);
+  CK(cudaGetLastError());
+  return IMODEL_SWM_OK;
+}
+int moist_out(Handle *H, const double *src, double *dst, bool edges) {
+  const int n = edges ? H->ne : H->nv;
+  double *stage = edges ? H->d_stage_u : H->d_stage_h;
+  imodel::launch_scatter_out(n, edges ? H->d_edge_n2o : H->d_cell_n2o, src, stage, 0.0,
+                             H->d_flags, H->stream);
+  CK(cudaMemcpyAsync(dst, stage, sizeof(double) * n, cudaMemcpyDeviceToHost, H->stream));
+  CK(cudaGetLastError());
+  return IMODEL_SWM_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int imodel_moist_create(const imodel_swm_mesh *m, const imodel_moist_opts *o, void **handle) {
+  if (!handle) return IMODEL_SWM_EINVAL;
+  *handle = nullptr;
+  Moist *X = new (std::nothrow) Moist();
+  if (!X) return IMODEL_SWM_ENOMEM;
+  X->H = new (std::nothrow) Handle();
+  *handle = X;
+  if (!X->H) return IMODEL_SWM_ENOMEM;
+  Handle *H = X->H;
+  if (!m || !o || !o->theta) return imodel::set_error(H, IMODEL_SWM_EINVAL, "mesh, opts and theta are required");
+  if (o->testcase < 1 || o->testcase > 5)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "moist test cases are 1..5");
+  imodel_swm_opts so{};
+  so.precision = IMODEL_SWM_FP64;
+  so.testcase = o->testcase;
+  so.bt = o->bt;
+  so.device = o->device;
+  int rc;
+  try {
+    rc = imodel::create(H, m, &so);
+  } catch (const std::bad_alloc &) {
+    rc = imodel::set_error(H, IMODEL_SWM_ENOMEM, "host allocation failed");
+  }
+  if (rc) return rc;
+  X->testcase = o->testcase;
+  X->q0 = o->q0;
+  const size_t nv = H->nv, ne = H->ne;
+  for (double **p : {&X->th, &X->ex20, &X->qv, &X->qc, &X->qr})
+    if ((rc = imodel::dalloc(H, p, nv))) return rc;
+  for (int k = 0; k < 5; ++k)
+    for (int b = 0; b < 4; ++b)
+      if ((rc = imodel::dalloc(H, &X->q[k][b], nv))) return rc;
+  if ((rc = imodel::dalloc(H, &X->uphi, 5 * ne))) return rc;
+  // theta and exp(20 theta) of qsat (moist_swm.f90:618-622): theta is fixed
+  // in the RK4 path, so the exponential is formed once, here
+  std::vector<double> ex(nv);
+  for (size_t i = 0; i < nv; ++i) ex[i] = std::exp(20.0 * o->theta[i]);
+  if ((rc = moist_in(H, o->theta, X->th, false)) || (rc = moist_in(H, ex.data(), X->ex20, false)))
+    return rc;
+  if (cudaStreamSynchronize(H->stream) != cudaSuccess)
+    return imodel::set_error(H, IMODEL_SWM_ECUDA, "stream synchronize failed");
+  return IMODEL_SWM_OK;
+}
+
+int imodel_moist_set_state(void *handle, const double *const y[7], const double *qv,
+                           const double *qc, const double *qr) {
+  Moist *X = static_cast<Moist *>(handle);
+  if (!X || !X->H || !y || !qv || !qc || !qr) return IMODEL_SWM_EINVAL;
+  Handle *H = X->H;
+  if (H->nv == 0) return imodel::set_error(H, IMODEL_SWM_ESTATE, "handle was not created");
+  for (int k = 0; k < 7; ++k)
+    if (!y[k]) return IMODEL_SWM_EINVAL;
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  int rc;
+  if ((rc = moist_in(H, y[0], H->W64.yn_h, false)) || (rc = moist_in(H, y[1], H->W64.yn_u, true)))
+    return rc;
+  for (int k = 0; k < 5; ++k)
+    if ((rc = moist_in(H, y[2 + k], X->q[k][0], false))) return rc;
+  if ((rc = moist_in(H, qv, X->qv, false)) || (rc = moist_in(H, qc, X->qc, false)) ||
+      (rc = moist_in(H, qr, X->qr, false)))
+    return rc;
+  if (cudaStreamSynchronize(H->stream) != cudaSuccess)
+    return imodel::set_error(H, IMODEL_SWM_ECUDA, "stream synchronize failed");
+  X->state_set = true;
+  return IMODEL_SWM_OK;
+}
+
+int imodel_moist_advance(void *handle, double dt, int32_t nsteps) {
+  Moist *X = static_cast<Moist *>(handle);
+  if (!X || !X->H) return IMODEL_SWM_EINVAL;
+  Handle *H = X->H;
+  if (!X->state_set) return imodel::set_error(H, IMODEL_SWM_ESTATE, "no state set");
+  if (nsteps < 0 || !(dt > 0) || !std::isfinite(dt))
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "bad dt or nsteps");
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  imodel::Work<double> &W = H->W64;
+  const bool swm = X->testcase > 1;
+  const int active = swm ? (0xF | (X->testcase == 2 ? 0x10 : 0)) : 0x10;
+  // stage st reads y_n, a, b, a and writes a, b, a, y_n
+  auto in = [](int st, double *yn, double *a, double *b) { return st == 0 ? yn : (st == 2 ? b : a); };
+  auto out = [](int st, double *yn, double *a, double *b) {
+    return st == 0 ? a : (st == 1 ? b : (st == 2 ? a : yn));
+  };
+  for (int step = 0; step < nsteps; ++step) {
+    for (int st = 0; st < 4; ++st) {
+      imodel::MoistArgs A;
+      A.stage = st;
+      A.dt = dt;
+      A.swm = swm ? 1 : 0;
+      A.active = active;
+      const double *h_in = swm ? in(st, W.yn_h, W.ya_h, W.yb_h) : W.yn_h;
+      const double *u_in = swm ? in(st, W.yn_u, W.ya_u, W.yb_u) : W.yn_u;
+      if (swm)
+        imodel::launch_stage64(H->M, W, h_in, u_in, nullptr, nullptr, -1, dt, H->stream);
+      A.h_in = h_in;
+      A.u_in = u_in;
+      A.tend_h = W.tend_h;
+      A.tend_u = W.tend_u;
+      A.h_ed = W.h_ed;
+      A.yn_h = W.yn_h;
+      A.acc_h = W.acc_h;
+      A.h_out = out(st, W.yn_h, W.ya_h, W.yb_h);
+      A.yn_u = W.yn_u;
+      A.acc_u = W.acc_u;
+      A.u_out = out(st, W.yn_u, W.ya_u, W.yb_u);
+      for (int k = 0; k < 5; ++k) {
+        double **q = X->q[k];
+        const bool adv = (active >> k) & 1;
+        A.q_in[k] = adv ? in(st, q[0], q[1], q[2]) : q[0];
+        A.q_yn[k] = q[0];
+        A.q_acc[k] = q[3];
+        A.q_out[k] = out(st, q[0], q[1], q[2]);
+      }
+      A.uphi = X->uphi;
+      A.th = X->th;
+      A.ex20 = X->ex20;
+      A.qv = X->qv;
+      A.qc = X->qc;
+      A.qr = X->qr;
+      A.q0 = X->q0;
+      A.flags = H->d_flags;
+      imodel::launch_moist_stage(H->M, A, H->stream);
+    }
+    imodel::launch_moist_q(H->nv, W.yn_h, X->q[1][0], X->q[2][0], X->q[3][0], X->qv, X->qc,
+                           X->qr, H->d_flags, H->stream);
+  }
+  if (cudaGetLastError() != cudaSuccess) return imodel::set_error(H, IMODEL_SWM_ECUDA, "launch failed");
+  return imodel::check_flags(H);
+}
+
+int imodel_moist_get_state(void *handle, double *const y[7]) {
+  Moist *X = static_cast<Moist *>(handle);
+  if (!X || !X->H || !y) return IMODEL_SWM_EINVAL;
+  Handle *H = X->H;
+  if (!X->state_set) return imodel::set_error(H, IMODEL_SWM_ESTATE, "no state set");
+  for (int k = 0; k < 7; ++k)
+    if (!y[k]) return IMODEL_SWM_EINVAL;
+  if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  int rc;
+  if ((rc = moist_out(H, H->W64.yn_h, y[0], false)) || (rc = moist_out(H, H->W64.yn_u, y[1], true)))
+    return rc;
+  for (int k = 0; k < 5; ++k)
+    if ((rc = moist_out(H, X->q[k][0], y[2 + k], false))) return rc;
+  return imodel::check_flags(H);
+}
+
+int imodel_moist_destroy(void *handle) {
+  Moist *X = static_cast<Moist *>(handle);
+  if (!X) return IMODEL_SWM_OK;
+  imodel::destroy(X->H);
+  delete X;
+  return IMODEL_SWM_OK;
+}
+
+const char *imodel_moist_last_error(void *handle) {
+  Moist *X = static_cast<Moist *>(handle);
+  return X && X->H ? X->H->err.c_str() : "null handle";
 }
 
 }  // extern "C"

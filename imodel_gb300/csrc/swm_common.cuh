@@ -170,6 +170,32 @@ void launch_dif_coefs(const DevMesh &M, const double *kf, double k, bool take_sq
                       float *kc32, double *kt64, float *kt32, cudaStream_t s);
 
 
+// One RK stage of the moist shallow-water model (swm_moist.cu).  Tracer k of
+// {h theta, h qv, h qc, h qr, h tracer} is advanced when bit k of `active`
+// is set; swm != 0 adds the shallow-water terms (the caller has written
+// tend_h, tend_u and h_ed with a tendency evaluation of the stage input),
+// the thermal momentum source and the water sources.
+struct MoistArgs {
+  int stage = 0;
+  double dt = 0.0;
+  int swm = 0, active = 0;
+  const double *u_in = nullptr, *h_in = nullptr, *tend_u = nullptr, *tend_h = nullptr,
+               *h_ed = nullptr;
+  double *yn_u = nullptr, *acc_u = nullptr, *u_out = nullptr;
+  double *yn_h = nullptr, *acc_h = nullptr, *h_out = nullptr;
+  const double *q_in[5] = {};
+  double *q_yn[5] = {}, *q_acc[5] = {}, *q_out[5] = {};
+  double *uphi = nullptr;  // [5][ne]
+  // theta (frozen), exp(20 theta), and qv, qc, qr of the last step [nv]
+  const double *th = nullptr, *ex20 = nullptr, *qv = nullptr, *qc = nullptr, *qr = nullptr;
+  double q0 = 0.0;
+  int *flags = nullptr;
+};
+void launch_moist_stage(const DevMesh &M, const MoistArgs &A, cudaStream_t s);
+void launch_moist_q(int nv, const double *h, const double *hqv, const double *hqc,
+                    const double *hqr, double *qv, double *qc, double *qr, int *flags,
+                    cudaStream_t s);
+
 // reference order <-> device order, with precision conversion
 void launch_gather_in(int n, const int32_t *n2o, const double *src, double *dst, double shift,
                       cudaStream_t s);

@@ -66,6 +66,10 @@ struct EnsArgs {
   unsigned *bar_count;
   unsigned *bar_gen;
   int *flags;  // bit 0: PV division by ~0, bit 2: barrier timed out
+  // test hook: block stall_block (-1: none) leaves before its first
+  // barrier; spin_limit bounds every barrier wait (polls of ~64 ns)
+  int stall_block;
+  unsigned long long spin_limit;
 };
 
 // grid-wide barrier with a bounded wait (cooperative launch: all blocks are
@@ -86,7 +90,7 @@ __device__ bool grid_barrier(const EnsArgs &A) {
     } else {
       unsigned long long spins = 0;
       while (*gen == g0) {
-        if (++spins > (1ull << 26)) {  // several seconds: a phase takes < 10 ms
+        if (++spins > A.spin_limit) {  // 2^26: several seconds; a phase takes < 10 ms
           atomicOr(A.flags, 4);
           ok = 0;
           break;
@@ -112,6 +116,7 @@ template <int MINB>
 __global__ void __launch_bounds__(512, MINB) k_ensemble(EnsArgs A) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthr = gridDim.x * blockDim.x;
+  if (static_cast<int>(blockIdx.x) == A.stall_block) return;  // test hook
   for (int s = 0; s < A.macro_steps; ++s) {
     bool on[kMaxGrids];
     for (int k = 0; k < A.ngrids; ++k) on[k] = steps_now(s, A.g[k].nsteps, A.macro_steps);
@@ -206,6 +211,9 @@ struct Ens {
   cudaStream_t stream = nullptr;
   int block = 256, blocks_per_sm = 0, variant = 0;
   bool any_state = false;
+  // test hook for the next launch only (imodel_swm_ensemble_test_stall)
+  int test_stall_block = -1;
+  unsigned long long test_spin_limit = 0;
 };
 
 int fail(Ens *E, int code, const std::string &m) {
@@ -355,6 +363,10 @@ int ens_launch(Ens *E, const double *dt, const int32_t *nsteps, int block, int b
   A.bar_count = E->bar;
   A.bar_gen = E->bar + 1;
   A.flags = E->flags;
+  A.stall_block = E->test_stall_block;
+  A.spin_limit = E->test_spin_limit ? E->test_spin_limit : (1ull << 26);
+  E->test_stall_block = -1;
+  E->test_spin_limit = 0;
   int dev = E->device, sms = 0, coop = 0, occ = 0;
   EK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   EK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
@@ -450,6 +462,14 @@ int imodel_swm_ensemble_advance(void *ens, const double *dt, const int32_t *nste
   int rc = imodel::ens_launch(E, dt, nsteps, E->block, E->blocks_per_sm, E->variant);
   if (rc) return rc;
   return imodel::ens_flags(E);
+}
+
+int imodel_swm_ensemble_test_stall(void *ens, int32_t block, int64_t spin_limit) {
+  Ens *E = static_cast<Ens *>(ens);
+  if (!E || block < 0 || spin_limit < 1) return IMODEL_SWM_EINVAL;
+  E->test_stall_block = block;
+  E->test_spin_limit = static_cast<unsigned long long>(spin_limit);
+  return IMODEL_SWM_OK;
 }
 
 int imodel_swm_ensemble_tune(void *ens, const double *dt, int32_t nsteps, int32_t choice[3]) {

@@ -1,0 +1,144 @@
+// FP64 kernels of the moist shallow-water model (moist_swm.f90) beside the
+// shallow-water tendency of swm_k64.cu: the flux-form tracer advection of
+// advmtd = "trsk", the thermal momentum source, the condensation sources and
+// the RK4 stages of all seven fields.
+//
+// Compiled with --fmad=false and in the reference's operation order, so that
+// the GPU equals the CPU oracle bit for bit.  The one transcendental of the
+// sources, exp(20 theta) in qsat, is formed once on the host (theta keeps its
+// initial value in the reference's RK4 path) and read here.
+#include "swm_common.cuh"
+
+namespace imodel {
+namespace {
+
+// constants.f90:45 -- eps = epsilon(1.) (float epsilon)
+constexpr double kEps = 1.1920928955078125e-07;
+// initialize_moist_swm_fields (moist_swm.f90:730-732)
+constexpr double kLscale = 10.0, kGammaR = 0.001, kQprecip = 0.0001;
+
+__device__ __forceinline__ double rk_stage(int stage, double k, double yn, double *acc, double dt) {
+  // ode_rk4_moist_swm, moist_swm.f90:1880-1960
+  if (stage == 0) {
+    *acc = k;
+    return yn + dt * k / 2.0;
+  } else if (stage == 1) {
+    *acc = *acc + 2.0 * k;
+    return yn + dt * k / 2.0;
+  } else if (stage == 2) {
+    *acc = *acc + 2.0 * k;
+    return yn + dt * k;
+  }
+  return yn + dt * (*acc + k) / 6.0;
+}
+// Fortran max(0, x) / min(a, b) as std::max / std::min evaluate them
+__device__ __forceinline__ double fmax0(double x) { return (0.0 < x) ? x : 0.0; }
+__device__ __forceinline__ double fminq(double a, double b) { return (b < a) ? b : a; }
+
+// Edges: u q_e for every advanced tracer (scalar_hx2ed + scalar_elem_product,
+// divhx with advmtd = "trsk"); with the shallow-water terms on, the thermal
+// momentum source (source, moist_swm.f90:1299-1315) added to the momentum
+// tendency and u's RK stage.
+__global__ void __launch_bounds__(256) k_moist_edge(DevMesh M, MoistArgs A) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ne = M.ne;
+  if (e >= ne) return;
+  const int v1 = M.e_v[e], v2 = M.e_v[ne + e];
+  const double ue = A.u_in[e];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    if (!((A.active >> k) & 1)) continue;
+    const double qe = (A.q_in[k][v1] + A.q_in[k][v2]) * 0.5;
+    A.uphi[static_cast<size_t>(k) * ne + e] = ue * qe;
+  }
+  if (!A.swm) return;
+  const double l = M.e_leng[e], erad = M.erad, grav = M.grav;
+  double g = A.h_in[v2] * A.q_in[0][v2] - A.h_in[v1] * A.q_in[0][v1];
+  g = g / l / erad;
+  const double hed = A.h_ed[e];
+  double gpi_oh = 0.0;
+  if (fabs(hed) < kEps / 100000.0)
+    atomicOr(A.flags, 1);
+  else
+    gpi_oh = g / hed;
+  double gb = M.c_bt[v2] - M.c_bt[v1];
+  gb = gb / l / erad;
+  const double th_ed = (A.th[v1] + A.th[v2]) * 0.5;
+  const double su = (grav * 0.5) * gpi_oh + grav * (th_ed * gb);
+  const double momeq = A.tend_u[e] + su;
+  A.u_out[e] = rk_stage(A.stage, momeq, A.yn_u[e], A.acc_u + e, A.dt);
+}
+
+// Cells: the divergence of each advected tracer's flux (div_hx), the
+// condensation, evaporation and precipitation sources (source, :1317-1351)
+// and the RK stages of h and the tracers.
+__global__ void __launch_bounds__(256) k_moist_cell(DevMesh M, MoistArgs A) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nv = M.nv, ne = M.ne;
+  if (i >= nv) return;
+  double hs[4] = {0.0, 0.0, 0.0, 0.0};
+  if (A.swm) {
+    A.h_out[i] = rk_stage(A.stage, A.tend_h[i], A.yn_h[i], A.acc_h + i, A.dt);
+    const double hi = A.h_in[i];
+    const double qs = A.q0 * A.ex20[i] / ((hi + M.c_bt[i]) * M.grav);
+    double gamma_v = 1.0 + kLscale * (20.0 * qs);
+    gamma_v = 1.0 / gamma_v;
+    const double qv = A.qv[i], qc = A.qc[i];
+    double dqv = gamma_v * (qv - qs);
+    dqv = fmax0(dqv) / A.dt;
+    double dqc = fmax0(-gamma_v * (qv - qs));
+    dqc = fminq(qc, dqc) / A.dt;
+    const double dqr = fmax0(kGammaR * (qc - kQprecip)) / A.dt;
+    hs[1] = hi * (dqc - dqv);
+    hs[2] = hi * (dqv - dqc - dqr);
+    hs[3] = hi * dqr;
+    hs[0] = hi * (kLscale * (dqv - dqc));
+  }
+  const int n = M.c_nnb[i];
+  const double A_i = M.c_areag[i], erad = M.erad;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    if (!((A.active >> k) & 1)) continue;
+    const double *uphi = A.uphi + static_cast<size_t>(k) * ne;
+    double d = 0.0;
+    for (int j = 0; j < n; ++j) d = d + uphi[M.c_ed[j * nv + i]] * M.c_sd[j * nv + i];
+    double t = -(d / A_i / erad);
+    if (A.swm && k < 4) t = t + hs[k];
+    A.q_out[k][i] = rk_stage(A.stage, t, A.q_yn[k][i], A.q_acc[k] + i, A.dt);
+  }
+}
+
+// after a step: qv, qc, qr = h qv / h etc. (scalar_elem_divide, with its
+// guard), the fields the next step's sources read
+__global__ void k_moist_q(int nv, const double *__restrict__ h, const double *__restrict__ hqv,
+                          const double *__restrict__ hqc, const double *__restrict__ hqr,
+                          double *__restrict__ qv, double *__restrict__ qc,
+                          double *__restrict__ qr, int *flags) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  const double hi = h[i];
+  if (fabs(hi) < kEps / 100000.0) {
+    atomicOr(flags, 1);
+    return;
+  }
+  qv[i] = hqv[i] / hi;
+  qc[i] = hqc[i] / hi;
+  qr[i] = hqr[i] / hi;
+}
+
+inline int nblocks(int n, int t) { return (n + t - 1) / t; }
+
+}  // namespace
+
+void launch_moist_stage(const DevMesh &M, const MoistArgs &A, cudaStream_t s) {
+  k_moist_edge<<<nblocks(M.ne, 256), 256, 0, s>>>(M, A);
+  k_moist_cell<<<nblocks(M.nv, 256), 256, 0, s>>>(M, A);
+}
+
+void launch_moist_q(int nv, const double *h, const double *hqv, const double *hqc,
+                    const double *hqr, double *qv, double *qc, double *qr, int *flags,
+                    cudaStream_t s) {
+  k_moist_q<<<nblocks(nv, 256), 256, 0, s>>>(nv, h, hqv, hqc, hqr, qv, qc, qr, flags);
+}
+
+}  // namespace imodel

@@ -298,6 +298,13 @@ int imodel_swm_ensemble_advance(void *ens, const double *dt, const int32_t *nste
  * the fastest, restores the state.
  * choice = {block size, blocks per SM, variant}. */
 int imodel_swm_ensemble_tune(void *ens, const double *dt, int32_t nsteps, int32_t choice[3]);
+/* Test hook with no counterpart in the reference: in the next
+ * imodel_swm_ensemble_advance launch only, block `block` of the persistent
+ * launch leaves before its first grid-wide barrier and every barrier wait
+ * gives up after spin_limit polls (about 64 ns each).  The other blocks then
+ * time out, the launch ends and the advance returns IMODEL_SWM_ECUDA ("grid
+ * barrier timed out"); the ensemble stays usable (set the states again). */
+int imodel_swm_ensemble_test_stall(void *ens, int32_t block, int64_t spin_limit);
 int imodel_swm_ensemble_destroy(void *ens);
 const char *imodel_swm_ensemble_last_error(void *ens);
 void *imodel_swm_ensemble_stream(void *ens);

@@ -65,6 +65,13 @@ def lib() -> ctypes.CDLL:
         L.oracle_set_apvm.argtypes = [vp, ctypes.c_double, ctypes.c_double]
         L.oracle_set_scheme.argtypes = [vp, ctypes.c_int32]
         L.oracle_set_fcor.argtypes = [vp, ctypes.c_int32, ctypes.c_double]
+        L.oracle_moist_create.argtypes = [ctypes.POINTER(Mesh), ctypes.c_int32, f64p, f64p,
+                                          ctypes.c_double, ctypes.c_int32]
+        L.oracle_moist_create.restype = vp
+        L.oracle_moist_destroy.argtypes = [vp]
+        L.oracle_moist_destroy.restype = None
+        L.oracle_moist_set_q.argtypes = [vp, f64p, f64p, f64p]
+        L.oracle_moist_run.argtypes = [vp, ctypes.POINTER(f64p), ctypes.c_double, ctypes.c_int32]
         L.oracle_set_diffusion_fields.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
         _lib = L
     return _lib
@@ -196,3 +203,37 @@ def tc2(grid):
     u = np.zeros(grid.ne)
     lib().oracle_tc2(ctypes.byref(grid.c_struct()), _p(h), _p(u))
     return h, u
+
+
+class MoistOracle:
+    """The reference's moist shallow-water model (moist_swm.f90, advmtd =
+    "trsk", RK4) on the CPU, for one grid and test case; fields as in
+    imodel_gb300.moist.moist_fields."""
+
+    FIELDS = ("h", "u", "htheta", "hqv", "hqc", "hqr", "htracer")
+
+    def __init__(self, grid, testcase: int, fields: dict, nthreads: int = 0):
+        self.grid = grid
+        self._mesh = grid.c_struct()
+        self._bt = np.ascontiguousarray(fields["bt"], dtype=np.float64)
+        self._theta = np.ascontiguousarray(fields["theta"], dtype=np.float64)
+        n = nthreads if nthreads > 0 else (os.cpu_count() or 1)
+        self._h = lib().oracle_moist_create(ctypes.byref(self._mesh), testcase, _p(self._bt),
+                                            _p(self._theta), float(fields["q0"]), n)
+        if not self._h:
+            raise ValueError("moist test case must be 1..5")
+        q = [np.ascontiguousarray(fields[k], dtype=np.float64) for k in ("qv", "qc", "qr")]
+        lib().oracle_moist_set_q(self._h, _p(q[0]), _p(q[1]), _p(q[2]))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().oracle_moist_destroy(self._h)
+            self._h = None
+
+    def run(self, state: dict, dt: float, nsteps: int) -> dict:
+        ys = [np.array(state[k], dtype=np.float64) for k in self.FIELDS]
+        arr = (ctypes.POINTER(ctypes.c_double) * 7)(*[_p(y) for y in ys])
+        rc = lib().oracle_moist_run(self._h, arr, dt, nsteps)
+        if rc:
+            raise RuntimeError(f"oracle moist run status {rc}")
+        return dict(zip(self.FIELDS, ys))

@@ -1048,3 +1048,222 @@ int oracle_field(void *p, int32_t which, double *out) {
 }
 
 }  // extern "C"
+
+// ---- the moist shallow-water model (moist_swm.f90) ------------------------
+// Tracers h theta, h qv, h qc, h qr and a passive h tracer advected with
+// advmtd = "trsk" (divhx, highorder.f90:4901-4983: div_hx of u times
+// scalar_hx2ed of the tracer), the thermal momentum source and the
+// condensation / precipitation sources (source, moist_swm.f90:1278-1353),
+// classic RK4 (ode_rk4_moist_swm, :1819-2011, no monotonic filter).  theta,
+// qv, qc, qr are the module fields the sources read: theta keeps its
+// initial value in the RK4 path (nothing updates it there), qv, qc, qr are
+// hqv / h etc. after each step (moist_swm_tests, :1531-1533).
+struct MoistOracle {
+  Oracle *base;
+  int testcase;
+  double q0, dt;
+  std::vector<double> theta, qv, qc, qr;
+  std::vector<double> f[7][4];          // tendencies of the 7 fields per stage
+  std::vector<double> stage_in[7], tmp_out[7];
+  std::vector<double> uphi, div, su, hs[4];
+};
+
+namespace {
+constexpr double kLscale = 10.0, kGammaR = 0.001, kQprecip = 0.0001;
+
+// tendency_advection (highorder.f90:3936-3972) with advmtd = "trsk"
+void advection(MoistOracle &mo, const double *q, const double *u, double *phif) {
+  const imodel_swm_mesh &m = mo.base->m;
+  const int nv = m.nv, ne = m.ne, nth = mo.base->nthreads;
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int l = 0; l < ne; ++l) {
+    const double qe = (q[m.ed_v[2 * l] - 1] + q[m.ed_v[2 * l + 1] - 1]) * 0.5;
+    mo.uphi[l] = u[l] * qe;
+  }
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (int i = 0; i < nv; ++i) {
+    double d = 0.0;
+    for (int j = 0; j < m.nnb[i]; ++j) {
+      const int l = m.v_ed[I6(i, j)] - 1;
+      const double signcor = static_cast<double>(m.hx_ttgout[I6(i, j)]);
+      d = d + signcor * mo.uphi[l] * m.edhx_leng[l];
+    }
+    phif[i] = -(d / m.hx_areag[i] / m.erad);
+  }
+}
+
+// qsat (moist_swm.f90:618-622)
+inline double qsat(double T, double H, double B, double q0, double grav) {
+  return q0 * std::exp(20.0 * T) / ((H + B) * grav);
+}
+
+// tendency_moist_swm (moist_swm.f90:1151-1276) for RK4; out[0..6] = masseq,
+// momeq, tempeq, vapoureq, cloudeq, raineq, tracereq
+int moist_tendency(MoistOracle &mo, const double *const in[7], double *const out[7]) {
+  Oracle &o = *mo.base;
+  const imodel_swm_mesh &m = o.m;
+  const int nv = m.nv, ne = m.ne, nth = o.nthreads;
+  const double grav = m.grav, gravo2 = grav * 0.5, erad = m.erad;
+  const double *h = in[0], *u = in[1];
+  if (mo.testcase > 1) {
+    int rc = tendency(o, h, u, out[0], out[1]);
+    if (rc) return rc;
+    for (int k = 2; k < 6; ++k) advection(mo, in[k], u, out[k]);
+    if (mo.testcase == 2) advection(mo, in[6], u, out[6]);
+    // source (moist_swm.f90:1278-1353): momentum, from h^2 theta and the
+    // topography; h_ed is the tendency's
+    int bad = 0;
+#pragma omp parallel for schedule(static) num_threads(nth) reduction(+ : bad)
+    for (int l = 0; l < ne; ++l) {
+      const int v1 = m.ed_v[2 * l] - 1, v2 = m.ed_v[2 * l + 1] - 1;
+      double g = h[v2] * in[2][v2] - h[v1] * in[2][v1];
+      g = g / m.ed_leng[l] / erad;
+      double gpi_oh = 0.0;
+      if (std::fabs(o.h_ed[l]) < kEps / 100000.0)
+        bad += 1;
+      else
+        gpi_oh = g / o.h_ed[l];
+      double gb = o.bt[v2] - o.bt[v1];
+      gb = gb / m.ed_leng[l] / erad;
+      const double th_ed = (mo.theta[v1] + mo.theta[v2]) * 0.5;
+      mo.su[l] = gravo2 * gpi_oh + grav * (th_ed * gb);
+    }
+    if (bad) return IMODEL_SWM_EDIVZERO;
+#pragma omp parallel for schedule(static) num_threads(nth)
+    for (int i = 0; i < nv; ++i) {
+      const double qs = qsat(mo.theta[i], h[i], o.bt[i], mo.q0, grav);
+      double gamma_v = 1.0 + kLscale * (20.0 * qs);
+      gamma_v = 1.0 / gamma_v;
+      double dqv = gamma_v * (mo.qv[i] - qs);
+      dqv = std::max(0.0, dqv) / mo.dt;
+      double dqc = std::max(0.0, -gamma_v * (mo.qv[i] - qs));
+      dqc = std::min(mo.qc[i], dqc) / mo.dt;
+      const double dqr = std::max(0.0, kGammaR * (mo.qc[i] - kQprecip)) / mo.dt;
+      mo.hs[1][i] = h[i] * (dqc - dqv);
+      mo.hs[2][i] = h[i] * (dqv - dqc - dqr);
+      mo.hs[3][i] = h[i] * dqr;
+      mo.hs[0][i] = h[i] * (kLscale * (dqv - dqc));
+    }
+#pragma omp parallel for schedule(static) num_threads(nth)
+    for (int l = 0; l < ne; ++l) out[1][l] = out[1][l] + mo.su[l];
+#pragma omp parallel for schedule(static) num_threads(nth)
+    for (int i = 0; i < nv; ++i)
+      for (int k = 0; k < 4; ++k) out[2 + k][i] = out[2 + k][i] + mo.hs[k][i];
+  } else if (mo.testcase == 1) {
+    advection(mo, in[6], u, out[6]);
+  }
+  return IMODEL_SWM_OK;
+}
+}  // namespace
+
+extern "C" {
+
+void *oracle_moist_create(const imodel_swm_mesh *m, int32_t testcase, const double *bt,
+                          const double *theta, double q0, int32_t nthreads) {
+  if (!m || !theta || testcase < 1 || testcase > 5) return nullptr;
+  MoistOracle *mo = new MoistOracle();
+  mo->base = static_cast<Oracle *>(oracle_create(m, testcase, bt, nthreads));
+  mo->testcase = testcase;
+  mo->q0 = q0;
+  const size_t nv = m->nv, ne = m->ne;
+  mo->theta.assign(theta, theta + nv);
+  mo->qv.assign(nv, 0.0);
+  mo->qc.assign(nv, 0.0);
+  mo->qr.assign(nv, 0.0);
+  for (int k = 0; k < 7; ++k) {
+    const size_t n = k == 1 ? ne : nv;
+    for (int s = 0; s < 4; ++s) mo->f[k][s].assign(n, 0.0);
+    mo->stage_in[k].assign(n, 0.0);
+    mo->tmp_out[k].assign(n, 0.0);
+  }
+  mo->uphi.assign(ne, 0.0);
+  mo->su.assign(ne, 0.0);
+  for (int k = 0; k < 4; ++k) mo->hs[k].assign(nv, 0.0);
+  return mo;
+}
+
+void oracle_moist_destroy(void *p) {
+  MoistOracle *mo = static_cast<MoistOracle *>(p);
+  if (!mo) return;
+  oracle_destroy(mo->base);
+  delete mo;
+}
+
+// the module fields qv, qc, qr the next step's sources read
+int oracle_moist_set_q(void *p, const double *qv, const double *qc, const double *qr) {
+  MoistOracle &mo = *static_cast<MoistOracle *>(p);
+  const int nv = mo.base->m.nv;
+  mo.qv.assign(qv, qv + nv);
+  mo.qc.assign(qc, qc + nv);
+  mo.qr.assign(qr, qr + nv);
+  return IMODEL_SWM_OK;
+}
+
+// nsteps of the moist_swm_tests time loop: ode_rk4_moist_swm, then qv, qc,
+// qr = hq / h (scalar_elem_divide with its guard).  y[7] = h, u, h theta,
+// h qv, h qc, h qr, h tracer, advanced in place
+int oracle_moist_run(void *p, double *const y[7], double dt, int32_t nsteps) {
+  MoistOracle &mo = *static_cast<MoistOracle *>(p);
+  const imodel_swm_mesh &m = mo.base->m;
+  const int nv = m.nv, nth = mo.base->nthreads;
+  mo.dt = dt;
+  const size_t n[7] = {static_cast<size_t>(nv), static_cast<size_t>(m.ne), static_cast<size_t>(nv),
+                       static_cast<size_t>(nv), static_cast<size_t>(nv), static_cast<size_t>(nv),
+                       static_cast<size_t>(nv)};
+  // which fields a stage advances: all for testcase > 1 (the tracer for
+  // testcase 2 only), the tracer alone for testcase 1
+  bool adv[7];
+  for (int k = 0; k < 7; ++k)
+    adv[k] = mo.testcase > 1 ? (k < 6 || mo.testcase == 2) : k == 6;
+  for (int step = 0; step < nsteps; ++step) {
+    const double *in[7];
+    double *out[7];
+    for (int k = 0; k < 7; ++k) in[k] = y[k];
+    const double frac[3] = {0.5, 0.5, 1.0};
+    for (int s = 0; s < 4; ++s) {
+      for (int k = 0; k < 7; ++k) out[k] = mo.f[k][s].data();
+      int rc = moist_tendency(mo, in, out);
+      if (rc) return rc;
+      if (s == 3) break;
+      for (int k = 0; k < 7; ++k) {
+        std::vector<double> &nx = mo.stage_in[k];
+        const double *f0 = mo.f[k][s].data();
+        const double *yk = y[k];
+        if (!adv[k]) {
+          std::memcpy(nx.data(), yk, n[k] * sizeof(double));
+        } else if (frac[s] == 0.5) {
+#pragma omp parallel for schedule(static) num_threads(nth)
+          for (size_t i = 0; i < n[k]; ++i) nx[i] = yk[i] + dt * f0[i] / 2.0;
+        } else {
+#pragma omp parallel for schedule(static) num_threads(nth)
+          for (size_t i = 0; i < n[k]; ++i) nx[i] = yk[i] + dt * f0[i];
+        }
+        in[k] = nx.data();
+      }
+    }
+    for (int k = 0; k < 7; ++k) {
+      if (!adv[k]) continue;
+      const double *a = mo.f[k][0].data(), *b = mo.f[k][1].data(), *c = mo.f[k][2].data(),
+                   *d = mo.f[k][3].data();
+      double *yk = y[k];
+#pragma omp parallel for schedule(static) num_threads(nth)
+      for (size_t i = 0; i < n[k]; ++i)
+        yk[i] = yk[i] + dt * (a[i] + 2.0 * b[i] + 2.0 * c[i] + d[i]) / 6.0;
+    }
+    int bad = 0;
+    for (int i = 0; i < nv; ++i) {
+      const double hi = y[0][i];
+      if (std::fabs(hi) < kEps / 100000.0) {
+        bad += 1;
+        continue;
+      }
+      mo.qv[i] = y[3][i] / hi;
+      mo.qc[i] = y[4][i] / hi;
+      mo.qr[i] = y[5][i] / hi;
+    }
+    if (bad) return IMODEL_SWM_EDIVZERO;
+  }
+  return IMODEL_SWM_OK;
+}
+
+}  // extern "C"

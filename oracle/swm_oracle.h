@@ -52,6 +52,17 @@ int oracle_tc2(const imodel_swm_mesh *m, double *h, double *u);
  * 16 q_grad_ed, 17 h_rhb, 18 vhq_tr [nt][3], 19 v_hx [nv][3] */
 int oracle_field(void *o, int32_t which, double *out);
 
+/* the moist shallow-water model (moist_swm.f90) with advmtd = "trsk" and
+ * RK4: theta[nv] is the potential temperature the sources read (frozen at
+ * its initial value, as in the reference's RK4 path), q0 the saturation
+ * scale of its test case */
+void *oracle_moist_create(const imodel_swm_mesh *m, int32_t testcase, const double *bt,
+                          const double *theta, double q0, int32_t nthreads);
+void oracle_moist_destroy(void *o);
+int oracle_moist_set_q(void *o, const double *qv, const double *qc, const double *qr);
+/* y = {h[nv], u[ne], htheta, hqv, hqc, hqr, htracer [nv]}, advanced in place */
+int oracle_moist_run(void *o, double *const y[7], double dt, int32_t nsteps);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,6 +25,7 @@ def test_header_lists_match_python_mirror():
 
 def test_mlp_header_matches_python_mirror():
     assert _declared("imodel_mlp.h") == sorted(_capi.MLP_SYMBOLS)
+    assert _declared("imodel_moist.h") == sorted(_capi.MOIST_SYMBOLS)
 
 
 def test_mesh_library_exports():
@@ -38,7 +39,8 @@ def test_swm_library_exports():
     if not os.path.exists(path):
         pytest.skip("CUDA library not built (no nvcc)")
     lib = ctypes.CDLL(path)
-    for name in _declared("imodel_swm.h") + _declared("imodel_mlp.h"):
+    for name in _declared("imodel_swm.h") + _declared("imodel_mlp.h") + \
+            _declared("imodel_moist.h"):
         assert hasattr(lib, name), name
 
 

@@ -74,3 +74,34 @@ def test_ensemble_blowup_status(grid_at):
         ens.get_state(0, 0)
     assert ei.value.code == 3
     ens.close()
+
+
+def test_ensemble_barrier_timeout_status(grid_at):
+    """The persistent launch's grid-wide barriers wait a bounded time: when
+    one block never arrives (the test hook makes block 0 leave before its
+    first barrier) the others give up after a short wait, the advance reports
+    the timeout as a status, and the ensemble still works afterwards."""
+    from imodel_gb300 import _capi
+    g = grid_at(3)
+    states = _states(g, [7, 8], 8)
+    ens = Ensemble([g], [2])
+    for m, (h, u) in enumerate(states):
+        ens.set_state(0, m, h, u)
+    lib = _capi.swm_lib()
+    assert lib.imodel_swm_ensemble_test_stall(ens._handle, 0, 1 << 14) == 0
+    with pytest.raises(swm.SWMError) as ei:
+        ens.advance([1800.0], [3])
+    assert ei.value.code == _capi.ECUDA and "barrier" in str(ei.value)
+    # usable again: the same steps from the same states match a fresh ensemble
+    for m, (h, u) in enumerate(states):
+        ens.set_state(0, m, h, u)
+    ens.advance([1800.0], [3])
+    fresh = Ensemble([g], [2])
+    for m, (h, u) in enumerate(states):
+        fresh.set_state(0, m, h, u)
+    fresh.advance([1800.0], [3])
+    for m in range(2):
+        a, b = ens.get_state(0, m), fresh.get_state(0, m)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    ens.close()
+    fresh.close()
