@@ -68,12 +68,25 @@ def _run_parallel(jobs):
 
 
 def build_mesh_lib(force: bool = False) -> str:
-    os.makedirs(LIB_DIR, exist_ok=True)
+    """The grid builder: topology and host geometry (mesh.cpp, OpenMP) and
+    the GPU geometry kernels (mesh_gpu.cu, no multiply-add contraction)."""
+    os.makedirs(OBJ_DIR, exist_ok=True)
     out = os.path.join(LIB_DIR, "libimodel_mesh.so")
-    src = os.path.join(CSRC, "mesh.cpp")
-    deps = [src] + glob.glob(os.path.join(INCLUDE, "*.h"))
-    if force or _stale(out, deps):
-        _run_parallel([["g++"] + CXX_COMMON + ["-fopenmp", "-shared", src, "-o", out]])
+    headers = glob.glob(os.path.join(INCLUDE, "*.h")) + [os.path.join(CSRC, "mesh_internal.h")]
+    cpp = os.path.join(CSRC, "mesh.cpp")
+    cu = os.path.join(CSRC, "mesh_gpu.cu")
+    cpp_obj = os.path.join(OBJ_DIR, "mesh.o")
+    cu_obj = os.path.join(OBJ_DIR, "mesh_gpu.cu.o")
+    jobs = []
+    if force or _stale(cpp_obj, [cpp] + headers):
+        jobs.append(["g++"] + CXX_COMMON + ["-fopenmp", "-I" + CSRC, "-c", cpp, "-o", cpp_obj])
+    if force or _stale(cu_obj, [cu] + headers):
+        jobs.append([_nvcc()] + NVCC_COMMON + ["--fmad=false", "-c", cu, "-o", cu_obj])
+    if jobs:
+        _run_parallel(jobs)
+    if force or _stale(out, [cpp_obj, cu_obj]):
+        _run_parallel([[_nvcc(), "-shared"] + ARCH + [cpp_obj, cu_obj] +
+                       ["-o", out, "-Xcompiler", "-fopenmp", "-L" + _cuda_lib_dir(), "-lcudart"]])
     return out
 
 

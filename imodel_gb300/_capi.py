@@ -99,6 +99,7 @@ class Diag(ctypes.Structure):
 MESH_SYMBOLS = [
     "imodel_mesh_build", "imodel_mesh_view", "imodel_mesh_extra_view",
     "imodel_mesh_delaunay_violations", "imodel_mesh_free",
+    "imodel_mesh_build_gpu", "imodel_mesh_gpu_last_error",
 ]
 SWM_SYMBOLS = [
     "imodel_swm_create", "imodel_swm_step", "imodel_swm_tendency",
@@ -170,6 +171,11 @@ def mesh_lib() -> ctypes.CDLL:
             ctypes.POINTER(ctypes.c_double)]
         lib.imodel_mesh_free.argtypes = [ctypes.c_void_p]
         lib.imodel_mesh_free.restype = None
+        lib.imodel_mesh_build_gpu.argtypes = [ctypes.c_int32, ctypes.c_int32,
+                                              ctypes.c_int32,
+                                              ctypes.POINTER(ctypes.c_void_p)]
+        lib.imodel_mesh_gpu_last_error.argtypes = []
+        lib.imodel_mesh_gpu_last_error.restype = ctypes.c_char_p
         lib._typed = True
     return lib
 

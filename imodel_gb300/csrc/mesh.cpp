@@ -11,9 +11,16 @@
 // Topology: the reference triangulates each level with STRIPACK; for nodes
 // appended at edge midpoints that Delaunay triangulation is the 4-way
 // subdivision of the previous level, which is what this builder constructs.
-// delaunay_check() verifies the empty-circumcircle property on every edge.
+// The Delaunay check at the end verifies the empty-circumcircle property on
+// every edge.  Every loop runs on host threads (OpenMP); the numbering steps
+// that the reference does in one serial sweep (new nodes, edges and
+// triangles in the order of the lower node, then of its neighbour list) are
+// a per-node count, a prefix sum and a fill, which gives the same numbers.
+// The geometry has a second back end on the GPU (mesh_gpu.cu,
+// imodel_mesh_build_gpu) that starts from the same topology.
 
 #include "imodel_mesh.h"
+#include "mesh_internal.h"
 
 #include <algorithm>
 #include <array>
@@ -27,6 +34,9 @@
 #endif
 
 namespace {
+
+using imodel::mesh::Grid;
+using imodel::mesh::Topo;
 
 // constants.f90:31 -- pi is built from a default-real (float) literal.
 const double kPi = 4.0 * static_cast<double>(0.78539816339744830961566f);
@@ -154,55 +164,62 @@ struct Tri {
   int a, b, c;
 };
 
+// off[i + 1] = count(i), then the exclusive prefix sum: off[i] is the first
+// number node i hands out when nodes number in index order.
+template <class F>
+void count_scan(int n, F count, std::vector<int> &off) {
+  off.assign(static_cast<size_t>(n) + 1, 0);
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < n; ++i) off[static_cast<size_t>(i) + 1] = count(i);
+  for (int i = 0; i < n; ++i) off[static_cast<size_t>(i) + 1] += off[i];
+}
+
 // Counter-clockwise neighbour rings from a closed, consistently oriented
-// triangulation: in triangle (a,b,c), c follows b around a.
-void build_rings(int n, const std::vector<Tri> &tris, std::vector<int> &nnb,
+// triangulation: in triangle (a,b,c), c follows b around a.  Each ring
+// starts at the node's smallest-index neighbour.  False if a node has more
+// than six triangles (no icosahedral grid has).
+bool build_rings(int n, const std::vector<Tri> &tris, std::vector<int> &nnb,
                  std::vector<int> &ring) {
-  std::vector<int> cnt(n, 0);
-  std::vector<std::array<int, 16>> from(n), to(n);
-  auto add = [&](int v, int f, int t) {
-    int k = cnt[v]++;
-    if (k < 16) {
-      from[v][k] = f;
-      to[v][k] = t;
+  std::vector<int> cnt(n, 0), from(6 * static_cast<size_t>(n)), to(6 * static_cast<size_t>(n));
+  const int64_t ntr = static_cast<int64_t>(tris.size());
+  int over = 0;
+#pragma omp parallel for schedule(static) reduction(+ : over)
+  for (int64_t t = 0; t < ntr; ++t) {
+    const Tri &T = tris[t];
+    const int v[3] = {T.a, T.b, T.c}, f[3] = {T.b, T.c, T.a}, g[3] = {T.c, T.a, T.b};
+    for (int q = 0; q < 3; ++q) {
+      int k;
+#pragma omp atomic capture
+      k = cnt[v[q]]++;
+      if (k < 6) {
+        from[6 * static_cast<size_t>(v[q]) + k] = f[q];
+        to[6 * static_cast<size_t>(v[q]) + k] = g[q];
+      } else {
+        ++over;
+      }
     }
-  };
-  for (const Tri &t : tris) {
-    add(t.a, t.b, t.c);
-    add(t.b, t.c, t.a);
-    add(t.c, t.a, t.b);
   }
+  if (over) return false;
   nnb.assign(n, 0);
   ring.assign(static_cast<size_t>(n) * 6, -1);
+#pragma omp parallel for schedule(static)
   for (int v = 0; v < n; ++v) {
-    int k = cnt[v];
-    // start at the smallest-index neighbour
-    int start = from[v][0];
-    for (int i = 1; i < k; ++i) start = std::min(start, from[v][i]);
+    const int k = cnt[v];
+    const int *fv = &from[6 * static_cast<size_t>(v)], *tv = &to[6 * static_cast<size_t>(v)];
+    int start = fv[0];
+    for (int i = 1; i < k; ++i) start = std::min(start, fv[i]);
     int cur = start;
     for (int j = 0; j < k; ++j) {
       ring[static_cast<size_t>(v) * 6 + j] = cur;
       int nxt = -1;
       for (int i = 0; i < k; ++i)
-        if (from[v][i] == cur) nxt = to[v][i];
+        if (fv[i] == cur) nxt = tv[i];
       cur = nxt;
     }
     nnb[v] = k;
   }
+  return true;
 }
-
-struct Grid {
-  int nv = 0, ne = 0, nt = 0;
-  // 1-based index arrays, padded with 0
-  std::vector<int32_t> nnb, v_nb, v_ed, v_tr, ttgout, tnrccw, hx_nr;
-  std::vector<int32_t> ed_v, ed_sh, tr_v, tr_ed, tr_tg, tr_nr;
-  std::vector<double> hx_areag, hxtr, trskw, v_p, v_lat, v_lon;
-  std::vector<double> ed_leng, edhx_leng, ed_c, ed_c_lat, ed_c_lon, ed_tg, ed_nr;
-  std::vector<double> edhx_c, edhx_nr, edhx_tg;
-  std::vector<double> tr_areag, tr_trhx, tr_c, tr_c_lat;
-  int64_t delaunay_bad = 0;
-  double delaunay_margin = 0.0;
-};
 
 inline V3 getv(const std::vector<double> &a, size_t i) {
   return {a[3 * i], a[3 * i + 1], a[3 * i + 2]};
@@ -213,7 +230,12 @@ inline void setv(std::vector<double> &a, size_t i, const V3 &v) {
   a[3 * i + 2] = v.z;
 }
 
-int build(Grid &g, int level, int pos) {
+}  // namespace
+
+namespace imodel {
+namespace mesh {
+
+int topology(int level, int pos, Topo &T) {
   // --- nodes and subdivision triangulation -----------------------------
   std::vector<V3> P = icosanodes0(pos);
   // level-0 faces: triples of mutually adjacent nodes (edge = min distance)
@@ -234,171 +256,316 @@ int build(Grid &g, int level, int pos) {
           }
     if (tris.size() != 20) return IMODEL_SWM_EINVAL;
   }
-  std::vector<int> nnb, ring;
+  std::vector<int> nnb, ring, off;
+  auto NB = [&](int i, int j) { return ring[static_cast<size_t>(i) * 6 + j]; };
   for (int lev = 1; lev <= level; ++lev) {
-    int n1 = static_cast<int>(P.size());
-    build_rings(n1, tris, nnb, ring);
-    // meshrefin (smeshpack.f90:1655-1671): new node for every edge i<k in
-    // the order of i, then of i's neighbour list.
+    const int n1 = static_cast<int>(P.size());
+    if (!build_rings(n1, tris, nnb, ring)) return IMODEL_SWM_EINVAL;
+    // meshrefin (smeshpack.f90:1655-1671): a new node for every edge i < k
+    // in the order of i, then of i's neighbour list
+    count_scan(
+        n1,
+        [&](int i) {
+          int c = 0;
+          for (int j = 0; j < nnb[i]; ++j) c += NB(i, j) > i;
+          return c;
+        },
+        off);
     std::vector<int> mid(static_cast<size_t>(n1) * 6, -1);
-    P.reserve(static_cast<size_t>(4) * n1);
+    P.resize(static_cast<size_t>(n1) + off[n1]);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n1; ++i) {
+      int q = n1 + off[i];
       for (int j = 0; j < nnb[i]; ++j) {
-        int k = ring[static_cast<size_t>(i) * 6 + j];
+        const int k = NB(i, j);
         if (k > i) {
-          V3 q = {0.5 * (P[i].x + P[k].x), 0.5 * (P[i].y + P[k].y), 0.5 * (P[i].z + P[k].z)};
-          double r = std::sqrt(q.x * q.x + q.y * q.y + q.z * q.z);
-          q = divs(q, r);
-          mid[static_cast<size_t>(i) * 6 + j] = static_cast<int>(P.size());
-          P.push_back(q);
+          V3 m = {0.5 * (P[i].x + P[k].x), 0.5 * (P[i].y + P[k].y), 0.5 * (P[i].z + P[k].z)};
+          const double r = std::sqrt(m.x * m.x + m.y * m.y + m.z * m.z);
+          P[q] = divs(m, r);
+          mid[static_cast<size_t>(i) * 6 + j] = q;
+          ++q;
         }
       }
     }
     auto midof = [&](int a, int b) -> int {
-      int lo = std::min(a, b), hi = std::max(a, b);
+      const int lo = std::min(a, b), hi = std::max(a, b);
       for (int j = 0; j < nnb[lo]; ++j)
-        if (ring[static_cast<size_t>(lo) * 6 + j] == hi) return mid[static_cast<size_t>(lo) * 6 + j];
+        if (NB(lo, j) == hi) return mid[static_cast<size_t>(lo) * 6 + j];
       return -1;
     };
-    std::vector<Tri> nt;
-    nt.reserve(tris.size() * 4);
-    for (const Tri &t : tris) {
-      int ab = midof(t.a, t.b), bc = midof(t.b, t.c), ca = midof(t.c, t.a);
-      if (ab < 0 || bc < 0 || ca < 0) return IMODEL_SWM_EINVAL;
-      nt.push_back({t.a, ab, ca});
-      nt.push_back({ab, t.b, bc});
-      nt.push_back({ca, bc, t.c});
-      nt.push_back({ab, bc, ca});
+    const int64_t ntr = static_cast<int64_t>(tris.size());
+    std::vector<Tri> nt(4 * tris.size());
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+    for (int64_t t = 0; t < ntr; ++t) {
+      const Tri &o = tris[t];
+      const int ab = midof(o.a, o.b), bc = midof(o.b, o.c), ca = midof(o.c, o.a);
+      if (ab < 0 || bc < 0 || ca < 0) {
+        ++bad;
+        continue;
+      }
+      nt[4 * t] = {o.a, ab, ca};
+      nt[4 * t + 1] = {ab, o.b, bc};
+      nt[4 * t + 2] = {ca, bc, o.c};
+      nt[4 * t + 3] = {ab, bc, ca};
     }
+    if (bad) return IMODEL_SWM_EINVAL;
     tris.swap(nt);
   }
   const int nv = static_cast<int>(P.size());
-  build_rings(nv, tris, nnb, ring);
+  if (!build_rings(nv, tris, nnb, ring)) return IMODEL_SWM_EINVAL;
   const int nt = 2 * nv - 4;
   const int ne = 3 * nv - 6;
   if (static_cast<int>(tris.size()) != nt) return IMODEL_SWM_EINVAL;
+  T.nv = nv;
+  T.ne = ne;
+  T.nt = nt;
+  T.p.resize(3 * static_cast<size_t>(nv));
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < nv; ++i) setv(T.p, i, P[i]);
+  std::vector<V3>().swap(P);
+
+  // --- meshstruct numbering (smeshpack.f90:706-862), 0-based -------------
+  // edges: a new edge for every neighbour k > i, in the order of i, then of
+  // i's neighbour list; edge (i, k) with k < i is the one k numbered
+  std::vector<int> &ved = T.ved, &edv = T.edv;
+  ved.assign(static_cast<size_t>(nv) * 6, -1);
+  edv.assign(2 * static_cast<size_t>(ne), 0);
+  count_scan(
+      nv,
+      [&](int i) {
+        int c = 0;
+        for (int j = 0; j < nnb[i]; ++j) c += NB(i, j) > i;
+        return c;
+      },
+      off);
+  if (off[nv] != ne) return IMODEL_SWM_EINVAL;
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < nv; ++i) {
+    int l = off[i];
+    for (int j = 0; j < nnb[i]; ++j) {
+      const int k = NB(i, j);
+      if (k > i) {
+        ved[static_cast<size_t>(i) * 6 + j] = l;
+        edv[2 * static_cast<size_t>(l)] = i;
+        edv[2 * static_cast<size_t>(l) + 1] = k;
+        ++l;
+      }
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < nv; ++i) {
+    for (int j = 0; j < nnb[i]; ++j) {
+      const int k = NB(i, j);
+      if (k < i) {
+        for (int m = 0; m < nnb[k]; ++m)
+          if (NB(k, m) == i) {
+            ved[static_cast<size_t>(i) * 6 + j] = ved[static_cast<size_t>(k) * 6 + m];
+            break;
+          }
+      }
+    }
+  }
+  // triangles (i, NB(i,j), NB(i,j+1)): numbered by their smallest node, in
+  // the order of that node, then of its neighbour list; the others look
+  // their number up at the smallest node
+  std::vector<int> &vtr = T.vtr, &trv = T.trv;
+  vtr.assign(static_cast<size_t>(nv) * 6, -1);
+  trv.assign(3 * static_cast<size_t>(nt), 0);
+  auto corner = [&](int i, int j, int q) {
+    return q == 0 ? i : NB(i, (j + q - 1) % nnb[i]);
+  };
+  auto lowest = [&](int i, int j) {
+    return std::min(i, std::min(corner(i, j, 1), corner(i, j, 2)));
+  };
+  count_scan(
+      nv,
+      [&](int i) {
+        int c = 0;
+        for (int j = 0; j < nnb[i]; ++j) c += lowest(i, j) == i;
+        return c;
+      },
+      off);
+  if (off[nv] != nt) return IMODEL_SWM_EINVAL;
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < nv; ++i) {
+    int k = off[i];
+    for (int j = 0; j < nnb[i]; ++j)
+      if (lowest(i, j) == i) {
+        vtr[static_cast<size_t>(i) * 6 + j] = k;
+        for (int q = 0; q < 3; ++q) trv[3 * static_cast<size_t>(k) + q] = corner(i, j, q);
+        ++k;
+      }
+  }
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < nv; ++i) {
+    for (int j = 0; j < nnb[i]; ++j) {
+      const int minind = lowest(i, j);
+      if (minind == i) continue;
+      const int nm = nnb[minind];
+      for (int l = 0; l < nm; ++l) {
+        if (NB(minind, l) != i) continue;
+        if (minind == corner(i, j, 2)) {
+          vtr[static_cast<size_t>(i) * 6 + j] = vtr[static_cast<size_t>(minind) * 6 + l];
+        } else {
+          const int m = (l - 1 + nm) % nm;
+          vtr[static_cast<size_t>(i) * 6 + j] = vtr[static_cast<size_t>(minind) * 6 + m];
+        }
+        break;
+      }
+    }
+  }
+  // edges of each triangle (edge l joins corners l and l+1) and the two
+  // triangles of each edge, the lower number first (the order a sweep over
+  // the triangles meets them)
+  std::vector<int> &tred = T.tred, &edsh = T.edsh;
+  tred.assign(3 * static_cast<size_t>(nt), -1);
+  edsh.assign(2 * static_cast<size_t>(ne), -1);
+  auto getedge = [&](int a, int b) -> int {
+    for (int j = 0; j < nnb[a]; ++j)
+      if (NB(a, j) == b) return ved[static_cast<size_t>(a) * 6 + j];
+    return -1;
+  };
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+  for (int k = 0; k < nt; ++k)
+    for (int l = 0; l < 3; ++l) {
+      const int e = getedge(trv[3 * static_cast<size_t>(k) + l],
+                            trv[3 * static_cast<size_t>(k) + (l + 1) % 3]);
+      if (e < 0) ++bad;
+      tred[3 * static_cast<size_t>(k) + l] = e;
+    }
+  if (bad) return IMODEL_SWM_EINVAL;
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+  for (int i = 0; i < nv; ++i) {
+    const int nb = nnb[i];
+    for (int j = 0; j < nb; ++j) {
+      if (NB(i, j) < i) continue;
+      const int e = ved[static_cast<size_t>(i) * 6 + j];
+      const int a = vtr[static_cast<size_t>(i) * 6 + j];
+      const int b = vtr[static_cast<size_t>(i) * 6 + (j - 1 + nb) % nb];
+      if (e < 0 || a < 0 || b < 0 || a == b) {
+        ++bad;
+        continue;
+      }
+      edsh[2 * static_cast<size_t>(e)] = std::min(a, b);
+      edsh[2 * static_cast<size_t>(e) + 1] = std::max(a, b);
+    }
+  }
+  if (bad) return IMODEL_SWM_EINVAL;
+  // every index the geometry gathers is in range (both back ends read
+  // through them without further checks)
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+  for (int i = 0; i < nv; ++i) {
+    if (nnb[i] < 3 || nnb[i] > 6) ++bad;
+    for (int j = 0; j < nnb[i] && j < 6; ++j) {
+      const size_t q = static_cast<size_t>(i) * 6 + j;
+      if (ring[q] < 0 || ring[q] >= nv || ved[q] < 0 || ved[q] >= ne || vtr[q] < 0 || vtr[q] >= nt)
+        ++bad;
+    }
+  }
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+  for (int64_t q = 0; q < 2 * static_cast<int64_t>(ne); ++q)
+    if (edv[q] < 0 || edv[q] >= nv || edsh[q] < 0 || edsh[q] >= nt) ++bad;
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+  for (int64_t q = 0; q < 3 * static_cast<int64_t>(nt); ++q)
+    if (trv[q] < 0 || trv[q] >= nv || tred[q] < 0 || tred[q] >= ne) ++bad;
+  if (bad) return IMODEL_SWM_EINVAL;
+  T.nnb.swap(nnb);
+  T.ring.swap(ring);
+  return IMODEL_SWM_OK;
+}
+
+void export_topology(const Topo &T, Grid &g) {
+  const int nv = T.nv, ne = T.ne, nt = T.nt;
   g.nv = nv;
   g.ne = ne;
   g.nt = nt;
+  g.v_p = T.p;
+  g.nnb.assign(T.nnb.begin(), T.nnb.end());
+  g.v_nb.assign(6 * static_cast<size_t>(nv), 0);
+  g.v_ed.assign(6 * static_cast<size_t>(nv), 0);
+  g.v_tr.assign(6 * static_cast<size_t>(nv), 0);
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < nv; ++i)
+    for (int j = 0; j < T.nnb[i]; ++j) {
+      const size_t q = static_cast<size_t>(i) * 6 + j;
+      g.v_nb[q] = T.ring[q] + 1;
+      g.v_ed[q] = T.ved[q] + 1;
+      g.v_tr[q] = T.vtr[q] + 1;
+    }
+  g.ed_v.resize(2 * static_cast<size_t>(ne));
+  g.ed_sh.resize(2 * static_cast<size_t>(ne));
+#pragma omp parallel for schedule(static)
+  for (int64_t q = 0; q < 2 * static_cast<int64_t>(ne); ++q) {
+    g.ed_v[q] = T.edv[q] + 1;
+    g.ed_sh[q] = T.edsh[q] + 1;
+  }
+  g.tr_v.resize(3 * static_cast<size_t>(nt));
+  g.tr_ed.resize(3 * static_cast<size_t>(nt));
+#pragma omp parallel for schedule(static)
+  for (int64_t q = 0; q < 3 * static_cast<int64_t>(nt); ++q) {
+    g.tr_v[q] = T.trv[q] + 1;
+    g.tr_ed[q] = T.tred[q] + 1;
+  }
+}
 
-  // --- meshstruct (smeshpack.f90:370-1195), 0-based internally ----------
-  std::vector<int> ved(static_cast<size_t>(nv) * 6, -1), vtr(static_cast<size_t>(nv) * 6, -1);
-  g.v_p.resize(3 * static_cast<size_t>(nv));
+}  // namespace mesh
+}  // namespace imodel
+
+namespace {
+
+// meshstruct's geometry (smeshpack.f90:706-1151), the kite areas and the
+// TRSK weights on host threads, entity by entity in the reference's
+// arithmetic.  Returns an IMODEL_SWM_* status.
+int geometry_host(const Topo &T, Grid &g) {
+  const int nv = T.nv, ne = T.ne, nt = T.nt;
+  const std::vector<int> &nnb = T.nnb, &ved = T.ved, &vtr = T.vtr, &edv = T.edv,
+                         &edsh = T.edsh, &trv = T.trv, &tred = T.tred;
+  auto P = [&](int i) { return getv(T.p, i); };
   g.v_lat.resize(nv);
   g.v_lon.resize(nv);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < nv; ++i) {
-    setv(g.v_p, i, P[i]);
-    cart2sph(P[i].x, P[i].y, P[i].z, g.v_lon[i], g.v_lat[i]);
+    const V3 p = P(i);
+    cart2sph(p.x, p.y, p.z, g.v_lon[i], g.v_lat[i]);
   }
-  auto NB = [&](int i, int j) { return ring[static_cast<size_t>(i) * 6 + j]; };
 
   // edges (smeshpack.f90:706-752)
-  std::vector<int> edv(2 * static_cast<size_t>(ne));
   g.ed_c.resize(3 * static_cast<size_t>(ne));
   g.ed_c_lat.resize(ne);
   g.ed_c_lon.resize(ne);
   g.ed_nr.resize(3 * static_cast<size_t>(ne));
   g.ed_tg.resize(3 * static_cast<size_t>(ne));
   g.ed_leng.resize(ne);
-  {
-    int l = 0;
-    for (int i = 0; i < nv; ++i) {
-      for (int j = 0; j < nnb[i]; ++j) {
-        int k = NB(i, j);
-        if (k > i) {
-          if (l >= ne) return IMODEL_SWM_EINVAL;
-          ved[static_cast<size_t>(i) * 6 + j] = l;
-          edv[2 * static_cast<size_t>(l)] = i;
-          edv[2 * static_cast<size_t>(l) + 1] = k;
-          ++l;
-        } else {
-          for (int m = 0; m < nnb[k]; ++m)
-            if (NB(k, m) == i) {
-              ved[static_cast<size_t>(i) * 6 + j] = ved[static_cast<size_t>(k) * 6 + m];
-              break;
-            }
-        }
-      }
-    }
-    if (l != ne) return IMODEL_SWM_EINVAL;
-  }
 #pragma omp parallel for schedule(static)
   for (int l = 0; l < ne; ++l) {
-    int i = edv[2 * static_cast<size_t>(l)], k = edv[2 * static_cast<size_t>(l) + 1];
-    V3 c = midpoint(P[i], P[k]);
+    const V3 pi = P(edv[2 * static_cast<size_t>(l)]), pk = P(edv[2 * static_cast<size_t>(l) + 1]);
+    V3 c = midpoint(pi, pk);
     setv(g.ed_c, l, c);
     cart2sph(c.x, c.y, c.z, g.ed_c_lon[l], g.ed_c_lat[l]);
-    V3 nr = cross(P[i], P[k]);
+    V3 nr = cross(pi, pk);
     nr = divs(nr, norm(nr));
     V3 tg = cross(nr, c);
     tg = divs(tg, norm(tg));
     setv(g.ed_nr, l, nr);
     setv(g.ed_tg, l, tg);
-    g.ed_leng[l] = arclen(P[i], P[k]);
+    g.ed_leng[l] = arclen(pi, pk);
   }
-  auto getedge = [&](int a, int b) -> int {
-    for (int j = 0; j < nnb[a]; ++j)
-      if (NB(a, j) == b) return ved[static_cast<size_t>(a) * 6 + j];
-    return -1;
-  };
 
-  // triangles (smeshpack.f90:779-862)
-  std::vector<int> trv(3 * static_cast<size_t>(nt));
-  {
-    int k = 0;
-    for (int i = 0; i < nv; ++i) {
-      int nb = nnb[i];
-      for (int j = 0; j < nb; ++j) {
-        int ind[3] = {i, NB(i, j), NB(i, (j + 1) % nb)};
-        int minind = std::min(ind[0], std::min(ind[1], ind[2]));
-        if (minind == i) {
-          if (k >= nt) return IMODEL_SWM_EINVAL;
-          vtr[static_cast<size_t>(i) * 6 + j] = k;
-          for (int q = 0; q < 3; ++q) trv[3 * static_cast<size_t>(k) + q] = ind[q];
-          ++k;
-        } else {
-          int nm = nnb[minind];
-          for (int l = 0; l < nm; ++l) {
-            if (NB(minind, l) == i && minind == ind[2]) {
-              vtr[static_cast<size_t>(i) * 6 + j] = vtr[static_cast<size_t>(minind) * 6 + l];
-              break;
-            }
-            if (NB(minind, l) == i && minind == ind[1]) {
-              int m = (l - 1 + nm) % nm;
-              vtr[static_cast<size_t>(i) * 6 + j] = vtr[static_cast<size_t>(minind) * 6 + m];
-              break;
-            }
-          }
-        }
-      }
-    }
-    if (k != nt) return IMODEL_SWM_EINVAL;
-  }
-  std::vector<int> tred(3 * static_cast<size_t>(nt)), edsh(2 * static_cast<size_t>(ne), -1);
+  // triangles: edge orientation signs (smeshpack.f90:779-862)
   g.tr_tg.resize(3 * static_cast<size_t>(nt));
   g.tr_nr.resize(3 * static_cast<size_t>(nt));
-  for (int k = 0; k < nt; ++k) {
-    for (int l = 0; l < 3; ++l) {
-      int m = (l + 1) % 3;
-      int e = getedge(trv[3 * static_cast<size_t>(k) + l], trv[3 * static_cast<size_t>(k) + m]);
-      if (e < 0) return IMODEL_SWM_EINVAL;
-      tred[3 * static_cast<size_t>(k) + l] = e;
-      if (edsh[2 * static_cast<size_t>(e)] < 0)
-        edsh[2 * static_cast<size_t>(e)] = k;
-      else
-        edsh[2 * static_cast<size_t>(e) + 1] = k;
-    }
-  }
   int bad_sign = 0;
 #pragma omp parallel for schedule(static) reduction(+ : bad_sign)
   for (int k = 0; k < nt; ++k) {
     for (int l = 0; l < 3; ++l) {
-      int m = (l + 1) % 3;
-      int e = tred[3 * static_cast<size_t>(k) + l];
-      V3 nr = cross(P[trv[3 * static_cast<size_t>(k) + l]], P[trv[3 * static_cast<size_t>(k) + m]]);
+      const int m = (l + 1) % 3;
+      const int e = tred[3 * static_cast<size_t>(k) + l];
+      V3 nr = cross(P(trv[3 * static_cast<size_t>(k) + l]), P(trv[3 * static_cast<size_t>(k) + m]));
       nr = {-nr.x, -nr.y, -nr.z};
       nr = divs(nr, norm(nr));
-      double dp = dot(nr, getv(g.ed_nr, e));
+      const double dp = dot(nr, getv(g.ed_nr, e));
       if (std::fabs(std::fabs(dp) - 1.0) > kEps * 100.0) bad_sign += 1;
       if (dp > 0) {
         g.tr_nr[3 * static_cast<size_t>(k) + l] = 1;
@@ -417,9 +584,9 @@ int build(Grid &g, int level, int pos) {
   g.tr_areag.resize(nt);
 #pragma omp parallel for schedule(static)
   for (int k = 0; k < nt; ++k) {
-    V3 p1 = P[trv[3 * static_cast<size_t>(k)]], p2 = P[trv[3 * static_cast<size_t>(k) + 1]],
-       p3 = P[trv[3 * static_cast<size_t>(k) + 2]];
-    V3 c = trcircumc(p1, p2, p3);
+    const V3 p1 = P(trv[3 * static_cast<size_t>(k)]), p2 = P(trv[3 * static_cast<size_t>(k) + 1]),
+             p3 = P(trv[3 * static_cast<size_t>(k) + 2]);
+    const V3 c = trcircumc(p1, p2, p3);
     setv(g.tr_c, k, c);
     double lon;
     cart2sph(c.x, c.y, c.z, lon, g.tr_c_lat[k]);
@@ -433,9 +600,9 @@ int build(Grid &g, int level, int pos) {
   g.edhx_leng.resize(ne);
 #pragma omp parallel for schedule(static)
   for (int i = 0; i < ne; ++i) {
-    V3 c1 = getv(g.tr_c, edsh[2 * static_cast<size_t>(i)]);
-    V3 c2 = getv(g.tr_c, edsh[2 * static_cast<size_t>(i) + 1]);
-    V3 c = midpoint(c1, c2);
+    const V3 c1 = getv(g.tr_c, edsh[2 * static_cast<size_t>(i)]);
+    const V3 c2 = getv(g.tr_c, edsh[2 * static_cast<size_t>(i) + 1]);
+    const V3 c = midpoint(c1, c2);
     setv(g.edhx_c, i, c);
     V3 nr = cross(c1, c2);
     nr = divs(nr, norm(nr));
@@ -454,26 +621,26 @@ int build(Grid &g, int level, int pos) {
   int bad_hx = 0;
 #pragma omp parallel for schedule(static) reduction(+ : bad_hx)
   for (int i = 0; i < nv; ++i) {
-    int nb = nnb[i];
+    const int nb = nnb[i];
     double area = 0.0;
     for (int j = 0; j < nb; ++j) {
-      int j1 = vtr[static_cast<size_t>(i) * 6 + (j == 0 ? nb - 1 : j - 1)];
-      int j2 = vtr[static_cast<size_t>(i) * 6 + j];
-      int e = ved[static_cast<size_t>(i) * 6 + j];
-      V3 cj1 = getv(g.tr_c, j1), cj2 = getv(g.tr_c, j2);
+      const int j1 = vtr[static_cast<size_t>(i) * 6 + (j == 0 ? nb - 1 : j - 1)];
+      const int j2 = vtr[static_cast<size_t>(i) * 6 + j];
+      const int e = ved[static_cast<size_t>(i) * 6 + j];
+      const V3 cj1 = getv(g.tr_c, j1), cj2 = getv(g.tr_c, j2);
       V3 nr = cross(cj1, cj2);
       nr = {-nr.x, -nr.y, -nr.z};
       nr = divs(nr, norm(nr));
-      double dp = dot(nr, getv(g.edhx_nr, e));
+      const double dp = dot(nr, getv(g.edhx_nr, e));
       if (std::fabs(std::fabs(dp) - 1.0) > kEps * 100.0) bad_hx += 1;
-      int hnr = dp > 0 ? 1 : -1;
-      int htg = -hnr;
+      const int hnr = dp > 0 ? 1 : -1;
+      const int htg = -hnr;
       g.hx_nr[static_cast<size_t>(i) * 6 + j] = hnr;
-      double d1 = dot(getv(g.ed_tg, e), muls(getv(g.edhx_nr, e), static_cast<double>(hnr)));
+      const double d1 = dot(getv(g.ed_tg, e), muls(getv(g.edhx_nr, e), static_cast<double>(hnr)));
       g.ttgout[static_cast<size_t>(i) * 6 + j] = static_cast<int>(std::copysign(1.0, d1));
-      double d2 = dot(getv(g.ed_nr, e), muls(getv(g.edhx_tg, e), static_cast<double>(htg)));
+      const double d2 = dot(getv(g.ed_nr, e), muls(getv(g.edhx_tg, e), static_cast<double>(htg)));
       g.tnrccw[static_cast<size_t>(i) * 6 + j] = static_cast<int>(std::copysign(1.0, d2));
-      area = area + sphtriarea(P[i], cj1, cj2);
+      area = area + sphtriarea(P(i), cj1, cj2);
     }
     g.hx_areag[i] = area;
   }
@@ -483,12 +650,12 @@ int build(Grid &g, int level, int pos) {
   g.tr_trhx.resize(3 * static_cast<size_t>(nt));
 #pragma omp parallel for schedule(static)
   for (int k = 0; k < nt; ++k) {
-    V3 pc = getv(g.tr_c, k);
+    const V3 pc = getv(g.tr_c, k);
     for (int j = 0; j < 3; ++j) {
-      int ed1 = tred[3 * static_cast<size_t>(k) + (j == 0 ? 2 : j - 1)];
-      int ed2 = tred[3 * static_cast<size_t>(k) + j];
-      V3 ped1 = getv(g.ed_c, ed1), ped2 = getv(g.ed_c, ed2);
-      V3 pv = P[trv[3 * static_cast<size_t>(k) + j]];
+      const int ed1 = tred[3 * static_cast<size_t>(k) + (j == 0 ? 2 : j - 1)];
+      const int ed2 = tred[3 * static_cast<size_t>(k) + j];
+      const V3 ped1 = getv(g.ed_c, ed1), ped2 = getv(g.ed_c, ed2);
+      const V3 pv = P(trv[3 * static_cast<size_t>(k) + j]);
       double a1 = sphtriarea(pc, ped1, pv);
       if (det3(pc, ped1, pv) < 0) a1 = -a1;
       double a2 = sphtriarea(pc, pv, ped2);
@@ -503,19 +670,19 @@ int build(Grid &g, int level, int pos) {
   g.trskw.assign(36 * static_cast<size_t>(nv), 0.0);
 #pragma omp parallel for schedule(static)
   for (int c = 0; c < nv; ++c) {
-    int n = nnb[c];
-    V3 pc = P[c];
+    const int n = nnb[c];
+    const V3 pc = P(c);
     double R[6];
     for (int j = 0; j < n; ++j) {
-      int ed1 = ved[static_cast<size_t>(c) * 6 + j];
-      int ed2 = ved[static_cast<size_t>(c) * 6 + (j + 1) % n];
-      V3 ped1 = getv(g.edhx_c, ed1), ped2 = getv(g.edhx_c, ed2);
-      V3 pv = getv(g.tr_c, vtr[static_cast<size_t>(c) * 6 + j]);
+      const int ed1 = ved[static_cast<size_t>(c) * 6 + j];
+      const int ed2 = ved[static_cast<size_t>(c) * 6 + (j + 1) % n];
+      const V3 ped1 = getv(g.edhx_c, ed1), ped2 = getv(g.edhx_c, ed2);
+      const V3 pv = getv(g.tr_c, vtr[static_cast<size_t>(c) * 6 + j]);
       double a1 = sphtriarea(pc, ped1, pv);
       if (det3(pc, ped1, pv) < 0) a1 = -a1;
       double a2 = sphtriarea(pc, pv, ped2);
       if (det3(pc, pv, ped2) < 0) a2 = -a2;
-      double a = a1 + a2;
+      const double a = a1 + a2;
       R[j] = a / g.hx_areag[c];
       g.hxtr[static_cast<size_t>(c) * 6 + j] = R[j];
     }
@@ -547,18 +714,22 @@ int build(Grid &g, int level, int pos) {
 #pragma omp parallel for schedule(static) reduction(+ : bad) reduction(max : worst)
     for (int e = 0; e < ne; ++e) {
       for (int s = 0; s < 2; ++s) {
-        int t = edsh[2 * static_cast<size_t>(e) + s];
-        int o = edsh[2 * static_cast<size_t>(e) + 1 - s];
-        int a = trv[3 * static_cast<size_t>(t)], b = trv[3 * static_cast<size_t>(t) + 1],
-            c = trv[3 * static_cast<size_t>(t) + 2];
+        const int t = edsh[2 * static_cast<size_t>(e) + s];
+        const int o = edsh[2 * static_cast<size_t>(e) + 1 - s];
+        const int a = trv[3 * static_cast<size_t>(t)], b = trv[3 * static_cast<size_t>(t) + 1],
+                  c = trv[3 * static_cast<size_t>(t) + 2];
         int d = -1;
         for (int q = 0; q < 3; ++q) {
-          int x = trv[3 * static_cast<size_t>(o) + q];
+          const int x = trv[3 * static_cast<size_t>(o) + q];
           if (x != edv[2 * static_cast<size_t>(e)] && x != edv[2 * static_cast<size_t>(e) + 1]) d = x;
         }
-        V3 nrm = cross(sub(P[b], P[a]), sub(P[c], P[a]));
+        if (d < 0) {  // the two triangles share all three nodes: not a grid
+          bad += 1;
+          continue;
+        }
+        V3 nrm = cross(sub(P(b), P(a)), sub(P(c), P(a)));
         nrm = divs(nrm, norm(nrm));
-        double m = dot(nrm, sub(P[d], P[a]));
+        const double m = dot(nrm, sub(P(d), P(a)));
         worst = std::max(worst, m);
         if (m > 1e-15) bad += 1;
       }
@@ -566,58 +737,27 @@ int build(Grid &g, int level, int pos) {
     g.delaunay_bad = bad;
     g.delaunay_margin = -worst;
   }
-
-  // --- export as 1-based reference arrays ------------------------------
-  g.nnb.assign(nnb.begin(), nnb.end());
-  g.v_nb.assign(6 * static_cast<size_t>(nv), 0);
-  g.v_ed.assign(6 * static_cast<size_t>(nv), 0);
-  g.v_tr.assign(6 * static_cast<size_t>(nv), 0);
-  for (int i = 0; i < nv; ++i)
-    for (int j = 0; j < nnb[i]; ++j) {
-      size_t q = static_cast<size_t>(i) * 6 + j;
-      g.v_nb[q] = ring[q] + 1;
-      g.v_ed[q] = ved[q] + 1;
-      g.v_tr[q] = vtr[q] + 1;
-    }
-  g.ed_v.resize(2 * static_cast<size_t>(ne));
-  g.ed_sh.resize(2 * static_cast<size_t>(ne));
-  for (size_t q = 0; q < 2 * static_cast<size_t>(ne); ++q) {
-    g.ed_v[q] = edv[q] + 1;
-    g.ed_sh[q] = edsh[q] + 1;
-  }
-  g.tr_v.resize(3 * static_cast<size_t>(nt));
-  g.tr_ed.resize(3 * static_cast<size_t>(nt));
-  for (size_t q = 0; q < 3 * static_cast<size_t>(nt); ++q) {
-    g.tr_v[q] = trv[q] + 1;
-    g.tr_ed[q] = tred[q] + 1;
-  }
   return IMODEL_SWM_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-int imodel_mesh_build(int32_t level, int32_t pos, int32_t nthreads, void **grid) {
+// topology, the index arrays and one geometry back end into a new grid
+template <class Geometry>
+int build_grid(int32_t level, int32_t pos, void **grid, Geometry geometry) {
   if (!grid || level < 0 || level > 11 || (pos != 0 && pos != 1)) return IMODEL_SWM_EINVAL;
   *grid = nullptr;
-#ifdef _OPENMP
-  int prev = omp_get_max_threads();
-  if (nthreads > 0) omp_set_num_threads(nthreads);
-#else
-  (void)nthreads;
-#endif
   Grid *g = new (std::nothrow) Grid();
   if (!g) return IMODEL_SWM_ENOMEM;
   int rc;
   try {
-    rc = build(*g, level, pos);
+    Topo t;
+    rc = imodel::mesh::topology(level, pos, t);
+    if (rc == IMODEL_SWM_OK) {
+      imodel::mesh::export_topology(t, *g);
+      rc = geometry(t, *g);
+    }
   } catch (const std::bad_alloc &) {
     rc = IMODEL_SWM_ENOMEM;
   }
-#ifdef _OPENMP
-  if (nthreads > 0) omp_set_num_threads(prev);
-#endif
   if (rc != IMODEL_SWM_OK) {
     delete g;
     return rc;
@@ -626,6 +766,36 @@ int imodel_mesh_build(int32_t level, int32_t pos, int32_t nthreads, void **grid)
   return IMODEL_SWM_OK;
 }
 
+// the message of the last failed GPU build on this thread
+thread_local const char *g_gpu_error = "";
+
+}  // namespace
+
+extern "C" {
+
+int imodel_mesh_build(int32_t level, int32_t pos, int32_t nthreads, void **grid) {
+#ifdef _OPENMP
+  const int prev = omp_get_max_threads();
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+  const int rc = build_grid(level, pos, grid, geometry_host);
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(prev);
+#endif
+  return rc;
+}
+
+int imodel_mesh_build_gpu(int32_t level, int32_t pos, int32_t device, void **grid) {
+  g_gpu_error = "";
+  if (device < 0) return IMODEL_SWM_EINVAL;
+  return build_grid(level, pos, grid, [&](const Topo &t, Grid &g) {
+    return imodel::mesh::geometry_gpu(t, g, device, &g_gpu_error);
+  });
+}
+
+const char *imodel_mesh_gpu_last_error(void) { return g_gpu_error ? g_gpu_error : ""; }
 int imodel_mesh_view(void *grid, imodel_swm_mesh *v) {
   if (!grid || !v) return IMODEL_SWM_EINVAL;
   Grid *g = static_cast<Grid *>(grid);

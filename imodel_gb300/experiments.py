@@ -316,7 +316,36 @@ def exp_williamson(args, pool):
     return out
 
 
-RUNS = {"tc2": exp_tc2, "williamson": exp_williamson, "balanced": exp_balanced, "ensemble": exp_ensemble,
+def exp_mesh(args, pool):
+    """Grid build times through the C ABI (imodel_mesh_build on all host
+    threads against imodel_mesh_build_gpu on device 0), levels 8 to
+    args.level (default 10), each the best of two builds."""
+    import ctypes
+
+    from . import _capi
+    lib = _capi.mesh_lib()
+    out = {}
+    for lvl in range(8, (args.level or 10) + 1):
+        row = {}
+        for name, call in (("host", lambda h: lib.imodel_mesh_build(lvl, 0, 0, h)),
+                           ("gpu", lambda h: lib.imodel_mesh_build_gpu(lvl, 0, 0, h))):
+            best = None
+            for _ in range(2):
+                h = ctypes.c_void_p()
+                t0 = time.perf_counter()
+                rc = call(ctypes.byref(h))
+                dt = time.perf_counter() - t0
+                lib.imodel_mesh_free(h)
+                if rc != 0:
+                    raise RuntimeError(f"{name} build of level {lvl} failed: {rc}")
+                best = dt if best is None else min(best, dt)
+            row[f"{name}_s"] = best
+        row["cells"] = 10 * 4 ** lvl + 2
+        out[f"level{lvl}"] = row
+    return out
+
+
+RUNS = {"tc2": exp_tc2, "mesh": exp_mesh, "williamson": exp_williamson, "balanced": exp_balanced, "ensemble": exp_ensemble,
         "mountains": exp_mountains, "fixed": exp_fixed, "large": exp_large}
 
 

@@ -1,5 +1,6 @@
 /*
- * imodel_mesh.h -- icosahedral Voronoi/Delaunay grid builder (host C++).
+ * imodel_mesh.h -- icosahedral Voronoi/Delaunay grid builder (host C++,
+ * with a GPU back end for the geometry).
  *
  * Builds the grid_structure fields that the shallow-water step consumes, for
  * the non-optimised hierarchical icosahedral grids of iModel:
@@ -39,6 +40,22 @@ extern "C" {
  * (0 = all).  Returns 0 or an IMODEL_SWM_E* code. */
 int imodel_mesh_build(int32_t level, int32_t pos, int32_t nthreads,
                       void **grid);
+
+/* The same grid with its geometry computed on CUDA device `device`: the
+ * topology (numbering) is built on host threads as by imodel_mesh_build,
+ * then one GPU kernel per meshstruct step forms every length, area, angle,
+ * sign, kite fraction and TRSK weight, and the Delaunay check
+ * (smeshpack.f90:706-1151, :4991-5154; interpack.f90:3978-4098).  Index
+ * and sign arrays equal imodel_mesh_build's; the GPU's atan, tan, atan2 and
+ * asin may differ from the host C library's in the last bit, so lengths,
+ * areas, angles and weights agree with imodel_mesh_build's to a few units in
+ * the last place.  The result is an ordinary grid handle (view, extra_view,
+ * delaunay_violations, free).  Returns 0, IMODEL_SWM_EINVAL,
+ * IMODEL_SWM_ENOMEM or IMODEL_SWM_ECUDA (message from
+ * imodel_mesh_gpu_last_error, per calling thread). */
+int imodel_mesh_build_gpu(int32_t level, int32_t pos, int32_t device,
+                          void **grid);
+const char *imodel_mesh_gpu_last_error(void);
 
 /* Fills *view with pointers into the grid's arrays (valid until free). */
 int imodel_mesh_view(void *grid, imodel_swm_mesh *view);

@@ -95,3 +95,34 @@ def test_pol_positions(grid_at):
     assert np.allclose(g.v_p[0], [0, 0, 1])
     assert g.delaunay_violations == 0
     assert abs(g.hx_areag.sum() - FOURPI) < 1e-12
+
+
+def _hashes():
+    import json
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", "mesh_hashes.json")
+    with open(path) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("pos", ["eqs", "pol"])
+@pytest.mark.parametrize("nthreads", [1, 0])
+def test_builder_reproduces_the_pinned_grids(pos, nthreads):
+    """Every array of the grids at levels 0-6 hashes to the fixture made
+    with one thread (tests/golden/make_mesh_hashes.py): the numbering steps
+    done as count + prefix sum + fill on many threads give the numbers of
+    the serial sweep, and the geometry is bit for bit the same."""
+    import importlib.util
+    import os
+    from imodel_gb300.mesh import meshbuild
+    spec = importlib.util.spec_from_file_location(
+        "make_mesh_hashes", os.path.join(os.path.dirname(__file__), "golden",
+                                         "make_mesh_hashes.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    table = _hashes()
+    for level in range(0, 7):
+        got = mk.grid_hashes(meshbuild(level, pos, nthreads=nthreads))
+        want = table[f"{pos}{level}"]
+        diff = sorted(k for k in want if want[k] != got.get(k))
+        assert not diff, (pos, level, diff)
