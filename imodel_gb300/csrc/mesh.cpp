@@ -221,10 +221,12 @@ bool build_rings(int n, const std::vector<Tri> &tris, std::vector<int> &nnb,
   return true;
 }
 
-inline V3 getv(const std::vector<double> &a, size_t i) {
+template <class A>
+inline V3 getv(const A &a, size_t i) {
   return {a[3 * i], a[3 * i + 1], a[3 * i + 2]};
 }
-inline void setv(std::vector<double> &a, size_t i, const V3 &v) {
+template <class A>
+inline void setv(A &a, size_t i, const V3 &v) {
   a[3 * i] = v.x;
   a[3 * i + 1] = v.y;
   a[3 * i + 2] = v.z;
@@ -481,19 +483,23 @@ void export_topology(const Topo &T, Grid &g) {
   g.nv = nv;
   g.ne = ne;
   g.nt = nt;
-  g.v_p = T.p;
-  g.nnb.assign(T.nnb.begin(), T.nnb.end());
-  g.v_nb.assign(6 * static_cast<size_t>(nv), 0);
-  g.v_ed.assign(6 * static_cast<size_t>(nv), 0);
-  g.v_tr.assign(6 * static_cast<size_t>(nv), 0);
+  g.v_p.resize(T.p.size());
+  g.nnb.resize(nv);
+  g.v_nb.resize(6 * static_cast<size_t>(nv));
+  g.v_ed.resize(6 * static_cast<size_t>(nv));
+  g.v_tr.resize(6 * static_cast<size_t>(nv));
 #pragma omp parallel for schedule(static)
-  for (int i = 0; i < nv; ++i)
-    for (int j = 0; j < T.nnb[i]; ++j) {
+  for (int i = 0; i < nv; ++i) {
+    for (int c = 0; c < 3; ++c) g.v_p[3 * static_cast<size_t>(i) + c] = T.p[3 * static_cast<size_t>(i) + c];
+    g.nnb[i] = T.nnb[i];
+    for (int j = 0; j < 6; ++j) {
       const size_t q = static_cast<size_t>(i) * 6 + j;
-      g.v_nb[q] = T.ring[q] + 1;
-      g.v_ed[q] = T.ved[q] + 1;
-      g.v_tr[q] = T.vtr[q] + 1;
+      const bool on = j < T.nnb[i];
+      g.v_nb[q] = on ? T.ring[q] + 1 : 0;
+      g.v_ed[q] = on ? T.ved[q] + 1 : 0;
+      g.v_tr[q] = on ? T.vtr[q] + 1 : 0;
     }
+  }
   g.ed_v.resize(2 * static_cast<size_t>(ne));
   g.ed_sh.resize(2 * static_cast<size_t>(ne));
 #pragma omp parallel for schedule(static)
@@ -507,6 +513,16 @@ void export_topology(const Topo &T, Grid &g) {
   for (int64_t q = 0; q < 3 * static_cast<int64_t>(nt); ++q) {
     g.tr_v[q] = T.trv[q] + 1;
     g.tr_ed[q] = T.tred[q] + 1;
+  }
+}
+
+void touch(void *p, size_t bytes) {
+  char *c = static_cast<char *>(p);
+  const int64_t chunk = int64_t{1} << 20, n = static_cast<int64_t>((bytes + chunk - 1) / chunk);
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < n; ++k) {
+    const size_t a = static_cast<size_t>(k) * chunk;
+    std::memset(c + a, 0, std::min(static_cast<size_t>(chunk), bytes - a));
   }
 }
 

@@ -341,9 +341,10 @@ struct Buffers {
       err = cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
     return d;
   }
-  template <class T>
-  void download(std::vector<T> &v, const T *d, size_t n) {
+  template <class A, class T>
+  void download(A &v, const T *d, size_t n) {
     v.resize(n);
+    touch(v.data(), n * sizeof(T));  // map the pages on host threads first
     if (err == cudaSuccess) err = cudaMemcpy(v.data(), d, n * sizeof(T), cudaMemcpyDeviceToHost);
   }
   ~Buffers() {

@@ -3,22 +3,50 @@
 // mesh_gpu.cu) start from.  Not part of the C ABI.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
+#include <memory>
+#include <new>
+#include <utility>
 #include <vector>
 
 namespace imodel {
 namespace mesh {
 
+// An allocator whose resize() leaves new elements uninitialised: every
+// array of a grid is written in full by the parallel loops (or the GPU copy)
+// that follow, so zero-filling it first on one thread is wasted time (about
+// 0.5 s for the 12 GB of a level-10 grid) and would put every page on the
+// first-touching thread's memory node.  assign(n, v) still fills.
+template <class T>
+struct NoInit : std::allocator<T> {
+  using std::allocator<T>::allocator;
+  template <class U>
+  struct rebind {
+    using other = NoInit<U>;
+  };
+  template <class U>
+  void construct(U *p) noexcept {
+    ::new (static_cast<void *>(p)) U;
+  }
+  template <class U, class... A>
+  void construct(U *p, A &&...a) {
+    ::new (static_cast<void *>(p)) U(std::forward<A>(a)...);
+  }
+};
+template <class T>
+using Array = std::vector<T, NoInit<T>>;
+
 // The grid_structure arrays of one grid, 1-based index arrays padded with 0
 // (the layouts of include/imodel_swm.h and include/imodel_mesh.h).
 struct Grid {
   int nv = 0, ne = 0, nt = 0;
-  std::vector<int32_t> nnb, v_nb, v_ed, v_tr, ttgout, tnrccw, hx_nr;
-  std::vector<int32_t> ed_v, ed_sh, tr_v, tr_ed, tr_tg, tr_nr;
-  std::vector<double> hx_areag, hxtr, trskw, v_p, v_lat, v_lon;
-  std::vector<double> ed_leng, edhx_leng, ed_c, ed_c_lat, ed_c_lon, ed_tg, ed_nr;
-  std::vector<double> edhx_c, edhx_nr, edhx_tg;
-  std::vector<double> tr_areag, tr_trhx, tr_c, tr_c_lat;
+  Array<int32_t> nnb, v_nb, v_ed, v_tr, ttgout, tnrccw, hx_nr;
+  Array<int32_t> ed_v, ed_sh, tr_v, tr_ed, tr_tg, tr_nr;
+  Array<double> hx_areag, hxtr, trskw, v_p, v_lat, v_lon;
+  Array<double> ed_leng, edhx_leng, ed_c, ed_c_lat, ed_c_lon, ed_tg, ed_nr;
+  Array<double> edhx_c, edhx_nr, edhx_tg;
+  Array<double> tr_areag, tr_trhx, tr_c, tr_c_lat;
   int64_t delaunay_bad = 0;
   double delaunay_margin = 0.0;
 };
@@ -43,6 +71,10 @@ int topology(int level, int pos, Topo &t);
 
 // The 1-based index arrays of g from t (host threads).
 void export_topology(const Topo &t, Grid &g);
+
+// Writes zeros over [p, p + bytes) on host threads, so that a buffer about
+// to be filled by one copy has its pages mapped in parallel.
+void touch(void *p, size_t bytes);
 
 // Geometry by the GPU kernels of mesh_gpu.cu on CUDA device `device`;
 // `why` receives a message on a CUDA error.  Returns an IMODEL_SWM_* status.
