@@ -134,7 +134,8 @@ class MoistOpts(ctypes.Structure):
     """struct imodel_moist_opts."""
 
     _fields_ = [("testcase", ctypes.c_int32), ("bt", c_f64p), ("theta", c_f64p),
-                ("q0", ctypes.c_double), ("device", ctypes.c_int32)]
+                ("q0", ctypes.c_double), ("device", ctypes.c_int32),
+                ("advection", ctypes.c_int32)]
 
 
 _libs: dict = {}

@@ -1414,6 +1414,7 @@ namespace {
 struct Moist {
   Handle *H = nullptr;  // the FP64 shallow-water handle: geometry, h and u
   int testcase = 0;
+  int upw1 = 0;  // tracer advection "upw1" instead of "trsk"
   double q0 = 0.0;
   double *th = nullptr, *ex20 = nullptr, *qv = nullptr, *qc = nullptr, *qr = nullptr;
   double *q[5][4] = {};  // per tracer: y_n, two stage buffers, RK accumulator
@@ -1455,6 +1456,8 @@ int imodel_moist_create(const imodel_swm_mesh *m, const imodel_moist_opts *o, vo
   if (!m || !o || !o->theta) return imodel::set_error(H, IMODEL_SWM_EINVAL, "mesh, opts and theta are required");
   if (o->testcase < 1 || o->testcase > 5)
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "moist test cases are 1..5");
+  if (o->advection != 0 && o->advection != 1)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "advection is 0 (trsk) or 1 (upw1)");
   imodel_swm_opts so{};
   so.precision = IMODEL_SWM_FP64;
   so.testcase = o->testcase;
@@ -1468,6 +1471,7 @@ int imodel_moist_create(const imodel_swm_mesh *m, const imodel_moist_opts *o, vo
   }
   if (rc) return rc;
   X->testcase = o->testcase;
+  X->upw1 = o->advection;
   X->q0 = o->q0;
   const size_t nv = H->nv, ne = H->ne;
   for (double **p : {&X->th, &X->ex20, &X->qv, &X->qc, &X->qr})
@@ -1533,6 +1537,7 @@ int imodel_moist_advance(void *handle, double dt, int32_t nsteps) {
       A.dt = dt;
       A.swm = swm ? 1 : 0;
       A.active = active;
+      A.upw1 = X->upw1;
       const double *h_in = swm ? in(st, W.yn_h, W.ya_h, W.yb_h) : W.yn_h;
       const double *u_in = swm ? in(st, W.yn_u, W.ya_u, W.yb_u) : W.yn_u;
       if (swm)

@@ -179,6 +179,7 @@ struct MoistArgs {
   int stage = 0;
   double dt = 0.0;
   int swm = 0, active = 0;
+  int upw1 = 0;  // tracer advection: 0 "trsk" (centred), 1 "upw1" (upwind)
   const double *u_in = nullptr, *h_in = nullptr, *tend_u = nullptr, *tend_h = nullptr,
                *h_ed = nullptr;
   double *yn_u = nullptr, *acc_u = nullptr, *u_out = nullptr;

@@ -35,21 +35,24 @@ __device__ __forceinline__ double rk_stage(int stage, double k, double yn, doubl
 __device__ __forceinline__ double fmax0(double x) { return (0.0 < x) ? x : 0.0; }
 __device__ __forceinline__ double fminq(double a, double b) { return (b < a) ? b : a; }
 
-// Edges: u q_e for every advanced tracer (scalar_hx2ed + scalar_elem_product,
-// divhx with advmtd = "trsk"); with the shallow-water terms on, the thermal
-// momentum source (source, moist_swm.f90:1299-1315) added to the momentum
-// tendency and u's RK stage.
+// Edges: u q_e for every advanced tracer with advmtd = "trsk" (scalar_hx2ed
+// + scalar_elem_product, divhx; "upw1" forms its fluxes in the cell
+// kernel); with the shallow-water terms on, the thermal momentum source
+// (source, moist_swm.f90:1299-1315) added to the momentum tendency and u's
+// RK stage.
 __global__ void __launch_bounds__(256) k_moist_edge(DevMesh M, MoistArgs A) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const int ne = M.ne;
   if (e >= ne) return;
   const int v1 = M.e_v[e], v2 = M.e_v[ne + e];
   const double ue = A.u_in[e];
+  if (!A.upw1) {
 #pragma unroll
-  for (int k = 0; k < 5; ++k) {
-    if (!((A.active >> k) & 1)) continue;
-    const double qe = (A.q_in[k][v1] + A.q_in[k][v2]) * 0.5;
-    A.uphi[static_cast<size_t>(k) * ne + e] = ue * qe;
+    for (int k = 0; k < 5; ++k) {
+      if (!((A.active >> k) & 1)) continue;
+      const double qe = (A.q_in[k][v1] + A.q_in[k][v2]) * 0.5;
+      A.uphi[static_cast<size_t>(k) * ne + e] = ue * qe;
+    }
   }
   if (!A.swm) return;
   const double l = M.e_leng[e], erad = M.erad, grav = M.grav;
@@ -69,7 +72,8 @@ __global__ void __launch_bounds__(256) k_moist_edge(DevMesh M, MoistArgs A) {
   A.u_out[e] = rk_stage(A.stage, momeq, A.yn_u[e], A.acc_u + e, A.dt);
 }
 
-// Cells: the divergence of each advected tracer's flux (div_hx), the
+// Cells: the divergence of each advected tracer's flux (div_hx, or
+// div_hx_upw1 with the upwind fluxes formed here), the
 // condensation, evaporation and precipitation sources (source, :1317-1351)
 // and the RK stages of h and the tracers.
 __global__ void __launch_bounds__(256) k_moist_cell(DevMesh M, MoistArgs A) {
@@ -99,9 +103,24 @@ __global__ void __launch_bounds__(256) k_moist_cell(DevMesh M, MoistArgs A) {
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     if (!((A.active >> k) & 1)) continue;
-    const double *uphi = A.uphi + static_cast<size_t>(k) * ne;
     double d = 0.0;
-    for (int j = 0; j < n; ++j) d = d + uphi[M.c_ed[j * nv + i]] * M.c_sd[j * nv + i];
+    if (A.upw1) {
+      // div_hx_upw1: c_sd = ttgout l_e, so (u c_sd) q is the reference's
+      // ((ttgout u) l_e) q bit for bit; the cell's own value where the
+      // flux leaves it (ttgout u > 0), the neighbour's where it enters
+      for (int j = 0; j < n; ++j) {
+        const int e = M.c_ed[j * nv + i];
+        const double sd = M.c_sd[j * nv + i], ue = A.u_in[e];
+        const double out = sd > 0.0 ? ue : -ue;
+        // the neighbour across slot j: the other end of edge e (mesh%v(i)%nb(j))
+        const int a = M.e_v[e], b = M.e_v[ne + e];
+        const double qu = out > 0.0 ? A.q_in[k][i] : A.q_in[k][a == i ? b : a];
+        d = d + ue * sd * qu;
+      }
+    } else {
+      const double *uphi = A.uphi + static_cast<size_t>(k) * ne;
+      for (int j = 0; j < n; ++j) d = d + uphi[M.c_ed[j * nv + i]] * M.c_sd[j * nv + i];
+    }
     double t = -(d / A_i / erad);
     if (A.swm && k < 4) t = t + hs[k];
     A.q_out[k][i] = rk_stage(A.stage, t, A.q_yn[k][i], A.q_acc[k] + i, A.dt);

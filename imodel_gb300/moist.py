@@ -3,7 +3,8 @@
 Beside h and u the model carries five cell tracers in flux form -- h theta
 (potential temperature), h qv, h qc, h qr (vapour, cloud, rain) and a
 passive h tracer -- advected by the same C-grid flux as the mass equation
-(advmtd = "trsk": div_hx(u * scalar_hx2ed(q)), highorder.f90:4901-4983), and
+(advmtd = "trsk": div_hx(u * scalar_hx2ed(q)), highorder.f90:4901-4983) or
+by first-order upwind fluxes (advmtd = "upw1", :5094-5139), and
 the sources of moist_swm.f90:1278-1353: a thermal momentum source
 g/2 grad(h^2 theta) / h_e + g theta_e grad(b) added to the shallow-water
 momentum tendency, and condensation, evaporation and precipitation between
@@ -12,8 +13,8 @@ the water species.  Time stepping is the model's classic RK4
 initial value (the RK4 path never updates it), and qv, qc, qr are hq / h
 after each step.
 
-``moist_fields`` restates the initial states of test cases 1-3
-(initialize_moist_swm_fields, moist_swm.f90:643-958).  ``Moist`` is the GPU
+``moist_fields`` restates the initial states of test cases 1-5
+(initialize_moist_swm_fields, moist_swm.f90:643-1139).  ``Moist`` is the GPU
 handle (include/imodel_moist.h): FP64, the reference's operation order.
 """
 from __future__ import annotations
@@ -62,8 +63,10 @@ def _tracer(grid: Grid):
 
 def moist_fields(grid: Grid, testcase: int) -> dict:
     """Initial fields of moist test case 1 (tracer advection by solid-body
-    rotation), 2 (a steady balanced moist flow) or 3 (moist flow over a
-    cone): h, u, bt, theta, qv, qc, qr, the flux-form tracers and q0."""
+    rotation), 2 (a steady balanced moist flow), 3 (moist flow over a
+    cone), 4 or 5 (the moist Galewsky jet, northern or southern
+    hemisphere): h, u, bt, theta, qv, qc, qr, the flux-form tracers and
+    q0."""
     nv = grid.nv
     lon = grid.v_lon
     lat = grid.v_lat
@@ -117,14 +120,40 @@ def moist_fields(grid: Grid, testcase: int) -> dict:
         u = _edge_u(grid, ut, vt)
         q0 = 0.02 / qv.max()
         del h0, xsi
+    elif testcase in (4, 5):
+        # the moist Galewsky jet (moist_swm.f90:955-1130): the barotropic jet
+        # and its tabulated balanced height of swm.f90's cases 22 (jet
+        # between pi/7 and 5 pi/14, case 4) and 52 (between 5 and 45 degrees
+        # south, case 5), a 120 m bump centred 0.93 pi east (case 4: 120
+        # degrees less) at latitude pi/4 (case 4) or -25 degrees (case 5),
+        # theta quadratic in latitude and qv at 98 % of saturation
+        from .testcases import galewsky
+        mu1, mu2 = 0.00002, 0.98
+        theta_sp, theta_eq, theta_np = -40.0 / 300.0, 30.0 / 300.0, -20.0 / 300.0
+        h, u, bt = galewsky(grid, 22 if testcase == 4 else 52)
+        hpert, alpha, beta = 120.0, 1.0 / 3.0, 1.0 / 15.0
+        lat2 = 0.5 * PIO2 if testcase == 4 else -25.0 * DEG2RAD
+        l1 = lon - 0.93 * PI
+        if testcase == 4:
+            l1 = l1 + 120.0 * DEG2RAD
+        e1 = np.exp(-(l1 / alpha) ** 2)
+        e2 = np.exp(-((lat2 - lat) / beta) ** 2)
+        h = h + hpert * np.cos(lat) * e1 * e2
+        theta = theta_sp * lat * (lat + PIO2) - (1.0 - mu1) * theta_eq * (lat + PIO2) * (lat - PIO2) \
+            + theta_np * lat * (lat - PIO2)
+        qv = mu2 * qsat(theta, h, bt, 1.0)
+        qc, qr = z.copy(), z.copy()
+        q0 = 0.02 / qv.max()
     else:
-        raise ValueError("moist test cases built: 1, 2, 3")
+        raise ValueError("moist test cases built: 1, 2, 3, 4, 5")
     # h qv is formed before the q0 scaling, then both are scaled
     hqv = h * qv
     if testcase >= 2:
         qv = q0 * qv
         hqv = q0 * hqv
-    tracer = _tracer(grid)
+    # cases 4 and 5 set no tracer (the reference leaves h tracer as
+    # allocated; neither case advects it)
+    tracer = _tracer(grid) if testcase <= 3 else z.copy()
     return {"h": h, "u": u, "bt": bt, "theta": theta, "qv": qv, "qc": qc, "qr": qr, "q0": q0,
             "htheta": h * theta, "hqv": hqv, "hqc": h * qc, "hqr": h * qr,
             "htracer": tracer * h, "tracer": tracer}
@@ -132,9 +161,14 @@ def moist_fields(grid: Grid, testcase: int) -> dict:
 
 class Moist:
     """The moist shallow-water model on the GPU (include/imodel_moist.h):
-    one grid, one test case, FP64 in the reference's operation order."""
+    one grid, one test case, FP64 in the reference's operation order; the
+    tracers advected with advmtd "trsk" (centred) or "upw1" (first-order
+    upwind, highorder.f90:5094-5139)."""
 
-    def __init__(self, grid: Grid, testcase: int, fields: dict, device: int = 0):
+    ADVECTION = {"trsk": 0, "upw1": 1}
+
+    def __init__(self, grid: Grid, testcase: int, fields: dict, device: int = 0,
+                 advection: str = "trsk"):
         self.grid = grid
         self.lib = _capi.swm_lib()
         self._mesh = grid.c_struct()
@@ -146,6 +180,9 @@ class Moist:
         o.theta = _capi.as_f64p(self._theta)
         o.q0 = float(fields["q0"])
         o.device = device
+        if advection not in self.ADVECTION:
+            raise ValueError(f"advection {advection!r}: built are {sorted(self.ADVECTION)}")
+        o.advection = self.ADVECTION[advection]
         self._handle = ctypes.c_void_p()
         rc = self.lib.imodel_moist_create(ctypes.byref(self._mesh), ctypes.byref(o),
                                           ctypes.byref(self._handle))

@@ -34,6 +34,9 @@ typedef struct imodel_moist_opts {
                           (the reference's RK4 path keeps its initial value)*/
   double q0;           /* saturation scale of the test case               */
   int32_t device;      /* CUDA device ordinal                             */
+  int32_t advection;   /* advmtd of the tracers: 0 = "trsk" (centred,
+                          divhx, highorder.f90:4967-4974), 1 = "upw1"
+                          (first-order upwind, div_hx_upw1, :5094-5139)   */
 } imodel_moist_opts;
 
 int imodel_moist_create(const imodel_swm_mesh *m, const imodel_moist_opts *o, void **handle);

@@ -71,6 +71,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_moist_destroy.argtypes = [vp]
         L.oracle_moist_destroy.restype = None
         L.oracle_moist_set_q.argtypes = [vp, f64p, f64p, f64p]
+        L.oracle_moist_set_advection.argtypes = [vp, ctypes.c_int32]
         L.oracle_moist_run.argtypes = [vp, ctypes.POINTER(f64p), ctypes.c_double, ctypes.c_int32]
         L.oracle_set_diffusion_fields.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
         _lib = L
@@ -206,13 +207,16 @@ def tc2(grid):
 
 
 class MoistOracle:
-    """The reference's moist shallow-water model (moist_swm.f90, advmtd =
-    "trsk", RK4) on the CPU, for one grid and test case; fields as in
+    """The reference's moist shallow-water model (moist_swm.f90, RK4, advmtd
+    "trsk" or "upw1") on the CPU, for one grid and test case; fields as in
     imodel_gb300.moist.moist_fields."""
 
     FIELDS = ("h", "u", "htheta", "hqv", "hqc", "hqr", "htracer")
 
-    def __init__(self, grid, testcase: int, fields: dict, nthreads: int = 0):
+    ADVECTION = {"trsk": 0, "upw1": 1}
+
+    def __init__(self, grid, testcase: int, fields: dict, nthreads: int = 0,
+                 advection: str = "trsk"):
         self.grid = grid
         self._mesh = grid.c_struct()
         self._bt = np.ascontiguousarray(fields["bt"], dtype=np.float64)
@@ -224,6 +228,11 @@ class MoistOracle:
             raise ValueError("moist test case must be 1..5")
         q = [np.ascontiguousarray(fields[k], dtype=np.float64) for k in ("qv", "qc", "qr")]
         lib().oracle_moist_set_q(self._h, _p(q[0]), _p(q[1]), _p(q[2]))
+        if advection not in self.ADVECTION or \
+                lib().oracle_moist_set_advection(self._h, self.ADVECTION[advection]):
+            lib().oracle_moist_destroy(self._h)
+            self._h = None
+            raise ValueError(f"advection {advection!r}: built are {sorted(self.ADVECTION)}")
 
     def __del__(self):
         if getattr(self, "_h", None):

@@ -1061,6 +1061,7 @@ int oracle_field(void *p, int32_t which, double *out) {
 struct MoistOracle {
   Oracle *base;
   int testcase;
+  int upw1 = 0;  // advmtd: 0 = "trsk", 1 = "upw1"
   double q0, dt;
   std::vector<double> theta, qv, qc, qr;
   std::vector<double> f[7][4];          // tendencies of the 7 fields per stage
@@ -1072,9 +1073,30 @@ namespace {
 constexpr double kLscale = 10.0, kGammaR = 0.001, kQprecip = 0.0001;
 
 // tendency_advection (highorder.f90:3936-3972) with advmtd = "trsk"
+// (divhx, :4967-4974: scalar_hx2ed, scalar_elem_product, div_hx) or "upw1"
+// (div_hx_upw1, :5094-5139: the first-order upwind flux, the cell's own
+// value where the flux leaves it, the neighbour's where it enters)
 void advection(MoistOracle &mo, const double *q, const double *u, double *phif) {
   const imodel_swm_mesh &m = mo.base->m;
   const int nv = m.nv, ne = m.ne, nth = mo.base->nthreads;
+  if (mo.upw1) {
+#pragma omp parallel for schedule(static) num_threads(nth)
+    for (int i = 0; i < nv; ++i) {
+      double d = 0.0;
+      for (int j = 0; j < m.nnb[i]; ++j) {
+        const int l = m.v_ed[I6(i, j)] - 1;
+        const int k = m.v_nb[I6(i, j)] - 1;
+        const double signcor = static_cast<double>(m.hx_ttgout[I6(i, j)]);
+        if (signcor * u[l] > 0.0)
+          d = d + signcor * u[l] * m.edhx_leng[l] * q[i];
+        else
+          d = d + signcor * u[l] * m.edhx_leng[l] * q[k];
+      }
+      d = d / m.hx_areag[i] / m.erad;
+      phif[i] = -d;
+    }
+    return;
+  }
 #pragma omp parallel for schedule(static) num_threads(nth)
   for (int l = 0; l < ne; ++l) {
     const double qe = (q[m.ed_v[2 * l] - 1] + q[m.ed_v[2 * l + 1] - 1]) * 0.5;
@@ -1157,6 +1179,12 @@ int moist_tendency(MoistOracle &mo, const double *const in[7], double *const out
 }  // namespace
 
 extern "C" {
+
+int oracle_moist_set_advection(void *h, int32_t upw1) {
+  if (!h || (upw1 != 0 && upw1 != 1)) return 1;
+  static_cast<MoistOracle *>(h)->upw1 = upw1;
+  return 0;
+}
 
 void *oracle_moist_create(const imodel_swm_mesh *m, int32_t testcase, const double *bt,
                           const double *theta, double q0, int32_t nthreads) {

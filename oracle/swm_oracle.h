@@ -60,6 +60,8 @@ void *oracle_moist_create(const imodel_swm_mesh *m, int32_t testcase, const doub
                           const double *theta, double q0, int32_t nthreads);
 void oracle_moist_destroy(void *o);
 int oracle_moist_set_q(void *o, const double *qv, const double *qc, const double *qr);
+/* advmtd of the tracer advection: 0 = "trsk" (the default), 1 = "upw1" */
+int oracle_moist_set_advection(void *o, int32_t upw1);
 /* y = {h[nv], u[ne], htheta, hqv, hqc, hqr, htracer [nv]}, advanced in place */
 int oracle_moist_run(void *o, double *const y[7], double dt, int32_t nsteps);
 

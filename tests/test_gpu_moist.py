@@ -11,18 +11,20 @@ from imodel_gb300.swm import SWMError
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("case,level,dt,n", [(1, 4, 1800.0, 48), (2, 4, 900.0, 48),
-                                            (3, 4, 600.0, 48), (3, 5, 300.0, 24)])
-def test_fp64_equals_oracle(grid_at, case, level, dt, n):
+@pytest.mark.parametrize("case,level,dt,n,adv", [
+    (1, 4, 1800.0, 48, "trsk"), (2, 4, 900.0, 48, "trsk"), (3, 4, 600.0, 48, "trsk"),
+    (3, 5, 300.0, 24, "trsk"), (4, 4, 600.0, 48, "trsk"), (5, 5, 300.0, 24, "trsk"),
+    (1, 4, 1800.0, 48, "upw1"), (3, 4, 600.0, 48, "upw1"), (4, 5, 300.0, 24, "upw1")])
+def test_fp64_equals_oracle(grid_at, case, level, dt, n, adv):
     g = grid_at(level)
     f = moist.moist_fields(g, case)
-    m = moist.Moist(g, case, f)
+    m = moist.Moist(g, case, f, advection=adv)
     m.set_state(f)
     m.advance(dt, n // 2)
     m.advance(dt, n - n // 2)
     s = m.get_state()
     m.close()
-    r = oracle.MoistOracle(g, case, f).run(f, dt, n)
+    r = oracle.MoistOracle(g, case, f, advection=adv).run(f, dt, n)
     for k in moist.FIELDS:
         assert np.array_equal(s[k], r[k]), (k, np.max(np.abs(s[k] - r[k])))
 
@@ -42,3 +44,15 @@ def test_call_order_and_arguments(grid_at):
     with pytest.raises(SWMError) as e:
         moist.Moist(g, 9, f)
     assert e.value.code == _capi.EINVAL
+    # an advection method that is not built is refused at create
+    import ctypes
+    o = _capi.MoistOpts()
+    o.testcase = 1
+    th = np.zeros(g.nv)
+    o.theta = _capi.as_f64p(th)
+    o.advection = 5
+    h = ctypes.c_void_p()
+    lib = _capi.swm_lib()
+    assert lib.imodel_moist_create(ctypes.byref(g.c_struct()), ctypes.byref(o),
+                                   ctypes.byref(h)) == _capi.EINVAL
+    lib.imodel_moist_destroy(h)

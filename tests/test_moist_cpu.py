@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import oracle
-from imodel_gb300 import moist
+from imodel_gb300 import moist, testcases
 
 
 def _rel(a, b, w):
@@ -37,7 +37,7 @@ def test_case2_steady_state_converges(grid_at):
     assert errs[2] < 5e-4
 
 
-@pytest.mark.parametrize("case", [2, 3])
+@pytest.mark.parametrize("case", [2, 3, 4, 5])
 def test_water_mass_and_tracer_are_conserved(grid_at, case):
     g = grid_at(4)
     f = moist.moist_fields(g, case)
@@ -47,8 +47,8 @@ def test_water_mass_and_tracer_are_conserved(grid_at, case):
     assert abs(water(s) / water(f) - 1.0) < 1e-14
     assert abs(np.sum(w * s["h"]) / np.sum(w * f["h"]) - 1.0) < 1e-14
     assert np.sum(w * s["hqc"]) > 0.0            # cloud formed from the vapour
-    if case == 3:
-        assert np.array_equal(s["htracer"], f["htracer"])   # not advected in case 3
+    if case >= 3:
+        assert np.array_equal(s["htracer"], f["htracer"])   # not advected in cases 3-5
 
 
 def test_initial_states(grid_at):
@@ -64,5 +64,36 @@ def test_initial_states(grid_at):
     # the cone stands at (120, 30) degrees
     assert abs(np.degrees(g.v_lon[k]) - 120.0) < 8.0 and abs(np.degrees(g.v_lat[k]) - 30.0) < 8.0
     assert abs(f3["qv"].max() - 0.02) < 1e-15
+    for case, base, lat2, lonc in ((4, 22, 45.0, 167.4 - 120.0), (5, 52, -25.0, 167.4)):
+        f = moist.moist_fields(g, case)
+        h0, u0, _ = testcases.galewsky(g, base)
+        assert np.array_equal(f["u"], u0)              # the barotropic jet
+        bump = f["h"] - h0                   # the 120 m cos(lat) bump, where stated
+        k = int(np.argmax(bump))
+        peak = 120.0 * np.cos(np.radians(lat2))
+        assert 0.85 * peak < bump[k] <= peak
+        assert abs(np.degrees(g.v_lat[k]) - lat2) < 6.0
+        assert abs(np.degrees(g.v_lon[k]) - lonc) < 8.0
+        assert abs(f["qv"].max() - 0.02) < 1e-15
+        np.testing.assert_allclose(f["qv"], moist.qsat(f["theta"], f["h"], 0.0, 0.98 * f["q0"]),
+                                   rtol=1e-14)
     with pytest.raises(ValueError):
         moist.moist_fields(g, 7)
+
+
+def test_upwind_advection_is_positive_and_conservative(grid_at):
+    """advmtd = "upw1" (div_hx_upw1, highorder.f90:5094-5139): the upwind
+    flux keeps case 1's tracer positive where the centred scheme undershoots,
+    spreads it more, and conserves it to round-off, as a flux form must."""
+    g = grid_at(4)
+    f = moist.moist_fields(g, 1)
+    w = g.hx_areag
+    out = {}
+    for adv in ("trsk", "upw1"):
+        s = oracle.MoistOracle(g, 1, f, advection=adv).run(f, 1800.0, 96)
+        out[adv] = s["htracer"] / s["h"]
+        assert abs(np.sum(w * s["htracer"]) / np.sum(w * f["htracer"]) - 1.0) < 1e-14
+    assert out["trsk"].min() < -1e-3 < 0.0 <= out["upw1"].min()
+    assert out["upw1"].max() < 0.8 * out["trsk"].max()
+    with pytest.raises(ValueError):
+        oracle.MoistOracle(g, 1, f, advection="og4")
