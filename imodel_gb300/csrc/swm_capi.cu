@@ -602,8 +602,6 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
   const int scheme = o ? o->scheme : IMODEL_SWM_TRSK10;
   if (scheme < IMODEL_SWM_TRSK10 || scheme > IMODEL_SWM_DTRED)
     return set_error(H, IMODEL_SWM_EINVAL, "unknown scheme");
-  if (scheme != IMODEL_SWM_TRSK10 && H->precision != IMODEL_SWM_FP64)
-    return set_error(H, IMODEL_SWM_EINVAL, "the pxt16, gass18 and dtred schemes run on FP64 handles");
   const int fsphere = o ? o->fsphere : 0;
   const double fcte = o ? o->fcte : 0.0;
   if (fsphere != 0 && fsphere != 2)
@@ -613,8 +611,8 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
   if (lmode < 0 || lmode > 2)
     return set_error(H, IMODEL_SWM_EINVAL,
                      "learned must be 0, 1 (per-step network) or 2 (learned weights)");
-  if (lmode == 2 && scheme != IMODEL_SWM_TRSK10)
-    return set_error(H, IMODEL_SWM_EINVAL, "the learned weights correct trsk10 only");
+  if (lmode != 0 && scheme != IMODEL_SWM_TRSK10)
+    return set_error(H, IMODEL_SWM_EINVAL, "the learned corrections are built on trsk10 only");
   imodel_swm_mesh mk{};
   const imodel_swm_mesh *mesh = m;
   if (lmode == 2) {
@@ -715,6 +713,9 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
       (rc = upload(H, L.t_edarea, &M.t_edarea)) || (rc = upload(H, L.e_nr, &M.e_nr)) ||
       (rc = upload(H, L.e_stq, &M.e_stq)))
     return rc;
+  if (H->precision == IMODEL_SWM_FP32 &&
+      ((rc = upload(H, L.e_qw32, &M.e_qw32)) || (rc = upload(H, L.e_dtc32, &M.e_dtc32))))
+    return rc;
   if (H->precision == IMODEL_SWM_FP32 && !L.t_apw32.empty()) {
     if ((rc = upload(H, L.t_apw32, &M.t_apw32)) || (rc = upload(H, L.t_cc32, &M.t_cc32)) ||
         (rc = upload(H, L.c_apw32, &M.c_apw32)) || (rc = upload(H, L.c_p32, &M.c_p32)))
@@ -757,6 +758,10 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
     if ((rc = alloc_work(H, H->W32))) return rc;
     H->W32.h_ref = keep;
     if ((rc = dalloc(H, &H->W32.zflux, static_cast<size_t>(kMaxNb) * L.nv))) return rc;
+    // the method wrappers run in the generic FP32 kernels (variant 0)
+    H->W32.scheme = scheme;
+    if (scheme != IMODEL_SWM_TRSK10) H->W32.tune.variant = 0;
+    if (scheme == IMODEL_SWM_GASS18 && (rc = dalloc(H, &H->W32.h_trs, L.nt))) return rc;
     if (o && o->learned == 1 && (rc = setup_learned(H, m, L, o))) return rc;
   }
   if (H->learned_mode == 2) {
@@ -1182,9 +1187,11 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
   const int sizes[3] = {128, 256, 512};
   imodel::Tune best;
   float best_ms = 1e30f;
-  // the learned correction is wired into the cell-centred variants only
-  // and APVM into the edge pre-pass of variant 0
-  for (int v = H->learned_mode == 1 ? 1 : 0; v <= (H->W32.apvm.on ? 0 : 2); ++v)
+  // the learned correction is wired into the cell-centred variants only,
+  // APVM into the edge pre-pass of variant 0 and the method wrappers into
+  // the variant-0 kernels
+  const bool v0_only = H->W32.apvm.on || H->W32.scheme != IMODEL_SWM_TRSK10;
+  for (int v = H->learned_mode == 1 ? 1 : 0; v <= (v0_only ? 0 : 2); ++v)
     for (int b : sizes) {
       imodel::Tune t;
       t.variant = v;
@@ -1261,6 +1268,8 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[6]) {
                              "the learned correction runs with the cell-centred variants (1, 2) only");
   if (H->W32.apvm.on && choice[0] != 0)
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "apvm runs with variant 0 only");
+  if (H->W32.scheme != IMODEL_SWM_TRSK10 && choice[0] != 0)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "pxt16, gass18 and dtred run with variant 0 only");
   imodel::Tune t;
   t.variant = choice[0];
   t.bs_tri = choice[1];

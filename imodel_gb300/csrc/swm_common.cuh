@@ -57,6 +57,9 @@ struct DevMesh {
   // [3][ne]
   const double *t_bary, *e_dist, *t_edarea, *e_nr;
   const int32_t *e_stq;
+  // their FP32 coefficients (swm_layout.h): q_e weights [2][ne] (pxt16,
+  // gass18), dtred's PV-flux coefficients [6][ne]
+  const float *e_qw32, *e_dtc32;
 };
 
 // Launch configuration of the FP32 stage kernels, chosen by the autotuner.

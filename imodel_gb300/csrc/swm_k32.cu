@@ -5,6 +5,7 @@
 // coefficient computed in FP64 and rounded once, and the thickness stored as
 // a deviation from a constant reference depth h_ref so that the FP32 state
 // keeps ~1e-5 m resolution on ~3 km deep layers.
+#include "imodel_swm.h"
 #include "swm_k32_body.cuh"
 
 namespace imodel {
@@ -16,13 +17,17 @@ __global__ void __launch_bounds__(512) k_tri32(DevMesh M, const float *__restric
                                                float *__restrict__ q_tr, float h_ref,
                                                int pv_on, int *flags,
                                                const float *__restrict__ kt,
-                                               float *__restrict__ coefvort) {
+                                               float *__restrict__ coefvort,
+                                               float *__restrict__ ht_out) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= M.nt) return;
-  tri_body(M, t, OneRun{}, hd, u, q_tr, h_ref, pv_on, flags, kt, coefvort);
+  tri_body(M, t, OneRun{}, hd, u, q_tr, h_ref, pv_on, flags, kt, coefvort, ht_out);
 }
 
-// h_e (deviation), flux F_e = u_e (h_ref + h_e), q_e
+// h_e (deviation), flux F_e = u_e (h_ref + h_e), q_e: the TRSK average
+// (scalar_tr2ed), the circumcentre-distance weights of pxt16 (qw) or
+// gass18's rhombus PV (qw and the triangle depths ht: (w1 eta1 + w2 eta2) /
+// (w1 h1 + w2 h2), eta = q h, with scalar_elem_divide's guard)
 __global__ void __launch_bounds__(512) k_edge_pre32(DevMesh M, const float *__restrict__ hd,
                                                     const float *__restrict__ u,
                                                     const float *__restrict__ q_tr,
@@ -31,7 +36,10 @@ __global__ void __launch_bounds__(512) k_edge_pre32(DevMesh M, const float *__re
                                                     float *__restrict__ q_ed, float h_ref,
                                                     const float *__restrict__ qg,
                                                     const float *__restrict__ vhx,
-                                                    float coef) {
+                                                    float coef,
+                                                    const float *__restrict__ qw,
+                                                    const float *__restrict__ ht, int pv_on,
+                                                    int *flags) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const int ne = M.ne;
   if (e >= ne) return;
@@ -40,7 +48,23 @@ __global__ void __launch_bounds__(512) k_edge_pre32(DevMesh M, const float *__re
   h_ed[e] = he;
   uh[e] = u[e] * (h_ref + he);
   const int t1 = __ldg(&M.e_sh[e]), t2 = __ldg(&M.e_sh[ne + e]);
-  float q = 0.5f * (q_tr[t1] + q_tr[t2]);
+  float q;
+  if (!qw) {
+    q = 0.5f * (q_tr[t1] + q_tr[t2]);
+  } else if (!ht) {
+    q = __ldg(&qw[e]) * q_tr[t1] + __ldg(&qw[ne + e]) * q_tr[t2];
+  } else {
+    const float w1 = __ldg(&qw[e]), w2 = __ldg(&qw[ne + e]);
+    const float h1 = ht[t1], h2 = ht[t2];
+    const float hr = w1 * h1 + w2 * h2;
+    q = 0.0f;
+    if (pv_on) {
+      if (fabsf(hr) < 1.1920928955078125e-12f)
+        atomicOr(flags, 1);
+      else
+        q = (w1 * q_tr[t1] * h1 + w2 * q_tr[t2] * h2) / hr;
+    }
+  }
   if (qg) {
     // apvm (swm_operators.f90:1495-1502), coef = pvspar dt
     const int nt = M.nt, nv = M.nv;
@@ -114,17 +138,31 @@ __global__ void __launch_bounds__(512) k_cell32(DevMesh M, const float *__restri
                                                 float *__restrict__ acc,
                                                 float *__restrict__ yout,
                                                 float *__restrict__ tend, int stage, float dt,
-                                                float grav) {
+                                                float grav, int perot) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int nv = M.nv;
   if (i >= nv) return;
   const int n = M.c_nnb[i];
   float d = 0.0f, k = 0.0f;
+  float v[3] = {0.0f, 0.0f, 0.0f};
   for (int j = 0; j < n; ++j) {
     const int e = __ldg(&M.c_ed[j * nv + i]);
     const float ue = u[e];
     d += __ldg(&M.c_div32[j * nv + i]) * uh[e];
-    k += __ldg(&M.c_kew32[j * nv + i]) * (ue * ue);
+    if (perot) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) v[c] = fmaf(ue, __ldg(&M.c_apw32[(3 * j + c) * nv + i]), v[c]);
+    } else {
+      k += __ldg(&M.c_kew32[j * nv + i]) * (ue * ue);
+    }
+  }
+  if (perot) {
+    // kinetic_energy_hx, perhx branch (pxt16): half the squared Perot
+    // velocity of the cell (vector_edhx2hx_perot), on the tangent plane
+    const float p0 = __ldg(&M.c_p32[i]), p1 = __ldg(&M.c_p32[nv + i]), p2 = __ldg(&M.c_p32[2 * nv + i]);
+    const float vp = v[0] * p0 + v[1] * p1 + v[2] * p2;
+    const float a0 = v[0] - vp * p0, a1 = v[1] - vp * p1, a2 = v[2] - vp * p2;
+    k = 0.5f * (a0 * a0 + a1 * a1 + a2 * a2);
   }
   bern[i] = grav * (hd[i] + __ldg(&M.c_bt32[i])) + k;
   const float masseq = -d;
@@ -143,17 +181,38 @@ __global__ void __launch_bounds__(512) k_edge32(DevMesh M, const float *__restri
                                                 float *__restrict__ yout,
                                                 float *__restrict__ tend, int stage, float dt,
                                                 int mom_on, const float *__restrict__ dif1,
-                                                const float *__restrict__ dif2) {
+                                                const float *__restrict__ dif2,
+                                                const int32_t *__restrict__ stq,
+                                                const float *__restrict__ q_tr, int dtred) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const int ne = M.ne;
   if (e >= ne) return;
   const float g = (bern[__ldg(&M.e_v[ne + e])] - bern[__ldg(&M.e_v[e])]) * __ldg(&M.e_grad32[e]);
-  const float qe = q_ed[e];
-  const int ns = M.e_nst[e];
   float q = 0.0f;
-  for (int s = 0; s < ns; ++s) {
-    const int k = __ldg(&M.e_stk[s * ne + e]);
-    q += __ldg(&M.e_stc32[s * ne + e]) * uh[k] * (qe + q_ed[k]);
+  if (dtred) {
+    // coriolis_ed's dtred branch: the Perot reconstructions of F q at the
+    // edge's two triangles, as six coefficients on their edges' fluxes
+    const int nt = M.nt;
+#pragma unroll
+    for (int si = 0; si < 2; ++si) {
+      const int t = __ldg(&M.e_sh[si * ne + e]);
+      float a = 0.0f;
+#pragma unroll
+      for (int s = 0; s < 3; ++s)
+        a += __ldg(&M.e_dtc32[(3 * si + s) * ne + e]) * uh[__ldg(&M.t_ed[s * nt + t])];
+      q += q_tr[t] * a;
+    }
+  } else {
+    // TRSK (trsk10, dtred's q_e aside), pered as coefficients on the same
+    // stencil (pxt16), or with gass18's connecting-edge PV (stq)
+    const float qe = q_ed[e];
+    const int ns = M.e_nst[e];
+    for (int s = 0; s < ns; ++s) {
+      const int k = __ldg(&M.e_stk[s * ne + e]);
+      const int c3 = stq ? __ldg(&stq[s * ne + e]) : -1;
+      const float qs = c3 >= 0 ? q_ed[c3] + q_ed[c3] : qe + q_ed[k];
+      q += __ldg(&M.e_stc32[s * ne + e]) * uh[k] * qs;
+    }
   }
   float momeq = -g - q;
   if (dif1) momeq += dif1[e];
@@ -337,8 +396,9 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
     k_tri32c<<<nblocks(M.nt, T.bs_tri), T.bs_tri, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ref,
                                                            W.pv_on, W.flags, D.kt, cvort);
   else
-    k_tri32<<<nblocks(M.nt, T.bs_tri), T.bs_tri, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ref,
-                                                          W.pv_on, W.flags, D.kt, cvort);
+    k_tri32<<<nblocks(M.nt, T.bs_tri), T.bs_tri, 0, s>>>(
+        M, h_in, u_in, W.q_tr, W.h_ref, W.pv_on, W.flags, D.kt, cvort,
+        W.scheme == IMODEL_SWM_GASS18 ? W.h_trs : nullptr);
   if (T.variant >= 1) {
     if (ev) cudaEventRecord(ev[1], s);
     // learned correction: formed once per step from the first stage's state
@@ -362,19 +422,22 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
     const int nbt = nblocks(M.nt, 256);
     k_apvm32<<<nbt + nblocks(M.nv, 256), 256, 0, s>>>(M, W.q_tr, u_in, A.qg, A.vhx, nbt);
   }
-  k_edge_pre32<<<nblocks(M.ne, T.bs_pre), T.bs_pre, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ed, W.uh,
-                                                             W.q_ed, W.h_ref,
-                                                             A.on ? A.qg : nullptr, A.vhx,
-                                                             A.coef);
+  // the method wrappers (variant 0 only): pxt16 (distance-weighted q_e,
+  // Perot KE, pered), gass18 (rhombus PV, connecting-edge PV), dtred
+  const int sch = W.scheme;
+  const bool pxt = sch == IMODEL_SWM_PXT16, gass = sch == IMODEL_SWM_GASS18;
+  k_edge_pre32<<<nblocks(M.ne, T.bs_pre), T.bs_pre, 0, s>>>(
+      M, h_in, u_in, W.q_tr, W.h_ed, W.uh, W.q_ed, W.h_ref, A.on ? A.qg : nullptr, A.vhx, A.coef,
+      pxt || gass ? M.e_qw32 : nullptr, gass ? W.h_trs : nullptr, W.pv_on, W.flags);
   if (ev) cudaEventRecord(ev[2], s);
   k_cell32<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(M, h_in, u_in, W.uh, W.bern, W.yn_h,
                                                            W.acc_h, h_out, W.tend_h, stage, dt,
-                                                           grav);
+                                                           grav, pxt ? 1 : 0);
   diffusion_tail();
   if (ev) cudaEventRecord(ev[3], s);
-  k_edge32<<<nblocks(M.ne, T.bs_edge), T.bs_edge, 0, s>>>(M, W.bern, W.uh, W.q_ed, W.yn_u,
-                                                           W.acc_u, u_out, W.tend_u, stage, dt,
-                                                           W.mom_on, dif1, dif2);
+  k_edge32<<<nblocks(M.ne, T.bs_edge), T.bs_edge, 0, s>>>(
+      M, W.bern, W.uh, W.q_ed, W.yn_u, W.acc_u, u_out, W.tend_u, stage, dt, W.mom_on, dif1, dif2,
+      gass ? M.e_stq : nullptr, W.q_tr, sch == IMODEL_SWM_DTRED ? 1 : 0);
   if (ev) cudaEventRecord(ev[4], s);
 }
 

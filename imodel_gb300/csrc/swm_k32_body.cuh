@@ -55,7 +55,8 @@ __device__ __forceinline__ void tri_core(int t, Ix ix, const int (&ed)[3], const
                                          const float *__restrict__ u, float *__restrict__ q_tr,
                                          float h_ref, int pv_on, int *flags,
                                          const float *__restrict__ kt = nullptr,
-                                         float *__restrict__ coefvort = nullptr) {
+                                         float *__restrict__ coefvort = nullptr,
+                                         float *__restrict__ ht_out = nullptr) {
   float eta = f;
   float ht = 0.0f, z = 0.0f;
 #pragma unroll
@@ -68,6 +69,8 @@ __device__ __forceinline__ void tri_core(int t, Ix ix, const int (&ed)[3], const
   // with diffusion on: K_tr times the relative vorticity
   if (coefvort) coefvort[ix(t)] = kt[t] * z;
   ht += h_ref;
+  // gass18: the depth at the triangle for the rhombus PV of the edges
+  if (ht_out) ht_out[ix(t)] = ht;
   float q = 0.0f;
   if (pv_on) {
     // scalar_elem_divide guard, swm_operators.f90:1604-1606
@@ -85,7 +88,8 @@ __device__ __forceinline__ void tri_body(const DevMesh &M, int t, Ix ix,
                                          const float *__restrict__ u, float *__restrict__ q_tr,
                                          float h_ref, int pv_on, int *flags,
                                          const float *__restrict__ kt = nullptr,
-                                         float *__restrict__ coefvort = nullptr) {
+                                         float *__restrict__ coefvort = nullptr,
+                                         float *__restrict__ ht_out = nullptr) {
   // three 16-byte records instead of 12 scalar streams (fewer load
   // instructions in flight per SM)
   const int4 a = __ldg(&M.t_recA[t]), b = __ldg(&M.t_recB[t]);
@@ -94,7 +98,7 @@ __device__ __forceinline__ void tri_body(const DevMesh &M, int t, Ix ix,
   const float circ[3] = {__int_as_float(b.z), __int_as_float(b.w), c.x};
   const float kite[3] = {c.y, c.z, c.w};
   tri_core<Ix, Ld>(t, ix, ed, cv, circ, kite, __ldg(&M.t_f32[t]), hd, u, q_tr, h_ref, pv_on,
-                   flags, kt, coefvort);
+                   flags, kt, coefvort, ht_out);
 }
 
 // the same from 40-byte records with 16-bit indices (single runs): a warp of

@@ -151,6 +151,101 @@ int edge_connection(const imodel_swm_mesh &m, int ed1, int ed2) {
   return -1;
 }
 
+// The FP32 coefficients of the pxt16, gass18 and dtred branches (Layout:
+// t_kite32, e_qw32, e_stc32, e_dtc32), from the FP64 geometry of the same
+// branches, which build_layout has filled in device order before.
+void scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
+  const size_t NV = L.nv, NE = L.ne, NT = L.nt;
+  (void)NV;
+  const int ne = L.ne, nt = L.nt;
+  if (scheme == IMODEL_SWM_PXT16 || scheme == IMODEL_SWM_GASS18) {
+    // the depth at the triangle as weights of its vertices
+    for (int i = 0; i < nt; ++i) {
+      const int t = L.tri_n2o[i];
+      double w[3] = {0.0, 0.0, 0.0};
+      if (scheme == IMODEL_SWM_PXT16) {
+        for (int s = 0; s < 3; ++s) w[s] = L.t_bary[s * NT + i];
+      } else {
+        // sum_s edarea_s (h_a + h_b) / 2 / A over the triangle's edges
+        const double A = m.tr_areag[t];
+        for (int s = 0; s < 3; ++s) {
+          const int e = m.tr_ed[3 * static_cast<size_t>(t) + s] - 1;
+          for (int end = 0; end < 2; ++end) {
+            const int c = m.ed_v[2 * static_cast<size_t>(e) + end] - 1;
+            for (int q = 0; q < 3; ++q)
+              if (m.tr_v[3 * static_cast<size_t>(t) + q] - 1 == c)
+                w[q] += 0.5 * L.t_edarea[s * NT + i] / A;
+          }
+        }
+      }
+      for (int s = 0; s < 3; ++s) L.t_kite32[s * NT + i] = static_cast<float>(w[s]);
+    }
+    // q_e from the edge's two triangles
+    L.e_qw32.assign(2 * NE, 0.0f);
+    for (int i = 0; i < ne; ++i) {
+      double a, b;
+      if (scheme == IMODEL_SWM_PXT16) {
+        a = L.e_dist[NE + i];  // triangle 1 takes the other one's distance
+        b = L.e_dist[i];
+      } else {
+        a = L.t_areag[L.e_sh[i]];
+        b = L.t_areag[L.e_sh[NE + i]];
+      }
+      L.e_qw32[i] = static_cast<float>(a / (a + b));
+      L.e_qw32[NE + i] = static_cast<float>(b / (a + b));
+    }
+  }
+  if (scheme == IMODEL_SWM_PXT16) {
+    // pered on the TRSK stencil's slots, in the order build_layout made them
+    for (int i = 0; i < ne; ++i) {
+      const int e = L.edge_n2o[i];
+      const double *nr = m.ed_nr + 3 * static_cast<size_t>(e);
+      int ns = 0;
+      for (int s = 0; s < 2; ++s) {
+        const int node = m.ed_v[2 * static_cast<size_t>(e) + s] - 1;
+        const int n = m.nnb[node];
+        int own = -1;
+        for (int j = 0; j < n; ++j)
+          if (m.v_ed[6 * static_cast<size_t>(node) + j] - 1 == e) own = j;
+        for (int j = 0; j < n; ++j) {
+          if (j == own) continue;
+          const int k = m.v_ed[6 * static_cast<size_t>(node) + j] - 1;
+          double d = 0.0;
+          for (int c = 0; c < 3; ++c)
+            d += (m.ed_c[3 * static_cast<size_t>(k) + c] - m.v_p[3 * static_cast<size_t>(node) + c]) *
+                 nr[c];
+          const double sg = static_cast<double>(m.hx_ttgout[6 * static_cast<size_t>(node) + j]);
+          L.e_stc32[ns * NE + i] =
+              static_cast<float>(-0.25 * sg * d * m.edhx_leng[k] / m.hx_areag[node]);
+          ++ns;
+        }
+      }
+    }
+  }
+  if (scheme == IMODEL_SWM_DTRED) {
+    L.e_dtc32.assign(6 * NE, 0.0f);
+    for (int i = 0; i < ne; ++i) {
+      const double d1 = L.e_dist[i], d2 = L.e_dist[NE + i];
+      const double w[2] = {d2 / (d1 + d2), d1 / (d1 + d2)};
+      const double nr[3] = {L.e_nr[i], L.e_nr[NE + i], L.e_nr[2 * NE + i]};
+      for (int si = 0; si < 2; ++si) {
+        const int ti = L.e_sh[si * NE + i];
+        const double tc[3] = {L.t_c[ti], L.t_c[NT + ti], L.t_c[2 * NT + ti]};
+        for (int s = 0; s < 3; ++s) {
+          const int ed = L.t_ed[s * NT + ti];
+          const double ec[3] = {L.e_c[ed], L.e_c[NE + ed], L.e_c[2 * NE + ed]};
+          const double cr[3] = {tc[1] * ec[2] - tc[2] * ec[1], tc[2] * ec[0] - tc[0] * ec[2],
+                                tc[0] * ec[1] - tc[1] * ec[0]};
+          const double dn = cr[0] * nr[0] + cr[1] * nr[1] + cr[2] * nr[2];
+          const double sg = L.t_lt[s * NT + ti] < 0.0 ? -1.0 : 1.0;
+          L.e_dtc32[(3 * si + s) * NE + i] =
+              static_cast<float>(-w[si] * sg * L.e_leng[ed] * dn / L.t_areag[ti]);
+        }
+      }
+    }
+  }
+}
+
 }  // namespace
 
 std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, int scheme,
@@ -520,6 +615,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
     L.e_nr.resize(3 * NE);
     for (int i = 0; i < ne; ++i)
       for (int k = 0; k < 3; ++k) L.e_nr[k * NE + i] = m.ed_nr[3 * static_cast<size_t>(L.edge_n2o[i]) + k];
+    scheme_fp32(m, L, scheme);
   }
   L.t_recA.resize(4 * NT);
   L.t_recB.resize(4 * NT);

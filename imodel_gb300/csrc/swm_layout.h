@@ -123,6 +123,23 @@ struct Layout {
   //   e_nr    [3][ne] ed%nr (pered, dtred)
   std::vector<double> t_bary, e_dist, t_edarea, e_nr;
   std::vector<int32_t> e_stq;
+  // ... and their FP32 forms for the FP32 step (variant 0), each constant
+  // factor folded in FP64 and rounded once:
+  //   t_kite32 holds the depth weights of the triangle's vertices instead of
+  //           the kite fractions: tr%c%b (pxt16) or, for gass18, half the
+  //           edge areas of the two triangle edges at the vertex over A
+  //   e_qw32  [2][ne] weights of q_e from the edge's triangles: d2, d1 over
+  //           d1 + d2 (pxt16), a1, a2 over a1 + a2 (gass18, rhombus PV)
+  //   e_stc32 (pxt16) the pered coefficients of the TRSK stencil slots: at
+  //           each of the edge's cells c, -(1/4) ttgout (ed%c%p - v%p) . nr_e
+  //           edhx%leng / hx%areag, so that sum_k c_k F_k (q_e + q_k) is the
+  //           -(v . nr) of coriolis_ed's pered branch (the tangent-plane
+  //           projections drop out: nr_e is normal to the edge midpoint and
+  //           both cells, which also zeroes the edge's own term)
+  //   e_dtc32 [6][ne] (dtred) per triangle i of the edge and its edge slot s,
+  //           -w_i sign(tr%tg) l_s (tr%c x ed(s)%c) . nr_e / tr%areag, w_i =
+  //           d2, d1 over d1 + d2: the PV flux is sum q_i c_is F_s
+  std::vector<float> e_qw32, e_dtc32;
 };
 
 // Builds the layout from a reference mesh; returns "" or an error message.

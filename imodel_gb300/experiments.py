@@ -316,6 +316,49 @@ def exp_williamson(args, pool):
     return out
 
 
+def exp_schemes(args, pool):
+    """The method wrappers on FP64 and FP32 handles: cell-steps/s over
+    args.days (default 0.5) of a seeded balanced state at args.level
+    (default 8; dt 110 s scaled by the grid spacing), and the FP32 state's
+    relative L2 distance from the FP64 one after the run."""
+    from . import fields
+    from .mesh import meshbuild
+    from .swm import SWM
+    lvl = args.level or 8
+    g = meshbuild(lvl)
+    dt = 110.0 * 2.0 ** (8 - lvl)
+    n = swm_steps(args.days or 0.5, dt)
+    h, u = fields.balanced_state(g, lmax=32, seed=0, evaluator=fields.PoolEvaluator(pool))
+    out = {"level": lvl, "dt": dt, "steps": n}
+    for scheme in ("trsk10", "pxt16", "gass18", "dtred"):
+        row = {}
+        r64 = None
+        for prec in ("fp64", "fp32"):
+            m = SWM(g, prec, scheme=scheme)
+            m.set_state(h, u)
+            m.advance(dt, 2)                     # graph capture and warm-up
+            m.set_state(h, u)
+            t0 = time.perf_counter()
+            m.advance(dt, n)
+            hh, uu = m.get_state()
+            sec = time.perf_counter() - t0
+            m.close()
+            row[prec] = {"cell_steps_per_s": g.nv * n / sec, "seconds": sec}
+            if prec == "fp64":
+                r64 = (hh, uu)
+            else:
+                row[prec]["h_vs_fp64"] = rel_errors(hh, r64[0], g.hx_areag)
+                row[prec]["u_vs_fp64"] = rel_errors(uu, r64[1], _edge_w(g))
+        row["fp32_over_fp64"] = row["fp32"]["cell_steps_per_s"] / row["fp64"]["cell_steps_per_s"]
+        out[scheme] = row
+    return out
+
+
+def swm_steps(days, dt):
+    from . import swm
+    return swm.ntime_for(days, dt)
+
+
 def exp_mesh(args, pool):
     """Grid build times through the C ABI (imodel_mesh_build on all host
     threads against imodel_mesh_build_gpu on device 0), levels 8 to
@@ -345,7 +388,7 @@ def exp_mesh(args, pool):
     return out
 
 
-RUNS = {"tc2": exp_tc2, "mesh": exp_mesh, "williamson": exp_williamson, "balanced": exp_balanced, "ensemble": exp_ensemble,
+RUNS = {"tc2": exp_tc2, "mesh": exp_mesh, "schemes": exp_schemes, "williamson": exp_williamson, "balanced": exp_balanced, "ensemble": exp_ensemble,
         "mountains": exp_mountains, "fixed": exp_fixed, "large": exp_large}
 
 

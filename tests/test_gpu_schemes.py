@@ -1,7 +1,8 @@
-"""The pxt16, gass18 and dtred method wrappers on the GPU (FP64 handles)
-against the CPU oracle: tendencies and RK4 runs bit for bit, alone and with
-APVM and diffusion; the options an FP32 handle or a mesh without ed_nr
-cannot take are refused."""
+"""The pxt16, gass18 and dtred method wrappers on the GPU against the CPU
+oracle: FP64 handles bit for bit (tendencies and RK4 runs, alone and with
+APVM and diffusion); FP32 handles (the generic variant-0 kernels with the
+branches' coefficients folded in FP64) within FP32 round-off of the oracle;
+the options such handles or a mesh without ed_nr cannot take are refused."""
 import ctypes
 
 import numpy as np
@@ -14,6 +15,11 @@ from imodel_gb300.swm import SWM, SWMError
 pytestmark = pytest.mark.gpu
 
 SCHEMES = ("pxt16", "gass18", "dtred")
+# FP32 against the FP64 oracle, relative: the tendency (max / max) and a
+# 1.7-day run (L2).  Measured on a GB300: tendencies 9e-7 (mass) and
+# 3e-6 to 5e-6 (momentum), runs h 4e-8, u 6e-7 to 8e-7; bounds about 5-10x
+FP32_TEND = 2e-5
+FP32_RUN_H, FP32_RUN_U = 4e-7, 8e-6
 
 
 @pytest.mark.parametrize("scheme", SCHEMES)
@@ -76,10 +82,79 @@ def test_launch_counts(grid_at):
     assert SWM(g, "fp64", scheme="dtred").launch_count(1) == base + 4
 
 
+def rel_max(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+def rel_l2(a, b, w):
+    return float(np.sqrt(np.sum(w * (a - b) ** 2) / np.sum(w * b * b)))
+
+
+@pytest.mark.parametrize("scheme", SCHEMES)
+@pytest.mark.parametrize("level", [3, 5])
+def test_fp32_tendency_against_the_oracle(grid_at, scheme, level):
+    """Every term of the FP32 branch (depth at the triangles, q_e, the
+    kinetic energy, the PV flux) against the FP64 oracle on an unbalanced
+    state."""
+    g = grid_at(level)
+    h, u = swm.initialize_fields_tc2(g)
+    rng = np.random.default_rng(level + 10)
+    h = h + rng.normal(0, 5.0, g.nv)
+    u = u + rng.normal(0, 2.0, g.ne)
+    m = SWM(g, "fp32", scheme=scheme)
+    mg, ug = m.tendency(h, u)
+    m.close()
+    mr, ur = oracle.Oracle(g, 2, scheme=scheme).tendency(h, u)
+    em, eu = rel_max(mg, mr), rel_max(ug, ur)
+    print(f"{scheme} level {level}: FP32 tendency vs oracle (max / max) mass {em:.1e}, "
+          f"momentum {eu:.1e}")
+    assert em < FP32_TEND and eu < FP32_TEND
+
+
+@pytest.mark.parametrize("scheme", SCHEMES)
+def test_fp32_run_against_the_oracle(grid_at, scheme):
+    """320 RK4 steps (1.7 days) of a seeded balanced state at level 5."""
+    g = grid_at(5)
+    h, u = fields.balanced_state(g, lmax=24, seed=23)
+    m = SWM(g, "fp32", scheme=scheme)
+    assert m.launch_count(1) == 16   # four variant-0 kernels per stage, dtred included
+    m.set_state(h, u)
+    m.advance(450.0, 320)
+    hg, ug = m.get_state()
+    m.close()
+    hr, ur = oracle.Oracle(g, 2, scheme=scheme).run(h, u, 450.0, 320)
+    eh, eu = rel_l2(hg, hr, g.hx_areag), rel_l2(ug, ur, g.ed_leng * g.edhx_leng)
+    dh = rel_l2(hr, h, g.hx_areag)
+    print(f"{scheme}: FP32 vs FP64 oracle after 320 steps h {eh:.1e}, u {eu:.1e} "
+          f"(the flow itself changed h by {dh:.1e})")
+    assert eh < FP32_RUN_H and eu < FP32_RUN_U
+
+
+def test_fp32_with_apvm(grid_at):
+    g = grid_at(4)
+    h, u = fields.balanced_state(g, lmax=12, seed=24)
+    dt = 600.0
+    m = SWM(g, "fp32", scheme="pxt16")
+    m.set_apvm(0.5, dt)
+    hg, ug = m.ode_rk4(h, u, dt, 48)
+    m.close()
+    hr, ur = oracle.Oracle(g, 2, scheme="pxt16", pvspar=0.5, dt=dt).run(h, u, dt, 48)
+    eh, eu = rel_l2(hg, hr, g.hx_areag), rel_l2(ug, ur, g.ed_leng * g.edhx_leng)
+    print(f"pxt16 + apvm: FP32 vs FP64 oracle after 48 steps h {eh:.1e}, u {eu:.1e}")
+    assert eh < FP32_RUN_H and eu < FP32_RUN_U
+
+
 def test_refusals(grid_at):
     g = grid_at(3)
+    # the FP32 branches run in the variant-0 kernels only, and the learned
+    # corrections are built on trsk10
+    m = SWM(g, "fp32", scheme="pxt16")
     with pytest.raises(SWMError) as e:
-        SWM(g, "fp32", scheme="pxt16")
+        m.set_tuning(variant=1)
+    assert e.value.code == _capi.EINVAL
+    m.close()
+    with pytest.raises(SWMError) as e:
+        SWM(g, "fp32", scheme="gass18", learned_params=np.zeros(100, dtype=np.float32))
     assert e.value.code == _capi.EINVAL
     # a mesh without ed_nr cannot feed pered / dtred / the circumcentres
     mesh = _capi.Mesh.from_buffer_copy(g.c_struct())  # the grid's own struct stays intact
