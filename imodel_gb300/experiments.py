@@ -135,7 +135,7 @@ def exp_balanced(args, pool):
     h, u = fields.balanced_state(g, lmax=64, seed=0, evaluator=fields.PoolEvaluator(pool))
     r64 = run(g, "fp64", h, u, dt, n)
     out = {"level": g.level, "dt": dt, "steps": n, "fp64": _summary(r64)}
-    for path in ("fp32", "fp32l"):
+    for path in ("fp32", "fp32w", "fp32l"):
         r = run(g, path, h, u, dt, n, params=_params(args) if path == "fp32l" else None)
         out[path] = dict(_summary(r), h_vs_fp64=rel_errors(r["h"], r64["h"], g.hx_areag),
                          u_vs_fp64=rel_errors(r["u"], r64["u"], _edge_w(g)))
@@ -217,7 +217,7 @@ def exp_mountains(args, pool):
     out = {"coarse": {"level": 8, "dt": dtc, "steps": nc},
            "reference": dict(_summary(ref), level=9, dt=dtf, path="fp64")}
     p = _params(args)
-    for path in ("fp64", "fp32", "fp32l"):
+    for path in ("fp64", "fp32", "fp32w", "fp32l"):
         r = run(gc, path, hc, uc, dtc, nc, bt=btc, params=p)
         # the topography is the same at the shared nodes: depth error =
         # free-surface error
