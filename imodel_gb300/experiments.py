@@ -273,7 +273,7 @@ def exp_large(args, pool):
                                  evaluator=fields.PoolEvaluator(pool))
     r64 = run(g, "fp64", h, u, dt, n, chunk=2000)
     out = {"level": 10, "dt": dt, "steps": n, "fp64": _summary(r64)}
-    for path in ("fp32", "fp32l"):
+    for path in ("fp32", "fp32w", "fp32l"):
         r = run(g, path, h, u, dt, n, params=_params(args) if path == "fp32l" else None)
         out[path] = dict(_summary(r), h_vs_fp64=rel_errors(r["h"], r64["h"], g.hx_areag),
                          u_vs_fp64=rel_errors(r["u"], r64["u"], _edge_w(g)))
