@@ -125,15 +125,17 @@ typedef struct imodel_swm_opts {
   size_t mlp_bytes;
   double drift_bound; /* relative total-energy drift above which the
                          learned correction is switched off (0 = 1e-3); it
-                         is also switched off when max |u| grows by more
-                         than 10 % within one check interval or exceeds 3x
-                         its value when the state was set.  Checked every
-                         32 steps; the interval that failed is stepped
-                         again with the plain scheme                     */
+                         is also switched off when max |u| exceeds 3x its
+                         value when the state was set or, for the per-step
+                         correction (learned = 1), grows by more than 10 %
+                         within one check interval.  Checked every 32
+                         steps; the interval that failed is stepped again
+                         with the plain scheme                           */
   int32_t scheme;     /* IMODEL_SWM_TRSK10 (0) ... IMODEL_SWM_DTRED; the
-                         other wrappers need the mesh's ed_nr and ed_c and
-                         run on FP64 handles (an FP32 handle, the learned
-                         correction or an ensemble takes trsk10 only)   */
+                         other wrappers need the mesh's ed_nr and ed_c;
+                         FP32 handles run them in the variant-0 kernels
+                         (the learned corrections and ensembles take
+                         trsk10 only)                                    */
   int32_t fsphere;    /* Coriolis parameter of vort_tr (swm_operators.f90:
                          551-611): 0 f = 2 Omega sin(lat) at the triangle
                          circumcentres; 2 the constant fcte (f-sphere, test
