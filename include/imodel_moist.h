@@ -2,15 +2,16 @@
  * imodel_moist.h -- C ABI of the moist shallow-water model on the GPU.
  *
  * Replaces the time loop of iModel's moist shallow-water model
- * (moist_swm_tests, src/moist_swm.f90:1394-1600) with advmtd = "trsk" and
- * time_integrator = "rk4" and no monotonic filter:
+ * (moist_swm_tests, src/moist_swm.f90:1394-1600) with advmtd = "trsk" or
+ * "upw1", time_integrator = "rk4" and no monotonic filter:
  *
  *   reference call                                       replaced by
  *   ---------------------------------------------------  ----------------------
  *   initialize_global_moist_swm_vars, mesh set-up        imodel_moist_create
  *   ode_rk4_moist_swm (moist_swm.f90:1819-2011)          imodel_moist_advance
  *     tendency_moist_swm (:1151-1276), source (:1278-1353),
- *     tendency_advection / divhx (highorder.f90:3936-3972, :4901-4983)
+ *     tendency_advection / divhx (highorder.f90:3936-3972, :4901-4983,
+ *     div_hx_upw1 :5094-5139)
  *   qv, qc, qr = hq / h after each step (:1531-1533)     inside imodel_moist_advance
  *
  * The shallow-water part is the trsk10 / HTC / geodesic-area tendency of
