@@ -77,6 +77,7 @@ class Opts(ctypes.Structure):
         ("learned", ctypes.c_int32), ("mlp_weights", ctypes.c_void_p),
         ("mlp_bytes", ctypes.c_size_t), ("drift_bound", ctypes.c_double),
         ("scheme", ctypes.c_int32), ("fsphere", ctypes.c_int32), ("fcte", ctypes.c_double),
+        ("error_bound", ctypes.c_double),
     ]
 
 
@@ -108,7 +109,7 @@ SWM_SYMBOLS = [
     "imodel_swm_get_state", "imodel_swm_advance", "imodel_swm_profile",
     "imodel_swm_autotune", "imodel_swm_set_tuning", "imodel_swm_set_diffusion",
     "imodel_swm_set_diffusion_fields", "imodel_swm_set_apvm", "imodel_swm_test_fail_alloc",
-    "imodel_swm_learned_weights",
+    "imodel_swm_learned_weights", "imodel_swm_learned_error_proxy",
     "imodel_swm_launch_count",
     "imodel_swm_main_kernel", "imodel_swm_stream", "imodel_swm_weighted_sums_noalloc",
     "imodel_swm_ensemble_create", "imodel_swm_ensemble_set_state",
@@ -214,6 +215,7 @@ def swm_lib() -> ctypes.CDLL:
         lib.imodel_swm_weighted_sums_noalloc.argtypes = [vp, vp, ctypes.c_int64, vp, vp]
         lib.imodel_swm_test_fail_alloc.argtypes = [ctypes.c_int32]
         lib.imodel_swm_learned_weights.argtypes = [vp, c_f64p, c_f64p]
+        lib.imodel_swm_learned_error_proxy.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
         lib.imodel_swm_ensemble_create.argtypes = [ctypes.POINTER(Mesh), ctypes.c_int32, c_i32p,
                                                    ctypes.c_int32, ctypes.c_int32,
                                                    ctypes.POINTER(vp)]

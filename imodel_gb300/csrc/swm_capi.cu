@@ -68,6 +68,13 @@ struct Handle {
   } w_learned, w_plain;
   std::vector<double> kite_hxtr, kite_trskw;
   double drift_bound = 1e-3;
+  // the error proxy: bound, the learned and the plain momentum tendency
+  // ([2][ne]), and the steps left until the next check (<= 0: at the next
+  // guard check)
+  double error_bound = 0.25;
+  float *proxy_u = nullptr;
+  int64_t proxy_left = 0;
+  double last_proxy = -1.0;  // the last value measured (-1: none yet)
   double te_ref = 0.0, umax_ref = 0.0;
   double umax_last = 0.0;  // max |u| at the start of the current guard interval
   bool te_ref_set = false;
@@ -99,6 +106,9 @@ constexpr int kGuardSteps = 32;
 // weights keep TRSK's antisymmetry and are judged by energy and the cap only.
 constexpr double kUmaxStep = 1.1;
 constexpr double kUmaxCap = 3.0;
+// steps between two evaluations of the error proxy (two tendencies: about
+// 0.2 % of the step time at this spacing)
+constexpr int kProxySteps = 256;
 
 #define CK(call)                                                                  \
   do {                                                                            \
@@ -232,7 +242,7 @@ void *host_view(Handle *H, const void *p, size_t bytes) {
 // host FP64 arrays (reference order) -> device state yn, plus h_ed and the
 // "last stage input" ya, as after the reference's initial tendency call
 // (swm.f90:214)
-int learned_guard(Handle *H, bool *tripped = nullptr);
+int learned_guard(Handle *H, bool *tripped = nullptr, int steps = 0);
 
 // new_run: the state starts a new run (set_state), so the learned correction
 // is switched back on and its energy reference is taken again
@@ -312,6 +322,7 @@ int load_state(Handle *H, const double *h, const double *u, bool new_run) {
       learned_switch(H, true);
     }
     H->te_ref_set = false;
+    H->proxy_left = 0;
     return learned_guard(H);
   }
   return IMODEL_SWM_OK;
@@ -429,13 +440,73 @@ bool guard_decide(Handle *H, double te, double umax) {
   return true;
 }
 
-int learned_guard(Handle *H, bool *tripped) {
+// The error proxy (opts.error_bound): how far the learned scheme moves the
+// PV flux of plain TRSK on the current state, ||T_l - T_p|| / ||T_0 - T_p||
+// (L2, edge weights l d), with T_l, T_p the momentum tendencies of the
+// learned and the plain scheme and T_0 the plain one with the PV off (-grad
+// B), so that the denominator is the plain PV flux itself (the whole
+// tendency nearly vanishes on a steady flow).  Without a reference
+// solution, how far the network moves the term it corrects is the error it
+// can add: the learned weights move it by a few per cent, a network gone
+// wrong by far more.  The plain tendencies are launched with local copies
+// of the device mesh and work fields, so the handle (and its captured
+// graph) keep the learned scheme.  Due every kProxySteps steps.
+int error_proxy(Handle *H, int steps, bool *trip) {
+  *trip = false;
+  H->proxy_left -= steps;
+  if (H->proxy_left > 0 || !H->learned_active || H->precision != IMODEL_SWM_FP32) return IMODEL_SWM_OK;
+  H->proxy_left = kProxySteps;
+  auto &W = H->W32;
+  imodel::launch_stage32(H->M, W, W.yn_h, W.yn_u, nullptr, nullptr, -1, 1.0f, H->stream, nullptr);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(H->proxy_u, W.tend_u, sizeof(float) * H->ne, cudaMemcpyDeviceToDevice,
+                     H->stream));
+  DevMesh Mp = H->M;
+  imodel::Work<float> Wp = W;
+  if (H->learned_mode == 2) {
+    Mp.e_stw = H->w_plain.e_stw;
+    Mp.e_stc32 = H->w_plain.e_stc32;
+    Mp.c_R32 = H->w_plain.c_R32;
+    Mp.c_pk = H->w_plain.c_pk;
+  } else {
+    Wp.learned = nullptr;
+  }
+  imodel::launch_stage32(Mp, Wp, W.yn_h, W.yn_u, nullptr, nullptr, -1, 1.0f, H->stream, nullptr);
+  float *plain_u = H->proxy_u + H->ne;
+  CK(cudaMemcpyAsync(plain_u, W.tend_u, sizeof(float) * H->ne, cudaMemcpyDeviceToDevice,
+                     H->stream));
+  Wp.pv_on = 0;  // q = 0: the tendency without the PV flux
+  imodel::launch_stage32(Mp, Wp, W.yn_h, W.yn_u, nullptr, nullptr, -1, 1.0f, H->stream, nullptr);
+  imodel::launch_departure(H->M, H->proxy_u, plain_u, W.tend_u, H->d_scratch, kRedBlocks,
+                           H->stream);
+  CK(cudaGetLastError());
+  std::vector<double> part(2 * static_cast<size_t>(kRedBlocks));
+  CK(cudaMemcpyAsync(part.data(), H->d_scratch, sizeof(double) * part.size(),
+                     cudaMemcpyDeviceToHost, H->stream));
+  CK(cudaStreamSynchronize(H->stream));
+  double d2 = 0.0, b2 = 0.0;
+  for (int k = 0; k < kRedBlocks; ++k) {
+    d2 += part[2 * k];
+    b2 += part[2 * k + 1];
+  }
+  const double dep = b2 > 0.0 ? std::sqrt(d2 / b2) : (d2 > 0.0 ? INFINITY : 0.0);
+  H->last_proxy = dep;
+  if (!(dep <= H->error_bound)) {
+    H->learned_active = false;
+    learned_switch(H, false);
+    *trip = true;
+  }
+  return IMODEL_SWM_OK;
+}
+
+int learned_guard(Handle *H, bool *tripped, int steps) {
   if (tripped) *tripped = false;
   if (!H->learned_active) return IMODEL_SWM_OK;
   double te = 0.0, umax = 0.0;
   int rc = total_energy(H, &te, &umax);
   if (rc) return rc;
-  const bool t = guard_decide(H, te, umax);
+  bool t = guard_decide(H, te, umax);
+  if (!t && (rc = error_proxy(H, steps, &t))) return rc;
   if (tripped) *tripped = t;
   return IMODEL_SWM_OK;
 }
@@ -489,7 +560,7 @@ int advance(Handle *H, double dt, int nsteps) {
     if (rc) return rc;
     if ((rc = launch_steps(H, dt, k))) return rc;
     bool tripped = false;
-    if ((rc = learned_guard(H, &tripped))) return rc;
+    if ((rc = learned_guard(H, &tripped, k))) return rc;
     if (tripped) {
       if ((rc = roll_back(H))) return rc;
       if ((rc = launch_steps(H, dt, k))) return rc;
@@ -523,11 +594,23 @@ int step_host(Handle *H, double *h, double *u, double dt, int nsteps) {
   int f = 0;
   if ((rc = read_flags(H, &f))) return rc;
   const double te = H->h_result[Q_PE] + H->h_result[Q_KE];
-  if (!guard_decide(H, te, H->h_result[Q_UMAX])) return flags_status(H, f);
+  bool trip = guard_decide(H, te, H->h_result[Q_UMAX]);
+  if (!trip && (rc = error_proxy(H, nsteps, &trip))) return rc;
+  if (!trip) return flags_status(H, f);
   if ((rc = roll_back(H)) || (rc = launch_steps(H, dt, nsteps)) ||
       (rc = store_state(H, h, u)))
     return rc;
   return check_flags(H);
+}
+
+// the guard's bounds and the error proxy's buffer (FP32 learned handles)
+int setup_guard(Handle *H, const imodel_swm_opts *o, int ne) {
+  if (!std::isfinite(o->drift_bound) || o->drift_bound < 0 || !std::isfinite(o->error_bound) ||
+      o->error_bound < 0)
+    return set_error(H, IMODEL_SWM_EINVAL, "drift_bound and error_bound must be finite and >= 0");
+  H->drift_bound = o->drift_bound > 0 ? o->drift_bound : 1e-3;
+  H->error_bound = o->error_bound > 0 ? o->error_bound : 0.25;
+  return dalloc(H, &H->proxy_u, 2 * static_cast<size_t>(ne));
 }
 
 int setup_learned(Handle *H, const imodel_swm_mesh *m, const Layout &L, const imodel_swm_opts *o) {
@@ -551,7 +634,7 @@ int setup_learned(Handle *H, const imodel_swm_mesh *m, const Layout &L, const im
   if (H->learned.p) H->allocs.push_back(H->learned.p);
   if (H->learned.img) H->allocs.push_back(H->learned.img);
   if (rc) return set_error(H, rc, "learned correction set-up failed");
-  H->drift_bound = o->drift_bound > 0 ? o->drift_bound : 1e-3;
+  if ((rc = setup_guard(H, o, L.ne))) return rc;
   H->learned_on = H->learned_active = true;
   H->learned_mode = 1;
   H->W32.learned = &H->learned;
@@ -787,7 +870,7 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
       CK(cudaStreamCreateWithFlags(&H->side, cudaStreamNonBlocking));
       CK(cudaEventCreateWithFlags(&H->ev_steps, cudaEventDisableTiming));
       CK(cudaEventCreateWithFlags(&H->ev_side, cudaEventDisableTiming));
-      H->drift_bound = o->drift_bound > 0 ? o->drift_bound : 1e-3;
+      if ((rc = setup_guard(H, o, L.ne))) return rc;
       H->learned_on = H->learned_active = true;
     }
   }
@@ -1344,6 +1427,15 @@ int imodel_swm_learned_weights(void *handle, double *hxtr_area, double *trskw) {
     return imodel::set_error(H, IMODEL_SWM_ESTATE, "the handle was not created with learned weights");
   std::memcpy(hxtr_area, H->kite_hxtr.data(), sizeof(double) * H->kite_hxtr.size());
   std::memcpy(trskw, H->kite_trskw.data(), sizeof(double) * H->kite_trskw.size());
+  return IMODEL_SWM_OK;
+}
+
+int imodel_swm_learned_error_proxy(void *handle, double *value) {
+  Handle *H = static_cast<Handle *>(handle);
+  if (!H || !value) return IMODEL_SWM_EINVAL;
+  if (!H->learned_on || !H->proxy_u)
+    return imodel::set_error(H, IMODEL_SWM_ESTATE, "the handle has no guarded learned correction");
+  *value = H->last_proxy;
   return IMODEL_SWM_OK;
 }
 

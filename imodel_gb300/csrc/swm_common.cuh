@@ -135,6 +135,11 @@ struct Work {
 void launch_stage64(const DevMesh &M, const Work<double> &W, const double *h_in,
                     const double *u_in, double *h_out, double *u_out, int stage,
                     double dt, cudaStream_t s, cudaEvent_t *ev = nullptr);
+// The learned corrections' error proxy: per block part[2 b] = sum w (a -
+// b)^2 and part[2 b + 1] = sum w (b - c)^2 over the edges, in FP64, w = l d
+// / 2 (e_area32); nblk blocks of 256 threads
+void launch_departure(const DevMesh &M, const float *a, const float *b, const float *c,
+                      double *part, int nblk, cudaStream_t s);
 void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
                     const float *u_in, float *h_out, float *u_out, int stage, float dt,
                     cudaStream_t s, cudaEvent_t *ev = nullptr);

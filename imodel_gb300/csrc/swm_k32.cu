@@ -366,9 +366,49 @@ __global__ void __launch_bounds__(512) k_edge32v2(DevMesh M, const float *__rest
   }
 }
 
+// the error proxy's sums (launch_departure): grid-stride over the edges,
+// warp shuffles, one pair of FP64 partial sums per block
+__global__ void __launch_bounds__(256) k_departure(DevMesh M, const float *__restrict__ a,
+                                                   const float *__restrict__ b,
+                                                   const float *__restrict__ c,
+                                                   double *__restrict__ part) {
+  __shared__ double sd[8], sb[8];
+  double d2 = 0.0, b2 = 0.0;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < M.ne; e += gridDim.x * blockDim.x) {
+    const double w = __ldg(&M.e_area32[e]), bb = b[e];
+    const double dd = static_cast<double>(a[e]) - bb, rr = bb - static_cast<double>(c[e]);
+    d2 += w * dd * dd;
+    b2 += w * rr * rr;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    d2 += __shfl_down_sync(0xffffffffu, d2, o);
+    b2 += __shfl_down_sync(0xffffffffu, b2, o);
+  }
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    sd[wid] = d2;
+    sb[wid] = b2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double x = 0.0, y = 0.0;
+    for (int k = 0; k < 8; ++k) {
+      x += sd[k];
+      y += sb[k];
+    }
+    part[2 * blockIdx.x] = x;
+    part[2 * blockIdx.x + 1] = y;
+  }
+}
+
 inline int nblocks(int n, int t) { return (n + t - 1) / t; }
 
 }  // namespace
+
+void launch_departure(const DevMesh &M, const float *a, const float *b, const float *c,
+                      double *part, int nblk, cudaStream_t s) {
+  k_departure<<<nblk, 256, 0, s>>>(M, a, b, c, part);
+}
 
 void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
                     const float *u_in, float *h_out, float *u_out, int stage, float dt,

@@ -115,18 +115,19 @@ class SWM:
     precision: "fp64" reproduces the reference's FP64 operation order;
     "fp32" runs FP32 state and operators with FP64 integrals.
     scheme: the method wrapper of swm.par, "trsk10", "pxt16", "gass18", or
-    "dtred" (trsk10 with the dtred Coriolis reconstruction); the last three
-    on "fp64" handles.  fsphere = 2 replaces f = 2 Omega sin(lat) by the
-    constant fcte (the f-sphere of test cases 33, 35, 40-42).
+    "dtred" (trsk10 with the dtred Coriolis reconstruction).  fsphere = 2
+    replaces f = 2 Omega sin(lat) by the constant fcte (the f-sphere of test
+    cases 33, 35, 40-42).
     learned_params: the per-step learned correction (FP32); learned_weights:
     network parameters of the learned TRSK weights (imodel_gb300.
-    learned_weights), applied once at creation.
+    learned_weights), applied once at creation.  drift_bound, error_bound:
+    the guard's energy-drift and error-proxy bounds (include/imodel_swm.h).
     """
 
     def __init__(self, grid: Grid, precision: str = "fp64", testcase: int = 2,
                  bt=None, h_ref: float = 0.0, device: int = 0, learned_params=None,
                  drift_bound: float = 0.0, scheme: str = "trsk10", fsphere: int = 0,
-                 fcte: float = 0.0, learned_weights=None):
+                 fcte: float = 0.0, learned_weights=None, error_bound: float = 0.0):
         self.grid = grid
         self.lib = _capi.swm_lib()
         self.precision = precision
@@ -157,6 +158,7 @@ class SWM:
             opts.mlp_weights = self._mlp.ctypes.data
             opts.mlp_bytes = self._mlp.nbytes
             opts.drift_bound = drift_bound
+            opts.error_bound = error_bound
         self._handle = ctypes.c_void_p()
         rc = self.lib.imodel_swm_create(ctypes.byref(self._mesh), ctypes.byref(opts),
                                         ctypes.byref(self._handle))
@@ -261,6 +263,14 @@ class SWM:
         self._check(self.lib.imodel_swm_learned_weights(self._handle, _capi.as_f64p(R),
                                                         _capi.as_f64p(w)))
         return R, w
+
+    def learned_error_proxy(self) -> float:
+        """The guard's error proxy as last measured (-1 before the first):
+        relative L2 difference of the learned and the plain momentum
+        tendency on the state of that check."""
+        v = ctypes.c_double()
+        self._check(self.lib.imodel_swm_learned_error_proxy(self._handle, ctypes.byref(v)))
+        return v.value
 
     def diagnostics(self) -> dict:
         """sumf_areas + calc_energies + RMS divergence of the current state."""

@@ -143,6 +143,14 @@ typedef struct imodel_swm_opts {
                          the normal-mode cases is not a time step and is
                          refused                                         */
   double fcte;        /* f for fsphere = 2 (s^-1)                          */
+  double error_bound; /* FP32 learned corrections: the error proxy's bound
+                         (0 = 0.25).  Every 256 steps (and at the first
+                         check after a state is set) the momentum tendency
+                         of the learned scheme is compared with plain TRSK's
+                         on the current state; a relative difference (L2,
+                         edge weights l d) above the bound switches the
+                         correction off like the energy check: the
+                         interval is stepped again with the plain scheme  */
 } imodel_swm_opts;
 
 /* ---- diagnostics (swm.f90:293-322, :2686-2752, :3394-3440) ------------- */
@@ -255,6 +263,12 @@ int imodel_swm_set_apvm(void *handle, double pvspar, double dt);
  * that puts them into its grid_structure runs the same scheme on the CPU.
  * IMODEL_SWM_ESTATE for other handles.  No counterpart in the reference. */
 int imodel_swm_learned_weights(void *handle, double *hxtr_area, double *trskw);
+/* The error proxy (see imodel_swm_opts.error_bound) as last measured: the
+ * relative L2 difference between the learned scheme's momentum tendency and
+ * plain TRSK's; -1 before the first measurement.  IMODEL_SWM_ESTATE for a
+ * handle without a guarded learned correction.  No counterpart in the
+ * reference. */
+int imodel_swm_learned_error_proxy(void *handle, double *value);
 /* Test hook with no counterpart in the reference: when after > 0, the
  * after-th device allocation made by any handle from now on fails with
  * IMODEL_SWM_ENOMEM as if the device were full (0 switches the injection

@@ -50,12 +50,19 @@ def test_correction_term_matches_host_inputs(grid_at):
 
 def test_energy_drift_guard_switches_off(grid_at):
     """A network far from the TRSK error destroys energy neutrality; once the
-    drift exceeds the bound the plain scheme takes over."""
+    drift exceeds the bound the plain scheme takes over.  (The error proxy
+    would switch this network off at once: it moves the PV flux by far more
+    than its bound.  A huge error_bound leaves the energy check alone.)"""
     g = grid_at(4)
     h, u = fields.balanced_state(g, lmax=16, seed=1)
     p = mo.init_params(8) * 50.0
     p[-1] = 30.0
-    m = SWM(g, "fp32", learned_params=p, drift_bound=1e-6)
+    wild = SWM(g, "fp32", learned_params=p)
+    wild.set_state(h, u)
+    assert wild.diagnostics()["learned_active"] == 0
+    assert wild.learned_error_proxy() > 0.25
+    wild.close()
+    m = SWM(g, "fp32", learned_params=p, drift_bound=1e-6, error_bound=1e30)
     m.set_state(h, u)
     assert m.diagnostics()["learned_active"] == 1
     for _ in range(20):

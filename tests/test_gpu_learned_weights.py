@@ -148,3 +148,73 @@ def test_launches_and_refusals(grid_at):
     assert lib.imodel_swm_create(ctypes.byref(g.c_struct()), ctypes.byref(opts),
                                  ctypes.byref(h)) == _capi.EINVAL
     lib.imodel_swm_destroy(h)
+
+
+def test_error_proxy_measures_the_departure_and_trips_the_guard(grid_at):
+    """The guard's error proxy (imodel_swm_opts.error_bound): how far the
+    learned weights move plain TRSK's PV flux, ||T_learned - T_plain|| /
+    ||Q_plain|| (L2, edge weights l d), measured when the state is set and
+    every 256 steps.  It equals the same ratio formed from the two handles'
+    tendencies and the oracle's PV flux; a bound below it switches the
+    learned weights off at once, and the run then equals a plain run bit
+    for bit."""
+    g = grid_at(5)
+    h, u = fields.balanced_state(g, lmax=16, seed=34)
+    m = SWM(g, "fp32", learned_weights=_params())
+    m.set_state(h, u)
+    v0 = m.learned_error_proxy()
+    _, tl = m.tendency(h, u)
+    p = SWM(g, "fp32")
+    _, tp = p.tendency(h, u)
+    p.close()
+    o = oracle.Oracle(g, 2)
+    o.tendency(h, u)
+    q = o.field("uhq_perp")
+    w = g.ed_leng * g.edhx_leng
+    ref = float(np.sqrt(np.sum(w * (tl - tp) ** 2) / np.sum(w * q * q)))
+    m.set_state(h, u)
+    m.advance(450.0, 300)
+    v1 = m.learned_error_proxy()
+    assert m.diagnostics()["learned_active"] == 1
+    m.close()
+    print(f"error proxy of the learned weights: {v0:.4f} at the start (host {ref:.4f}), "
+          f"{v1:.4f} after 256 steps")
+    assert abs(v0 - ref) <= 1e-3 * ref
+    assert 0.001 < v0 < 0.25 and 0.001 < v1 < 0.25 and v1 != v0
+    # a bound below the measured departure: off at once, then plain TRSK
+    m = SWM(g, "fp32", learned_weights=_params(), error_bound=0.5 * v0)
+    m.set_state(h, u)
+    assert m.diagnostics()["learned_active"] == 0
+    m.advance(450.0, 40)
+    hg, ug = m.get_state()
+    m.close()
+    p = SWM(g, "fp32")
+    p.set_state(h, u)
+    p.advance(450.0, 40)
+    hp, up = p.get_state()
+    p.close()
+    assert np.array_equal(hg, hp) and np.array_equal(ug, up)
+
+
+def test_error_proxy_of_the_per_step_network(grid_at):
+    g = grid_at(5)
+    h, u = fields.balanced_state(g, lmax=16, seed=35)
+    pn = learned.trained_params()
+    if pn is None:
+        pytest.skip("no trained per-step network in imodel_gb300/data")
+    m = SWM(g, "fp32", learned_params=pn)
+    m.set_state(h, u)
+    v = m.learned_error_proxy()
+    m.close()
+    print(f"error proxy of the per-step network: {v:.4f}")
+    assert 0.0 < v < 0.25
+    m = SWM(g, "fp32", learned_params=pn, error_bound=0.5 * v)
+    m.set_state(h, u)
+    assert m.diagnostics()["learned_active"] == 0
+    m.close()
+    with pytest.raises(SWMError) as e:
+        SWM(g, "fp32").learned_error_proxy()
+    assert e.value.code == _capi.ESTATE
+    with pytest.raises(SWMError) as e:
+        SWM(g, "fp32", learned_params=pn, error_bound=-1.0)
+    assert e.value.code == _capi.EINVAL
