@@ -105,3 +105,38 @@ def test_ensemble_barrier_timeout_status(grid_at):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     ens.close()
     fresh.close()
+
+
+def test_ensemble_with_the_learned_trsk_weights(grid_at):
+    """The headline method in an ensemble: the learned TRSK weights are a
+    corrected mesh, so an ensemble on the weights a learned-weights handle
+    exports (imodel_swm_learned_weights) steps every member as that handle
+    steps it, bit for bit."""
+    from imodel_gb300 import learned, learned_weights as lw
+    g = grid_at(4)
+    p = lw.trained_params()
+    if p is None:
+        p = learned.init_params(7)
+    probe = SWM(g, "fp32", learned_weights=p)
+    R, w = probe.learned_weights()
+    probe.close()
+    g2 = lw.with_weights(g, R, w)
+    states = _states(g, [7, 8], 16)
+    ens = Ensemble([g2], [2])
+    for m, (h, u) in enumerate(states):
+        ens.set_state(0, m, h, u)
+    ens.advance([900.0], [24])
+    s = a = 0.0
+    for ai, hi in zip(g.hx_areag.tolist(), states[0][0].tolist()):
+        a += ai
+        s += ai * hi
+    h_ref = float(np.float32(s / a))
+    for m, (h, u) in enumerate(states):
+        single = SWM(g, "fp32", h_ref=h_ref, learned_weights=p)
+        single.set_tuning(variant=1)
+        hs, us = single.ode_rk4(h, u, 900.0, 24)
+        assert single.diagnostics()["learned_active"] == 1
+        single.close()
+        he, ue = ens.get_state(0, m)
+        assert np.array_equal(he, hs) and np.array_equal(ue, us), m
+    ens.close()
