@@ -119,12 +119,12 @@ def build_swm_lib(force: bool = False) -> str:
     obj = os.path.join(OBJ_DIR, "swm_layout.o")
     objs.append(obj)
     if force or _stale(obj, [src] + headers):
-        jobs.append(["g++"] + CXX_COMMON + ["-I" + CSRC, "-c", src, "-o", obj])
+        jobs.append(["g++"] + CXX_COMMON + ["-fopenmp", "-I" + CSRC, "-c", src, "-o", obj])
     if jobs:
         _run_parallel(jobs)
     if force or _stale(out, objs):
         _run_parallel([[nvcc, "-shared"] + ARCH + objs +
-                       ["-o", out, "-L" + _cuda_lib_dir(), "-lcudart"]])
+                       ["-o", out, "-Xcompiler", "-fopenmp", "-L" + _cuda_lib_dir(), "-lcudart"]])
     return out
 
 

@@ -47,15 +47,59 @@ uint32_t quant(double x, int b) {
   return static_cast<uint32_t>(q);
 }
 
+// n2o: the indices 0..n-1 in the order of their keys, equal keys in index
+// order (the order std::stable_sort gives), by a least-significant-digit
+// radix sort of (key, index) pairs, 8-bit digits, skipping the digits that
+// are the same in every key; o2n its inverse
 template <class Key>
 void sort_perm(std::vector<int32_t> &n2o, std::vector<int32_t> &o2n, const std::vector<Key> &key) {
   const size_t n = key.size();
-  n2o.resize(n);
-  std::iota(n2o.begin(), n2o.end(), 0);
-  std::stable_sort(n2o.begin(), n2o.end(),
-                   [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+  std::vector<Key> ka(key), kb(n);
+  std::vector<int32_t> ia(n), ib(n);
+  std::iota(ia.begin(), ia.end(), 0);
+  Key any = 0, all = static_cast<Key>(~Key(0));
+  for (size_t i = 0; i < n; ++i) {
+    any |= key[i];
+    all &= key[i];
+  }
+  for (int shift = 0; shift < static_cast<int>(8 * sizeof(Key)); shift += 8) {
+    if ((((any ^ all) >> shift) & 0xFF) == 0) continue;
+    size_t cnt[257] = {0};
+    for (size_t i = 0; i < n; ++i) ++cnt[((ka[i] >> shift) & 0xFF) + 1];
+    for (int d = 0; d < 256; ++d) cnt[d + 1] += cnt[d];
+    for (size_t i = 0; i < n; ++i) {
+      const size_t to = cnt[(ka[i] >> shift) & 0xFF]++;
+      kb[to] = ka[i];
+      ib[to] = ia[i];
+    }
+    ka.swap(kb);
+    ia.swap(ib);
+  }
+  n2o.swap(ia);
   o2n.resize(n);
-  for (size_t i = 0; i < n; ++i) o2n[n2o[i]] = static_cast<int32_t>(i);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < static_cast<int64_t>(n); ++i) o2n[n2o[i]] = static_cast<int32_t>(i);
+}
+
+// body(i) for i in [0, n) on host threads; body returns "" or an error
+// message, and the message of the lowest failing i comes back: the one a
+// serial loop would have stopped at
+template <class F>
+std::string par_for(int64_t n, F body) {
+  int64_t first = INT64_MAX;
+  std::string msg;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    std::string e = body(i);
+    if (!e.empty()) {
+#pragma omp critical(imodel_layout_first_error)
+      if (i < first) {
+        first = i;
+        msg = std::move(e);
+      }
+    }
+  }
+  return msg;
 }
 
 // tr%c%p of triangle t (0-based): the unit normal of the plane through its
@@ -160,6 +204,7 @@ void scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
   const int ne = L.ne, nt = L.nt;
   if (scheme == IMODEL_SWM_PXT16 || scheme == IMODEL_SWM_GASS18) {
     // the depth at the triangle as weights of its vertices
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nt; ++i) {
       const int t = L.tri_n2o[i];
       double w[3] = {0.0, 0.0, 0.0};
@@ -182,6 +227,7 @@ void scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
     }
     // q_e from the edge's two triangles
     L.e_qw32.assign(2 * NE, 0.0f);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < ne; ++i) {
       double a, b;
       if (scheme == IMODEL_SWM_PXT16) {
@@ -197,6 +243,7 @@ void scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
   }
   if (scheme == IMODEL_SWM_PXT16) {
     // pered on the TRSK stencil's slots, in the order build_layout made them
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < ne; ++i) {
       const int e = L.edge_n2o[i];
       const double *nr = m.ed_nr + 3 * static_cast<size_t>(e);
@@ -224,6 +271,7 @@ void scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
   }
   if (scheme == IMODEL_SWM_DTRED) {
     L.e_dtc32.assign(6 * NE, 0.0f);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < ne; ++i) {
       const double d1 = L.e_dist[i], d2 = L.e_dist[NE + i];
       const double w[2] = {d2 / (d1 + d2), d1 / (d1 + d2)};
@@ -251,13 +299,15 @@ void scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
 std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, int scheme,
                          int fsphere, double fcte) {
   const int nv = m.nv, ne = m.ne, nt = m.nt;
+  std::string err;  // the first error of a parallel loop
   if (nv < 4 || ne < 6 || nt < 4) return "mesh sizes too small";
   if (!m.nnb || !m.v_ed || !m.v_tr || !m.hx_ttgout || !m.hx_tnrccw || !m.hx_areag ||
       !m.hx_trskw || !m.v_p || !m.ed_v || !m.ed_sh || !m.ed_leng || !m.edhx_leng ||
       !m.tr_v || !m.tr_ed || !m.tr_tg || !m.tr_areag || !m.tr_trhx_area || !m.tr_c_lat)
     return "mesh array pointer is NULL";
   if (!(m.erad > 0) || !(m.grav > 0)) return "erad and grav must be positive";
-  for (int i = 0; i < nv; ++i) {
+  err = par_for(nv, [&](int64_t i64) -> std::string {
+    const int i = static_cast<int>(i64);
     int n = m.nnb[i];
     if (n < 3 || n > kMaxNb) return "nnb outside 3..6 at cell " + std::to_string(i + 1);
     for (int j = 0; j < n; ++j) {
@@ -265,23 +315,31 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
       if (e < 1 || e > ne) return "v_ed index out of range at cell " + std::to_string(i + 1);
     }
     if (!(m.hx_areag[i] > 0)) return "non-positive hx_areag at cell " + std::to_string(i + 1);
-  }
-  for (int e = 0; e < ne; ++e) {
+    return std::string();
+  });
+  if (!err.empty()) return err;
+  err = par_for(ne, [&](int64_t e64) -> std::string {
+    const int e = static_cast<int>(e64);
     for (int s = 0; s < 2; ++s) {
       int c = m.ed_v[2 * static_cast<size_t>(e) + s], t = m.ed_sh[2 * static_cast<size_t>(e) + s];
       if (c < 1 || c > nv) return "ed_v index out of range at edge " + std::to_string(e + 1);
       if (t < 1 || t > nt) return "ed_sh index out of range at edge " + std::to_string(e + 1);
     }
     if (!(m.ed_leng[e] > 0)) return "non-positive ed_leng at edge " + std::to_string(e + 1);
-  }
-  for (int t = 0; t < nt; ++t) {
+    return std::string();
+  });
+  if (!err.empty()) return err;
+  err = par_for(nt, [&](int64_t t64) -> std::string {
+    const int t = static_cast<int>(t64);
     for (int s = 0; s < 3; ++s) {
       int c = m.tr_v[3 * static_cast<size_t>(t) + s], e = m.tr_ed[3 * static_cast<size_t>(t) + s];
       if (c < 1 || c > nv || e < 1 || e > ne)
         return "tr_v/tr_ed index out of range at triangle " + std::to_string(t + 1);
     }
     if (!(m.tr_areag[t] > 0)) return "non-positive tr_areag at triangle " + std::to_string(t + 1);
-  }
+    return std::string();
+  });
+  if (!err.empty()) return err;
 
   L.nv = nv;
   L.ne = ne;
@@ -294,6 +352,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
   {
     std::vector<uint64_t> key(nv);
     const int b = 20;
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nv; ++i) {
       const double *p = m.v_p + 3 * static_cast<size_t>(i);
       key[i] = hilbert3(quant(p[0], b), quant(p[1], b), quant(p[2], b), b);
@@ -302,6 +361,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
   }
   {
     std::vector<uint64_t> key(ne);
+#pragma omp parallel for schedule(static)
     for (int e = 0; e < ne; ++e) {
       uint64_t a = static_cast<uint64_t>(L.cell_o2n[m.ed_v[2 * static_cast<size_t>(e)] - 1]);
       uint64_t c = static_cast<uint64_t>(L.cell_o2n[m.ed_v[2 * static_cast<size_t>(e) + 1] - 1]);
@@ -311,6 +371,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
   }
   {
     std::vector<uint64_t> key(nt);
+#pragma omp parallel for schedule(static)
     for (int t = 0; t < nt; ++t) {
       uint64_t v[3];
       for (int s = 0; s < 3; ++s)
@@ -340,7 +401,8 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
   L.c_inva32.resize(NV);
   L.c_meta.resize(NV);
   if (nv >= (1 << 28)) return "more than 2^28 cells";
-  for (int i = 0; i < nv; ++i) {
+  err = par_for(nv, [&](int64_t i64) -> std::string {
+    const int i = static_cast<int>(i64);
     const int c = L.cell_n2o[i];
     const int n = m.nnb[c];
     uint32_t tbits = 0;
@@ -365,7 +427,10 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
     }
     L.c_meta[i] = static_cast<uint32_t>(n) | (tbits << 8);
     L.c_inva32[i] = static_cast<float>(1.0 / (m.hx_areag[c] * m.erad));
-  }
+    return std::string();
+  });
+  if (!err.empty()) return err;
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < nv; ++i) {
     const int c = L.cell_n2o[i];
     const int n = m.nnb[c];
@@ -406,7 +471,8 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
   L.e_stc32.assign(kMaxSt * NE, 0.0f);
   if (scheme == IMODEL_SWM_GASS18) L.e_stq.assign(kMaxSt * NE, -1);
   L.e_vs.assign(2 * NE, 0u);
-  for (int i = 0; i < ne; ++i) {
+  err = par_for(ne, [&](int64_t i64) -> std::string {
+    const int i = static_cast<int>(i64);
     const int e = L.edge_n2o[i];
     for (int s = 0; s < 2; ++s) {
       L.e_v[s * NE + i] = L.cell_o2n[m.ed_v[2 * static_cast<size_t>(e) + s] - 1];
@@ -467,11 +533,14 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
       }
     }
     L.e_nst[i] = static_cast<int8_t>(ns);
-  }
+    return std::string();
+  });
+  if (!err.empty()) return err;
 
   // packed cell slots and edge cell words for vector loads
   L.c_pk.assign(kMaxNb * NV * 4, 0);
   L.c_kd.assign(kMaxNb * NV * 2, 0.0f);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < nv; ++i) {
     const int n = L.c_nnb[i];
     for (int j = 0; j < kMaxNb; ++j) {
@@ -489,6 +558,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
     }
   }
   L.e_vs2.resize(2 * NE);
+#pragma omp parallel for schedule(static)
   for (size_t e = 0; e < NE; ++e) {
     L.e_vs2[2 * e] = L.e_vs[e];
     L.e_vs2[2 * e + 1] = L.e_vs[NE + e];
@@ -504,6 +574,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
   L.t_areag.resize(NT);
   L.t_f.resize(NT);
   L.t_f32.resize(NT);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < nt; ++i) {
     const int t = L.tri_n2o[i];
     const double A = m.tr_areag[t];
@@ -530,17 +601,21 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
     L.t_c.resize(3 * NT);
     L.e_c.resize(3 * NE);
     L.c_p.resize(3 * NV);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nt; ++i) {
       double c[3];
       circumcentre(m, L.tri_n2o[i], c);
       for (int k = 0; k < 3; ++k) L.t_c[k * NT + i] = c[k];
     }
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < ne; ++i)
       for (int k = 0; k < 3; ++k) L.e_c[k * NE + i] = m.ed_c[3 * static_cast<size_t>(L.edge_n2o[i]) + k];
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nv; ++i)
       for (int k = 0; k < 3; ++k) L.c_p[k * NV + i] = m.v_p[3 * static_cast<size_t>(L.cell_n2o[i]) + k];
     L.t_apw32.assign(9 * NT, 0.0f);
     L.t_cc32.assign(3 * NT, 0.0f);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nt; ++i) {
       const int t = L.tri_n2o[i];
       for (int s = 0; s < 3; ++s) {
@@ -555,6 +630,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
     }
     L.c_apw32.assign(18 * NV, 0.0f);
     L.c_p32.assign(3 * NV, 0.0f);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nv; ++i) {
       const int c = L.cell_n2o[i];
       for (int j = 0; j < m.nnb[c]; ++j) {
@@ -574,6 +650,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
     if (!m.ed_nr || !m.ed_c) return "the pxt16, gass18 and dtred schemes need ed_nr and ed_c";
     if (scheme == IMODEL_SWM_PXT16) {
       L.t_bary.resize(3 * NT);
+#pragma omp parallel for schedule(static)
       for (int i = 0; i < nt; ++i) {
         const int t = L.tri_n2o[i];
         const double pc[3] = {L.t_c[i], L.t_c[NT + i], L.t_c[2 * NT + i]};
@@ -590,6 +667,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
     }
     if (scheme == IMODEL_SWM_PXT16 || scheme == IMODEL_SWM_DTRED) {
       L.e_dist.resize(2 * NE);
+#pragma omp parallel for schedule(static)
       for (int i = 0; i < ne; ++i) {
         const int e = L.edge_n2o[i];
         for (int s = 0; s < 2; ++s) {
@@ -601,6 +679,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
     }
     if (scheme == IMODEL_SWM_GASS18) {
       L.t_edarea.resize(3 * NT);
+#pragma omp parallel for schedule(static)
       for (int i = 0; i < nt; ++i) {
         const int t = L.tri_n2o[i];
         const double pc[3] = {L.t_c[i], L.t_c[NT + i], L.t_c[2 * NT + i]};
@@ -613,6 +692,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
       }
     }
     L.e_nr.resize(3 * NE);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < ne; ++i)
       for (int k = 0; k < 3; ++k) L.e_nr[k * NE + i] = m.ed_nr[3 * static_cast<size_t>(L.edge_n2o[i]) + k];
     scheme_fp32(m, L, scheme);
@@ -625,6 +705,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
     std::memcpy(&b, &f, sizeof(b));
     return b;
   };
+#pragma omp parallel for schedule(static)
   for (size_t i = 0; i < NT; ++i) {
     int32_t *a = &L.t_recA[4 * i], *b = &L.t_recB[4 * i], *c = &L.t_recC[4 * i];
     a[0] = L.t_ed[i];
@@ -647,6 +728,7 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
     L.t_c16B.assign(4 * NT, 0.0f);
     L.t_c16C.assign(2 * NT, 0.0f);
     L.t_wb.assign(2 * nw, 0);
+#pragma omp parallel for schedule(static)
     for (size_t w = 0; w < nw; ++w) {
       const size_t t0 = 32 * w, t1 = std::min(NT, t0 + 32);
       int32_t lo[2] = {INT32_MAX, INT32_MAX}, hi[2] = {INT32_MIN, INT32_MIN};
@@ -718,6 +800,7 @@ std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, Lear
   auto put_i32 = [&](int64_t i, int off, int k, int32_t v) {
     std::memcpy(at(i, off, k, 4), &v, 4);
   };
+#pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < ne; ++i) {
     const int64_t r = i % T;
     put_i32(i, LearnedLayout::kEsh, static_cast<int>(r), L.e_sh[i]);
@@ -728,7 +811,8 @@ std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, Lear
   double lmean = 0.0;
   for (int e = 0; e < ne; ++e) lmean += m.ed_leng[e];
   lmean /= ne;
-  for (int e = 0; e < ne; ++e) {
+  return par_for(ne, [&](int64_t e64) -> std::string {
+    const int e = static_cast<int>(e64);
     const int i = L.edge_o2n[e];
     const int r = i % T;
     const double l = m.ed_leng[e], d = m.edhx_leng[e];
@@ -764,8 +848,8 @@ std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, Lear
       const uint16_t b16 = bf16_bits(g[q]);
       std::memcpy(at(i, LearnedLayout::kGeo, 16 * r + q, 2), &b16, 2);
     }
-  }
-  return "";
+    return std::string();
+  });
 }
 
 // ---- learned TRSK weights ----------------------------------------------------
@@ -779,19 +863,19 @@ std::string build_kite_inputs(const imodel_swm_mesh &m, KiteInputs &K) {
   K.cell.resize(nrow);
   K.slot.resize(nrow);
   // row of (c, j): slot-major, the cells with nnb > j in order
-  std::vector<size_t> next(6, 0);
+  std::vector<size_t> row_of(6 * static_cast<size_t>(nv), 0);
   {
     size_t acc = 0;
-    for (int j = 0; j < 6; ++j) {
-      next[j] = acc;
-      for (int c = 0; c < nv; ++c) acc += m.nnb[c] > j ? 1 : 0;
-    }
+    for (int j = 0; j < 6; ++j)
+      for (int c = 0; c < nv; ++c)
+        if (m.nnb[c] > j) row_of[6 * static_cast<size_t>(c) + j] = acc++;
   }
   auto tangent = [](const double *v, const double *p, double *t) {
     const double vp = dot3(v, p);
     for (int k = 0; k < 3; ++k) t[k] = v[k] - vp * p[k];
   };
   static const int kDj[6] = {0, -1, 1, -2, 2, 3};
+#pragma omp parallel for schedule(static)
   for (int c = 0; c < nv; ++c) {
     const int n = m.nnb[c];
     const double *P = m.v_p + 3 * static_cast<size_t>(c);
@@ -830,7 +914,7 @@ std::string build_kite_inputs(const imodel_swm_mesh &m, KiteInputs &K) {
       f[11] = 10.0 * (m.ed_leng[e0] / mean_l - 1.0);
       f[12] = 10.0 * (m.ed_leng[e1] / mean_l - 1.0);
       f[13] = 10.0 * (r[j] / mean_r - 1.0);
-      const size_t row = next[j]++;
+      const size_t row = row_of[6 * static_cast<size_t>(c) + j];
       for (int q = 0; q < 24; ++q) K.x[24 * row + q] = bf16_bits(static_cast<float>(f[q]));
       K.cell[row] = c;
       K.slot[row] = static_cast<int8_t>(j);
@@ -843,10 +927,12 @@ void apply_kite_outputs(const imodel_swm_mesh &m, const KiteInputs &K, const flo
                         std::vector<double> &hxtr, std::vector<double> &trskw) {
   const int nv = m.nv;
   std::vector<double> dR(6 * static_cast<size_t>(nv), 0.0);
-  for (size_t r = 0; r < K.cell.size(); ++r)
+#pragma omp parallel for schedule(static)
+  for (int64_t r = 0; r < static_cast<int64_t>(K.cell.size()); ++r)
     dR[6 * static_cast<size_t>(K.cell[r]) + K.slot[r]] = 0.1 * static_cast<double>(y[r]);
   hxtr.assign(m.hx_hxtr_area, m.hx_hxtr_area + 6 * static_cast<size_t>(nv));
   trskw.assign(36 * static_cast<size_t>(nv), 0.0);
+#pragma omp parallel for schedule(static)
   for (int c = 0; c < nv; ++c) {
     const int n = m.nnb[c];
     double *R = hxtr.data() + 6 * static_cast<size_t>(c);
