@@ -98,6 +98,30 @@ class Grid:
         return self.ed_sh.astype(np.int64) - 1
 
 
+class _GridMemory:
+    """Owns a grid built by the library; every array of the Grid views its
+    memory and holds a reference, so it is freed with the last of them."""
+
+    def __init__(self, lib, handle):
+        self.lib, self.handle = lib, handle
+
+    def __del__(self):
+        if self.handle:
+            self.lib.imodel_mesh_free(self.handle)
+            self.handle = None
+
+
+def _view(ptr, n: int, owner: _GridMemory) -> np.ndarray:
+    """A writable numpy view of n elements at the ctypes pointer ptr that
+    keeps `owner` alive (no copy: a level-10 grid is about 12 GB)."""
+    ctype = ptr._type_
+    if n == 0:
+        return np.zeros(0, dtype=np.dtype(ctype))
+    raw = (ctype * n).from_address(ctypes.cast(ptr, ctypes.c_void_p).value)
+    raw._owner = owner
+    return np.frombuffer(raw, dtype=np.dtype(ctype))
+
+
 def meshbuild(level: int, pos: str = "eqs", nthreads: int = 0, device=None) -> Grid:
     """Builds icosahedral grid ``level`` ("eqs" or "pol" base positions).
 
@@ -119,36 +143,20 @@ def meshbuild(level: int, pos: str = "eqs", nthreads: int = 0, device=None) -> G
         if device is not None:
             msg = f"{msg} {lib.imodel_mesh_gpu_last_error().decode()}"
         raise RuntimeError(f"{what} failed: {msg}")
-    try:
-        view = _capi.Mesh()
-        lib.imodel_mesh_view(handle, ctypes.byref(view))
-        extra = _capi.MeshExtra()
-        lib.imodel_mesh_extra_view(handle, ctypes.byref(extra))
-        n = {"nv": view.nv, "ne": view.ne, "nt": view.nt}
-        arrays = {}
-        for k, shp in _I32.items():
-            cnt = n[_COUNT[k]]
-            shape = (cnt,) if shp == (1,) else (cnt,) + shp
-            arrays[k] = np.ctypeslib.as_array(getattr(view, k),
-                                              shape=(int(np.prod(shape)),)).reshape(shape).copy()
-        for k, shp in _F64.items():
-            cnt = n[_COUNT[k]]
-            shape = (cnt,) if shp == (1,) else (cnt,) + shp
-            arrays[k] = np.ctypeslib.as_array(getattr(view, k),
-                                              shape=(int(np.prod(shape)),)).reshape(shape).copy()
-        for k, (cnt_name, shp) in _EXTRA_F64.items():
-            cnt = n[cnt_name]
-            shape = (cnt,) if shp == (1,) else (cnt,) + shp
-            arrays[k] = np.ctypeslib.as_array(getattr(extra, k),
-                                              shape=(int(np.prod(shape)),)).reshape(shape).copy()
-        for k, (cnt_name, shp) in _EXTRA_I32.items():
-            cnt = n[cnt_name]
-            shape = (cnt,) + shp
-            arrays[k] = np.ctypeslib.as_array(getattr(extra, k),
-                                              shape=(int(np.prod(shape)),)).reshape(shape).copy()
-        cnt = ctypes.c_int64()
-        margin = ctypes.c_double()
-        lib.imodel_mesh_delaunay_violations(handle, ctypes.byref(cnt), ctypes.byref(margin))
-    finally:
-        lib.imodel_mesh_free(handle)
+    owner = _GridMemory(lib, handle)
+    view = _capi.Mesh()
+    lib.imodel_mesh_view(handle, ctypes.byref(view))
+    extra = _capi.MeshExtra()
+    lib.imodel_mesh_extra_view(handle, ctypes.byref(extra))
+    n = {"nv": view.nv, "ne": view.ne, "nt": view.nt}
+    arrays = {}
+    fields = [(k, view, n[_COUNT[k]], shp) for k, shp in list(_I32.items()) + list(_F64.items())]
+    fields += [(k, extra, n[c], shp) for k, (c, shp) in
+               list(_EXTRA_F64.items()) + list(_EXTRA_I32.items())]
+    for k, src, cnt, shp in fields:
+        shape = (cnt,) if shp == (1,) else (cnt,) + shp
+        arrays[k] = _view(getattr(src, k), int(np.prod(shape)), owner).reshape(shape)
+    cnt = ctypes.c_int64()
+    margin = ctypes.c_double()
+    lib.imodel_mesh_delaunay_violations(handle, ctypes.byref(cnt), ctypes.byref(margin))
     return Grid(arrays, level=level, pos=pos, delaunay=(cnt.value, margin.value))
