@@ -110,6 +110,7 @@ SWM_SYMBOLS = [
     "imodel_swm_autotune", "imodel_swm_set_tuning", "imodel_swm_set_diffusion",
     "imodel_swm_set_diffusion_fields", "imodel_swm_set_apvm", "imodel_swm_test_fail_alloc",
     "imodel_swm_learned_weights", "imodel_swm_learned_error_proxy",
+    "imodel_swm_test_layout_digest",
     "imodel_swm_launch_count",
     "imodel_swm_main_kernel", "imodel_swm_stream", "imodel_swm_weighted_sums_noalloc",
     "imodel_swm_ensemble_create", "imodel_swm_ensemble_set_state",
@@ -216,6 +217,9 @@ def swm_lib() -> ctypes.CDLL:
         lib.imodel_swm_test_fail_alloc.argtypes = [ctypes.c_int32]
         lib.imodel_swm_learned_weights.argtypes = [vp, c_f64p, c_f64p]
         lib.imodel_swm_learned_error_proxy.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+        lib.imodel_swm_test_layout_digest.argtypes = [ctypes.POINTER(Mesh), ctypes.c_int32,
+                                                       ctypes.c_int32,
+                                                       ctypes.POINTER(ctypes.c_uint64)]
         lib.imodel_swm_ensemble_create.argtypes = [ctypes.POINTER(Mesh), ctypes.c_int32, c_i32p,
                                                    ctypes.c_int32, ctypes.c_int32,
                                                    ctypes.POINTER(vp)]

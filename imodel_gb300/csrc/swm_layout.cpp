@@ -959,3 +959,69 @@ void apply_kite_outputs(const imodel_swm_mesh &m, const KiteInputs &K, const flo
 }
 
 }  // namespace imodel
+
+// ---- test hook: a digest of the whole layout ---------------------------------
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+uint64_t fnv1a(const void *p, size_t n, uint64_t h) {
+  const unsigned char *c = static_cast<const unsigned char *>(p);
+  for (size_t i = 0; i < n; ++i) {
+    h ^= c[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+template <class T>
+uint64_t digest_of(const std::vector<T> &v, uint64_t h) {
+  h = fnv1a(v.data(), v.size() * sizeof(T), h);
+  const uint64_t n = v.size();
+  return fnv1a(&n, sizeof(n), h);
+}
+
+}  // namespace
+
+extern "C" int imodel_swm_test_layout_digest(const imodel_swm_mesh *m, int32_t scheme,
+                                             int32_t nthreads, uint64_t *digest) {
+  if (!m || !digest || nthreads < 0) return IMODEL_SWM_EINVAL;
+#ifdef _OPENMP
+  const int prev = omp_get_max_threads();
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  imodel::Layout L;
+  std::string msg;
+  try {
+    msg = imodel::build_layout(*m, nullptr, L, scheme, 0, 0.0);
+  } catch (const std::bad_alloc &) {
+    msg = "host allocation failed";
+  }
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(prev);
+#endif
+  if (!msg.empty()) return IMODEL_SWM_EINVAL;
+  uint64_t h = 1469598103934665603ull;
+#define IMODEL_DIGEST(f) h = digest_of(L.f, h);
+  IMODEL_DIGEST(cell_n2o) IMODEL_DIGEST(cell_o2n) IMODEL_DIGEST(edge_n2o) IMODEL_DIGEST(edge_o2n)
+  IMODEL_DIGEST(tri_n2o) IMODEL_DIGEST(tri_o2n) IMODEL_DIGEST(c_nnb) IMODEL_DIGEST(c_ed)
+  IMODEL_DIGEST(c_sd) IMODEL_DIGEST(c_areag) IMODEL_DIGEST(c_cellarea) IMODEL_DIGEST(c_bt)
+  IMODEL_DIGEST(c_div32) IMODEL_DIGEST(c_kew32) IMODEL_DIGEST(c_nb) IMODEL_DIGEST(c_tr)
+  IMODEL_DIGEST(c_R32) IMODEL_DIGEST(c_dg32) IMODEL_DIGEST(c_inva32) IMODEL_DIGEST(c_meta)
+  IMODEL_DIGEST(e_vs) IMODEL_DIGEST(c_pk) IMODEL_DIGEST(c_kd) IMODEL_DIGEST(e_vs2)
+  IMODEL_DIGEST(e_v) IMODEL_DIGEST(e_sh) IMODEL_DIGEST(e_leng) IMODEL_DIGEST(e_dleng)
+  IMODEL_DIGEST(e_kew) IMODEL_DIGEST(e_grad32) IMODEL_DIGEST(e_sgtg) IMODEL_DIGEST(e_gtg32)
+  IMODEL_DIGEST(e_nst) IMODEL_DIGEST(e_stk) IMODEL_DIGEST(e_stw) IMODEL_DIGEST(e_stc32)
+  IMODEL_DIGEST(t_ed) IMODEL_DIGEST(t_v) IMODEL_DIGEST(t_lt) IMODEL_DIGEST(t_kite)
+  IMODEL_DIGEST(t_areag) IMODEL_DIGEST(t_f) IMODEL_DIGEST(e_c) IMODEL_DIGEST(t_c)
+  IMODEL_DIGEST(c_p) IMODEL_DIGEST(t_apw32) IMODEL_DIGEST(t_cc32) IMODEL_DIGEST(c_apw32)
+  IMODEL_DIGEST(c_p32) IMODEL_DIGEST(t_recA) IMODEL_DIGEST(t_recB) IMODEL_DIGEST(t_recC)
+  IMODEL_DIGEST(t_c16A) IMODEL_DIGEST(t_c16B) IMODEL_DIGEST(t_c16C) IMODEL_DIGEST(t_wb)
+  IMODEL_DIGEST(t_circ32) IMODEL_DIGEST(t_kite32) IMODEL_DIGEST(t_f32) IMODEL_DIGEST(e_area)
+  IMODEL_DIGEST(t_bary) IMODEL_DIGEST(e_dist) IMODEL_DIGEST(t_edarea) IMODEL_DIGEST(e_nr)
+  IMODEL_DIGEST(e_stq) IMODEL_DIGEST(e_qw32) IMODEL_DIGEST(e_dtc32)
+#undef IMODEL_DIGEST
+  *digest = h;
+  return IMODEL_SWM_OK;
+}

@@ -269,6 +269,12 @@ int imodel_swm_learned_weights(void *handle, double *hxtr_area, double *trskw);
  * handle without a guarded learned correction.  No counterpart in the
  * reference. */
 int imodel_swm_learned_error_proxy(void *handle, double *value);
+/* Test hook with no counterpart in the reference and no GPU use: builds the
+ * device layout of mesh m for `scheme` on the host with `nthreads` threads
+ * (0 = all) and returns a 64-bit FNV-1a digest of every layout array, so
+ * that a test can show the layout does not depend on the thread count. */
+int imodel_swm_test_layout_digest(const imodel_swm_mesh *m, int32_t scheme, int32_t nthreads,
+                                  uint64_t *digest);
 /* Test hook with no counterpart in the reference: when after > 0, the
  * after-th device allocation made by any handle from now on fails with
  * IMODEL_SWM_ENOMEM as if the device were full (0 switches the injection
