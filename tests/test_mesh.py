@@ -126,3 +126,17 @@ def test_builder_reproduces_the_pinned_grids(pos, nthreads):
         want = table[f"{pos}{level}"]
         diff = sorted(k for k in want if want[k] != got.get(k))
         assert not diff, (pos, level, diff)
+
+
+def test_grid_arrays_outlive_the_grid():
+    """The Grid's arrays view the library's grid without copying it; the
+    grid is freed only when the last of them is gone."""
+    import gc
+    from imodel_gb300.mesh import meshbuild
+    g = meshbuild(3)
+    area, trskw = g.hx_areag, g.hx_trskw
+    del g
+    gc.collect()
+    assert abs(float(area.sum()) - FOURPI) < 1e-12
+    assert trskw.shape == (642, 6, 6) and np.all(np.isfinite(trskw))
+    assert area.flags.writeable
