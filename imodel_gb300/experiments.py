@@ -302,7 +302,7 @@ def exp_williamson(args, pool):
         res = {"dt": dt, "steps": n, "days": days}
         r64 = run(g, "fp64", h, u, dt, n, bt=btp, testcase=case)
         res["fp64"] = _summary(r64)
-        paths = ("fp32",) if case < 2 else ("fp32", "fp32l")
+        paths = ("fp32",) if case < 2 else ("fp32", "fp32w", "fp32l")
         for path in paths:
             r = run(g, path, h, u, dt, n, bt=btp, testcase=case,
                     params=_params(args) if path == "fp32l" else None)
@@ -313,6 +313,32 @@ def exp_williamson(args, pool):
         if case == 1:
             res["fp64"]["h_vs_exact"] = rel_errors(r64["h"], h, g.hx_areag)
         out[f"case{case}"] = res
+    return out
+
+
+def exp_case2(args, pool):
+    """Williamson case 2 (a steady flow with a known answer, swm.f90:1205-1326)
+    at levels 5 to args.level (default 9) for args.days (default 5), plain
+    FP32 TRSK against FP32 with the learned TRSK weights: h and u errors
+    against the initial (exact) state.  The network was fitted on levels 5
+    and 6 only.  dt = 900 s at level 5, halved per level."""
+    from . import swm
+    from .mesh import meshbuild
+    days = args.days or 5.0
+    out = {"days": days}
+    for lvl in range(5, (args.level or 9) + 1):
+        g = meshbuild(lvl, device=0)
+        h, u = swm.initialize_fields_tc2(g)
+        dt = 900.0 * 2.0 ** (5 - lvl)
+        n = swm.ntime_for(days, dt)
+        row = {"dt": dt, "steps": n}
+        for path in ("fp32", "fp32w"):
+            r = run(g, path, h, u, dt, n)
+            row[path] = dict(_summary(r), h_err=rel_errors(r["h"], h, g.hx_areag),
+                             u_err=rel_errors(r["u"], u, _edge_w(g)))
+        row["h_l2_ratio"] = row["fp32"]["h_err"]["l2"] / row["fp32w"]["h_err"]["l2"]
+        row["u_l2_ratio"] = row["fp32"]["u_err"]["l2"] / row["fp32w"]["u_err"]["l2"]
+        out[f"level{lvl}"] = row
     return out
 
 
@@ -388,7 +414,7 @@ def exp_mesh(args, pool):
     return out
 
 
-RUNS = {"tc2": exp_tc2, "mesh": exp_mesh, "schemes": exp_schemes, "williamson": exp_williamson, "balanced": exp_balanced, "ensemble": exp_ensemble,
+RUNS = {"tc2": exp_tc2, "mesh": exp_mesh, "schemes": exp_schemes, "case2": exp_case2, "williamson": exp_williamson, "balanced": exp_balanced, "ensemble": exp_ensemble,
         "mountains": exp_mountains, "fixed": exp_fixed, "large": exp_large}
 
 
