@@ -32,6 +32,8 @@ bottom).  One "step" is one RK4 time step of the whole grid.
              model
   cpu_baseline  the CPU oracle (C++ restatement of the Fortran, OpenMP on
              all host threads) on a bounded sample of the same workload
+  setup      seconds to build the grid (host threads; geometry on the GPU)
+             and to create each path's handle (layout, learned weights)
 
 ``--impl reference`` times that CPU implementation alone and prints its line.
 Run under torchrun for N GPUs: each rank advances its own replica (no data
@@ -407,13 +409,20 @@ def main():
     from imodel_gb300 import _build, learned, swm
     from imodel_gb300.mesh import meshbuild
     _build.build_all()
+    t_set = time.perf_counter()
     g = meshbuild(args.level)
+    setup = {"level": args.level, "mesh_host_s": time.perf_counter() - t_set}
     # the state is computed by a process pool before this process touches
     # the GPU
     h, u = bench_state(g, max(1, (os.cpu_count() or 1) // max(ws, 1)))
     cr = Cudart()
     assert cr.lib.cudaSetDevice(local) == 0
     D = Dist(local)
+    # the same grid with its geometry built on the GPU (timed only)
+    t_set = time.perf_counter()
+    meshbuild(args.level, device=local)
+    setup["mesh_gpu_s"] = time.perf_counter() - t_set
+    setup["create_s"] = {}
 
     from imodel_gb300 import learned_weights
     params_n = learned.trained_params()
@@ -430,9 +439,11 @@ def main():
     paths = [p for p in args.precisions.split(",") if p]
     headline = "fp32l" if "fp32l" in paths else "fp32"
     for path in paths:
+        t_set = time.perf_counter()
         m = swm.SWM(g, precision="fp64" if path == "fp64" else "fp32", device=local,
                     learned_params=params_n if path == "fp32n" else None,
                     learned_weights=params_w if path == "fp32l" else None)
+        setup["create_s"][path] = time.perf_counter() - t_set
         m.set_state(h, u)
         if args.apvm > 0 and path not in ("fp32l", "fp32n"):
             m.set_apvm(args.apvm, DT)
@@ -563,6 +574,7 @@ def main():
             "e2e": e2e_line(rh),
             "gpu_launches": rh["launches"],
             "clocks": rh["clocks"],
+            "setup": setup,
         }
         if "fp32" in results and headline != "fp32":
             line["fp32_plain"] = {"value": rate(results["fp32"]), "unit": UNIT,
