@@ -507,8 +507,9 @@ def main():
             and results[headline]["prof"])
     if rank == 0 and not full:
         # profiler runs: a short line with the timed paths only
-        print(json.dumps({k: {"ms_per_step": v["ms"] / args.steps} for k, v in results.items()
-                          if k in ("fp32", "fp32l", "fp32n", "fp64")}))
+        short = {k: {"ms_per_step": v["ms"] / args.steps} for k, v in results.items()
+                 if k in ("fp32", "fp32l", "fp32n", "fp64")}
+        print(json.dumps(dict(short, setup=setup)))
     elif rank == 0:
         rh, r64 = results[headline], results["fp64"]
         total_cells = g.nv * ws
