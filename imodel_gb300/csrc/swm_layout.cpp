@@ -6,6 +6,9 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 namespace imodel {
 namespace {
@@ -50,35 +53,65 @@ uint32_t quant(double x, int b) {
 // n2o: the indices 0..n-1 in the order of their keys, equal keys in index
 // order (the order std::stable_sort gives), by a least-significant-digit
 // radix sort of (key, index) pairs, 8-bit digits, skipping the digits that
-// are the same in every key; o2n its inverse
+// are the same in every key; o2n its inverse.  Each pass runs on host
+// threads: every thread counts the digits of its own contiguous chunk, a
+// prefix over (digit, thread) gives each thread its output positions, and
+// each thread moves its chunk in order, so the pass stays stable.
 template <class Key>
 void sort_perm(std::vector<int32_t> &n2o, std::vector<int32_t> &o2n, const std::vector<Key> &key) {
-  const size_t n = key.size();
-  std::vector<Key> ka(key), kb(n);
-  std::vector<int32_t> ia(n), ib(n);
-  std::iota(ia.begin(), ia.end(), 0);
+  const int64_t n = static_cast<int64_t>(key.size());
+  std::vector<Key> ka(key), kb(key.size());
+  std::vector<int32_t> ia(key.size()), ib(key.size());
   Key any = 0, all = static_cast<Key>(~Key(0));
-  for (size_t i = 0; i < n; ++i) {
+#pragma omp parallel for schedule(static) reduction(| : any) reduction(& : all)
+  for (int64_t i = 0; i < n; ++i) {
+    ia[i] = static_cast<int32_t>(i);
     any |= key[i];
     all &= key[i];
   }
+#ifdef _OPENMP
+  const int tmax = omp_get_max_threads();
+#else
+  const int tmax = 1;
+#endif
+  std::vector<int64_t> cnt(static_cast<size_t>(tmax) * 256);
   for (int shift = 0; shift < static_cast<int>(8 * sizeof(Key)); shift += 8) {
     if ((((any ^ all) >> shift) & 0xFF) == 0) continue;
-    size_t cnt[257] = {0};
-    for (size_t i = 0; i < n; ++i) ++cnt[((ka[i] >> shift) & 0xFF) + 1];
-    for (int d = 0; d < 256; ++d) cnt[d + 1] += cnt[d];
-    for (size_t i = 0; i < n; ++i) {
-      const size_t to = cnt[(ka[i] >> shift) & 0xFF]++;
-      kb[to] = ka[i];
-      ib[to] = ia[i];
+#pragma omp parallel num_threads(tmax)
+    {
+#ifdef _OPENMP
+      const int t = omp_get_thread_num(), nth = omp_get_num_threads();
+#else
+      const int t = 0, nth = 1;
+#endif
+      const int64_t lo = n * t / nth, hi = n * (t + 1) / nth;
+      int64_t *c = &cnt[static_cast<size_t>(t) * 256];
+      for (int d = 0; d < 256; ++d) c[d] = 0;
+      for (int64_t i = lo; i < hi; ++i) ++c[(ka[i] >> shift) & 0xFF];
+#pragma omp barrier
+#pragma omp single
+      {
+        int64_t acc = 0;
+        for (int d = 0; d < 256; ++d)
+          for (int u = 0; u < nth; ++u) {
+            const int64_t v = cnt[static_cast<size_t>(u) * 256 + d];
+            cnt[static_cast<size_t>(u) * 256 + d] = acc;
+            acc += v;
+          }
+      }
+      for (int64_t i = lo; i < hi; ++i) {
+        const int64_t to = c[(ka[i] >> shift) & 0xFF]++;
+        kb[to] = ka[i];
+        ib[to] = ia[i];
+      }
     }
     ka.swap(kb);
     ia.swap(ib);
   }
   n2o.swap(ia);
-  o2n.resize(n);
+  o2n.resize(key.size());
 #pragma omp parallel for schedule(static)
-  for (int64_t i = 0; i < static_cast<int64_t>(n); ++i) o2n[n2o[i]] = static_cast<int32_t>(i);
+  for (int64_t i = 0; i < n; ++i) o2n[n2o[i]] = static_cast<int32_t>(i);
 }
 
 // body(i) for i in [0, n) on host threads; body returns "" or an error
@@ -961,9 +994,6 @@ void apply_kite_outputs(const imodel_swm_mesh &m, const KiteInputs &K, const flo
 }  // namespace imodel
 
 // ---- test hook: a digest of the whole layout ---------------------------------
-#ifdef _OPENMP
-#include <omp.h>
-#endif
 
 namespace {
 
