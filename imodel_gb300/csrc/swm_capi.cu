@@ -855,8 +855,8 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
     H->w_learned = {M.e_stw, M.e_stc32, M.c_R32, M.c_pk};
     if (H->precision == IMODEL_SWM_FP32) {
       // the guard's fallback: the plain scheme's weight-dependent arrays
-      Layout Lp;
-      msg = build_layout(*m, o ? o->bt : nullptr, Lp, scheme, fsphere, fcte);
+      WeightArrays Lp;
+      msg = build_weight_arrays(*m, L, Lp);
       if (!msg.empty()) return set_error(H, IMODEL_SWM_EINVAL, msg);
       const int32_t *pk = nullptr;
       if ((rc = upload(H, Lp.e_stw, &H->w_plain.e_stw)) ||

@@ -885,6 +885,65 @@ std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, Lear
   });
 }
 
+std::string build_weight_arrays(const imodel_swm_mesh &m, const Layout &L, WeightArrays &W) {
+  const int nv = L.nv, ne = L.ne;
+  const size_t NV = nv, NE = ne;
+  if (m.nv != nv || m.ne != ne) return "mesh sizes differ from the layout's";
+  W.e_stw.assign(kMaxSt * NE, 0.0);
+  W.e_stc32.assign(kMaxSt * NE, 0.0f);
+  // the TRSK stencil slots in build_layout's order (cells ed%v(1), ed%v(2),
+  // each ccw, the edge's own slot left out)
+  std::string err = par_for(ne, [&](int64_t i64) -> std::string {
+    const int i = static_cast<int>(i64);
+    const int e = L.edge_n2o[i];
+    const double l = m.ed_leng[e];
+    int ns = 0;
+    for (int s = 0; s < 2; ++s) {
+      const int node = m.ed_v[2 * static_cast<size_t>(e) + s] - 1;
+      const int n = m.nnb[node];
+      int edcelli = -1;
+      for (int j = 0; j < n; ++j)
+        if (m.v_ed[6 * static_cast<size_t>(node) + j] - 1 == e) {
+          edcelli = j;
+          break;
+        }
+      if (edcelli < 0) return "edge " + std::to_string(e + 1) + " missing from its cell's edge list";
+      for (int j = 0; j < n; ++j) {
+        if (j == edcelli) continue;
+        const int k = m.v_ed[6 * static_cast<size_t>(node) + j] - 1;
+        if (ns >= kMaxSt || L.e_stk[ns * NE + i] != L.edge_o2n[k])
+          return "the mesh's stencil differs from the layout's at edge " + std::to_string(e + 1);
+        const double sc = std::copysign(
+            1.0, 1.0 * m.hx_ttgout[6 * static_cast<size_t>(node) + j] *
+                     m.hx_tnrccw[6 * static_cast<size_t>(node) + edcelli]);
+        const double w = m.hx_trskw[36 * static_cast<size_t>(node) + 6 * static_cast<size_t>(j) + edcelli];
+        W.e_stw[ns * NE + i] = w * sc;
+        W.e_stc32[ns * NE + i] = static_cast<float>(0.5 * w * sc * m.edhx_leng[k] / l);
+        ++ns;
+      }
+    }
+    return std::string();
+  });
+  if (!err.empty()) return err;
+  W.c_R32.assign(kMaxNb * NV, 0.0f);
+  W.c_pk = L.c_pk;
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < nv; ++i) {
+    const int c = L.cell_n2o[i];
+    const int n = m.nnb[c];
+    for (int j = 0; j < n; ++j)
+      W.c_R32[j * NV + i] = static_cast<float>(m.hx_hxtr_area[6 * static_cast<size_t>(c) + j]);
+    for (int j = 0; j < kMaxNb; ++j) {
+      const int src = j < n ? j : 0;
+      const float r = j < n ? W.c_R32[src * NV + i] : 0.0f;
+      int32_t rb;
+      std::memcpy(&rb, &r, sizeof(rb));
+      W.c_pk[4 * (static_cast<size_t>(j) * NV + i) + 3] = rb;
+    }
+  }
+  return "";
+}
+
 // ---- learned TRSK weights ----------------------------------------------------
 std::string build_kite_inputs(const imodel_swm_mesh &m, KiteInputs &K) {
   const int nv = m.nv;

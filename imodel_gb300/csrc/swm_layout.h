@@ -167,6 +167,17 @@ struct LearnedLayout {
 };
 std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, LearnedLayout &LL);
 
+// The arrays of a trsk10 layout that depend on the TRSK weights and kite
+// fractions (e_stw, e_stc32, c_R32, c_pk), for mesh m whose topology and
+// node positions are those L was built from (so L's orderings hold): what
+// build_layout would give for m, without building the rest again.
+struct WeightArrays {
+  std::vector<double> e_stw;
+  std::vector<float> e_stc32, c_R32;
+  std::vector<int32_t> c_pk;
+};
+std::string build_weight_arrays(const imodel_swm_mesh &m, const Layout &L, WeightArrays &W);
+
 // float -> BF16 bit pattern, round to nearest, ties to even
 uint16_t bf16_bits(float v);
 
