@@ -119,8 +119,8 @@ constexpr int kProxySteps = 256;
     }                                                                             \
   } while (0)
 
-template <class V>
-int upload(Handle *H, const std::vector<V> &v, const V **dst) {
+template <class V, class A>
+int upload(Handle *H, const std::vector<V, A> &v, const V **dst) {
   if (v.empty()) {
     *dst = nullptr;
     return IMODEL_SWM_OK;

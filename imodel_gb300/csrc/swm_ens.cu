@@ -229,8 +229,8 @@ int fail(Ens *E, int code, const std::string &m) {
                   std::string(#call) + ": " + cudaGetErrorString(e_));             \
   } while (0)
 
-template <class V>
-int up(Ens *E, const std::vector<V> &v, const V **dst) {
+template <class V, class A>
+int up(Ens *E, const std::vector<V, A> &v, const V **dst) {
   void *p = nullptr;
   EK(cudaMalloc(&p, (v.empty() ? 1 : v.size()) * sizeof(V)));
   E->allocs.push_back(p);

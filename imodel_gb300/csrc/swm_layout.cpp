@@ -57,11 +57,11 @@ uint32_t quant(double x, int b) {
 // threads: every thread counts the digits of its own contiguous chunk, a
 // prefix over (digit, thread) gives each thread its output positions, and
 // each thread moves its chunk in order, so the pass stays stable.
-template <class Key>
-void sort_perm(std::vector<int32_t> &n2o, std::vector<int32_t> &o2n, const std::vector<Key> &key) {
+template <class Key, class V>
+void sort_perm(V &n2o, V &o2n, const std::vector<Key> &key) {
   const int64_t n = static_cast<int64_t>(key.size());
-  std::vector<Key> ka(key), kb(key.size());
-  std::vector<int32_t> ia(key.size()), ib(key.size());
+  HVec<Key> ka(key.begin(), key.end()), kb(key.size());
+  V ia(key.size()), ib(key.size());
   Key any = 0, all = static_cast<Key>(~Key(0));
 #pragma omp parallel for schedule(static) reduction(| : any) reduction(& : all)
   for (int64_t i = 0; i < n; ++i) {
@@ -133,6 +133,17 @@ std::string par_for(int64_t n, F body) {
     }
   }
   return msg;
+}
+
+// v = n copies of x, filled on host threads
+template <class V, class T>
+void fill(V &v, size_t n, T x) {
+  v.resize(n);
+  const int64_t m = static_cast<int64_t>(n);
+  typename V::value_type *d = v.data();
+  const typename V::value_type y = static_cast<typename V::value_type>(x);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < m; ++i) d[i] = y;
 }
 
 // tr%c%p of triangle t (0-based): the unit normal of the plane through its
@@ -259,7 +270,7 @@ void scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
       for (int s = 0; s < 3; ++s) L.t_kite32[s * NT + i] = static_cast<float>(w[s]);
     }
     // q_e from the edge's two triangles
-    L.e_qw32.assign(2 * NE, 0.0f);
+    fill(L.e_qw32, 2 * NE, 0.0f);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < ne; ++i) {
       double a, b;
@@ -303,7 +314,7 @@ void scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
     }
   }
   if (scheme == IMODEL_SWM_DTRED) {
-    L.e_dtc32.assign(6 * NE, 0.0f);
+    fill(L.e_dtc32, 6 * NE, 0.0f);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < ne; ++i) {
       const double d1 = L.e_dist[i], d2 = L.e_dist[NE + i];
@@ -419,18 +430,18 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
 
   // --- cells ----------------------------------------------------------
   const size_t NV = nv, NE = ne, NT = nt;
-  L.c_nnb.assign(NV, 0);
-  L.c_ed.assign(kMaxNb * NV, -1);
-  L.c_sd.assign(kMaxNb * NV, 0.0);
-  L.c_div32.assign(kMaxNb * NV, 0.0f);
-  L.c_kew32.assign(kMaxNb * NV, 0.0f);
+  fill(L.c_nnb, NV, 0);
+  fill(L.c_ed, kMaxNb * NV, -1);
+  fill(L.c_sd, kMaxNb * NV, 0.0);
+  fill(L.c_div32, kMaxNb * NV, 0.0f);
+  fill(L.c_kew32, kMaxNb * NV, 0.0f);
   L.c_areag.resize(NV);
   L.c_cellarea.resize(NV);
-  L.c_bt.assign(NV, 0.0);
-  L.c_nb.assign(kMaxNb * NV, 0);
-  L.c_tr.assign(kMaxNb * NV, 0);
-  L.c_R32.assign(kMaxNb * NV, 0.0f);
-  L.c_dg32.assign(kMaxNb * NV, 0.0f);
+  fill(L.c_bt, NV, 0.0);
+  fill(L.c_nb, kMaxNb * NV, 0);
+  fill(L.c_tr, kMaxNb * NV, 0);
+  fill(L.c_R32, kMaxNb * NV, 0.0f);
+  fill(L.c_dg32, kMaxNb * NV, 0.0f);
   L.c_inva32.resize(NV);
   L.c_meta.resize(NV);
   if (nv >= (1 << 28)) return "more than 2^28 cells";
@@ -498,12 +509,12 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
   L.e_grad32.resize(NE);
   L.e_sgtg.resize(NE);
   L.e_gtg32.resize(NE);
-  L.e_nst.assign(NE, 0);
-  L.e_stk.assign(kMaxSt * NE, 0);
-  L.e_stw.assign(kMaxSt * NE, 0.0);
-  L.e_stc32.assign(kMaxSt * NE, 0.0f);
-  if (scheme == IMODEL_SWM_GASS18) L.e_stq.assign(kMaxSt * NE, -1);
-  L.e_vs.assign(2 * NE, 0u);
+  fill(L.e_nst, NE, 0);
+  fill(L.e_stk, kMaxSt * NE, 0);
+  fill(L.e_stw, kMaxSt * NE, 0.0);
+  fill(L.e_stc32, kMaxSt * NE, 0.0f);
+  if (scheme == IMODEL_SWM_GASS18) fill(L.e_stq, kMaxSt * NE, -1);
+  fill(L.e_vs, 2 * NE, 0u);
   err = par_for(ne, [&](int64_t i64) -> std::string {
     const int i = static_cast<int>(i64);
     const int e = L.edge_n2o[i];
@@ -571,8 +582,8 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
   if (!err.empty()) return err;
 
   // packed cell slots and edge cell words for vector loads
-  L.c_pk.assign(kMaxNb * NV * 4, 0);
-  L.c_kd.assign(kMaxNb * NV * 2, 0.0f);
+  fill(L.c_pk, kMaxNb * NV * 4, 0);
+  fill(L.c_kd, kMaxNb * NV * 2, 0.0f);
 #pragma omp parallel for schedule(static)
   for (int i = 0; i < nv; ++i) {
     const int n = L.c_nnb[i];
@@ -646,8 +657,8 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < nv; ++i)
       for (int k = 0; k < 3; ++k) L.c_p[k * NV + i] = m.v_p[3 * static_cast<size_t>(L.cell_n2o[i]) + k];
-    L.t_apw32.assign(9 * NT, 0.0f);
-    L.t_cc32.assign(3 * NT, 0.0f);
+    fill(L.t_apw32, 9 * NT, 0.0f);
+    fill(L.t_cc32, 3 * NT, 0.0f);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < nt; ++i) {
       const int t = L.tri_n2o[i];
@@ -661,8 +672,8 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
       }
       for (int k = 0; k < 3; ++k) L.t_cc32[k * NT + i] = static_cast<float>(L.t_c[k * NT + i]);
     }
-    L.c_apw32.assign(18 * NV, 0.0f);
-    L.c_p32.assign(3 * NV, 0.0f);
+    fill(L.c_apw32, 18 * NV, 0.0f);
+    fill(L.c_p32, 3 * NV, 0.0f);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < nv; ++i) {
       const int c = L.cell_n2o[i];
@@ -757,10 +768,10 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
   {
     // 16-bit triangle records: bases per warp of 32 triangles
     const size_t nw = (NT + 31) / 32;
-    L.t_c16A.assign(4 * NT, 0u);
-    L.t_c16B.assign(4 * NT, 0.0f);
-    L.t_c16C.assign(2 * NT, 0.0f);
-    L.t_wb.assign(2 * nw, 0);
+    fill(L.t_c16A, 4 * NT, 0u);
+    fill(L.t_c16B, 4 * NT, 0.0f);
+    fill(L.t_c16C, 2 * NT, 0.0f);
+    fill(L.t_wb, 2 * nw, 0);
 #pragma omp parallel for schedule(static)
     for (size_t w = 0; w < nw; ++w) {
       const size_t t0 = 32 * w, t1 = std::min(NT, t0 + 32);
@@ -824,7 +835,7 @@ std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, Lear
   const int ne = m.ne;
   constexpr int T = LearnedLayout::kTile;
   LL.ntiles = (static_cast<int64_t>(ne) + T - 1) / T;
-  LL.blocks.assign(static_cast<size_t>(LL.ntiles) * LearnedLayout::kBlockBytes, 0);
+  fill(LL.blocks, static_cast<size_t>(LL.ntiles) * LearnedLayout::kBlockBytes, 0);
   // entry k of array `off` (element size `sz`) in the block of device edge i
   auto at = [&](int64_t i, int off, int k, int sz) -> uint8_t * {
     return LL.blocks.data() + (i / T) * LearnedLayout::kBlockBytes + off +
@@ -889,8 +900,8 @@ std::string build_weight_arrays(const imodel_swm_mesh &m, const Layout &L, Weigh
   const int nv = L.nv, ne = L.ne;
   const size_t NV = nv, NE = ne;
   if (m.nv != nv || m.ne != ne) return "mesh sizes differ from the layout's";
-  W.e_stw.assign(kMaxSt * NE, 0.0);
-  W.e_stc32.assign(kMaxSt * NE, 0.0f);
+  fill(W.e_stw, kMaxSt * NE, 0.0);
+  fill(W.e_stc32, kMaxSt * NE, 0.0f);
   // the TRSK stencil slots in build_layout's order (cells ed%v(1), ed%v(2),
   // each ccw, the edge's own slot left out)
   std::string err = par_for(ne, [&](int64_t i64) -> std::string {
@@ -925,7 +936,7 @@ std::string build_weight_arrays(const imodel_swm_mesh &m, const Layout &L, Weigh
     return std::string();
   });
   if (!err.empty()) return err;
-  W.c_R32.assign(kMaxNb * NV, 0.0f);
+  fill(W.c_R32, kMaxNb * NV, 0.0f);
   W.c_pk = L.c_pk;
 #pragma omp parallel for schedule(static)
   for (int i = 0; i < nv; ++i) {
@@ -1064,9 +1075,9 @@ uint64_t fnv1a(const void *p, size_t n, uint64_t h) {
   }
   return h;
 }
-template <class T>
-uint64_t digest_of(const std::vector<T> &v, uint64_t h) {
-  h = fnv1a(v.data(), v.size() * sizeof(T), h);
+template <class V>
+uint64_t digest_of(const V &v, uint64_t h) {
+  h = fnv1a(v.data(), v.size() * sizeof(typename V::value_type), h);
   const uint64_t n = v.size();
   return fnv1a(&n, sizeof(n), h);
 }

@@ -17,12 +17,38 @@
 //    coefficient computed in FP64 and rounded once.
 #pragma once
 #include <cstdint>
+#include <memory>
+#include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "imodel_swm.h"
 
 namespace imodel {
+
+// An allocator whose resize() leaves new elements uninitialised: the layout
+// builder writes every element of the arrays it resizes and fills the
+// padded ones in parallel, so the serial zero-filling of a level-10 layout's
+// ~15 GB is skipped.  assign(n, v) still fills.
+template <class T>
+struct HostAlloc : std::allocator<T> {
+  using std::allocator<T>::allocator;
+  template <class U>
+  struct rebind {
+    using other = HostAlloc<U>;
+  };
+  template <class U>
+  void construct(U *p) noexcept {
+    ::new (static_cast<void *>(p)) U;
+  }
+  template <class U, class... A>
+  void construct(U *p, A &&...a) {
+    ::new (static_cast<void *>(p)) U(std::forward<A>(a)...);
+  }
+};
+template <class T>
+using HVec = std::vector<T, HostAlloc<T>>;
 
 constexpr int kMaxNb = 6;     // cells have 5 or 6 edges on icosahedral grids
 constexpr int kMaxSt = 10;    // TRSK stencil: nnb(c1) + nnb(c2) - 2 <= 10
@@ -32,82 +58,82 @@ struct Layout {
   double erad = 0, grav = 0, omega = 0;
 
   // permutations (new index -> reference index, 0-based) and inverses
-  std::vector<int32_t> cell_n2o, cell_o2n, edge_n2o, edge_o2n, tri_n2o, tri_o2n;
+  HVec<int32_t> cell_n2o, cell_o2n, edge_n2o, edge_o2n, tri_n2o, tri_o2n;
 
   // cells, slot-major [kMaxNb][nv]
-  std::vector<int8_t> c_nnb;                 // [nv]
-  std::vector<int32_t> c_ed;                 // edge of slot j (-1 pad)
-  std::vector<double> c_sd;                  // ttgout * edhx%leng of slot j
-  std::vector<double> c_areag;               // [nv] hx%areag
-  std::vector<double> c_cellarea;            // [nv] sum_j 0.25*l*d (KE tiled area)
-  std::vector<double> c_bt;                  // [nv] bottom topography
-  std::vector<float> c_div32;                // ttgout*d/(A*erad)
-  std::vector<float> c_kew32;                // 0.25*l*d / cell_area
+  HVec<int8_t> c_nnb;                 // [nv]
+  HVec<int32_t> c_ed;                 // edge of slot j (-1 pad)
+  HVec<double> c_sd;                  // ttgout * edhx%leng of slot j
+  HVec<double> c_areag;               // [nv] hx%areag
+  HVec<double> c_cellarea;            // [nv] sum_j 0.25*l*d (KE tiled area)
+  HVec<double> c_bt;                  // [nv] bottom topography
+  HVec<float> c_div32;                // ttgout*d/(A*erad)
+  HVec<float> c_kew32;                // 0.25*l*d / cell_area
   // cell-centred TRSK variant (FP32): the PV flux of an edge is assembled
   // from the two cells' kite fractions instead of a 10-entry edge stencil
-  std::vector<int32_t> c_nb;                 // neighbour cell across slot j
-  std::vector<int32_t> c_tr;                 // triangle v%tr(j) (edges j, j+1)
-  std::vector<float> c_R32;                  // kite fraction hxtr_area(j)
-  std::vector<float> c_dg32;                 // ttgout(j) * edhx%leng(j)
-  std::vector<float> c_inva32;               // [nv] 1/(A*erad)
-  std::vector<uint32_t> c_meta;              // [nv] nnb | tnrccw<0 bits << 8
-  std::vector<uint32_t> e_vs;                // [2][ne] cell | slot << 28
+  HVec<int32_t> c_nb;                 // neighbour cell across slot j
+  HVec<int32_t> c_tr;                 // triangle v%tr(j) (edges j, j+1)
+  HVec<float> c_R32;                  // kite fraction hxtr_area(j)
+  HVec<float> c_dg32;                 // ttgout(j) * edhx%leng(j)
+  HVec<float> c_inva32;               // [nv] 1/(A*erad)
+  HVec<uint32_t> c_meta;              // [nv] nnb | tnrccw<0 bits << 8
+  HVec<uint32_t> e_vs;                // [2][ne] cell | slot << 28
   // the same per-slot data packed for 16-byte loads, slot-major [6][nv]:
   // {edge, neighbour, triangle, kite fraction bits} and {KE weight,
   // ttgout*d}; unused slots of pentagons repeat slot 0 with zero weights
-  std::vector<int32_t> c_pk;                 // [6][nv][4]
-  std::vector<float> c_kd;                   // [6][nv][2]
-  std::vector<uint32_t> e_vs2;               // [ne][2] both cell words of an edge
+  HVec<int32_t> c_pk;                 // [6][nv][4]
+  HVec<float> c_kd;                   // [6][nv][2]
+  HVec<uint32_t> e_vs2;               // [ne][2] both cell words of an edge
 
   // edges [ne] and [2][ne]
-  std::vector<int32_t> e_v;                  // [2][ne] cells (ed%v = edhx%sh)
-  std::vector<int32_t> e_sh;                 // [2][ne] triangles (ed%sh)
-  std::vector<double> e_leng;                // ed%leng
-  std::vector<double> e_dleng;               // edhx%leng
-  std::vector<double> e_kew;                 // 0.25*l*d (KE weight, FP64)
-  std::vector<float> e_grad32;               // 1/(l*erad)
+  HVec<int32_t> e_v;                  // [2][ne] cells (ed%v = edhx%sh)
+  HVec<int32_t> e_sh;                 // [2][ne] triangles (ed%sh)
+  HVec<double> e_leng;                // ed%leng
+  HVec<double> e_dleng;               // edhx%leng
+  HVec<double> e_kew;                 // 0.25*l*d (KE weight, FP64)
+  HVec<float> e_grad32;               // 1/(l*erad)
   // grad_ed_tg (swm_operators.f90:738-777, HTC): sign of ed%nr . (c2 - c1)
   // for the circumcentres c1, c2 of ed%sh(1), ed%sh(2), and the FP32 factor
   // sign / (edhx%leng * erad); used by the (hyper)diffusion terms
-  std::vector<double> e_sgtg;
-  std::vector<float> e_gtg32;
-  std::vector<int8_t> e_nst;                 // stencil length
-  std::vector<int32_t> e_stk;                // [kMaxSt][ne] stencil edges
-  std::vector<double> e_stw;                 // [kMaxSt][ne] trskw * signcor
-  std::vector<float> e_stc32;                // [kMaxSt][ne] 0.5*w*s*d_k/l_e
+  HVec<double> e_sgtg;
+  HVec<float> e_gtg32;
+  HVec<int8_t> e_nst;                 // stencil length
+  HVec<int32_t> e_stk;                // [kMaxSt][ne] stencil edges
+  HVec<double> e_stw;                 // [kMaxSt][ne] trskw * signcor
+  HVec<float> e_stc32;                // [kMaxSt][ne] 0.5*w*s*d_k/l_e
 
   // triangles, slot-major [3][nt]
-  std::vector<int32_t> t_ed, t_v;
-  std::vector<double> t_lt;                  // ed%leng * tr%tg
-  std::vector<double> t_kite;                // tr%trhx_area
-  std::vector<double> t_areag;               // [nt]
-  std::vector<double> t_f;                   // [nt] 2*omega*sin(lat_c)
+  HVec<int32_t> t_ed, t_v;
+  HVec<double> t_lt;                  // ed%leng * tr%tg
+  HVec<double> t_kite;                // tr%trhx_area
+  HVec<double> t_areag;               // [nt]
+  HVec<double> t_f;                   // [nt] 2*omega*sin(lat_c)
   // APVM points, [3][n] in device order, empty without ed%nr: ed%c%p, the
   // circumcentre direction of each triangle (circumcentre()), v%p
-  std::vector<double> e_c, t_c, c_p;
+  HVec<double> e_c, t_c, c_p;
   // the FP32 step's APVM weights: per triangle slot s and component k,
   // t_apw32[(3s+k)][nt] = -tr%tg (ed%c%p - tr%c%p)_k ed%leng / tr%areag,
   // per cell slot j, c_apw32[(3j+k)][nv] = ttgout (ed%c%p - v%p)_k
   // edhx%leng / hx%areag (0 in a pentagon's sixth slot); the unit vectors
   // t_cc32 [3][nt] and c_p32 [3][nv] for the tangent-plane projections
-  std::vector<float> t_apw32, t_cc32, c_apw32, c_p32;
+  HVec<float> t_apw32, t_cc32, c_apw32, c_p32;
   // a triangle's FP32 stage inputs as three 16-byte records, [nt] each:
   //   A {edge 0, edge 1, edge 2, cell 0}  B {cell 1, cell 2, circ 0, circ 1}
   //   C {circ 2, kite 0, kite 1, kite 2}  (circ, kite: FP32 bit patterns)
-  std::vector<int32_t> t_recA, t_recB, t_recC;
+  HVec<int32_t> t_recA, t_recB, t_recC;
   // the same with 16-bit indices against per-warp bases t_wb [nwarps][2] =
   // {edge, cell} (cell = -1: the warp keeps the 32-bit records):
   //   A {e0 | e1 << 16, e2 | c0 << 16, c1 | c2 << 16, circ 0}
   //   B {circ 1, circ 2, kite 0, kite 1}  C {kite 2, f}
-  std::vector<uint32_t> t_c16A;
-  std::vector<float> t_c16B, t_c16C;
-  std::vector<int32_t> t_wb;
-  std::vector<float> t_circ32;               // l*tg/(A*erad)
-  std::vector<float> t_kite32;               // kite/A
-  std::vector<float> t_f32;
+  HVec<uint32_t> t_c16A;
+  HVec<float> t_c16B, t_c16C;
+  HVec<int32_t> t_wb;
+  HVec<float> t_circ32;               // l*tg/(A*erad)
+  HVec<float> t_kite32;               // kite/A
+  HVec<float> t_f32;
 
   // per-edge reference-ordered weight for edge integrals: l*d*0.5
-  std::vector<double> e_area;
+  HVec<double> e_area;
 
   // the geometry of the other method wrappers (FP64, device order; empty for
   // trsk10), as initialize_gridprop precomputes it (swm.f90:1005-1028):
@@ -121,8 +147,8 @@ struct Layout {
   //           gethxedgeconnection(e, k) (smeshpack.f90:4174-4244) whose PV the
   //           gass Coriolis term takes, or -1 for the TRSK average (gass18)
   //   e_nr    [3][ne] ed%nr (pered, dtred)
-  std::vector<double> t_bary, e_dist, t_edarea, e_nr;
-  std::vector<int32_t> e_stq;
+  HVec<double> t_bary, e_dist, t_edarea, e_nr;
+  HVec<int32_t> e_stq;
   // ... and their FP32 forms for the FP32 step (variant 0), each constant
   // factor folded in FP64 and rounded once:
   //   t_kite32 holds the depth weights of the triangle's vertices instead of
@@ -139,7 +165,7 @@ struct Layout {
   //   e_dtc32 [6][ne] (dtred) per triangle i of the edge and its edge slot s,
   //           -w_i sign(tr%tg) l_s (tr%c x ed(s)%c) . nr_e / tr%areag, w_i =
   //           d2, d1 over d1 + d2: the PV flux is sum q_i c_is F_s
-  std::vector<float> e_qw32, e_dtc32;
+  HVec<float> e_qw32, e_dtc32;
 };
 
 // Builds the layout from a reference mesh; returns "" or an error message.
@@ -163,7 +189,7 @@ struct LearnedLayout {
   static constexpr int kTile = 128, kBlockBytes = 11264;
   static constexpr int kLst = 0, kGeo = 5120, kEsh = 9216, kEvs = 10240;
   int64_t ntiles = 0;
-  std::vector<uint8_t> blocks;  // [ntiles][kBlockBytes]
+  HVec<uint8_t> blocks;  // [ntiles][kBlockBytes]
 };
 std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, LearnedLayout &LL);
 
@@ -172,9 +198,9 @@ std::string build_learned_layout(const imodel_swm_mesh &m, const Layout &L, Lear
 // node positions are those L was built from (so L's orderings hold): what
 // build_layout would give for m, without building the rest again.
 struct WeightArrays {
-  std::vector<double> e_stw;
-  std::vector<float> e_stc32, c_R32;
-  std::vector<int32_t> c_pk;
+  HVec<double> e_stw;
+  HVec<float> e_stc32, c_R32;
+  HVec<int32_t> c_pk;
 };
 std::string build_weight_arrays(const imodel_swm_mesh &m, const Layout &L, WeightArrays &W);
 
