@@ -16,8 +16,8 @@
 // that the reference does in one serial sweep (new nodes, edges and
 // triangles in the order of the lower node, then of its neighbour list) are
 // a per-node count, a prefix sum and a fill, which gives the same numbers.
-// The geometry has a second back end on the GPU (mesh_gpu.cu,
-// imodel_mesh_build_gpu) that starts from the same topology.
+// The GPU back end (mesh_gpu.cu, imodel_mesh_build_gpu) runs the same
+// construction as kernels, numbering included.
 
 #include "imodel_mesh.h"
 #include "mesh_internal.h"
@@ -232,32 +232,50 @@ inline void setv(A &a, size_t i, const V3 &v) {
   a[3 * i + 2] = v.z;
 }
 
+// level-0 faces: triples of mutually adjacent nodes (edge = min distance),
+// counter-clockwise seen from outside
+bool level0_faces(const std::vector<V3> &P, std::vector<Tri> &tris) {
+  double dmin = 1e9;
+  for (int i = 0; i < 12; ++i)
+    for (int j = i + 1; j < 12; ++j) dmin = std::min(dmin, norm(sub(P[i], P[j])));
+  auto adj = [&](int i, int j) { return norm(sub(P[i], P[j])) < dmin * (1.0 + 1e-6); };
+  for (int i = 0; i < 12; ++i)
+    for (int j = i + 1; j < 12; ++j)
+      for (int k = j + 1; k < 12; ++k)
+        if (adj(i, j) && adj(j, k) && adj(i, k)) {
+          if (det3(P[i], P[j], P[k]) > 0)
+            tris.push_back({i, j, k});
+          else
+            tris.push_back({i, k, j});
+        }
+  return tris.size() == 20;
+}
+
 }  // namespace
 
 namespace imodel {
 namespace mesh {
 
+int level0(int pos, std::vector<double> &p, std::vector<int> &tri) {
+  const std::vector<V3> P = icosanodes0(pos);
+  std::vector<Tri> tris;
+  if (!level0_faces(P, tris)) return IMODEL_SWM_EINVAL;
+  p.resize(36);
+  for (int i = 0; i < 12; ++i) setv(p, i, P[i]);
+  tri.resize(60);
+  for (int t = 0; t < 20; ++t) {
+    tri[3 * t] = tris[t].a;
+    tri[3 * t + 1] = tris[t].b;
+    tri[3 * t + 2] = tris[t].c;
+  }
+  return IMODEL_SWM_OK;
+}
+
 int topology(int level, int pos, Topo &T) {
   // --- nodes and subdivision triangulation -----------------------------
   std::vector<V3> P = icosanodes0(pos);
-  // level-0 faces: triples of mutually adjacent nodes (edge = min distance)
   std::vector<Tri> tris;
-  {
-    double dmin = 1e9;
-    for (int i = 0; i < 12; ++i)
-      for (int j = i + 1; j < 12; ++j) dmin = std::min(dmin, norm(sub(P[i], P[j])));
-    auto adj = [&](int i, int j) { return norm(sub(P[i], P[j])) < dmin * (1.0 + 1e-6); };
-    for (int i = 0; i < 12; ++i)
-      for (int j = i + 1; j < 12; ++j)
-        for (int k = j + 1; k < 12; ++k)
-          if (adj(i, j) && adj(j, k) && adj(i, k)) {
-            if (det3(P[i], P[j], P[k]) > 0)
-              tris.push_back({i, j, k});
-            else
-              tris.push_back({i, k, j});
-          }
-    if (tris.size() != 20) return IMODEL_SWM_EINVAL;
-  }
+  if (!level0_faces(P, tris)) return IMODEL_SWM_EINVAL;
   std::vector<int> nnb, ring, off;
   auto NB = [&](int i, int j) { return ring[static_cast<size_t>(i) * 6 + j]; };
   for (int lev = 1; lev <= level; ++lev) {
@@ -805,10 +823,23 @@ int imodel_mesh_build(int32_t level, int32_t pos, int32_t nthreads, void **grid)
 
 int imodel_mesh_build_gpu(int32_t level, int32_t pos, int32_t device, void **grid) {
   g_gpu_error = "";
-  if (device < 0) return IMODEL_SWM_EINVAL;
-  return build_grid(level, pos, grid, [&](const Topo &t, Grid &g) {
-    return imodel::mesh::geometry_gpu(t, g, device, &g_gpu_error);
-  });
+  if (!grid || device < 0 || level < 0 || level > 11 || (pos != 0 && pos != 1))
+    return IMODEL_SWM_EINVAL;
+  *grid = nullptr;
+  Grid *g = new (std::nothrow) Grid();
+  if (!g) return IMODEL_SWM_ENOMEM;
+  int rc;
+  try {
+    rc = imodel::mesh::build_gpu(level, pos, device, *g, &g_gpu_error);
+  } catch (const std::bad_alloc &) {
+    rc = IMODEL_SWM_ENOMEM;
+  }
+  if (rc != IMODEL_SWM_OK) {
+    delete g;
+    return rc;
+  }
+  *grid = g;
+  return IMODEL_SWM_OK;
 }
 
 const char *imodel_mesh_gpu_last_error(void) { return g_gpu_error ? g_gpu_error : ""; }

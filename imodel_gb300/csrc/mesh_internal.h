@@ -69,6 +69,10 @@ struct Topo {
 // host threads (OpenMP).  Returns an IMODEL_SWM_* status.
 int topology(int level, int pos, Topo &t);
 
+// The 12 nodes ([12][3]) and 20 counter-clockwise faces ([20][3], 0-based)
+// of the level-0 icosahedron.  Returns an IMODEL_SWM_* status.
+int level0(int pos, std::vector<double> &p, std::vector<int> &tri);
+
 // The 1-based index arrays of g from t (host threads).
 void export_topology(const Topo &t, Grid &g);
 
@@ -79,6 +83,11 @@ void touch(void *p, size_t bytes);
 // Geometry by the GPU kernels of mesh_gpu.cu on CUDA device `device`;
 // `why` receives a message on a CUDA error.  Returns an IMODEL_SWM_* status.
 int geometry_gpu(const Topo &t, Grid &g, int device, const char **why);
+
+// The whole grid on CUDA device `device`: the topology by kernels that give
+// topology()'s numbers (and bit-identical node positions), then the
+// geometry of geometry_gpu.  Returns an IMODEL_SWM_* status.
+int build_gpu(int level, int pos, int device, Grid &g, const char **why);
 
 }  // namespace mesh
 }  // namespace imodel

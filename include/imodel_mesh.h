@@ -41,12 +41,14 @@ extern "C" {
 int imodel_mesh_build(int32_t level, int32_t pos, int32_t nthreads,
                       void **grid);
 
-/* The same grid with its geometry computed on CUDA device `device`: the
- * topology (numbering) is built on host threads as by imodel_mesh_build,
- * then one GPU kernel per meshstruct step forms every length, area, angle,
- * sign, kite fraction and TRSK weight, and the Delaunay check
- * (smeshpack.f90:706-1151, :4991-5154; interpack.f90:3978-4098).  Index
- * and sign arrays equal imodel_mesh_build's; the GPU's atan, tan, atan2 and
+/* The same grid built on CUDA device `device`: the subdivision (meshrefin,
+ * smeshpack.f90:1587-1675), the neighbour rings and meshstruct's numbering
+ * of edges and triangles (:706-862) by kernels that hand out
+ * imodel_mesh_build's numbers, then one GPU kernel per meshstruct step forms
+ * every length, area, angle, sign, kite fraction and TRSK weight, and the
+ * Delaunay check (smeshpack.f90:706-1151, :4991-5154; interpack.f90:
+ * 3978-4098).  Node positions, index and sign arrays equal
+ * imodel_mesh_build's bit for bit; the GPU's atan, tan, atan2 and
  * asin may differ from the host C library's in the last bit, so lengths,
  * areas, angles and weights agree with imodel_mesh_build's to a few units in
  * the last place.  The result is an ordinary grid handle (view, extra_view,

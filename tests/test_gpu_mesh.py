@@ -1,7 +1,7 @@
 """The GPU back end of the grid builder (imodel_mesh_build_gpu).
 
-* the grid it returns has the host builder's numbering and signs exactly,
-  and its lengths, areas, angles, kite fractions and TRSK weights within a
+* the grid it returns has the host builder's numbering, signs and node
+  positions exactly (the numbering built by GPU kernels), and its lengths, areas, angles, kite fractions and TRSK weights within a
   few units in the last place of the host values (the GPU's atan, tan, atan2
   and asin against the host C library's; every other operation rounds the
   same way);
@@ -35,6 +35,8 @@ def ulps_of_scale(a, b):
 def compare(gh, gg):
     for k in INTS:
         assert np.array_equal(getattr(gh, k), getattr(gg, k)), k
+    # the subdivision's midpoints round as on the host
+    assert np.array_equal(gh.v_p, gg.v_p)
     worst = {}
     for k in FLOATS:
         a, b = getattr(gh, k), getattr(gg, k)
