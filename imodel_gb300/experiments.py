@@ -380,6 +380,49 @@ def exp_schemes(args, pool):
     return out
 
 
+def exp_moist(args, pool):
+    """Throughput of the moist model (FP64 GPU handle, test case 2, trsk
+    and upw1 advection) against the dry FP64 and FP32 steps from the same
+    h and u, at levels 8 to args.level (default 9), dt 110 s scaled by the
+    grid spacing; each timed over args.days (default 0.1) after a 2-step
+    warm-up."""
+    from .mesh import meshbuild
+    from .moist import Moist, moist_fields
+    from .swm import SWM
+    out = {}
+    for lvl in range(8, (args.level or 9) + 1):
+        g = meshbuild(lvl, device=0)
+        dt = 110.0 * 2.0 ** (8 - lvl)
+        n = swm_steps(args.days or 0.1, dt)
+        f = moist_fields(g, 2)
+        row = {"dt": dt, "steps": n, "cells": g.nv}
+        for adv in ("trsk", "upw1"):
+            m = Moist(g, 2, f, advection=adv)
+            m.set_state(f)
+            m.advance(dt, 2)
+            m.set_state(f)
+            t0 = time.perf_counter()
+            m.advance(dt, n)
+            sec = time.perf_counter() - t0
+            st = m.get_state()
+            m.close()
+            row[f"moist_{adv}"] = {"cell_steps_per_s": g.nv * n / sec, "seconds": sec,
+                                   "finite": bool(np.all(np.isfinite(st["h"])))}
+        for prec in ("fp64", "fp32"):
+            m = SWM(g, prec)
+            m.set_state(f["h"], f["u"])
+            m.advance(dt, 2)
+            m.set_state(f["h"], f["u"])
+            t0 = time.perf_counter()
+            m.advance(dt, n)
+            m.get_state()
+            sec = time.perf_counter() - t0
+            m.close()
+            row[f"dry_{prec}"] = {"cell_steps_per_s": g.nv * n / sec, "seconds": sec}
+        out[f"level{lvl}"] = row
+    return out
+
+
 def swm_steps(days, dt):
     from . import swm
     return swm.ntime_for(days, dt)
@@ -414,7 +457,7 @@ def exp_mesh(args, pool):
     return out
 
 
-RUNS = {"tc2": exp_tc2, "mesh": exp_mesh, "schemes": exp_schemes, "case2": exp_case2, "williamson": exp_williamson, "balanced": exp_balanced, "ensemble": exp_ensemble,
+RUNS = {"tc2": exp_tc2, "mesh": exp_mesh, "moist": exp_moist, "schemes": exp_schemes, "case2": exp_case2, "williamson": exp_williamson, "balanced": exp_balanced, "ensemble": exp_ensemble,
         "mountains": exp_mountains, "fixed": exp_fixed, "large": exp_large}
 
 
