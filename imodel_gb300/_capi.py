@@ -137,7 +137,7 @@ class MoistOpts(ctypes.Structure):
 
     _fields_ = [("testcase", ctypes.c_int32), ("bt", c_f64p), ("theta", c_f64p),
                 ("q0", ctypes.c_double), ("device", ctypes.c_int32),
-                ("advection", ctypes.c_int32)]
+                ("advection", ctypes.c_int32), ("precision", ctypes.c_int32)]
 
 
 _libs: dict = {}

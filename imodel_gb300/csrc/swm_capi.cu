@@ -1517,13 +1517,16 @@ const char *imodel_swm_last_error(void *handle) {
 // ---- the moist shallow-water model ---------------------------------------------
 namespace {
 struct Moist {
-  Handle *H = nullptr;  // the FP64 shallow-water handle: geometry, h and u
+  Handle *H = nullptr;  // the shallow-water handle: geometry, h and u
   int testcase = 0;
   int upw1 = 0;  // tracer advection "upw1" instead of "trsk"
+  bool fp32 = false;  // FP32 handle: the f_ buffers instead of the FP64 ones
   double q0 = 0.0;
   double *th = nullptr, *ex20 = nullptr, *qv = nullptr, *qc = nullptr, *qr = nullptr;
   double *q[5][4] = {};  // per tracer: y_n, two stage buffers, RK accumulator
   double *uphi = nullptr;
+  float *f_th = nullptr, *f_ex20 = nullptr, *f_qv = nullptr, *f_qc = nullptr, *f_qr = nullptr;
+  float *f_q[5][4] = {};
   bool state_set = false;
 };
 
@@ -1545,6 +1548,87 @@ int moist_out(Handle *H, const double *src, double *dst, bool edges) {
   CK(cudaGetLastError());
   return IMODEL_SWM_OK;
 }
+// the same into and out of FP32 device arrays, dst = src - shift and back
+int moist_in32(Handle *H, const double *src, float *dst, bool edges, double shift) {
+  const int n = edges ? H->ne : H->nv;
+  double *stage = edges ? H->d_stage_u : H->d_stage_h;
+  CK(cudaMemcpyAsync(stage, src, sizeof(double) * n, cudaMemcpyHostToDevice, H->stream));
+  imodel::launch_gather_in32(n, edges ? H->d_edge_n2o : H->d_cell_n2o, stage, dst, shift,
+                             H->stream);
+  CK(cudaGetLastError());
+  return IMODEL_SWM_OK;
+}
+int moist_out32(Handle *H, const float *src, double *dst, bool edges, double shift) {
+  const int n = edges ? H->ne : H->nv;
+  double *stage = edges ? H->d_stage_u : H->d_stage_h;
+  imodel::launch_scatter_out32(n, edges ? H->d_edge_n2o : H->d_cell_n2o, src, stage, shift,
+                               H->d_flags, H->stream);
+  CK(cudaMemcpyAsync(dst, stage, sizeof(double) * n, cudaMemcpyDeviceToHost, H->stream));
+  CK(cudaGetLastError());
+  return IMODEL_SWM_OK;
+}
+
+// stage st of the RK4 loop reads y_n, a, b, a and writes a, b, a, y_n
+template <class T>
+T *stage_in(int st, T *yn, T *a, T *b) {
+  return st == 0 ? yn : (st == 2 ? b : a);
+}
+template <class T>
+T *stage_out(int st, T *yn, T *a, T *b) {
+  return st == 0 ? a : (st == 1 ? b : (st == 2 ? a : yn));
+}
+
+// imodel_moist_advance on an FP32 handle: the FP32 step's tendency (its
+// tuned variant, tendencies only), then the moist kernels in FP32
+void moist_advance32(Moist *X, double dt, int nsteps) {
+  Handle *H = X->H;
+  imodel::Work<float> &W = H->W32;
+  const float fdt = static_cast<float>(dt);
+  const bool swm = X->testcase > 1;
+  const int active = swm ? (0xF | (X->testcase == 2 ? 0x10 : 0)) : 0x10;
+  for (int step = 0; step < nsteps; ++step) {
+    for (int st = 0; st < 4; ++st) {
+      imodel::MoistArgs32 A;
+      A.stage = st;
+      A.dt = fdt;
+      A.swm = swm ? 1 : 0;
+      A.active = active;
+      A.upw1 = X->upw1;
+      A.h_ref = W.h_ref;
+      const float *h_in = swm ? stage_in(st, W.yn_h, W.ya_h, W.yb_h) : W.yn_h;
+      const float *u_in = swm ? stage_in(st, W.yn_u, W.ya_u, W.yb_u) : W.yn_u;
+      if (swm) imodel::launch_stage32(H->M, W, h_in, u_in, nullptr, nullptr, -1, fdt, H->stream);
+      A.h_in = h_in;
+      A.u_in = u_in;
+      A.tend_h = W.tend_h;
+      A.tend_u = W.tend_u;
+      A.yn_h = W.yn_h;
+      A.acc_h = W.acc_h;
+      A.h_out = stage_out(st, W.yn_h, W.ya_h, W.yb_h);
+      A.yn_u = W.yn_u;
+      A.acc_u = W.acc_u;
+      A.u_out = stage_out(st, W.yn_u, W.ya_u, W.yb_u);
+      for (int k = 0; k < 5; ++k) {
+        float **q = X->f_q[k];
+        const bool adv = (active >> k) & 1;
+        A.q_in[k] = adv ? stage_in(st, q[0], q[1], q[2]) : q[0];
+        A.q_yn[k] = q[0];
+        A.q_acc[k] = q[3];
+        A.q_out[k] = stage_out(st, q[0], q[1], q[2]);
+      }
+      A.th = X->f_th;
+      A.ex20 = X->f_ex20;
+      A.qv = X->f_qv;
+      A.qc = X->f_qc;
+      A.qr = X->f_qr;
+      A.q0 = static_cast<float>(X->q0);
+      A.flags = H->d_flags;
+      imodel::launch_moist_stage32(H->M, A, H->stream);
+    }
+    imodel::launch_moist_q32(H->nv, W.yn_h, W.h_ref, X->f_q[1][0], X->f_q[2][0], X->f_q[3][0],
+                             X->f_qv, X->f_qc, X->f_qr, H->d_flags, H->stream);
+  }
+}
 }  // namespace
 
 extern "C" {
@@ -1563,8 +1647,10 @@ int imodel_moist_create(const imodel_swm_mesh *m, const imodel_moist_opts *o, vo
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "moist test cases are 1..5");
   if (o->advection != 0 && o->advection != 1)
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "advection is 0 (trsk) or 1 (upw1)");
+  if (o->precision != IMODEL_SWM_FP64 && o->precision != IMODEL_SWM_FP32)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "precision is IMODEL_SWM_FP64 or IMODEL_SWM_FP32");
   imodel_swm_opts so{};
-  so.precision = IMODEL_SWM_FP64;
+  so.precision = o->precision;
   so.testcase = o->testcase;
   so.bt = o->bt;
   so.device = o->device;
@@ -1578,19 +1664,31 @@ int imodel_moist_create(const imodel_swm_mesh *m, const imodel_moist_opts *o, vo
   X->testcase = o->testcase;
   X->upw1 = o->advection;
   X->q0 = o->q0;
+  X->fp32 = o->precision == IMODEL_SWM_FP32;
   const size_t nv = H->nv, ne = H->ne;
-  for (double **p : {&X->th, &X->ex20, &X->qv, &X->qc, &X->qr})
-    if ((rc = imodel::dalloc(H, p, nv))) return rc;
-  for (int k = 0; k < 5; ++k)
-    for (int b = 0; b < 4; ++b)
-      if ((rc = imodel::dalloc(H, &X->q[k][b], nv))) return rc;
-  if ((rc = imodel::dalloc(H, &X->uphi, 5 * ne))) return rc;
   // theta and exp(20 theta) of qsat (moist_swm.f90:618-622): theta is fixed
   // in the RK4 path, so the exponential is formed once, here
   std::vector<double> ex(nv);
   for (size_t i = 0; i < nv; ++i) ex[i] = std::exp(20.0 * o->theta[i]);
-  if ((rc = moist_in(H, o->theta, X->th, false)) || (rc = moist_in(H, ex.data(), X->ex20, false)))
-    return rc;
+  if (X->fp32) {
+    for (float **p : {&X->f_th, &X->f_ex20, &X->f_qv, &X->f_qc, &X->f_qr})
+      if ((rc = imodel::dalloc(H, p, nv))) return rc;
+    for (int k = 0; k < 5; ++k)
+      for (int b = 0; b < 4; ++b)
+        if ((rc = imodel::dalloc(H, &X->f_q[k][b], nv))) return rc;
+    if ((rc = moist_in32(H, o->theta, X->f_th, false, 0.0)) ||
+        (rc = moist_in32(H, ex.data(), X->f_ex20, false, 0.0)))
+      return rc;
+  } else {
+    for (double **p : {&X->th, &X->ex20, &X->qv, &X->qc, &X->qr})
+      if ((rc = imodel::dalloc(H, p, nv))) return rc;
+    for (int k = 0; k < 5; ++k)
+      for (int b = 0; b < 4; ++b)
+        if ((rc = imodel::dalloc(H, &X->q[k][b], nv))) return rc;
+    if ((rc = imodel::dalloc(H, &X->uphi, 5 * ne))) return rc;
+    if ((rc = moist_in(H, o->theta, X->th, false)) || (rc = moist_in(H, ex.data(), X->ex20, false)))
+      return rc;
+  }
   if (cudaStreamSynchronize(H->stream) != cudaSuccess)
     return imodel::set_error(H, IMODEL_SWM_ECUDA, "stream synchronize failed");
   return IMODEL_SWM_OK;
@@ -1606,13 +1704,37 @@ int imodel_moist_set_state(void *handle, const double *const y[7], const double 
     if (!y[k]) return IMODEL_SWM_EINVAL;
   if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
   int rc;
-  if ((rc = moist_in(H, y[0], H->W64.yn_h, false)) || (rc = moist_in(H, y[1], H->W64.yn_u, true)))
-    return rc;
-  for (int k = 0; k < 5; ++k)
-    if ((rc = moist_in(H, y[2 + k], X->q[k][0], false))) return rc;
-  if ((rc = moist_in(H, qv, X->qv, false)) || (rc = moist_in(H, qc, X->qc, false)) ||
-      (rc = moist_in(H, qr, X->qr, false)))
-    return rc;
+  if (X->fp32) {
+    // h is stored as h - h_ref, h_ref the area-weighted mean of the first
+    // state set (in FP32), as for the FP32 shallow-water handle
+    if (!H->href_fixed) {
+      double s = 0.0, a = 0.0;
+      for (int i = 0; i < H->nv; ++i) {
+        a += H->h_areag[i];
+        s += H->h_areag[i] * y[0][i];
+      }
+      H->W32.h_ref = static_cast<float>(s / a);
+      H->h_ref = static_cast<double>(H->W32.h_ref);
+      H->href_fixed = true;
+    }
+    if ((rc = moist_in32(H, y[0], H->W32.yn_h, false, H->h_ref)) ||
+        (rc = moist_in32(H, y[1], H->W32.yn_u, true, 0.0)))
+      return rc;
+    for (int k = 0; k < 5; ++k)
+      if ((rc = moist_in32(H, y[2 + k], X->f_q[k][0], false, 0.0))) return rc;
+    if ((rc = moist_in32(H, qv, X->f_qv, false, 0.0)) ||
+        (rc = moist_in32(H, qc, X->f_qc, false, 0.0)) ||
+        (rc = moist_in32(H, qr, X->f_qr, false, 0.0)))
+      return rc;
+  } else {
+    if ((rc = moist_in(H, y[0], H->W64.yn_h, false)) || (rc = moist_in(H, y[1], H->W64.yn_u, true)))
+      return rc;
+    for (int k = 0; k < 5; ++k)
+      if ((rc = moist_in(H, y[2 + k], X->q[k][0], false))) return rc;
+    if ((rc = moist_in(H, qv, X->qv, false)) || (rc = moist_in(H, qc, X->qc, false)) ||
+        (rc = moist_in(H, qr, X->qr, false)))
+      return rc;
+  }
   if (cudaStreamSynchronize(H->stream) != cudaSuccess)
     return imodel::set_error(H, IMODEL_SWM_ECUDA, "stream synchronize failed");
   X->state_set = true;
@@ -1627,6 +1749,11 @@ int imodel_moist_advance(void *handle, double dt, int32_t nsteps) {
   if (nsteps < 0 || !(dt > 0) || !std::isfinite(dt))
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "bad dt or nsteps");
   if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  if (X->fp32) {
+    moist_advance32(X, dt, nsteps);
+    if (cudaGetLastError() != cudaSuccess) return imodel::set_error(H, IMODEL_SWM_ECUDA, "launch failed");
+    return imodel::check_flags(H);
+  }
   imodel::Work<double> &W = H->W64;
   const bool swm = X->testcase > 1;
   const int active = swm ? (0xF | (X->testcase == 2 ? 0x10 : 0)) : 0x10;
@@ -1692,6 +1819,14 @@ int imodel_moist_get_state(void *handle, double *const y[7]) {
     if (!y[k]) return IMODEL_SWM_EINVAL;
   if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
   int rc;
+  if (X->fp32) {
+    if ((rc = moist_out32(H, H->W32.yn_h, y[0], false, H->h_ref)) ||
+        (rc = moist_out32(H, H->W32.yn_u, y[1], true, 0.0)))
+      return rc;
+    for (int k = 0; k < 5; ++k)
+      if ((rc = moist_out32(H, X->f_q[k][0], y[2 + k], false, 0.0))) return rc;
+    return imodel::check_flags(H);
+  }
   if ((rc = moist_out(H, H->W64.yn_h, y[0], false)) || (rc = moist_out(H, H->W64.yn_u, y[1], true)))
     return rc;
   for (int k = 0; k < 5; ++k)

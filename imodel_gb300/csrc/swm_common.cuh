@@ -204,6 +204,28 @@ void launch_moist_stage(const DevMesh &M, const MoistArgs &A, cudaStream_t s);
 void launch_moist_q(int nv, const double *h, const double *hqv, const double *hqc,
                     const double *hqr, double *qv, double *qc, double *qr, int *flags,
                     cudaStream_t s);
+// The same in FP32 beside the FP32 step (tendencies of any variant): h as
+// h - h_ref, the tracers h q as they are, the geometry's folded FP32
+// coefficients; the cells form the tracer fluxes themselves
+struct MoistArgs32 {
+  int stage = 0;
+  float dt = 0.0f;
+  int swm = 0, active = 0;
+  int upw1 = 0;
+  float h_ref = 0.0f;
+  const float *u_in = nullptr, *h_in = nullptr, *tend_u = nullptr, *tend_h = nullptr;
+  float *yn_u = nullptr, *acc_u = nullptr, *u_out = nullptr;
+  float *yn_h = nullptr, *acc_h = nullptr, *h_out = nullptr;
+  const float *q_in[5] = {};
+  float *q_yn[5] = {}, *q_acc[5] = {}, *q_out[5] = {};
+  const float *th = nullptr, *ex20 = nullptr, *qv = nullptr, *qc = nullptr, *qr = nullptr;
+  float q0 = 0.0f;
+  int *flags = nullptr;
+};
+void launch_moist_stage32(const DevMesh &M, const MoistArgs32 &A, cudaStream_t s);
+void launch_moist_q32(int nv, const float *hd, float h_ref, const float *hqv, const float *hqc,
+                      const float *hqr, float *qv, float *qc, float *qr, int *flags,
+                      cudaStream_t s);
 
 // reference order <-> device order, with precision conversion
 void launch_gather_in(int n, const int32_t *n2o, const double *src, double *dst, double shift,

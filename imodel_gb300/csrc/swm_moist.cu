@@ -145,9 +145,143 @@ __global__ void k_moist_q(int nv, const double *__restrict__ h, const double *__
   qr[i] = hqr[i] / hi;
 }
 
+// ---- FP32 --------------------------------------------------------------------
+// The same model beside the FP32 step (any of its variants, tendencies
+// only): h is stored as h - h_ref, so h itself is h_ref + h_d where the
+// sources and the thermal term need it; the gradient of h (h theta) is
+// formed as
+//   h2 Q2 - h1 Q1 = (h_d2 - h_d1) (Q1 + Q2) / 2 + (Q2 - Q1) (h1 + h2) / 2
+// (exact in real arithmetic), which keeps the difference of the depths free
+// of h_ref's rounding.  The divergences use the cells' folded coefficients
+// c_div32 = ttgout l_e / (A erad), the gradients e_grad32 = 1 / (l erad).
+// Each cell forms the tracer flux of its edges itself from its neighbour
+// across the edge (c_nb): u_e (q_i + q_nb) / 2 with "trsk", the upwind
+// value with "upw1"; the two cells of an edge form the same flux, since
+// q_i + q_nb and q_nb + q_i round alike, so no flux array goes through
+// memory.
+
+__device__ __forceinline__ float rk_stage32m(int stage, float k, float yn, float *acc, float dt) {
+  if (stage == 0) {
+    *acc = k;
+    return yn + dt * k * 0.5f;
+  } else if (stage == 1) {
+    *acc = *acc + 2.0f * k;
+    return yn + dt * k * 0.5f;
+  } else if (stage == 2) {
+    *acc = *acc + 2.0f * k;
+    return yn + dt * k;
+  }
+  return yn + dt * (*acc + k) * (1.0f / 6.0f);
+}
+
+// the thermal momentum source and u's RK stage (shallow-water cases only)
+__global__ void __launch_bounds__(256) k_moist_edge32(DevMesh M, MoistArgs32 A) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ne = M.ne;
+  if (e >= ne) return;
+  const int v1 = __ldg(&M.e_v[e]), v2 = __ldg(&M.e_v[ne + e]);
+  const float gr = __ldg(&M.e_grad32[e]), grav = static_cast<float>(M.grav);
+  const float hd1 = A.h_in[v1], hd2 = A.h_in[v2];
+  const float Q1 = A.q_in[0][v1], Q2 = A.q_in[0][v2];
+  const float h1 = A.h_ref + hd1, h2 = A.h_ref + hd2;
+  const float g = ((hd2 - hd1) * (Q1 + Q2) * 0.5f + (Q2 - Q1) * (h1 + h2) * 0.5f) * gr;
+  // scalar_hx2ed of h
+  const float hed = A.h_ref + 0.5f * (hd1 + hd2);
+  float gpi_oh = 0.0f;
+  if (fabsf(hed) < 1.1920928955078125e-12f)
+    atomicOr(A.flags, 1);
+  else
+    gpi_oh = g / hed;
+  const float gb = (__ldg(&M.c_bt32[v2]) - __ldg(&M.c_bt32[v1])) * gr;
+  const float th_ed = (A.th[v1] + A.th[v2]) * 0.5f;
+  const float su = (grav * 0.5f) * gpi_oh + grav * (th_ed * gb);
+  const float momeq = A.tend_u[e] + su;
+  A.u_out[e] = rk_stage32m(A.stage, momeq, A.yn_u[e], A.acc_u + e, A.dt);
+}
+
+__global__ void __launch_bounds__(256) k_moist_cell32(DevMesh M, MoistArgs32 A) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nv = M.nv;
+  if (i >= nv) return;
+  float hs[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  if (A.swm) {
+    A.h_out[i] = rk_stage32m(A.stage, A.tend_h[i], A.yn_h[i], A.acc_h + i, A.dt);
+    const float hi = A.h_ref + A.h_in[i];
+    const float qs = A.q0 * A.ex20[i] / ((hi + __ldg(&M.c_bt32[i])) * static_cast<float>(M.grav));
+    const float gamma_v = 1.0f / (1.0f + kLscale * (20.0f * qs));
+    const float qv = A.qv[i], qc = A.qc[i];
+    const float r = gamma_v * (qv - qs);
+    const float dqv = fmaxf(r, 0.0f) / A.dt;
+    const float dqc = fminf(qc, fmaxf(-r, 0.0f)) / A.dt;
+    const float dqr = fmaxf(static_cast<float>(kGammaR) * (qc - static_cast<float>(kQprecip)), 0.0f) / A.dt;
+    hs[1] = hi * (dqc - dqv);
+    hs[2] = hi * (dqv - dqc - dqr);
+    hs[3] = hi * dqr;
+    hs[0] = hi * (static_cast<float>(kLscale) * (dqv - dqc));
+  }
+  // the cell's edges: the normal velocity times c_div32, and the neighbour
+  const int n = M.c_nnb[i];
+  float w[6];
+  int nb[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    w[j] = 0.0f;
+    nb[j] = i;
+    if (j < n) {
+      w[j] = A.u_in[__ldg(&M.c_ed[j * nv + i])] * __ldg(&M.c_div32[j * nv + i]);
+      nb[j] = __ldg(&M.c_nb[j * nv + i]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    if (!((A.active >> k) & 1)) continue;
+    const float *q = A.q_in[k];
+    const float qi = q[i];
+    float d = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      if (j >= n) continue;
+      const float qn = q[nb[j]];
+      // "upw1": the cell's own value where the flux leaves it (w > 0)
+      const float qf = A.upw1 ? (w[j] > 0.0f ? qi : qn) : (qi + qn) * 0.5f;
+      d += w[j] * qf;
+    }
+    float t = -d;
+    if (A.swm && k < 4) t = t + hs[k];
+    A.q_out[k][i] = rk_stage32m(A.stage, t, A.q_yn[k][i], A.q_acc[k] + i, A.dt);
+  }
+}
+
+__global__ void k_moist_q32(int nv, const float *__restrict__ hd, float h_ref,
+                            const float *__restrict__ hqv, const float *__restrict__ hqc,
+                            const float *__restrict__ hqr, float *__restrict__ qv,
+                            float *__restrict__ qc, float *__restrict__ qr, int *flags) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  const float hi = h_ref + hd[i];
+  if (fabsf(hi) < 1.1920928955078125e-12f) {
+    atomicOr(flags, 1);
+    return;
+  }
+  qv[i] = hqv[i] / hi;
+  qc[i] = hqc[i] / hi;
+  qr[i] = hqr[i] / hi;
+}
+
 inline int nblocks(int n, int t) { return (n + t - 1) / t; }
 
 }  // namespace
+
+void launch_moist_stage32(const DevMesh &M, const MoistArgs32 &A, cudaStream_t s) {
+  if (A.swm) k_moist_edge32<<<nblocks(M.ne, 256), 256, 0, s>>>(M, A);
+  k_moist_cell32<<<nblocks(M.nv, 256), 256, 0, s>>>(M, A);
+}
+
+void launch_moist_q32(int nv, const float *hd, float h_ref, const float *hqv, const float *hqc,
+                      const float *hqr, float *qv, float *qc, float *qr, int *flags,
+                      cudaStream_t s) {
+  k_moist_q32<<<nblocks(nv, 256), 256, 0, s>>>(nv, hd, h_ref, hqv, hqc, hqr, qv, qc, qr, flags);
+}
 
 void launch_moist_stage(const DevMesh &M, const MoistArgs &A, cudaStream_t s) {
   k_moist_edge<<<nblocks(M.ne, 256), 256, 0, s>>>(M, A);

@@ -381,9 +381,9 @@ def exp_schemes(args, pool):
 
 
 def exp_moist(args, pool):
-    """Throughput of the moist model (FP64 GPU handle, test case 2, trsk
-    and upw1 advection) against the dry FP64 and FP32 steps from the same
-    h and u, at levels 8 to args.level (default 9), dt 110 s scaled by the
+    """Throughput of the moist model (FP64 and FP32 GPU handles, test case
+    2, trsk and upw1 advection; FP32's relative L2 distance from FP64) against
+    the dry FP64 and FP32 steps from the same h and u, at levels 8 to args.level (default 9), dt 110 s scaled by the
     grid spacing; each timed over args.days (default 0.1) after a 2-step
     warm-up."""
     from .mesh import meshbuild
@@ -396,18 +396,25 @@ def exp_moist(args, pool):
         n = swm_steps(args.days or 0.1, dt)
         f = moist_fields(g, 2)
         row = {"dt": dt, "steps": n, "cells": g.nv}
-        for adv in ("trsk", "upw1"):
-            m = Moist(g, 2, f, advection=adv)
-            m.set_state(f)
-            m.advance(dt, 2)
-            m.set_state(f)
-            t0 = time.perf_counter()
-            m.advance(dt, n)
-            sec = time.perf_counter() - t0
-            st = m.get_state()
-            m.close()
-            row[f"moist_{adv}"] = {"cell_steps_per_s": g.nv * n / sec, "seconds": sec,
-                                   "finite": bool(np.all(np.isfinite(st["h"])))}
+        ref = {}
+        for prec in ("fp64", "fp32"):
+            for adv in ("trsk", "upw1"):
+                m = Moist(g, 2, f, advection=adv, precision=prec)
+                m.set_state(f)
+                m.advance(dt, 2)
+                m.set_state(f)
+                t0 = time.perf_counter()
+                m.advance(dt, n)
+                sec = time.perf_counter() - t0
+                st = m.get_state()
+                m.close()
+                r = {"cell_steps_per_s": g.nv * n / sec, "seconds": sec}
+                if prec == "fp64":
+                    ref[adv] = st
+                else:
+                    r["h_vs_fp64"] = rel_errors(st["h"], ref[adv]["h"], g.hx_areag)
+                    r["hqv_vs_fp64"] = rel_errors(st["hqv"], ref[adv]["hqv"], g.hx_areag)
+                row[f"moist_{prec}_{adv}"] = r
         for prec in ("fp64", "fp32"):
             m = SWM(g, prec)
             m.set_state(f["h"], f["u"])

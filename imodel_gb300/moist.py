@@ -15,7 +15,8 @@ after each step.
 
 ``moist_fields`` restates the initial states of test cases 1-5
 (initialize_moist_swm_fields, moist_swm.f90:643-1139).  ``Moist`` is the GPU
-handle (include/imodel_moist.h): FP64, the reference's operation order.
+handle (include/imodel_moist.h): FP64 in the reference's operation order,
+or FP32.
 """
 from __future__ import annotations
 
@@ -161,14 +162,15 @@ def moist_fields(grid: Grid, testcase: int) -> dict:
 
 class Moist:
     """The moist shallow-water model on the GPU (include/imodel_moist.h):
-    one grid, one test case, FP64 in the reference's operation order; the
-    tracers advected with advmtd "trsk" (centred) or "upw1" (first-order
-    upwind, highorder.f90:5094-5139)."""
+    one grid, one test case, FP64 in the reference's operation order or
+    FP32; the tracers advected with advmtd "trsk" (centred) or "upw1"
+    (first-order upwind, highorder.f90:5094-5139)."""
 
     ADVECTION = {"trsk": 0, "upw1": 1}
+    PRECISION = {"fp64": 0, "fp32": 1}
 
     def __init__(self, grid: Grid, testcase: int, fields: dict, device: int = 0,
-                 advection: str = "trsk"):
+                 advection: str = "trsk", precision: str = "fp64"):
         self.grid = grid
         self.lib = _capi.swm_lib()
         self._mesh = grid.c_struct()
@@ -183,6 +185,9 @@ class Moist:
         if advection not in self.ADVECTION:
             raise ValueError(f"advection {advection!r}: built are {sorted(self.ADVECTION)}")
         o.advection = self.ADVECTION[advection]
+        if precision not in self.PRECISION:
+            raise ValueError(f"precision {precision!r}: built are {sorted(self.PRECISION)}")
+        o.precision = self.PRECISION[precision]
         self._handle = ctypes.c_void_p()
         rc = self.lib.imodel_moist_create(ctypes.byref(self._mesh), ctypes.byref(o),
                                           ctypes.byref(self._handle))

@@ -15,8 +15,9 @@
  *   qv, qc, qr = hq / h after each step (:1531-1533)     inside imodel_moist_advance
  *
  * The shallow-water part is the trsk10 / HTC / geodesic-area tendency of
- * imodel_swm.h in FP64, the reference's operation order (bit-equal to the
- * CPU oracle).  Mesh arrays as in imodel_swm.h; status codes IMODEL_SWM_*.
+ * imodel_swm.h, in FP64 in the reference's operation order (bit-equal to
+ * the CPU oracle) or in FP32.  Mesh arrays as in imodel_swm.h; status codes
+ * IMODEL_SWM_*.
  */
 #ifndef IMODEL_MOIST_H
 #define IMODEL_MOIST_H
@@ -38,6 +39,11 @@ typedef struct imodel_moist_opts {
   int32_t advection;   /* advmtd of the tracers: 0 = "trsk" (centred,
                           divhx, highorder.f90:4967-4974), 1 = "upw1"
                           (first-order upwind, div_hx_upw1, :5094-5139)   */
+  int32_t precision;   /* IMODEL_SWM_FP64 (0: the reference's operation
+                          order, bit-equal to the oracle) or
+                          IMODEL_SWM_FP32 (FP32 state, tracers and sources
+                          beside the FP32 step; h stored as h - h_ref, h_ref
+                          the area-weighted mean of the first state set)  */
 } imodel_moist_opts;
 
 int imodel_moist_create(const imodel_swm_mesh *m, const imodel_moist_opts *o, void **handle);
