@@ -1274,10 +1274,9 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
   const int sizes[3] = {128, 256, 512};
   imodel::Tune best;
   float best_ms = 1e30f;
-  // the learned correction is wired into the cell-centred variants only,
-  // APVM into the edge pre-pass of variant 0 and the method wrappers into
-  // the variant-0 kernels
-  const bool v0_only = H->W32.apvm.on || H->W32.scheme != IMODEL_SWM_TRSK10;
+  // the learned correction is wired into the cell-centred variants only and
+  // the method wrappers into the variant-0 kernels
+  const bool v0_only = H->W32.scheme != IMODEL_SWM_TRSK10;
   for (int v = H->learned_mode == 1 ? 1 : 0; v <= (v0_only ? 0 : 2); ++v)
     for (int b : sizes) {
       imodel::Tune t;
@@ -1353,8 +1352,6 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[6]) {
   if (H->learned_mode == 1 && choice[0] == 0)
     return imodel::set_error(H, IMODEL_SWM_EINVAL,
                              "the learned correction runs with the cell-centred variants (1, 2) only");
-  if (H->W32.apvm.on && choice[0] != 0)
-    return imodel::set_error(H, IMODEL_SWM_EINVAL, "apvm runs with variant 0 only");
   if (H->W32.scheme != IMODEL_SWM_TRSK10 && choice[0] != 0)
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "pxt16, gass18 and dtred run with variant 0 only");
   imodel::Tune t;
@@ -1456,14 +1453,11 @@ int imodel_swm_set_apvm(void *handle, double pvspar, double dt) {
   const bool fp32 = H->precision == IMODEL_SWM_FP32;
   if (pvspar > 0 && !(fp32 ? H->M.t_apw32 != nullptr : H->M.t_c != nullptr))
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "apvm needs the mesh's ed_nr and ed_c");
-  if (pvspar > 0 && H->learned_mode == 1)
-    return imodel::set_error(H, IMODEL_SWM_EINVAL,
-                             "apvm runs with FP32 variant 0, the learned correction with 1 and 2");
   if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
+  // FP32: the correction is applied in the edge pre-pass, which variants 1
+  // and 2 run before their cell kernel when APVM is on
   const int rc = fp32 ? imodel::setup_apvm(H, H->W32, pvspar, dt)
                       : imodel::setup_apvm(H, H->W64, pvspar, dt);
-  // FP32: the correction is applied in the edge pre-pass of variant 0
-  if (!rc && fp32 && pvspar > 0) H->W32.tune.variant = 0;
   if (H->graph) {
     cudaGraphExecDestroy(H->graph);
     H->graph = nullptr;

@@ -167,7 +167,8 @@ inline int launches_per_stage(int precision_fp32, int variant, bool dif_on = fal
   int n = (precision_fp32 && variant >= 1) ? 3 : 4;
   if (scheme == 3) n += 1;  // dtred: the triangle reconstruction of uh q
   if (dif_on) n += (dif_k4 ? 3 : 1) + ((precision_fp32 && variant == 0) ? 1 : 0);
-  if (apvm_on) n += precision_fp32 ? 1 : 2;
+  // FP32: the reconstructions, plus the edge pre-pass in variants 1 and 2
+  if (apvm_on) n += precision_fp32 ? (variant >= 1 ? 2 : 1) : 2;
   return n;
 }
 // The diffusion coefficients from the cell field kf (device order, FP64;

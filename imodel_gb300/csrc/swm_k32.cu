@@ -268,6 +268,8 @@ __global__ void __launch_bounds__(256) k_diflap32(DevMesh M, const float *__rest
 }
 
 // ---- cell-centred TRSK (variant 1), bodies in swm_k32_body.cuh ------------
+// kEdgePV: q_tr is the edges' PV from the edge pre-pass (APVM)
+template <bool kEdgePV>
 __global__ void __launch_bounds__(512) k_cell32v2(DevMesh M, const float *__restrict__ hd,
                                                   const float *__restrict__ u,
                                                   const float *__restrict__ q_tr,
@@ -282,8 +284,8 @@ __global__ void __launch_bounds__(512) k_cell32v2(DevMesh M, const float *__rest
                                                   float *__restrict__ coefdiv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= M.nv) return;
-  cell_body(M, i, OneRun{}, hd, u, q_tr, bern, zflux, yn, acc, yout, tend, stage, dt, grav, h_ref,
-            kcv, coefdiv);
+  cell_body<OneRun, LdPlain, kEdgePV>(M, i, OneRun{}, hd, u, q_tr, bern, zflux, yn, acc, yout,
+                                      tend, stage, dt, grav, h_ref, kcv, coefdiv);
 }
 
 // ---- variant 2: the triangle kernel on records with 16-bit indices -------
@@ -444,10 +446,25 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
     // learned correction: formed once per step from the first stage's state
     if (W.learned && stage <= 0)
       learned_launch(M, *W.learned, h_in, u_in, W.q_tr, W.h_ref, T.mlp_gather, W.flags, s);
+    const Apvm<float> &A = W.apvm;
+    if (A.on) {
+      // APVM (swm_operators.f90:1495-1502): the upwinded PV of every edge
+      // from the edge pre-pass, read by the cells in place of the triangle
+      // average
+      k_apvm32<<<nbt + nblocks(M.nv, 256), 256, 0, s>>>(M, W.q_tr, u_in, A.qg, A.vhx, nbt);
+      k_edge_pre32<<<nblocks(M.ne, T.bs_pre), T.bs_pre, 0, s>>>(
+          M, h_in, u_in, W.q_tr, W.h_ed, W.uh, W.q_ed, W.h_ref, A.qg, A.vhx, A.coef, nullptr,
+          nullptr, W.pv_on, W.flags);
+    }
     if (ev) cudaEventRecord(ev[2], s);
-    k_cell32v2<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
-        M, h_in, u_in, W.q_tr, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
-        grav, W.h_ref, D.kcv, D.on ? D.coefdiv : nullptr);
+    if (A.on)
+      k_cell32v2<true><<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
+          M, h_in, u_in, W.q_ed, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
+          grav, W.h_ref, D.kcv, D.on ? D.coefdiv : nullptr);
+    else
+      k_cell32v2<false><<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
+          M, h_in, u_in, W.q_tr, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
+          grav, W.h_ref, D.kcv, D.on ? D.coefdiv : nullptr);
     diffusion_tail();
     if (ev) cudaEventRecord(ev[3], s);
     k_edge32v2<<<nblocks((M.ne + 1) / 2, T.bs_edge), T.bs_edge, 0, s>>>(

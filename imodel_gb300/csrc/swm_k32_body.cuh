@@ -166,8 +166,10 @@ __device__ __forceinline__ void trsk_cell(const float (&G)[6], const float (&qs)
 
 // the arithmetic of one cell from its gathered values: div F, K, the
 // Bernoulli potential, the PV-flux contributions Z (cell-major zflux) and
-// the mass RK stage
-template <class Ix = OneRun>
+// the mass RK stage.  kEdgePV: qt holds the PV of the cell's edges (formed
+// by the edge pre-pass, APVM's upwinding included) instead of the PV of its
+// triangles.
+template <class Ix = OneRun, bool kEdgePV = false>
 __device__ __forceinline__ void cell_math(int i, uint32_t meta, const float (&R)[6],
                                           const float2 (&kd)[6], const float (&ue)[6],
                                           const float (&hn)[6], const float (&qt)[6], float hi,
@@ -189,7 +191,7 @@ __device__ __forceinline__ void cell_math(int i, uint32_t meta, const float (&R)
     const float F = ue[j] * (h_ref + 0.5f * (hi + hn[j]));
     G[j] = F * kd[j].y;
     // q_e: edge j lies between triangles j-1 and j (scalar_tr2ed)
-    qs[j] = 0.5f * ((j == 0 ? qlast : qt[j - 1]) + qt[j]);
+    qs[j] = kEdgePV ? qt[j] : 0.5f * ((j == 0 ? qlast : qt[j - 1]) + qt[j]);
     div += G[j];
     ke += kd[j].x * (ue[j] * ue[j]);
     du += ue[j] * kd[j].y;
@@ -226,7 +228,7 @@ __device__ __forceinline__ void cell_math(int i, uint32_t meta, const float (&R)
 // weights), gathering its neighbours' values.  The cell's own values come in
 // as arguments: h (deviation) hi, b bt, 1/(A a) inva, y_n ynv and the RK
 // accumulator accv (read for stages 1-3).
-template <class Ix, class Ld>
+template <class Ix, class Ld, bool kEdgePV = false>
 __device__ __forceinline__ void cell_core(int i, Ix ix, uint32_t meta,
                                           const int (&ed)[6], const int (&nb)[6],
                                           const int (&tr)[6], const float (&R)[6],
@@ -244,10 +246,11 @@ __device__ __forceinline__ void cell_core(int i, Ix ix, uint32_t meta,
   for (int j = 0; j < 6; ++j) {
     ue[j] = Ld::ld(u + ix(ed[j]));
     hn[j] = Ld::ld(hd + ix(nb[j]));
-    qt[j] = Ld::ld(q_tr + ix(tr[j]));
+    // kEdgePV: q_tr is the edges' PV, indexed by the slot's edge
+    qt[j] = Ld::ld(q_tr + ix(kEdgePV ? ed[j] : tr[j]));
   }
-  cell_math(i, meta, R, kd, ue, hn, qt, hi, bt, inva, ynv, accv, bern, zflux, acc, yout, tend,
-            stage, dt, grav, h_ref, ix, kcv, coefdiv);
+  cell_math<Ix, kEdgePV>(i, meta, R, kd, ue, hn, qt, hi, bt, inva, ynv, accv, bern, zflux, acc,
+                         yout, tend, stage, dt, grav, h_ref, ix, kcv, coefdiv);
 }
 
 // the cell's own values from global memory
@@ -264,7 +267,7 @@ __device__ __forceinline__ void cell_own(const DevMesh &M, int i, Ix ix,
   accv = stage >= 1 ? Ld::ld(acc + ix(i)) : 0.0f;
 }
 
-template <class Ix, class Ld = LdPlain>
+template <class Ix, class Ld = LdPlain, bool kEdgePV = false>
 __device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
                                           const float *__restrict__ hd,
                                           const float *__restrict__ u,
@@ -293,8 +296,8 @@ __device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
   }
   float hi, bt, inva, ynv, accv;
   cell_own<Ix, Ld>(M, i, ix, hd, yn, acc, stage, hi, bt, inva, ynv, accv);
-  cell_core<Ix, Ld>(i, ix, meta, ed, nb, tr, R, kd, hi, bt, inva, ynv, accv, hd, u, q_tr, bern,
-                    zflux, acc, yout, tend, stage, dt, grav, h_ref, kcv, coefdiv);
+  cell_core<Ix, Ld, kEdgePV>(i, ix, meta, ed, nb, tr, R, kd, hi, bt, inva, ynv, accv, hd, u, q_tr,
+                             bern, zflux, acc, yout, tend, stage, dt, grav, h_ref, kcv, coefdiv);
 }
 
 // -grad B - (Z_c1 + Z_c2) / l_e and the momentum RK stage of edge e

@@ -380,6 +380,49 @@ def exp_schemes(args, pool):
     return out
 
 
+def exp_apvm(args, pool):
+    """APVM (pvspar 0.5) on a seeded balanced state at args.level (default
+    9, dt 110 s scaled by the grid spacing): cell-steps/s of the FP64 step
+    and of the FP32 step in each variant and as autotuned, over args.days
+    (default 0.1) after a 2-step warm-up, with FP32's distance from FP64."""
+    from . import fields
+    from .mesh import meshbuild
+    from .swm import SWM
+    lvl = args.level or 9
+    g = meshbuild(lvl, device=0)
+    dt = 110.0 * 2.0 ** (8 - lvl)
+    n = swm_steps(args.days or 0.1, dt)
+    h, u = fields.balanced_state(g, lmax=32, seed=0, evaluator=fields.PoolEvaluator(pool))
+    out = {"level": lvl, "dt": dt, "steps": n}
+    r64 = None
+    for name, prec, variant in (("fp64", "fp64", None), ("fp32_v0", "fp32", 0),
+                                ("fp32_v1", "fp32", 1), ("fp32_v2", "fp32", 2),
+                                ("fp32_tuned", "fp32", -1)):
+        m = SWM(g, prec)
+        m.set_apvm(0.5, dt)
+        m.set_state(h, u)
+        row = {}
+        if variant == -1:
+            row["tuning"] = m.autotune(dt)
+        elif variant is not None:
+            m.set_tuning(variant=variant)
+        m.advance(dt, 2)
+        m.set_state(h, u)
+        t0 = time.perf_counter()
+        m.advance(dt, n)
+        hh, uu = m.get_state()
+        sec = time.perf_counter() - t0
+        m.close()
+        row.update({"cell_steps_per_s": g.nv * n / sec, "seconds": sec})
+        if r64 is None:
+            r64 = (hh, uu)
+        else:
+            row["h_vs_fp64"] = rel_errors(hh, r64[0], g.hx_areag)
+            row["u_vs_fp64"] = rel_errors(uu, r64[1], _edge_w(g))
+        out[name] = row
+    return out
+
+
 def exp_moist(args, pool):
     """Throughput of the moist model (FP64 and FP32 GPU handles, test case
     2, trsk and upw1 advection; FP32's relative L2 distance from FP64) against
@@ -464,7 +507,7 @@ def exp_mesh(args, pool):
     return out
 
 
-RUNS = {"tc2": exp_tc2, "mesh": exp_mesh, "moist": exp_moist, "schemes": exp_schemes, "case2": exp_case2, "williamson": exp_williamson, "balanced": exp_balanced, "ensemble": exp_ensemble,
+RUNS = {"tc2": exp_tc2, "mesh": exp_mesh, "moist": exp_moist, "apvm": exp_apvm, "schemes": exp_schemes, "case2": exp_case2, "williamson": exp_williamson, "balanced": exp_balanced, "ensemble": exp_ensemble,
         "mountains": exp_mountains, "fixed": exp_fixed, "large": exp_large}
 
 

@@ -250,8 +250,9 @@ class SWM:
 
     def set_apvm(self, pvspar: float, dt: float):
         """pv_stab = "apvm" (swm_operators.f90:1465-1543) with parameter
-        pvspar (0 = off) and the run's time step dt; moves an FP32 handle
-        to stencil variant 0."""
+        pvspar (0 = off) and the run's time step dt; FP32 handles keep
+        their variant (1 and 2 add the edge pre-pass before their cell
+        kernel)."""
         self._check(self.lib.imodel_swm_set_apvm(self._handle, pvspar, dt))
 
     def learned_weights(self):

@@ -251,10 +251,11 @@ int imodel_swm_set_diffusion_fields(void *handle, const double *k2_hx, const dou
  * that of u at the cells (apvm, swm_operators.f90:1465-1543; called at
  * swm.f90:2557-2559).  dt is the run's time step, which the reference's
  * tendency reads from its module: pass the dt the steps use.  FP32 handles
- * move to stencil variant 0 (the correction sits in its edge pre-pass);
- * set_tuning then refuses variants 1 and 2, and a handle with the learned
- * correction refuses APVM (IMODEL_SWM_EINVAL).  Needs the mesh's ed_nr and
- * ed_c.  May be called at any time; applies from the next step. */
+ * keep their variant: variant 0 applies the correction in its edge
+ * pre-pass, variants 1 and 2 run that pre-pass before their cell kernel,
+ * which then reads the edges' PV; it combines with the learned corrections.
+ * Needs the mesh's ed_nr and ed_c.  May be called at any time; applies from
+ * the next step. */
 int imodel_swm_set_apvm(void *handle, double pvspar, double dt);
 /* The kite fractions hxtr_area[nv][6] and TRSK weights trskw[nv][6][6]
  * (trskw(i, j) at [c][j][i], the mesh's layout) a handle created with

@@ -1,9 +1,9 @@
 """The anticipated potential vorticity method on the GPU
 (imodel_swm_set_apvm): the FP64 step equals the oracle bit for bit,
-tendency and RK4 steps, alone and with diffusion; the FP32 step (variant 0)
-stays within FP32 round-off of it; it costs one launch per stage; it
-switches off again; the learned correction and the cell-centred variants
-exclude it."""
+tendency and RK4 steps, alone and with diffusion; the FP32 step (the stencil
+variant and both cell-centred variants) stays within FP32 round-off of it;
+it costs one launch per stage in variant 0, two in the others; it switches
+off again; it runs together with the per-step learned correction."""
 import numpy as np
 import pytest
 
@@ -62,12 +62,16 @@ def test_launch_count_and_switching_off(grid_at):
     assert np.array_equal(ha, hb) and np.array_equal(ua, ub)
 
 
-def test_fp32_close_to_oracle(grid_at):
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_fp32_close_to_oracle(grid_at, variant):
     g = grid_at(5)
     h, u = fields.balanced_state(g, lmax=16, seed=7)
     m = SWM(g, "fp32")
     m.set_apvm(0.5, 450.0)
-    assert m.launch_count(1) == 4 * 5          # variant 0 and the reconstructions
+    m.set_tuning(variant=variant)
+    # variant 0: four kernels and the reconstructions; 1 and 2: three, the
+    # reconstructions and the edge pre-pass
+    assert m.launch_count(1) == 4 * 5
     hg, ug = m.ode_rk4(h, u, 450.0, 24)
     hr, ur = oracle.Oracle(g, 2, pvspar=0.5, dt=450.0).run(h, u, 450.0, 24)
     hp, up = oracle.Oracle(g, 2).run(h, u, 450.0, 24)
@@ -75,25 +79,45 @@ def test_fp32_close_to_oracle(grid_at):
     rel_h = lambda a, b: np.sqrt(np.sum(g.hx_areag * (a - b) ** 2) / np.sum(g.hx_areag * b ** 2))
     rel_u = lambda a, b: np.sqrt(np.sum(w * (a - b) ** 2) / np.sum(w * b ** 2))
     eh, eu = rel_h(hg, hr), rel_u(ug, ur)
+    print(f"variant {variant}: FP32 + APVM vs the oracle: h {eh:.2e}, u {eu:.2e}")
     assert eh < 1e-6 and eu < 1e-5, (eh, eu)
     # the correction itself is far above that (1.4e-4 in h, 3.9e-3 in u)
     assert rel_h(hg, hp) > 50 * eh and rel_u(ug, up) > 50 * eu
 
 
-def test_refusals(grid_at):
+def test_apvm_with_the_per_step_learned_correction(grid_at):
+    """APVM and the per-step network correction (cell-centred variants) run
+    together: the step differs from either alone and from plain FP32 by
+    about the sum of the two changes."""
     from imodel_gb300 import learned
+    g = grid_at(5)
+    h, u = fields.balanced_state(g, lmax=16, seed=9)
+    dt, n = 450.0, 24
+    w = g.ed_leng * g.edhx_leng
+    rel_u = lambda a, b: np.sqrt(np.sum(w * (a - b) ** 2) / np.sum(w * b ** 2))
+    runs = {}
+    for name, net, pv in (("plain", False, 0.0), ("apvm", False, 0.5), ("net", True, 0.0),
+                          ("both", True, 0.5)):
+        m = SWM(g, "fp32", learned_params=learned.trained_params()) if net else SWM(g, "fp32")
+        if pv:
+            m.set_apvm(pv, dt)
+        runs[name] = m.ode_rk4(h, u, dt, n)
+        m.close()
+    up = runs["plain"][1]
+    da, dn, db = (rel_u(runs[k][1], up) for k in ("apvm", "net", "both"))
+    print(f"u vs plain FP32: apvm {da:.2e}, network {dn:.2e}, both {db:.2e}")
+    assert all(np.all(np.isfinite(x)) for r in runs.values() for x in r)
+    assert da > 1e-5 and dn > 1e-5
+    assert rel_u(runs["both"][1], runs["apvm"][1]) > 0.3 * dn
+    assert rel_u(runs["both"][1], runs["net"][1]) > 0.3 * da
+
+
+def test_refusals(grid_at):
     g = grid_at(3)
     m = SWM(g, "fp32")
     m.set_apvm(0.5, 600.0)
-    with pytest.raises(SWMError) as ei:  # the cell-centred variants have no pre-pass
-        m.set_tuning(variant=1)
-    assert ei.value.code == _capi.EINVAL
-    m.set_apvm(0.0, 600.0)              # off again: every variant is open
-    m.set_tuning(variant=2)
-    n = SWM(g, "fp32", learned_params=learned.trained_params())
-    with pytest.raises(SWMError) as ei:
-        n.set_apvm(0.5, 600.0)
-    assert ei.value.code == _capi.EINVAL
+    for v in (1, 2, 0):                 # every variant runs APVM
+        m.set_tuning(variant=v)
     d = SWM(g, "fp64")
     for pv, dt in ((-0.5, 600.0), (float("nan"), 600.0), (0.5, 0.0), (0.5, float("inf"))):
         with pytest.raises(SWMError) as ei:
