@@ -66,7 +66,7 @@ struct Handle {
     const float *e_stc32 = nullptr, *c_R32 = nullptr;
     const int4 *c_pk = nullptr;
   } w_learned, w_plain;
-  std::vector<double> kite_hxtr, kite_trskw;
+  imodel::HVec<double> kite_hxtr, kite_trskw;
   double drift_bound = 1e-3;
   // the error proxy: bound, the learned and the plain momentum tendency
   // ([2][ne]), and the steps left until the next check (<= 0: at the next
@@ -655,7 +655,8 @@ int learned_weights(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *
   std::string msg = build_kite_inputs(*m, K);
   if (!msg.empty()) return set_error(H, IMODEL_SWM_EINVAL, msg);
   const int64_t n = static_cast<int64_t>(K.cell.size());
-  std::vector<float> y(static_cast<size_t>(n));
+  imodel::HVec<float> y;  // every output written by the network
+  y.resize(static_cast<size_t>(n));
   void *net = nullptr;
   int rc = imodel_mlp_create(H->device, &net);
   if (!rc) rc = imodel_mlp_set_params(net, static_cast<const float *>(o->mlp_weights),

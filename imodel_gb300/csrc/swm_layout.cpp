@@ -962,7 +962,8 @@ std::string build_kite_inputs(const imodel_swm_mesh &m, KiteInputs &K) {
     return "the learned weights need v_p, v_tr and tr_v";
   size_t nrow = 0;
   for (int c = 0; c < nv; ++c) nrow += static_cast<size_t>(m.nnb[c]);
-  K.x.assign(nrow * 24, 0);
+  // every row is written in full by the loop below
+  K.x.resize(nrow * 24);
   K.cell.resize(nrow);
   K.slot.resize(nrow);
   // row of (c, j): slot-major, the cells with nnb > j in order
@@ -1027,14 +1028,21 @@ std::string build_kite_inputs(const imodel_swm_mesh &m, KiteInputs &K) {
 }
 
 void apply_kite_outputs(const imodel_swm_mesh &m, const KiteInputs &K, const float *y,
-                        std::vector<double> &hxtr, std::vector<double> &trskw) {
+                        HVec<double> &hxtr, HVec<double> &trskw) {
   const int nv = m.nv;
-  std::vector<double> dR(6 * static_cast<size_t>(nv), 0.0);
+  HVec<double> dR;
+  fill(dR, 6 * static_cast<size_t>(nv), 0.0);
 #pragma omp parallel for schedule(static)
   for (int64_t r = 0; r < static_cast<int64_t>(K.cell.size()); ++r)
     dR[6 * static_cast<size_t>(K.cell[r]) + K.slot[r]] = 0.1 * static_cast<double>(y[r]);
-  hxtr.assign(m.hx_hxtr_area, m.hx_hxtr_area + 6 * static_cast<size_t>(nv));
-  trskw.assign(36 * static_cast<size_t>(nv), 0.0);
+  hxtr.resize(6 * static_cast<size_t>(nv));
+  {
+    const int64_t n6 = 6 * static_cast<int64_t>(nv);
+    double *d = hxtr.data();
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < n6; ++q) d[q] = m.hx_hxtr_area[q];
+  }
+  fill(trskw, 36 * static_cast<size_t>(nv), 0.0);
 #pragma omp parallel for schedule(static)
   for (int c = 0; c < nv; ++c) {
     const int n = m.nnb[c];

@@ -212,9 +212,9 @@ uint16_t bf16_bits(float v);
 // slot-major (all slot-0 kites, then slot 1, ...), and each row's cell and
 // slot (0-based, reference numbering).
 struct KiteInputs {
-  std::vector<uint16_t> x;    // [n][24]
-  std::vector<int32_t> cell;  // [n]
-  std::vector<int8_t> slot;   // [n]
+  HVec<uint16_t> x;    // [n][24]
+  HVec<int32_t> cell;  // [n]
+  HVec<int8_t> slot;   // [n]
 };
 std::string build_kite_inputs(const imodel_swm_mesh &m, KiteInputs &K);
 // Kite fractions R' = R + 0.1 y (y the network outputs, projected to sum
@@ -222,6 +222,6 @@ std::string build_kite_inputs(const imodel_swm_mesh &m, KiteInputs &K);
 // (calc_trisk_weights, interpack.f90:4046-4095), in the mesh's layout:
 // hxtr[nv][6], trskw[nv][6][6] with trskw(i, j) at [c][j][i].
 void apply_kite_outputs(const imodel_swm_mesh &m, const KiteInputs &K, const float *y,
-                        std::vector<double> &hxtr, std::vector<double> &trskw);
+                        HVec<double> &hxtr, HVec<double> &trskw);
 
 }  // namespace imodel
