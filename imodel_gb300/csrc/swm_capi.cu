@@ -1523,6 +1523,9 @@ struct Moist {
   float *f_th = nullptr, *f_ex20 = nullptr, *f_qv = nullptr, *f_qc = nullptr, *f_qr = nullptr;
   float *f_q[5][4] = {};
   bool state_set = false;
+  // one step's launches, captured once per dt and replayed
+  cudaGraphExec_t graph = nullptr;
+  double graph_dt = 0.0;
 };
 
 // host array (reference order, nv or ne values) -> device array (device order)
@@ -1573,15 +1576,15 @@ T *stage_out(int st, T *yn, T *a, T *b) {
   return st == 0 ? a : (st == 1 ? b : (st == 2 ? a : yn));
 }
 
-// imodel_moist_advance on an FP32 handle: the FP32 step's tendency (its
-// tuned variant, tendencies only), then the moist kernels in FP32
-void moist_advance32(Moist *X, double dt, int nsteps) {
+// one step of an FP32 handle: the FP32 step's tendency (its tuned variant,
+// tendencies only), then the moist kernels in FP32
+void moist_step32(Moist *X, double dt) {
   Handle *H = X->H;
   imodel::Work<float> &W = H->W32;
   const float fdt = static_cast<float>(dt);
   const bool swm = X->testcase > 1;
   const int active = swm ? (0xF | (X->testcase == 2 ? 0x10 : 0)) : 0x10;
-  for (int step = 0; step < nsteps; ++step) {
+  {
     for (int st = 0; st < 4; ++st) {
       imodel::MoistArgs32 A;
       A.stage = st;
@@ -1623,6 +1626,90 @@ void moist_advance32(Moist *X, double dt, int nsteps) {
     imodel::launch_moist_q32(H->nv, W.yn_h, W.h_ref, X->f_q[1][0], X->f_q[2][0], X->f_q[3][0],
                              X->f_qv, X->f_qc, X->f_qr, H->d_flags, H->stream);
   }
+}
+
+// one step of an FP64 handle: the FP64 tendency (tendencies only), then
+// the moist kernels
+void moist_step64(Moist *X, double dt) {
+  Handle *H = X->H;
+  imodel::Work<double> &W = H->W64;
+  const bool swm = X->testcase > 1;
+  const int active = swm ? (0xF | (X->testcase == 2 ? 0x10 : 0)) : 0x10;
+  // stage st reads y_n, a, b, a and writes a, b, a, y_n
+  auto in = [](int st, double *yn, double *a, double *b) { return st == 0 ? yn : (st == 2 ? b : a); };
+  auto out = [](int st, double *yn, double *a, double *b) {
+    return st == 0 ? a : (st == 1 ? b : (st == 2 ? a : yn));
+  };
+  {
+    for (int st = 0; st < 4; ++st) {
+      imodel::MoistArgs A;
+      A.stage = st;
+      A.dt = dt;
+      A.swm = swm ? 1 : 0;
+      A.active = active;
+      A.upw1 = X->upw1;
+      const double *h_in = swm ? in(st, W.yn_h, W.ya_h, W.yb_h) : W.yn_h;
+      const double *u_in = swm ? in(st, W.yn_u, W.ya_u, W.yb_u) : W.yn_u;
+      if (swm)
+        imodel::launch_stage64(H->M, W, h_in, u_in, nullptr, nullptr, -1, dt, H->stream);
+      A.h_in = h_in;
+      A.u_in = u_in;
+      A.tend_h = W.tend_h;
+      A.tend_u = W.tend_u;
+      A.h_ed = W.h_ed;
+      A.yn_h = W.yn_h;
+      A.acc_h = W.acc_h;
+      A.h_out = out(st, W.yn_h, W.ya_h, W.yb_h);
+      A.yn_u = W.yn_u;
+      A.acc_u = W.acc_u;
+      A.u_out = out(st, W.yn_u, W.ya_u, W.yb_u);
+      for (int k = 0; k < 5; ++k) {
+        double **q = X->q[k];
+        const bool adv = (active >> k) & 1;
+        A.q_in[k] = adv ? in(st, q[0], q[1], q[2]) : q[0];
+        A.q_yn[k] = q[0];
+        A.q_acc[k] = q[3];
+        A.q_out[k] = out(st, q[0], q[1], q[2]);
+      }
+      A.uphi = X->uphi;
+      A.th = X->th;
+      A.ex20 = X->ex20;
+      A.qv = X->qv;
+      A.qc = X->qc;
+      A.qr = X->qr;
+      A.q0 = X->q0;
+      A.flags = H->d_flags;
+      imodel::launch_moist_stage(H->M, A, H->stream);
+    }
+    imodel::launch_moist_q(H->nv, W.yn_h, X->q[1][0], X->q[2][0], X->q[3][0], X->qv, X->qc,
+                           X->qr, H->d_flags, H->stream);
+  }
+}
+
+// X->graph: one step's launches for this dt (captured anew when dt changes)
+int moist_graph(Moist *X, double dt) {
+  Handle *H = X->H;
+  if (X->graph && X->graph_dt == dt) return IMODEL_SWM_OK;
+  if (X->graph) {
+    cudaGraphExecDestroy(X->graph);
+    X->graph = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(H->stream, cudaStreamCaptureModeThreadLocal));
+  if (X->fp32)
+    moist_step32(X, dt);
+  else
+    moist_step64(X, dt);
+  CK(cudaStreamEndCapture(H->stream, &g));
+  cudaError_t e = cudaGraphInstantiate(&X->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    X->graph = nullptr;
+    return imodel::set_error(H, IMODEL_SWM_ECUDA,
+                             std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  }
+  X->graph_dt = dt;
+  return IMODEL_SWM_OK;
 }
 }  // namespace
 
@@ -1744,63 +1831,11 @@ int imodel_moist_advance(void *handle, double dt, int32_t nsteps) {
   if (nsteps < 0 || !(dt > 0) || !std::isfinite(dt))
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "bad dt or nsteps");
   if (cudaSetDevice(H->device) != cudaSuccess) return IMODEL_SWM_ECUDA;
-  if (X->fp32) {
-    moist_advance32(X, dt, nsteps);
-    if (cudaGetLastError() != cudaSuccess) return imodel::set_error(H, IMODEL_SWM_ECUDA, "launch failed");
-    return imodel::check_flags(H);
-  }
-  imodel::Work<double> &W = H->W64;
-  const bool swm = X->testcase > 1;
-  const int active = swm ? (0xF | (X->testcase == 2 ? 0x10 : 0)) : 0x10;
-  // stage st reads y_n, a, b, a and writes a, b, a, y_n
-  auto in = [](int st, double *yn, double *a, double *b) { return st == 0 ? yn : (st == 2 ? b : a); };
-  auto out = [](int st, double *yn, double *a, double *b) {
-    return st == 0 ? a : (st == 1 ? b : (st == 2 ? a : yn));
-  };
-  for (int step = 0; step < nsteps; ++step) {
-    for (int st = 0; st < 4; ++st) {
-      imodel::MoistArgs A;
-      A.stage = st;
-      A.dt = dt;
-      A.swm = swm ? 1 : 0;
-      A.active = active;
-      A.upw1 = X->upw1;
-      const double *h_in = swm ? in(st, W.yn_h, W.ya_h, W.yb_h) : W.yn_h;
-      const double *u_in = swm ? in(st, W.yn_u, W.ya_u, W.yb_u) : W.yn_u;
-      if (swm)
-        imodel::launch_stage64(H->M, W, h_in, u_in, nullptr, nullptr, -1, dt, H->stream);
-      A.h_in = h_in;
-      A.u_in = u_in;
-      A.tend_h = W.tend_h;
-      A.tend_u = W.tend_u;
-      A.h_ed = W.h_ed;
-      A.yn_h = W.yn_h;
-      A.acc_h = W.acc_h;
-      A.h_out = out(st, W.yn_h, W.ya_h, W.yb_h);
-      A.yn_u = W.yn_u;
-      A.acc_u = W.acc_u;
-      A.u_out = out(st, W.yn_u, W.ya_u, W.yb_u);
-      for (int k = 0; k < 5; ++k) {
-        double **q = X->q[k];
-        const bool adv = (active >> k) & 1;
-        A.q_in[k] = adv ? in(st, q[0], q[1], q[2]) : q[0];
-        A.q_yn[k] = q[0];
-        A.q_acc[k] = q[3];
-        A.q_out[k] = out(st, q[0], q[1], q[2]);
-      }
-      A.uphi = X->uphi;
-      A.th = X->th;
-      A.ex20 = X->ex20;
-      A.qv = X->qv;
-      A.qc = X->qc;
-      A.qr = X->qr;
-      A.q0 = X->q0;
-      A.flags = H->d_flags;
-      imodel::launch_moist_stage(H->M, A, H->stream);
-    }
-    imodel::launch_moist_q(H->nv, W.yn_h, X->q[1][0], X->q[2][0], X->q[3][0], X->qv, X->qc,
-                           X->qr, H->d_flags, H->stream);
-  }
+  int rc = moist_graph(X, dt);
+  if (rc) return rc;
+  for (int step = 0; step < nsteps; ++step)
+    if (cudaGraphLaunch(X->graph, H->stream) != cudaSuccess)
+      return imodel::set_error(H, IMODEL_SWM_ECUDA, "cudaGraphLaunch failed");
   if (cudaGetLastError() != cudaSuccess) return imodel::set_error(H, IMODEL_SWM_ECUDA, "launch failed");
   return imodel::check_flags(H);
 }
@@ -1832,6 +1867,7 @@ int imodel_moist_get_state(void *handle, double *const y[7]) {
 int imodel_moist_destroy(void *handle) {
   Moist *X = static_cast<Moist *>(handle);
   if (!X) return IMODEL_SWM_OK;
+  if (X->graph) cudaGraphExecDestroy(X->graph);
   imodel::destroy(X->H);
   delete X;
   return IMODEL_SWM_OK;
