@@ -60,6 +60,8 @@ struct DevMesh {
   // their FP32 coefficients (swm_layout.h): q_e weights [2][ne] (pxt16,
   // gass18), dtred's PV-flux coefficients [6][ne]
   const float *e_qw32, *e_dtc32;
+  // pxt16's pered coefficients by cell [36][nv] (the cell-centred variants)
+  const float *c_C32;
 };
 
 // Launch configuration of the FP32 stage kernels, chosen by the autotuner.
@@ -165,10 +167,12 @@ void learned_launch(const DevMesh &M, const LearnedDev &L, const float *hd, cons
 inline int launches_per_stage(int precision_fp32, int variant, bool dif_on = false,
                               bool dif_k4 = false, bool apvm_on = false, int scheme = 0) {
   int n = (precision_fp32 && variant >= 1) ? 3 : 4;
-  if (scheme == 3) n += 1;  // dtred: the triangle reconstruction of uh q
+  if (!precision_fp32 && scheme == 3) n += 1;  // dtred: the triangle reconstruction of uh q
   if (dif_on) n += (dif_k4 ? 3 : 1) + ((precision_fp32 && variant == 0) ? 1 : 0);
-  // FP32: the reconstructions, plus the edge pre-pass in variants 1 and 2
-  if (apvm_on) n += precision_fp32 ? (variant >= 1 ? 2 : 1) : 2;
+  // FP32 variants 1 and 2: the edge pre-pass for APVM's or pxt16's edge PV
+  if (precision_fp32 && variant >= 1 && (apvm_on || scheme == 1)) n += 1;
+  // the reconstructions
+  if (apvm_on) n += precision_fp32 ? 1 : 2;
   return n;
 }
 // The diffusion coefficients from the cell field kf (device order, FP64;

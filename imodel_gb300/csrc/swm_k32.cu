@@ -288,6 +288,85 @@ __global__ void __launch_bounds__(512) k_cell32v2(DevMesh M, const float *__rest
                                       tend, stage, dt, grav, h_ref, kcv, coefdiv);
 }
 
+// ---- pxt16 in the cell-centred form (variants 1, 2) ------------------------
+// The pass of k_cell32v2 with pxt16's pieces: each slot's edge PV from the
+// edge pre-pass (the distance-weighted q_e of scalar_tr2ed's bary branch,
+// APVM's upwinding when on), the Perot kinetic energy (kinetic_energy_hx,
+// perhx branch: half the squared Perot velocity of the cell on its tangent
+// plane) and pered's coefficients by cell in place of TRSK's kite fractions:
+//     Z_c(i) = sum_{j != i} C_c(i, j) F_j (q_i + q_j)
+// (coriolis_ed's pered branch, swm_operators.f90:1330-1377, split by cell).
+__global__ void __launch_bounds__(512) k_cell32p(DevMesh M, const float *__restrict__ hd,
+                                                 const float *__restrict__ u,
+                                                 const float *__restrict__ q_ed,
+                                                 float *__restrict__ bern,
+                                                 float *__restrict__ zflux,
+                                                 const float *__restrict__ yn,
+                                                 float *__restrict__ acc,
+                                                 float *__restrict__ yout,
+                                                 float *__restrict__ tend, int stage, float dt,
+                                                 float grav, float h_ref,
+                                                 const float *__restrict__ kcv,
+                                                 float *__restrict__ coefdiv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nv = M.nv;
+  if (i >= nv) return;
+  const int n = static_cast<int>(__ldg(&M.c_meta[i]) & 7u);
+  int ed[6], nb[6];
+  float2 kd[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const int4 pk = __ldg(&M.c_pk[j * nv + i]);
+    kd[j] = __ldg(&M.c_kd[j * nv + i]);
+    ed[j] = pk.x;
+    nb[j] = pk.y;
+  }
+  const float hi = hd[i], bt = __ldg(&M.c_bt32[i]), inva = __ldg(&M.c_inva32[i]);
+  const float ynv = stage >= 0 ? yn[i] : 0.0f, accv = stage >= 1 ? acc[i] : 0.0f;
+  float ue[6], hn[6], qs[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    ue[j] = u[ed[j]];
+    hn[j] = hd[nb[j]];
+    qs[j] = q_ed[ed[j]];
+  }
+  // unused pentagon slots repeat slot 0 with zero weights (c_kd, c_apw32)
+  float F[6], div = 0.0f, du = 0.0f, v[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    F[j] = ue[j] * (h_ref + 0.5f * (hi + hn[j]));
+    div += F[j] * kd[j].y;
+    du += ue[j] * kd[j].y;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c] = fmaf(ue[j], __ldg(&M.c_apw32[(3 * j + c) * nv + i]), v[c]);
+  }
+  const float p0 = __ldg(&M.c_p32[i]), p1 = __ldg(&M.c_p32[nv + i]), p2 = __ldg(&M.c_p32[2 * nv + i]);
+  const float vp = v[0] * p0 + v[1] * p1 + v[2] * p2;
+  const float a0 = v[0] - vp * p0, a1 = v[1] - vp * p1, a2 = v[2] - vp * p2;
+  const float ke = 0.5f * (a0 * a0 + a1 * a1 + a2 * a2);
+  if (coefdiv) coefdiv[i] = kcv[i] * (du * inva);
+  bern[i] = grav * (hi + bt) + ke;
+#pragma unroll
+  for (int si = 0; si < 6; ++si) {
+    if (si >= n) break;
+    float z = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      if (j == si || j >= n) continue;
+      z += __ldg(&M.c_C32[(6 * si + j) * nv + i]) * F[j] * (qs[si] + qs[j]);
+    }
+    zflux[6 * i + si] = z;
+  }
+  const float masseq = -div * inva;
+  if (stage < 0) {
+    tend[i] = masseq;
+  } else {
+    float a = accv;
+    yout[i] = rk_stage32(stage, masseq, ynv, &a, dt);
+    if (stage < 3) acc[i] = a;
+  }
+}
+
 // ---- variant 2: the triangle kernel on records with 16-bit indices -------
 __global__ void __launch_bounds__(512) k_tri32c(DevMesh M, const float *__restrict__ hd,
                                                 const float *__restrict__ u,
@@ -447,17 +526,22 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
     if (W.learned && stage <= 0)
       learned_launch(M, *W.learned, h_in, u_in, W.q_tr, W.h_ref, T.mlp_gather, W.flags, s);
     const Apvm<float> &A = W.apvm;
-    if (A.on) {
-      // APVM (swm_operators.f90:1495-1502): the upwinded PV of every edge
-      // from the edge pre-pass, read by the cells in place of the triangle
-      // average
-      k_apvm32<<<nbt + nblocks(M.nv, 256), 256, 0, s>>>(M, W.q_tr, u_in, A.qg, A.vhx, nbt);
-      k_edge_pre32<<<nblocks(M.ne, T.bs_pre), T.bs_pre, 0, s>>>(
-          M, h_in, u_in, W.q_tr, W.h_ed, W.uh, W.q_ed, W.h_ref, A.qg, A.vhx, A.coef, nullptr,
-          nullptr, W.pv_on, W.flags);
-    }
-    if (ev) cudaEventRecord(ev[2], s);
+    const bool pxt = W.scheme == IMODEL_SWM_PXT16;
+    // APVM (swm_operators.f90:1495-1502) and pxt16's distance-weighted q_e:
+    // the PV of every edge from the edge pre-pass, read by the cells in
+    // place of the triangle average
     if (A.on)
+      k_apvm32<<<nbt + nblocks(M.nv, 256), 256, 0, s>>>(M, W.q_tr, u_in, A.qg, A.vhx, nbt);
+    if (A.on || pxt)
+      k_edge_pre32<<<nblocks(M.ne, T.bs_pre), T.bs_pre, 0, s>>>(
+          M, h_in, u_in, W.q_tr, W.h_ed, W.uh, W.q_ed, W.h_ref, A.on ? A.qg : nullptr, A.vhx,
+          A.coef, pxt ? M.e_qw32 : nullptr, nullptr, W.pv_on, W.flags);
+    if (ev) cudaEventRecord(ev[2], s);
+    if (pxt)
+      k_cell32p<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
+          M, h_in, u_in, W.q_ed, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
+          grav, W.h_ref, D.kcv, D.on ? D.coefdiv : nullptr);
+    else if (A.on)
       k_cell32v2<true><<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
           M, h_in, u_in, W.q_ed, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
           grav, W.h_ref, D.kcv, D.on ? D.coefdiv : nullptr);

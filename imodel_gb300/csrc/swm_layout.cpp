@@ -312,6 +312,28 @@ void scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
         }
       }
     }
+    // the same coefficients by cell, for the cell-centred variants
+    const int nv = L.nv;
+    fill(L.c_C32, 36 * NV, 0.0f);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nv; ++i) {
+      const int c = L.cell_n2o[i];
+      const int n = m.nnb[c];
+      for (int si = 0; si < n; ++si) {
+        const int e = m.v_ed[6 * static_cast<size_t>(c) + si] - 1;
+        const double *nr = m.ed_nr + 3 * static_cast<size_t>(e);
+        for (int j = 0; j < n; ++j) {
+          if (j == si) continue;
+          const int k = m.v_ed[6 * static_cast<size_t>(c) + j] - 1;
+          double d = 0.0;
+          for (int q = 0; q < 3; ++q)
+            d += (m.ed_c[3 * static_cast<size_t>(k) + q] - m.v_p[3 * static_cast<size_t>(c) + q]) * nr[q];
+          const double sg = static_cast<double>(m.hx_ttgout[6 * static_cast<size_t>(c) + j]);
+          L.c_C32[static_cast<size_t>(6 * si + j) * NV + i] = static_cast<float>(
+              -0.25 * sg * d * m.edhx_leng[k] / m.hx_areag[c] * m.ed_leng[e]);
+        }
+      }
+    }
   }
   if (scheme == IMODEL_SWM_DTRED) {
     fill(L.e_dtc32, 6 * NE, 0.0f);
@@ -1128,7 +1150,7 @@ extern "C" int imodel_swm_test_layout_digest(const imodel_swm_mesh *m, int32_t s
   IMODEL_DIGEST(t_c16A) IMODEL_DIGEST(t_c16B) IMODEL_DIGEST(t_c16C) IMODEL_DIGEST(t_wb)
   IMODEL_DIGEST(t_circ32) IMODEL_DIGEST(t_kite32) IMODEL_DIGEST(t_f32) IMODEL_DIGEST(e_area)
   IMODEL_DIGEST(t_bary) IMODEL_DIGEST(e_dist) IMODEL_DIGEST(t_edarea) IMODEL_DIGEST(e_nr)
-  IMODEL_DIGEST(e_stq) IMODEL_DIGEST(e_qw32) IMODEL_DIGEST(e_dtc32)
+  IMODEL_DIGEST(e_stq) IMODEL_DIGEST(e_qw32) IMODEL_DIGEST(e_dtc32) IMODEL_DIGEST(c_C32)
 #undef IMODEL_DIGEST
   *digest = h;
   return IMODEL_SWM_OK;

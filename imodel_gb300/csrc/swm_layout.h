@@ -166,6 +166,12 @@ struct Layout {
   //           -w_i sign(tr%tg) l_s (tr%c x ed(s)%c) . nr_e / tr%areag, w_i =
   //           d2, d1 over d1 + d2: the PV flux is sum q_i c_is F_s
   HVec<float> e_qw32, e_dtc32;
+  // c_C32 [36][nv] (pxt16, the cell-centred variants) the pered coefficients
+  //           by cell: c_C32[6 i + j] couples the flux F_j (q_i + q_j) of
+  //           the cell's slot-j edge into the PV flux of its slot-i edge,
+  //           times that edge's ed%leng (the edge kernel divides the sum of
+  //           its two cells' contributions by l_e)
+  HVec<float> c_C32;
 };
 
 // Builds the layout from a reference mesh; returns "" or an error message.

@@ -85,6 +85,24 @@ def test_fp32_close_to_oracle(grid_at, variant):
     assert rel_h(hg, hp) > 50 * eh and rel_u(ug, up) > 50 * eu
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_fp32_with_diffusion_close_to_oracle(grid_at, variant):
+    """APVM with Laplacian and hyperdiffusion on, in each FP32 variant."""
+    g = grid_at(4)
+    h, u = fields.balanced_state(g, lmax=12, seed=12)
+    m = SWM(g, "fp32")
+    m.set_apvm(1.0, 600.0)
+    m.set_diffusion(1.0e5, 1.0e13)
+    m.set_tuning(variant=variant)
+    hg, ug = m.ode_rk4(h, u, 600.0, 12)
+    hr, ur = oracle.Oracle(g, 2, k2=1.0e5, k4=1.0e13, pvspar=1.0, dt=600.0).run(h, u, 600.0, 12)
+    w = g.ed_leng * g.edhx_leng
+    eh = np.sqrt(np.sum(g.hx_areag * (hg - hr) ** 2) / np.sum(g.hx_areag * hr ** 2))
+    eu = np.sqrt(np.sum(w * (ug - ur) ** 2) / np.sum(w * ur ** 2))
+    print(f"variant {variant}: FP32 + APVM + diffusion vs the oracle: h {eh:.2e}, u {eu:.2e}")
+    assert eh < 1e-6 and eu < 1e-5, (eh, eu)
+
+
 def test_apvm_with_the_per_step_learned_correction(grid_at):
     """APVM and the per-step network correction (cell-centred variants) run
     together: the step differs from either alone and from plain FP32 by

@@ -1,8 +1,10 @@
 """The pxt16, gass18 and dtred method wrappers on the GPU against the CPU
 oracle: FP64 handles bit for bit (tendencies and RK4 runs, alone and with
 APVM and diffusion); FP32 handles (the generic variant-0 kernels with the
-branches' coefficients folded in FP64) within FP32 round-off of the oracle;
-the options such handles or a mesh without ed_nr cannot take are refused."""
+branches' coefficients folded in FP64, and for pxt16 also the cell-centred
+variants with pered's coefficients by cell) within FP32 round-off of the
+oracle; the options such handles or a mesh without ed_nr cannot take are
+refused."""
 import ctypes
 
 import numpy as np
@@ -90,9 +92,13 @@ def rel_l2(a, b, w):
     return float(np.sqrt(np.sum(w * (a - b) ** 2) / np.sum(w * b * b)))
 
 
-@pytest.mark.parametrize("scheme", SCHEMES)
+# (scheme, FP32 variant): pxt16 runs in all three
+FP32_CASES = [("pxt16", 0), ("pxt16", 1), ("pxt16", 2), ("gass18", 0), ("dtred", 0)]
+
+
+@pytest.mark.parametrize("scheme,variant", FP32_CASES)
 @pytest.mark.parametrize("level", [3, 5])
-def test_fp32_tendency_against_the_oracle(grid_at, scheme, level):
+def test_fp32_tendency_against_the_oracle(grid_at, scheme, variant, level):
     """Every term of the FP32 branch (depth at the triangles, q_e, the
     kinetic energy, the PV flux) against the FP64 oracle on an unbalanced
     state."""
@@ -102,22 +108,26 @@ def test_fp32_tendency_against_the_oracle(grid_at, scheme, level):
     h = h + rng.normal(0, 5.0, g.nv)
     u = u + rng.normal(0, 2.0, g.ne)
     m = SWM(g, "fp32", scheme=scheme)
+    m.set_tuning(variant=variant)
     mg, ug = m.tendency(h, u)
     m.close()
     mr, ur = oracle.Oracle(g, 2, scheme=scheme).tendency(h, u)
     em, eu = rel_max(mg, mr), rel_max(ug, ur)
-    print(f"{scheme} level {level}: FP32 tendency vs oracle (max / max) mass {em:.1e}, "
-          f"momentum {eu:.1e}")
+    print(f"{scheme} variant {variant} level {level}: FP32 tendency vs oracle (max / max) "
+          f"mass {em:.1e}, momentum {eu:.1e}")
     assert em < FP32_TEND and eu < FP32_TEND
 
 
-@pytest.mark.parametrize("scheme", SCHEMES)
-def test_fp32_run_against_the_oracle(grid_at, scheme):
+@pytest.mark.parametrize("scheme,variant", FP32_CASES)
+def test_fp32_run_against_the_oracle(grid_at, scheme, variant):
     """320 RK4 steps (1.7 days) of a seeded balanced state at level 5."""
     g = grid_at(5)
     h, u = fields.balanced_state(g, lmax=24, seed=23)
     m = SWM(g, "fp32", scheme=scheme)
-    assert m.launch_count(1) == 16   # four variant-0 kernels per stage, dtred included
+    m.set_tuning(variant=variant)
+    # four kernels per stage: variant 0's, dtred included, or the
+    # cell-centred three and the edge pre-pass of pxt16's q_e
+    assert m.launch_count(1) == 16
     m.set_state(h, u)
     m.advance(450.0, 320)
     hg, ug = m.get_state()
@@ -125,33 +135,41 @@ def test_fp32_run_against_the_oracle(grid_at, scheme):
     hr, ur = oracle.Oracle(g, 2, scheme=scheme).run(h, u, 450.0, 320)
     eh, eu = rel_l2(hg, hr, g.hx_areag), rel_l2(ug, ur, g.ed_leng * g.edhx_leng)
     dh = rel_l2(hr, h, g.hx_areag)
-    print(f"{scheme}: FP32 vs FP64 oracle after 320 steps h {eh:.1e}, u {eu:.1e} "
-          f"(the flow itself changed h by {dh:.1e})")
+    print(f"{scheme} variant {variant}: FP32 vs FP64 oracle after 320 steps h {eh:.1e}, "
+          f"u {eu:.1e} (the flow itself changed h by {dh:.1e})")
     assert eh < FP32_RUN_H and eu < FP32_RUN_U
 
 
-def test_fp32_with_apvm(grid_at):
+@pytest.mark.parametrize("variant", [0, 1])
+def test_fp32_with_apvm(grid_at, variant):
     g = grid_at(4)
     h, u = fields.balanced_state(g, lmax=12, seed=24)
     dt = 600.0
     m = SWM(g, "fp32", scheme="pxt16")
     m.set_apvm(0.5, dt)
+    m.set_tuning(variant=variant)
     hg, ug = m.ode_rk4(h, u, dt, 48)
     m.close()
     hr, ur = oracle.Oracle(g, 2, scheme="pxt16", pvspar=0.5, dt=dt).run(h, u, dt, 48)
     eh, eu = rel_l2(hg, hr, g.hx_areag), rel_l2(ug, ur, g.ed_leng * g.edhx_leng)
-    print(f"pxt16 + apvm: FP32 vs FP64 oracle after 48 steps h {eh:.1e}, u {eu:.1e}")
+    print(f"pxt16 + apvm, variant {variant}: FP32 vs FP64 oracle after 48 steps h {eh:.1e}, "
+          f"u {eu:.1e}")
     assert eh < FP32_RUN_H and eu < FP32_RUN_U
 
 
 def test_refusals(grid_at):
     g = grid_at(3)
-    # the FP32 branches run in the variant-0 kernels only, and the learned
+    # gass18 and dtred run in the variant-0 kernels only, and the learned
     # corrections are built on trsk10
+    for scheme in ("gass18", "dtred"):
+        m = SWM(g, "fp32", scheme=scheme)
+        with pytest.raises(SWMError) as e:
+            m.set_tuning(variant=1)
+        assert e.value.code == _capi.EINVAL
+        m.close()
     m = SWM(g, "fp32", scheme="pxt16")
-    with pytest.raises(SWMError) as e:
-        m.set_tuning(variant=1)
-    assert e.value.code == _capi.EINVAL
+    for v in (1, 2, 0):
+        m.set_tuning(variant=v)
     m.close()
     with pytest.raises(SWMError) as e:
         SWM(g, "fp32", scheme="gass18", learned_params=np.zeros(100, dtype=np.float32))
