@@ -797,7 +797,10 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
       return rc;
   }
   // the other method wrappers' geometry (empty vectors upload as NULL)
-  if (H->precision == IMODEL_SWM_FP32 && (rc = upload(H, L.c_C32, &M.c_C32))) return rc;
+  if (H->precision == IMODEL_SWM_FP32 &&
+      ((rc = upload(H, L.c_C32, &M.c_C32)) || (rc = upload(H, L.c_gsel, &M.c_gsel)) ||
+       (rc = upload(H, L.c_gout, &M.c_gout))))
+    return rc;
   if ((rc = upload(H, L.t_bary, &M.t_bary)) || (rc = upload(H, L.e_dist, &M.e_dist)) ||
       (rc = upload(H, L.t_edarea, &M.t_edarea)) || (rc = upload(H, L.e_nr, &M.e_nr)) ||
       (rc = upload(H, L.e_stq, &M.e_stq)))
@@ -847,10 +850,10 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
     if ((rc = alloc_work(H, H->W32))) return rc;
     H->W32.h_ref = keep;
     if ((rc = dalloc(H, &H->W32.zflux, static_cast<size_t>(kMaxNb) * L.nv))) return rc;
-    // gass18 and dtred run in the generic FP32 kernels (variant 0), pxt16
+    // dtred runs in the generic FP32 kernels (variant 0), pxt16 and gass18
     // also in the cell-centred variants
     H->W32.scheme = scheme;
-    if (scheme == IMODEL_SWM_GASS18 || scheme == IMODEL_SWM_DTRED) H->W32.tune.variant = 0;
+    if (scheme == IMODEL_SWM_DTRED) H->W32.tune.variant = 0;
     if (scheme == IMODEL_SWM_GASS18 && (rc = dalloc(H, &H->W32.h_trs, L.nt))) return rc;
     if (o && o->learned == 1 && (rc = setup_learned(H, m, L, o))) return rc;
   }
@@ -1278,8 +1281,8 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
   imodel::Tune best;
   float best_ms = 1e30f;
   // the learned correction is wired into the cell-centred variants only,
-  // gass18 and dtred into the variant-0 kernels
-  const bool v0_only = H->W32.scheme == IMODEL_SWM_GASS18 || H->W32.scheme == IMODEL_SWM_DTRED;
+  // dtred into the variant-0 kernels
+  const bool v0_only = H->W32.scheme == IMODEL_SWM_DTRED;
   for (int v = H->learned_mode == 1 ? 1 : 0; v <= (v0_only ? 0 : 2); ++v)
     for (int b : sizes) {
       imodel::Tune t;
@@ -1355,8 +1358,8 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[6]) {
   if (H->learned_mode == 1 && choice[0] == 0)
     return imodel::set_error(H, IMODEL_SWM_EINVAL,
                              "the learned correction runs with the cell-centred variants (1, 2) only");
-  if ((H->W32.scheme == IMODEL_SWM_GASS18 || H->W32.scheme == IMODEL_SWM_DTRED) && choice[0] != 0)
-    return imodel::set_error(H, IMODEL_SWM_EINVAL, "gass18 and dtred run with variant 0 only");
+  if (H->W32.scheme == IMODEL_SWM_DTRED && choice[0] != 0)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL, "dtred runs with variant 0 only");
   imodel::Tune t;
   t.variant = choice[0];
   t.bs_tri = choice[1];

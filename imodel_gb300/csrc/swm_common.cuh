@@ -60,8 +60,12 @@ struct DevMesh {
   // their FP32 coefficients (swm_layout.h): q_e weights [2][ne] (pxt16,
   // gass18), dtred's PV-flux coefficients [6][ne]
   const float *e_qw32, *e_dtc32;
-  // pxt16's pered coefficients by cell [36][nv] (the cell-centred variants)
+  // pxt16's pered coefficients by cell [36][nv], gass18's connecting-edge
+  // selectors [36][nv] and outer triangle edges [6][nv] (the cell-centred
+  // variants; swm_layout.h)
   const float *c_C32;
+  const int8_t *c_gsel;
+  const int32_t *c_gout;
 };
 
 // Launch configuration of the FP32 stage kernels, chosen by the autotuner.
@@ -170,7 +174,7 @@ inline int launches_per_stage(int precision_fp32, int variant, bool dif_on = fal
   if (!precision_fp32 && scheme == 3) n += 1;  // dtred: the triangle reconstruction of uh q
   if (dif_on) n += (dif_k4 ? 3 : 1) + ((precision_fp32 && variant == 0) ? 1 : 0);
   // FP32 variants 1 and 2: the edge pre-pass for APVM's or pxt16's edge PV
-  if (precision_fp32 && variant >= 1 && (apvm_on || scheme == 1)) n += 1;
+  if (precision_fp32 && variant >= 1 && (apvm_on || scheme == 1 || scheme == 2)) n += 1;
   // the reconstructions
   if (apvm_on) n += precision_fp32 ? 1 : 2;
   return n;

@@ -367,6 +367,116 @@ __global__ void __launch_bounds__(512) k_cell32p(DevMesh M, const float *__restr
   }
 }
 
+// ---- gass18 in the cell-centred form (variants 1, 2) ------------------------
+// TRSK's weights and kinetic energy with gass18's PV: each slot's edge PV
+// from the edge pre-pass (the rhombus PV of scalar_tr2ed's gass branch) and,
+// in the pair (i, j) of coriolis_ed's gass branch (swm_operators.f90:
+// 1378-1414), twice the PV of the connecting edge in place of q_i + q_j
+// where there is one: a cell edge or the outer edge of a cell triangle
+// (c_gsel, c_gout).
+__device__ __forceinline__ float pick12(int sel, const float (&a)[6], const float (&b)[6]) {
+  float v = a[0];
+#pragma unroll
+  for (int k = 1; k < 6; ++k) v = sel == k ? a[k] : v;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) v = sel == 6 + k ? b[k] : v;
+  return v;
+}
+
+template <int N>
+__device__ __forceinline__ void gass_cell(const DevMesh &M, int c, const float (&G)[6],
+                                          const float (&qs)[6], const float (&qo)[6],
+                                          const float (&R)[6], unsigned tneg, float (&Z)[6]) {
+  const int nv = M.nv;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    float w = 0.0f, acc = 0.0f;
+#pragma unroll
+    for (int s = 1; s < N; ++s) {
+      const int j = (i + s) % N;
+      w += R[(i + s - 1) % N];
+      const int sel = __ldg(&M.c_gsel[(6 * i + j) * nv + c]);
+      const float P = sel < 0 ? qs[i] + qs[j] : 2.0f * pick12(sel, qs, qo);
+      acc += (w - 0.5f) * G[j] * P;
+    }
+    const float z = 0.5f * acc;
+    Z[i] = ((tneg >> i) & 1u) ? -z : z;
+  }
+}
+
+__global__ void __launch_bounds__(512) k_cell32g(DevMesh M, const float *__restrict__ hd,
+                                                 const float *__restrict__ u,
+                                                 const float *__restrict__ q_ed,
+                                                 float *__restrict__ bern,
+                                                 float *__restrict__ zflux,
+                                                 const float *__restrict__ yn,
+                                                 float *__restrict__ acc,
+                                                 float *__restrict__ yout,
+                                                 float *__restrict__ tend, int stage, float dt,
+                                                 float grav, float h_ref,
+                                                 const float *__restrict__ kcv,
+                                                 float *__restrict__ coefdiv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nv = M.nv;
+  if (i >= nv) return;
+  const uint32_t meta = __ldg(&M.c_meta[i]);
+  const int n = static_cast<int>(meta & 7u);
+  const unsigned tneg = meta >> 8;
+  int ed[6], nb[6], og[6];
+  float R[6];
+  float2 kd[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const int4 pk = __ldg(&M.c_pk[j * nv + i]);
+    kd[j] = __ldg(&M.c_kd[j * nv + i]);
+    ed[j] = pk.x;
+    nb[j] = pk.y;
+    R[j] = __int_as_float(pk.w);
+    og[j] = __ldg(&M.c_gout[j * nv + i]);
+  }
+  const float hi = hd[i], bt = __ldg(&M.c_bt32[i]), inva = __ldg(&M.c_inva32[i]);
+  const float ynv = stage >= 0 ? yn[i] : 0.0f, accv = stage >= 1 ? acc[i] : 0.0f;
+  float ue[6], hn[6], qs[6], qo[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    ue[j] = u[ed[j]];
+    hn[j] = hd[nb[j]];
+    qs[j] = q_ed[ed[j]];
+    qo[j] = q_ed[og[j]];
+  }
+  float G[6], div = 0.0f, ke = 0.0f, du = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const float F = ue[j] * (h_ref + 0.5f * (hi + hn[j]));
+    G[j] = F * kd[j].y;
+    div += G[j];
+    ke += kd[j].x * (ue[j] * ue[j]);
+    du += ue[j] * kd[j].y;
+  }
+  if (coefdiv) coefdiv[i] = kcv[i] * (du * inva);
+  bern[i] = grav * (hi + bt) + ke;
+  float Z[6];
+  if (n == 6)
+    gass_cell<6>(M, i, G, qs, qo, R, tneg, Z);
+  else if (n == 5)
+    gass_cell<5>(M, i, G, qs, qo, R, tneg, Z);
+  else if (n == 4)
+    gass_cell<4>(M, i, G, qs, qo, R, tneg, Z);
+  else
+    gass_cell<3>(M, i, G, qs, qo, R, tneg, Z);
+#pragma unroll
+  for (int j = 0; j < 6; ++j)
+    if (j < n) zflux[6 * i + j] = Z[j];
+  const float masseq = -div * inva;
+  if (stage < 0) {
+    tend[i] = masseq;
+  } else {
+    float a = accv;
+    yout[i] = rk_stage32(stage, masseq, ynv, &a, dt);
+    if (stage < 3) acc[i] = a;
+  }
+}
+
 // ---- variant 2: the triangle kernel on records with 16-bit indices -------
 __global__ void __launch_bounds__(512) k_tri32c(DevMesh M, const float *__restrict__ hd,
                                                 const float *__restrict__ u,
@@ -513,7 +623,8 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
   if (T.variant == 0 && D.on)  // variant 0: K div u and K_tr zeta in their own pass
     k_difcv32<<<nbc + nbt, 256, 0, s>>>(M, u_in, D.kcv, D.kt, D.coefdiv, D.coefvort, nbc);
   float *cvort = (T.variant >= 1 && D.on) ? D.coefvort : nullptr;
-  if (T.variant == 2)
+  // gass18 needs the triangle depths of the 32-bit triangle kernel
+  if (T.variant == 2 && W.scheme != IMODEL_SWM_GASS18)
     k_tri32c<<<nblocks(M.nt, T.bs_tri), T.bs_tri, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ref,
                                                            W.pv_on, W.flags, D.kt, cvort);
   else
@@ -526,18 +637,22 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
     if (W.learned && stage <= 0)
       learned_launch(M, *W.learned, h_in, u_in, W.q_tr, W.h_ref, T.mlp_gather, W.flags, s);
     const Apvm<float> &A = W.apvm;
-    const bool pxt = W.scheme == IMODEL_SWM_PXT16;
+    const bool pxt = W.scheme == IMODEL_SWM_PXT16, gass = W.scheme == IMODEL_SWM_GASS18;
     // APVM (swm_operators.f90:1495-1502) and pxt16's distance-weighted q_e:
     // the PV of every edge from the edge pre-pass, read by the cells in
     // place of the triangle average
     if (A.on)
       k_apvm32<<<nbt + nblocks(M.nv, 256), 256, 0, s>>>(M, W.q_tr, u_in, A.qg, A.vhx, nbt);
-    if (A.on || pxt)
+    if (A.on || pxt || gass)
       k_edge_pre32<<<nblocks(M.ne, T.bs_pre), T.bs_pre, 0, s>>>(
           M, h_in, u_in, W.q_tr, W.h_ed, W.uh, W.q_ed, W.h_ref, A.on ? A.qg : nullptr, A.vhx,
-          A.coef, pxt ? M.e_qw32 : nullptr, nullptr, W.pv_on, W.flags);
+          A.coef, pxt || gass ? M.e_qw32 : nullptr, gass ? W.h_trs : nullptr, W.pv_on, W.flags);
     if (ev) cudaEventRecord(ev[2], s);
-    if (pxt)
+    if (gass)
+      k_cell32g<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
+          M, h_in, u_in, W.q_ed, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
+          grav, W.h_ref, D.kcv, D.on ? D.coefdiv : nullptr);
+    else if (pxt)
       k_cell32p<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
           M, h_in, u_in, W.q_ed, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
           grav, W.h_ref, D.kcv, D.on ? D.coefdiv : nullptr);

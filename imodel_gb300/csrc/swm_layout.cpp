@@ -242,7 +242,7 @@ int edge_connection(const imodel_swm_mesh &m, int ed1, int ed2) {
 // The FP32 coefficients of the pxt16, gass18 and dtred branches (Layout:
 // t_kite32, e_qw32, e_stc32, e_dtc32), from the FP64 geometry of the same
 // branches, which build_layout has filled in device order before.
-void scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
+std::string scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
   const size_t NV = L.nv, NE = L.ne, NT = L.nt;
   (void)NV;
   const int ne = L.ne, nt = L.nt;
@@ -358,6 +358,54 @@ void scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
       }
     }
   }
+  if (scheme == IMODEL_SWM_GASS18) {
+    // the connecting edges by cell, for the cell-centred variants
+    const int nv = L.nv;
+    fill(L.c_gsel, 36 * NV, static_cast<int8_t>(-1));
+    L.c_gout.resize(6 * NV);
+    const std::string err = par_for(nv, [&](int64_t i64) -> std::string {
+      const int i = static_cast<int>(i64);
+      const int c = L.cell_n2o[i];
+      const int n = m.nnb[c];
+      int outer[6];
+      for (int t = 0; t < 6; ++t) {
+        outer[t] = -1;
+        if (t >= n) {
+          L.c_gout[static_cast<size_t>(t) * NV + i] = L.c_gout[i];
+          continue;
+        }
+        const int tr = m.v_tr[6 * static_cast<size_t>(c) + t] - 1;
+        for (int q = 0; q < 3; ++q) {
+          const int e = m.tr_ed[3 * static_cast<size_t>(tr) + q] - 1;
+          if (m.ed_v[2 * static_cast<size_t>(e)] - 1 != c && m.ed_v[2 * static_cast<size_t>(e) + 1] - 1 != c)
+            outer[t] = e;
+        }
+        if (outer[t] < 0) return "triangle " + std::to_string(tr + 1) + " has no edge opposite cell " + std::to_string(c + 1);
+        L.c_gout[static_cast<size_t>(t) * NV + i] = L.edge_o2n[outer[t]];
+      }
+      for (int si = 0; si < n; ++si) {
+        const int e = m.v_ed[6 * static_cast<size_t>(c) + si] - 1;
+        for (int j = 0; j < n; ++j) {
+          if (j == si) continue;
+          const int k = m.v_ed[6 * static_cast<size_t>(c) + j] - 1;
+          const int c3 = edge_connection(m, e, k);
+          if (c3 < 0) continue;
+          int sel = -1;
+          for (int q = 0; q < n && sel < 0; ++q)
+            if (m.v_ed[6 * static_cast<size_t>(c) + q] - 1 == c3) sel = q;
+          for (int t = 0; t < n && sel < 0; ++t)
+            if (outer[t] == c3) sel = 6 + t;
+          if (sel < 0)
+            return "gass18's connecting edge " + std::to_string(c3 + 1) + " lies outside cell " +
+                   std::to_string(c + 1) + " and its triangles";
+          L.c_gsel[static_cast<size_t>(6 * si + j) * NV + i] = static_cast<int8_t>(sel);
+        }
+      }
+      return std::string();
+    });
+    if (!err.empty()) return err;
+  }
+  return "";
 }
 
 }  // namespace
@@ -761,7 +809,8 @@ std::string build_layout(const imodel_swm_mesh &m, const double *bt, Layout &L, 
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < ne; ++i)
       for (int k = 0; k < 3; ++k) L.e_nr[k * NE + i] = m.ed_nr[3 * static_cast<size_t>(L.edge_n2o[i]) + k];
-    scheme_fp32(m, L, scheme);
+    const std::string msg = scheme_fp32(m, L, scheme);
+    if (!msg.empty()) return msg;
   }
   L.t_recA.resize(4 * NT);
   L.t_recB.resize(4 * NT);
@@ -1150,7 +1199,7 @@ extern "C" int imodel_swm_test_layout_digest(const imodel_swm_mesh *m, int32_t s
   IMODEL_DIGEST(t_c16A) IMODEL_DIGEST(t_c16B) IMODEL_DIGEST(t_c16C) IMODEL_DIGEST(t_wb)
   IMODEL_DIGEST(t_circ32) IMODEL_DIGEST(t_kite32) IMODEL_DIGEST(t_f32) IMODEL_DIGEST(e_area)
   IMODEL_DIGEST(t_bary) IMODEL_DIGEST(e_dist) IMODEL_DIGEST(t_edarea) IMODEL_DIGEST(e_nr)
-  IMODEL_DIGEST(e_stq) IMODEL_DIGEST(e_qw32) IMODEL_DIGEST(e_dtc32) IMODEL_DIGEST(c_C32)
+  IMODEL_DIGEST(e_stq) IMODEL_DIGEST(e_qw32) IMODEL_DIGEST(e_dtc32) IMODEL_DIGEST(c_C32) IMODEL_DIGEST(c_gsel) IMODEL_DIGEST(c_gout)
 #undef IMODEL_DIGEST
   *digest = h;
   return IMODEL_SWM_OK;

@@ -172,6 +172,14 @@ struct Layout {
   //           times that edge's ed%leng (the edge kernel divides the sum of
   //           its two cells' contributions by l_e)
   HVec<float> c_C32;
+  // c_gsel [36][nv], c_gout [6][nv] (gass18, the cell-centred variants):
+  //           the edge whose PV, twice, replaces q_i + q_j in the cell's pair
+  //           of slots (i, j) (gass18's connecting edge, edge_connection):
+  //           -1 none, 0-5 the cell's edge in that slot, 6-11 the outer
+  //           edge of the cell's triangle in slot sel - 6, whose device
+  //           index c_gout holds
+  HVec<int8_t> c_gsel;
+  HVec<int32_t> c_gout;
 };
 
 // Builds the layout from a reference mesh; returns "" or an error message.

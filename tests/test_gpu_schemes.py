@@ -1,9 +1,9 @@
 """The pxt16, gass18 and dtred method wrappers on the GPU against the CPU
 oracle: FP64 handles bit for bit (tendencies and RK4 runs, alone and with
 APVM and diffusion); FP32 handles (the generic variant-0 kernels with the
-branches' coefficients folded in FP64, and for pxt16 also the cell-centred
-variants with pered's coefficients by cell) within FP32 round-off of the
-oracle; the options such handles or a mesh without ed_nr cannot take are
+branches' coefficients folded in FP64, and for pxt16 and gass18 also the
+cell-centred variants: pered's coefficients and gass18's connecting edges
+by cell) within FP32 round-off of the oracle; the options such handles or a mesh without ed_nr cannot take are
 refused."""
 import ctypes
 
@@ -92,8 +92,9 @@ def rel_l2(a, b, w):
     return float(np.sqrt(np.sum(w * (a - b) ** 2) / np.sum(w * b * b)))
 
 
-# (scheme, FP32 variant): pxt16 runs in all three
-FP32_CASES = [("pxt16", 0), ("pxt16", 1), ("pxt16", 2), ("gass18", 0), ("dtred", 0)]
+# (scheme, FP32 variant): pxt16 and gass18 run in all three
+FP32_CASES = [("pxt16", 0), ("pxt16", 1), ("pxt16", 2), ("gass18", 0), ("gass18", 1),
+              ("gass18", 2), ("dtred", 0)]
 
 
 @pytest.mark.parametrize("scheme,variant", FP32_CASES)
@@ -159,18 +160,18 @@ def test_fp32_with_apvm(grid_at, variant):
 
 def test_refusals(grid_at):
     g = grid_at(3)
-    # gass18 and dtred run in the variant-0 kernels only, and the learned
-    # corrections are built on trsk10
-    for scheme in ("gass18", "dtred"):
-        m = SWM(g, "fp32", scheme=scheme)
-        with pytest.raises(SWMError) as e:
-            m.set_tuning(variant=1)
-        assert e.value.code == _capi.EINVAL
-        m.close()
-    m = SWM(g, "fp32", scheme="pxt16")
-    for v in (1, 2, 0):
-        m.set_tuning(variant=v)
+    # dtred runs in the variant-0 kernels only, and the learned corrections
+    # are built on trsk10
+    m = SWM(g, "fp32", scheme="dtred")
+    with pytest.raises(SWMError) as e:
+        m.set_tuning(variant=1)
+    assert e.value.code == _capi.EINVAL
     m.close()
+    for scheme in ("pxt16", "gass18"):
+        m = SWM(g, "fp32", scheme=scheme)
+        for v in (1, 2, 0):
+            m.set_tuning(variant=v)
+        m.close()
     with pytest.raises(SWMError) as e:
         SWM(g, "fp32", scheme="gass18", learned_params=np.zeros(100, dtype=np.float32))
     assert e.value.code == _capi.EINVAL
