@@ -1493,6 +1493,8 @@ const char *imodel_swm_main_kernel(void *handle) {
     return H->W64.scheme == IMODEL_SWM_PXT16 || H->W64.scheme == IMODEL_SWM_DTRED ? "k_edge64r"
                                                                                   : "k_edge64";
   const int v = H->W32.tune.variant;
+  if (v >= 1 && H->W32.scheme == IMODEL_SWM_PXT16) return "k_cell32p";
+  if (v >= 1 && H->W32.scheme == IMODEL_SWM_GASS18) return "k_cell32g";
   return v >= 1 ? "k_cell32v2" : "k_edge32";
 }
 
