@@ -799,7 +799,9 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
   // the other method wrappers' geometry (empty vectors upload as NULL)
   if (H->precision == IMODEL_SWM_FP32 &&
       ((rc = upload(H, L.c_C32, &M.c_C32)) || (rc = upload(H, L.c_gsel, &M.c_gsel)) ||
-       (rc = upload(H, L.c_gout, &M.c_gout))))
+       (rc = upload(H, L.c_gout, &M.c_gout)) || (rc = upload(H, L.t_dpa32, &M.t_dpa32)) ||
+       (rc = upload(H, L.t_dopp, &M.t_dopp)) || (rc = upload(H, L.e_nr32, &M.e_nr32)) ||
+       (rc = upload(H, L.e_dw32, &M.e_dw32))))
     return rc;
   if ((rc = upload(H, L.t_bary, &M.t_bary)) || (rc = upload(H, L.e_dist, &M.e_dist)) ||
       (rc = upload(H, L.t_edarea, &M.t_edarea)) || (rc = upload(H, L.e_nr, &M.e_nr)) ||
@@ -850,11 +852,12 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
     if ((rc = alloc_work(H, H->W32))) return rc;
     H->W32.h_ref = keep;
     if ((rc = dalloc(H, &H->W32.zflux, static_cast<size_t>(kMaxNb) * L.nv))) return rc;
-    // dtred runs in the generic FP32 kernels (variant 0), pxt16 and gass18
-    // also in the cell-centred variants
+    // the method wrappers run in every variant (the cell-centred ones with
+    // their coefficients by cell or, for dtred, by triangle)
     H->W32.scheme = scheme;
-    if (scheme == IMODEL_SWM_DTRED) H->W32.tune.variant = 0;
     if (scheme == IMODEL_SWM_GASS18 && (rc = dalloc(H, &H->W32.h_trs, L.nt))) return rc;
+    if (scheme == IMODEL_SWM_DTRED && (rc = dalloc(H, &H->W32.vhq, 3 * static_cast<size_t>(L.nt))))
+      return rc;
     if (o && o->learned == 1 && (rc = setup_learned(H, m, L, o))) return rc;
   }
   if (H->learned_mode == 2) {
@@ -1280,10 +1283,8 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
   const int sizes[3] = {128, 256, 512};
   imodel::Tune best;
   float best_ms = 1e30f;
-  // the learned correction is wired into the cell-centred variants only,
-  // dtred into the variant-0 kernels
-  const bool v0_only = H->W32.scheme == IMODEL_SWM_DTRED;
-  for (int v = H->learned_mode == 1 ? 1 : 0; v <= (v0_only ? 0 : 2); ++v)
+  // the learned correction is wired into the cell-centred variants only
+  for (int v = H->learned_mode == 1 ? 1 : 0; v <= 2; ++v)
     for (int b : sizes) {
       imodel::Tune t;
       t.variant = v;
@@ -1358,8 +1359,6 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[6]) {
   if (H->learned_mode == 1 && choice[0] == 0)
     return imodel::set_error(H, IMODEL_SWM_EINVAL,
                              "the learned correction runs with the cell-centred variants (1, 2) only");
-  if (H->W32.scheme == IMODEL_SWM_DTRED && choice[0] != 0)
-    return imodel::set_error(H, IMODEL_SWM_EINVAL, "dtred runs with variant 0 only");
   imodel::Tune t;
   t.variant = choice[0];
   t.bs_tri = choice[1];
@@ -1495,6 +1494,7 @@ const char *imodel_swm_main_kernel(void *handle) {
   const int v = H->W32.tune.variant;
   if (v >= 1 && H->W32.scheme == IMODEL_SWM_PXT16) return "k_cell32p";
   if (v >= 1 && H->W32.scheme == IMODEL_SWM_GASS18) return "k_cell32g";
+  if (v >= 1 && H->W32.scheme == IMODEL_SWM_DTRED) return "k_cell32v2";
   return v >= 1 ? "k_cell32v2" : "k_edge32";
 }
 

@@ -66,6 +66,10 @@ struct DevMesh {
   const float *c_C32;
   const int8_t *c_gsel;
   const int32_t *c_gout;
+  // dtred's Perot weights by triangle [9][nt], opposite corners [nt], and
+  // per edge nr [3][ne] and the triangle weights [2][ne] (swm_layout.h)
+  const float *t_dpa32, *e_nr32, *e_dw32;
+  const uint8_t *t_dopp;
 };
 
 // Launch configuration of the FP32 stage kernels, chosen by the autotuner.
@@ -129,6 +133,7 @@ struct Work {
   int scheme = 0;
   T *eta_t = nullptr, *h_trs = nullptr;  // [nt] gass18: eta and h_tr for the rhombus PV
   T *vhq = nullptr;                      // [3][nt] dtred: Perot reconstruction of uh, times q
+                                         // (FP64, and FP32 variants 1 and 2)
   T h_ref;           // FP32: h is stored as h - h_ref
   int pv_on;         // testcase >= 2: q = eta / h_tr, else q = 0
   int mom_on;        // testcase >= 2: momentum tendency kept, else zeroed

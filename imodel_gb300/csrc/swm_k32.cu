@@ -268,8 +268,9 @@ __global__ void __launch_bounds__(256) k_diflap32(DevMesh M, const float *__rest
 }
 
 // ---- cell-centred TRSK (variant 1), bodies in swm_k32_body.cuh ------------
-// kEdgePV: q_tr is the edges' PV from the edge pre-pass (APVM)
-template <bool kEdgePV>
+// kEdgePV: q_tr is the edges' PV from the edge pre-pass (APVM); kZ false:
+// no PV-flux terms (dtred forms its PV flux at the triangles)
+template <bool kEdgePV, bool kZ = true>
 __global__ void __launch_bounds__(512) k_cell32v2(DevMesh M, const float *__restrict__ hd,
                                                   const float *__restrict__ u,
                                                   const float *__restrict__ q_tr,
@@ -284,8 +285,8 @@ __global__ void __launch_bounds__(512) k_cell32v2(DevMesh M, const float *__rest
                                                   float *__restrict__ coefdiv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= M.nv) return;
-  cell_body<OneRun, LdPlain, kEdgePV>(M, i, OneRun{}, hd, u, q_tr, bern, zflux, yn, acc, yout,
-                                      tend, stage, dt, grav, h_ref, kcv, coefdiv);
+  cell_body<OneRun, LdPlain, kEdgePV, kZ>(M, i, OneRun{}, hd, u, q_tr, bern, zflux, yn, acc,
+                                          yout, tend, stage, dt, grav, h_ref, kcv, coefdiv);
 }
 
 // ---- pxt16 in the cell-centred form (variants 1, 2) ------------------------
@@ -477,6 +478,77 @@ __global__ void __launch_bounds__(512) k_cell32g(DevMesh M, const float *__restr
   }
 }
 
+// ---- dtred in the cell-centred form (variants 1, 2) ------------------------
+// coriolis_ed's dtred branch (swm_operators.f90:1310-1329) reconstructs q F
+// at the edge's two triangles: Q_e = -sum_i w_i q_ti (P_ti . nr_e), P_t the
+// Perot vector of uh over the triangle's edges.  The triangle kernel forms
+// q_t P_t once per triangle (uh_s = u_s (h_ref + the mean of the two
+// corners on edge s), the edge pre-pass's F bit for bit); the edge kernel
+// projects the two triangles' vectors on its normal.
+__global__ void __launch_bounds__(512) k_tri32d(DevMesh M, const float *__restrict__ hd,
+                                                const float *__restrict__ u,
+                                                float *__restrict__ q_tr, float h_ref,
+                                                int pv_on, int *flags,
+                                                const float *__restrict__ kt,
+                                                float *__restrict__ coefvort,
+                                                float *__restrict__ wq) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = M.nt;
+  if (t >= nt) return;
+  const int4 a = __ldg(&M.t_recA[t]), b = __ldg(&M.t_recB[t]);
+  const float4 c = __ldg(&M.t_recC[t]);
+  const int ed[3] = {a.x, a.y, a.z}, cv[3] = {a.w, b.x, b.y};
+  const float circ[3] = {__int_as_float(b.z), __int_as_float(b.w), c.x};
+  const float kite[3] = {c.y, c.z, c.w};
+  tri_core<OneRun, LdPlain>(t, OneRun{}, ed, cv, circ, kite, __ldg(&M.t_f32[t]), hd, u, q_tr,
+                            h_ref, pv_on, flags, kt, coefvort, nullptr);
+  const float q = q_tr[t];
+  const unsigned opp = __ldg(&M.t_dopp[t]);
+  const float hc[3] = {hd[cv[0]], hd[cv[1]], hd[cv[2]]};
+  float P[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    const int o = static_cast<int>((opp >> (2 * s)) & 3u);
+    const float ha = o == 0 ? hc[1] : hc[0], hb = o == 2 ? hc[1] : hc[2];
+    const float uh = u[ed[s]] * (h_ref + 0.5f * (ha + hb));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) P[k] = fmaf(uh, __ldg(&M.t_dpa32[(3 * s + k) * nt + t]), P[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) wq[k * nt + t] = q * P[k];
+}
+
+// -grad B - Q_e and the momentum RK stage of edge e (dtred)
+__global__ void __launch_bounds__(512) k_edge32d(DevMesh M, const float *__restrict__ bern,
+                                                 const float *__restrict__ wq,
+                                                 const float *__restrict__ yn,
+                                                 float *__restrict__ acc,
+                                                 float *__restrict__ yout,
+                                                 float *__restrict__ tend, int stage, float dt,
+                                                 int mom_on, const float *__restrict__ dif1,
+                                                 const float *__restrict__ dif2) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ne = M.ne, nt = M.nt;
+  if (e >= ne) return;
+  const float g = (bern[__ldg(&M.e_v[ne + e])] - bern[__ldg(&M.e_v[e])]) * __ldg(&M.e_grad32[e]);
+  const float n0 = __ldg(&M.e_nr32[e]), n1 = __ldg(&M.e_nr32[ne + e]), n2 = __ldg(&M.e_nr32[2 * ne + e]);
+  float q = 0.0f;
+#pragma unroll
+  for (int si = 0; si < 2; ++si) {
+    const int t = __ldg(&M.e_sh[si * ne + e]);
+    const float d = wq[t] * n0 + wq[nt + t] * n1 + wq[2 * nt + t] * n2;
+    q -= __ldg(&M.e_dw32[si * ne + e]) * d;
+  }
+  float momeq = -g - q;
+  if (dif1) momeq += dif1[e];
+  if (dif2) momeq -= dif2[e];
+  if (!mom_on) momeq = 0.0f;
+  if (stage < 0)
+    tend[e] = momeq;
+  else
+    yout[e] = rk_stage32(stage, momeq, yn[e], acc + e, dt);
+}
+
 // ---- variant 2: the triangle kernel on records with 16-bit indices -------
 __global__ void __launch_bounds__(512) k_tri32c(DevMesh M, const float *__restrict__ hd,
                                                 const float *__restrict__ u,
@@ -623,8 +695,13 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
   if (T.variant == 0 && D.on)  // variant 0: K div u and K_tr zeta in their own pass
     k_difcv32<<<nbc + nbt, 256, 0, s>>>(M, u_in, D.kcv, D.kt, D.coefdiv, D.coefvort, nbc);
   float *cvort = (T.variant >= 1 && D.on) ? D.coefvort : nullptr;
-  // gass18 needs the triangle depths of the 32-bit triangle kernel
-  if (T.variant == 2 && W.scheme != IMODEL_SWM_GASS18)
+  const bool dtred1 = T.variant >= 1 && W.scheme == IMODEL_SWM_DTRED;
+  // gass18 needs the triangle depths of the 32-bit triangle kernel, dtred
+  // the Perot vectors of its own
+  if (dtred1)
+    k_tri32d<<<nblocks(M.nt, T.bs_tri), T.bs_tri, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ref,
+                                                           W.pv_on, W.flags, D.kt, cvort, W.vhq);
+  else if (T.variant == 2 && W.scheme != IMODEL_SWM_GASS18)
     k_tri32c<<<nblocks(M.nt, T.bs_tri), T.bs_tri, 0, s>>>(M, h_in, u_in, W.q_tr, W.h_ref,
                                                            W.pv_on, W.flags, D.kt, cvort);
   else
@@ -656,6 +733,10 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
       k_cell32p<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
           M, h_in, u_in, W.q_ed, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
           grav, W.h_ref, D.kcv, D.on ? D.coefdiv : nullptr);
+    else if (dtred1)
+      k_cell32v2<false, false><<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
+          M, h_in, u_in, W.q_tr, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
+          grav, W.h_ref, D.kcv, D.on ? D.coefdiv : nullptr);
     else if (A.on)
       k_cell32v2<true><<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
           M, h_in, u_in, W.q_ed, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
@@ -666,9 +747,13 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
           grav, W.h_ref, D.kcv, D.on ? D.coefdiv : nullptr);
     diffusion_tail();
     if (ev) cudaEventRecord(ev[3], s);
-    k_edge32v2<<<nblocks((M.ne + 1) / 2, T.bs_edge), T.bs_edge, 0, s>>>(
-        M, W.bern, W.zflux, W.yn_u, W.acc_u, u_out, W.tend_u, stage, dt, W.mom_on,
-        static_cast<float>(M.erad), W.learned ? W.learned->corr : nullptr, dif1, dif2);
+    if (dtred1)
+      k_edge32d<<<nblocks(M.ne, T.bs_edge), T.bs_edge, 0, s>>>(
+          M, W.bern, W.vhq, W.yn_u, W.acc_u, u_out, W.tend_u, stage, dt, W.mom_on, dif1, dif2);
+    else
+      k_edge32v2<<<nblocks((M.ne + 1) / 2, T.bs_edge), T.bs_edge, 0, s>>>(
+          M, W.bern, W.zflux, W.yn_u, W.acc_u, u_out, W.tend_u, stage, dt, W.mom_on,
+          static_cast<float>(M.erad), W.learned ? W.learned->corr : nullptr, dif1, dif2);
     if (ev) cudaEventRecord(ev[4], s);
     return;
   }

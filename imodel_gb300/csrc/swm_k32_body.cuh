@@ -169,7 +169,7 @@ __device__ __forceinline__ void trsk_cell(const float (&G)[6], const float (&qs)
 // the mass RK stage.  kEdgePV: qt holds the PV of the cell's edges (formed
 // by the edge pre-pass, APVM's upwinding included) instead of the PV of its
 // triangles.
-template <class Ix = OneRun, bool kEdgePV = false>
+template <class Ix = OneRun, bool kEdgePV = false, bool kZ = true>
 __device__ __forceinline__ void cell_math(int i, uint32_t meta, const float (&R)[6],
                                           const float2 (&kd)[6], const float (&ue)[6],
                                           const float (&hn)[6], const float (&qt)[6], float hi,
@@ -199,18 +199,21 @@ __device__ __forceinline__ void cell_math(int i, uint32_t meta, const float (&R)
   // with diffusion on: K times the divergence of u
   if (coefdiv) coefdiv[ix(i)] = kcv[ix(i)] * (du * inva);
   bern[ix(i)] = grav * (hi + bt) + ke;
-  float Z[6];
-  if (n == 6)
-    trsk_cell<6>(G, qs, R, tneg, Z);
-  else if (n == 5)
-    trsk_cell<5>(G, qs, R, tneg, Z);
-  else if (n == 4)
-    trsk_cell<4>(G, qs, R, tneg, Z);
-  else
-    trsk_cell<3>(G, qs, R, tneg, Z);
+  // kZ false (dtred): the edges form their PV flux from the triangles
+  if (kZ) {
+    float Z[6];
+    if (n == 6)
+      trsk_cell<6>(G, qs, R, tneg, Z);
+    else if (n == 5)
+      trsk_cell<5>(G, qs, R, tneg, Z);
+    else if (n == 4)
+      trsk_cell<4>(G, qs, R, tneg, Z);
+    else
+      trsk_cell<3>(G, qs, R, tneg, Z);
 #pragma unroll
-  for (int j = 0; j < 6; ++j)
-    if (j < n) zflux[ix(6 * i + j)] = Z[j];
+    for (int j = 0; j < 6; ++j)
+      if (j < n) zflux[ix(6 * i + j)] = Z[j];
+  }
   const float masseq = -div * inva;
   if (stage < 0) {
     tend[ix(i)] = masseq;
@@ -228,7 +231,7 @@ __device__ __forceinline__ void cell_math(int i, uint32_t meta, const float (&R)
 // weights), gathering its neighbours' values.  The cell's own values come in
 // as arguments: h (deviation) hi, b bt, 1/(A a) inva, y_n ynv and the RK
 // accumulator accv (read for stages 1-3).
-template <class Ix, class Ld, bool kEdgePV = false>
+template <class Ix, class Ld, bool kEdgePV = false, bool kZ = true>
 __device__ __forceinline__ void cell_core(int i, Ix ix, uint32_t meta,
                                           const int (&ed)[6], const int (&nb)[6],
                                           const int (&tr)[6], const float (&R)[6],
@@ -249,8 +252,8 @@ __device__ __forceinline__ void cell_core(int i, Ix ix, uint32_t meta,
     // kEdgePV: q_tr is the edges' PV, indexed by the slot's edge
     qt[j] = Ld::ld(q_tr + ix(kEdgePV ? ed[j] : tr[j]));
   }
-  cell_math<Ix, kEdgePV>(i, meta, R, kd, ue, hn, qt, hi, bt, inva, ynv, accv, bern, zflux, acc,
-                         yout, tend, stage, dt, grav, h_ref, ix, kcv, coefdiv);
+  cell_math<Ix, kEdgePV, kZ>(i, meta, R, kd, ue, hn, qt, hi, bt, inva, ynv, accv, bern, zflux,
+                             acc, yout, tend, stage, dt, grav, h_ref, ix, kcv, coefdiv);
 }
 
 // the cell's own values from global memory
@@ -267,7 +270,7 @@ __device__ __forceinline__ void cell_own(const DevMesh &M, int i, Ix ix,
   accv = stage >= 1 ? Ld::ld(acc + ix(i)) : 0.0f;
 }
 
-template <class Ix, class Ld = LdPlain, bool kEdgePV = false>
+template <class Ix, class Ld = LdPlain, bool kEdgePV = false, bool kZ = true>
 __device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
                                           const float *__restrict__ hd,
                                           const float *__restrict__ u,
@@ -296,8 +299,9 @@ __device__ __forceinline__ void cell_body(const DevMesh &M, int i, Ix ix,
   }
   float hi, bt, inva, ynv, accv;
   cell_own<Ix, Ld>(M, i, ix, hd, yn, acc, stage, hi, bt, inva, ynv, accv);
-  cell_core<Ix, Ld, kEdgePV>(i, ix, meta, ed, nb, tr, R, kd, hi, bt, inva, ynv, accv, hd, u, q_tr,
-                             bern, zflux, acc, yout, tend, stage, dt, grav, h_ref, kcv, coefdiv);
+  cell_core<Ix, Ld, kEdgePV, kZ>(i, ix, meta, ed, nb, tr, R, kd, hi, bt, inva, ynv, accv, hd, u,
+                                 q_tr, bern, zflux, acc, yout, tend, stage, dt, grav, h_ref, kcv,
+                                 coefdiv);
 }
 
 // -grad B - (Z_c1 + Z_c2) / l_e and the momentum RK stage of edge e

@@ -357,6 +357,48 @@ std::string scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
         }
       }
     }
+    // the same by triangle, for the cell-centred variants: the Perot
+    // vector of uh at each triangle, P_t = sum_s uh_s a_ts with a_ts =
+    // sign(tr%tg) l_s (tr%c x ed(s)%c) / tr%areag, the corner opposite each
+    // edge slot (the edge's depth is the mean of the other two), and per
+    // edge nr_e and the weights w_i
+    fill(L.t_dpa32, 9 * NT, 0.0f);
+    L.t_dopp.resize(NT);
+    const std::string err = par_for(nt, [&](int64_t i64) -> std::string {
+      const int ti = static_cast<int>(i64);
+      const double tc[3] = {L.t_c[ti], L.t_c[NT + ti], L.t_c[2 * NT + ti]};
+      uint8_t opp = 0;
+      for (int s = 0; s < 3; ++s) {
+        const int ed = L.t_ed[s * NT + ti];
+        const double ec[3] = {L.e_c[ed], L.e_c[NE + ed], L.e_c[2 * NE + ed]};
+        const double cr[3] = {tc[1] * ec[2] - tc[2] * ec[1], tc[2] * ec[0] - tc[0] * ec[2],
+                              tc[0] * ec[1] - tc[1] * ec[0]};
+        const double sg = L.t_lt[s * NT + ti] < 0.0 ? -1.0 : 1.0;
+        for (int k = 0; k < 3; ++k)
+          L.t_dpa32[(3 * s + k) * NT + ti] =
+              static_cast<float>(sg * L.e_leng[ed] * cr[k] / L.t_areag[ti]);
+        int o = -1;
+        for (int q = 0; q < 3; ++q) {
+          const int c = L.t_v[q * NT + ti];
+          if (c != L.e_v[ed] && c != L.e_v[NE + ed]) o = q;
+        }
+        if (o < 0) return "triangle " + std::to_string(L.tri_n2o[ti] + 1) + ": edge slot " +
+                          std::to_string(s) + " has no opposite corner";
+        opp = static_cast<uint8_t>(opp | (o << (2 * s)));
+      }
+      L.t_dopp[ti] = opp;
+      return std::string();
+    });
+    if (!err.empty()) return err;
+    L.e_nr32.resize(3 * NE);
+    L.e_dw32.resize(2 * NE);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < ne; ++i) {
+      const double d1 = L.e_dist[i], d2 = L.e_dist[NE + i];
+      L.e_dw32[i] = static_cast<float>(d2 / (d1 + d2));
+      L.e_dw32[NE + i] = static_cast<float>(d1 / (d1 + d2));
+      for (int k = 0; k < 3; ++k) L.e_nr32[k * NE + i] = static_cast<float>(L.e_nr[k * NE + i]);
+    }
   }
   if (scheme == IMODEL_SWM_GASS18) {
     // the connecting edges by cell, for the cell-centred variants
@@ -1200,6 +1242,7 @@ extern "C" int imodel_swm_test_layout_digest(const imodel_swm_mesh *m, int32_t s
   IMODEL_DIGEST(t_circ32) IMODEL_DIGEST(t_kite32) IMODEL_DIGEST(t_f32) IMODEL_DIGEST(e_area)
   IMODEL_DIGEST(t_bary) IMODEL_DIGEST(e_dist) IMODEL_DIGEST(t_edarea) IMODEL_DIGEST(e_nr)
   IMODEL_DIGEST(e_stq) IMODEL_DIGEST(e_qw32) IMODEL_DIGEST(e_dtc32) IMODEL_DIGEST(c_C32) IMODEL_DIGEST(c_gsel) IMODEL_DIGEST(c_gout)
+  IMODEL_DIGEST(t_dpa32) IMODEL_DIGEST(t_dopp) IMODEL_DIGEST(e_nr32) IMODEL_DIGEST(e_dw32)
 #undef IMODEL_DIGEST
   *digest = h;
   return IMODEL_SWM_OK;

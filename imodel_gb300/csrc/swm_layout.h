@@ -180,6 +180,14 @@ struct Layout {
   //           index c_gout holds
   HVec<int8_t> c_gsel;
   HVec<int32_t> c_gout;
+  // dtred in the cell-centred variants: t_dpa32 [3 slots][3][nt] the
+  //           Perot weights a_ts = sign(tr%tg) l_s (tr%c x ed(s)%c) /
+  //           tr%areag of the triangle's edges (P_t = sum_s uh_s a_ts);
+  //           t_dopp [nt] the corner opposite edge slot s in bits 2s, 2s+1;
+  //           e_nr32 [3][ne] ed%nr; e_dw32 [2][ne] d2, d1 over d1 + d2.  The
+  //           PV flux is -sum_i w_i q_ti (P_ti . nr_e)
+  HVec<float> t_dpa32, e_nr32, e_dw32;
+  HVec<uint8_t> t_dopp;
 };
 
 // Builds the layout from a reference mesh; returns "" or an error message.

@@ -133,10 +133,10 @@ typedef struct imodel_swm_opts {
                          with the plain scheme                           */
   int32_t scheme;     /* IMODEL_SWM_TRSK10 (0) ... IMODEL_SWM_DTRED; the
                          other wrappers need the mesh's ed_nr and ed_c;
-                         FP32 handles run dtred in the variant-0 kernels,
-                         pxt16 and gass18 in every variant (the
-                         cell-centred ones with pered's coefficients and
-                         gass18's connecting edges by cell); the learned
+                         FP32 handles run every wrapper in every variant
+                         (the cell-centred ones with pered's coefficients
+                         and gass18's connecting edges by cell, dtred's
+                         Perot vectors by triangle); the learned
                          corrections and ensembles take trsk10 only      */
   int32_t fsphere;    /* Coriolis parameter of vort_tr (swm_operators.f90:
                          551-611): 0 f = 2 Omega sin(lat) at the triangle

@@ -1,9 +1,9 @@
 """The pxt16, gass18 and dtred method wrappers on the GPU against the CPU
 oracle: FP64 handles bit for bit (tendencies and RK4 runs, alone and with
 APVM and diffusion); FP32 handles (the generic variant-0 kernels with the
-branches' coefficients folded in FP64, and for pxt16 and gass18 also the
-cell-centred variants: pered's coefficients and gass18's connecting edges
-by cell) within FP32 round-off of the oracle; the options such handles or a mesh without ed_nr cannot take are
+branches' coefficients folded in FP64, and the cell-centred variants:
+pered's coefficients and gass18's connecting edges by cell, dtred's Perot
+vectors by triangle) within FP32 round-off of the oracle; the options such handles or a mesh without ed_nr cannot take are
 refused."""
 import ctypes
 
@@ -92,9 +92,8 @@ def rel_l2(a, b, w):
     return float(np.sqrt(np.sum(w * (a - b) ** 2) / np.sum(w * b * b)))
 
 
-# (scheme, FP32 variant): pxt16 and gass18 run in all three
-FP32_CASES = [("pxt16", 0), ("pxt16", 1), ("pxt16", 2), ("gass18", 0), ("gass18", 1),
-              ("gass18", 2), ("dtred", 0)]
+# (scheme, FP32 variant): every wrapper runs in all three
+FP32_CASES = [(s, v) for s in SCHEMES for v in (0, 1, 2)]
 
 
 @pytest.mark.parametrize("scheme,variant", FP32_CASES)
@@ -126,9 +125,10 @@ def test_fp32_run_against_the_oracle(grid_at, scheme, variant):
     h, u = fields.balanced_state(g, lmax=24, seed=23)
     m = SWM(g, "fp32", scheme=scheme)
     m.set_tuning(variant=variant)
-    # four kernels per stage: variant 0's, dtred included, or the
-    # cell-centred three and the edge pre-pass of pxt16's q_e
-    assert m.launch_count(1) == 16
+    # four kernels per stage: variant 0's, or the cell-centred three and
+    # the edge pre-pass of pxt16's and gass18's q_e; dtred's cell-centred
+    # form needs no pre-pass (its triangles form q uh)
+    assert m.launch_count(1) == (12 if scheme == "dtred" and variant else 16)
     m.set_state(h, u)
     m.advance(450.0, 320)
     hg, ug = m.get_state()
@@ -160,14 +160,9 @@ def test_fp32_with_apvm(grid_at, variant):
 
 def test_refusals(grid_at):
     g = grid_at(3)
-    # dtred runs in the variant-0 kernels only, and the learned corrections
-    # are built on trsk10
-    m = SWM(g, "fp32", scheme="dtred")
-    with pytest.raises(SWMError) as e:
-        m.set_tuning(variant=1)
-    assert e.value.code == _capi.EINVAL
-    m.close()
-    for scheme in ("pxt16", "gass18"):
+    # every wrapper runs in every FP32 variant; the learned corrections are
+    # built on trsk10
+    for scheme in SCHEMES:
         m = SWM(g, "fp32", scheme=scheme)
         for v in (1, 2, 0):
             m.set_tuning(variant=v)
