@@ -24,6 +24,9 @@ namespace imodel {
 namespace {
 
 struct Handle {
+  // gass18 on a grid whose connecting edges do not follow the cells'
+  // structure (Layout::gass_cells false): the stencil variant only
+  bool v0_only = false;
   std::string err;
   int device = 0;
   int precision = IMODEL_SWM_FP64;
@@ -798,8 +801,7 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
   }
   // the other method wrappers' geometry (empty vectors upload as NULL)
   if (H->precision == IMODEL_SWM_FP32 &&
-      ((rc = upload(H, L.c_C32, &M.c_C32)) || (rc = upload(H, L.c_gsel, &M.c_gsel)) ||
-       (rc = upload(H, L.c_gout, &M.c_gout)) || (rc = upload(H, L.t_dpa32, &M.t_dpa32)) ||
+      ((rc = upload(H, L.c_C32, &M.c_C32)) || (rc = upload(H, L.c_gout, &M.c_gout)) || (rc = upload(H, L.t_dpa32, &M.t_dpa32)) ||
        (rc = upload(H, L.t_dopp, &M.t_dopp)) || (rc = upload(H, L.e_nr32, &M.e_nr32)) ||
        (rc = upload(H, L.e_dw32, &M.e_dw32))))
     return rc;
@@ -855,6 +857,8 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
     // the method wrappers run in every variant (the cell-centred ones with
     // their coefficients by cell or, for dtred, by triangle)
     H->W32.scheme = scheme;
+    H->v0_only = scheme == IMODEL_SWM_GASS18 && !L.gass_cells;
+    if (H->v0_only) H->W32.tune.variant = 0;
     if (scheme == IMODEL_SWM_GASS18 && (rc = dalloc(H, &H->W32.h_trs, L.nt))) return rc;
     if (scheme == IMODEL_SWM_DTRED && (rc = dalloc(H, &H->W32.vhq, 3 * static_cast<size_t>(L.nt))))
       return rc;
@@ -1284,7 +1288,7 @@ int imodel_swm_autotune(void *handle, double dt, int32_t nsteps, int32_t choice[
   imodel::Tune best;
   float best_ms = 1e30f;
   // the learned correction is wired into the cell-centred variants only
-  for (int v = H->learned_mode == 1 ? 1 : 0; v <= 2; ++v)
+  for (int v = H->learned_mode == 1 ? 1 : 0; v <= (H->v0_only ? 0 : 2); ++v)
     for (int b : sizes) {
       imodel::Tune t;
       t.variant = v;
@@ -1356,6 +1360,10 @@ int imodel_swm_set_tuning(void *handle, const int32_t choice[6]) {
       return imodel::set_error(H, IMODEL_SWM_EINVAL, "block sizes must be 128, 256 or 512");
   if (choice[0] < 0 || choice[0] > 2)
     return imodel::set_error(H, IMODEL_SWM_EINVAL, "variant must be 0, 1 or 2");
+  if (H->v0_only && choice[0] != 0)
+    return imodel::set_error(H, IMODEL_SWM_EINVAL,
+                             "gass18 runs with variant 0 only on this grid (its connecting edges "
+                             "do not follow the cells' structure)");
   if (H->learned_mode == 1 && choice[0] == 0)
     return imodel::set_error(H, IMODEL_SWM_EINVAL,
                              "the learned correction runs with the cell-centred variants (1, 2) only");

@@ -60,11 +60,9 @@ struct DevMesh {
   // their FP32 coefficients (swm_layout.h): q_e weights [2][ne] (pxt16,
   // gass18), dtred's PV-flux coefficients [6][ne]
   const float *e_qw32, *e_dtc32;
-  // pxt16's pered coefficients by cell [36][nv], gass18's connecting-edge
-  // selectors [36][nv] and outer triangle edges [6][nv] (the cell-centred
-  // variants; swm_layout.h)
+  // pxt16's pered coefficients by cell [36][nv] and gass18's outer
+  // triangle edges [6][nv] (the cell-centred variants; swm_layout.h)
   const float *c_C32;
-  const int8_t *c_gsel;
   const int32_t *c_gout;
   // dtred's Perot weights by triangle [9][nt], opposite corners [nt], and
   // per edge nr [3][ne] and the triangle weights [2][ne] (swm_layout.h)

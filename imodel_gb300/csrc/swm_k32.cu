@@ -372,23 +372,14 @@ __global__ void __launch_bounds__(512) k_cell32p(DevMesh M, const float *__restr
 // TRSK's weights and kinetic energy with gass18's PV: each slot's edge PV
 // from the edge pre-pass (the rhombus PV of scalar_tr2ed's gass branch) and,
 // in the pair (i, j) of coriolis_ed's gass branch (swm_operators.f90:
-// 1378-1414), twice the PV of the connecting edge in place of q_i + q_j
-// where there is one: a cell edge or the outer edge of a cell triangle
-// (c_gsel, c_gout).
-__device__ __forceinline__ float pick12(int sel, const float (&a)[6], const float (&b)[6]) {
-  float v = a[0];
-#pragma unroll
-  for (int k = 1; k < 6; ++k) v = sel == k ? a[k] : v;
-#pragma unroll
-  for (int k = 0; k < 6; ++k) v = sel == 6 + k ? b[k] : v;
-  return v;
-}
-
+// 1378-1414), twice the PV of the connecting edge in place of q_i + q_j:
+// the outer edge of the triangle shared by adjacent edges (c_gout), the
+// cell edge between edges two apart, none for opposite edges (the layout
+// checks this rule against edge_connection for every pair of every cell).
 template <int N>
-__device__ __forceinline__ void gass_cell(const DevMesh &M, int c, const float (&G)[6],
-                                          const float (&qs)[6], const float (&qo)[6],
-                                          const float (&R)[6], unsigned tneg, float (&Z)[6]) {
-  const int nv = M.nv;
+__device__ __forceinline__ void gass_cell(const float (&G)[6], const float (&qs)[6],
+                                          const float (&qo)[6], const float (&R)[6],
+                                          unsigned tneg, float (&Z)[6]) {
 #pragma unroll
   for (int i = 0; i < N; ++i) {
     float w = 0.0f, acc = 0.0f;
@@ -396,8 +387,17 @@ __device__ __forceinline__ void gass_cell(const DevMesh &M, int c, const float (
     for (int s = 1; s < N; ++s) {
       const int j = (i + s) % N;
       w += R[(i + s - 1) % N];
-      const int sel = __ldg(&M.c_gsel[(6 * i + j) * nv + c]);
-      const float P = sel < 0 ? qs[i] + qs[j] : 2.0f * pick12(sel, qs, qo);
+      float P;
+      if (s == 1)
+        P = 2.0f * qo[i];
+      else if (s == N - 1)
+        P = 2.0f * qo[j];
+      else if (s == 2)
+        P = 2.0f * qs[(i + 1) % N];
+      else if (s == N - 2)
+        P = 2.0f * qs[(i + N - 1) % N];
+      else
+        P = qs[i] + qs[j];
       acc += (w - 0.5f) * G[j] * P;
     }
     const float z = 0.5f * acc;
@@ -456,15 +456,12 @@ __global__ void __launch_bounds__(512) k_cell32g(DevMesh M, const float *__restr
   }
   if (coefdiv) coefdiv[i] = kcv[i] * (du * inva);
   bern[i] = grav * (hi + bt) + ke;
+  // the layout admits this kernel only on pentagons and hexagons
   float Z[6];
   if (n == 6)
-    gass_cell<6>(M, i, G, qs, qo, R, tneg, Z);
-  else if (n == 5)
-    gass_cell<5>(M, i, G, qs, qo, R, tneg, Z);
-  else if (n == 4)
-    gass_cell<4>(M, i, G, qs, qo, R, tneg, Z);
+    gass_cell<6>(G, qs, qo, R, tneg, Z);
   else
-    gass_cell<3>(M, i, G, qs, qo, R, tneg, Z);
+    gass_cell<5>(G, qs, qo, R, tneg, Z);
 #pragma unroll
   for (int j = 0; j < 6; ++j)
     if (j < n) zflux[6 * i + j] = Z[j];

@@ -401,14 +401,19 @@ std::string scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
     }
   }
   if (scheme == IMODEL_SWM_GASS18) {
-    // the connecting edges by cell, for the cell-centred variants
+    // the connecting edges by cell, for the cell-centred variants: on the
+    // grid's hexagons and pentagons the connecting edge of two cell edges is
+    // the outer edge of their triangle when they are adjacent, the edge
+    // between them when one edge lies between, none when they are opposite;
+    // gass_cells records that every cell follows that rule (the kernels
+    // then need no per-pair table)
     const int nv = L.nv;
-    fill(L.c_gsel, 36 * NV, static_cast<int8_t>(-1));
     L.c_gout.resize(6 * NV);
     const std::string err = par_for(nv, [&](int64_t i64) -> std::string {
       const int i = static_cast<int>(i64);
       const int c = L.cell_n2o[i];
       const int n = m.nnb[c];
+      const std::string off = "cell " + std::to_string(c + 1);
       int outer[6];
       for (int t = 0; t < 6; ++t) {
         outer[t] = -1;
@@ -422,30 +427,32 @@ std::string scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
           if (m.ed_v[2 * static_cast<size_t>(e)] - 1 != c && m.ed_v[2 * static_cast<size_t>(e) + 1] - 1 != c)
             outer[t] = e;
         }
-        if (outer[t] < 0) return "triangle " + std::to_string(tr + 1) + " has no edge opposite cell " + std::to_string(c + 1);
+        if (outer[t] < 0) return off;
         L.c_gout[static_cast<size_t>(t) * NV + i] = L.edge_o2n[outer[t]];
       }
+      if (n != 5 && n != 6) return off;
       for (int si = 0; si < n; ++si) {
         const int e = m.v_ed[6 * static_cast<size_t>(c) + si] - 1;
         for (int j = 0; j < n; ++j) {
           if (j == si) continue;
           const int k = m.v_ed[6 * static_cast<size_t>(c) + j] - 1;
           const int c3 = edge_connection(m, e, k);
-          if (c3 < 0) continue;
-          int sel = -1;
-          for (int q = 0; q < n && sel < 0; ++q)
-            if (m.v_ed[6 * static_cast<size_t>(c) + q] - 1 == c3) sel = q;
-          for (int t = 0; t < n && sel < 0; ++t)
-            if (outer[t] == c3) sel = 6 + t;
-          if (sel < 0)
-            return "gass18's connecting edge " + std::to_string(c3 + 1) + " lies outside cell " +
-                   std::to_string(c + 1) + " and its triangles";
-          L.c_gsel[static_cast<size_t>(6 * si + j) * NV + i] = static_cast<int8_t>(sel);
+          const int d = (j - si + n) % n;
+          int want = -1;
+          if (d == 1)
+            want = outer[si];
+          else if (d == n - 1)
+            want = outer[j];
+          else if (d == 2)
+            want = m.v_ed[6 * static_cast<size_t>(c) + (si + 1) % n] - 1;
+          else if (d == n - 2)
+            want = m.v_ed[6 * static_cast<size_t>(c) + (si + n - 1) % n] - 1;
+          if (c3 != want) return off;
         }
       }
       return std::string();
     });
-    if (!err.empty()) return err;
+    L.gass_cells = err.empty();
   }
   return "";
 }
@@ -1241,7 +1248,7 @@ extern "C" int imodel_swm_test_layout_digest(const imodel_swm_mesh *m, int32_t s
   IMODEL_DIGEST(t_c16A) IMODEL_DIGEST(t_c16B) IMODEL_DIGEST(t_c16C) IMODEL_DIGEST(t_wb)
   IMODEL_DIGEST(t_circ32) IMODEL_DIGEST(t_kite32) IMODEL_DIGEST(t_f32) IMODEL_DIGEST(e_area)
   IMODEL_DIGEST(t_bary) IMODEL_DIGEST(e_dist) IMODEL_DIGEST(t_edarea) IMODEL_DIGEST(e_nr)
-  IMODEL_DIGEST(e_stq) IMODEL_DIGEST(e_qw32) IMODEL_DIGEST(e_dtc32) IMODEL_DIGEST(c_C32) IMODEL_DIGEST(c_gsel) IMODEL_DIGEST(c_gout)
+  IMODEL_DIGEST(e_stq) IMODEL_DIGEST(e_qw32) IMODEL_DIGEST(e_dtc32) IMODEL_DIGEST(c_C32) IMODEL_DIGEST(c_gout)
   IMODEL_DIGEST(t_dpa32) IMODEL_DIGEST(t_dopp) IMODEL_DIGEST(e_nr32) IMODEL_DIGEST(e_dw32)
 #undef IMODEL_DIGEST
   *digest = h;

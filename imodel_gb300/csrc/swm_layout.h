@@ -172,14 +172,17 @@ struct Layout {
   //           times that edge's ed%leng (the edge kernel divides the sum of
   //           its two cells' contributions by l_e)
   HVec<float> c_C32;
-  // c_gsel [36][nv], c_gout [6][nv] (gass18, the cell-centred variants):
-  //           the edge whose PV, twice, replaces q_i + q_j in the cell's pair
-  //           of slots (i, j) (gass18's connecting edge, edge_connection):
-  //           -1 none, 0-5 the cell's edge in that slot, 6-11 the outer
-  //           edge of the cell's triangle in slot sel - 6, whose device
-  //           index c_gout holds
-  HVec<int8_t> c_gsel;
+  // c_gout [6][nv] (gass18, the cell-centred variants) the outer edge of
+  //           the cell's triangle in each slot (device index).  gass18's
+  //           connecting edge of the cell's edge pair (i, j)
+  //           (edge_connection) is that of triangle i for j = i + 1 (of
+  //           triangle j for j = i - 1), the cell's edge i + 1 for j = i + 2
+  //           (i - 1 for j = i - 2) and none for opposite edges; gass_cells
+  //           is true when every cell is a pentagon or hexagon that follows
+  //           this rule (checked against edge_connection pair by pair), and
+  //           only then do the cell-centred variants run gass18
   HVec<int32_t> c_gout;
+  bool gass_cells = false;
   // dtred in the cell-centred variants: t_dpa32 [3 slots][3][nt] the
   //           Perot weights a_ts = sign(tr%tg) l_s (tr%c x ed(s)%c) /
   //           tr%areag of the triangle's edges (P_t = sum_s uh_s a_ts);
