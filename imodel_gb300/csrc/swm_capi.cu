@@ -801,7 +801,8 @@ int create(Handle *H, const imodel_swm_mesh *m, const imodel_swm_opts *o) {
   }
   // the other method wrappers' geometry (empty vectors upload as NULL)
   if (H->precision == IMODEL_SWM_FP32 &&
-      ((rc = upload(H, L.c_C32, &M.c_C32)) || (rc = upload(H, L.c_gout, &M.c_gout)) || (rc = upload(H, L.t_dpa32, &M.t_dpa32)) ||
+      ((rc = upload(H, L.c_C32, &M.c_C32)) || (rc = upload(H, L.c_gout, &M.c_gout)) ||
+       (rc = upload(H, L.c_qw32, &M.c_qw32)) || (rc = upload(H, L.t_dpa32, &M.t_dpa32)) ||
        (rc = upload(H, L.t_dopp, &M.t_dopp)) || (rc = upload(H, L.e_nr32, &M.e_nr32)) ||
        (rc = upload(H, L.e_dw32, &M.e_dw32))))
     return rc;

@@ -64,6 +64,7 @@ struct DevMesh {
   // triangle edges [6][nv] (the cell-centred variants; swm_layout.h)
   const float *c_C32;
   const int32_t *c_gout;
+  const float *c_qw32;  // [12][nv] the q_e weights by cell slot (pxt16)
   // dtred's Perot weights by triangle [9][nt], opposite corners [nt], and
   // per edge nr [3][ne] and the triangle weights [2][ne] (swm_layout.h)
   const float *t_dpa32, *e_nr32, *e_dw32;
@@ -176,8 +177,8 @@ inline int launches_per_stage(int precision_fp32, int variant, bool dif_on = fal
   int n = (precision_fp32 && variant >= 1) ? 3 : 4;
   if (!precision_fp32 && scheme == 3) n += 1;  // dtred: the triangle reconstruction of uh q
   if (dif_on) n += (dif_k4 ? 3 : 1) + ((precision_fp32 && variant == 0) ? 1 : 0);
-  // FP32 variants 1 and 2: the edge pre-pass for APVM's or pxt16's edge PV
-  if (precision_fp32 && variant >= 1 && (apvm_on || scheme == 1 || scheme == 2)) n += 1;
+  // FP32 variants 1 and 2: the edge pre-pass for APVM's or gass18's edge PV
+  if (precision_fp32 && variant >= 1 && (apvm_on || scheme == 2)) n += 1;
   // the reconstructions
   if (apvm_on) n += precision_fp32 ? 1 : 2;
   return n;

@@ -297,6 +297,9 @@ __global__ void __launch_bounds__(512) k_cell32v2(DevMesh M, const float *__rest
 // plane) and pered's coefficients by cell in place of TRSK's kite fractions:
 //     Z_c(i) = sum_{j != i} C_c(i, j) F_j (q_i + q_j)
 // (coriolis_ed's pered branch, swm_operators.f90:1330-1377, split by cell).
+// kEdgePV: the edges' PV from the edge pre-pass (APVM on); otherwise the
+// cell forms pxt16's q_e from its triangles with the slot weights (c_qw32)
+template <bool kEdgePV>
 __global__ void __launch_bounds__(512) k_cell32p(DevMesh M, const float *__restrict__ hd,
                                                  const float *__restrict__ u,
                                                  const float *__restrict__ q_ed,
@@ -313,7 +316,7 @@ __global__ void __launch_bounds__(512) k_cell32p(DevMesh M, const float *__restr
   const int nv = M.nv;
   if (i >= nv) return;
   const int n = static_cast<int>(__ldg(&M.c_meta[i]) & 7u);
-  int ed[6], nb[6];
+  int ed[6], nb[6], tr[6];
   float2 kd[6];
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
@@ -321,6 +324,7 @@ __global__ void __launch_bounds__(512) k_cell32p(DevMesh M, const float *__restr
     kd[j] = __ldg(&M.c_kd[j * nv + i]);
     ed[j] = pk.x;
     nb[j] = pk.y;
+    tr[j] = pk.z;
   }
   const float hi = hd[i], bt = __ldg(&M.c_bt32[i]), inva = __ldg(&M.c_inva32[i]);
   const float ynv = stage >= 0 ? yn[i] : 0.0f, accv = stage >= 1 ? acc[i] : 0.0f;
@@ -329,7 +333,19 @@ __global__ void __launch_bounds__(512) k_cell32p(DevMesh M, const float *__restr
   for (int j = 0; j < 6; ++j) {
     ue[j] = u[ed[j]];
     hn[j] = hd[nb[j]];
-    qs[j] = q_ed[ed[j]];
+    // q_tr here is the triangles' PV (kEdgePV false) or the edges' (true)
+    qs[j] = q_ed[kEdgePV ? ed[j] : tr[j]];
+  }
+  if (!kEdgePV) {
+    // scalar_tr2ed's bary branch: slot j's edge between triangles j-1, j
+    float qt[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) qt[j] = qs[j];
+    const float qlast = n == 6 ? qt[5] : qt[4];
+#pragma unroll
+    for (int j = 0; j < 6; ++j)
+      qs[j] = __ldg(&M.c_qw32[(2 * j) * nv + i]) * (j == 0 ? qlast : qt[j - 1]) +
+              __ldg(&M.c_qw32[(2 * j + 1) * nv + i]) * qt[j];
   }
   // unused pentagon slots repeat slot 0 with zero weights (c_kd, c_apw32)
   float F[6], div = 0.0f, du = 0.0f, v[3] = {0.0f, 0.0f, 0.0f};
@@ -717,7 +733,7 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
     // place of the triangle average
     if (A.on)
       k_apvm32<<<nbt + nblocks(M.nv, 256), 256, 0, s>>>(M, W.q_tr, u_in, A.qg, A.vhx, nbt);
-    if (A.on || pxt || gass)
+    if (A.on || gass)
       k_edge_pre32<<<nblocks(M.ne, T.bs_pre), T.bs_pre, 0, s>>>(
           M, h_in, u_in, W.q_tr, W.h_ed, W.uh, W.q_ed, W.h_ref, A.on ? A.qg : nullptr, A.vhx,
           A.coef, pxt || gass ? M.e_qw32 : nullptr, gass ? W.h_trs : nullptr, W.pv_on, W.flags);
@@ -726,9 +742,13 @@ void launch_stage32(const DevMesh &M, const Work<float> &W, const float *h_in,
       k_cell32g<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
           M, h_in, u_in, W.q_ed, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
           grav, W.h_ref, D.kcv, D.on ? D.coefdiv : nullptr);
-    else if (pxt)
-      k_cell32p<<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
+    else if (pxt && A.on)
+      k_cell32p<true><<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
           M, h_in, u_in, W.q_ed, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
+          grav, W.h_ref, D.kcv, D.on ? D.coefdiv : nullptr);
+    else if (pxt)
+      k_cell32p<false><<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(
+          M, h_in, u_in, W.q_tr, W.bern, W.zflux, W.yn_h, W.acc_h, h_out, W.tend_h, stage, dt,
           grav, W.h_ref, D.kcv, D.on ? D.coefdiv : nullptr);
     else if (dtred1)
       k_cell32v2<false, false><<<nblocks(M.nv, T.bs_cell), T.bs_cell, 0, s>>>(

@@ -286,6 +286,29 @@ std::string scheme_fp32(const imodel_swm_mesh &m, Layout &L, int scheme) {
     }
   }
   if (scheme == IMODEL_SWM_PXT16) {
+    // the q_e weights by cell slot, for the cell-centred variants: slot j's
+    // edge lies between the cell's triangles j - 1 and j (c_tr);
+    // c_qw32[2 j] weighs triangle j - 1, c_qw32[2 j + 1] triangle j
+    const int nv = L.nv;
+    fill(L.c_qw32, 12 * NV, 0.0f);
+    const std::string err = par_for(nv, [&](int64_t i64) -> std::string {
+      const int i = static_cast<int>(i64);
+      const int n = L.c_nnb[i];
+      for (int j = 0; j < n; ++j) {
+        const int ie = L.c_ed[j * NV + i];
+        const int ta = L.c_tr[((j + n - 1) % n) * NV + i], tb = L.c_tr[j * NV + i];
+        const int t1 = L.e_sh[ie], t2 = L.e_sh[NE + ie];
+        if (!((ta == t1 && tb == t2) || (ta == t2 && tb == t1)))
+          return "cell " + std::to_string(L.cell_n2o[i] + 1) + ": slot " + std::to_string(j) +
+                 "'s edge does not lie between the slot's triangles";
+        L.c_qw32[static_cast<size_t>(2 * j) * NV + i] = ta == t1 ? L.e_qw32[ie] : L.e_qw32[NE + ie];
+        L.c_qw32[static_cast<size_t>(2 * j + 1) * NV + i] = tb == t1 ? L.e_qw32[ie] : L.e_qw32[NE + ie];
+      }
+      return std::string();
+    });
+    if (!err.empty()) return err;
+  }
+  if (scheme == IMODEL_SWM_PXT16) {
     // pered on the TRSK stencil's slots, in the order build_layout made them
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < ne; ++i) {
@@ -1248,7 +1271,7 @@ extern "C" int imodel_swm_test_layout_digest(const imodel_swm_mesh *m, int32_t s
   IMODEL_DIGEST(t_c16A) IMODEL_DIGEST(t_c16B) IMODEL_DIGEST(t_c16C) IMODEL_DIGEST(t_wb)
   IMODEL_DIGEST(t_circ32) IMODEL_DIGEST(t_kite32) IMODEL_DIGEST(t_f32) IMODEL_DIGEST(e_area)
   IMODEL_DIGEST(t_bary) IMODEL_DIGEST(e_dist) IMODEL_DIGEST(t_edarea) IMODEL_DIGEST(e_nr)
-  IMODEL_DIGEST(e_stq) IMODEL_DIGEST(e_qw32) IMODEL_DIGEST(e_dtc32) IMODEL_DIGEST(c_C32) IMODEL_DIGEST(c_gout)
+  IMODEL_DIGEST(e_stq) IMODEL_DIGEST(e_qw32) IMODEL_DIGEST(e_dtc32) IMODEL_DIGEST(c_C32) IMODEL_DIGEST(c_gout) IMODEL_DIGEST(c_qw32)
   IMODEL_DIGEST(t_dpa32) IMODEL_DIGEST(t_dopp) IMODEL_DIGEST(e_nr32) IMODEL_DIGEST(e_dw32)
 #undef IMODEL_DIGEST
   *digest = h;

@@ -183,6 +183,10 @@ struct Layout {
   //           only then do the cell-centred variants run gass18
   HVec<int32_t> c_gout;
   bool gass_cells = false;
+  // c_qw32 [6 slots][2][nv] (pxt16, the cell-centred variants)
+  //           e_qw32 by cell slot: the weights of the slot's triangles j - 1
+  //           and j in its edge's q_e
+  HVec<float> c_qw32;
   // dtred in the cell-centred variants: t_dpa32 [3 slots][3][nt] the
   //           Perot weights a_ts = sign(tr%tg) l_s (tr%c x ed(s)%c) /
   //           tr%areag of the triangle's edges (P_t = sum_s uh_s a_ts);
