@@ -158,6 +158,28 @@ def test_fp32_with_apvm(grid_at, variant):
     assert eh < FP32_RUN_H and eu < FP32_RUN_U
 
 
+@pytest.mark.parametrize("scheme", SCHEMES)
+@pytest.mark.parametrize("variant", [1, 2])
+def test_fp32_cell_centred_with_apvm_and_diffusion(grid_at, scheme, variant):
+    """Each wrapper in the cell-centred variants with APVM, Laplacian and
+    hyperdiffusion on, against the FP64 oracle of the same options."""
+    g = grid_at(4)
+    h, u = fields.balanced_state(g, lmax=12, seed=25)
+    dt = 600.0
+    m = SWM(g, "fp32", scheme=scheme)
+    m.set_apvm(0.5, dt)
+    m.set_diffusion(1.0e5, 1.0e13)
+    m.set_tuning(variant=variant)
+    hg, ug = m.ode_rk4(h, u, dt, 24)
+    m.close()
+    hr, ur = oracle.Oracle(g, 2, scheme=scheme, pvspar=0.5, dt=dt, k2=1.0e5,
+                           k4=1.0e13).run(h, u, dt, 24)
+    eh, eu = rel_l2(hg, hr, g.hx_areag), rel_l2(ug, ur, g.ed_leng * g.edhx_leng)
+    print(f"{scheme} + apvm + diffusion, variant {variant}: FP32 vs FP64 oracle after 24 steps "
+          f"h {eh:.1e}, u {eu:.1e}")
+    assert eh < FP32_RUN_H and eu < FP32_RUN_U
+
+
 def test_refusals(grid_at):
     g = grid_at(3)
     # every wrapper runs in every FP32 variant; the learned corrections are
